@@ -1,0 +1,272 @@
+/*
+ * mdx_gpu.h -- C ABI of the GB300 (sm_103a) force path for MDynaMix.
+ *
+ * The library replaces the per-step force path of MDynaMix v5.3 (Fortran).
+ * The Fortran driver keeps its COMMON blocks, its input, its output and its
+ * step loop; at the points below it calls these functions instead of the
+ * Fortran routines.  Every entry point states the reference routine it
+ * replaces (file:line within the MDynaMix source tree).
+ *
+ *   mdx_chcnb        <- CHCNB(LRDF)            forces.f:1813-2205
+ *   mdx_fforces      <- FFORCES(LAVER)         forces.f:36-51
+ *   mdx_slforces     <- SLFORCES               forces.f:55-73
+ *   mdx_allforce     <- ALLFORCE               forces.f:77-100
+ *   mdx_getcom       <- GETCOM                 service.f:463-563
+ *   mdx_double       <- DOUBLE (whole body)    mdstep.f:281-530
+ *   mdx_double_steps <- DOUBLE loop 2.3 only   mdstep.f:324-436
+ *   mdx_sultan       <- SULTAN (whole body)    mdstep.f:29-260
+ *   mdx_sultan_steps <- SULTAN loop 1.3 only   mdstep.f:83-162
+ *   mdx_set_lambda   <- RECINT                 mdee.f:86-140
+ *   mdx_inifur       <- INIFUR                 forces.f:1356-1449
+ *
+ * Conventions
+ *  - Plain C: pointers and sizes only.  All arrays are copied in at the call;
+ *    no host pointer is retained after a call returns.
+ *  - Index arrays are the Fortran ones, 1-based, exactly as they sit in the
+ *    COMMON blocks (ITYPE, NNUM, NSITE, INBB, IBI, ...).  Two-dimensional
+ *    Fortran arrays are passed column-major with their leading dimension.
+ *  - Coordinates are in Angstrom; every other quantity is in the reference's
+ *    internal units (setup.f:95-113), i.e. the tables the Fortran has already
+ *    converted (A6LJ, B12LJ, FB, COULF, MASSDI, ...).
+ *  - Velocities are the reference's VX/VY/VZ, which hold momenta
+ *    (kinetic energy = sum VX**2*MASSDI/2, service.f:50-60).
+ *  - Return value: MDX_OK (0) or an MDX_ERR_* code; mdx_last_error() gives
+ *    the message.  The Fortran shim turns a nonzero code into a message and
+ *    CALL FINAL, which is what the reference does on the same conditions.
+ *  - One context = one system on one CUDA stream, single host thread.
+ */
+#ifndef MDX_GPU_H
+#define MDX_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDX_NTPS 10                                  /* dimpar.h:26  NTPS  */
+#define MDX_NTPP ((MDX_NTPS * (MDX_NTPS + 1)) / 2 + 1) /* dimpar.h:50  NTPP  */
+
+/* return codes */
+enum {
+  MDX_OK = 0,
+  MDX_ERR_ARG = 1,            /* bad argument or inconsistent sizes           */
+  MDX_ERR_CUDA = 2,           /* CUDA runtime error                           */
+  MDX_ERR_LIST_OVERFLOW = 3,  /* neighbour list capacity (forces.f:2188-2194)  */
+  MDX_ERR_SHAKE = 4,          /* SHAKE did not converge in MAXIT (mdstep.f:1264)*/
+  MDX_ERR_NAN = 5,            /* non-finite force, energy or coordinate        */
+  MDX_ERR_TIMEOUT = 6,        /* a bounded device wait ran out                 */
+  MDX_ERR_STATE = 7,          /* call made before what it depends on           */
+  MDX_ERR_NOMEM = 8,          /* device allocation failed                      */
+  MDX_ERR_KVEC = 9,           /* more k-vectors than NKVM (forces.f:1414-1419) */
+  MDX_ERR_UNSUPPORTED = 10    /* option outside the built path                 */
+};
+
+/* precision of the force path */
+enum { MDX_FP64 = 0, MDX_MIXED = 1 };
+
+/* Sizes fixed for the life of a context (the dimpar.h role). */
+typedef struct {
+  int32_t nstot;      /* NSTOT  atoms                                  */
+  int32_t nop;        /* NOP    molecules                              */
+  int32_t ntypes;     /* NTYPES molecule types (<= MDX_NTPS)           */
+  int32_t nsites;     /* NSITES sites, summed over types               */
+  int32_t nnbt;       /* NNBT   non-bonded (LJ) types                  */
+  int32_t nrbb;       /* NRBB   bond records over all types            */
+  int32_t nraa;       /* NRAA   angle records                          */
+  int32_t nrtt;       /* NRTT   torsion records                        */
+  int32_t nrbt;       /* NRBT   bond instances (all molecules)         */
+  int32_t nrat;       /* NRAT   angle instances                        */
+  int32_t nrrt;       /* NRRT   torsion instances                      */
+  int32_t nbdmax;     /* NBDMAX columns of INBB                        */
+  int32_t cap_short;  /* short-list pairs owned per atom (NBSMX role)  */
+  int32_t cap_long;   /* long-list pairs owned per atom (NBLMX role)   */
+  int32_t nkv_max;    /* NKVM   maximum k-vectors                      */
+  int32_t precision;  /* MDX_FP64 or MDX_MIXED                         */
+} mdx_dims;
+
+/* Topology and tables, as produced by IUNITS/BNDLST (setup.f:27-888). */
+typedef struct {
+  /* per atom, length nstot (/ADDREFS/, /SITSITM/) */
+  const int32_t *itype;   /* ITYPE atom -> molecule type  */
+  const int32_t *nnum;    /* NNUM  atom -> molecule       */
+  const int32_t *nsite;   /* NSITE atom -> site           */
+  const double *massdi;   /* MASSDI inverse mass          */
+  const double *q;        /* Q charge (EE-scaled)         */
+  /* per site, length nsites (/SITTES/) */
+  const double *charge;   /* CHARGE                       */
+  const double *mass;     /* MASS (atomic units)          */
+  const int32_t *inbt;    /* INBT site -> LJ type         */
+  /* per molecule type, length ntypes (/MOLTYP/, /SOMMOL/, /MDEEI/) */
+  const int32_t *nspec, *nsits;
+  const int32_t *isadr;   /* ISADR(ityp)  sites before type  */
+  const int32_t *isaddr;  /* ISADDR(ityp) atoms before type  */
+  const int32_t *iaddr;   /* IADDR(ityp)  molecules before   */
+  const int32_t *ipot;    /* IPOT special water potential    */
+  const int32_t *nrb;     /* NRB bonds per molecule          */
+  const int32_t *iadb;    /* IADB first bond record of type  */
+  const int32_t *ishejk;  /* ISHEJK constrain this type      */
+  const int32_t *iee;     /* IEE 0 = expanded-ensemble type  */
+  const int32_t *lmove;   /* LMOVE (0/1)                     */
+  const double *c14el, *c14lj, *summas;
+  /* LJ tables NNBT x NNBT, column-major, leading dimension ld_lj (/SITTES/) */
+  const double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
+  int32_t ld_lj;
+  /* MDX(ityp,jtyp) type-pair index, column-major, leading dimension ld_mdx */
+  const int32_t *mdx;
+  int32_t ld_mdx;
+  /* exclusions from BNDLST: NNBB(nstot), INBB(ld_inbb, nbdmax) signed */
+  const int32_t *nnbb;
+  const int32_t *inbb;
+  int32_t ld_inbb;
+  /* bond records, length nrbb (/BONBON/) */
+  const int32_t *ib, *jb, *id;
+  const double *rb, *fb, *db, *ro;
+  /* bond instances, length nrbt */
+  const int32_t *ibi, *jbj, *ibuk;
+  /* angle records, length nraa, and instances, length nrat (/ANGANG/) */
+  const double *ra, *fa;
+  const int32_t *iai, *jaj, *kak, *iauk;
+  /* torsion records, length nrtt, and instances, length nrrt (/TORTOR/) */
+  const int32_t *itors, *nmul;
+  const double *ft, *rt, *ft1, *ft2, *ft3, *ft4, *ft5;
+  const int32_t *iti, *jtj, *ktk, *ltl, *ituk;
+} mdx_topo;
+
+/* Run parameters (/SIZES/, /ENERGY/, /NVTNPT/, main.f:380-450, 729-812). */
+typedef struct {
+  double boxl, boyl, bozl;   /* box lengths (Angstrom)                   */
+  int32_t icell;             /* ICELL 0 rect, 1 truncated oct, 2 hex     */
+  int32_t lmnbl;             /* reaction field instead of Ewald          */
+  double coulf;              /* COULF                                    */
+  double alphad;             /* ALPHAD Ewald alpha (1/Angstrom)          */
+  double fexp;               /* FEXP  (B): |k|^2 <= 4 alpha^2 B          */
+  double rcut;               /* RCUT (RCUTT; RSSQ = RCUTT**2)            */
+  double rshort;             /* SHORT                                    */
+  double rskin;              /* 0 = reference list; >0 list at rcut+skin */
+  double rff, rff2;          /* reaction-field constants                 */
+  double tstep, tsteb;       /* TSTEP, TSTEB                             */
+  int32_t nfreq;             /* NFREQ short steps per long step          */
+  int32_t ichnb;             /* ICHNB list refresh period (long steps)   */
+  int32_t lshejk;            /* SHAKE on                                 */
+  int32_t maxit;             /* SHAKE MAXIT (2000 in mdstep.f:1110)      */
+  double toler, bdtol;       /* TOLER, BDTOL                             */
+  int32_t lnvt, lnpt, lsep, lsctd, lp_xy, lsclt, lscft;
+  double trtemp, tdelt;      /* TRTEMP, TDELT                            */
+  double trpres, trpresx, trpresy, trpresz;
+  double dqt, dqp, rtp;      /* thermostat/barostat constants (main.f)   */
+  double fnst, fnop;         /* FNST degrees of freedom, FNOP            */
+  double ftscl, ftimes;      /* SCLFRC level, FTIMES                     */
+  double convet;             /* CONVET (setup.f:119)                     */
+  double unitp;              /* UNITP                                    */
+  double efact;              /* EFACT = 1.D3/AVSNO/UNITE (setup.f:395)   */
+  double tfact[MDX_NTPS];    /* TFACT per type                           */
+  double tridm_coef;         /* NOP*BOLTZ*1e-5/UNITL**3                  */
+  double tridee_coef;        /* (1-EC(ME))*NDEL*BOLTZ*TRTEMP*1e-5/UNITL**3 */
+  double epd, vird;          /* LJ tail corrections EPD, VIRD (ELRCLJ)   */
+  double chktf;              /* temperature watchdog factor (0 = off)    */
+  int32_t lmdee;             /* expanded ensemble active                 */
+  double raex;               /* RAEX soft-core shift                     */
+  double ec_me;              /* EC(ME) for INIFUR's self-energy          */
+  int32_t ntyp1;             /* NTYPES+1                                 */
+  int32_t molint;            /* MOLINT = type pairs + 1                  */
+} mdx_params;
+
+/* Energies and virials of one force evaluation (/ENERGY/, /VIRRR/, /SOMMOL/). */
+typedef struct {
+  double pe1, pels1, pe2, pels2, spe, pint, qpe;
+  double vir1, vir2, virb, virx, viry, virz, virfx, virfy, virfz;
+  double wirs, wirss;
+  double pote1[MDX_NTPP], potl1[MDX_NTPP];
+  double pes141[MDX_NTPS], psr141[MDX_NTPS], spee[MDX_NTPS];
+  int32_t mbsh, mbln, nkv;   /* list sizes and k-vectors in use           */
+  int32_t lscfl;             /* SCLFRC cut forces in this evaluation      */
+} mdx_scalars;
+
+/* Thermostat/barostat state and derived quantities (/NVTNPT/, GETEMP, SCALING). */
+typedef struct {
+  double sc, scl, sclx, scly, sclz;
+  double scm[MDX_NTPS];
+  double eabs;
+  double boxl, boyl, bozl, vol;
+  /* outputs */
+  double tke, temp, tempr[MDX_NTPS + 4], ekin[MDX_NTPS + 4];
+  double virkx, virky, virkz;
+  double vira[3], viran[3];
+  double tryck, tryckm, tryckx, trycky, tryckz;
+  int32_t shake_iter_max;    /* largest SHAKE iteration count seen        */
+  int32_t shake_fail;        /* molecules past MAXIT; the reference prints
+                                a message and goes on (mdstep.f:1264-1269) */
+  int32_t nscale;            /* forced velocity rescalings (NRTSC)        */
+  int32_t npt_fail;          /* NPT "too strong fluctuations" count (ISKK) */
+} mdx_thermo;
+
+/* One record per long step, filled on the device and copied back once. */
+typedef struct {
+  int32_t mstep;
+  int32_t mbsh, mbln;
+  int32_t shake_iter;
+  double pe1, pels1, pe2, pels2, spe, pint;
+  double vir1, vir2, virb, virx, viry, virz, virfx, virfy, virfz, wirs, wirss;
+  double tke, temp, sc, scl, tryck, tryckm;
+  double boxl, boyl, bozl, vol;
+  double eabs;
+} mdx_step_record;
+
+typedef struct mdx_ctx mdx_ctx;
+
+/* lifetime */
+int mdx_open(const mdx_dims *dims, mdx_ctx **out);
+int mdx_close(mdx_ctx *ctx);
+const char *mdx_last_error(const mdx_ctx *ctx);
+const char *mdx_strerror(int code);
+int mdx_version(void);
+
+/* data in and out */
+int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *topo);
+int mdx_set_params(mdx_ctx *ctx, const mdx_params *par);
+int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
+                     const double *sz, const double *vx, const double *vy,
+                     const double *vz, const mdx_thermo *th);
+int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
+                       double *vx, double *vy, double *vz, mdx_thermo *th);
+/* which: 1 = H (fast), 2 = G (slow), 3 = F = G + H */
+int mdx_download_forces(mdx_ctx *ctx, int which, double *fx, double *fy,
+                        double *fz);
+
+/* routines of forces.f / service.f */
+int mdx_inifur(mdx_ctx *ctx, int32_t *nkv);
+int mdx_chcnb(mdx_ctx *ctx, int32_t *mbsh, int32_t *mbln);
+/* The lists of the last mdx_chcnb in the reference's layout and order:
+ * NBS1/NBS2 (short, 1-4 pairs with negative first index) and NBL1/NBL2. */
+int mdx_get_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
+                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
+int mdx_getcom(mdx_ctx *ctx);
+int mdx_fforces(mdx_ctx *ctx, int laver, mdx_scalars *out);
+int mdx_slforces(mdx_ctx *ctx, mdx_scalars *out);
+int mdx_allforce(mdx_ctx *ctx, mdx_scalars *out);
+
+/* integrators of mdstep.f; rec (optional) receives nsteps records */
+int mdx_double(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot,
+               mdx_step_record *rec);
+int mdx_double_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0,
+                     mdx_step_record *rec);
+int mdx_sultan(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot,
+               mdx_step_record *rec);
+int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0,
+                     mdx_step_record *rec);
+
+/* expanded-ensemble scaling (RECINT) */
+int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,
+                   double bee);
+
+/* measurement helpers: the stream the context launches on, and a count of
+ * the kernels it has launched since open */
+void *mdx_stream(mdx_ctx *ctx);
+int64_t mdx_launch_count(const mdx_ctx *ctx);
+int mdx_sync(mdx_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDX_GPU_H */

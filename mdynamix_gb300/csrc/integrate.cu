@@ -1,0 +1,1062 @@
+// integrate.cu -- collectors and integrator pieces of the step:
+//   ZEROFS service.f:397-453, SCLFRC service.f:182-287, CM_ADDLA
+//   scalar.f:88-116, GETCOM service.f:463-563, GETEMP service.f:35-117,
+//   SCALING mdstep.f:534-1093 (as device stages), SHEJK mdstep.f:1105-1283,
+//   and the kick/drift loops of DOUBLE (mdstep.f:346-431) and SULTAN
+//   (mdstep.f:89-113).
+// All state stays on the device; scalar logic (thermostat, barostat) runs in
+// single-thread stage kernels that read and write the mdx_thermo block, so a
+// whole step is a fixed sequence of launches with no host round trip.
+#include <cmath>
+
+#include "mdx_internal.cuh"
+
+namespace {
+
+// ------------------------------------------------------------- zeroing ---
+__global__ void k_zero_scalars(mdx_scalars *sc, int which, int molint, int ntypes) {
+  int k = threadIdx.x;
+  if (k < molint) {
+    sc->pote1[k] = 0.0;
+    sc->potl1[k] = 0.0;
+  }
+  if (k < ntypes) {
+    sc->pes141[k] = 0.0;
+    sc->psr141[k] = 0.0;
+  }
+  if (k == 0) {
+    if (which == 1) {
+      sc->pels2 = 0.; sc->pint = 0.; sc->pe2 = 0.; sc->virb = 0.; sc->vir2 = 0.;
+      sc->wirss = 0.; sc->virfx = 0.; sc->virfy = 0.; sc->virfz = 0.;
+    } else {
+      sc->wirs = 0.; sc->vir1 = 0.; sc->pe1 = 0.; sc->pels1 = 0.;
+      sc->virx = 0.; sc->viry = 0.; sc->virz = 0.; sc->qpe = 0.;
+      sc->lscfl = 0;
+    }
+  }
+}
+
+__global__ void k_fix_fold(int n, const unsigned long long *__restrict__ f,
+                           double inv, double *__restrict__ x,
+                           double *__restrict__ y, double *__restrict__ z) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] = (double)(long long)f[i] * inv;
+  y[i] = (double)(long long)f[n + i] * inv;
+  z[i] = (double)(long long)f[2 * n + i] * inv;
+}
+
+// SCLFRC (service.f:182-287)
+__global__ void k_sclfrc(int n, double fct, const double *__restrict__ massdi,
+                         double *x, double *y, double *z, mdx_scalars *sc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double f = x[i] * x[i] + y[i] * y[i] + z[i] * z[i];
+  f = sqrt(f) * fct * massdi[i];
+  if (f > 1.0) {
+    if (f > 1.0e20) {
+      x[i] = 0.; y[i] = 0.; z[i] = 0.;
+    } else {
+      x[i] = x[i] / f; y[i] = y[i] / f; z[i] = z[i] / f;
+    }
+    sc->lscfl = 1;
+  }
+}
+
+// CM_ADDLA: F = G + H (scalar.f:106-113)
+__global__ void k_sum_forces(int n, const double *gx, const double *gy,
+                             const double *gz, const double *hx,
+                             const double *hy, const double *hz, double *fx,
+                             double *fy, double *fz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fx[i] = gx[i] + hx[i];
+  fy[i] = gy[i] + hy[i];
+  fz[i] = gz[i] + hz[i];
+}
+
+// ----------------------------------------------------------------- GETCOM
+struct MolConst {
+  double summas[MDX_NT];
+};
+
+__global__ void k_getcom(int nop, const int *__restrict__ mol_first,
+                         const int *__restrict__ mol_nat,
+                         const int *__restrict__ mol_type,
+                         const double *__restrict__ amass, dbl4 *pos, double *X,
+                         double *Y, double *Z, MolConst mc, double bx, double by,
+                         double bz) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nop) return;
+  const int f = mol_first[m], na = mol_nat[m];
+  const double summ = mc.summas[mol_type[m]];
+  double x = 0., y = 0., z = 0.;
+  for (int k = 0; k < na; ++k) {
+    const dbl4 p = pos[f + k];
+    const double ms = amass[f + k];
+    x = x + ms * p.x;
+    y = y + ms * p.y;
+    z = z + ms * p.z;
+  }
+  x = x / summ;
+  y = y / summ;
+  z = z / summ;
+  double xw = x, yw = y, zw = z;
+  pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  X[m] = xw;
+  Y[m] = yw;
+  Z[m] = zw;
+  if (xw != x || yw != y || zw != z) {
+    for (int k = 0; k < na; ++k) {
+      dbl4 p = pos[f + k];
+      p.x = (p.x - x) + xw;
+      p.y = (p.y - y) + yw;
+      p.z = (p.z - z) + zw;
+      pos[f + k] = p;
+    }
+  } else {
+    // the reference rebuilds every coordinate as (S - X) + X (service.f:549-552)
+    for (int k = 0; k < na; ++k) {
+      dbl4 p = pos[f + k];
+      p.x = (p.x - x) + x;
+      p.y = (p.y - y) + y;
+      p.z = (p.z - z) + z;
+      pos[f + k] = p;
+    }
+  }
+}
+
+// ------------------------------------------------------------ kick/drift
+struct MoveConst {
+  int lmove[MDX_NT];
+};
+
+__global__ void k_kick(int n, const int4 *__restrict__ ainfo, MoveConst mv,
+                       double h, const double *__restrict__ ax,
+                       const double *__restrict__ ay, const double *__restrict__ az,
+                       double *vx, double *vy, double *vz,
+                       const double *__restrict__ vscale) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t = ainfo[i].x;
+  if (!mv.lmove[t]) return;
+  double x = vx[i], y = vy[i], z = vz[i];
+  if (vscale) {  // thermostat factor of SCALING applied first (mdstep.f:818-828)
+    const double s = vscale[t];
+    x = x * s;
+    y = y * s;
+    z = z * s;
+  }
+  vx[i] = x + h * ax[i];
+  vy[i] = y + h * ay[i];
+  vz[i] = z + h * az[i];
+}
+
+// DOUBLE 2.3.5.3-2.3.5.4 (mdstep.f:366-373), optionally preceded by the
+// closing fast half-kick of the previous short step (mdstep.f:407-409).
+__global__ void k_kick_drift(int n, const int4 *__restrict__ ainfo, MoveConst mv,
+                             double htsteb, double tsteb, int prev,
+                             const double *__restrict__ hx,
+                             const double *__restrict__ hy,
+                             const double *__restrict__ hz,
+                             const double *__restrict__ massdi, double *vx,
+                             double *vy, double *vz, dbl4 *pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!mv.lmove[ainfo[i].x]) return;
+  double x = vx[i], y = vy[i], z = vz[i];
+  const double fx = hx[i], fy = hy[i], fz = hz[i];
+  if (prev) {
+    x = x + htsteb * fx;
+    y = y + htsteb * fy;
+    z = z + htsteb * fz;
+  }
+  x = x + htsteb * fx;
+  y = y + htsteb * fy;
+  z = z + htsteb * fz;
+  vx[i] = x;
+  vy[i] = y;
+  vz[i] = z;
+  dbl4 p = pos[i];
+  const double mi = massdi[i];
+  p.x = x * tsteb * mi + p.x;
+  p.y = y * tsteb * mi + p.y;
+  p.z = z * tsteb * mi + p.z;
+  pos[i] = p;
+}
+
+// SULTAN 1.3.1-1.3.2.2 (mdstep.f:89-113): OX = SX, V += TSTEP F,
+// SX += TSTEP V MASSDI.
+__global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
+                           double tstep, const double *__restrict__ fx,
+                           const double *__restrict__ fy,
+                           const double *__restrict__ fz,
+                           const double *__restrict__ massdi, double *vx,
+                           double *vy, double *vz, dbl4 *pos, double *ox,
+                           double *oy, double *oz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!mv.lmove[ainfo[i].x]) return;
+  dbl4 p = pos[i];
+  ox[i] = p.x;
+  oy[i] = p.y;
+  oz[i] = p.z;
+  const double x = vx[i] + tstep * fx[i];
+  const double y = vy[i] + tstep * fy[i];
+  const double z = vz[i] + tstep * fz[i];
+  vx[i] = x;
+  vy[i] = y;
+  vz[i] = z;
+  const double mi = massdi[i];
+  p.x = p.x + tstep * x * mi;
+  p.y = p.y + tstep * y * mi;
+  p.z = p.z + tstep * z * mi;
+  pos[i] = p;
+}
+
+// ------------------------------------------------------------------ GETEMP
+// ekin layout as the reference's EKIN: [0..ntypes-1] per type, then total,
+// VIRKX, VIRKY, VIRKZ.
+__global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
+                         int ntypes, const double *__restrict__ massdi,
+                         const double *__restrict__ vx,
+                         const double *__restrict__ vy,
+                         const double *__restrict__ vz, double *ekacc) {
+  double e[MDX_NT + 4];
+#pragma unroll
+  for (int k = 0; k < MDX_NT + 4; ++k) e[k] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const int t = ainfo[i].x;
+    if (!mv.lmove[t]) continue;
+    const double m = massdi[i];
+    const double VVX = m * (vx[i] * vx[i]);
+    const double VVY = m * (vy[i] * vy[i]);
+    const double VVZ = m * (vz[i] * vz[i]);
+    const double VSC = VVX + VVY + VVZ;
+    e[MDX_NT + 1] += VVX;
+    e[MDX_NT + 2] += VVY;
+    e[MDX_NT + 3] += VVZ;
+    e[MDX_NT] += VSC;
+#pragma unroll
+    for (int k = 0; k < MDX_NT; ++k)
+      if (k == t) e[k] += 0.5 * VSC;
+  }
+  // block reduction of MDX_NT+4 values
+  __shared__ double sh[32][MDX_NT + 4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MDX_NT + 4; ++k) e[k] = warp_sum(e[k]);
+  if (lane == 0)
+    for (int k = 0; k < MDX_NT + 4; ++k) sh[wid][k] = e[k];
+  __syncthreads();
+  if (threadIdx.x < MDX_NT + 4) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+    if (threadIdx.x < ntypes || threadIdx.x >= MDX_NT) atomicAdd(&ekacc[threadIdx.x], s);
+  }
+}
+
+// Device scratch of SCALING between stages.
+struct ScalScratch {
+  double dpe[5];
+  double dke;
+  double dte[MDX_NT];
+  double vscale[MDX_NT];  // per-type velocity factor of the next kick
+  double scvx, scvy, scvz, drcx, drcy, drcz, drcv, dxc;
+  double ekacc[MDX_NT + 4];
+  int iskk;
+};
+
+struct ScalConst {
+  int ntypes, lnvt, lnpt, lsep, lsctd, lp_xy, lshejk, lsclt;
+  double tstep, htstep, trtemp, tdelt, trpres, trpresx, trpresy, trpresz, dqt,
+      dqp, rtp, fnst, fnop, unitp, vird, tridm_coef, tridee_coef, convet, chktf;
+  double tfact[MDX_NT];
+  int lmove[MDX_NT];
+};
+
+// GETEMP finalisation (service.f:63-80) from the block sums.
+__device__ void getemp_fold(const ScalConst &c, ScalScratch *ss, mdx_thermo *th,
+                            int *err) {
+  const int nt = c.ntypes;
+  for (int t = 0; t < nt; ++t) th->ekin[t] = ss->ekacc[t];
+  // TEMPR(NTYP1) = 0.5*VSQ
+  const double tke = 0.5 * ss->ekacc[MDX_NT];
+  th->ekin[nt] = tke;
+  th->ekin[nt + 1] = ss->ekacc[MDX_NT + 1];
+  th->ekin[nt + 2] = ss->ekacc[MDX_NT + 2];
+  th->ekin[nt + 3] = ss->ekacc[MDX_NT + 3];
+  th->tke = tke;
+  th->virkx = th->ekin[nt + 1];
+  th->virky = th->ekin[nt + 2];
+  th->virkz = th->ekin[nt + 3];
+  for (int t = 0; t < nt + 4; ++t) th->tempr[t] = th->ekin[t];
+  for (int t = 0; t < nt; ++t) th->tempr[t] = th->ekin[t] * c.tfact[t];
+  th->temp = th->tke * c.convet;
+  for (int k = 0; k < MDX_NT + 4; ++k) ss->ekacc[k] = 0.0;
+  if (c.chktf > 0.0 && (th->temp > c.chktf * c.trtemp || th->temp <= c.trtemp / c.chktf))
+    atomicOr(err, DERR_TEMP);
+  if (!(th->temp == th->temp)) atomicOr(err, DERR_NAN);
+}
+
+__device__ void npt_guard(ScalScratch *ss, mdx_thermo *th, double f, int *err) {
+  if (fabs(f) >= 0.1) {
+    th->npt_fail += 1;
+    if (th->npt_fail > 100) atomicOr(err, DERR_NPT);
+  }
+}
+
+// Stage codes of the SCALING sequence.
+enum {
+  ST_GETEMP = 1,   // fold GETEMP
+  ST_PRESS,        // 3.3.2-3.3.3 pressures and deviations
+  ST_1A,           // IAL=1: 3.4.1 + 3.4.2.1-3.4.2.3
+  ST_1NVT,         // IAL=1 NVT velocity factor (3.4.3)
+  ST_1RECLEN,      // IAL=1 NPT box
+  ST_EABS,         // 3.4.4 / 3.5.7 / 3.6.4
+  ST_2V,           // IAL=2 3.5.1 factor
+  ST_2NPTV,        // IAL=2 3.5.2 factor
+  ST_2SCL,         // IAL=2 3.5.4-3.5.5
+  ST_2SC,          // IAL=2 3.5.6
+  ST_3V,           // IAL=3 3.2 factor
+  ST_3A,           // IAL=3 3.6.1-3.6.2.3
+  ST_3B,           // IAL=3 3.6.2.5-3.6.2.6 (box, SC)
+  ST_SCLT,         // 3.7 factor
+  ST_MSTEP1,       // SULTAN first step correction factor (mdstep.f:131-139)
+};
+
+__device__ void reclen_dev(mdx_thermo *th, double sx, double sy, double sz) {
+  th->boxl = sx * th->boxl;
+  th->boyl = sy * th->boyl;
+  th->bozl = sz * th->bozl;
+  th->vol = th->boxl * th->boyl * th->bozl;
+}
+
+__global__ void k_scal(int stage, ScalConst c, ScalScratch *ss, mdx_thermo *th,
+                       const mdx_scalars *s, int *err) {
+  const double TSTEP = c.tstep, HTSTEP = c.htstep, FNST = c.fnst;
+  const double DQT = c.dqt, DQP = c.dqp, RTP = c.rtp;
+  const double VOL = th->vol;
+  switch (stage) {
+    case ST_GETEMP:
+      getemp_fold(c, ss, th, err);
+      break;
+    case ST_PRESS: {
+      const double VIRSUM = s->vir1 + s->vir2 + s->virb + s->pels1 + s->pels2 + s->spe +
+                            c.vird + th->vira[0] + th->vira[1] + th->vira[2];
+      const double WIRSUM =
+          s->vir1 + s->vir2 + s->pels1 + s->pels2 + s->spe + c.vird + s->wirs + s->wirss;
+      const double TRIDEE = c.tridee_coef / VOL;
+      const double TRID = 2. * th->tke * c.unitp / (3. * VOL) - TRIDEE;
+      const double TRIDM = c.tridm_coef * th->temp / VOL - TRIDEE;
+      const double TRIDX = th->virkx * c.unitp / VOL - TRIDEE / 3.;
+      const double TRIDY = th->virky * c.unitp / VOL - TRIDEE / 3.;
+      const double TRIDZ = th->virkz * c.unitp / VOL - TRIDEE / 3.;
+      th->tryck = VIRSUM * c.unitp / (3. * VOL) + TRID;
+      th->tryckm = WIRSUM * c.unitp / (3. * VOL) + TRIDM;
+      th->tryckx = (s->virx + s->virfx + c.vird / 3. + th->vira[0]) * c.unitp / VOL + TRIDX;
+      th->trycky = (s->viry + s->virfy + c.vird / 3. + th->vira[1]) * c.unitp / VOL + TRIDY;
+      th->tryckz = (s->virz + s->virfz + c.vird / 3. + th->vira[2]) * c.unitp / VOL + TRIDZ;
+      ss->dke = th->temp / c.trtemp - 1.0;
+      for (int t = 0; t < c.ntypes; ++t) ss->dte[t] = th->tempr[t] / c.trtemp - 1.0;
+      if (s->lscfl) {
+        for (int k = 1; k <= 4; ++k) ss->dpe[k] = 0.;
+      } else {
+        ss->dpe[1] = c.lshejk ? th->tryckm - c.trpres : th->tryck - c.trpres;
+        ss->dpe[2] = th->tryckx - c.trpresx;
+        ss->dpe[3] = th->trycky - c.trpresy;
+        if (c.lp_xy) {
+          ss->dpe[2] = 0.5 * (ss->dpe[2] + ss->dpe[3]);
+          ss->dpe[3] = ss->dpe[2];
+        }
+        ss->dpe[4] = th->tryckz - c.trpresz;
+      }
+      break;
+    }
+    case ST_1A: {
+      if (c.lsctd) {
+        double SCA = 0.;
+        for (int t = 0; t < c.ntypes; ++t) {
+          th->scm[t] = th->scm[t] + ss->dte[t] * DQT * HTSTEP;
+          SCA = SCA + th->scm[t] * th->ekin[t];
+        }
+        th->sc = SCA / th->tke;
+      } else {
+        th->sc = th->sc + ss->dke * DQT * HTSTEP;
+      }
+      if (c.lnpt) {
+        if (c.lsctd) {
+          double SCA = 0.;
+          for (int t = 0; t < c.ntypes; ++t) {
+            th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+            SCA = SCA + th->scm[t] * th->ekin[t];
+          }
+          th->sc = SCA / th->tke;
+        } else {
+          th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+        }
+        const double *DPE = ss->dpe;
+        if (c.lsep) {
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+          if (c.lp_xy) {
+            th->sclx = 0.5 * (th->sclx + th->scly);
+            th->scly = th->sclx;
+          }
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+          th->scl = th->sclx + th->scly + th->sclz;
+        } else {
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+          th->sclx = th->scl;
+          th->scly = th->scl;
+          th->sclz = th->scl;
+          npt_guard(ss, th, th->scl * HTSTEP, err);
+        }
+        double SCVX = 1. - ((1. - 3. / FNST) * th->sclx + th->sc) * HTSTEP;
+        double SCVY = 1. - ((1. - 3. / FNST) * th->scly + th->sc) * HTSTEP;
+        double SCVZ = 1. - ((1. - 3. / FNST) * th->sclz + th->sc) * HTSTEP;
+        if (c.lp_xy) {
+          SCVX = 0.5 * (SCVX + SCVY);
+          SCVY = SCVX;
+        }
+        double DRCX = TSTEP * th->sclx, DRCY = TSTEP * th->scly, DRCZ = TSTEP * th->sclz;
+        const double DRC = (DRCX + DRCY + DRCZ) / 3.;
+        ss->drcv = DRC * HTSTEP;
+        ss->drcx = 1. + DRCX + 0.5 * (DRCX * DRCX);
+        ss->drcy = 1. + DRCY + 0.5 * (DRCY * DRCY);
+        ss->drcz = 1. + DRCZ + 0.5 * (DRCZ * DRCZ);
+        ss->scvx = SCVX;
+        ss->scvy = SCVY;
+        ss->scvz = SCVZ;
+      }
+      break;
+    }
+    case ST_1RECLEN:
+      reclen_dev(th, ss->drcx, ss->drcy, ss->drcz);
+      break;
+    case ST_1NVT:
+    case ST_2V:
+      for (int t = 0; t < MDX_NT; ++t)
+        ss->vscale[t] = c.lsctd ? 1. - th->scm[t] * HTSTEP : 1. - th->sc * HTSTEP;
+      break;
+    case ST_3V:
+      for (int t = 0; t < MDX_NT; ++t)
+        ss->vscale[t] = c.lsctd ? 1. - th->scm[t] * TSTEP : 1. - th->sc * TSTEP;
+      break;
+    case ST_EABS:
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+      break;
+    case ST_2NPTV: {
+      double SCVX = 1. - (1. - 3. / c.fnop) * th->sclx * HTSTEP;
+      double SCVY = 1. - (1. - 3. / c.fnop) * th->scly * HTSTEP;
+      double SCVZ = 1. - (1. - 3. / c.fnop) * th->sclz * HTSTEP;
+      if (c.lp_xy) {
+        SCVX = 0.5 * (SCVX + SCVY);
+        SCVY = SCVX;
+      }
+      ss->scvx = SCVX;
+      ss->scvy = SCVY;
+      ss->scvz = SCVZ;
+      break;
+    }
+    case ST_2SCL: {
+      const double *DPE = ss->dpe;
+      if (c.lsep) {
+        th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
+        th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+        if (c.lp_xy) {
+          th->sclx = 0.5 * (th->sclx + th->scly);
+          th->scly = th->sclx;
+        }
+        th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+        th->scl = th->sclx + th->scly + th->sclz;
+      } else {
+        th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+        th->sclx = th->scl;
+        th->scly = th->scl;
+        th->sclz = th->scl;
+        npt_guard(ss, th, th->scl * HTSTEP, err);
+      }
+      th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+      if (c.lsctd)
+        for (int t = 0; t < c.ntypes; ++t)
+          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+      break;
+    }
+    case ST_2SC: {
+      if (c.lsctd) {
+        double SCA = 0.;
+        for (int t = 0; t < c.ntypes; ++t) {
+          const double DTE = th->tempr[t] / c.trtemp - 1.0;
+          th->scm[t] = th->scm[t] + DTE * DQT * HTSTEP;
+          SCA = SCA + th->scm[t] * th->ekin[t];
+        }
+        th->sc = SCA / th->tke;
+      } else {
+        const double DKE = th->temp / c.trtemp - 1.0;
+        th->sc = th->sc + DKE * DQT * HTSTEP;
+      }
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+      break;
+    }
+    case ST_3A: {
+      th->sc = th->sc + ss->dke * DQT * TSTEP;
+      if (c.lsctd) {
+        double SCA = 0.;
+        for (int t = 0; t < c.ntypes; ++t) {
+          th->scm[t] = th->scm[t] + ss->dte[t] * DQT * TSTEP;
+          SCA = SCA + th->scm[t] * th->ekin[t];
+        }
+        th->sc = SCA / th->tke;
+      }
+      if (c.lnpt) {
+        const double *DPE = ss->dpe;
+        if (c.lsep) {
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * TSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * TSTEP;
+          if (c.lp_xy) {
+            th->sclx = 0.5 * (th->sclx + th->scly);
+            th->scly = th->sclx;
+          }
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * TSTEP;
+          th->scl = th->sclx + th->scly + th->sclz;
+        } else {
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * TSTEP;
+          th->sclx = th->scl;
+          th->scly = th->scl;
+          th->sclz = th->scl;
+          npt_guard(ss, th, th->scl * TSTEP, err);
+        }
+        ss->dxc = ((1. - 3. / FNST) * th->scl) * TSTEP;  // SCV of 3.6.2.2
+        ss->drcx = TSTEP * th->sclx;
+        ss->drcy = TSTEP * th->scly;
+        ss->drcz = TSTEP * th->sclz;
+      }
+      break;
+    }
+    case ST_3B: {
+      reclen_dev(th, ss->drcx + 1., ss->drcy + 1., ss->drcz + 1.);
+      th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+      if (c.lsctd) {
+        double SCA = 0.;
+        for (int t = 0; t < c.ntypes; ++t) {
+          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+          SCA = SCA + th->scm[t] * th->ekin[t];
+        }
+        th->sc = SCA / th->tke;
+      }
+      break;
+    }
+    case ST_SCLT: {
+      for (int t = 0; t < MDX_NT; ++t) ss->vscale[t] = 1.0;
+      if (c.lsctd) {
+        for (int t = 0; t < c.ntypes; ++t)
+          if (fabs(c.trtemp - th->tempr[t]) > c.tdelt && c.lmove[t]) {
+            ss->vscale[t] = sqrt(c.trtemp / th->tempr[t]);
+            th->nscale += 1;
+          }
+      } else if (fabs(c.trtemp - th->temp) > c.tdelt) {
+        const double SCV = sqrt(c.trtemp / th->temp);
+        for (int t = 0; t < MDX_NT; ++t) ss->vscale[t] = SCV;
+        th->nscale += 1;
+      }
+      break;
+    }
+    case ST_MSTEP1: {
+      const double FTMP = sqrt(c.trtemp / th->temp);
+      for (int t = 0; t < MDX_NT; ++t) ss->vscale[t] = FTMP;
+      break;
+    }
+  }
+}
+
+// Velocity (and position) scaling of the SCALING stages.
+// mode 0: V *= vscale[type] (LMOVE atoms); mode 1: all atoms (SULTAN first
+// step); mode 2: IAL=1 NPT (V *= SCV?, S = S*DRC? + V*DRCV*MASSDI);
+// mode 3: IAL=2 NPT V *= SCV?.
+__global__ void k_scale_atoms(int n, int mode, const int4 *__restrict__ ainfo,
+                              MoveConst mv, const ScalScratch *ss,
+                              const double *__restrict__ massdi, double *vx,
+                              double *vy, double *vz, dbl4 *pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t = ainfo[i].x;
+  if (mode != 1 && !mv.lmove[t]) return;
+  if (mode <= 1) {
+    const double s = ss->vscale[t];
+    vx[i] = vx[i] * s;
+    vy[i] = vy[i] * s;
+    vz[i] = vz[i] * s;
+  } else {
+    const double x = vx[i] * ss->scvx, y = vy[i] * ss->scvy, z = vz[i] * ss->scvz;
+    vx[i] = x;
+    vy[i] = y;
+    vz[i] = z;
+    if (mode == 2) {
+      dbl4 p = pos[i];
+      const double mi = massdi[i];
+      p.x = p.x * ss->drcx + x * ss->drcv * mi;
+      p.y = p.y * ss->drcy + y * ss->drcv * mi;
+      p.z = p.z * ss->drcz + z * ss->drcv * mi;
+      pos[i] = p;
+    }
+  }
+}
+
+// SCALING(3) NPT molecular correction (mdstep.f:953-1003): per molecule.
+__global__ void k_com_scale(int nop, const int *__restrict__ mol_first,
+                            const int *__restrict__ mol_nat,
+                            const int *__restrict__ mol_type,
+                            const double *__restrict__ amass, MolConst mc,
+                            MoveConst mv, const ScalScratch *ss, double *vx,
+                            double *vy, double *vz, dbl4 *pos) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nop) return;
+  const int t = mol_type[m];
+  if (!mv.lmove[t]) return;
+  const int f = mol_first[m], na = mol_nat[m];
+  const double SUMM = mc.summas[t];
+  double XC = 0., YC = 0., ZC = 0., PXC = 0., PYC = 0., PZC = 0.;
+  for (int k = 0; k < na; ++k) {
+    const dbl4 p = pos[f + k];
+    const double ms = amass[f + k];
+    XC = XC + ms * p.x;
+    YC = YC + ms * p.y;
+    ZC = ZC + ms * p.z;
+    PXC = PXC + vx[f + k];
+    PYC = PYC + vy[f + k];
+    PZC = PZC + vz[f + k];
+  }
+  XC = XC / SUMM;
+  YC = YC / SUMM;
+  ZC = ZC / SUMM;
+  const double SCV = ss->dxc;
+  const double DVX = PXC * SCV, DVY = PYC * SCV, DVZ = PZC * SCV;
+  const double DXC = XC * ss->drcx, DYC = YC * ss->drcy, DZC = ZC * ss->drcz;
+  for (int k = 0; k < na; ++k) {
+    const double FAC = amass[f + k] / SUMM;
+    vx[f + k] = vx[f + k] - DVX * FAC;
+    vy[f + k] = vy[f + k] - DVY * FAC;
+    vz[f + k] = vz[f + k] - DVZ * FAC;
+    dbl4 p = pos[f + k];
+    p.x = p.x + DXC;
+    p.y = p.y + DYC;
+    p.z = p.z + DZC;
+    pos[f + k] = p;
+  }
+}
+
+// ------------------------------------------------------------------ SHEJK
+struct ShakeConst {
+  int iadb[MDX_NT], nrb[MDX_NT], ishejk[MDX_NT];
+  int maxit;
+  double tol2, tstep;
+};
+
+__global__ void k_shejk(int nop, const int *__restrict__ mol_first,
+                        const int *__restrict__ mol_nat,
+                        const int *__restrict__ mol_type, MoveConst mv,
+                        ShakeConst sk, const int *__restrict__ bib,
+                        const int *__restrict__ bjb, const int *__restrict__ bid,
+                        const double *__restrict__ brb,
+                        const double *__restrict__ massdi, dbl4 *pos,
+                        double *vx, double *vy, double *vz,
+                        const double *__restrict__ ox,
+                        const double *__restrict__ oy,
+                        const double *__restrict__ oz, double *fx, double *fy,
+                        double *fz, double bx, double by, double bz,
+                        mdx_thermo *th, int *err) {
+  double vir[3] = {0, 0, 0};
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int iter_out = 0;
+  if (m < nop) {
+    const int t = mol_type[m];
+    const int nrbs = sk.nrb[t];
+    if (mv.lmove[t] && sk.ishejk[t] > 0 && nrbs > 0) {
+      const int f = mol_first[m], na = mol_nat[m];
+      const int nb0 = sk.iadb[t] - 1;  // 0-based first bond record
+      for (int k = 0; k < na; ++k) {
+        const dbl4 p = pos[f + k];
+        fx[f + k] = p.x;
+        fy[f + k] = p.y;
+        fz[f + k] = p.z;
+      }
+      // MOVING / MOVED flags as bit masks over the molecule's atoms (<= 128)
+      unsigned long long moving[2] = {0, 0}, moved[2] = {0, 0};
+      for (int b = 0; b < nrbs; ++b) {
+        if (bid[nb0 + b] == 2) continue;
+        const int li = bib[nb0 + b] - 1, lj = bjb[nb0 + b] - 1;
+        moved[li >> 6] |= 1ull << (li & 63);
+        moved[lj >> 6] |= 1ull << (lj & 63);
+      }
+      int ITER = 0;
+      bool DONE = false;
+      for (;;) {
+        if (ITER > sk.maxit || DONE) break;
+        DONE = true;
+        for (int b = 0; b < nrbs; ++b) {
+          if (bid[nb0 + b] == 2) continue;
+          const int li = bib[nb0 + b] - 1, lj = bjb[nb0 + b] - 1;
+          const bool mvi = (moved[li >> 6] >> (li & 63)) & 1ull;
+          const bool mvj = (moved[lj >> 6] >> (lj & 63)) & 1ull;
+          if (!(mvi || mvj)) continue;
+          const int I = f + li, J = f + lj;
+          const double rbb = brb[nb0 + b];
+          const double BNDSQ = rbb * rbb;
+          dbl4 pi = pos[I], pj = pos[J];
+          double BXN = pi.x - pj.x, BYN = pi.y - pj.y, BZN = pi.z - pj.z;
+          pbc_rect(BXN, BYN, BZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+          const double BSQ = BXN * BXN + BYN * BYN + BZN * BZN;
+          const double DIFFSQ = BNDSQ - BSQ;
+          if (fabs(DIFFSQ) > (BNDSQ * sk.tol2)) {
+            double DXN = ox[I] - ox[J], DYN = oy[I] - oy[J], DZN = oz[I] - oz[J];
+            pbc_rect(DXN, DYN, DZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+            const double VDOT = BXN * DXN + BYN * DYN + BZN * DZN;
+            const double RMA = massdi[I], RMB = massdi[J];
+            const double GAB = DIFFSQ / (2.0 * (RMA + RMB) * VDOT);
+            DXN = DXN * GAB;
+            DYN = DYN * GAB;
+            DZN = DZN * GAB;
+            pi.x = pi.x + RMA * DXN;
+            pi.y = pi.y + RMA * DYN;
+            pi.z = pi.z + RMA * DZN;
+            pj.x = pj.x - RMB * DXN;
+            pj.y = pj.y - RMB * DYN;
+            pj.z = pj.z - RMB * DZN;
+            pos[I] = pi;
+            pos[J] = pj;
+            moving[li >> 6] |= 1ull << (li & 63);
+            moving[lj >> 6] |= 1ull << (lj & 63);
+            DONE = false;
+          }
+        }
+        // MOVED := MOVING restricted to constrained atoms; MOVING := 0
+        moved[0] = moving[0];
+        moved[1] = moving[1];
+        moving[0] = moving[1] = 0;
+        ITER = ITER + 1;
+      }
+      iter_out = ITER;
+      if (ITER >= sk.maxit) {
+        atomicAdd(&th->shake_fail, 1);
+        atomicOr(err, DERR_SHAKE);
+      }
+      const double TS = sk.tstep;
+      for (int k = 0; k < na; ++k) {
+        const int I = f + k;
+        const dbl4 p = pos[I];
+        const double DIX = (p.x - fx[I]) / (massdi[I] * TS);
+        const double DIY = (p.y - fy[I]) / (massdi[I] * TS);
+        const double DIZ = (p.z - fz[I]) / (massdi[I] * TS);
+        vir[0] += DIX * ox[I] / TS;
+        vir[1] += DIY * oy[I] / TS;
+        vir[2] += DIZ * oz[I] / TS;
+        vx[I] = vx[I] + DIX;
+        vy[I] = vy[I] + DIY;
+        vz[I] = vz[I] + DIZ;
+      }
+    }
+  }
+  double *dst[3] = {&th->viran[0], &th->viran[1], &th->viran[2]};
+  block_add<3>(vir, dst);
+  if (iter_out > 0) atomicMax(&th->shake_iter_max, iter_out);
+}
+
+__global__ void k_shake_prep(mdx_thermo *th) {
+  th->viran[0] = th->viran[1] = th->viran[2] = 0.0;
+  th->shake_iter_max = 0;
+}
+__global__ void k_vira_from_viran(mdx_thermo *th) {
+  th->vira[0] = th->viran[0];
+  th->vira[1] = th->viran[1];
+  th->vira[2] = th->viran[2];
+}
+__global__ void k_vira_zero(mdx_thermo *th) {
+  th->vira[0] = th->vira[1] = th->vira[2] = 0.0;
+}
+
+// ------------------------------------------------------------------ record
+__global__ void k_record(mdx_step_record *rec, int slot, int mstep,
+                         const mdx_scalars *s, const mdx_thermo *th) {
+  mdx_step_record &r = rec[slot];
+  r.mstep = mstep;
+  r.mbsh = s->mbsh;
+  r.mbln = s->mbln;
+  r.shake_iter = th->shake_iter_max;
+  r.pe1 = s->pe1; r.pels1 = s->pels1; r.pe2 = s->pe2; r.pels2 = s->pels2;
+  r.spe = s->spe; r.pint = s->pint;
+  r.vir1 = s->vir1; r.vir2 = s->vir2; r.virb = s->virb;
+  r.virx = s->virx; r.viry = s->viry; r.virz = s->virz;
+  r.virfx = s->virfx; r.virfy = s->virfy; r.virfz = s->virfz;
+  r.wirs = s->wirs; r.wirss = s->wirss;
+  r.tke = th->tke; r.temp = th->temp; r.sc = th->sc; r.scl = th->scl;
+  r.tryck = th->tryck; r.tryckm = th->tryckm;
+  r.boxl = th->boxl; r.boyl = th->boyl; r.bozl = th->bozl; r.vol = th->vol;
+  r.eabs = th->eabs;
+}
+
+// ------------------------------------------------------------- host side
+MoveConst move_const(mdx_ctx *ctx) {
+  MoveConst m{};
+  for (int t = 0; t < MDX_NT; ++t) m.lmove[t] = ctx->tc.lmove[t];
+  return m;
+}
+MolConst mol_const(mdx_ctx *ctx) {
+  MolConst m{};
+  for (int t = 0; t < MDX_NT; ++t) m.summas[t] = ctx->summas[t];
+  return m;
+}
+
+}  // namespace
+
+int launch_getemp(mdx_ctx *ctx);
+
+// Scratch of the SCALING stages lives at a fixed place of the context.
+static ScalScratch *scratch(mdx_ctx *ctx) {
+  return reinterpret_cast<ScalScratch *>(ctx->dv.scal_scratch);
+}
+
+size_t scal_scratch_bytes() { return sizeof(ScalScratch); }
+
+static ScalConst scal_const(mdx_ctx *ctx) {
+  const mdx_params &p = ctx->p;
+  ScalConst c{};
+  c.ntypes = ctx->d.ntypes;
+  c.lnvt = p.lnvt; c.lnpt = p.lnpt; c.lsep = p.lsep; c.lsctd = p.lsctd;
+  c.lp_xy = p.lp_xy; c.lshejk = p.lshejk; c.lsclt = p.lsclt;
+  c.tstep = p.tstep; c.htstep = 0.5 * p.tstep; c.trtemp = p.trtemp; c.tdelt = p.tdelt;
+  c.trpres = p.trpres; c.trpresx = p.trpresx; c.trpresy = p.trpresy; c.trpresz = p.trpresz;
+  c.dqt = p.dqt; c.dqp = p.dqp; c.rtp = p.rtp; c.fnst = p.fnst; c.fnop = p.fnop;
+  c.unitp = p.unitp; c.vird = p.vird; c.tridm_coef = p.tridm_coef;
+  c.tridee_coef = p.tridee_coef; c.convet = p.convet; c.chktf = p.chktf;
+  for (int t = 0; t < MDX_NT; ++t) {
+    c.tfact[t] = p.tfact[t];
+    c.lmove[t] = ctx->tc.lmove[t];
+  }
+  return c;
+}
+
+static int stage(mdx_ctx *ctx, int st) {
+  k_scal<<<1, 1, 0, ctx->stream>>>(st, scal_const(ctx), scratch(ctx), ctx->dv.th,
+                                   ctx->dv.sc, ctx->dv.err);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_getemp(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_getemp<<<160, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), ctx->d.ntypes,
+                                         d.massdi, d.vx, d.vy, d.vz, scratch(ctx)->ekacc);
+  MDX_LAUNCHED(ctx);
+  return stage(ctx, ST_GETEMP);
+}
+
+static int scale_atoms(mdx_ctx *ctx, int mode) {
+  DevData &d = ctx->dv;
+  k_scale_atoms<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, mode, d.ainfo, move_const(ctx), scratch(ctx), d.massdi, d.vx, d.vy, d.vz, d.pos);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+#define RC(x)                  \
+  do {                         \
+    int rc_ = (x);             \
+    if (rc_) return rc_;       \
+  } while (0)
+
+// SCALING(IAL).  For IAL=1 in NVT (no NPT) the final velocity factor is left
+// in the scratch for the following slow half-kick, which applies it first
+// (same operation order as the reference: V*SCV, then V + HTSTEP*G);
+// *pending_vscale tells the caller.
+int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
+  const mdx_params &p = ctx->p;
+  if (pending_vscale) *pending_vscale = false;
+  if (ial == 3 && p.lnvt) {
+    RC(stage(ctx, ST_3V));
+    RC(scale_atoms(ctx, 0));
+  }
+  RC(launch_getemp(ctx));
+  RC(stage(ctx, ST_PRESS));
+  if (ial == 1) {
+    if (p.lnvt) {
+      RC(stage(ctx, ST_1A));
+      if (p.lnpt) {
+        RC(scale_atoms(ctx, 2));
+        RC(stage(ctx, ST_1RECLEN));
+      } else {
+        // 3.4.3 calls GETEMP again on unchanged velocities: same values
+        RC(stage(ctx, ST_1NVT));
+        if (pending_vscale) *pending_vscale = true;
+        else RC(scale_atoms(ctx, 0));
+      }
+      RC(stage(ctx, ST_EABS));
+    }
+  } else if (ial == 2) {
+    if (p.lnvt) {
+      RC(stage(ctx, ST_2V));
+      RC(scale_atoms(ctx, 0));
+      if (p.lnpt) {
+        RC(stage(ctx, ST_2NPTV));
+        RC(scale_atoms(ctx, 3));
+        RC(launch_getemp(ctx));
+        RC(stage(ctx, ST_2SCL));
+      } else {
+        RC(launch_getemp(ctx));
+      }
+      RC(stage(ctx, ST_2SC));
+    }
+  } else if (ial == 3) {
+    if (p.lnvt) {
+      RC(stage(ctx, ST_3A));
+      if (p.lnpt) {
+        DevData &d = ctx->dv;
+        k_com_scale<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
+            d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, mol_const(ctx),
+            move_const(ctx), scratch(ctx), d.vx, d.vy, d.vz, d.pos);
+        MDX_LAUNCHED(ctx);
+        RC(stage(ctx, ST_3B));
+      }
+      RC(stage(ctx, ST_EABS));
+    }
+  }
+  if (p.lsclt && (ial == 2 || ial == 3)) {
+    RC(stage(ctx, ST_SCLT));
+    RC(scale_atoms(ctx, 0));
+    RC(launch_getemp(ctx));
+  }
+  return MDX_OK;
+}
+
+int launch_mstep1_rescale(mdx_ctx *ctx) {
+  RC(launch_getemp(ctx));
+  RC(stage(ctx, ST_MSTEP1));
+  return scale_atoms(ctx, 1);
+}
+
+int launch_zero_fast(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_zero_scalars<<<1, 64, 0, ctx->stream>>>(d.sc, 1, ctx->p.molint, ctx->d.ntypes);
+  MDX_LAUNCHED(ctx);
+  if (ctx->mixed()) {
+    MDX_CUDA(cudaMemsetAsync(d.hfix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
+  } else {
+    MDX_CUDA(cudaMemsetAsync(d.hx, 0, sizeof(double) * 3 * d.n, ctx->stream));
+  }
+  return MDX_OK;
+}
+
+int launch_zero_slow(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_zero_scalars<<<1, 64, 0, ctx->stream>>>(d.sc, 2, ctx->p.molint, ctx->d.ntypes);
+  MDX_LAUNCHED(ctx);
+  if (ctx->mixed()) {
+    MDX_CUDA(cudaMemsetAsync(d.gfix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
+  } else {
+    MDX_CUDA(cudaMemsetAsync(d.gx, 0, sizeof(double) * 3 * d.n, ctx->stream));
+  }
+  return MDX_OK;
+}
+
+int launch_fix_to_double(mdx_ctx *ctx, int which) {
+  DevData &d = ctx->dv;
+  const unsigned long long *f = which == 1 ? d.hfix : d.gfix;
+  double *x = which == 1 ? d.hx : d.gx, *y = which == 1 ? d.hy : d.gy,
+         *z = which == 1 ? d.hz : d.gz;
+  k_fix_fold<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, f, ctx->fix.inv, x, y, z);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_sclfrc(mdx_ctx *ctx, int nnn) {
+  if (!ctx->p.lscft) return MDX_OK;
+  DevData &d = ctx->dv;
+  const double fct = nnn == 1 ? ctx->p.ftscl * ctx->p.ftimes : ctx->p.ftscl;
+  double *x = nnn == 1 ? d.hx : nnn == 2 ? d.gx : d.fx;
+  double *y = nnn == 1 ? d.hy : nnn == 2 ? d.gy : d.fy;
+  double *z = nnn == 1 ? d.hz : nnn == 2 ? d.gz : d.fz;
+  k_sclfrc<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, fct, d.massdi, x, y, z, d.sc);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_sum_forces(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_sum_forces<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.gx, d.gy, d.gz, d.hx,
+                                                           d.hy, d.hz, d.fx, d.fy, d.fz);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_getcom(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_getcom<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
+      d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z,
+      mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale) {
+  DevData &d = ctx->dv;
+  const double *x = which == 1 ? d.hx : which == 2 ? d.gx : d.fx;
+  const double *y = which == 1 ? d.hy : which == 2 ? d.gy : d.fy;
+  const double *z = which == 1 ? d.hz : which == 2 ? d.gz : d.fz;
+  k_kick<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, d.ainfo, move_const(ctx), h, x, y, z, d.vx, d.vy, d.vz,
+      apply_vscale ? scratch(ctx)->vscale : nullptr);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev) {
+  DevData &d = ctx->dv;
+  k_kick_drift<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, d.ainfo, move_const(ctx), htsteb, tsteb, prev, d.hx, d.hy, d.hz, d.massdi,
+      d.vx, d.vy, d.vz, d.pos);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_leapfrog_shake(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_leapfrog<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, d.ainfo, move_const(ctx), ctx->p.tstep, d.fx, d.fy, d.fz, d.massdi, d.vx,
+      d.vy, d.vz, d.pos, d.ox, d.oy, d.oz);
+  MDX_LAUNCHED(ctx);
+  k_shake_prep<<<1, 1, 0, ctx->stream>>>(d.th);
+  MDX_LAUNCHED(ctx);
+  if (ctx->p.lshejk) {
+    ShakeConst sk{};
+    for (int t = 0; t < MDX_NT; ++t) {
+      sk.iadb[t] = ctx->iadb[t];
+      sk.nrb[t] = ctx->nrb[t];
+      sk.ishejk[t] = ctx->ishejk[t];
+    }
+    sk.maxit = ctx->p.maxit > 0 ? ctx->p.maxit : 2000;
+    sk.tol2 = ctx->p.toler * ctx->p.toler;
+    sk.tstep = ctx->p.tstep;
+    k_shejk<<<(d.nop + 63) / 64, 64, 0, ctx->stream>>>(
+        d.nop, d.mol_first, d.mol_nat, d.mol_type, move_const(ctx), sk, d.bib, d.bjb,
+        d.bid, d.brb, d.massdi, d.pos, d.vx, d.vy, d.vz, d.ox, d.oy, d.oz, d.fx, d.fy,
+        d.fz, ctx->boxl, ctx->boyl, ctx->bozl, d.th, d.err);
+    MDX_LAUNCHED(ctx);
+  }
+  return MDX_OK;
+}
+
+int launch_vira(mdx_ctx *ctx, int from_viran) {
+  if (from_viran)
+    k_vira_from_viran<<<1, 1, 0, ctx->stream>>>(ctx->dv.th);
+  else
+    k_vira_zero<<<1, 1, 0, ctx->stream>>>(ctx->dv.th);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_record(mdx_ctx *ctx, int slot, int mstep) {
+  k_record<<<1, 1, 0, ctx->stream>>>(ctx->dv.rec, slot, mstep, ctx->dv.sc, ctx->dv.th);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}

@@ -1,0 +1,950 @@
+// mdx_api.cu -- the C ABI of include/mdx_gpu.h: context lifetime, uploads,
+// the force collectors FFORCES/SLFORCES/ALLFORCE (forces.f:36-100) and the
+// DOUBLE / SULTAN step loops (mdstep.f:29-530), all device resident.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mdx_internal.cuh"
+
+// integrate.cu
+int launch_getemp(mdx_ctx *ctx);
+int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale);
+int launch_mstep1_rescale(mdx_ctx *ctx);
+int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
+int launch_leapfrog_shake(mdx_ctx *ctx);
+int launch_vira(mdx_ctx *ctx, int from_viran);
+size_t scal_scratch_bytes();
+// bonded.cu
+int launch_bonded(mdx_ctx *ctx, int laver);
+
+namespace {
+
+#define RC(x)                \
+  do {                       \
+    int rc_ = (x);           \
+    if (rc_) return rc_;     \
+  } while (0)
+
+template <typename T>
+int dmalloc(mdx_ctx *ctx, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * n);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return MDX_ERR_NOMEM;
+  }
+  cudaMemset(*p, 0, sizeof(T) * n);
+  return MDX_OK;
+}
+
+template <typename T>
+int upload(mdx_ctx *ctx, T *dst, const T *src, size_t n) {
+  if (!n) return MDX_OK;
+  if (!src) {
+    ctx->err = "null input array";
+    return MDX_ERR_ARG;
+  }
+  MDX_CUDA(cudaMemcpy(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+  return MDX_OK;
+}
+
+__global__ void k_com_only(int nop, const int *mol_first, const int *mol_nat,
+                           const int *mol_type, const double *amass,
+                           const dbl4 *pos, double *X, double *Y, double *Z,
+                           const double *summas, double bx, double by,
+                           double bz) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nop) return;
+  const int f = mol_first[m], na = mol_nat[m];
+  double x = 0., y = 0., z = 0.;
+  for (int k = 0; k < na; ++k) {
+    const dbl4 p = pos[f + k];
+    x = x + amass[f + k] * p.x;
+    y = y + amass[f + k] * p.y;
+    z = z + amass[f + k] * p.z;
+  }
+  const double s = summas[mol_type[m]];
+  x = x / s;
+  y = y / s;
+  z = z / s;
+  pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  X[m] = x;
+  Y[m] = y;
+  Z[m] = z;
+}
+
+__global__ void k_set_pos(int n, const double *sx, const double *sy,
+                          const double *sz, const double *q, dbl4 *pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dbl4 p;
+  p.x = sx[i];
+  p.y = sy[i];
+  p.z = sz[i];
+  p.w = q[i];
+  pos[i] = p;
+}
+
+__global__ void k_get_pos(int n, const dbl4 *pos, double *sx, double *sy,
+                          double *sz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const dbl4 p = pos[i];
+  sx[i] = p.x;
+  sy[i] = p.y;
+  sz[i] = p.z;
+}
+
+__global__ void k_set_q(int n, const double *q, dbl4 *pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  pos[i].w = q[i];
+}
+
+int check_err(mdx_ctx *ctx) {
+  int herr = 0;
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  MDX_CUDA(cudaMemcpy(&herr, ctx->dv.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!herr) return MDX_OK;
+  MDX_CUDA(cudaMemset(ctx->dv.err, 0, sizeof(int)));
+  if (herr & (DERR_LIST_SHORT | DERR_LIST_LONG)) {
+    int need[2] = {0, 0};
+    cudaMemcpy(need, ctx->dv.shake_iter + 4, sizeof(int) * 2, cudaMemcpyDeviceToHost);
+    char b[256];
+    snprintf(b, sizeof b,
+             "neighbour list overfilled: short row needs %d (cap %d), long row "
+             "needs %d (cap %d); reopen with larger cap_short/cap_long",
+             need[0], ctx->dv.cap_s, need[1], ctx->dv.cap_l);
+    ctx->err = b;
+    return MDX_ERR_LIST_OVERFLOW;
+  }
+  if (herr & DERR_TEMP) {
+    ctx->err = "Temperature control stopped the program";
+    return MDX_ERR_NAN;
+  }
+  if (herr & DERR_NAN) {
+    ctx->err = "non-finite value";
+    return MDX_ERR_NAN;
+  }
+  if (herr & DERR_NPT) {
+    ctx->err = "repeated failure of NPT-algorithm";
+    return MDX_ERR_NAN;
+  }
+  if (herr & DERR_SHAKE) {
+    // the reference prints and continues (mdstep.f:1264-1269); the count is
+    // in mdx_thermo.shake_fail
+    return MDX_OK;
+  }
+  ctx->err = "device error";
+  return MDX_ERR_CUDA;
+}
+
+int copy_scalars(mdx_ctx *ctx, mdx_scalars *out) {
+  if (!out) return MDX_OK;
+  MDX_CUDA(cudaMemcpy(out, ctx->dv.sc, sizeof(mdx_scalars), cudaMemcpyDeviceToHost));
+  out->nkv = ctx->nkv;
+  return MDX_OK;
+}
+
+// fixed-point scales of the mixed path: a force count is 1e-10 kJ/mol/A and
+// an energy count 1e-9 kJ/mol, rounded to powers of two
+void set_fix_scales(mdx_ctx *ctx) {
+  const double efact = ctx->p.efact > 0 ? ctx->p.efact : 1.0;
+  const double fs = std::exp2(std::round(std::log2(1.0e10 / efact)));
+  const double es = std::exp2(std::round(std::log2(1.0e9 / efact)));
+  ctx->fix.scale = fs;
+  ctx->fix.inv = 1.0 / fs;
+  ctx->fix.escale = es;
+  ctx->fix.einv = 1.0 / es;
+}
+
+int require(mdx_ctx *ctx, bool topo, bool par, bool state) {
+  if ((topo && !ctx->have_topo) || (par && !ctx->have_params) ||
+      (state && !ctx->have_state)) {
+    ctx->err = "call order: topology, parameters and state must be uploaded first";
+    return MDX_ERR_STATE;
+  }
+  return MDX_OK;
+}
+
+// ---------------------------------------------------------------- forces
+int do_fforces(mdx_ctx *ctx, int laver, bool split) {
+  RC(launch_zero_fast(ctx));
+  if (ctx->mixed()) RC(launch_mirror_f32(ctx));
+  RC(launch_localf(ctx, split));
+  if (!ctx->mixed()) RC(launch_wir(ctx, 1));
+  RC(launch_bonded(ctx, laver));
+  if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
+  RC(launch_sclfrc(ctx, 1));
+  return MDX_OK;
+}
+
+int do_slow_parts(mdx_ctx *ctx, bool split) {
+  if (ctx->mixed()) {
+    RC(launch_mirror_f32(ctx));
+    RC(launch_forces_long(ctx, split));  // stores G first
+    RC(launch_furir(ctx));
+    RC(launch_eterms(ctx));
+    RC(launch_fix_to_double(ctx, 2));
+  } else {
+    RC(launch_furir(ctx));
+    RC(launch_eterms(ctx));
+    RC(launch_forces_long(ctx, split));
+  }
+  return MDX_OK;
+}
+
+int do_slforces(mdx_ctx *ctx, bool split) {
+  RC(launch_zero_slow(ctx));
+  RC(do_slow_parts(ctx, split));
+  RC(launch_wir(ctx, 2));
+  RC(launch_sclfrc(ctx, 2));
+  return MDX_OK;
+}
+
+int do_allforce(mdx_ctx *ctx, bool split) {
+  RC(launch_zero_fast(ctx));
+  RC(launch_zero_slow(ctx));
+  if (ctx->mixed()) RC(launch_mirror_f32(ctx));
+  RC(launch_localf(ctx, split));
+  if (!ctx->mixed()) RC(launch_wir(ctx, 1));
+  RC(launch_bonded(ctx, split ? 1 : 0));
+  if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
+  RC(do_slow_parts(ctx, split));
+  RC(launch_wir(ctx, 2));
+  RC(launch_sum_forces(ctx));
+  RC(launch_sclfrc(ctx, 3));
+  return MDX_OK;
+}
+
+int sync_box_from_device(mdx_ctx *ctx) {
+  double b[3];
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  MDX_CUDA(cudaMemcpy(b, &ctx->dv.th->boxl, sizeof b, cudaMemcpyDeviceToHost));
+  ctx->boxl = b[0];
+  ctx->boyl = b[1];
+  ctx->bozl = b[2];
+  return MDX_OK;
+}
+
+// one long step of DOUBLE (mdstep.f:324-436)
+int double_step(mdx_ctx *ctx, int mstep, int slot) {
+  const mdx_params &p = ctx->p;
+  const int NFREQ = p.nfreq, NFREQ2 = NFREQ / 2 + 1;
+  const double HTSTEP = 0.5 * p.tstep, TSTEB = p.tsteb, HTSTEB = 0.5 * p.tsteb;
+  bool pend = false;
+  RC(launch_scaling(ctx, 1, &pend));
+  if (p.lnpt) RC(sync_box_from_device(ctx));
+  RC(launch_kick(ctx, 2, HTSTEP, pend));
+  for (int s = 1; s <= NFREQ; ++s) {
+    RC(launch_kick_drift(ctx, HTSTEB, TSTEB, s > 1 ? 1 : 0));
+    RC(launch_getcom(ctx));
+    if (s == NFREQ2 && mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
+    if (s == NFREQ) {
+      RC(do_slforces(ctx, false));
+      RC(do_fforces(ctx, 0, false));
+    } else {
+      RC(do_fforces(ctx, 0, false));
+    }
+  }
+  RC(launch_kick(ctx, 1, HTSTEB, false));
+  RC(launch_kick(ctx, 2, HTSTEP, false));
+  RC(launch_scaling(ctx, 2, nullptr));
+  if (p.lnpt) RC(sync_box_from_device(ctx));
+  if (slot >= 0) RC(launch_record(ctx, slot, mstep));
+  return MDX_OK;
+}
+
+// one step of SULTAN (mdstep.f:83-162)
+int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
+  const mdx_params &p = ctx->p;
+  RC(launch_leapfrog_shake(ctx));
+  if (mstep == 1) RC(launch_mstep1_rescale(ctx));
+  RC(launch_vira(ctx, 1));
+  RC(launch_scaling(ctx, 3, nullptr));
+  if (p.lnpt) RC(sync_box_from_device(ctx));
+  RC(launch_getcom(ctx));
+  if (mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
+  RC(do_allforce(ctx, false));
+  if (slot >= 0) RC(launch_record(ctx, slot, mstep));
+  return MDX_OK;
+}
+
+int ensure_records(mdx_ctx *ctx, int n) {
+  if (n <= ctx->dv.rec_cap) return MDX_OK;
+  if (ctx->dv.rec) cudaFree(ctx->dv.rec);
+  RC(dmalloc(ctx, &ctx->dv.rec, (size_t)n));
+  ctx->dv.rec_cap = n;
+  return MDX_OK;
+}
+
+int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
+              mdx_step_record *rec) {
+  RC(require(ctx, true, true, true));
+  if (!ctx->have_lists) {
+    ctx->err = "neighbour lists not built (call the prologue first)";
+    return MDX_ERR_STATE;
+  }
+  if (rec) RC(ensure_records(ctx, nsteps));
+  for (int s = 1; s <= nsteps; ++s) {
+    const int mstep = mstep0 + s;
+    if (dbl)
+      RC(double_step(ctx, mstep, rec ? s - 1 : -1));
+    else
+      RC(sultan_step(ctx, mstep, rec ? s - 1 : -1));
+  }
+  RC(check_err(ctx));
+  if (rec) {
+    MDX_CUDA(cudaMemcpy(rec, ctx->dv.rec, sizeof(mdx_step_record) * nsteps,
+                        cudaMemcpyDeviceToHost));
+  }
+  return MDX_OK;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int mdx_version(void) { return 1; }
+
+const char *mdx_strerror(int code) {
+  switch (code) {
+    case MDX_OK: return "ok";
+    case MDX_ERR_ARG: return "bad argument";
+    case MDX_ERR_CUDA: return "CUDA error";
+    case MDX_ERR_LIST_OVERFLOW: return "neighbour list overflow";
+    case MDX_ERR_SHAKE: return "SHAKE did not converge";
+    case MDX_ERR_NAN: return "non-finite value or watchdog";
+    case MDX_ERR_TIMEOUT: return "device wait timed out";
+    case MDX_ERR_STATE: return "call order";
+    case MDX_ERR_NOMEM: return "device allocation failed";
+    case MDX_ERR_KVEC: return "too many k-vectors";
+    case MDX_ERR_UNSUPPORTED: return "unsupported option";
+  }
+  return "unknown";
+}
+
+const char *mdx_last_error(const mdx_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
+  if (!dims || !out) return MDX_ERR_ARG;
+  *out = nullptr;
+  if (dims->nstot <= 0 || dims->nop <= 0 || dims->ntypes <= 0 ||
+      dims->ntypes > MDX_NT || dims->nnbt <= 0 || dims->nsites <= 0 ||
+      (dims->precision != MDX_FP64 && dims->precision != MDX_MIXED))
+    return MDX_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MDX_ERR_CUDA;
+  mdx_ctx *ctx = new (std::nothrow) mdx_ctx();
+  if (!ctx) return MDX_ERR_NOMEM;
+  ctx->d = *dims;
+  if (ctx->d.cap_short <= 0) ctx->d.cap_short = 64;
+  if (ctx->d.cap_long <= 0) ctx->d.cap_long = 1000;
+  if (ctx->d.nkv_max <= 0) ctx->d.nkv_max = 100000;
+  if (ctx->d.precision == MDX_MIXED) {  // full rows hold both copies of a pair
+    ctx->d.cap_short *= 2;
+    ctx->d.cap_long *= 2;
+  }
+  cudaGetDevice(&ctx->device);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return MDX_ERR_CUDA;
+  }
+  DevData &d = ctx->dv;
+  const size_t n = dims->nstot;
+  d.n = dims->nstot;
+  d.nop = dims->nop;
+  d.ntypes = dims->ntypes;
+  d.nnbt = dims->nnbt;
+  d.nbdmax = std::max(1, dims->nbdmax);
+  d.cap_s = ctx->d.cap_short;
+  d.cap_l = ctx->d.cap_long;
+  int rc = MDX_OK;
+#define AL(p, cnt) \
+  if (!rc) rc = dmalloc(ctx, &p, cnt)
+  AL(d.pos, n);
+  AL(d.posf, n);
+  AL(d.posi, n);
+  AL(d.qsitef, n);
+  AL(d.vx, 3 * n);
+  AL(d.massdi, n);
+  AL(d.amass, n);
+  AL(d.qsite, n);
+  AL(d.ainfo, n);
+  AL(d.nnbb, n);
+  AL(d.inbb, n * d.nbdmax);
+  AL(d.mol_first, (size_t)dims->nop);
+  AL(d.mol_nat, (size_t)dims->nop);
+  AL(d.mol_type, (size_t)dims->nop);
+  AL(d.X, 3 * (size_t)dims->nop);
+  AL(d.gx, 9 * n);
+  AL(d.ox, 3 * n);
+  AL(d.ns_cnt, n);
+  AL(d.nl_cnt, n);
+  AL(d.ns_idx, n * d.cap_s);
+  AL(d.nl_idx, n * d.cap_l);
+  AL(d.atom_cell, n);
+  AL(d.cell_list, n);
+  AL(d.sc, 1);
+  AL(d.th, 1);
+  AL(d.err, 4);
+  AL(d.shake_iter, 32);
+  AL(d.red, 512);
+  if (!rc) {
+    unsigned char *ss = nullptr;
+    rc = dmalloc(ctx, &ss, scal_scratch_bytes());
+    d.scal_scratch = ss;
+  }
+  if (!rc && dims->precision == MDX_MIXED) {
+    AL(d.gfix, 3 * n);
+    AL(d.hfix, 3 * n);
+  }
+#undef AL
+  if (rc) {
+    std::string e = ctx->err;
+    mdx_close(ctx);
+    return rc;
+  }
+  d.vy = d.vx + n;
+  d.vz = d.vy + n;
+  d.Y = d.X + dims->nop;
+  d.Z = d.Y + dims->nop;
+  d.gy = d.gx + n;
+  d.gz = d.gy + n;
+  d.hx = d.gz + n;
+  d.hy = d.hx + n;
+  d.hz = d.hy + n;
+  d.fx = d.hz + n;
+  d.fy = d.fx + n;
+  d.fz = d.fy + n;
+  d.oy = d.ox + n;
+  d.oz = d.oy + n;
+  *out = ctx;
+  return MDX_OK;
+}
+
+int mdx_close(mdx_ctx *ctx) {
+  if (!ctx) return MDX_OK;
+  DevData &d = ctx->dv;
+  void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.vx, d.massdi, d.amass, d.qsite,
+                  d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
+                  d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
+                  d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f,
+                  d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
+                  d.ar, d.tr, d.cols, d.kchunks, d.tabx, d.tabxf, d.sk, d.sc, d.th,
+                  d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MDX_OK;
+}
+
+int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
+  if (!ctx || !t) return MDX_ERR_ARG;
+  DevData &d = ctx->dv;
+  const int n = d.n, nt = ctx->d.ntypes, ns = ctx->d.nsites, nb = ctx->d.nnbt;
+  ctx->h_itype.assign(t->itype, t->itype + n);
+  ctx->h_nnum.assign(t->nnum, t->nnum + n);
+  ctx->h_nsite.assign(t->nsite, t->nsite + n);
+  ctx->h_charge.assign(t->charge, t->charge + ns);
+  ctx->h_mass.assign(t->mass, t->mass + ns);
+  for (int i = 0; i < n; ++i)
+    if (t->itype[i] < 1 || t->itype[i] > nt || t->nnum[i] < 1 ||
+        t->nnum[i] > ctx->d.nop || t->nsite[i] < 1 || t->nsite[i] > ns) {
+      ctx->err = "ITYPE/NNUM/NSITE out of range";
+      return MDX_ERR_ARG;
+    }
+  // per type
+  TypeConst &tc = ctx->tc;
+  tc = TypeConst{};
+  tc.ntypes = nt;
+  for (int k = 0; k < nt; ++k) {
+    tc.lmove[k] = t->lmove[k];
+    tc.iee[k] = t->iee[k];
+    tc.ipot[k] = t->ipot[k];
+    tc.c14el[k] = t->c14el[k];
+    tc.c14lj[k] = t->c14lj[k];
+    for (int j = 0; j < nt; ++j) tc.mdx[k][j] = t->mdx[(size_t)k + (size_t)j * t->ld_mdx] - 1;
+    ctx->nspec[k] = t->nspec[k];
+    ctx->nsits[k] = t->nsits[k];
+    ctx->isadr[k] = t->isadr[k];
+    ctx->isaddr[k] = t->isaddr[k];
+    ctx->iaddr[k] = t->iaddr[k];
+    ctx->nrb[k] = t->nrb[k];
+    ctx->iadb[k] = t->iadb[k];
+    ctx->ishejk[k] = t->ishejk[k];
+    ctx->summas[k] = t->summas[k];
+  }
+  // per atom
+  std::vector<int4> ai(n);
+  std::vector<double> amass(n), qsite(n);
+  std::vector<float> qsitef(n);
+  for (int i = 0; i < n; ++i) {
+    const int site = t->nsite[i] - 1;
+    ai[i] = make_int4(t->itype[i] - 1, t->nnum[i] - 1, t->inbt[site] - 1, site);
+    amass[i] = t->mass[site];
+    qsite[i] = t->charge[site];
+    qsitef[i] = (float)t->charge[site];
+  }
+  RC(upload(ctx, d.ainfo, ai.data(), n));
+  RC(upload(ctx, d.massdi, t->massdi, n));
+  RC(upload(ctx, d.amass, amass.data(), n));
+  RC(upload(ctx, d.qsite, qsite.data(), n));
+  RC(upload(ctx, d.qsitef, qsitef.data(), n));
+  ctx->h_q.assign(t->q, t->q + n);
+  // molecules: atoms are contiguous per molecule, molecules per type
+  std::vector<int> mf(d.nop, -1), mn(d.nop, 0), mt(d.nop, 0);
+  for (int i = 0; i < n; ++i) {
+    const int m = t->nnum[i] - 1;
+    if (mf[m] < 0) mf[m] = i;
+    mn[m] += 1;
+    mt[m] = t->itype[i] - 1;
+  }
+  for (int m = 0; m < d.nop; ++m)
+    if (mn[m] > 128) {
+      ctx->err = "molecules above 128 atoms are not supported by SHEJK";
+      return MDX_ERR_UNSUPPORTED;
+    }
+  RC(upload(ctx, d.mol_first, mf.data(), d.nop));
+  RC(upload(ctx, d.mol_nat, mn.data(), d.nop));
+  RC(upload(ctx, d.mol_type, mt.data(), d.nop));
+  // exclusions INBB(ld, nbdmax) -> row-major [atom][k]
+  std::vector<int> inbb((size_t)n * d.nbdmax, 0);
+  for (int k = 0; k < ctx->d.nbdmax; ++k)
+    for (int i = 0; i < n; ++i) inbb[(size_t)i * d.nbdmax + k] = t->inbb[(size_t)i + (size_t)k * t->ld_inbb];
+  RC(upload(ctx, d.nnbb, t->nnbb, n));
+  RC(upload(ctx, d.inbb, inbb.data(), inbb.size()));
+  // LJ tables (column-major ld_lj) -> [i*nnbt + j], double and float
+  const size_t nn = (size_t)nb * nb;
+  if (!d.a6lj) {
+    RC(dmalloc(ctx, &d.a6lj, 6 * nn));
+    RC(dmalloc(ctx, &d.a6f, 6 * nn));
+  }
+  d.b12lj = d.a6lj + nn; d.a6lj0 = d.b12lj + nn; d.b12lj0 = d.a6lj0 + nn;
+  d.a6_14 = d.b12lj0 + nn; d.b12_14 = d.a6_14 + nn;
+  d.b12f = d.a6f + nn; d.a60f = d.b12f + nn; d.b120f = d.a60f + nn;
+  d.a614f = d.b120f + nn; d.b1214f = d.a614f + nn;
+  std::vector<double> lj(6 * nn);
+  std::vector<float> ljf(6 * nn);
+  const double *src[6] = {t->a6lj, t->b12lj, t->a6lj0, t->b12lj0, t->a6_14, t->b12_14};
+  for (int k = 0; k < 6; ++k)
+    for (int i = 0; i < nb; ++i)
+      for (int j = 0; j < nb; ++j) {
+        double v = src[k][(size_t)i + (size_t)j * t->ld_lj];
+        lj[k * nn + (size_t)i * nb + j] = v;
+        ljf[k * nn + (size_t)i * nb + j] = (float)v;
+      }
+  RC(upload(ctx, d.a6lj, lj.data(), lj.size()));
+  RC(upload(ctx, d.a6f, ljf.data(), ljf.size()));
+  ctx->h_a6lj0.assign(lj.begin() + 2 * nn, lj.begin() + 3 * nn);
+  ctx->h_b12lj0.assign(lj.begin() + 3 * nn, lj.begin() + 4 * nn);
+  ctx->h_inbt.assign(t->inbt, t->inbt + ns);
+  // bonded: records and instances (indices to 0-based)
+  d.nrbb = ctx->d.nrbb; d.nraa = ctx->d.nraa; d.nrtt = ctx->d.nrtt;
+  d.nrbt = ctx->d.nrbt; d.nrat = ctx->d.nrat; d.nrrt = ctx->d.nrrt;
+  ctx->h_rb.assign(t->rb, t->rb + d.nrbb);
+  ctx->h_fb.assign(t->fb, t->fb + d.nrbb);
+  ctx->h_db.assign(t->db, t->db + d.nrbb);
+  ctx->h_ro.assign(t->ro, t->ro + d.nrbb);
+  auto m1 = [](const int32_t *a, int cnt) {
+    std::vector<int> v(cnt);
+    for (int i = 0; i < cnt; ++i) v[i] = a[i] - 1;
+    return v;
+  };
+  if (!d.bid) {
+    RC(dmalloc(ctx, &d.bid, 3 * (size_t)std::max(1, d.nrbb)));
+    RC(dmalloc(ctx, &d.brb, 4 * (size_t)std::max(1, d.nrbb)));
+    RC(dmalloc(ctx, &d.ibi, 3 * (size_t)std::max(1, d.nrbt)));
+    RC(dmalloc(ctx, &d.ara, 2 * (size_t)std::max(1, d.nraa)));
+    RC(dmalloc(ctx, &d.iai, 4 * (size_t)std::max(1, d.nrat)));
+    RC(dmalloc(ctx, &d.titors, 2 * (size_t)std::max(1, d.nrtt)));
+    RC(dmalloc(ctx, &d.tft, 7 * (size_t)std::max(1, d.nrtt)));
+    RC(dmalloc(ctx, &d.iti, 5 * (size_t)std::max(1, d.nrrt)));
+    RC(dmalloc(ctx, &d.br, 2 * (size_t)std::max(1, d.nrbb)));
+    RC(dmalloc(ctx, &d.ar, 2 * (size_t)std::max(1, d.nraa)));
+    RC(dmalloc(ctx, &d.tr, 2 * (size_t)std::max(1, d.nrtt)));
+    RC(dmalloc(ctx, &d.nspec_d, MDX_NT));
+  }
+  const int rbb = std::max(1, d.nrbb);
+  d.bib = d.bid + rbb; d.bjb = d.bib + rbb;
+  d.bfb = d.brb + rbb; d.bdb = d.bfb + rbb; d.bro = d.bdb + rbb;
+  d.jbj = d.ibi + std::max(1, d.nrbt); d.ibuk = d.jbj + std::max(1, d.nrbt);
+  d.afa = d.ara + std::max(1, d.nraa);
+  d.jaj = d.iai + std::max(1, d.nrat); d.kak = d.jaj + std::max(1, d.nrat);
+  d.iauk = d.kak + std::max(1, d.nrat);
+  d.tnmul = d.titors + std::max(1, d.nrtt);
+  {
+    const int r = std::max(1, d.nrtt);
+    d.trt = d.tft + r; d.tft1 = d.trt + r; d.tft2 = d.tft1 + r; d.tft3 = d.tft2 + r;
+    d.tft4 = d.tft3 + r; d.tft5 = d.tft4 + r;
+  }
+  {
+    const int r = std::max(1, d.nrrt);
+    d.jtj = d.iti + r; d.ktk = d.jtj + r; d.ltl = d.ktk + r; d.ituk = d.ltl + r;
+  }
+  d.be = d.br + std::max(1, d.nrbb);
+  d.ae = d.ar + std::max(1, d.nraa);
+  d.te = d.tr + std::max(1, d.nrtt);
+  RC(upload(ctx, d.bid, t->id, d.nrbb));
+  RC(upload(ctx, d.bib, t->ib, d.nrbb));
+  RC(upload(ctx, d.bjb, t->jb, d.nrbb));
+  RC(upload(ctx, d.brb, t->rb, d.nrbb));
+  RC(upload(ctx, d.bfb, t->fb, d.nrbb));
+  RC(upload(ctx, d.bdb, t->db, d.nrbb));
+  RC(upload(ctx, d.bro, t->ro, d.nrbb));
+  if (d.nrbt) {
+    auto a = m1(t->ibi, d.nrbt), b = m1(t->jbj, d.nrbt), c = m1(t->ibuk, d.nrbt);
+    RC(upload(ctx, d.ibi, a.data(), d.nrbt));
+    RC(upload(ctx, d.jbj, b.data(), d.nrbt));
+    RC(upload(ctx, d.ibuk, c.data(), d.nrbt));
+  }
+  RC(upload(ctx, d.ara, t->ra, d.nraa));
+  RC(upload(ctx, d.afa, t->fa, d.nraa));
+  if (d.nrat) {
+    auto a = m1(t->iai, d.nrat), b = m1(t->jaj, d.nrat), c = m1(t->kak, d.nrat),
+         e = m1(t->iauk, d.nrat);
+    RC(upload(ctx, d.iai, a.data(), d.nrat));
+    RC(upload(ctx, d.jaj, b.data(), d.nrat));
+    RC(upload(ctx, d.kak, c.data(), d.nrat));
+    RC(upload(ctx, d.iauk, e.data(), d.nrat));
+  }
+  RC(upload(ctx, d.titors, t->itors, d.nrtt));
+  RC(upload(ctx, d.tnmul, t->nmul, d.nrtt));
+  RC(upload(ctx, d.tft, t->ft, d.nrtt));
+  RC(upload(ctx, d.trt, t->rt, d.nrtt));
+  RC(upload(ctx, d.tft1, t->ft1, d.nrtt));
+  RC(upload(ctx, d.tft2, t->ft2, d.nrtt));
+  RC(upload(ctx, d.tft3, t->ft3, d.nrtt));
+  RC(upload(ctx, d.tft4, t->ft4, d.nrtt));
+  RC(upload(ctx, d.tft5, t->ft5, d.nrtt));
+  if (d.nrrt) {
+    auto a = m1(t->iti, d.nrrt), b = m1(t->jtj, d.nrrt), c = m1(t->ktk, d.nrrt),
+         e = m1(t->ltl, d.nrrt), f = m1(t->ituk, d.nrrt);
+    RC(upload(ctx, d.iti, a.data(), d.nrrt));
+    RC(upload(ctx, d.jtj, b.data(), d.nrrt));
+    RC(upload(ctx, d.ktk, c.data(), d.nrrt));
+    RC(upload(ctx, d.ltl, e.data(), d.nrrt));
+    RC(upload(ctx, d.ituk, f.data(), d.nrrt));
+  }
+  RC(upload(ctx, d.nspec_d, t->nspec, nt));
+  ctx->have_topo = true;
+  return MDX_OK;
+}
+
+int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
+  if (!ctx || !p) return MDX_ERR_ARG;
+  if (p->icell != 0) {
+    ctx->err = "only rectangular cells (ICELL=0) are built";
+    return MDX_ERR_UNSUPPORTED;
+  }
+  if (p->boxl <= 0 || p->boyl <= 0 || p->bozl <= 0 || p->rcut <= 0 || p->nfreq < 1 ||
+      p->ichnb < 1) {
+    ctx->err = "bad box, cutoff, NFREQ or ICHNB";
+    return MDX_ERR_ARG;
+  }
+  if (2.0 * (p->rcut + p->rskin) > std::min(p->boxl, std::min(p->boyl, p->bozl)) + 1e-9 &&
+      p->rcut + p->rskin > 0.5 * std::min(p->boxl, std::min(p->boyl, p->bozl))) {
+    // the reference allows it (single image per pair); so does the list build
+  }
+  ctx->p = *p;
+  ctx->pc.coulf = p->coulf;
+  ctx->pc.alphad = p->alphad;
+  ctx->pc.raex = p->raex;
+  ctx->pc.rff = p->rff;
+  ctx->pc.rff2 = p->rff2;
+  ctx->pc.lmnbl = p->lmnbl;
+  ctx->pc.lmdee = p->lmdee;
+  ctx->pc.nnbt = ctx->d.nnbt;
+  ctx->boxl = p->boxl;
+  ctx->boyl = p->boyl;
+  ctx->bozl = p->bozl;
+  ctx->furir_init = false;
+  set_fix_scales(ctx);
+  ctx->have_params = true;
+  return MDX_OK;
+}
+
+int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
+                     const double *sz, const double *vx, const double *vy,
+                     const double *vz, const mdx_thermo *th) {
+  if (!ctx || !sx || !sy || !sz || !vx || !vy || !vz) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, false));
+  DevData &d = ctx->dv;
+  const size_t n = d.n;
+  double *tmp = nullptr;
+  RC(dmalloc(ctx, &tmp, 4 * n));
+  int rc = MDX_OK;
+  rc = rc ? rc : upload(ctx, tmp, sx, n);
+  rc = rc ? rc : upload(ctx, tmp + n, sy, n);
+  rc = rc ? rc : upload(ctx, tmp + 2 * n, sz, n);
+  rc = rc ? rc : upload(ctx, tmp + 3 * n, ctx->h_q.data(), n);
+  if (!rc) {
+    k_set_pos<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, tmp, tmp + n, tmp + 2 * n,
+                                                         tmp + 3 * n, d.pos);
+    ctx->launches++;
+  }
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(tmp);
+  if (rc) return rc;
+  RC(upload(ctx, d.vx, vx, n));
+  RC(upload(ctx, d.vy, vy, n));
+  RC(upload(ctx, d.vz, vz, n));
+  mdx_thermo h{};
+  if (th) h = *th;
+  if (h.boxl > 0) {
+    ctx->boxl = h.boxl;
+    ctx->boyl = h.boyl;
+    ctx->bozl = h.bozl;
+  } else {
+    h.boxl = ctx->boxl;
+    h.boyl = ctx->boyl;
+    h.bozl = ctx->bozl;
+  }
+  h.vol = h.boxl * h.boyl * h.bozl;
+  RC(upload(ctx, d.th, &h, 1));
+  // molecular centres (the driver's last GETCOM left them consistent)
+  std::vector<double> sm(MDX_NT, 1.0);
+  for (int t = 0; t < ctx->d.ntypes; ++t) sm[t] = ctx->summas[t];
+  double *dsm = d.red + 256;
+  RC(upload(ctx, dsm, sm.data(), MDX_NT));
+  k_com_only<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
+      d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z, dsm,
+      ctx->boxl, ctx->boyl, ctx->bozl);
+  ctx->launches++;
+  RC(launch_mirror_f32(ctx));
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->have_state = true;
+  ctx->have_lists = false;
+  return MDX_OK;
+}
+
+int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
+                       double *vx, double *vy, double *vz, mdx_thermo *th) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  DevData &d = ctx->dv;
+  const size_t n = d.n;
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (sx || sy || sz) {
+    double *tmp = nullptr;
+    RC(dmalloc(ctx, &tmp, 3 * n));
+    k_get_pos<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.pos, tmp, tmp + n, tmp + 2 * n);
+    ctx->launches++;
+    cudaStreamSynchronize(ctx->stream);
+    if (sx) cudaMemcpy(sx, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (sy) cudaMemcpy(sy, tmp + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (sz) cudaMemcpy(sz, tmp + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+  }
+  if (vx) MDX_CUDA(cudaMemcpy(vx, d.vx, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (vy) MDX_CUDA(cudaMemcpy(vy, d.vy, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (vz) MDX_CUDA(cudaMemcpy(vz, d.vz, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (th) MDX_CUDA(cudaMemcpy(th, d.th, sizeof(mdx_thermo), cudaMemcpyDeviceToHost));
+  return MDX_OK;
+}
+
+int mdx_download_forces(mdx_ctx *ctx, int which, double *fx, double *fy, double *fz) {
+  if (!ctx || !fx || !fy || !fz || which < 1 || which > 3) return MDX_ERR_ARG;
+  DevData &d = ctx->dv;
+  const double *x = which == 1 ? d.hx : which == 2 ? d.gx : d.fx;
+  const double *y = which == 1 ? d.hy : which == 2 ? d.gy : d.fy;
+  const double *z = which == 1 ? d.hz : which == 2 ? d.gz : d.fz;
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  MDX_CUDA(cudaMemcpy(fx, x, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(fy, y, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(fz, z, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  return MDX_OK;
+}
+
+int mdx_inifur(mdx_ctx *ctx, int32_t *nkv) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, false));
+  RC(host_inifur(ctx));
+  ctx->furir_init = true;
+  ctx->boxlo = ctx->boxl;
+  ctx->boylo = ctx->boyl;
+  ctx->bozlo = ctx->bozl;
+  if (nkv) *nkv = ctx->nkv;
+  return MDX_OK;
+}
+
+int mdx_chcnb(mdx_ctx *ctx, int32_t *mbsh, int32_t *mbln) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  if (ctx->p.lmnbl) {
+    ctx->err = "reaction-field molecular cutoff list is not built";
+    return MDX_ERR_UNSUPPORTED;
+  }
+  RC(launch_build_lists(ctx));
+  RC(check_err(ctx));
+  int c[2];
+  MDX_CUDA(cudaMemcpy(c, &ctx->dv.sc->mbsh, sizeof c, cudaMemcpyDeviceToHost));
+  ctx->mbsh = c[0];
+  ctx->mbln = c[1];
+  if (mbsh) *mbsh = c[0];
+  if (mbln) *mbln = c[1];
+  return MDX_OK;
+}
+
+int mdx_get_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
+                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l) {
+  if (!ctx || !nbs1 || !nbs2 || !nbl1 || !nbl2) return MDX_ERR_ARG;
+  if (!ctx->have_lists) {
+    ctx->err = "no lists built";
+    return MDX_ERR_STATE;
+  }
+  return export_lists(ctx, nbs1, nbs2, cap_s, nbl1, nbl2, cap_l);
+}
+
+int mdx_getcom(mdx_ctx *ctx) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  RC(launch_getcom(ctx));
+  return check_err(ctx);
+}
+
+int mdx_fforces(mdx_ctx *ctx, int laver, mdx_scalars *out) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  if (!ctx->have_lists) {
+    ctx->err = "lists not built";
+    return MDX_ERR_STATE;
+  }
+  RC(do_fforces(ctx, laver, true));
+  RC(check_err(ctx));
+  return copy_scalars(ctx, out);
+}
+
+int mdx_slforces(mdx_ctx *ctx, mdx_scalars *out) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  if (!ctx->have_lists) {
+    ctx->err = "lists not built";
+    return MDX_ERR_STATE;
+  }
+  RC(do_slforces(ctx, true));
+  RC(check_err(ctx));
+  return copy_scalars(ctx, out);
+}
+
+int mdx_allforce(mdx_ctx *ctx, mdx_scalars *out) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  if (!ctx->have_lists) {
+    ctx->err = "lists not built";
+    return MDX_ERR_STATE;
+  }
+  RC(do_allforce(ctx, true));
+  RC(check_err(ctx));
+  return copy_scalars(ctx, out);
+}
+
+int mdx_double_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, mdx_step_record *rec) {
+  if (!ctx || nsteps < 0) return MDX_ERR_ARG;
+  return run_steps(ctx, true, nsteps, mstep0, rec);
+}
+
+int mdx_double(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot, mdx_step_record *rec) {
+  if (!ctx || nsteps < 0) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  RC(launch_vira(ctx, 0));
+  RC(launch_build_lists(ctx));
+  RC(launch_getcom(ctx));
+  RC(do_slforces(ctx, false));
+  RC(do_fforces(ctx, 1, false));
+  RC(check_err(ctx));
+  return run_steps(ctx, true, nsteps, nsttot, rec);
+}
+
+int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, mdx_step_record *rec) {
+  if (!ctx || nsteps < 0) return MDX_ERR_ARG;
+  return run_steps(ctx, false, nsteps, mstep0, rec);
+}
+
+int mdx_sultan(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot, mdx_step_record *rec) {
+  if (!ctx || nsteps < 0) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  RC(launch_build_lists(ctx));
+  RC(launch_getemp(ctx));
+  RC(do_allforce(ctx, false));
+  RC(check_err(ctx));
+  return run_steps(ctx, false, nsteps, nsttot, rec);
+}
+
+// RECINT (mdee.f:86-140)
+int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, false));
+  DevData &d = ctx->dv;
+  const int nt = ctx->d.ntypes, nb = ctx->d.nnbt;
+  const size_t nn = (size_t)nb * nb;
+  std::vector<double> a6(nn), b12(nn);
+  std::vector<float> a6f(nn), b12f(nn);
+  MDX_CUDA(cudaMemcpy(a6.data(), d.a6lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(b12.data(), d.b12lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  ctx->spei = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    const double ESCI = ctx->tc.iee[t] == 0 ? std::pow(ec, pw1) : 1.0;
+    for (int I = ctx->isadr[t] + 1; I <= ctx->isadr[t] + ctx->nsits[t]; ++I) {
+      const int IS = ctx->h_inbt[I - 1] - 1;
+      for (int u = 0; u < nt; ++u) {
+        double ESCL = ESCI;
+        if (ctx->tc.iee[u] == 0) ESCL = std::pow(ec, pw1);
+        for (int J = ctx->isadr[u] + 1; J <= ctx->isadr[u] + ctx->nsits[u]; ++J) {
+          const int JS = ctx->h_inbt[J - 1] - 1;
+          a6[(size_t)IS * nb + JS] = ESCL * ctx->h_a6lj0[(size_t)IS * nb + JS];
+          b12[(size_t)IS * nb + JS] = ESCL * ctx->h_b12lj0[(size_t)IS * nb + JS];
+        }
+      }
+    }
+    for (int ISP = ctx->isaddr[t] + 1; ISP <= ctx->isaddr[t] + ctx->nsits[t] * ctx->nspec[t]; ++ISP)
+      ctx->h_q[ISP - 1] = ESCI * ctx->h_charge[ctx->h_nsite[ISP - 1] - 1];
+    double SPET = 0.0;
+    for (int I = 1; I <= ctx->nsits[t]; ++I) {
+      const int IS = ctx->isadr[t] + I;
+      const double eq = ESCI * ctx->h_charge[IS - 1];
+      const double QII = ctx->p.coulf * (eq * eq);
+      SPET = SPET - ctx->nspec[t] * ctx->p.alphad * QII / std::sqrt(3.1415926536);
+    }
+    ctx->speei[t] = SPET;
+    ctx->spei = ctx->spei + SPET;
+  }
+  for (size_t k = 0; k < nn; ++k) {
+    a6f[k] = (float)a6[k];
+    b12f[k] = (float)b12[k];
+  }
+  RC(upload(ctx, d.a6lj, a6.data(), nn));
+  RC(upload(ctx, d.b12lj, b12.data(), nn));
+  RC(upload(ctx, d.a6f, a6f.data(), nn));
+  RC(upload(ctx, d.b12f, b12f.data(), nn));
+  ctx->p.raex = bee * (1. - std::pow(ec, pw2));
+  ctx->p.ec_me = ec;
+  ctx->pc.raex = ctx->p.raex;
+  if (ctx->have_state) {
+    double *dq = nullptr;
+    RC(dmalloc(ctx, &dq, d.n));
+    RC(upload(ctx, dq, ctx->h_q.data(), d.n));
+    k_set_q<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, dq, d.pos);
+    ctx->launches++;
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(dq);
+  }
+  return MDX_OK;
+}
+
+void *mdx_stream(mdx_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+int64_t mdx_launch_count(const mdx_ctx *ctx) { return ctx ? ctx->launches : 0; }
+int mdx_sync(mdx_ctx *ctx) {
+  if (!ctx) return MDX_ERR_ARG;
+  return check_err(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,302 @@
+// mdx_internal.cuh -- device data layout and shared helpers of libmdxgpu.
+//
+// One context holds one system resident in HBM.  Layout (structure of
+// arrays, one entry per atom unless noted):
+//   pos     dbl4 {x, y, z, Q}       master coordinates + (EE-scaled) charge
+//   posf    float4  {x, y, z, Q}       FP32 mirror for the mixed path
+//   vx..vz  double                     momenta (the reference's VX/VY/VZ)
+//   ainfo   int4 {type, molecule, LJ type, site}   all 0-based
+//   gx..hz  double                     slow (G) and fast (H) forces
+//   gfix..  long long                  64-bit fixed-point force sums (mixed)
+//   lists   int [atom][cap]            per-owner neighbour rows (see nblist)
+// Scalars (energies, virials) live in one mdx_scalars block, thermostat state
+// in one mdx_thermo block, both in device memory so that a whole long step
+// runs without a host round trip.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mdx_gpu.h"
+
+#define MDX_NT MDX_NTPS
+
+// 32-byte aligned double4: one 256-bit load per atom record.
+typedef double4_32a dbl4;
+
+// Constants of the reference (common_inc.f:22-33).
+#define MDX_A1 0.254829592
+#define MDX_A2 (-0.284496736)
+#define MDX_A3 1.421413741
+#define MDX_A4 (-1.453152027)
+#define MDX_A5 1.061405429
+#define MDX_B1 0.3275911
+#define MDX_PI 3.1415926536
+#define MDX_TOTPI 1.128379169
+
+// Device error word bits.
+enum : int {
+  DERR_LIST_SHORT = 1,
+  DERR_LIST_LONG = 2,
+  DERR_NAN = 4,
+  DERR_SHAKE = 8,
+  DERR_NPT = 16,
+  DERR_TEMP = 32,
+  DERR_CELL = 64,
+};
+
+// Per-type constants passed by value to kernels.
+struct TypeConst {
+  int ntypes;
+  int lmove[MDX_NT];
+  int iee[MDX_NT];
+  int ipot[MDX_NT];
+  double c14el[MDX_NT];
+  double c14lj[MDX_NT];
+  int mdx[MDX_NT][MDX_NT];  // 0-based type pair index
+};
+
+// Box and electrostatics parameters for the force kernels.
+struct PairConst {
+  double coulf, alphad, raex, rff, rff2;
+  int lmnbl, lmdee, nnbt;
+};
+
+// Cell grid used by the list build.
+struct CellGrid {
+  int nx, ny, nz, ncell;
+  double cx, cy, cz;  // cell edge lengths
+};
+
+// Ewald k-space layout: k-vectors grouped in columns of fixed (nx, ny) with a
+// contiguous nz range; tables of per-atom phase factors e^{i n theta}.
+struct KCol {
+  int nx, ny, nzlo, nzhi;  // integer k components (rectangular cell)
+  int koff;                // first k of the column in the column-ordered list
+};
+
+// Scratch for fixed-point accumulation of the mixed path: forces are stored
+// as round(F * 2^fx_shift) in 64-bit integers.
+struct FixScale {
+  double scale, inv;    // forces
+  double escale, einv;  // energies and virials
+};
+
+// Destination pointers of a block reduction, passed by value to kernels.
+struct Dst6 {
+  double *p[6];
+};
+
+struct DevData {
+  int n, nop, ntypes, nnbt, nbdmax;
+  dbl4 *pos;
+  float4 *posf;      // FP32 mirror (list prefilter)
+  int4 *posi;        // 32-bit fixed-point coordinates + FP32 charge bits
+  float *qsitef;     // CHARGE(NSITE(i)) in FP32
+  double *vx, *vy, *vz;
+  double *massdi, *amass, *qsite;
+  int4 *ainfo;
+  int *nnbb, *inbb;  // inbb[i*nbdmax + k] = signed 1-based partner (Fortran value)
+  // molecules
+  int *mol_first, *mol_nat, *mol_type;
+  double *X, *Y, *Z;
+  // forces
+  double *gx, *gy, *gz, *hx, *hy, *hz, *fx, *fy, *fz;
+  double *ox, *oy, *oz;
+  unsigned long long *gfix, *hfix;  // 3n each, x then y then z
+  // lists
+  int cap_s, cap_l;
+  int *ns_cnt, *nl_cnt, *ns_idx, *nl_idx;
+  int *cell_cnt, *cell_start, *cell_list, *atom_cell;
+  // LJ tables [i*nnbt + j]
+  double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
+  float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
+  // bonded
+  int nrbb, nraa, nrtt, nrbt, nrat, nrrt;
+  int *bid, *bib, *bjb;
+  double *brb, *bfb, *bdb, *bro;
+  int *ibi, *jbj, *ibuk;
+  double *ara, *afa;
+  int *iai, *jaj, *kak, *iauk;
+  int *titors, *tnmul;
+  double *tft, *trt, *tft1, *tft2, *tft3, *tft4, *tft5;
+  int *iti, *jtj, *ktk, *ltl, *ituk;
+  double *br, *be, *ar, *ae, *tr, *te;
+  // SHAKE (per type: first bond record, bond count)
+  // Ewald
+  int nkv, ncol, kx, ky, kz;  // kx,ky,kz: table lengths (max |n| + 1)
+  KCol *cols;
+  void *kchunks;                // column chunks of the S(k) kernel
+  int nchunk;
+  double2 *tabx, *taby, *tabz;  // [atom][n]
+  float2 *tabxf, *tabyf, *tabzf;
+  double2 *sk;                  // structure factors, column order
+  double2 *wk, *wkz;            // AK2*conj(S), kz*AK2*conj(S)
+  double *kscal;                // per-k scratch of the energy/virial kernel
+  // scalars and state blocks
+  mdx_scalars *sc;
+  mdx_thermo *th;
+  mdx_step_record *rec;
+  int rec_cap;
+  int *err;
+  int *shake_iter;   // [4..5]: list capacity needed after an overflow
+  double *red;       // reduction scratch
+  void *scal_scratch;  // SCALING stage scratch (integrate.cu)
+  int *nspec_d;        // NSPEC per type
+};
+
+struct mdx_ctx {
+  mdx_dims d{};
+  mdx_params p{};
+  TypeConst tc{};
+  PairConst pc{};
+  DevData dv{};
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int64_t launches = 0;
+  bool have_topo = false, have_params = false, have_state = false,
+       have_lists = false, have_com = false;
+  std::string err;
+  // host copies of what the host logic needs
+  std::vector<int> h_itype, h_nnum, h_nsite;
+  std::vector<double> h_charge, h_mass;
+  int nspec[MDX_NT], nsits[MDX_NT], isadr[MDX_NT + 1], isaddr[MDX_NT + 1],
+      iaddr[MDX_NT + 1], nrb[MDX_NT], iadb[MDX_NT], ishejk[MDX_NT];
+  double summas[MDX_NT];
+  std::vector<double> h_a6lj0, h_b12lj0, h_q, h_rb, h_fb, h_db, h_ro;
+  std::vector<int> h_inbt;
+  // box mirror (host), Ewald bookkeeping
+  double boxl = 0, boyl = 0, bozl = 0;
+  double boxlo = 0, boylo = 0, bozlo = 0;
+  bool furir_init = false;
+  int nkv = 0;
+  double spei = 0, speei[MDX_NT]{};
+  CellGrid grid{};
+  double list_rl2 = 0;  // squared list radius used by the last build
+  FixScale fix{};
+  int mbsh = 0, mbln = 0;
+  bool mixed() const { return d.precision == MDX_MIXED; }
+};
+
+// --------------------------------------------------------------- helpers --
+#define MDX_CUDA(call)                                                      \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);        \
+      return MDX_ERR_CUDA;                                                  \
+    }                                                                       \
+  } while (0)
+
+#define MDX_LAUNCHED(ctx)                                                   \
+  do {                                                                      \
+    (ctx)->launches++;                                                      \
+    cudaError_t e_ = cudaGetLastError();                                    \
+    if (e_ != cudaSuccess) {                                                \
+      (ctx)->err = std::string("launch: ") + cudaGetErrorString(e_);        \
+      return MDX_ERR_CUDA;                                                  \
+    }                                                                       \
+  } while (0)
+
+// Fortran SIGN(a, b) for b != -0 handling as gfortran on IEEE (sign bit).
+__device__ __forceinline__ double fsign(double a, double b) {
+  return copysign(fabs(a), b);
+}
+__device__ __forceinline__ float fsignf(float a, float b) {
+  return copysignf(fabsf(a), b);
+}
+
+// Minimum image of the reference's inlined PBC for a rectangular cell
+// (service.f:953-990 with LHEX = LOCT = false); hbz is the half box used for
+// the z test (HBOXL in LOCALF, forces.f:871; HBOZL elsewhere).
+__device__ __forceinline__ void pbc_rect(double &dx, double &dy, double &dz,
+                                         double bx, double by, double bz,
+                                         double hbx, double hby, double hbz) {
+  if (fabs(dx) > hbx) dx = dx - fsign(bx, dx);
+  if (fabs(dz) > hbz) dz = dz - fsign(bz, dz);
+  if (fabs(dy) > hby) dy = dy - fsign(by, dy);
+}
+__device__ __forceinline__ void pbc_rectf(float &dx, float &dy, float &dz,
+                                          float bx, float by, float bz,
+                                          float hbx, float hby, float hbz) {
+  if (fabsf(dx) > hbx) dx = dx - fsignf(bx, dx);
+  if (fabsf(dz) > hbz) dz = dz - fsignf(bz, dz);
+  if (fabsf(dy) > hby) dy = dy - fsignf(by, dy);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of NV doubles into dst with one atomicAdd per value per
+// block.  All threads of the block must call it.
+template <int NV>
+__device__ __forceinline__ void block_add(double (&v)[NV], double *const *dst) {
+  __shared__ double sh[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[wid][k] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = lane < nw ? sh[lane][k] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0 && dst[k]) atomicAdd(dst[k], t);
+    }
+  }
+  __syncthreads();
+}
+
+// Fixed-point force accumulation of the mixed path: two's complement in an
+// unsigned 64-bit word, so that integer addition is associative and the sum
+// is independent of the order of contributions.
+__device__ __forceinline__ void fix_add(unsigned long long *a, double v,
+                                        double scale) {
+  long long q = __double2ll_rn(v * scale);
+  atomicAdd(a, (unsigned long long)q);
+}
+__device__ __forceinline__ void fix_addf(unsigned long long *a, float v,
+                                         float scale) {
+  long long q = __float2ll_rn(v * scale);
+  atomicAdd(a, (unsigned long long)q);
+}
+
+// ---------------------------------------------------------- host launchers
+// nblist.cu
+int launch_build_lists(mdx_ctx *ctx);
+int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
+                 int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
+// pair.cu
+int launch_localf(mdx_ctx *ctx, bool split);
+int launch_forces_long(mdx_ctx *ctx, bool split);
+int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
+// ewald.cu
+int host_inifur(mdx_ctx *ctx);
+int launch_furir(mdx_ctx *ctx);
+int launch_eterms(mdx_ctx *ctx);
+// integrate.cu
+int launch_zero_fast(mdx_ctx *ctx);
+int launch_zero_slow(mdx_ctx *ctx);
+int launch_fix_to_double(mdx_ctx *ctx, int which);  // mixed: int64 -> G/H
+int launch_sclfrc(mdx_ctx *ctx, int nnn);
+int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
+int launch_getcom(mdx_ctx *ctx);
+int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev);
+int launch_record(mdx_ctx *ctx, int slot, int mstep);
+// nblist.cu
+int launch_mirror_f32(mdx_ctx *ctx);

@@ -1,0 +1,414 @@
+// nblist.cu -- CHCNB (forces.f:1813-2205) as an O(N) cell-grid build.
+//
+// The reference scans all pairs in "parity strips": outer atom I takes
+// J = I-2, I-4, ... (same parity, J < I) and J = I+1, I+3, ... (opposite
+// parity, J > I).  That rule fixes which atom owns each pair; it is kept here
+// so that every owner row holds about half of the atom's neighbours (load
+// balance for free) and so that the export reproduces the reference's lists
+// entry for entry.  Candidates come from the 27 (or fewer, for small boxes)
+// neighbouring cells; each candidate is classified with the reference's exact
+// FP64 arithmetic (minimum image, RR2 <= RSSQ, RR2 <= SHORT2, the 8 A bound
+// on the intramolecular bonded check, 1-4 pairs to the short list), after an
+// FP32 prefilter that only decides pairs far from every boundary.
+//
+// Rows: nl_idx[i*cap_l + k] (long), ns_idx[i*cap_s + k] (short; bit 31 marks
+// a 1-4 pair), counts in nl_cnt / ns_cnt.  Row order is deterministic.
+#include <algorithm>
+#include <cmath>
+
+#include "mdx_internal.cuh"
+
+namespace {
+
+struct BoxD {
+  double bx, by, bz, hbx, hby, hbz;
+};
+
+__device__ __forceinline__ int wrap_cell(double x, double L, double cw, int n) {
+  double u = (x + 0.5 * L) / cw;
+  int c = (int)floor(u);
+  c %= n;
+  if (c < 0) c += n;
+  return c;
+}
+
+__global__ void k_cell_count(int n, const dbl4 *__restrict__ pos, BoxD b,
+                             CellGrid g, int *__restrict__ cell_cnt,
+                             int *__restrict__ atom_cell) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dbl4 p = pos[i];
+  int cx = wrap_cell(p.x, b.bx, g.cx, g.nx);
+  int cy = wrap_cell(p.y, b.by, g.cy, g.ny);
+  int cz = wrap_cell(p.z, b.bz, g.cz, g.nz);
+  int c = (cz * g.ny + cy) * g.nx + cx;
+  atom_cell[i] = c;
+  atomicAdd(&cell_cnt[c], 1);
+}
+
+// Single-block exclusive scan of the cell counts (ncell is small).
+__global__ void k_cell_scan(int ncell, const int *__restrict__ cnt,
+                            int *__restrict__ start, int *__restrict__ fill) {
+  __shared__ int sh[1024];
+  int carry = 0;
+  for (int base = 0; base < ncell; base += 1024) {
+    int i = base + threadIdx.x;
+    int v = i < ncell ? cnt[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      int t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < ncell) {
+      start[i] = carry + sh[threadIdx.x] - v;
+      fill[i] = 0;
+    }
+    int tot = sh[1023];
+    __syncthreads();
+    carry += tot;
+  }
+  if (threadIdx.x == 0) start[ncell] = carry;
+}
+
+__global__ void k_cell_scatter(int n, const int *__restrict__ atom_cell,
+                               const int *__restrict__ start,
+                               int *__restrict__ fill,
+                               int *__restrict__ list) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = atom_cell[i];
+  int k = atomicAdd(&fill[c], 1);
+  list[start[c] + k] = i;
+}
+
+// Sort each cell's atoms by index (one warp per cell, odd-even transposition
+// over the small cell population) so that rows come out in a fixed order.
+__global__ void k_cell_sort(int ncell, const int *__restrict__ start,
+                            int *__restrict__ list) {
+  int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  int b = start[c], e = start[c + 1], m = e - b;
+  for (int pass = 0; pass < m; ++pass) {
+    int par = pass & 1;
+    for (int k = par + 2 * lane; k + 1 < m; k += 64) {
+      int a0 = list[b + k], a1 = list[b + k + 1];
+      if (a0 > a1) {
+        list[b + k] = a1;
+        list[b + k + 1] = a0;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Ownership of pair (i, j) in the strip loop: i owns it when (i-j) is even
+// and j < i, or (i-j) is odd and j > i (forces.f:1834, 2014).
+__device__ __forceinline__ bool owns(int i, int j) {
+  return (((i - j) & 1) == 0) ? (j < i) : (j > i);
+}
+
+// Exact classification (forces.f:1938-1981): 0 none, 1 short, 2 long,
+// 3 short 1-4, -1 excluded bonded pair.
+__device__ __forceinline__ int classify_exact(
+    int i, int j, bool same_mol, const dbl4 &pi, const dbl4 &pj,
+    const BoxD &b, double short2, double rl2, const int *__restrict__ nnbb,
+    const int *__restrict__ inbb, int nbdmax) {
+  double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+  pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+  double rr2 = dx * dx + dy * dy + dz * dz;
+  if (same_mol && rr2 <= 64.0) {
+    int nb = nnbb[i];
+    const int jf = j + 1;
+    for (int k = 0; k < nb; ++k) {
+      int v = inbb[i * nbdmax + k];
+      if (v == jf) return -1;
+      if (v == -jf) return 3;
+    }
+  }
+  if (rr2 <= short2) return 1;
+  if (rr2 <= rl2) return 2;
+  return 0;
+}
+
+template <int BLK>
+__global__ void __launch_bounds__(BLK) k_build(
+    int n, const dbl4 *__restrict__ pos, const float4 *__restrict__ posf,
+    const int4 *__restrict__ ainfo, const int *__restrict__ nnbb,
+    const int *__restrict__ inbb, int nbdmax, BoxD b, CellGrid g,
+    const int *__restrict__ atom_cell, const int *__restrict__ cell_start,
+    const int *__restrict__ cell_list, double short2, double rl2, int cap_s,
+    int cap_l, int *__restrict__ ns_cnt, int *__restrict__ nl_cnt,
+    int *__restrict__ ns_idx, int *__restrict__ nl_idx, int *__restrict__ err,
+    int *__restrict__ need, int full) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (BLK / 32) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  const dbl4 pi = pos[i];
+  const float4 pf = posf[i];
+  const int imol = ainfo[i].y;
+  const int c0 = atom_cell[i];
+  const int cx0 = c0 % g.nx, cy0 = (c0 / g.nx) % g.ny, cz0 = c0 / (g.nx * g.ny);
+  const float fbx = (float)b.bx, fby = (float)b.by, fbz = (float)b.bz;
+  const float fhx = (float)b.hbx, fhy = (float)b.hby, fhz = (float)b.hbz;
+  const float rl2f_hi = (float)(rl2 * (1.0 + 1e-4)), rl2f_lo = (float)(rl2 * (1.0 - 1e-4));
+  const float s2f_hi = (float)(short2 * (1.0 + 1e-4)), s2f_lo = (float)(short2 * (1.0 - 1e-4));
+  int ns = 0, nl = 0;
+  const int ox0 = g.nx >= 3 ? -1 : 0, ox1 = g.nx >= 3 ? 1 : g.nx - 1;
+  const int oy0 = g.ny >= 3 ? -1 : 0, oy1 = g.ny >= 3 ? 1 : g.ny - 1;
+  const int oz0 = g.nz >= 3 ? -1 : 0, oz1 = g.nz >= 3 ? 1 : g.nz - 1;
+  for (int oz = oz0; oz <= oz1; ++oz)
+    for (int oy = oy0; oy <= oy1; ++oy)
+      for (int ox = ox0; ox <= ox1; ++ox) {
+        int cx = g.nx >= 3 ? (cx0 + ox + g.nx) % g.nx : ox;
+        int cy = g.ny >= 3 ? (cy0 + oy + g.ny) % g.ny : oy;
+        int cz = g.nz >= 3 ? (cz0 + oz + g.nz) % g.nz : oz;
+        int c = (cz * g.ny + cy) * g.nx + cx;
+        int s = cell_start[c], e = cell_start[c + 1];
+        for (int base = s; base < e; base += 32) {
+          int kind = 0;
+          int j = -1;
+          if (base + lane < e) {
+            j = cell_list[base + lane];
+            if (j != i && (full || owns(i, j))) {
+              bool same = ainfo[j].y == imol;
+              if (same) {
+                kind = classify_exact(i, j, true, pi, pos[j], b, short2, rl2,
+                                      nnbb, inbb, nbdmax);
+              } else {
+                float4 q = posf[j];
+                float dx = pf.x - q.x, dy = pf.y - q.y, dz = pf.z - q.z;
+                pbc_rectf(dx, dy, dz, fbx, fby, fbz, fhx, fhy, fhz);
+                float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 > rl2f_hi) {
+                  kind = 0;
+                } else if (d2 < rl2f_lo && (d2 < s2f_lo || d2 > s2f_hi)) {
+                  kind = d2 < s2f_lo ? 1 : 2;
+                } else {
+                  kind = classify_exact(i, j, false, pi, pos[j], b, short2, rl2,
+                                        nnbb, inbb, nbdmax);
+                }
+              }
+            }
+          }
+          unsigned ms = __ballot_sync(0xffffffffu, kind == 1 || kind == 3);
+          unsigned ml = __ballot_sync(0xffffffffu, kind == 2);
+          unsigned lower = (1u << lane) - 1u;
+          if (kind == 1 || kind == 3) {
+            int k = ns + __popc(ms & lower);
+            if (k < cap_s)
+              ns_idx[(size_t)i * cap_s + k] = j | (kind == 3 ? (int)0x80000000 : 0);
+          } else if (kind == 2) {
+            int k = nl + __popc(ml & lower);
+            if (k < cap_l) nl_idx[(size_t)i * cap_l + k] = j;
+          }
+          ns += __popc(ms);
+          nl += __popc(ml);
+        }
+      }
+  if (lane == 0) {
+    ns_cnt[i] = min(ns, cap_s);
+    nl_cnt[i] = min(nl, cap_l);
+    if (ns > cap_s) {
+      atomicOr(err, DERR_LIST_SHORT);
+      atomicMax(&need[0], ns);
+    }
+    if (nl > cap_l) {
+      atomicOr(err, DERR_LIST_LONG);
+      atomicMax(&need[1], nl);
+    }
+  }
+}
+
+// FP32 mirror for the list prefilter and, for the mixed path, 32-bit
+// fixed-point coordinates: round(x / L * 2^32) kept modulo 2^32.
+__global__ void k_mirror(int n, const dbl4 *__restrict__ pos,
+                         float4 *__restrict__ posf, int4 *__restrict__ posi,
+                         double ibx, double iby, double ibz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dbl4 p = pos[i];
+  posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+  if (posi) {
+    const double two32 = 4294967296.0;
+    long long xi = __double2ll_rn(p.x * ibx * two32);
+    long long yi = __double2ll_rn(p.y * iby * two32);
+    long long zi = __double2ll_rn(p.z * ibz * two32);
+    posi[i] = make_int4((int)(unsigned)(unsigned long long)xi,
+                        (int)(unsigned)(unsigned long long)yi,
+                        (int)(unsigned)(unsigned long long)zi,
+                        __float_as_int((float)p.w));
+  }
+}
+
+__global__ void k_count_totals(int n, const int *__restrict__ ns_cnt,
+                               const int *__restrict__ nl_cnt,
+                               mdx_scalars *sc) {
+  int s = 0, l = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    s += ns_cnt[i];
+    l += nl_cnt[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    l += __shfl_xor_sync(0xffffffffu, l, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&sc->mbsh, s);
+    atomicAdd(&sc->mbln, l);
+  }
+}
+
+__global__ void k_halve_counts(mdx_scalars *sc) {
+  sc->mbsh /= 2;
+  sc->mbln /= 2;
+}
+
+}  // namespace
+
+int launch_mirror_f32(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  k_mirror<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, 1.0 / ctx->boxl,
+      1.0 / ctx->boyl, 1.0 / ctx->bozl);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_build_lists(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  const double rl = ctx->p.rcut + ctx->p.rskin;
+  BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
+         0.5 * ctx->bozl};
+  CellGrid g;
+  g.nx = std::max(1, (int)std::floor(ctx->boxl / rl));
+  g.ny = std::max(1, (int)std::floor(ctx->boyl / rl));
+  g.nz = std::max(1, (int)std::floor(ctx->bozl / rl));
+  // the stencil needs cells at least rl wide; below 3 cells a dimension is
+  // scanned whole
+  g.cx = ctx->boxl / g.nx;
+  g.cy = ctx->boyl / g.ny;
+  g.cz = ctx->bozl / g.nz;
+  g.ncell = g.nx * g.ny * g.nz;
+  if (g.ncell != ctx->grid.ncell) {
+    if (d.cell_cnt) cudaFree(d.cell_cnt);
+    if (d.cell_start) cudaFree(d.cell_start);
+    MDX_CUDA(cudaMalloc(&d.cell_cnt, sizeof(int) * (g.ncell + 1) * 2));
+    MDX_CUDA(cudaMalloc(&d.cell_start, sizeof(int) * (g.ncell + 1)));
+  }
+  ctx->grid = g;
+  ctx->list_rl2 = rl * rl;
+  int *fill = d.cell_cnt + (g.ncell + 1);
+  MDX_CUDA(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * (g.ncell + 1),
+                           ctx->stream));
+  const int T = 256;
+  k_mirror<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
+      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, 1.0 / ctx->boxl,
+      1.0 / ctx->boyl, 1.0 / ctx->bozl);
+  MDX_LAUNCHED(ctx);
+  k_cell_count<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(d.n, d.pos, b, g,
+                                                          d.cell_cnt,
+                                                          d.atom_cell);
+  MDX_LAUNCHED(ctx);
+  k_cell_scan<<<1, 1024, 0, ctx->stream>>>(g.ncell, d.cell_cnt, d.cell_start,
+                                           fill);
+  MDX_LAUNCHED(ctx);
+  k_cell_scatter<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
+      d.n, d.atom_cell, d.cell_start, fill, d.cell_list);
+  MDX_LAUNCHED(ctx);
+  k_cell_sort<<<(g.ncell + 7) / 8, 256, 0, ctx->stream>>>(g.ncell, d.cell_start,
+                                                          d.cell_list);
+  MDX_LAUNCHED(ctx);
+  int *need = d.shake_iter + 4;  // two ints of scratch after the SHAKE counter
+  MDX_CUDA(cudaMemsetAsync(need, 0, sizeof(int) * 2, ctx->stream));
+  const int BLK = 256;
+  k_build<BLK><<<(d.n + BLK / 32 - 1) / (BLK / 32), BLK, 0, ctx->stream>>>(
+      d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,
+      d.cell_start, d.cell_list, ctx->p.rshort * ctx->p.rshort, rl * rl,
+      d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
+      ctx->mixed() ? 1 : 0);
+  MDX_LAUNCHED(ctx);
+  MDX_CUDA(cudaMemsetAsync(&d.sc->mbsh, 0, sizeof(int) * 2, ctx->stream));
+  k_count_totals<<<64, 256, 0, ctx->stream>>>(d.n, d.ns_cnt, d.nl_cnt, d.sc);
+  MDX_LAUNCHED(ctx);
+  if (ctx->mixed()) {  // full rows count every pair twice
+    k_halve_counts<<<1, 1, 0, ctx->stream>>>(d.sc);
+    MDX_LAUNCHED(ctx);
+  }
+  ctx->have_lists = true;
+  return MDX_OK;
+}
+
+// Reference layout and order of the lists (forces.f:1956-1957, 2127-2140):
+// outer atom I ascending; inside, the even strip (J = I-2, I-4, ...) and then
+// the odd strip (J = I+1, I+3, ...); a normal pair is stored (larger, smaller)
+// and a 1-4 pair (-I, J).
+int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
+                 int32_t *nbl1, int32_t *nbl2, int32_t cap_l) {
+  DevData &d = ctx->dv;
+  const int n = d.n;
+  std::vector<int> cs(n), cl(n), rs((size_t)n * d.cap_s), rl((size_t)n * d.cap_l);
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  MDX_CUDA(cudaMemcpy(cs.data(), d.ns_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(cl.data(), d.nl_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(rs.data(), d.ns_idx, sizeof(int) * rs.size(), cudaMemcpyDeviceToHost));
+  MDX_CUDA(cudaMemcpy(rl.data(), d.nl_idx, sizeof(int) * rl.size(), cudaMemcpyDeviceToHost));
+  long ks = 0, kl = 0;
+  std::vector<int> row;
+  for (int i = 0; i < n; ++i) {
+    const int I = i + 1;
+    for (int pass = 0; pass < 2; ++pass) {
+      const int cnt = pass == 0 ? cs[i] : cl[i];
+      const int *src = pass == 0 ? &rs[(size_t)i * d.cap_s] : &rl[(size_t)i * d.cap_l];
+      row.clear();
+      for (int k = 0; k < cnt; ++k) {
+        // the mixed path keeps full rows (each pair in both atoms' rows);
+        // the reference list holds the owner's copy only
+        const int j = src[k] & 0x7fffffff;
+        const bool own = ((i - j) & 1) == 0 ? (j < i) : (j > i);
+        if (own) row.push_back(src[k]);
+      }
+      std::sort(row.begin(), row.end(), [I](int a, int b) {
+        int ja = (a & 0x7fffffff) + 1, jb = (b & 0x7fffffff) + 1;
+        long ka = ja < I ? (long)(I - ja) : (1L << 40) + (ja - I);
+        long kb = jb < I ? (long)(I - jb) : (1L << 40) + (jb - I);
+        return ka < kb;
+      });
+      for (int v : row) {
+        const bool is14 = (v & 0x80000000) != 0;
+        const int J = (v & 0x7fffffff) + 1;
+        int a, b2;
+        if (is14) {
+          a = -I;
+          b2 = J;
+        } else {
+          a = std::max(I, J);
+          b2 = std::min(I, J);
+        }
+        if (pass == 0) {
+          if (ks < cap_s) {
+            nbs1[ks] = a;
+            nbs2[ks] = b2;
+          }
+          ++ks;
+        } else {
+          if (kl < cap_l) {
+            nbl1[kl] = a;
+            nbl2[kl] = b2;
+          }
+          ++kl;
+        }
+      }
+    }
+  }
+  if (ks > cap_s || kl > cap_l) {
+    ctx->err = "export buffers too small";
+    return MDX_ERR_ARG;
+  }
+  return MDX_OK;
+}

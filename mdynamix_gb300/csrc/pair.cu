@@ -1,0 +1,540 @@
+// pair.cu -- real-space LJ + erfc-Coulomb over the neighbour rows:
+//   LOCALF (forces.f:813-998) on the short rows into H,
+//   FORCES (forces.f:1014-1202) on the long rows into G.
+//
+// FP64 path: one warp per owner atom walks its half row (every pair once,
+// as in the reference list); the owner's force is reduced in registers and
+// the partner's goes out with FP64 atomics.  The arithmetic is the
+// reference's, statement by statement.
+//
+// Mixed path: rows are full (both atoms of a pair hold it), so a warp writes
+// only its own atom and there is no scattered atomic at all.  Pair geometry
+// comes from 32-bit fixed-point coordinates (x / L * 2^32): the difference of
+// two such integers is exact and wraps to the minimum image by itself, and is
+// converted to FP32 only as a short vector.  Pair and LJ math is FP32; per
+// lane partial forces are rounded to 64-bit fixed point and summed as
+// integers, so the result does not depend on the order of the sums.  Energy
+// and virial lane partials go the same way into 64-bit integer slots.
+#include <cmath>
+
+#include "mdx_internal.cuh"
+
+namespace {
+
+// Per-pair parameters (forces.f:838-862 / 1040-1066).
+struct PairTables {
+  const double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
+  const float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
+};
+
+// Output slots of one pair sweep.
+enum {
+  P_EES = 0,   // PELS1/PELS2
+  P_ESR,       // PE1/PE2
+  P_VIR,       // VIR1/VIR2
+  P_VX, P_VY, P_VZ,  // VIRX.. (FORCES) or VIRFX.. (LOCALF)
+  P_EE_SAME, P_EE_DIFF, P_ESR_SAME, P_ESR_DIFF,
+  P_WIR,       // WIRSS (mixed LOCALF only)
+  P_NSLOT
+};
+
+__device__ __forceinline__ double ewald_erfc_poly(double ttt, double exp2a) {
+  return ((((MDX_A5 * ttt + MDX_A4) * ttt + MDX_A3) * ttt + MDX_A2) * ttt +
+          MDX_A1) * ttt * exp2a;
+}
+__device__ __forceinline__ float ewald_erfc_polyf(float ttt, float exp2a) {
+  return (((((float)MDX_A5 * ttt + (float)MDX_A4) * ttt + (float)MDX_A3) * ttt +
+           (float)MDX_A2) * ttt + (float)MDX_A1) * ttt * exp2a;
+}
+
+// ---------------------------------------------------------------- FP64 ---
+template <bool SHORT, bool SPLIT>
+__global__ void __launch_bounds__(256) k_pair64(
+    int n, const dbl4 *__restrict__ pos, const int4 *__restrict__ ainfo,
+    const double *__restrict__ qsite, const int *__restrict__ cnt,
+    const int *__restrict__ idx, int cap, PairTables tb, TypeConst tc,
+    PairConst pc, double bx, double by, double bz, double *__restrict__ fx,
+    double *__restrict__ fy, double *__restrict__ fz,
+    Dst6 dst, double *__restrict__ split) {
+  __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
+  if (SPLIT) {
+    for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const double hbx = 0.5 * bx, hby = 0.5 * by, hbz = 0.5 * bz;
+  // LOCALF tests DZ against HBOXL (forces.f:871); FORCES against HBOZL
+  const double hbzt = SHORT ? hbx : hbz;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  if (i < n) {
+    const dbl4 pi = pos[i];
+    const int4 ai = ainfo[i];
+    const int ti = ai.x, mi = ai.y, ni = ai.z;
+    const double qsi = qsite[i];
+    const int c = cnt[i];
+    double fix = 0.0, fiy = 0.0, fiz = 0.0;
+    const int *row = idx + (size_t)i * cap;
+    for (int k = lane; k < c; k += 32) {
+      const int v = row[k];
+      const bool is14 = SHORT && v < 0;
+      const int j = v & 0x7fffffff;
+      const dbl4 pj = pos[j];
+      const int4 aj = ainfo[j];
+      const int tj = aj.x, nj = aj.z;
+      const bool same = aj.y == mi;
+      const int mtr = tc.mdx[ti][tj];
+      double QIJ, A6, B12, RAE = 0.0;
+      const int tix = ni * pc.nnbt + nj;
+      if (same) {
+        if (is14) {
+          QIJ = qsi * qsite[j] * pc.coulf * tc.c14el[ti];
+          A6 = __ldg(&tb.a6_14[tix]) * tc.c14lj[ti];
+          B12 = __ldg(&tb.b12_14[tix]) * tc.c14lj[ti];
+        } else {
+          QIJ = qsi * qsite[j] * pc.coulf;
+          A6 = __ldg(&tb.a6lj0[tix]);
+          B12 = __ldg(&tb.b12lj0[tix]);
+        }
+      } else {
+        QIJ = pi.w * pj.w * pc.coulf;
+        A6 = __ldg(&tb.a6lj[tix]);
+        B12 = __ldg(&tb.b12lj[tix]);
+        if (pc.lmdee) RAE = (tc.iee[ti] * tc.iee[tj] == 0) ? pc.raex : 0.0;
+      }
+      double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
+      pbc_rect(DX, DY, DZ, bx, by, bz, hbx, hby, hbzt);
+      const double RR = DX * DX + DY * DY + DZ * DZ;
+      const double R1 = sqrt(RR);
+      const double R1I = 1. / R1;
+      const double R1E = R1 + RAE;
+      const double R1EI = RAE == 0.0 ? R1I : 1. / R1E;
+      double EE1, EES, FORCE;
+      if (is14 || (same && tc.iee[ti] == 0)) {
+        if (SHORT) {
+          EE1 = QIJ * R1I;
+          FORCE = tc.lmove[ti] ? EE1 * (R1I * R1I) : 0.0;
+        } else {
+          EE1 = QIJ / R1;
+          FORCE = tc.lmove[ti] ? EE1 / (R1 * R1) : 0.0;
+        }
+        EES = EE1;
+      } else if (pc.lmnbl) {
+        EE1 = QIJ * (1.0 / R1E - 0.5 * pc.rff2 * (R1E * R1E) + pc.rff);
+        EES = EE1;
+        if (SHORT) {
+          FORCE = QIJ * (1. / (R1E * R1E * R1E) + pc.rff2);
+          acc[P_VIR] += QIJ * (1.5 * pc.rff2 / (R1E * R1E) - pc.rff);
+        } else {
+          FORCE = QIJ * (1.0 / ((R1E * R1E) * R1) + pc.rff2);
+          acc[P_VIR] += QIJ * (1.5 * pc.rff2 * RR - pc.rff);
+        }
+      } else {
+        const double ALPHAR = pc.alphad * R1;
+        const double TTT = 1.0 / (1.0 + MDX_B1 * ALPHAR);
+        const double EXP2A = exp(-(ALPHAR * ALPHAR));
+        const double ERFCT = ewald_erfc_poly(TTT, EXP2A);
+        EE1 = QIJ * R1EI;
+        EES = EE1 * ERFCT;
+        FORCE = EE1 * (MDX_TOTPI * pc.alphad * EXP2A + ERFCT * R1EI) * R1I;
+      }
+      if (SPLIT) {
+        if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], EE1);
+        else atomicAdd(&s_split[mtr], EE1);
+      }
+      acc[P_EES] += EES;
+      if (B12 != 0.0) {
+        const double R2I = R1EI * R1EI;
+        const double R6I = R2I * R2I * R2I;
+        double ESR = (A6 + B12 * R6I) * R6I;
+        const double FSR = (6.0 * A6 + 12.0 * B12 * R6I) * R6I * R1EI;
+        FORCE = FORCE + FSR * R1I;
+        if (same) {
+          if (SHORT) {
+            if (tc.lmove[ti]) {
+              if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], ESR);
+              acc[P_VIR] += FSR * R1;
+            } else {
+              ESR = 0.0;
+              FORCE = 0.0;
+            }
+          } else {
+            if (tc.lmove[ti]) acc[P_VIR] += FSR * R1;
+            if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], ESR);
+          }
+        } else {
+          if (SPLIT) atomicAdd(&s_split[MDX_NTPP + mtr], ESR);
+          acc[P_VIR] += FSR * R1;
+        }
+        acc[P_ESR] += ESR;
+      }
+      if (SHORT || !same || tc.lmove[ti]) {
+        acc[3] += FORCE * (DX * DX);
+        acc[4] += FORCE * (DY * DY);
+        acc[5] += FORCE * (DZ * DZ);
+      }
+      const double gxv = FORCE * DX, gyv = FORCE * DY, gzv = FORCE * DZ;
+      fix += gxv;
+      fiy += gyv;
+      fiz += gzv;
+      atomicAdd(&fx[j], -gxv);
+      atomicAdd(&fy[j], -gyv);
+      atomicAdd(&fz[j], -gzv);
+    }
+    fix = warp_sum(fix);
+    fiy = warp_sum(fiy);
+    fiz = warp_sum(fiz);
+    if (lane == 0 && c > 0) {
+      atomicAdd(&fx[i], fix);
+      atomicAdd(&fy[i], fiy);
+      atomicAdd(&fz[i], fiz);
+    }
+  }
+  block_add<6>(acc, dst.p);
+  if (SPLIT) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x)
+      if (s_split[k] != 0.0) atomicAdd(&split[k], s_split[k]);
+  }
+}
+
+// WIRSS / WIRS: -sum F . (S - COM(molecule)) (forces.f:991-995,
+// scalar.f:77-82), FP64 path.
+__global__ void k_wir(int n, const dbl4 *__restrict__ pos,
+                      const int4 *__restrict__ ainfo, const double *__restrict__ X,
+                      const double *__restrict__ Y, const double *__restrict__ Z,
+                      const double *__restrict__ fx, const double *__restrict__ fy,
+                      const double *__restrict__ fz, double *dst) {
+  double w[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const dbl4 p = pos[i];
+    const int m = ainfo[i].y;
+    w[0] = w[0] - fx[i] * (p.x - X[m]) - fy[i] * (p.y - Y[m]) - fz[i] * (p.z - Z[m]);
+  }
+  double *d[1] = {dst};
+  block_add<1>(w, d);
+}
+
+// ---------------------------------------------------------------- mixed ---
+__device__ __forceinline__ float idiff(int a, int b, float s) {
+  return (float)(int)((unsigned)a - (unsigned)b) * s;
+}
+
+template <bool SHORT, bool SPLIT>
+__global__ void __launch_bounds__(256) k_pair32(
+    int n, const int4 *__restrict__ posi, const dbl4 *__restrict__ pos,
+    const int4 *__restrict__ ainfo, const float *__restrict__ qsitef,
+    const int *__restrict__ cnt, const int *__restrict__ idx, int cap,
+    PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
+    FixScale fsc, unsigned long long *__restrict__ ffix,
+    const double *__restrict__ X, const double *__restrict__ Y,
+    const double *__restrict__ Z, double escale,
+    unsigned long long *__restrict__ slots, double *__restrict__ split) {
+  __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
+  if (SPLIT) {
+    for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  long long tot[P_NSLOT];
+#pragma unroll
+  for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
+  if (i < n) {
+    const int4 pi = posi[i];
+    const int4 ai = ainfo[i];
+    const int ti = ai.x, mi = ai.y, ni = ai.z;
+    const float qi = __int_as_float(pi.w);
+    const float qsi = qsitef[i];
+    const float coulf = (float)pc.coulf, alphad = (float)pc.alphad;
+    const float raex = (float)pc.raex;
+    const int c = cnt[i];
+    float fxa = 0.f, fya = 0.f, fza = 0.f;
+    float a[P_NSLOT];
+#pragma unroll
+    for (int k = 0; k < P_NSLOT; ++k) a[k] = 0.f;
+    const int *row = idx + (size_t)i * cap;
+    for (int k = lane; k < c; k += 32) {
+      const int v = row[k];
+      const bool is14 = SHORT && v < 0;
+      const int j = v & 0x7fffffff;
+      const int4 pj = posi[j];
+      const int4 aj = ainfo[j];
+      const int tj = aj.x, nj = aj.z;
+      const bool same = aj.y == mi;
+      const int tix = ni * pc.nnbt + nj;
+      float QIJ, A6, B12, RAE = 0.f;
+      if (same) {
+        if (is14) {
+          QIJ = qsi * qsitef[j] * coulf * (float)tc.c14el[ti];
+          A6 = __ldg(&tb.a614f[tix]) * (float)tc.c14lj[ti];
+          B12 = __ldg(&tb.b1214f[tix]) * (float)tc.c14lj[ti];
+        } else {
+          QIJ = qsi * qsitef[j] * coulf;
+          A6 = __ldg(&tb.a60f[tix]);
+          B12 = __ldg(&tb.b120f[tix]);
+        }
+      } else {
+        QIJ = qi * __int_as_float(pj.w) * coulf;
+        A6 = __ldg(&tb.a6f[tix]);
+        B12 = __ldg(&tb.b12f[tix]);
+        if (pc.lmdee) RAE = (tc.iee[ti] * tc.iee[tj] == 0) ? raex : 0.f;
+      }
+      const float DX = idiff(pi.x, pj.x, sx);
+      const float DY = idiff(pi.y, pj.y, sy);
+      const float DZ = idiff(pi.z, pj.z, sz);
+      const float RR = DX * DX + DY * DY + DZ * DZ;
+      const float R1I = rsqrtf(RR);
+      const float R1 = RR * R1I;
+      const float R1EI = RAE == 0.f ? R1I : 1.f / (R1 + RAE);
+      const float R1E = R1 + RAE;
+      float EE1, EES, FORCE;
+      if (is14 || (same && tc.iee[ti] == 0)) {
+        EE1 = QIJ * R1I;
+        FORCE = tc.lmove[ti] ? EE1 * (R1I * R1I) : 0.f;
+        EES = EE1;
+      } else if (pc.lmnbl) {
+        const float rff = (float)pc.rff, rff2 = (float)pc.rff2;
+        EE1 = QIJ * (1.f / R1E - 0.5f * rff2 * (R1E * R1E) + rff);
+        EES = EE1;
+        if (SHORT) {
+          FORCE = QIJ * (R1EI * R1EI * R1EI + rff2);
+          a[P_VIR] += QIJ * (1.5f * rff2 * R1EI * R1EI - rff);
+        } else {
+          FORCE = QIJ * (R1EI * R1EI * R1I + rff2);
+          a[P_VIR] += QIJ * (1.5f * rff2 * RR - rff);
+        }
+      } else {
+        const float ALPHAR = alphad * R1;
+        const float TTT = __frcp_rn(1.f + (float)MDX_B1 * ALPHAR);
+        const float EXP2A = __expf(-(ALPHAR * ALPHAR));
+        const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
+        EE1 = QIJ * R1EI;
+        EES = EE1 * ERFCT;
+        FORCE = EE1 * ((float)MDX_TOTPI * alphad * EXP2A + ERFCT * R1EI) * R1I;
+      }
+      if (SPLIT) {
+        const int mtr = tc.mdx[ti][tj];
+        if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], (double)EE1);
+        else atomicAdd(&s_split[mtr], (double)EE1);
+      }
+      if (same) a[P_EE_SAME] += EE1; else a[P_EE_DIFF] += EE1;
+      a[P_EES] += EES;
+      if (B12 != 0.f) {
+        const float R2I = R1EI * R1EI;
+        const float R6I = R2I * R2I * R2I;
+        float ESR = (A6 + B12 * R6I) * R6I;
+        const float FSR = (6.f * A6 + 12.f * B12 * R6I) * R6I * R1EI;
+        FORCE = FORCE + FSR * R1I;
+        bool count_esr_split = true;
+        if (same) {
+          if (SHORT) {
+            if (tc.lmove[ti]) {
+              a[P_VIR] += FSR * R1;
+            } else {
+              ESR = 0.f;
+              FORCE = 0.f;
+              count_esr_split = false;
+            }
+          } else {
+            if (tc.lmove[ti]) a[P_VIR] += FSR * R1;
+          }
+          if (count_esr_split) {
+            a[P_ESR_SAME] += ESR;
+            if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], (double)ESR);
+          }
+        } else {
+          a[P_ESR_DIFF] += ESR;
+          if (SPLIT) atomicAdd(&s_split[MDX_NTPP + tc.mdx[ti][tj]], (double)ESR);
+          a[P_VIR] += FSR * R1;
+        }
+        a[P_ESR] += ESR;
+      }
+      if (SHORT || !same || tc.lmove[ti]) {
+        a[P_VX] += FORCE * (DX * DX);
+        a[P_VY] += FORCE * (DY * DY);
+        a[P_VZ] += FORCE * (DZ * DZ);
+      }
+      fxa += FORCE * DX;
+      fya += FORCE * DY;
+      fza += FORCE * DZ;
+    }
+    // forces: lane partials -> fixed point -> integer warp sum -> one store
+    long long qx = __float2ll_rn(fxa * (float)fsc.scale);
+    long long qy = __float2ll_rn(fya * (float)fsc.scale);
+    long long qz = __float2ll_rn(fza * (float)fsc.scale);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      qx += __shfl_xor_sync(0xffffffffu, qx, o);
+      qy += __shfl_xor_sync(0xffffffffu, qy, o);
+      qz += __shfl_xor_sync(0xffffffffu, qz, o);
+    }
+    if (lane == 0) {
+      ffix[i] = (unsigned long long)qx;
+      ffix[n + i] = (unsigned long long)qy;
+      ffix[2 * n + i] = (unsigned long long)qz;
+      if (SHORT) {
+        // WIRSS needs the pair force on the atom (forces.f:991-995)
+        const dbl4 p = pos[i];
+        const double inv = fsc.inv;
+        const double w = -(double)qx * inv * (p.x - X[mi]) -
+                         (double)qy * inv * (p.y - Y[mi]) -
+                         (double)qz * inv * (p.z - Z[mi]);
+        tot[P_WIR] = __double2ll_rn(w * escale);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < P_WIR; ++k) {
+      float t = warp_sumf(a[k]);
+      if (lane == 0) tot[k] = __float2ll_rn(t * (float)escale);
+    }
+  }
+  // block sum of the integer slots, one atomic per slot per block
+  __shared__ long long sh[8][P_NSLOT];
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < P_NSLOT; ++k) sh[wid][k] = tot[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < P_NSLOT) {
+    long long s = 0;
+    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+    if (s != 0) atomicAdd(&slots[threadIdx.x], (unsigned long long)s);
+  }
+  if (SPLIT) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x)
+      if (s_split[k] != 0.0) atomicAdd(&split[k], 0.5 * s_split[k]);
+  }
+}
+
+// Fold the integer slots of a mixed sweep into mdx_scalars (full rows count
+// each pair twice, hence the 1/2 on pair sums).
+__global__ void k_fold_slots(unsigned long long *slots, double einv,
+                             mdx_scalars *sc, int which, int ntypes,
+                             int split) {
+  double v[P_NSLOT];
+  for (int k = 0; k < P_NSLOT; ++k) {
+    v[k] = (double)(long long)slots[k] * einv;
+    slots[k] = 0ull;
+  }
+  for (int k = 0; k < P_WIR; ++k) v[k] *= 0.5;
+  if (which == 1) {
+    sc->pels2 += v[P_EES];
+    sc->pe2 += v[P_ESR];
+    sc->vir2 += v[P_VIR];
+    sc->virfx += v[P_VX];
+    sc->virfy += v[P_VY];
+    sc->virfz += v[P_VZ];
+    sc->wirss += v[P_WIR];
+  } else {
+    sc->pels1 += v[P_EES];
+    sc->pe1 += v[P_ESR];
+    sc->vir1 += v[P_VIR];
+    sc->virx += v[P_VX];
+    sc->viry += v[P_VY];
+    sc->virz += v[P_VZ];
+  }
+  if (ntypes == 1 && !split) {
+    sc->pote1[0] += v[P_EE_DIFF];
+    sc->potl1[0] += v[P_ESR_DIFF];
+    sc->pes141[0] += v[P_EE_SAME];
+    sc->psr141[0] += v[P_ESR_SAME];
+  }
+}
+
+// Copy the split accumulators (POTE1, POTL1, PES141, PSR141) out.
+__global__ void k_fold_split(double *split, mdx_scalars *sc) {
+  int k = threadIdx.x;
+  if (k < MDX_NTPP) {
+    sc->pote1[k] += split[k];
+    sc->potl1[k] += split[MDX_NTPP + k];
+    split[k] = 0.0;
+    split[MDX_NTPP + k] = 0.0;
+  }
+  if (k < MDX_NT) {
+    sc->pes141[k] += split[2 * MDX_NTPP + k];
+    sc->psr141[k] += split[2 * MDX_NTPP + MDX_NT + k];
+    split[2 * MDX_NTPP + k] = 0.0;
+    split[2 * MDX_NTPP + MDX_NT + k] = 0.0;
+  }
+}
+
+// FP64 path with one molecule type: POTE1 etc. from same/different sums is
+// not available (the FP64 sweep sums totals only), so the split sweep is used
+// whenever the caller asks for the per-type energies.
+
+PairTables tables(const DevData &d) {
+  return PairTables{d.a6lj, d.b12lj, d.a6lj0, d.b12lj0, d.a6_14, d.b12_14,
+                    d.a6f,  d.b12f,  d.a60f,  d.b120f,  d.a614f, d.b1214f};
+}
+
+int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
+  DevData &d = ctx->dv;
+  const int T = 256, WPB = T / 32;
+  const int grid = (d.n + WPB - 1) / WPB;
+  const int *cnt = shrt ? d.ns_cnt : d.nl_cnt;
+  const int *idx = shrt ? d.ns_idx : d.nl_idx;
+  const int cap = shrt ? d.cap_s : d.cap_l;
+  double *split_buf = d.red + 64;
+  if (!ctx->mixed()) {
+    double *fx = shrt ? d.hx : d.gx, *fy = shrt ? d.hy : d.gy, *fz = shrt ? d.hz : d.gz;
+    mdx_scalars *sc = d.sc;
+    Dst6 ddst = shrt ? Dst6{{&sc->pels2, &sc->pe2, &sc->vir2, &sc->virfx, &sc->virfy, &sc->virfz}}
+                     : Dst6{{&sc->pels1, &sc->pe1, &sc->vir1, &sc->virx, &sc->viry, &sc->virz}};
+#define LP64(S, P)                                                                \
+  k_pair64<S, P><<<grid, T, 0, ctx->stream>>>(                                    \
+      d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
+      ctx->boxl, ctx->boyl, ctx->bozl, fx, fy, fz, ddst, split_buf)
+    if (shrt) {
+      if (split) LP64(true, true); else LP64(true, false);
+    } else {
+      if (split) LP64(false, true); else LP64(false, false);
+    }
+#undef LP64
+    MDX_LAUNCHED(ctx);
+  } else {
+    unsigned long long *ffix = shrt ? d.hfix : d.gfix;
+    unsigned long long *slots = reinterpret_cast<unsigned long long *>(d.red);
+    const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
+                 szs = ctx->bozl / 4294967296.0;
+    const double escale = ctx->fix.escale;
+#define LP32(S, P)                                                                \
+  k_pair32<S, P><<<grid, T, 0, ctx->stream>>>(                                    \
+      d.n, d.posi, d.pos, d.ainfo, d.qsitef, cnt, idx, cap, tables(d),            \
+      ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
+      d.Y, d.Z, escale, slots, split_buf)
+    if (shrt) {
+      if (split) LP32(true, true); else LP32(true, false);
+    } else {
+      if (split) LP32(false, true); else LP32(false, false);
+    }
+#undef LP32
+    MDX_LAUNCHED(ctx);
+    k_fold_slots<<<1, 1, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
+                                            ctx->d.ntypes, split ? 1 : 0);
+    MDX_LAUNCHED(ctx);
+  }
+  if (split) {
+    k_fold_split<<<1, 64, 0, ctx->stream>>>(split_buf, d.sc);
+    MDX_LAUNCHED(ctx);
+  }
+  return MDX_OK;
+}
+
+}  // namespace
+
+int launch_localf(mdx_ctx *ctx, bool split) { return launch_pair(ctx, true, split); }
+int launch_forces_long(mdx_ctx *ctx, bool split) { return launch_pair(ctx, false, split); }
+
+int launch_wir(mdx_ctx *ctx, int which) {
+  DevData &d = ctx->dv;
+  double *dst = which == 1 ? &d.sc->wirss : &d.sc->wirs;
+  const double *fx = which == 1 ? d.hx : d.gx, *fy = which == 1 ? d.hy : d.gy,
+               *fz = which == 1 ? d.hz : d.gz;
+  k_wir<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz, dst);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}

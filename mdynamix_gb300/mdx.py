@@ -1,0 +1,207 @@
+"""Python binding of the GB300 force path (libmdxgpu.so, C ABI).
+
+``ForcePath`` exposes the reference's routines under their own names:
+
+    chcnb()        CHCNB     forces.f:1813   neighbour lists
+    fforces(laver) FFORCES   forces.f:36     fast forces H
+    slforces()     SLFORCES  forces.f:55     slow forces G
+    allforce()     ALLFORCE  forces.f:77     F = G + H
+    getcom()       GETCOM    service.f:463
+    double(n)      DOUBLE    mdstep.f:281    double time step loop
+    sultan(n)      SULTAN    mdstep.f:29     leap-frog + SHAKE loop
+    set_lambda()   RECINT    mdee.f:86
+
+Errors come back as ``MdxError`` carrying the library's code and message,
+where the reference would print and stop.  There is no CPU fallback: if the
+CUDA library is missing or no GPU is present, construction fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (ERRORS, F64P, I32P, MDX_FP64, MDX_MIXED, MdxDims, MdxParams,
+                  MdxScalars, MdxStepRecord, MdxThermo, MdxTopo, Packed, pack,
+                  thermo_init)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libmdxgpu.so")
+
+_lib = None
+
+
+class MdxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load libmdxgpu.so and declare its C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    L.mdx_open.argtypes = [C.POINTER(MdxDims), C.POINTER(P)]
+    L.mdx_close.argtypes = [P]
+    L.mdx_last_error.argtypes = [P]
+    L.mdx_last_error.restype = C.c_char_p
+    L.mdx_strerror.argtypes = [C.c_int]
+    L.mdx_strerror.restype = C.c_char_p
+    L.mdx_upload_topology.argtypes = [P, C.POINTER(MdxTopo)]
+    L.mdx_set_params.argtypes = [P, C.POINTER(MdxParams)]
+    L.mdx_upload_state.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P, C.POINTER(MdxThermo)]
+    L.mdx_download_state.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P, C.POINTER(MdxThermo)]
+    L.mdx_download_forces.argtypes = [P, C.c_int, F64P, F64P, F64P]
+    L.mdx_inifur.argtypes = [P, I32P]
+    L.mdx_chcnb.argtypes = [P, I32P, I32P]
+    L.mdx_get_lists.argtypes = [P, I32P, I32P, C.c_int32, I32P, I32P, C.c_int32]
+    L.mdx_getcom.argtypes = [P]
+    L.mdx_fforces.argtypes = [P, C.c_int, C.POINTER(MdxScalars)]
+    L.mdx_slforces.argtypes = [P, C.POINTER(MdxScalars)]
+    L.mdx_allforce.argtypes = [P, C.POINTER(MdxScalars)]
+    for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
+        getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
+    L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.mdx_stream.argtypes = [P]
+    L.mdx_stream.restype = C.c_void_p
+    L.mdx_launch_count.argtypes = [P]
+    L.mdx_launch_count.restype = C.c_int64
+    L.mdx_sync.argtypes = [P]
+    L.mdx_version.restype = C.c_int
+    _lib = L
+    return L
+
+
+def _fp(a):
+    return a.ctypes.data_as(F64P)
+
+
+class ForcePath:
+    """One system resident on the GPU behind the C ABI."""
+
+    def __init__(self, system, precision: int = MDX_FP64, packed: Packed = None, **caps):
+        self.L = load()
+        self.system = system
+        self.packed = packed or pack(system, precision=precision, **caps)
+        self.n = system.nstot
+        h = C.c_void_p()
+        rc = self.L.mdx_open(C.byref(self.packed.dims), C.byref(h))
+        if rc != 0:
+            raise MdxError(rc, "mdx_open failed (no GPU or bad sizes)")
+        self.h = h
+        self._check(self.L.mdx_upload_topology(self.h, C.byref(self.packed.topo)))
+        self._check(self.L.mdx_set_params(self.h, C.byref(self.packed.params)))
+
+    # ---------------------------------------------------------------- util
+    def _check(self, rc):
+        if rc != 0:
+            raise MdxError(rc, self.L.mdx_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mdx_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self.L.mdx_stream(self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.L.mdx_launch_count(self.h)
+
+    def sync(self):
+        self._check(self.L.mdx_sync(self.h))
+
+    # ---------------------------------------------------------------- data
+    def set_params(self, params: MdxParams):
+        self._check(self.L.mdx_set_params(self.h, C.byref(params)))
+
+    def set_state(self, sx, sy, sz, vx, vy, vz, thermo: MdxThermo = None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (sx, sy, sz, vx, vy, vz)]
+        th = thermo if thermo is not None else thermo_init(self.system)
+        self._check(self.L.mdx_upload_state(self.h, *[_fp(a) for a in arrs], C.byref(th)))
+
+    def get_state(self):
+        out = [np.zeros(self.n) for _ in range(6)]
+        th = MdxThermo()
+        self._check(self.L.mdx_download_state(self.h, *[_fp(a) for a in out], C.byref(th)))
+        return out, th
+
+    def forces(self, which: int = 3) -> np.ndarray:
+        out = [np.zeros(self.n) for _ in range(3)]
+        self._check(self.L.mdx_download_forces(self.h, which, *[_fp(a) for a in out]))
+        return np.stack(out, axis=1)
+
+    # ------------------------------------------------------------ routines
+    def inifur(self) -> int:
+        n = C.c_int32()
+        self._check(self.L.mdx_inifur(self.h, C.byref(n)))
+        return n.value
+
+    def chcnb(self):
+        a, b = C.c_int32(), C.c_int32()
+        self._check(self.L.mdx_chcnb(self.h, C.byref(a), C.byref(b)))
+        self.counts = (a.value, b.value)
+        return self.counts
+
+    def lists(self):
+        ms, ml = self.counts
+        a1, a2 = np.zeros(ms, np.int32), np.zeros(ms, np.int32)
+        b1, b2 = np.zeros(ml, np.int32), np.zeros(ml, np.int32)
+        self._check(self.L.mdx_get_lists(self.h, a1.ctypes.data_as(I32P), a2.ctypes.data_as(I32P),
+                                         ms, b1.ctypes.data_as(I32P), b2.ctypes.data_as(I32P), ml))
+        return (a1, a2), (b1, b2)
+
+    def getcom(self):
+        self._check(self.L.mdx_getcom(self.h))
+
+    def fforces(self, laver: bool = True) -> MdxScalars:
+        s = MdxScalars()
+        self._check(self.L.mdx_fforces(self.h, int(laver), C.byref(s)))
+        return s
+
+    def slforces(self) -> MdxScalars:
+        s = MdxScalars()
+        self._check(self.L.mdx_slforces(self.h, C.byref(s)))
+        return s
+
+    def allforce(self) -> MdxScalars:
+        s = MdxScalars()
+        self._check(self.L.mdx_allforce(self.h, C.byref(s)))
+        return s
+
+    def _run(self, fn, nsteps, start, records=True):
+        recs = (MdxStepRecord * max(1, nsteps))() if records else None
+        self._check(getattr(self.L, fn)(self.h, nsteps, start, recs))
+        return [recs[i] for i in range(nsteps)] if records else None
+
+    def double(self, nsteps: int, nsttot: int = 0, records: bool = True):
+        return self._run("mdx_double", nsteps, nsttot, records)
+
+    def double_steps(self, nsteps: int, mstep0: int, records: bool = True):
+        return self._run("mdx_double_steps", nsteps, mstep0, records)
+
+    def sultan(self, nsteps: int, nsttot: int = 0, records: bool = True):
+        return self._run("mdx_sultan", nsteps, nsttot, records)
+
+    def sultan_steps(self, nsteps: int, mstep0: int, records: bool = True):
+        return self._run("mdx_sultan_steps", nsteps, mstep0, records)
+
+    def set_lambda(self, ec: float, pw1: float = 1.0, pw2: float = 1.0 / 3.0, bee: float = 3.0):
+        self._check(self.L.mdx_set_lambda(self.h, ec, pw1, pw2, bee))
+
+
+__all__ = ["ForcePath", "MdxError", "load", "MDX_FP64", "MDX_MIXED"]

@@ -1,0 +1,2234 @@
+/*
+ * mdx_oracle.c -- CPU restatement of MDynaMix v5.3's force path and
+ * integrators, used as the parity oracle for the GPU library.
+ *
+ * TEST INFRASTRUCTURE ONLY: tests, the smoke check and the benchmark's
+ * CPU-baseline leg call it; the product never does.
+ *
+ * Parity unpinned against the reference binary (Fortran; no compiler on
+ * either machine).  Pinned by invariants in the tests: momentum conservation
+ * of pair and bonded forces, finite-difference forces, alpha independence of
+ * the Ewald total, NVE energy conservation.
+ *
+ * Each routine follows the Fortran statement by statement, in double
+ * precision, with the same operation order.  Arrays are indexed 1..N as in
+ * the Fortran (element 0 unused).  Build flags keep IEEE semantics
+ * (-O2 -ffp-contract=off, no fast-math) so that x86 and Arm agree.
+ *
+ *   ox_chcnb      CHCNB     forces.f:1813-2205
+ *   localf        LOCALF    forces.f:813-998
+ *   forces_long   FORCES    forces.f:1014-1202
+ *   furir         FURIR     forces.f:1217-1339
+ *   ox_inifur     INIFUR    forces.f:1356-1449
+ *   eterms        ETERMS    forces.f:1482-1676
+ *   getbnd        GETBND    forces.f:113-204
+ *   getang        GETANG    forces.f:216-309
+ *   gettrs        GETTRS    forces.f:323-513
+ *   strbnd        STRBND    forces.f:530-800
+ *   ox_fforces    FFORCES   forces.f:36-51   (+ CM_ADDF scalar.f:28-60)
+ *   ox_slforces   SLFORCES  forces.f:55-73   (+ CM_ADDLF scalar.f:64-84)
+ *   ox_allforce   ALLFORCE  forces.f:77-100  (+ CM_ADDLA scalar.f:88-116)
+ *   sclfrc        SCLFRC    service.f:182-287
+ *   zerofs        ZEROFS    service.f:397-453
+ *   ox_getcom     GETCOM    service.f:463-563
+ *   reclen        RECLEN    service.f:572-605
+ *   getemp        GETEMP    service.f:35-117
+ *   pbc           PBC       service.f:953-990
+ *   scaling       SCALING   mdstep.f:534-1093
+ *   shejk         SHEJK     mdstep.f:1105-1283
+ *   ox_double     DOUBLE    mdstep.f:281-530
+ *   ox_sultan     SULTAN    mdstep.f:29-260
+ *   ox_set_lambda RECINT    mdee.f:86-140
+ */
+#include "mdx_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* common_inc.f:22-33 */
+#define A1 0.254829592
+#define A2 (-0.284496736)
+#define A3 1.421413741
+#define A4 (-1.453152027)
+#define A5 1.061405429
+#define B1 0.3275911
+#define PI 3.1415926536
+#define TOTPI 1.128379169
+#define NT MDX_NTPS
+
+struct ox_state {
+  int nstot, nop, ntypes, nsites, nnbt, nrbb, nraa, nrtt, nrbt, nrat, nrrt;
+  int nbdmax, nkvm, caps, capl;
+  int *itype, *nnum, *nsite, *itm;
+  double *massdi, *q;
+  double *charge, *mass;
+  int *inbt;
+  int nspec[NT + 2], nsits[NT + 2], isadr[NT + 2], isaddr[NT + 2],
+      iaddr[NT + 2], ipot[NT + 2], nrb[NT + 2], iadb[NT + 2], ishejk[NT + 2],
+      iee[NT + 2], lmove[NT + 2];
+  double c14el[NT + 2], c14lj[NT + 2], summas[NT + 2];
+  double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
+  int mdxt[NT + 2][NT + 2];
+  int *nnbb, *inbb;
+  int *ib, *jb, *id;
+  double *rb, *fb, *db, *ro;
+  int *ibi, *jbj, *ibuk;
+  double *ra, *fa;
+  int *iai, *jaj, *kak, *iauk;
+  int *itors, *nmul;
+  double *ft, *rt, *ft1, *ft2, *ft3, *ft4, *ft5;
+  int *iti, *jtj, *ktk, *ltl, *ituk;
+  mdx_params p;
+  double boxl, boyl, bozl, hboxl, hboyl, hbozl, boxy3, vol, rssq, short2;
+  int lhex, loct;
+  double *sx, *sy, *sz, *vx, *vy, *vz, *fx, *fy, *fz, *gx, *gy, *gz, *hx,
+      *hy, *hz, *ox, *oy, *oz, *wx, *wy, *wz;
+  double *X, *Y, *Z, *PX, *PY, *PZ;
+  int mbsh, mbln;
+  int *nbs1, *nbs2, *nbl1, *nbl2;
+  int nkv, furir_init;
+  double *rkx, *rky, *rkz;
+  double boxlo, boylo, bozlo;
+  double spei, speei[NT + 2];
+  mdx_scalars s;
+  double *br, *be, *ar, *ae, *tr, *te;
+  mdx_thermo th;
+  int lscfl, nthreads;
+  char msg[256];
+};
+
+#define IDX2(i, j, ld) ((size_t)((i)-1) + (size_t)((j)-1) * (size_t)(ld))
+
+/* Fortran SIGN(A,B): |A| with the sign bit of B, as gfortran on IEEE. */
+static double sgn(double a, double b) { return copysign(fabs(a), b); }
+
+static void *xcalloc(size_t n, size_t sz) {
+  void *p = calloc(n ? n : 1, sz);
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    abort();
+  }
+  return p;
+}
+
+static int *copy_i(const int32_t *src, int n) {
+  int *d = (int *)xcalloc((size_t)n + 1, sizeof(int));
+  if (src)
+    for (int i = 0; i < n; ++i) d[i + 1] = src[i];
+  return d;
+}
+
+static double *copy_d(const double *src, int n) {
+  double *d = (double *)xcalloc((size_t)n + 1, sizeof(double));
+  if (src)
+    for (int i = 0; i < n; ++i) d[i + 1] = src[i];
+  return d;
+}
+
+/* RECLEN (service.f:572-605): box-dependent quantities. */
+static void reclen(ox_state *st, double scx, double scy, double scz) {
+  const double cos30 = (double)0.8660254037844386f;
+  st->boxl = scx * st->boxl;
+  if (st->lhex) {
+    st->boyl = st->boxl * cos30;
+    st->boxy3 = 0.66666666666666666667 * st->boyl;
+    st->bozl = scz * st->bozl;
+  } else if (st->loct) {
+    st->boxl = (scx + scy + scz) * st->boxl / (3. * scx);
+    st->boyl = st->boxl;
+    st->bozl = st->boxl;
+  } else {
+    st->boyl = scy * st->boyl;
+    st->bozl = scz * st->bozl;
+  }
+  st->hboxl = 0.5 * st->boxl;
+  st->hboyl = 0.5 * st->boyl;
+  st->hbozl = 0.5 * st->bozl;
+  st->rssq = st->p.rcut * st->p.rcut;
+  st->vol = st->boxl * st->boyl * st->bozl;
+  if (st->p.icell == 1) st->vol = 0.5 * st->vol;
+}
+
+/* Minimum image as inlined in the force loops and PBC (service.f:953-990).
+ * hbz is HBOZL everywhere except LOCALF, which tests DZ against HBOXL
+ * (forces.f:871); the restatement keeps that. */
+static inline void pbc_h(const ox_state *st, double *xx, double *yy,
+                         double *zz, double hbz) {
+  const double cos30 = (double)0.8660254037844386f;
+  const double boxyc = 0.5 / cos30;
+  double XX = *xx, YY = *yy, ZZ = *zz;
+  if (fabs(XX) > st->hboxl) XX = XX - sgn(st->boxl, XX);
+  if (fabs(ZZ) > hbz) ZZ = ZZ - sgn(st->bozl, ZZ);
+  if (st->lhex) {
+    double XY = boxyc * XX;
+    if (YY > st->boxy3 - XY && (XX > 0. || YY > 2. * st->boxy3 - XY)) {
+      YY = YY - st->boyl;
+      XX = XX - st->hboxl;
+      XY = boxyc * XX;
+    }
+    if (YY < -st->boxy3 - XY && (XX < 0. || YY < -2. * st->boxy3 - XY)) {
+      YY = YY + st->boyl;
+      XX = XX + st->hboxl;
+      XY = boxyc * XX;
+    }
+    if (YY > st->boxy3 + XY) {
+      YY = YY - st->boyl;
+      XX = XX + st->hboxl;
+      XY = boxyc * XX;
+    }
+    if (YY < -st->boxy3 + XY) {
+      YY = YY + st->boyl;
+      XX = XX - st->hboxl;
+    }
+  } else {
+    if (fabs(YY) > st->hboyl) YY = YY - sgn(st->boyl, YY);
+  }
+  if (st->loct) {
+    double corss = st->hboxl *
+                   (double)(int)((double)(4.0f / 3.0f) *
+                                 (fabs(XX) + fabs(YY) + fabs(ZZ)) / st->boxl);
+    XX = XX - sgn(corss, XX);
+    YY = YY - sgn(corss, YY);
+    ZZ = ZZ - sgn(corss, ZZ);
+  }
+  *xx = XX;
+  *yy = YY;
+  *zz = ZZ;
+}
+
+static inline void pbc(const ox_state *st, double *x, double *y, double *z) {
+  pbc_h(st, x, y, z, st->hbozl);
+}
+
+/* ------------------------------------------------------------------ open */
+int ox_open(const mdx_dims *d, const mdx_topo *t, const mdx_params *p,
+            ox_state **out) {
+  ox_state *st = (ox_state *)xcalloc(1, sizeof(ox_state));
+  st->nstot = d->nstot;
+  st->nop = d->nop;
+  st->ntypes = d->ntypes;
+  st->nsites = d->nsites;
+  st->nnbt = d->nnbt;
+  st->nrbb = d->nrbb;
+  st->nraa = d->nraa;
+  st->nrtt = d->nrtt;
+  st->nrbt = d->nrbt;
+  st->nrat = d->nrat;
+  st->nrrt = d->nrrt;
+  st->nbdmax = d->nbdmax;
+  st->nkvm = d->nkv_max;
+  st->nthreads = 1;
+  if (st->ntypes > NT || st->ntypes < 1) {
+    free(st);
+    return MDX_ERR_ARG;
+  }
+  int n = st->nstot;
+  st->itype = copy_i(t->itype, n);
+  st->nnum = copy_i(t->nnum, n);
+  st->nsite = copy_i(t->nsite, n);
+  st->massdi = copy_d(t->massdi, n);
+  st->q = copy_d(t->q, n);
+  st->charge = copy_d(t->charge, st->nsites);
+  st->mass = copy_d(t->mass, st->nsites);
+  st->inbt = copy_i(t->inbt, st->nsites);
+  for (int i = 0; i < st->ntypes; ++i) {
+    st->nspec[i + 1] = t->nspec[i];
+    st->nsits[i + 1] = t->nsits[i];
+    st->isadr[i + 1] = t->isadr[i];
+    st->isaddr[i + 1] = t->isaddr[i];
+    st->iaddr[i + 1] = t->iaddr[i];
+    st->ipot[i + 1] = t->ipot[i];
+    st->nrb[i + 1] = t->nrb[i];
+    st->iadb[i + 1] = t->iadb[i];
+    st->ishejk[i + 1] = t->ishejk[i];
+    st->iee[i + 1] = t->iee[i];
+    st->lmove[i + 1] = t->lmove[i];
+    st->c14el[i + 1] = t->c14el[i];
+    st->c14lj[i + 1] = t->c14lj[i];
+    st->summas[i + 1] = t->summas[i];
+  }
+  st->isadr[st->ntypes + 1] = st->isadr[st->ntypes] + st->nsits[st->ntypes];
+  st->isaddr[st->ntypes + 1] =
+      st->isaddr[st->ntypes] + st->nsits[st->ntypes] * st->nspec[st->ntypes];
+  st->iaddr[st->ntypes + 1] = st->iaddr[st->ntypes] + st->nspec[st->ntypes];
+  int nb = st->nnbt;
+  double **tabs[6] = {&st->a6lj, &st->b12lj, &st->a6lj0,
+                      &st->b12lj0, &st->a6_14, &st->b12_14};
+  const double *srcs[6] = {t->a6lj, t->b12lj, t->a6lj0,
+                           t->b12lj0, t->a6_14, t->b12_14};
+  for (int k = 0; k < 6; ++k) {
+    double *a = (double *)xcalloc((size_t)nb * nb, sizeof(double));
+    for (int j = 1; j <= nb; ++j)
+      for (int i = 1; i <= nb; ++i)
+        a[IDX2(i, j, nb)] = srcs[k][IDX2(i, j, t->ld_lj)];
+    *tabs[k] = a;
+  }
+  for (int j = 1; j <= st->ntypes; ++j)
+    for (int i = 1; i <= st->ntypes; ++i)
+      st->mdxt[i][j] = t->mdx[IDX2(i, j, t->ld_mdx)];
+  st->nnbb = copy_i(t->nnbb, n);
+  st->inbb = (int *)xcalloc((size_t)n * (st->nbdmax > 0 ? st->nbdmax : 1),
+                            sizeof(int));
+  for (int k = 1; k <= st->nbdmax; ++k)
+    for (int i = 1; i <= n; ++i)
+      st->inbb[IDX2(i, k, n)] = t->inbb[IDX2(i, k, t->ld_inbb)];
+  st->ib = copy_i(t->ib, st->nrbb);
+  st->jb = copy_i(t->jb, st->nrbb);
+  st->id = copy_i(t->id, st->nrbb);
+  st->rb = copy_d(t->rb, st->nrbb);
+  st->fb = copy_d(t->fb, st->nrbb);
+  st->db = copy_d(t->db, st->nrbb);
+  st->ro = copy_d(t->ro, st->nrbb);
+  st->ibi = copy_i(t->ibi, st->nrbt);
+  st->jbj = copy_i(t->jbj, st->nrbt);
+  st->ibuk = copy_i(t->ibuk, st->nrbt);
+  st->ra = copy_d(t->ra, st->nraa);
+  st->fa = copy_d(t->fa, st->nraa);
+  st->iai = copy_i(t->iai, st->nrat);
+  st->jaj = copy_i(t->jaj, st->nrat);
+  st->kak = copy_i(t->kak, st->nrat);
+  st->iauk = copy_i(t->iauk, st->nrat);
+  st->itors = copy_i(t->itors, st->nrtt);
+  st->nmul = copy_i(t->nmul, st->nrtt);
+  st->ft = copy_d(t->ft, st->nrtt);
+  st->rt = copy_d(t->rt, st->nrtt);
+  st->ft1 = copy_d(t->ft1, st->nrtt);
+  st->ft2 = copy_d(t->ft2, st->nrtt);
+  st->ft3 = copy_d(t->ft3, st->nrtt);
+  st->ft4 = copy_d(t->ft4, st->nrtt);
+  st->ft5 = copy_d(t->ft5, st->nrtt);
+  st->iti = copy_i(t->iti, st->nrrt);
+  st->jtj = copy_i(t->jtj, st->nrrt);
+  st->ktk = copy_i(t->ktk, st->nrrt);
+  st->ltl = copy_i(t->ltl, st->nrrt);
+  st->ituk = copy_i(t->ituk, st->nrrt);
+  st->itm = (int *)xcalloc((size_t)st->nop + 1, sizeof(int));
+  for (int i = 1; i <= n; ++i) st->itm[st->nnum[i]] = st->itype[i];
+  double **arr[] = {&st->sx, &st->sy, &st->sz, &st->vx, &st->vy, &st->vz,
+                    &st->fx, &st->fy, &st->fz, &st->gx, &st->gy, &st->gz,
+                    &st->hx, &st->hy, &st->hz, &st->ox, &st->oy, &st->oz,
+                    &st->wx, &st->wy, &st->wz};
+  for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); ++k)
+    *arr[k] = (double *)xcalloc((size_t)n + 1, sizeof(double));
+  double **marr[] = {&st->X, &st->Y, &st->Z, &st->PX, &st->PY, &st->PZ};
+  for (int k = 0; k < 6; ++k)
+    *marr[k] = (double *)xcalloc((size_t)st->nop + 1, sizeof(double));
+  st->caps = d->cap_short > 0 ? d->cap_short : 64;
+  st->capl = d->cap_long > 0 ? d->cap_long : 1000;
+  st->nbs1 = (int *)xcalloc((size_t)st->caps * n + 1, sizeof(int));
+  st->nbs2 = (int *)xcalloc((size_t)st->caps * n + 1, sizeof(int));
+  st->nbl1 = (int *)xcalloc((size_t)st->capl * n + 1, sizeof(int));
+  st->nbl2 = (int *)xcalloc((size_t)st->capl * n + 1, sizeof(int));
+  st->rkx = (double *)xcalloc((size_t)st->nkvm + 1, sizeof(double));
+  st->rky = (double *)xcalloc((size_t)st->nkvm + 1, sizeof(double));
+  st->rkz = (double *)xcalloc((size_t)st->nkvm + 1, sizeof(double));
+  st->br = (double *)xcalloc((size_t)st->nrbb + 1, sizeof(double));
+  st->be = (double *)xcalloc((size_t)st->nrbb + 1, sizeof(double));
+  st->ar = (double *)xcalloc((size_t)st->nraa + 1, sizeof(double));
+  st->ae = (double *)xcalloc((size_t)st->nraa + 1, sizeof(double));
+  st->tr = (double *)xcalloc((size_t)st->nrtt + 1, sizeof(double));
+  st->te = (double *)xcalloc((size_t)st->nrtt + 1, sizeof(double));
+  ox_set_params(st, p);
+  *out = st;
+  return MDX_OK;
+}
+
+int ox_set_params(ox_state *st, const mdx_params *p) {
+  st->p = *p;
+  st->lhex = p->icell == 2;
+  st->loct = p->icell == 1;
+  st->boxl = p->boxl;
+  st->boyl = p->boyl;
+  st->bozl = p->bozl;
+  st->th.boxl = p->boxl;
+  st->th.boyl = p->boyl;
+  st->th.bozl = p->bozl;
+  if (st->lhex) st->boxy3 = 0.66666666666666666667 * st->boyl;
+  reclen(st, 1.0, 1.0, 1.0);
+  st->short2 = p->rshort * p->rshort;
+  st->furir_init = 0;
+  return MDX_OK;
+}
+
+void ox_close(ox_state *st) {
+  if (!st) return;
+  void *ptrs[] = {st->itype, st->nnum, st->nsite, st->itm, st->massdi, st->q,
+                  st->charge, st->mass, st->inbt, st->a6lj, st->b12lj,
+                  st->a6lj0, st->b12lj0, st->a6_14, st->b12_14, st->nnbb,
+                  st->inbb, st->ib, st->jb, st->id, st->rb, st->fb, st->db,
+                  st->ro, st->ibi, st->jbj, st->ibuk, st->ra, st->fa, st->iai,
+                  st->jaj, st->kak, st->iauk, st->itors, st->nmul, st->ft,
+                  st->rt, st->ft1, st->ft2, st->ft3, st->ft4, st->ft5, st->iti,
+                  st->jtj, st->ktk, st->ltl, st->ituk, st->sx, st->sy, st->sz,
+                  st->vx, st->vy, st->vz, st->fx, st->fy, st->fz, st->gx,
+                  st->gy, st->gz, st->hx, st->hy, st->hz, st->ox, st->oy,
+                  st->oz, st->wx, st->wy, st->wz, st->X, st->Y, st->Z, st->PX,
+                  st->PY, st->PZ, st->nbs1, st->nbs2, st->nbl1, st->nbl2,
+                  st->rkx, st->rky, st->rkz, st->br, st->be, st->ar, st->ae,
+                  st->tr, st->te};
+  for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k) free(ptrs[k]);
+  free(st);
+}
+
+const char *ox_last_error(const ox_state *st) { return st ? st->msg : ""; }
+
+int ox_set_threads(ox_state *st, int n) {
+  st->nthreads = n > 0 ? n : 1;
+  return MDX_OK;
+}
+
+int ox_set_state(ox_state *st, const double *sx, const double *sy,
+                 const double *sz, const double *vx, const double *vy,
+                 const double *vz, const mdx_thermo *th) {
+  for (int i = 0; i < st->nstot; ++i) {
+    st->sx[i + 1] = sx[i];
+    st->sy[i + 1] = sy[i];
+    st->sz[i + 1] = sz[i];
+    st->vx[i + 1] = vx[i];
+    st->vy[i + 1] = vy[i];
+    st->vz[i + 1] = vz[i];
+  }
+  if (th) {
+    double bl = st->boxl, by = st->boyl, bz = st->bozl;
+    st->th = *th;
+    if (th->boxl > 0.0) {
+      st->boxl = th->boxl;
+      st->boyl = th->boyl;
+      st->bozl = th->bozl;
+      if (st->lhex) st->boxy3 = 0.66666666666666666667 * st->boyl;
+      reclen(st, 1.0, 1.0, 1.0);
+    } else {
+      st->th.boxl = bl;
+      st->th.boyl = by;
+      st->th.bozl = bz;
+    }
+  }
+  /* molecular centres as the driver's last GETCOM left them: wrapped COM of
+   * the given coordinates, coordinates untouched */
+  {
+    int N = 0, I = 0;
+    for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP)
+      for (int J = 1; J <= st->nspec[ITYP]; ++J) {
+        I = I + 1;
+        double x = 0., y = 0., z = 0.;
+        for (int IS = st->isadr[ITYP] + 1; IS <= st->isadr[ITYP + 1]; ++IS) {
+          N = N + 1;
+          x = x + st->mass[IS] * st->sx[N];
+          y = y + st->mass[IS] * st->sy[N];
+          z = z + st->mass[IS] * st->sz[N];
+        }
+        x = x / st->summas[ITYP];
+        y = y / st->summas[ITYP];
+        z = z / st->summas[ITYP];
+        pbc(st, &x, &y, &z);
+        st->X[I] = x;
+        st->Y[I] = y;
+        st->Z[I] = z;
+      }
+  }
+  return MDX_OK;
+}
+
+static void sync_thermo_box(ox_state *st) {
+  st->th.boxl = st->boxl;
+  st->th.boyl = st->boyl;
+  st->th.bozl = st->bozl;
+  st->th.vol = st->vol;
+}
+
+int ox_get_state(ox_state *st, double *sx, double *sy, double *sz, double *vx,
+                 double *vy, double *vz, mdx_thermo *th) {
+  for (int i = 0; i < st->nstot; ++i) {
+    if (sx) sx[i] = st->sx[i + 1];
+    if (sy) sy[i] = st->sy[i + 1];
+    if (sz) sz[i] = st->sz[i + 1];
+    if (vx) vx[i] = st->vx[i + 1];
+    if (vy) vy[i] = st->vy[i + 1];
+    if (vz) vz[i] = st->vz[i + 1];
+  }
+  sync_thermo_box(st);
+  if (th) *th = st->th;
+  return MDX_OK;
+}
+
+int ox_get_forces(ox_state *st, int which, double *fx, double *fy,
+                  double *fz) {
+  const double *ax = which == 1 ? st->hx : which == 2 ? st->gx : st->fx;
+  const double *ay = which == 1 ? st->hy : which == 2 ? st->gy : st->fy;
+  const double *az = which == 1 ? st->hz : which == 2 ? st->gz : st->fz;
+  for (int i = 0; i < st->nstot; ++i) {
+    fx[i] = ax[i + 1];
+    fy[i] = ay[i + 1];
+    fz[i] = az[i + 1];
+  }
+  return MDX_OK;
+}
+
+int ox_get_bonded_averages(ox_state *st, double *br, double *be, double *ar,
+                           double *ae, double *tr, double *te) {
+  for (int i = 0; i < st->nrbb; ++i) {
+    if (br) br[i] = st->br[i + 1];
+    if (be) be[i] = st->be[i + 1];
+  }
+  for (int i = 0; i < st->nraa; ++i) {
+    if (ar) ar[i] = st->ar[i + 1];
+    if (ae) ae[i] = st->ae[i + 1];
+  }
+  for (int i = 0; i < st->nrtt; ++i) {
+    if (tr) tr[i] = st->tr[i + 1];
+    if (te) te[i] = st->te[i + 1];
+  }
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- CHCNB */
+/* Classify one candidate pair of the strip loop (forces.f:1838-2134).
+ * Returns 0 none, 1 short, 2 long, 3 short 1-4, -1 excluded. */
+static inline int chcnb_pair(const ox_state *st, int I, int J, int imol) {
+  int jmol = st->nnum[J];
+  double DX = st->sx[I] - st->sx[J];
+  double DY = st->sy[I] - st->sy[J];
+  double DZ = st->sz[I] - st->sz[J];
+  pbc(st, &DX, &DY, &DZ);
+  double RR2 = DX * DX + DY * DY + DZ * DZ;
+  double RRM = RR2; /* Ewald: atomic cutoff (LMNBL handled by the caller) */
+  if (imol == jmol) {
+    if (RR2 <= 64.0) {
+      int nb = st->nnbb[I];
+      for (int K = 1; K <= nb; ++K) {
+        int v = st->inbb[IDX2(I, K, st->nstot)];
+        if (v == J) return -1;
+        if (v == -J) return 3;
+      }
+    }
+  }
+  if (RRM <= st->short2) return 1;
+  if (RRM <= st->rssq) return 2;
+  return 0;
+}
+
+int ox_chcnb(ox_state *st, int32_t *mbsh, int32_t *mbln) {
+  if (st->p.lmnbl) {
+    snprintf(st->msg, sizeof st->msg, "reaction-field list not restated");
+    return MDX_ERR_UNSUPPORTED;
+  }
+  const int n = st->nstot;
+  long capS = (long)st->caps * n, capL = (long)st->capl * n;
+  long MBSH = 0, MBLN = 0;
+  int iover = 0;
+  int nth = st->nthreads;
+  if (nth <= 1) {
+    for (int I = 1; I <= n; ++I) {
+      int imol = st->nnum[I];
+      for (int J = I - 2; J >= 1; J -= 2) { /* even strip */
+        int c = chcnb_pair(st, I, J, imol);
+        if (c == 3) {
+          if (MBSH < capS) { st->nbs1[MBSH + 1] = -I; st->nbs2[MBSH + 1] = J; }
+          ++MBSH;
+        } else if (c == 1) {
+          if (MBSH < capS) { st->nbs1[MBSH + 1] = I; st->nbs2[MBSH + 1] = J; }
+          ++MBSH;
+        } else if (c == 2) {
+          if (MBLN < capL) { st->nbl1[MBLN + 1] = I; st->nbl2[MBLN + 1] = J; }
+          else iover = 1;
+          ++MBLN;
+        }
+      }
+      for (int J = I + 1; J <= n; J += 2) { /* odd strip */
+        int c = chcnb_pair(st, I, J, imol);
+        if (c == 3) {
+          if (MBSH < capS) { st->nbs1[MBSH + 1] = -I; st->nbs2[MBSH + 1] = J; }
+          ++MBSH;
+        } else if (c == 1) {
+          if (MBSH < capS) { st->nbs1[MBSH + 1] = J; st->nbs2[MBSH + 1] = I; }
+          ++MBSH;
+        } else if (c == 2) {
+          if (MBLN < capL) { st->nbl1[MBLN + 1] = J; st->nbl2[MBLN + 1] = I; }
+          else iover = 1;
+          ++MBLN;
+        }
+      }
+    }
+  } else {
+    /* Threads scan disjoint blocks of I into private buffers which are
+     * concatenated in I order: the same lists as the serial scan. */
+    int nblk = nth * 8;
+    long *cs = (long *)xcalloc((size_t)nblk + 1, sizeof(long));
+    long *cl = (long *)xcalloc((size_t)nblk + 1, sizeof(long));
+    int **bs = (int **)xcalloc((size_t)nblk, sizeof(int *));
+    int **bl = (int **)xcalloc((size_t)nblk, sizeof(int *));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+    for (int b = 0; b < nblk; ++b) {
+      int i0 = 1 + (int)((long)n * b / nblk), i1 = (int)((long)n * (b + 1) / nblk);
+      long cap_s = 64, cap_l = 1024, ns = 0, nl = 0;
+      int *ps = (int *)malloc(sizeof(int) * 2 * cap_s);
+      int *pl = (int *)malloc(sizeof(int) * 2 * cap_l);
+      for (int I = i0; I <= i1; ++I) {
+        int imol = st->nnum[I];
+        for (int pass = 0; pass < 2; ++pass) {
+          int J = pass == 0 ? I - 2 : I + 1;
+          int step = pass == 0 ? -2 : 2;
+          for (; pass == 0 ? J >= 1 : J <= n; J += step) {
+            int c = chcnb_pair(st, I, J, imol);
+            if (c <= 0) continue;
+            int a, bb;
+            if (c == 3) { a = -I; bb = J; }
+            else if (pass == 0) { a = I; bb = J; }
+            else { a = J; bb = I; }
+            if (c == 2) {
+              if (nl == cap_l) { cap_l *= 2; pl = (int *)realloc(pl, sizeof(int) * 2 * cap_l); }
+              pl[2 * nl] = a; pl[2 * nl + 1] = bb; ++nl;
+            } else {
+              if (ns == cap_s) { cap_s *= 2; ps = (int *)realloc(ps, sizeof(int) * 2 * cap_s); }
+              ps[2 * ns] = a; ps[2 * ns + 1] = bb; ++ns;
+            }
+          }
+        }
+      }
+      bs[b] = ps; bl[b] = pl; cs[b + 1] = ns; cl[b + 1] = nl;
+    }
+    for (int b = 0; b < nblk; ++b) {
+      for (long k = 0; k < cs[b + 1]; ++k) {
+        if (MBSH < capS) { st->nbs1[MBSH + 1] = bs[b][2 * k]; st->nbs2[MBSH + 1] = bs[b][2 * k + 1]; }
+        ++MBSH;
+      }
+      for (long k = 0; k < cl[b + 1]; ++k) {
+        if (MBLN < capL) { st->nbl1[MBLN + 1] = bl[b][2 * k]; st->nbl2[MBLN + 1] = bl[b][2 * k + 1]; }
+        else iover = 1;
+        ++MBLN;
+      }
+      free(bs[b]); free(bl[b]);
+    }
+    free(bs); free(bl); free(cs); free(cl);
+  }
+  st->mbsh = (int)(MBSH < capS ? MBSH : capS);
+  st->mbln = (int)(MBLN < capL ? MBLN : capL);
+  if (mbsh) *mbsh = (int32_t)MBSH;
+  if (mbln) *mbln = (int32_t)MBLN;
+  if (MBSH > capS) {
+    snprintf(st->msg, sizeof st->msg,
+             "list of closest neighbours overfilled: %ld > %ld", MBSH, capS);
+    return MDX_ERR_LIST_OVERFLOW;
+  }
+  if (iover || MBLN > capL) {
+    snprintf(st->msg, sizeof st->msg,
+             "list of far neighbours overfilled: need %ld > %ld", MBLN, capL);
+    return MDX_ERR_LIST_OVERFLOW;
+  }
+  return MDX_OK;
+}
+
+int ox_get_lists(ox_state *st, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
+                 int32_t *nbl1, int32_t *nbl2, int32_t cap_l) {
+  if (st->mbsh > cap_s || st->mbln > cap_l) return MDX_ERR_ARG;
+  for (int k = 0; k < st->mbsh; ++k) {
+    nbs1[k] = st->nbs1[k + 1];
+    nbs2[k] = st->nbs2[k + 1];
+  }
+  for (int k = 0; k < st->mbln; ++k) {
+    nbl1[k] = st->nbl1[k + 1];
+    nbl2[k] = st->nbl2[k + 1];
+  }
+  return MDX_OK;
+}
+
+/* --------------------------------------------------------------- ZEROFS */
+static void zerofs(ox_state *st, int nnn) {
+  mdx_scalars *s = &st->s;
+  int molint = st->p.molint;
+  if (nnn == 1) {
+    s->pels2 = 0.; s->pint = 0.; s->pe2 = 0.; s->virb = 0.; s->vir2 = 0.;
+    s->wirss = 0.; s->virfx = 0.; s->virfy = 0.; s->virfz = 0.;
+    for (int i = 0; i < molint; ++i) { s->pote1[i] = 0.; s->potl1[i] = 0.; }
+    for (int i = 0; i < st->ntypes; ++i) { s->pes141[i] = 0.; s->psr141[i] = 0.; }
+    for (int i = 1; i <= st->nstot; ++i) { st->hx[i] = 0.; st->hy[i] = 0.; st->hz[i] = 0.; }
+  } else {
+    for (int i = 0; i < molint; ++i) { s->pote1[i] = 0.; s->potl1[i] = 0.; }
+    for (int i = 0; i < st->ntypes; ++i) { s->pes141[i] = 0.; s->psr141[i] = 0.; }
+    s->wirs = 0.; s->vir1 = 0.; s->pe1 = 0.; s->pels1 = 0.;
+    s->virx = 0.; s->viry = 0.; s->virz = 0.;
+    for (int i = 1; i <= st->nstot; ++i) { st->gx[i] = 0.; st->gy[i] = 0.; st->gz[i] = 0.; }
+  }
+}
+
+/* Pair parameters common to LOCALF and FORCES (forces.f:838-862). */
+static inline void pair_params(const ox_state *st, int ISP0, int ISP, int JSP,
+                               double *QIJ, double *A6, double *B12,
+                               double *RAE) {
+  int ITYP = st->itype[ISP], JTYP = st->itype[JSP];
+  int ISB = st->nsite[ISP], JSB = st->nsite[JSP];
+  int IMOL = st->nnum[ISP], JMOL = st->nnum[JSP];
+  int ISN = st->inbt[ISB], JSN = st->inbt[JSB];
+  int nb = st->nnbt;
+  if (IMOL == JMOL) {
+    if (ISP0 < 0) {
+      *QIJ = st->charge[ISB] * st->charge[JSB] * st->p.coulf * st->c14el[ITYP];
+      *A6 = st->a6_14[IDX2(ISN, JSN, nb)] * st->c14lj[ITYP];
+      *B12 = st->b12_14[IDX2(ISN, JSN, nb)] * st->c14lj[ITYP];
+    } else {
+      *QIJ = st->charge[ISB] * st->charge[JSB] * st->p.coulf;
+      *A6 = st->a6lj0[IDX2(ISN, JSN, nb)];
+      *B12 = st->b12lj0[IDX2(ISN, JSN, nb)];
+    }
+    *RAE = 0.;
+  } else {
+    *QIJ = st->q[ISP] * st->q[JSP] * st->p.coulf;
+    *A6 = st->a6lj[IDX2(ISN, JSN, nb)];
+    *B12 = st->b12lj[IDX2(ISN, JSN, nb)];
+    *RAE = 0.;
+    if (st->p.lmdee) {
+      if (st->iee[ITYP] * st->iee[JTYP] == 0)
+        *RAE = st->p.raex;
+      else
+        *RAE = 0.;
+    }
+  }
+}
+
+/* --------------------------------------------------------------- LOCALF */
+static void localf(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  const double ALPHAD = st->p.alphad;
+  for (int INP = 1; INP <= st->mbsh; ++INP) {
+    int ISP0 = st->nbs1[INP];
+    int ISP = abs(ISP0);
+    int JSP = st->nbs2[INP];
+    int ITYP = st->itype[ISP], JTYP = st->itype[JSP];
+    int IMOL = st->nnum[ISP], JMOL = st->nnum[JSP];
+    int MTR = st->mdxt[ITYP][JTYP];
+    double QIJ, A6, B12, RAE;
+    (void)JTYP;
+    pair_params(st, ISP0, ISP, JSP, &QIJ, &A6, &B12, &RAE);
+    double DX = st->sx[ISP] - st->sx[JSP];
+    double DY = st->sy[ISP] - st->sy[JSP];
+    double DZ = st->sz[ISP] - st->sz[JSP];
+    pbc_h(st, &DX, &DY, &DZ, st->hboxl); /* forces.f:871 tests DZ vs HBOXL */
+    double RR = DX * DX + DY * DY + DZ * DZ;
+    double R1 = sqrt(RR);
+    double R1I = 1. / R1;
+    double R1E = R1 + RAE;
+    double R1EI = 1. / R1E;
+    double EE1, EES, FORCE;
+    if (ISP0 <= 0 || (IMOL == JMOL && st->iee[ITYP] == 0)) {
+      EE1 = QIJ * R1I;
+      if (st->lmove[ITYP])
+        FORCE = EE1 * (R1I * R1I);
+      else
+        FORCE = 0.;
+      EES = EE1;
+    } else if (st->p.lmnbl) {
+      EE1 = QIJ * (1 / R1E - 0.5 * st->p.rff2 * (R1E * R1E) + st->p.rff);
+      EES = EE1;
+      FORCE = QIJ * (1. / (R1E * R1E * R1E) + st->p.rff2);
+      s->vir2 = s->vir2 + QIJ * (1.5 * st->p.rff2 / (R1E * R1E) - st->p.rff);
+    } else {
+      double ALPHAR = ALPHAD * R1;
+      double TTT = 1.0 / (1.0 + B1 * ALPHAR);
+      double EXP2A = exp(-(ALPHAR * ALPHAR));
+      double ERFCT = ((((A5 * TTT + A4) * TTT + A3) * TTT + A2) * TTT + A1) * TTT * EXP2A;
+      EE1 = QIJ * R1EI;
+      EES = EE1 * ERFCT;
+      FORCE = EE1 * (TOTPI * ALPHAD * EXP2A + ERFCT * R1EI) * R1I;
+    }
+    if (IMOL == JMOL)
+      s->pes141[ITYP - 1] = s->pes141[ITYP - 1] + EE1;
+    else
+      s->pote1[MTR - 1] = s->pote1[MTR - 1] + EE1;
+    s->pels2 = s->pels2 + EES;
+    if (B12 != 0.0) {
+      double R2I = R1EI * R1EI;
+      double R6I = R2I * R2I * R2I;
+      double ESR = (A6 + B12 * R6I) * R6I;
+      double FSR = (6.0 * A6 + 12.0 * B12 * R6I) * R6I * R1EI;
+      FORCE = FORCE + FSR * R1I;
+      if (IMOL == JMOL) {
+        if (st->lmove[ITYP]) {
+          s->psr141[ITYP - 1] = s->psr141[ITYP - 1] + ESR;
+          s->vir2 = s->vir2 + FSR * R1;
+        } else {
+          ESR = 0.;
+          FORCE = 0.;
+        }
+      } else {
+        s->potl1[MTR - 1] = s->potl1[MTR - 1] + ESR;
+        s->vir2 = s->vir2 + FSR * R1;
+      }
+      s->pe2 = s->pe2 + ESR;
+    }
+    st->hx[ISP] = st->hx[ISP] + FORCE * DX;
+    st->hy[ISP] = st->hy[ISP] + FORCE * DY;
+    st->hz[ISP] = st->hz[ISP] + FORCE * DZ;
+    st->hx[JSP] = st->hx[JSP] - FORCE * DX;
+    st->hy[JSP] = st->hy[JSP] - FORCE * DY;
+    st->hz[JSP] = st->hz[JSP] - FORCE * DZ;
+    s->virfx = s->virfx + FORCE * (DX * DX);
+    s->virfy = s->virfy + FORCE * (DY * DY);
+    s->virfz = s->virfz + FORCE * (DZ * DZ);
+  }
+  for (int N = 1; N <= st->nstot; ++N) {
+    int M = st->nnum[N];
+    s->wirss = s->wirss - st->hx[N] * (st->sx[N] - st->X[M]) -
+               st->hy[N] * (st->sy[N] - st->Y[M]) -
+               st->hz[N] * (st->sz[N] - st->Z[M]);
+  }
+}
+
+/* --------------------------------------------------------------- FORCES */
+static void forces_long(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  const double ALPHAD = st->p.alphad;
+  for (int INP = 1; INP <= st->mbln; ++INP) {
+    int ISP0 = st->nbl1[INP];
+    int JSP = st->nbl2[INP];
+    int ISP = abs(ISP0);
+    int ITYP = st->itype[ISP], JTYP = st->itype[JSP];
+    int IMOL = st->nnum[ISP], JMOL = st->nnum[JSP];
+    int MTR = st->mdxt[ITYP][JTYP];
+    double QIJ, A6, B12, RAE;
+    pair_params(st, ISP0, ISP, JSP, &QIJ, &A6, &B12, &RAE);
+    double DX = st->sx[ISP] - st->sx[JSP];
+    double DY = st->sy[ISP] - st->sy[JSP];
+    double DZ = st->sz[ISP] - st->sz[JSP];
+    pbc(st, &DX, &DY, &DZ);
+    double RR = DX * DX + DY * DY + DZ * DZ;
+    double R1 = sqrt(RR);
+    double R1I = 1. / R1;
+    double R1E = R1 + RAE;
+    double R1EI = 1. / R1E;
+    double EE1, EES, FORCE;
+    (void)R1I;
+    if (ISP0 <= 0 || (IMOL == JMOL && st->iee[ITYP] == 0)) {
+      EE1 = QIJ / R1;
+      if (st->lmove[ITYP])
+        FORCE = EE1 / (R1 * R1);
+      else
+        FORCE = 0.;
+      EES = EE1;
+    } else if (st->p.lmnbl) {
+      EE1 = QIJ * (1 / R1E - 0.5 * st->p.rff2 * (R1E * R1E) + st->p.rff);
+      EES = EE1;
+      FORCE = QIJ * (1 / ((R1E * R1E) * R1) + st->p.rff2);
+      s->vir1 = s->vir1 + QIJ * (1.5 * st->p.rff2 * RR - st->p.rff);
+    } else {
+      double ALPHAR = ALPHAD * R1;
+      double TTT = 1.0 / (1.0 + B1 * ALPHAR);
+      double EXP2A = exp(-(ALPHAR * ALPHAR));
+      double ERFCT = ((((A5 * TTT + A4) * TTT + A3) * TTT + A2) * TTT + A1) * TTT * EXP2A;
+      EE1 = QIJ * R1EI;
+      EES = EE1 * ERFCT;
+      FORCE = EE1 * (TOTPI * ALPHAD * EXP2A + ERFCT * R1EI) * R1I;
+    }
+    if (IMOL == JMOL)
+      s->pes141[ITYP - 1] = s->pes141[ITYP - 1] + EE1;
+    else
+      s->pote1[MTR - 1] = s->pote1[MTR - 1] + EE1;
+    s->pels1 = s->pels1 + EES;
+    if (B12 != 0.0) {
+      double R2I = R1EI * R1EI;
+      double R6I = R2I * R2I * R2I;
+      double ESR = (A6 + B12 * R6I) * R6I;
+      double FSR = (6.0 * A6 + 12.0 * B12 * R6I) * R6I * R1EI;
+      FORCE = FORCE + FSR * R1I;
+      if (IMOL == JMOL) {
+        if (st->lmove[ITYP]) s->vir1 = s->vir1 + FSR * R1;
+        s->psr141[ITYP - 1] = s->psr141[ITYP - 1] + ESR;
+      } else {
+        s->potl1[MTR - 1] = s->potl1[MTR - 1] + ESR;
+        s->vir1 = s->vir1 + FSR * R1;
+      }
+      s->pe1 = s->pe1 + ESR;
+    }
+    if (IMOL != JMOL || st->lmove[ITYP]) {
+      s->virx = s->virx + FORCE * (DX * DX);
+      s->viry = s->viry + FORCE * (DY * DY);
+      s->virz = s->virz + FORCE * (DZ * DZ);
+    }
+    st->gx[ISP] = st->gx[ISP] + FORCE * DX;
+    st->gy[ISP] = st->gy[ISP] + FORCE * DY;
+    st->gz[ISP] = st->gz[ISP] + FORCE * DZ;
+    st->gx[JSP] = st->gx[JSP] - FORCE * DX;
+    st->gy[JSP] = st->gy[JSP] - FORCE * DY;
+    st->gz[JSP] = st->gz[JSP] - FORCE * DZ;
+  }
+}
+
+/* ---------------------------------------------------------------- INIFUR */
+int ox_inifur(ox_state *st, int32_t *nkv) {
+  double ALP2 = st->p.alphad * st->p.alphad;
+  double CUTK2 = 4.0 * ALP2 * st->p.fexp;
+  double CUTK = sqrt(CUTK2);
+  double TWOPI = 2.0 * PI;
+  int IKV = 0;
+  int KMAX = (int)(CUTK * st->boxl / TWOPI + 1);
+  int KMAY = (int)(CUTK * st->boyl / TWOPI + 1);
+  int KMAZ = (int)(CUTK * st->bozl / TWOPI + 1);
+  for (int IKZ = -KMAZ; IKZ <= KMAZ; ++IKZ)
+    for (int IKX = 0; IKX <= KMAX; ++IKX) {
+      int KY1, KY2;
+      if (IKX == 0) {
+        KY1 = IKZ > 0 ? 0 : 1;
+        KY2 = KMAY;
+      } else {
+        KY1 = -KMAY;
+        KY2 = KMAY;
+      }
+      for (int IKY = KY1; IKY <= KY2; ++IKY) {
+        double RXV, RYV, RZV;
+        if (st->p.icell == 1) {
+          RXV = TWOPI * IKX; RYV = TWOPI * IKY; RZV = TWOPI * (-IKX + IKY + 2 * IKZ);
+        } else if (st->p.icell == 2) {
+          RXV = TWOPI * IKX; RYV = TWOPI * IKY + PI * IKX; RZV = TWOPI * IKZ;
+        } else {
+          RXV = TWOPI * IKX; RYV = TWOPI * IKY; RZV = TWOPI * IKZ;
+        }
+        double rx = RXV / st->boxl, ry = RYV / st->boyl, rz = RZV / st->bozl;
+        double RK2 = rx * rx + ry * ry + rz * rz;
+        if (RK2 <= CUTK2) {
+          IKV = IKV + 1;
+          if (IKV > st->nkvm) {
+            snprintf(st->msg, sizeof st->msg, "max number of reciprocal vectors exceeded");
+            return MDX_ERR_KVEC;
+          }
+          st->rkx[IKV] = RXV;
+          st->rky[IKV] = RYV;
+          st->rkz[IKV] = RZV;
+        }
+      }
+    }
+  st->nkv = IKV;
+  double ABC = st->p.alphad / sqrt(PI);
+  st->spei = 0.;
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+    double SPET = 0.;
+    double ESCI = st->iee[ITYP] == 0 ? st->p.ec_me : 1.0;
+    for (int I = 1; I <= st->nsits[ITYP]; ++I) {
+      int IS = st->isadr[ITYP] + I;
+      double eq = ESCI * st->charge[IS];
+      double QII = st->p.coulf * (eq * eq);
+      SPET = SPET - st->nspec[ITYP] * ABC * QII;
+    }
+    st->speei[ITYP] = SPET;
+    st->spei = st->spei + SPET;
+  }
+  if (nkv) *nkv = IKV;
+  return MDX_OK;
+}
+
+/* ----------------------------------------------------------------- FURIR */
+static int furir(ox_state *st) {
+  const double FKTX = 1.05, FKTS = 0.95;
+  mdx_scalars *s = &st->s;
+  int rc;
+  if (!st->furir_init) {
+    st->furir_init = 1;
+    st->boxlo = st->boxl;
+    st->boylo = st->boyl;
+    st->bozlo = st->bozl;
+    if (st->p.alphad > 0.0) {
+      if ((rc = ox_inifur(st, NULL))) return rc;
+    } else {
+      st->nkv = 0;
+    }
+  }
+  double DBX = st->boxl / st->boxlo, DBY = st->boyl / st->boylo, DBZ = st->bozl / st->bozlo;
+  if (DBX > FKTX || DBX < FKTS || DBY > FKTX || DBY < FKTS || DBZ > FKTX || DBZ < FKTS) {
+    st->boxlo = st->boxl;
+    st->boylo = st->boyl;
+    st->bozlo = st->bozl;
+    if ((rc = ox_inifur(st, NULL))) return rc;
+  }
+  s->nkv = st->nkv;
+  if (st->nkv == 0 || (st->ntypes == 1 && st->nspec[1] == 1)) return MDX_OK;
+  const double ALP2 = st->p.alphad * st->p.alphad;
+  const double CFUR = 4.0 * PI * st->p.coulf / st->vol;
+  const int n = st->nstot;
+  double QPE = 0.0, vx_ = 0., vy_ = 0., vz_ = 0.;
+  int nth = st->nthreads;
+  if (nth <= 1) {
+    double *TSIN = (double *)xcalloc((size_t)n + 1, sizeof(double));
+    double *TCOS = (double *)xcalloc((size_t)n + 1, sizeof(double));
+    for (int IKV = 1; IKV <= st->nkv; ++IKV) {
+      double RXV = st->rkx[IKV] / st->boxl;
+      double RYV = st->rky[IKV] / st->boyl;
+      double RZV = st->rkz[IKV] / st->bozl;
+      double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
+      double SCS = 0., SSN = 0.;
+      for (int I = 1; I <= n; ++I) {
+        double SCP = RXV * st->sx[I] + RYV * st->sy[I] + RZV * st->sz[I];
+        double QQ = st->q[I];
+        double SINSC = QQ * sin(SCP);
+        double COSSC = QQ * cos(SCP);
+        TSIN[I] = SINSC;
+        TCOS[I] = COSSC;
+        SSN = SSN + SINSC;
+        SCS = SCS + COSSC;
+      }
+      double AKC = CFUR * exp(-0.25 * RK2 / ALP2) / RK2;
+      QPE = QPE + AKC * (SSN * SSN + SCS * SCS);
+      double AK2 = 2.0 * AKC;
+      for (int I = 1; I <= n; ++I) {
+        double QFOR = AK2 * (SCS * TSIN[I] - SSN * TCOS[I]);
+        st->gx[I] = st->gx[I] + RXV * QFOR;
+        st->gy[I] = st->gy[I] + RYV * QFOR;
+        st->gz[I] = st->gz[I] + RZV * QFOR;
+      }
+      double AKV = 0.5 * AKC * (4. * ALP2 + RK2) / (ALP2 * RK2);
+      double S2 = SSN * SSN + SCS * SCS;
+      s->virx = s->virx - (RXV * RXV) * AKV * S2;
+      s->viry = s->viry - (RYV * RYV) * AKV * S2;
+      s->virz = s->virz - (RZV * RZV) * AKV * S2;
+    }
+    free(TSIN);
+    free(TCOS);
+  } else {
+    /* threads take disjoint k ranges with private force buffers */
+    double *gacc = (double *)xcalloc((size_t)nth * 3 * (n + 1), sizeof(double));
+    double *eacc = (double *)xcalloc((size_t)nth * 4, sizeof(double));
+#pragma omp parallel num_threads(nth)
+    {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      double *gx = gacc + (size_t)tid * 3 * (n + 1), *gy = gx + (n + 1), *gz = gy + (n + 1);
+      double *TSIN = (double *)malloc(sizeof(double) * (n + 1));
+      double *TCOS = (double *)malloc(sizeof(double) * (n + 1));
+      double qpe = 0., v1 = 0., v2 = 0., v3 = 0.;
+#pragma omp for schedule(static)
+      for (int IKV = 1; IKV <= st->nkv; ++IKV) {
+        double RXV = st->rkx[IKV] / st->boxl, RYV = st->rky[IKV] / st->boyl, RZV = st->rkz[IKV] / st->bozl;
+        double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
+        double SCS = 0., SSN = 0.;
+        for (int I = 1; I <= n; ++I) {
+          double SCP = RXV * st->sx[I] + RYV * st->sy[I] + RZV * st->sz[I];
+          double QQ = st->q[I];
+          TSIN[I] = QQ * sin(SCP);
+          TCOS[I] = QQ * cos(SCP);
+          SSN += TSIN[I];
+          SCS += TCOS[I];
+        }
+        double AKC = CFUR * exp(-0.25 * RK2 / ALP2) / RK2;
+        qpe += AKC * (SSN * SSN + SCS * SCS);
+        double AK2 = 2.0 * AKC;
+        for (int I = 1; I <= n; ++I) {
+          double QFOR = AK2 * (SCS * TSIN[I] - SSN * TCOS[I]);
+          gx[I] += RXV * QFOR; gy[I] += RYV * QFOR; gz[I] += RZV * QFOR;
+        }
+        double AKV = 0.5 * AKC * (4. * ALP2 + RK2) / (ALP2 * RK2);
+        double S2 = SSN * SSN + SCS * SCS;
+        v1 -= RXV * RXV * AKV * S2; v2 -= RYV * RYV * AKV * S2; v3 -= RZV * RZV * AKV * S2;
+      }
+      eacc[4 * tid] = qpe; eacc[4 * tid + 1] = v1; eacc[4 * tid + 2] = v2; eacc[4 * tid + 3] = v3;
+      free(TSIN); free(TCOS);
+    }
+    for (int t = 0; t < nth; ++t) {
+      double *gx = gacc + (size_t)t * 3 * (n + 1), *gy = gx + (n + 1), *gz = gy + (n + 1);
+      for (int I = 1; I <= n; ++I) { st->gx[I] += gx[I]; st->gy[I] += gy[I]; st->gz[I] += gz[I]; }
+      QPE += eacc[4 * t]; vx_ += eacc[4 * t + 1]; vy_ += eacc[4 * t + 2]; vz_ += eacc[4 * t + 3];
+    }
+    s->virx += vx_; s->viry += vy_; s->virz += vz_;
+    free(gacc); free(eacc);
+  }
+  s->virx = s->virx + QPE;
+  s->viry = s->viry + QPE;
+  s->virz = s->virz + QPE;
+  s->pels1 = s->pels1 + QPE;
+  s->qpe = QPE;
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- ETERMS */
+static void eterms_pair(ox_state *st, int ISP, int JSP, int ITYP) {
+  mdx_scalars *s = &st->s;
+  const double ALPHAD = st->p.alphad;
+  double QIJ = st->p.coulf * st->q[ISP] * st->q[JSP];
+  double DX = st->sx[ISP] - st->sx[JSP];
+  double DY = st->sy[ISP] - st->sy[JSP];
+  double DZ = st->sz[ISP] - st->sz[JSP];
+  pbc(st, &DX, &DY, &DZ);
+  double R2 = DX * DX + DY * DY + DZ * DZ;
+  double R2I = 1.0 / R2;
+  double R1 = sqrt(R2);
+  double R1I = R1 * R2I;
+  double ALPHAR = ALPHAD * R1;
+  double TTT = 1.0 / (1.0 + B1 * ALPHAR);
+  double EXP2A = exp(-(ALPHAR * ALPHAR));
+  double ERFC = ((((A5 * TTT + A4) * TTT + A3) * TTT + A2) * TTT + A1) * TTT * EXP2A;
+  double EES = QIJ * (ERFC - 1.0) * R1I;
+  s->spe = s->spe + EES;
+  s->spee[ITYP - 1] = s->spee[ITYP - 1] + EES;
+  if (st->lmove[ITYP]) {
+    double FES = QIJ * ((TOTPI * ALPHAR * EXP2A + ERFC) - 1.0) * R1I * R2I;
+    st->gx[ISP] = st->gx[ISP] + FES * DX;
+    st->gy[ISP] = st->gy[ISP] + FES * DY;
+    st->gz[ISP] = st->gz[ISP] + FES * DZ;
+    st->gx[JSP] = st->gx[JSP] - FES * DX;
+    st->gy[JSP] = st->gy[JSP] - FES * DY;
+    st->gz[JSP] = st->gz[JSP] - FES * DZ;
+    s->virx = s->virx + FES * (DX * DX);
+    s->viry = s->viry + FES * (DY * DY);
+    s->virz = s->virz + FES * (DZ * DZ);
+  }
+}
+
+static void eterms(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  if (st->p.lmnbl) return;
+  for (int I = 1; I <= st->ntypes; ++I) s->spee[I - 1] = st->speei[I];
+  s->spe = st->spei;
+  for (int ISP = 1; ISP <= st->nstot; ++ISP) {
+    int ITYP = st->itype[ISP];
+    if (st->iee[ITYP] != 0) {
+      int NSP = st->nnbb[ISP];
+      for (int J = 1; J <= NSP; ++J) {
+        int JSP = st->inbb[IDX2(ISP, J, st->nstot)];
+        if (JSP <= 0) JSP = -JSP;
+        if (ISP > JSP) eterms_pair(st, ISP, JSP, ITYP);
+      }
+    }
+  }
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+    if (st->iee[ITYP] == 0) {
+      for (int IM = 0; IM <= st->nspec[ITYP] - 1; ++IM) {
+        int NSP = st->nsits[ITYP];
+        int ISPI = st->isaddr[ITYP] + NSP * IM;
+        if (NSP > 1)
+          for (int ISM = 2; ISM <= NSP; ++ISM)
+            for (int JSM = 1; JSM <= ISM - 1; ++JSM)
+              eterms_pair(st, ISPI + ISM, ISPI + JSM, ITYP);
+      }
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- GETBND */
+static void strbnd(ox_state *st, int ITYP);
+
+static void getbnd(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  for (int M = 1; M <= st->nrbb; ++M) {
+    st->br[M] = 0.;
+    st->be[M] = 0.;
+  }
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP)
+    if (st->ipot[ITYP] == 1 || st->ipot[ITYP] == 2) strbnd(st, ITYP);
+  if (st->nrbb <= 0) return;
+  for (int N = 1; N <= st->nrbt; ++N) {
+    int I = st->ibi[N];
+    int ITYP = st->itype[I];
+    int M = st->ibuk[N];
+    int J = st->jbj[N];
+    int NSP = st->nspec[ITYP];
+    double FNSPI = 1.0 / (double)NSP;
+    double REQ = st->rb[M];
+    double BX = st->sx[J] - st->sx[I];
+    double BY = st->sy[J] - st->sy[I];
+    double BZ = st->sz[J] - st->sz[I];
+    pbc(st, &BX, &BY, &BZ);
+    double BSQ = BX * BX + BY * BY + BZ * BZ;
+    double BD = sqrt(BSQ);
+    double R1I = 1.0 / BD;
+    double BBB = BD - REQ;
+    double EBDD, FORB;
+    if (st->id[M] != 1 || BBB > REQ) {
+      double FCN = st->fb[M];
+      double DBND = BBB * FCN;
+      EBDD = DBND * BBB;
+      FORB = -2.0 * DBND * R1I;
+    } else {
+      double DDIS = st->db[M];
+      double ROH = st->ro[M];
+      double EXM = exp(-ROH * BBB);
+      double EXMP = 1 - EXM;
+      EBDD = DDIS * (EXMP * EXMP);
+      FORB = -2.0 * DDIS * ROH * EXM * EXMP * R1I;
+    }
+    st->br[M] = st->br[M] + BD * FNSPI;
+    st->be[M] = st->be[M] + EBDD * FNSPI;
+    s->pint = s->pint + EBDD;
+    if (st->lmove[ITYP]) {
+      st->hx[I] = st->hx[I] - BX * FORB;
+      st->hy[I] = st->hy[I] - BY * FORB;
+      st->hz[I] = st->hz[I] - BZ * FORB;
+      st->hx[J] = st->hx[J] + BX * FORB;
+      st->hy[J] = st->hy[J] + BY * FORB;
+      st->hz[J] = st->hz[J] + BZ * FORB;
+      s->virb = s->virb + FORB * BSQ;
+      s->virfx = s->virfx + FORB * (BX * BX);
+      s->virfy = s->virfy + FORB * (BY * BY);
+      s->virfz = s->virfz + FORB * (BZ * BZ);
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- GETANG */
+static void getang(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  if (st->nraa <= 0) return;
+  for (int M = 1; M <= st->nraa; ++M) {
+    st->ar[M] = 0.;
+    st->ae[M] = 0.;
+  }
+  for (int N = 1; N <= st->nrat; ++N) {
+    int I = st->iai[N];
+    int ITYP = st->itype[I];
+    int J = st->jaj[N];
+    int K = st->kak[N];
+    int M = st->iauk[N];
+    double FCN = st->fa[M];
+    double AEQ = st->ra[M];
+    int NSP = st->nspec[ITYP];
+    double FNSPI = 1.0 / (double)NSP;
+    double AX = st->sx[I] - st->sx[J];
+    double AY = st->sy[I] - st->sy[J];
+    double AZ = st->sz[I] - st->sz[J];
+    pbc(st, &AX, &AY, &AZ);
+    double ASQ = AX * AX + AY * AY + AZ * AZ;
+    double ASQI = 1.0 / ASQ;
+    double BX = st->sx[K] - st->sx[J];
+    double BY = st->sy[K] - st->sy[J];
+    double BZ = st->sz[K] - st->sz[J];
+    pbc(st, &BX, &BY, &BZ);
+    double BSQ = BX * BX + BY * BY + BZ * BZ;
+    double BSQI = 1.0 / BSQ;
+    double AB = sqrt(ASQ * BSQ);
+    double ABI = 1.0 / AB;
+    double COSA = AX * BX + AY * BY + AZ * BZ;
+    COSA = COSA * ABI;
+    COSA = fmin(COSA, 1.0);
+    COSA = fmax(COSA, -1.0);
+    double ALF = acos(COSA);
+    double SINA = sin(ALF);
+    double SINAI = 1.0 / SINA;
+    double DALF = ALF - AEQ;
+    double ABC = DALF * FCN;
+    double EANG = ABC * DALF;
+    st->ar[M] = st->ar[M] + ALF * FNSPI;
+    st->ae[M] = st->ae[M] + EANG * FNSPI;
+    s->pint = s->pint + EANG;
+    if (st->lmove[ITYP]) {
+      double SAB = -2.0 * ABC * SINAI;
+      double CAB = SAB * COSA;
+      double FAB = SAB * ABI;
+      double FAA = CAB * ASQI;
+      double FBB = CAB * BSQI;
+      double FAX = FAB * BX - FAA * AX;
+      double FAY = FAB * BY - FAA * AY;
+      double FAZ = FAB * BZ - FAA * AZ;
+      double FBX = FAB * AX - FBB * BX;
+      double FBY = FAB * AY - FBB * BY;
+      double FBZ = FAB * AZ - FBB * BZ;
+      st->hx[I] = st->hx[I] - FAX;
+      st->hy[I] = st->hy[I] - FAY;
+      st->hz[I] = st->hz[I] - FAZ;
+      st->hx[J] = st->hx[J] + FAX + FBX;
+      st->hy[J] = st->hy[J] + FAY + FBY;
+      st->hz[J] = st->hz[J] + FAZ + FBZ;
+      st->hx[K] = st->hx[K] - FBX;
+      st->hy[K] = st->hy[K] - FBY;
+      st->hz[K] = st->hz[K] - FBZ;
+      s->virfx = s->virfx - AX * FAX - BX * FBX;
+      s->virfy = s->virfy - AY * FAY - BY * FBY;
+      s->virfz = s->virfz - AZ * FAZ - BZ * FBZ;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- GETTRS */
+static void gettrs(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  if (st->nrtt <= 0) return;
+  for (int M = 1; M <= st->nrtt; ++M) {
+    st->tr[M] = 0.;
+    st->te[M] = 0.;
+  }
+  for (int N = 1; N <= st->nrrt; ++N) {
+    int I = st->iti[N], ITYP = st->itype[I];
+    int J = st->jtj[N], K = st->ktk[N], L = st->ltl[N], M = st->ituk[N];
+    int NSP = st->nspec[ITYP];
+    double FNSPI = 1.0 / (double)NSP;
+    double ax = st->sx[J] - st->sx[I], ay = st->sy[J] - st->sy[I], az = st->sz[J] - st->sz[I];
+    double bx = st->sx[K] - st->sx[J], by = st->sy[K] - st->sy[J], bz = st->sz[K] - st->sz[J];
+    double cx = st->sx[L] - st->sx[K], cy = st->sy[L] - st->sy[K], cz = st->sz[L] - st->sz[K];
+    pbc(st, &ax, &ay, &az);
+    pbc(st, &bx, &by, &bz);
+    pbc(st, &cx, &cy, &cz);
+    double ab = ax * bx + ay * by + az * bz;
+    double bc = bx * cx + by * cy + bz * cz;
+    double ac = ax * cx + ay * cy + az * cz;
+    double at = ax * ax + ay * ay + az * az;
+    double bt = bx * bx + by * by + bz * bz;
+    double ct = cx * cx + cy * cy + cz * cz;
+    double axb = (at * bt) - (ab * ab);
+    double bxc = (bt * ct) - (bc * bc);
+    double fnum = (ab * bc) - (ac * bt);
+    double den = axb * bxc;
+    if (!(den > 1.0e-10)) continue;
+    den = sqrt(den);
+    double co = fnum / den;
+    co = fmin(co, 1.0);
+    co = fmax(co, -1.0);
+    double signum = ax * (by * cz - cy * bz) + ay * (bz * cx - cz * bx) + az * (bx * cy - cx * by);
+    double arg = sgn(acos(co), signum);
+    double SIN1F = sin(arg);
+    double si = SIN1F;
+    if (fabs(si) < 1.0e-10) si = sgn(1.0e-10, si);
+    double POTT, DERI;
+    int it = st->itors[M];
+    if (it == 0) {
+      double FCN = st->ft[M], TEQ = st->rt[M];
+      int MUL = st->nmul[M];
+      double EARG = MUL * arg - TEQ;
+      POTT = FCN * (1.0 + cos(EARG));
+      DERI = -FCN * MUL * sin(EARG);
+    } else if (it == 1) {
+      double FN1 = st->ft1[M], FN2 = st->ft2[M], FN3 = st->ft3[M];
+      double COS1F = cos(arg);
+      double COS2F = 2.0 * (COS1F * COS1F) - 1.0;
+      double COS3F = COS1F * (2.0 * COS2F - 1.0);
+      double SIN2F = 2.0 * SIN1F * COS1F;
+      double SIN3F = SIN1F * COS2F + SIN2F * COS1F;
+      POTT = FN1 * (1.0 + COS1F) + FN2 * (1.0 - COS2F) + FN3 * (1.0 + COS3F);
+      DERI = -FN1 * SIN1F + 2.0 * FN2 * SIN2F - 3.0 * FN3 * SIN3F;
+    } else if (it == 5) {
+      double FN0 = st->ft[M], FN1 = st->ft1[M], FN2 = st->ft2[M], FN3 = st->ft3[M],
+             FN4 = st->ft4[M], FN5 = st->ft5[M], TEQ = st->rt[M];
+      double EARG = arg - TEQ;
+      double COSI = cos(EARG);
+      double COSI2 = COSI * COSI, COSI3 = COSI * COSI2, COSI4 = COSI * COSI3, COSI5 = COSI * COSI4;
+      double SINI = sin(EARG);
+      POTT = FN0 + FN1 * COSI + FN2 * COSI2 + FN3 * COSI3 + FN4 * COSI4 + FN5 * COSI5;
+      DERI = -SINI * (FN1 + 2.0 * FN2 * COSI + 3.0 * FN3 * COSI2 + 4.0 * FN4 * COSI3 +
+                      5.0 * FN5 * COSI4);
+    } else if (it == -1) {
+      double FCN = st->ft[M], TEQ = st->rt[M];
+      double EARG = arg - TEQ;
+      POTT = FCN * (EARG * EARG);
+      DERI = 2.0 * FCN * EARG;
+    } else {
+      continue;
+    }
+    st->tr[M] = st->tr[M] + fabs(arg * FNSPI);
+    st->te[M] = st->te[M] + POTT * FNSPI;
+    s->pint = s->pint + POTT;
+    if (st->lmove[ITYP]) {
+      double de1 = DERI / den / si;
+      axb = axb / den * co;
+      bxc = bxc / den * co;
+      double dnum, dden;
+      dnum = cx * bt - bx * bc;
+      dden = (ab * bx - ax * bt) * bxc;
+      double FFI1 = (dnum - dden) * de1;
+      dnum = ((bx - ax) * bc - ab * cx) + (2.0 * ac * bx - cx * bt);
+      dden = axb * (bc * cx - bx * ct) + (ax * bt - at * bx - ab * (bx - ax)) * bxc;
+      double FFJ1 = (dnum - dden) * de1;
+      dnum = ab * bx - ax * bt;
+      dden = axb * (bt * cx - bc * bx);
+      double FFL1 = (dnum - dden) * de1;
+      double FFK1 = -(FFI1 + FFJ1 + FFL1);
+      st->hx[I] += FFI1; st->hx[J] += FFJ1; st->hx[K] += FFK1; st->hx[L] += FFL1;
+      dnum = cy * bt - by * bc;
+      dden = (ab * by - ay * bt) * bxc;
+      double FFI2 = (dnum - dden) * de1;
+      dnum = ((by - ay) * bc - ab * cy) + (2.0 * ac * by - cy * bt);
+      dden = axb * (bc * cy - by * ct) + (ay * bt - at * by - ab * (by - ay)) * bxc;
+      double FFJ2 = (dnum - dden) * de1;
+      dnum = ab * by - ay * bt;
+      dden = axb * (bt * cy - bc * by);
+      double FFL2 = (dnum - dden) * de1;
+      double FFK2 = -(FFI2 + FFJ2 + FFL2);
+      st->hy[I] += FFI2; st->hy[J] += FFJ2; st->hy[K] += FFK2; st->hy[L] += FFL2;
+      dnum = cz * bt - bz * bc;
+      dden = (ab * bz - az * bt) * bxc;
+      double FFI3 = (dnum - dden) * de1;
+      dnum = ((bz - az) * bc - ab * cz) + (2.0 * ac * bz - cz * bt);
+      dden = axb * (bc * cz - bz * ct) + (az * bt - at * bz - ab * (bz - az)) * bxc;
+      double FFJ3 = (dnum - dden) * de1;
+      dnum = ab * bz - az * bt;
+      dden = axb * (bt * cz - bc * bz);
+      double FFL3 = (dnum - dden) * de1;
+      double FFK3 = -(FFI3 + FFJ3 + FFL3);
+      st->hz[I] += FFI3; st->hz[J] += FFJ3; st->hz[K] += FFK3; st->hz[L] += FFL3;
+      s->virfx = s->virfx - (ax + bx) * FFI1 - bx * FFJ1 + cx * FFL1;
+      s->virfy = s->virfy - (ay + by) * FFI2 - by * FFJ2 + cy * FFL2;
+      s->virfz = s->virfz - (az + bz) * FFI3 - bz * FFJ3 + cz * FFL3;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- STRBND */
+static void strbnd(ox_state *st, int ITYP) {
+  mdx_scalars *s = &st->s;
+  const double EEP = -884.63, GGP = 467.31;
+  const double BBMA = (double)1.3f, BBSA = (double)1.4f;
+  int I1 = st->iadb[ITYP], I2 = I1 + 1, I3 = I2 + 1;
+  int NSP = st->nspec[ITYP], NSS = st->nsits[ITYP];
+  double FNSPI = 1.0 / (double)NSP;
+  double ROH1 = st->rb[I1], ROH2 = st->rb[I2], RH1H2 = st->rb[I3];
+  const double FACTOR = st->p.efact; /* 1.D3/AVSNO/UNITE, forces.f:593 */
+  int IPT = st->ipot[ITYP];
+  double AAA, BBB;
+  if (IPT == 2) {
+    AAA = st->db[I1];
+    BBB = st->db[I2];
+  } else {
+    AAA = st->fb[I1];
+    BBB = st->fb[I2];
+  }
+  double CCC = st->fb[I3];
+  double EEE = EEP * FACTOR;
+  double FFF = EEP * FACTOR;
+  double GGG = GGP * FACTOR;
+  double BBM = BBMA, BBS = BBSA;
+  double AADD = AAA * st->ro[I1];
+  double BBDD = BBB * st->ro[I2];
+  int ISHF = st->isaddr[ITYP];
+  int IBB = ISHF + 1, JBB = ISHF + 2, KBB = ISHF + 3;
+  for (int N = 1; N <= NSP; ++N) {
+    int I = (N - 1) * NSS + IBB, J = (N - 1) * NSS + JBB, K = (N - 1) * NSS + KBB;
+    double AX = st->sx[J] - st->sx[I], AY = st->sy[J] - st->sy[I], AZ = st->sz[J] - st->sz[I];
+    double BX = st->sx[K] - st->sx[I], BY = st->sy[K] - st->sy[I], BZ = st->sz[K] - st->sz[I];
+    double CX = st->sx[K] - st->sx[J], CY = st->sy[K] - st->sy[J], CZ = st->sz[K] - st->sz[J];
+    if (IPT == 2) {
+      pbc(st, &AX, &AY, &AZ);
+      pbc(st, &BX, &BY, &BZ);
+      pbc(st, &CX, &CY, &CZ);
+    }
+    double RRA = AX * AX + AY * AY + AZ * AZ;
+    double RRB = BX * BX + BY * BY + BZ * BZ;
+    double RRC = CX * CX + CY * CY + CZ * CZ;
+    double ASS = sqrt(RRA), BSS = sqrt(RRB), CSS = sqrt(RRC);
+    double SA = ASS - ROH1, SB = BSS - ROH2, SH = CSS - RH1H2;
+    double WB1, WB2, WB3, FB3A, FB3B, FB3C;
+    if (IPT == 2) {
+      double EXPA = exp(-st->ro[I1] * SA);
+      double EXPAM = 1.0 - EXPA;
+      double EXPB = exp(-st->ro[I2] * SB);
+      double EXPBM = 1.0 - EXPB;
+      WB1 = AAA * (EXPAM * EXPAM) + EEE * SA * SH;
+      WB2 = BBB * (EXPBM * EXPBM) + FFF * SB * SH;
+      WB3 = CCC * SH * SH + GGG * SA * SB;
+    } else {
+      WB1 = AAA * SA * SA + EEE * SA * SH;
+      WB2 = BBB * SB * SB + FFF * SB * SH;
+      WB3 = CCC * SH * SH + GGG * SA * SB;
+    }
+    st->br[I1] += ASS * FNSPI;
+    st->br[I2] += BSS * FNSPI;
+    st->br[I3] += CSS * FNSPI;
+    st->be[I1] += WB1 * FNSPI;
+    st->be[I2] += WB2 * FNSPI;
+    st->be[I3] += WB3 * FNSPI;
+    s->pint = s->pint + WB1 + WB2 + WB3;
+    if (!st->lmove[ITYP]) continue;
+    if (IPT == 2) {
+      double EXPA = exp(-st->ro[I1] * SA), EXPAM = 1.0 - EXPA;
+      double EXPB = exp(-st->ro[I2] * SB), EXPBM = 1.0 - EXPB;
+      if (ASS > BBM)
+        FB3A = -2. * SA * AADD * st->ro[I1];
+      else
+        FB3A = -2. * AADD * EXPA * EXPAM;
+      FB3A = FB3A - EEE * SH - GGG * SB;
+      if (BSS > BBM)
+        FB3B = -2. * SB * BBDD * st->ro[I1];
+      else
+        FB3B = -2. * BBDD * EXPB * EXPBM;
+      FB3B = FB3B - FFF * SH - GGG * SA;
+      FB3C = -2.0 * CCC * SH - EEE * SA - FFF * SB;
+    } else {
+      FB3A = -2.0 * AAA * SA - EEE * SH - GGG * SB;
+      FB3B = -2.0 * BBB * SB - FFF * SH - GGG * SA;
+      FB3C = -2.0 * CCC * SH - EEE * SA - FFF * SB;
+    }
+    (void)BBS;
+    FB3A = FB3A / ASS;
+    FB3B = FB3B / BSS;
+    FB3C = FB3C / CSS;
+    double AXX = FB3A * AX, AYY = FB3A * AY, AZZ = FB3A * AZ;
+    double BXX = FB3B * BX, BYY = FB3B * BY, BZZ = FB3B * BZ;
+    double CXX = FB3C * CX, CYY = FB3C * CY, CZZ = FB3C * CZ;
+    st->hx[I] = st->hx[I] - AXX - BXX;
+    st->hy[I] = st->hy[I] - AYY - BYY;
+    st->hz[I] = st->hz[I] - AZZ - BZZ;
+    st->hx[J] = st->hx[J] + AXX - CXX;
+    st->hy[J] = st->hy[J] + AYY - CYY;
+    st->hz[J] = st->hz[J] + AZZ - CZZ;
+    st->hx[K] = st->hx[K] + BXX + CXX;
+    st->hy[K] = st->hy[K] + BYY + CYY;
+    st->hz[K] = st->hz[K] + BZZ + CZZ;
+    double VIX = AX * AXX + BX * BXX + CX * CXX;
+    double VIY = AY * AYY + BY * BYY + CY * CYY;
+    double VIZ = AZ * AZZ + BZ * BZZ + CZ * CZZ;
+    s->virb = s->virb + VIX + VIY + VIZ;
+    s->virfx = s->virfx + VIX;
+    s->virfy = s->virfy + VIY;
+    s->virfz = s->virfz + VIZ;
+  }
+}
+
+/* ---------------------------------------------------------------- SCLFRC */
+static void sclfrc(ox_state *st, int nnn) {
+  st->lscfl = 0;
+  if (!st->p.lscft) return;
+  double fct = nnn == 1 ? st->p.ftscl * st->p.ftimes : st->p.ftscl;
+  double *ax = nnn == 1 ? st->hx : nnn == 2 ? st->gx : st->fx;
+  double *ay = nnn == 1 ? st->hy : nnn == 2 ? st->gy : st->fy;
+  double *az = nnn == 1 ? st->hz : nnn == 2 ? st->gz : st->fz;
+  for (int I = 1; I <= st->nstot; ++I) {
+    double f = ax[I] * ax[I] + ay[I] * ay[I] + az[I] * az[I];
+    f = sqrt(f) * fct * st->massdi[I];
+    if (f > 1.0) {
+      if (f > 1.0e20) {
+        ax[I] = 0.; ay[I] = 0.; az[I] = 0.;
+      } else {
+        ax[I] = ax[I] / f; ay[I] = ay[I] / f; az[I] = az[I] / f;
+      }
+      st->lscfl = 1;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- GETCOM */
+int ox_getcom(ox_state *st) {
+  int N = 0, I = 0;
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+    int NSBEG = st->isadr[ITYP] + 1, NSEND = st->isadr[ITYP + 1];
+    double SUMM = st->summas[ITYP];
+    for (int J = 1; J <= st->nspec[ITYP]; ++J) {
+      I = I + 1;
+      st->X[I] = 0.; st->Y[I] = 0.; st->Z[I] = 0.;
+      st->PX[I] = 0.; st->PY[I] = 0.; st->PZ[I] = 0.;
+      for (int IS = NSBEG; IS <= NSEND; ++IS) {
+        N = N + 1;
+        st->X[I] = st->X[I] + st->mass[IS] * st->sx[N];
+        st->Y[I] = st->Y[I] + st->mass[IS] * st->sy[N];
+        st->Z[I] = st->Z[I] + st->mass[IS] * st->sz[N];
+        st->PX[I] = st->PX[I] + st->vx[N];
+        st->PY[I] = st->PY[I] + st->vy[N];
+        st->PZ[I] = st->PZ[I] + st->vz[N];
+      }
+      st->X[I] = st->X[I] / SUMM;
+      st->Y[I] = st->Y[I] / SUMM;
+      st->Z[I] = st->Z[I] / SUMM;
+    }
+  }
+  for (int n = 1; n <= st->nstot; ++n) {
+    int M = st->nnum[n];
+    st->wx[n] = st->sx[n] - st->X[M];
+    st->wy[n] = st->sy[n] - st->Y[M];
+    st->wz[n] = st->sz[n] - st->Z[M];
+  }
+  for (int i = 1; i <= st->nop; ++i) pbc(st, &st->X[i], &st->Y[i], &st->Z[i]);
+  for (int n = 1; n <= st->nstot; ++n) {
+    int M = st->nnum[n];
+    st->sx[n] = st->wx[n] + st->X[M];
+    st->sy[n] = st->wy[n] + st->Y[M];
+    st->sz[n] = st->wz[n] + st->Z[M];
+  }
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- GETEMP */
+static int getemp(ox_state *st) {
+  mdx_thermo *th = &st->th;
+  int nt = st->ntypes;
+  double VIRKX = 0., VIRKY = 0., VIRKZ = 0., VSQ = 0.;
+  double tempr[NT + 5];
+  for (int i = 0; i < NT + 5; ++i) tempr[i] = 0.;
+  for (int I = 1; I <= st->nstot; ++I) {
+    int ITYP = st->itype[I];
+    if (st->lmove[ITYP]) {
+      double VVX = st->massdi[I] * (st->vx[I] * st->vx[I]);
+      double VVY = st->massdi[I] * (st->vy[I] * st->vy[I]);
+      double VVZ = st->massdi[I] * (st->vz[I] * st->vz[I]);
+      double VSC = VVX + VVY + VVZ;
+      VIRKX = VIRKX + VVX;
+      VIRKY = VIRKY + VVY;
+      VIRKZ = VIRKZ + VVZ;
+      VSQ = VSQ + VSC;
+      tempr[ITYP] = tempr[ITYP] + 0.5 * VSC;
+    }
+  }
+  double TEMP = 0.5 * VSQ;
+  int NTYP1 = nt + 1;
+  tempr[NTYP1] = TEMP;
+  tempr[NTYP1 + 1] = VIRKX;
+  tempr[NTYP1 + 2] = VIRKY;
+  tempr[NTYP1 + 3] = VIRKZ;
+  for (int i = 1; i <= NTYP1 + 3; ++i) th->ekin[i - 1] = tempr[i];
+  th->tke = th->ekin[NTYP1 - 1];
+  th->virkx = th->ekin[NTYP1];
+  th->virky = th->ekin[NTYP1 + 1];
+  th->virkz = th->ekin[NTYP1 + 2];
+  for (int i = 1; i <= NTYP1 + 3; ++i) th->tempr[i - 1] = tempr[i];
+  for (int ITYP = 1; ITYP <= nt; ++ITYP)
+    th->tempr[ITYP - 1] = th->ekin[ITYP - 1] * st->p.tfact[ITYP - 1];
+  th->temp = th->tke * st->p.convet;
+  if (st->p.chktf > 0.0 &&
+      (th->temp > st->p.chktf * st->p.trtemp || th->temp <= st->p.trtemp / st->p.chktf)) {
+    snprintf(st->msg, sizeof st->msg, "Temperature control stopped the program: T=%g", th->temp);
+    return MDX_ERR_NAN;
+  }
+  return MDX_OK;
+}
+
+/* ------------------------------------------------------- force collectors */
+int ox_fforces(ox_state *st, int laver, mdx_scalars *out) {
+  (void)laver; /* CM_ADDF only adds to averaging accumulators (L5) */
+  zerofs(st, 1);
+  localf(st);
+  getbnd(st);
+  getang(st);
+  gettrs(st);
+  sclfrc(st, 1);
+  st->s.mbsh = st->mbsh;
+  st->s.mbln = st->mbln;
+  st->s.lscfl = st->lscfl;
+  if (out) *out = st->s;
+  return MDX_OK;
+}
+
+static void cm_addl_wirs(ox_state *st) {
+  for (int N = 1; N <= st->nstot; ++N) {
+    int M = st->nnum[N];
+    st->s.wirs = st->s.wirs - st->gx[N] * (st->sx[N] - st->X[M]) -
+                 st->gy[N] * (st->sy[N] - st->Y[M]) -
+                 st->gz[N] * (st->sz[N] - st->Z[M]);
+  }
+}
+
+int ox_slforces(ox_state *st, mdx_scalars *out) {
+  int rc;
+  zerofs(st, 2);
+  st->s.qpe = 0.;
+  if ((rc = furir(st))) return rc;
+  eterms(st);
+  forces_long(st);
+  cm_addl_wirs(st); /* CM_ADDLF, scalar.f:77-82 */
+  sclfrc(st, 2);
+  st->s.mbsh = st->mbsh;
+  st->s.mbln = st->mbln;
+  st->s.lscfl = st->lscfl;
+  if (out) *out = st->s;
+  return MDX_OK;
+}
+
+int ox_allforce(ox_state *st, mdx_scalars *out) {
+  int rc;
+  zerofs(st, 1);
+  zerofs(st, 2);
+  st->s.qpe = 0.;
+  localf(st);
+  getbnd(st);
+  getang(st);
+  gettrs(st);
+  if ((rc = furir(st))) return rc;
+  eterms(st);
+  forces_long(st);
+  for (int N = 1; N <= st->nstot; ++N) { /* CM_ADDLA, scalar.f:106-113 */
+    st->fx[N] = st->gx[N] + st->hx[N];
+    st->fy[N] = st->gy[N] + st->hy[N];
+    st->fz[N] = st->gz[N] + st->hz[N];
+    int M = st->nnum[N];
+    st->s.wirs = st->s.wirs - st->gx[N] * (st->sx[N] - st->X[M]) -
+                 st->gy[N] * (st->sy[N] - st->Y[M]) -
+                 st->gz[N] * (st->sz[N] - st->Z[M]);
+  }
+  sclfrc(st, 3);
+  st->s.mbsh = st->mbsh;
+  st->s.mbln = st->mbln;
+  st->s.lscfl = st->lscfl;
+  if (out) *out = st->s;
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- SCALING */
+static void scale_v(ox_state *st, double sx_, double sy_, double sz_) {
+  for (int I = 1; I <= st->nstot; ++I)
+    if (st->lmove[st->itype[I]]) {
+      st->vx[I] = st->vx[I] * sx_;
+      st->vy[I] = st->vy[I] * sy_;
+      st->vz[I] = st->vz[I] * sz_;
+    }
+}
+
+static void scale_v_types(ox_state *st, double h) {
+  for (int I = 1; I <= st->nstot; ++I) {
+    int ITYP = st->itype[I];
+    double SCV = 1. - st->th.scm[ITYP - 1] * h;
+    if (st->lmove[ITYP]) {
+      st->vx[I] = st->vx[I] * SCV;
+      st->vy[I] = st->vy[I] * SCV;
+      st->vz[I] = st->vz[I] * SCV;
+    }
+  }
+}
+
+static int npt_guard(ox_state *st, double f) {
+  if (fabs(f) >= 0.1) {
+    st->th.npt_fail += 1;
+    if (st->th.npt_fail > 100) {
+      snprintf(st->msg, sizeof st->msg, "repeated failure of NPT-algorithm");
+      return MDX_ERR_NAN;
+    }
+  }
+  return MDX_OK;
+}
+
+static int scaling(ox_state *st, int IAL) {
+  mdx_thermo *th = &st->th;
+  const mdx_params *p = &st->p;
+  mdx_scalars *s = &st->s;
+  int rc;
+  double DPE[5], DTE[NT + 1];
+  const double TSTEP = p->tstep, HTSTEP = 0.5 * p->tstep;
+  const double FNST = p->fnst;
+  if (IAL == 3 && p->lnvt) {
+    if (p->lsctd) {
+      scale_v_types(st, TSTEP);
+    } else {
+      double SCV = 1. - th->sc * TSTEP;
+      scale_v(st, SCV, SCV, SCV);
+    }
+  }
+  if ((rc = getemp(st))) return rc;
+  double VIRSUM = s->vir1 + s->vir2 + s->virb + s->pels1 + s->pels2 + s->spe + p->vird +
+                  th->vira[0] + th->vira[1] + th->vira[2];
+  double WIRSUM = s->vir1 + s->vir2 + s->pels1 + s->pels2 + s->spe + p->vird + s->wirs + s->wirss;
+  double VOL = st->vol;
+  double TRIDEE = p->tridee_coef / VOL;
+  double TRID = 2. * th->tke * p->unitp / (3. * VOL) - TRIDEE;
+  double TRIDM = p->tridm_coef * th->temp / VOL - TRIDEE;
+  double TRIDX = th->virkx * p->unitp / VOL - TRIDEE / 3.;
+  double TRIDY = th->virky * p->unitp / VOL - TRIDEE / 3.;
+  double TRIDZ = th->virkz * p->unitp / VOL - TRIDEE / 3.;
+  th->tryck = VIRSUM * p->unitp / (3. * VOL) + TRID;
+  th->tryckm = WIRSUM * p->unitp / (3. * VOL) + TRIDM;
+  th->tryckx = (s->virx + s->virfx + p->vird / 3. + th->vira[0]) * p->unitp / VOL + TRIDX;
+  th->trycky = (s->viry + s->virfy + p->vird / 3. + th->vira[1]) * p->unitp / VOL + TRIDY;
+  th->tryckz = (s->virz + s->virfz + p->vird / 3. + th->vira[2]) * p->unitp / VOL + TRIDZ;
+  double DKE = th->temp / p->trtemp - 1.0;
+  for (int I = 1; I <= st->ntypes; ++I) DTE[I] = th->tempr[I - 1] / p->trtemp - 1.0;
+  if (st->lscfl) {
+    for (int I = 1; I <= 4; ++I) DPE[I] = 0.;
+  } else {
+    DPE[1] = p->lshejk ? th->tryckm - p->trpres : th->tryck - p->trpres;
+    DPE[2] = th->tryckx - p->trpresx;
+    DPE[3] = th->trycky - p->trpresy;
+    if (p->lp_xy) {
+      DPE[2] = 0.5 * (DPE[2] + DPE[3]);
+      DPE[3] = DPE[2];
+    }
+    DPE[4] = th->tryckz - p->trpresz;
+  }
+  const double DQT = p->dqt, DQP = p->dqp, RTP = p->rtp;
+  if (IAL == 1) {
+    if (p->lnvt) {
+      if (p->lsctd) {
+        double SCA = 0.;
+        for (int I = 1; I <= st->ntypes; ++I) {
+          th->scm[I - 1] = th->scm[I - 1] + DTE[I] * DQT * HTSTEP;
+          SCA = SCA + th->scm[I - 1] * th->ekin[I - 1];
+        }
+        th->sc = SCA / th->tke;
+      } else {
+        th->sc = th->sc + DKE * DQT * HTSTEP;
+      }
+      if (p->lnpt) {
+        if (p->lsctd) {
+          double SCA = 0.;
+          for (int I = 1; I <= st->ntypes; ++I) {
+            th->scm[I - 1] = th->scm[I - 1] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+            SCA = SCA + th->scm[I - 1] * th->ekin[I - 1];
+          }
+          th->sc = SCA / th->tke;
+        } else {
+          th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+        }
+        if (p->lsep) {
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+          if (p->lp_xy) {
+            th->sclx = 0.5 * (th->sclx + th->scly);
+            th->scly = th->sclx;
+          }
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+          th->scl = th->sclx + th->scly + th->sclz;
+        } else {
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+          th->sclx = th->scl;
+          th->scly = th->scl;
+          th->sclz = th->scl;
+          if ((rc = npt_guard(st, th->scl * HTSTEP))) return rc;
+        }
+        double SCVX = 1. - ((1. - 3. / FNST) * th->sclx + th->sc) * HTSTEP;
+        double SCVY = 1. - ((1. - 3. / FNST) * th->scly + th->sc) * HTSTEP;
+        double SCVZ = 1. - ((1. - 3. / FNST) * th->sclz + th->sc) * HTSTEP;
+        if (p->lp_xy) {
+          SCVX = 0.5 * (SCVX + SCVY);
+          SCVY = SCVX;
+        }
+        double DRCX = TSTEP * th->sclx, DRCY = TSTEP * th->scly, DRCZ = TSTEP * th->sclz;
+        double DRC = (DRCX + DRCY + DRCZ) / 3.;
+        double DRCV = DRC * HTSTEP;
+        DRCX = 1. + DRCX + 0.5 * (DRCX * DRCX);
+        DRCY = 1. + DRCY + 0.5 * (DRCY * DRCY);
+        DRCZ = 1. + DRCZ + 0.5 * (DRCZ * DRCZ);
+        for (int I = 1; I <= st->nstot; ++I) {
+          if (st->lmove[st->itype[I]]) {
+            st->vx[I] = st->vx[I] * SCVX;
+            st->vy[I] = st->vy[I] * SCVY;
+            st->vz[I] = st->vz[I] * SCVZ;
+            st->sx[I] = st->sx[I] * DRCX + st->vx[I] * DRCV * st->massdi[I];
+            st->sy[I] = st->sy[I] * DRCY + st->vy[I] * DRCV * st->massdi[I];
+            st->sz[I] = st->sz[I] * DRCZ + st->vz[I] * DRCV * st->massdi[I];
+          }
+        }
+        reclen(st, DRCX, DRCY, DRCZ);
+      } else {
+        if ((rc = getemp(st))) return rc;
+        if (p->lsctd) {
+          scale_v_types(st, HTSTEP);
+        } else {
+          double SCV = 1. - th->sc * HTSTEP;
+          scale_v(st, SCV, SCV, SCV);
+        }
+      }
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+    }
+  } else if (IAL == 2) {
+    if (p->lnvt) {
+      if (p->lsctd) {
+        scale_v_types(st, HTSTEP);
+      } else {
+        double SCV = 1. - th->sc * HTSTEP;
+        scale_v(st, SCV, SCV, SCV);
+      }
+      if (p->lnpt) {
+        double SCVX = 1. - (1. - 3. / p->fnop) * th->sclx * HTSTEP;
+        double SCVY = 1. - (1. - 3. / p->fnop) * th->scly * HTSTEP;
+        double SCVZ = 1. - (1. - 3. / p->fnop) * th->sclz * HTSTEP;
+        if (p->lp_xy) {
+          SCVX = 0.5 * (SCVX + SCVY);
+          SCVY = SCVX;
+        }
+        scale_v(st, SCVX, SCVY, SCVZ);
+        if ((rc = getemp(st))) return rc;
+        if (p->lsep) {
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+          if (p->lp_xy) {
+            th->sclx = 0.5 * (th->sclx + th->scly);
+            th->scly = th->sclx;
+          }
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+          th->scl = th->sclx + th->scly + th->sclz;
+        } else {
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+          th->sclx = th->scl;
+          th->scly = th->scl;
+          th->sclz = th->scl;
+          if ((rc = npt_guard(st, th->scl * HTSTEP))) return rc;
+        }
+        th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+        if (p->lsctd)
+          for (int I = 1; I <= st->ntypes; ++I)
+            th->scm[I - 1] = th->scm[I - 1] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+      } else {
+        if ((rc = getemp(st))) return rc;
+      }
+      if (p->lsctd) {
+        double SCA = 0.;
+        for (int I = 1; I <= st->ntypes; ++I) {
+          DTE[I] = th->tempr[I - 1] / p->trtemp - 1.0;
+          th->scm[I - 1] = th->scm[I - 1] + DTE[I] * DQT * HTSTEP;
+          SCA = SCA + th->scm[I - 1] * th->ekin[I - 1];
+        }
+        th->sc = SCA / th->tke;
+      } else {
+        DKE = th->temp / p->trtemp - 1.0;
+        th->sc = th->sc + DKE * DQT * HTSTEP;
+      }
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+    }
+  } else if (IAL == 3) {
+    if (p->lnvt) {
+      th->sc = th->sc + DKE * DQT * TSTEP;
+      if (p->lsctd) {
+        double SCA = 0.;
+        for (int I = 1; I <= st->ntypes; ++I) {
+          th->scm[I - 1] = th->scm[I - 1] + DTE[I] * DQT * TSTEP;
+          SCA = SCA + th->scm[I - 1] * th->ekin[I - 1];
+        }
+        th->sc = SCA / th->tke;
+      }
+      if (p->lnpt) {
+        if (p->lsep) {
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * TSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * TSTEP;
+          if (p->lp_xy) {
+            th->sclx = 0.5 * (th->sclx + th->scly);
+            th->scly = th->sclx;
+          }
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * TSTEP;
+          th->scl = th->sclx + th->scly + th->sclz;
+        } else {
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * TSTEP;
+          th->sclx = th->scl;
+          th->scly = th->scl;
+          th->sclz = th->scl;
+          if ((rc = npt_guard(st, th->scl * TSTEP))) return rc;
+        }
+        double SCV = ((1. - 3. / FNST) * th->scl) * TSTEP;
+        double DRCX = TSTEP * th->sclx, DRCY = TSTEP * th->scly, DRCZ = TSTEP * th->sclz;
+        for (int IMOL = 1; IMOL <= st->nop; ++IMOL) {
+          int ITYP = st->itm[IMOL];
+          double SUMM = st->summas[ITYP];
+          if (!st->lmove[ITYP]) continue;
+          double XC = 0., YC = 0., ZC = 0., PXC = 0., PYC = 0., PZC = 0.;
+          int IBEG = st->isaddr[ITYP] + 1 + st->nsits[ITYP] * (IMOL - st->iaddr[ITYP] - 1);
+          int IEND = st->isaddr[ITYP] + st->nsits[ITYP] * (IMOL - st->iaddr[ITYP]);
+          for (int I = IBEG; I <= IEND; ++I) {
+            int IS = st->nsite[I];
+            XC = XC + st->mass[IS] * st->sx[I];
+            YC = YC + st->mass[IS] * st->sy[I];
+            ZC = ZC + st->mass[IS] * st->sz[I];
+            PXC = PXC + st->vx[I];
+            PYC = PYC + st->vy[I];
+            PZC = PZC + st->vz[I];
+          }
+          XC = XC / SUMM;
+          YC = YC / SUMM;
+          ZC = ZC / SUMM;
+          double DVX = PXC * SCV, DVY = PYC * SCV, DVZ = PZC * SCV;
+          double DXC = XC * DRCX, DYC = YC * DRCY, DZC = ZC * DRCZ;
+          for (int I = IBEG; I <= IEND; ++I) {
+            int IS = st->nsite[I];
+            double FAC = st->mass[IS] / SUMM;
+            st->vx[I] = st->vx[I] - DVX * FAC;
+            st->vy[I] = st->vy[I] - DVY * FAC;
+            st->vz[I] = st->vz[I] - DVZ * FAC;
+            st->sx[I] = st->sx[I] + DXC;
+            st->sy[I] = st->sy[I] + DYC;
+            st->sz[I] = st->sz[I] + DZC;
+          }
+        }
+        DRCX = DRCX + 1.;
+        DRCY = DRCY + 1.;
+        DRCZ = DRCZ + 1.;
+        reclen(st, DRCX, DRCY, DRCZ);
+        th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+        if (p->lsctd) {
+          double SCA = 0.;
+          for (int I = 1; I <= st->ntypes; ++I) {
+            th->scm[I - 1] = th->scm[I - 1] + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+            SCA = SCA + th->scm[I - 1] * th->ekin[I - 1];
+          }
+          th->sc = SCA / th->tke;
+        }
+      }
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+    }
+  }
+  if (p->lsclt && (IAL == 2 || IAL == 3)) {
+    if (p->lsctd) {
+      for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+        if (fabs(p->trtemp - th->tempr[ITYP - 1]) > p->tdelt && st->lmove[ITYP]) {
+          double SCV = sqrt(p->trtemp / th->tempr[ITYP - 1]);
+          for (int I = st->isaddr[ITYP] + 1; I <= st->isaddr[ITYP + 1]; ++I) {
+            st->vx[I] = SCV * st->vx[I];
+            st->vy[I] = SCV * st->vy[I];
+            st->vz[I] = SCV * st->vz[I];
+          }
+          th->nscale += 1;
+        }
+      }
+    } else if (fabs(p->trtemp - th->temp) > p->tdelt) {
+      double SCV = sqrt(p->trtemp / th->temp);
+      scale_v(st, SCV, SCV, SCV);
+      th->nscale += 1;
+    }
+    if ((rc = getemp(st))) return rc;
+  }
+  return MDX_OK;
+}
+
+/* ----------------------------------------------------------------- SHEJK */
+static void shejk(ox_state *st, int IMOL, unsigned char *moving,
+                  unsigned char *moved) {
+  mdx_thermo *th = &st->th;
+  int ITYP = st->itm[IMOL];
+  int NRBS = st->nrb[ITYP];
+  if (st->ishejk[ITYP] <= 0 || NRBS <= 0) return;
+  const int MAXIT = st->p.maxit > 0 ? st->p.maxit : 2000;
+  double TOL2 = st->p.toler * st->p.toler;
+  double TSTEP = st->p.tstep;
+  int NBBEG = st->iadb[ITYP];
+  int NBEND = NBBEG + NRBS - 1;
+  int ISHF = st->isaddr[ITYP] + st->nsits[ITYP] * (IMOL - st->iaddr[ITYP] - 1);
+  int ISBEG = ISHF + 1, ISEND = ISHF + st->nsits[ITYP];
+  for (int I = ISBEG; I <= ISEND; ++I) {
+    st->fx[I] = st->sx[I];
+    st->fy[I] = st->sy[I];
+    st->fz[I] = st->sz[I];
+  }
+  for (int M = NBBEG; M <= NBEND; ++M)
+    if (st->id[M] != 2) {
+      int LI = st->ib[M] + ISHF, LJ = st->jb[M] + ISHF;
+      moving[LI] = 0; moved[LI] = 1;
+      moving[LJ] = 0; moved[LJ] = 1;
+    }
+  int ITER = 0, DONE = 0;
+  for (;;) {
+    if (ITER > MAXIT) break;
+    if (DONE) break;
+    DONE = 1;
+    for (int M = NBBEG; M <= NBEND; ++M) {
+      if (st->id[M] == 2) continue;
+      int I = st->ib[M] + ISHF, J = st->jb[M] + ISHF;
+      if (!(moved[I] || moved[J])) continue;
+      double BNDSQ = st->rb[M] * st->rb[M];
+      double BXN = st->sx[I] - st->sx[J];
+      double BYN = st->sy[I] - st->sy[J];
+      double BZN = st->sz[I] - st->sz[J];
+      pbc(st, &BXN, &BYN, &BZN);
+      double BSQ = BXN * BXN + BYN * BYN + BZN * BZN;
+      double DIFFSQ = BNDSQ - BSQ;
+      if (fabs(DIFFSQ) > (BNDSQ * TOL2)) {
+        double DXN = st->ox[I] - st->ox[J];
+        double DYN = st->oy[I] - st->oy[J];
+        double DZN = st->oz[I] - st->oz[J];
+        pbc(st, &DXN, &DYN, &DZN);
+        double VDOT = BXN * DXN + BYN * DYN + BZN * DZN;
+        double RMA = st->massdi[I], RMB = st->massdi[J];
+        double GAB = DIFFSQ / (2.0 * (RMA + RMB) * VDOT);
+        DXN = DXN * GAB;
+        DYN = DYN * GAB;
+        DZN = DZN * GAB;
+        st->sx[I] = st->sx[I] + RMA * DXN;
+        st->sy[I] = st->sy[I] + RMA * DYN;
+        st->sz[I] = st->sz[I] + RMA * DZN;
+        st->sx[J] = st->sx[J] - RMB * DXN;
+        st->sy[J] = st->sy[J] - RMB * DYN;
+        st->sz[J] = st->sz[J] - RMB * DZN;
+        moving[I] = 1;
+        moving[J] = 1;
+        DONE = 0;
+      }
+    }
+    for (int M = NBBEG; M <= NBEND; ++M)
+      if (st->id[M] != 2) {
+        moved[st->ib[M] + ISHF] = 0;
+        moved[st->jb[M] + ISHF] = 0;
+      }
+    for (int M = NBBEG; M <= NBEND; ++M)
+      if (st->id[M] != 2) {
+        int I = st->ib[M] + ISHF, J = st->jb[M] + ISHF;
+        if (moving[I]) moved[I] = 1;
+        if (moving[J]) moved[J] = 1;
+        moving[I] = 0;
+        moving[J] = 0;
+      }
+    ITER = ITER + 1;
+  }
+  if (ITER > th->shake_iter_max) th->shake_iter_max = ITER;
+  if (ITER >= MAXIT) th->shake_fail += 1;
+  for (int I = ISBEG; I <= ISEND; ++I) {
+    double DIX = (st->sx[I] - st->fx[I]) / (st->massdi[I] * TSTEP);
+    double DIY = (st->sy[I] - st->fy[I]) / (st->massdi[I] * TSTEP);
+    double DIZ = (st->sz[I] - st->fz[I]) / (st->massdi[I] * TSTEP);
+    th->viran[0] = th->viran[0] + DIX * st->ox[I] / TSTEP;
+    th->viran[1] = th->viran[1] + DIY * st->oy[I] / TSTEP;
+    th->viran[2] = th->viran[2] + DIZ * st->oz[I] / TSTEP;
+    st->vx[I] = st->vx[I] + DIX;
+    st->vy[I] = st->vy[I] + DIY;
+    st->vz[I] = st->vz[I] + DIZ;
+  }
+}
+
+static void fill_record(ox_state *st, int mstep, mdx_step_record *r) {
+  mdx_scalars *s = &st->s;
+  mdx_thermo *th = &st->th;
+  memset(r, 0, sizeof *r);
+  r->mstep = mstep;
+  r->mbsh = st->mbsh;
+  r->mbln = st->mbln;
+  r->shake_iter = th->shake_iter_max;
+  r->pe1 = s->pe1; r->pels1 = s->pels1; r->pe2 = s->pe2; r->pels2 = s->pels2;
+  r->spe = s->spe; r->pint = s->pint;
+  r->vir1 = s->vir1; r->vir2 = s->vir2; r->virb = s->virb;
+  r->virx = s->virx; r->viry = s->viry; r->virz = s->virz;
+  r->virfx = s->virfx; r->virfy = s->virfy; r->virfz = s->virfz;
+  r->wirs = s->wirs; r->wirss = s->wirss;
+  r->tke = th->tke; r->temp = th->temp; r->sc = th->sc; r->scl = th->scl;
+  r->tryck = th->tryck; r->tryckm = th->tryckm;
+  r->boxl = st->boxl; r->boyl = st->boyl; r->bozl = st->bozl; r->vol = st->vol;
+  r->eabs = th->eabs;
+}
+
+/* ---------------------------------------------------------------- DOUBLE */
+static void kick(ox_state *st, const double *ax, const double *ay,
+                 const double *az, double h) {
+  for (int I = 1; I <= st->nstot; ++I)
+    if (st->lmove[st->itype[I]]) {
+      st->vx[I] = st->vx[I] + h * ax[I];
+      st->vy[I] = st->vy[I] + h * ay[I];
+      st->vz[I] = st->vz[I] + h * az[I];
+    }
+}
+
+int ox_double_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
+                    mdx_step_record *rec) {
+  int rc;
+  const int NFREQ = st->p.nfreq;
+  const int NFREQ2 = NFREQ / 2 + 1;
+  const double HTSTEP = 0.5 * st->p.tstep;
+  const double TSTEB = st->p.tsteb, HTSTEB = 0.5 * st->p.tsteb;
+  for (int NSTEP = 1; NSTEP <= nsteps; ++NSTEP) {
+    int MSTEP = mstep0 + NSTEP;
+    if ((rc = scaling(st, 1))) return rc;
+    kick(st, st->gx, st->gy, st->gz, HTSTEP);
+    int LMEM = 0;
+    for (int NSTEB = 1; NSTEB <= NFREQ; ++NSTEB) {
+      for (int I = 1; I <= st->nstot; ++I)
+        if (st->lmove[st->itype[I]]) {
+          st->vx[I] = st->vx[I] + HTSTEB * st->hx[I];
+          st->vy[I] = st->vy[I] + HTSTEB * st->hy[I];
+          st->vz[I] = st->vz[I] + HTSTEB * st->hz[I];
+          st->sx[I] = st->vx[I] * TSTEB * st->massdi[I] + st->sx[I];
+          st->sy[I] = st->vy[I] * TSTEB * st->massdi[I] + st->sy[I];
+          st->sz[I] = st->vz[I] * TSTEB * st->massdi[I] + st->sz[I];
+        }
+      ox_getcom(st);
+      if (NSTEB == NFREQ2 && MSTEP % st->p.ichnb == 0)
+        if ((rc = ox_chcnb(st, NULL, NULL))) return rc;
+      if (NSTEB == NFREQ) {
+        if ((rc = ox_slforces(st, NULL))) return rc;
+        LMEM = st->lscfl;
+        ox_fforces(st, 1, NULL);
+      } else {
+        ox_fforces(st, 0, NULL);
+      }
+      kick(st, st->hx, st->hy, st->hz, HTSTEB);
+    }
+    if (LMEM) st->lscfl = 1;
+    kick(st, st->gx, st->gy, st->gz, HTSTEP);
+    if ((rc = scaling(st, 2))) return rc;
+    if (rec) fill_record(st, MSTEP, &rec[NSTEP - 1]);
+  }
+  return MDX_OK;
+}
+
+int ox_double(ox_state *st, int32_t nsteps, int32_t nsttot,
+              mdx_step_record *rec) {
+  int rc;
+  st->th.vira[0] = st->th.vira[1] = st->th.vira[2] = 0.;
+  if ((rc = ox_chcnb(st, NULL, NULL))) return rc;
+  ox_getcom(st);
+  if ((rc = ox_slforces(st, NULL))) return rc;
+  ox_fforces(st, 1, NULL);
+  return ox_double_steps(st, nsteps, nsttot, rec);
+}
+
+/* ---------------------------------------------------------------- SULTAN */
+int ox_sultan_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
+                    mdx_step_record *rec) {
+  int rc;
+  const double TSTEP = st->p.tstep;
+  unsigned char *moving = (unsigned char *)xcalloc((size_t)st->nstot + 1, 1);
+  unsigned char *moved = (unsigned char *)xcalloc((size_t)st->nstot + 1, 1);
+  for (int NSTEP = 1; NSTEP <= nsteps; ++NSTEP) {
+    int MSTEP = mstep0 + NSTEP;
+    for (int I = 1; I <= st->nstot; ++I)
+      if (st->lmove[st->itype[I]]) {
+        st->ox[I] = st->sx[I];
+        st->oy[I] = st->sy[I];
+        st->oz[I] = st->sz[I];
+      }
+    for (int I = 1; I <= st->nstot; ++I)
+      if (st->lmove[st->itype[I]]) {
+        st->vx[I] = st->vx[I] + TSTEP * st->fx[I];
+        st->vy[I] = st->vy[I] + TSTEP * st->fy[I];
+        st->vz[I] = st->vz[I] + TSTEP * st->fz[I];
+        st->sx[I] = st->sx[I] + TSTEP * st->vx[I] * st->massdi[I];
+        st->sy[I] = st->sy[I] + TSTEP * st->vy[I] * st->massdi[I];
+        st->sz[I] = st->sz[I] + TSTEP * st->vz[I] * st->massdi[I];
+      }
+    st->th.viran[0] = st->th.viran[1] = st->th.viran[2] = 0.;
+    st->th.shake_iter_max = 0;
+    if (st->p.lshejk)
+      for (int IMOL = 1; IMOL <= st->nop; ++IMOL)
+        if (st->lmove[st->itm[IMOL]]) shejk(st, IMOL, moving, moved);
+    if (MSTEP == 1) {
+      if ((rc = getemp(st))) goto out;
+      double FTMP = sqrt(st->p.trtemp / st->th.temp);
+      for (int N = 1; N <= st->nstot; ++N) {
+        st->vx[N] = st->vx[N] * FTMP;
+        st->vy[N] = st->vy[N] * FTMP;
+        st->vz[N] = st->vz[N] * FTMP;
+      }
+    }
+    for (int k = 0; k < 3; ++k) st->th.vira[k] = st->th.viran[k];
+    if ((rc = scaling(st, 3))) goto out;
+    ox_getcom(st);
+    if (MSTEP % st->p.ichnb == 0)
+      if ((rc = ox_chcnb(st, NULL, NULL))) goto out;
+    if ((rc = ox_allforce(st, NULL))) goto out;
+    if (rec) fill_record(st, MSTEP, &rec[NSTEP - 1]);
+  }
+  rc = MDX_OK;
+out:
+  free(moving);
+  free(moved);
+  return rc;
+}
+
+int ox_sultan(ox_state *st, int32_t nsteps, int32_t nsttot,
+              mdx_step_record *rec) {
+  int rc;
+  if ((rc = ox_chcnb(st, NULL, NULL))) return rc;
+  if ((rc = getemp(st))) return rc;
+  if ((rc = ox_allforce(st, NULL))) return rc;
+  return ox_sultan_steps(st, nsteps, nsttot, rec);
+}
+
+/* ---------------------------------------------------------------- RECINT */
+int ox_set_lambda(ox_state *st, double ec, double pw1, double pw2,
+                  double bee) {
+  int nb = st->nnbt;
+  st->spei = 0.;
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+    double ESCI = st->iee[ITYP] == 0 ? pow(ec, pw1) : 1.0;
+    for (int I = st->isadr[ITYP] + 1; I <= st->isadr[ITYP + 1]; ++I) {
+      int IS = st->inbt[I];
+      for (int JTYP = 1; JTYP <= st->ntypes; ++JTYP) {
+        double ESCL = ESCI;
+        if (st->iee[JTYP] == 0) ESCL = pow(ec, pw1);
+        for (int J = st->isadr[JTYP] + 1; J <= st->isadr[JTYP + 1]; ++J) {
+          int JS = st->inbt[J];
+          st->a6lj[IDX2(IS, JS, nb)] = ESCL * st->a6lj0[IDX2(IS, JS, nb)];
+          st->b12lj[IDX2(IS, JS, nb)] = ESCL * st->b12lj0[IDX2(IS, JS, nb)];
+        }
+      }
+    }
+    for (int ISP = st->isaddr[ITYP] + 1; ISP <= st->isaddr[ITYP + 1]; ++ISP)
+      st->q[ISP] = ESCI * st->charge[st->nsite[ISP]];
+    double SPET = 0.;
+    for (int I = 1; I <= st->nsits[ITYP]; ++I) {
+      int IS = st->isadr[ITYP] + I;
+      double eq = ESCI * st->charge[IS];
+      double QII = st->p.coulf * (eq * eq);
+      SPET = SPET - st->nspec[ITYP] * st->p.alphad * QII / sqrt(PI);
+    }
+    st->speei[ITYP] = SPET;
+    st->spei = st->spei + SPET;
+  }
+  st->p.raex = bee * (1. - pow(ec, pw2));
+  st->p.ec_me = ec;
+  return MDX_OK;
+}

@@ -1,0 +1,234 @@
+"""CPU tests: the oracle against physical invariants and an independent
+numpy restatement of the pair classification; the system builder; the C ABI
+layout and exported symbols (no GPU needed)."""
+import ctypes
+import math
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from mdynamix_gb300 import abi, system as S
+from tests import systems
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def etot(sc):
+    return sc.pe1 + sc.pe2 + sc.pels1 + sc.pels2 + sc.spe + sc.pint
+
+
+# ------------------------------------------------------------- builder ----
+def test_named_workloads_sizes():
+    s1 = S.System(S.spce_nacl_nve())
+    assert s1.nstot == 1544 and abs(s1.boxl - 25.042) < 1e-3
+    assert abs(s1.alphad - 0.28) < 1e-12
+    assert s1.fnst == 3 * 1544 - 3 * 512 - 3
+    s2 = S.System(S.spcfw_water())
+    assert s2.nstot == 98304 and abs(s2.boxl - 99.336) < 1e-3
+    assert abs(s2.alphad - 0.25) < 1e-12
+    assert s2.kvector_count() == 16700
+
+
+def test_units_literals():
+    s = S.System(systems.spcfw())
+    # UNITP carries the REAL*4 literal 1.e-5 of setup.f:103
+    assert s.unitp == s.unite * float(np.float32(1e-5)) / s.unitl ** 3
+    assert abs(s.tstep - 1.0) < 1e-12
+
+
+def test_lj_types_spce():
+    s = S.System(S.spce_nacl_nve())
+    assert s.nnbt == 4 and list(s.inbt) == [1, 2, 2, 3, 4]
+    a6, b12 = S.comb_rules(3.166, 3.166, 0.6507 * s.efact, 0.6507 * s.efact, 16, 16)
+    assert abs(s.a6lj[0, 0] - a6) < 1e-20 and abs(s.b12lj[0, 0] - b12) < 1e-16
+
+
+def test_exclusions_water_and_methanol():
+    s = S.System(systems.organics())
+    # fSPC water: O-H1, O-H2 bonded (1-2), H1-H2 via the H-H bond record
+    assert s.nnbb[0] == 2
+    # methanol has 1-4 pairs (H on C to H on O)
+    off = s.isaddr[1]
+    rows = [s.inbb[:s.nnbb[off + k], off + k] for k in range(6)]
+    assert any((r < 0).any() for r in rows)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/moldb"), reason="reference tree absent")
+def test_moldb_fixture_matches_mmol_files():
+    db = S.load_moldb()
+    for name in ("SPC_E", "SPC-FW", "H2O", "CH3OH", "dmpc"):
+        with open(f"/root/reference/moldb/{name}.mmol", encoding="latin-1") as fh:
+            parsed = S.parse_mmol(fh.read(), name)
+        assert parsed == db[name]
+
+
+# -------------------------------------------------------------- oracle ----
+def brute_lists(s, st):
+    """Independent restatement of CHCNB's pair set with numpy."""
+    x, y, z = st[0], st[1], st[2]
+    n = s.nstot
+    L = np.array([s.boxl, s.boyl, s.bozl])
+    short, long_, s14 = set(), set(), set()
+    excl = {}
+    for i in range(n):
+        excl[i + 1] = {int(v) for v in s.inbb[: s.nnbb[i], i]}
+    for I in range(1, n + 1):
+        J = np.arange(1, n + 1)
+        own = np.where(((I - J) % 2) == 0, J < I, J > I)
+        d = np.stack([x[I - 1] - x, y[I - 1] - y, z[I - 1] - z], axis=1)
+        for k in range(3):
+            m = np.abs(d[:, k]) > L[k] / 2
+            d[m, k] -= np.copysign(L[k], d[m, k])
+        rr = (d ** 2).sum(1)
+        for j in np.nonzero(own)[0]:
+            Jv = j + 1
+            if s.nnum[I - 1] == s.nnum[j] and rr[j] <= 64.0:
+                if Jv in excl[I]:
+                    continue
+                if -Jv in excl[I]:
+                    s14.add((I, Jv))
+                    continue
+            if rr[j] <= s.short2:
+                short.add((max(I, Jv), min(I, Jv)))
+            elif rr[j] <= s.rssq:
+                long_.add((max(I, Jv), min(I, Jv)))
+    return short, long_, s14
+
+
+@pytest.mark.parametrize("spec", [systems.spce_ions(n=64, ions=1), systems.organics(nw=40)])
+def test_oracle_lists_against_numpy(spec):
+    s = S.System(spec)
+    st = S.make_configuration(s, seed=5, jitter=0.05)
+    o = oracle.Oracle(s)
+    o.set_state(*st)
+    (a1, a2), (b1, b2) = o.chcnb_lists()
+    short, long_, s14 = brute_lists(s, st)
+    got_short = {(int(p), int(q)) for p, q in zip(a1, a2) if p > 0}
+    got_14 = {(-int(p), int(q)) for p, q in zip(a1, a2) if p < 0}
+    got_long = {(int(p), int(q)) for p, q in zip(b1, b2)}
+    assert got_short == short and got_long == long_ and got_14 == s14
+
+
+@pytest.mark.parametrize("spec", [systems.spce_ions(n=64, ions=1), systems.organics(nw=40),
+                                  systems.spcfw(n=64, rcut=6.0)])
+def test_oracle_newton_and_finite_difference(spec):
+    s = S.System(spec)
+    st = S.make_configuration(s, seed=3, jitter=0.05)
+    o = oracle.Oracle(s)
+    o.set_state(*st)
+    o.chcnb()
+    o.allforce()
+    F = o.forces(3)
+    assert np.abs(F.sum(0)).max() < 1e-10 * np.abs(F).max() * s.nstot
+    rng = np.random.default_rng(0)
+    fscale = np.sqrt((F ** 2).mean())
+    for _ in range(4):
+        i = int(rng.integers(s.nstot)); k = int(rng.integers(3)); h = 1e-5
+        arr = [st[0].copy(), st[1].copy(), st[2].copy()]
+        arr[k][i] += h
+        o.set_state(*arr, *st[3:]); ep = etot(o.allforce())
+        arr[k][i] -= 2 * h
+        o.set_state(*arr, *st[3:]); em = etot(o.allforce())
+        fd = -(ep - em) / (2 * h)
+        # the A&S erfc of the reference is not the antiderivative of its force
+        # (max error 1.5e-7), hence the 1e-4 bound relative to the force scale
+        assert abs(F[i, k] - fd) < 1e-4 * fscale
+
+
+def test_oracle_ewald_alpha_independence():
+    base = dict(molecules=[("SPC_E", 64), ("Na+", 1), ("Cl-", 1)], density=1.0, rcut=6.0,
+                rshort=5.0, ichnb=5)
+    es = []
+    # converged real space (erfc(A) < 1e-6) and reciprocal space (e^-B < 1e-6)
+    for a, b in ((3.5, 14.0), (4.0, 20.0)):
+        s = S.System(S.RunSpec(alpha=a, fexp=b, **base))
+        st = S.make_configuration(s, seed=9, jitter=0.05)
+        o = oracle.Oracle(s)
+        o.set_state(*st)
+        o.chcnb()
+        sc = o.allforce()
+        es.append(sc.pels1 + sc.pels2 + sc.spe)
+    assert abs(es[0] - es[1]) < 1e-3 * abs(es[0])
+
+
+def test_oracle_nve_conservation_double():
+    """Equilibrate 300 NVT long steps, then 200 NVE steps: the total energy
+    drift stays a small fraction of the kinetic-energy fluctuation."""
+    spec = S.RunSpec(molecules=[("SPC-FW", 64)], density=1.0, dt_fs=2.0, nfreq=10, rcut=6.0,
+                     rshort=5.0, alpha=2.6, fexp=12.0, ichnb=5, nvt=(300.0, 30.0))
+    s = S.System(spec)
+    st = S.make_configuration(s, seed=2, jitter=0.05)
+    o = oracle.Oracle(s)
+    o.set_state(*st)
+    o.double(300)
+    (x, y, z, vx, vy, vz), th = o.get_state()
+    p = o.packed.params
+    p.lnvt = 0
+    o.L.ox_set_params(o.h, p)
+    th.sc = 0.0
+    o.set_state(x, y, z, vx, vy, vz, th)
+    rec = o.double(200, 300)
+    e = np.array([etot_rec(r) for r in rec])
+    ke = np.array([r.tke for r in rec])
+    assert abs(e[-20:].mean() - e[:20].mean()) < 0.15 * ke.std()
+    assert e.std() < 0.3 * ke.std()
+
+
+def etot_rec(r):
+    return r.pe1 + r.pe2 + r.pels1 + r.pels2 + r.spe + r.pint + r.tke
+
+
+def test_oracle_shake_constraints_hold():
+    s = S.System(systems.spce_ions(n=64, ions=1, toler=1e-6))
+    st = S.make_configuration(s, seed=4, jitter=0.05)
+    o = oracle.Oracle(s)
+    o.set_state(*st)
+    o.sultan(5)
+    (x, y, z, *_), th = o.get_state()
+    for m in range(64):
+        i = 3 * m
+        d = math.dist((x[i], y[i], z[i]), (x[i + 1], y[i + 1], z[i + 1]))
+        assert abs(d - 1.0) < 1e-5
+
+
+# ------------------------------------------------------------------ ABI ---
+def test_abi_struct_sizes_match_c():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "mdx_gpu.h"
+int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_topo),
+ sizeof(mdx_params), sizeof(mdx_scalars), sizeof(mdx_thermo), sizeof(mdx_step_record));return 0;}
+'''
+    tmp = os.path.join(ROOT, "_build")
+    os.makedirs(tmp, exist_ok=True)
+    c = os.path.join(tmp, "abi_sizes.c")
+    exe = os.path.join(tmp, "abi_sizes")
+    with open(c, "w") as fh:
+        fh.write(src)
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+    got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
+    want = [ctypes.sizeof(t) for t in (abi.MdxDims, abi.MdxTopo, abi.MdxParams,
+                                       abi.MdxScalars, abi.MdxThermo, abi.MdxStepRecord)]
+    assert got == want
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "mdx_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(mdx_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from mdynamix_gb300.build import LIB, build
+    if not os.path.exists(LIB):
+        build()
+    lib = ctypes.CDLL(LIB)
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    lib.mdx_strerror.restype = ctypes.c_char_p
+    assert lib.mdx_strerror(3) == b"neighbour list overflow"
+    assert lib.mdx_version() >= 1

@@ -1,0 +1,165 @@
+"""GPU path against the CPU oracle, through the C ABI (FP64 and mixed)."""
+import numpy as np
+import pytest
+
+import oracle
+from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+from mdynamix_gb300.mdx import ForcePath, MdxError
+from tests import systems
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10      # relative, forces / energies / virials (FP64 drop-in bar)
+MIXED_TOL = 1e-5      # relative RMS force error of the mixed path
+
+CASES = {
+    "spce_ions": lambda: systems.build(systems.spce_ions()),
+    "spcfw": lambda: systems.build(systems.spcfw()),
+    "organics": lambda: systems.build(systems.organics()),
+}
+
+
+def pair(name, precision=MDX_FP64):
+    s, st = CASES[name]()
+    g = ForcePath(s, precision=precision)
+    o = oracle.Oracle(s)
+    g.set_state(*st)
+    o.set_state(*st)
+    return s, st, g, o
+
+
+def relmax(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_lists_bit_exact(name):
+    s, st, g, o = pair(name)
+    assert g.chcnb() == o.chcnb()
+    (gs1, gs2), (gl1, gl2) = g.lists()
+    o.chcnb_counts = o.chcnb()
+    (os1, os2), (ol1, ol2) = o.lists()
+    assert np.array_equal(gs1, os1) and np.array_equal(gs2, os2)
+    assert np.array_equal(gl1, ol1) and np.array_equal(gl2, ol2)
+    assert (gs1 < 0).sum() == (os1 < 0).sum()
+
+
+SCAL = ["pe1", "pels1", "pe2", "pels2", "spe", "pint", "qpe", "vir1", "vir2", "virb",
+        "virx", "viry", "virz", "virfx", "virfy", "virfz", "wirs", "wirss"]
+
+
+def check_scalars(a, b, names, tol, scale):
+    for n in names:
+        x, y = getattr(a, n), getattr(b, n)
+        assert abs(x - y) <= tol * max(abs(y), scale), (n, x, y)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("routine", ["fforces", "slforces", "allforce"])
+def test_forces_fp64(name, routine):
+    s, st, g, o = pair(name)
+    g.chcnb(); o.chcnb()
+    g.getcom(); o.getcom()
+    a = getattr(g, routine)()
+    b = getattr(o, routine)()
+    which = {"fforces": 1, "slforces": 2, "allforce": 3}[routine]
+    assert relmax(g.forces(which), o.forces(which)) < FP64_TOL
+    scale = max(abs(getattr(b, n)) for n in ("pe1", "pels1", "pe2", "pels2", "pint"))
+    check_scalars(a, b, SCAL, FP64_TOL, 1e-6 * scale)
+    for n in ("pote1", "potl1", "pes141", "psr141", "spee"):
+        x, y = np.array(getattr(a, n)), np.array(getattr(b, n))
+        assert np.abs(x - y).max() <= FP64_TOL * max(np.abs(y).max(), 1e-6 * scale), n
+
+
+@pytest.mark.parametrize("name", ["spcfw", "organics"])
+def test_double_fp64(name):
+    s, st, g, o = pair(name)
+    rg = g.double(3)
+    ro = o.double(3)
+    (gx, gy, gz, vx, vy, vz), tg = g.get_state()
+    (ox, oy, oz, wx, wy, wz), to = o.get_state()
+    dpos = max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max())
+    assert dpos < 1e-9
+    assert relmax(np.stack([vx, vy, vz]), np.stack([wx, wy, wz])) < 1e-8
+    for a, b in zip(rg, ro):
+        for n in ("pe1", "pels1", "pe2", "pels2", "pint", "tke", "temp", "tryck", "sc"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-8 * max(abs(getattr(b, n)), 1e-12), n
+
+
+def test_sultan_shake_fp64():
+    s, st, g, o = pair("spce_ions")
+    rg = g.sultan(3)
+    ro = o.sultan(3)
+    (gx, gy, gz, *_), tg = g.get_state()
+    (ox, oy, oz, *_), to = o.get_state()
+    dpos = max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max())
+    assert dpos < 1e-9
+    for a, b in zip(rg, ro):
+        assert abs(a.temp - b.temp) <= 1e-8 * b.temp
+        assert abs(a.pels1 - b.pels1) <= 1e-8 * abs(b.pels1)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_force_error(name):
+    s, st = CASES[name]()
+    g64 = ForcePath(s, precision=MDX_FP64)
+    g32 = ForcePath(s, precision=MDX_MIXED)
+    for g in (g64, g32):
+        g.set_state(*st)
+        g.chcnb()
+        g.getcom()
+    a = g64.allforce(); b = g32.allforce()
+    for which in (1, 2, 3):
+        f64, f32 = g64.forces(which), g32.forces(which)
+        rms = np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum())
+        assert rms < MIXED_TOL, (which, rms)
+    for n in ("pe1", "pels1", "pe2", "pels2", "pint", "spe"):
+        assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * abs(getattr(a, n)) + 1e-9, n
+
+
+def test_mixed_deterministic():
+    s, st = CASES["spcfw"]()
+    outs = []
+    for _ in range(2):
+        g = ForcePath(s, precision=MDX_MIXED)
+        g.set_state(*st)
+        g.double(2, records=False)
+        (x, y, z, *_), _ = g.get_state()
+        outs.append(np.stack([x, y, z]))
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_list_overflow_is_an_error():
+    s, st = CASES["spcfw"]()
+    g = ForcePath(s, cap_short=4, cap_long=16)
+    g.set_state(*st)
+    with pytest.raises(MdxError) as e:
+        g.chcnb()
+    assert e.value.code == 3 and "overfilled" in str(e.value)
+
+
+def test_call_order_is_an_error():
+    s, st = CASES["spcfw"]()
+    g = ForcePath(s)
+    with pytest.raises(MdxError) as e:
+        g.chcnb()
+    assert e.value.code == 7
+
+
+def test_set_lambda_matches_oracle():
+    s, st = systems.build(systems.__dict__["organics"]().__class__(
+        molecules=[("SPC-FW", 100), ("CH3OH", 1)], density=1.0, dt_fs=2.0, nfreq=10,
+        rcut=7.0, rshort=5.0, alpha=2.0, fexp=9.0, ichnb=10, nvt=(298.0, 30.0),
+        iee_type=2))
+    g = ForcePath(s)
+    o = oracle.Oracle(s)
+    g.packed.params.lmdee = 1
+    o_params = o.packed.params
+    o_params.lmdee = 1
+    g.set_params(g.packed.params)
+    o.L.ox_set_params(o.h, o_params)
+    g.set_state(*st); o.set_state(*st)
+    g.set_lambda(0.5); o.set_lambda(0.5)
+    g.chcnb(); o.chcnb()
+    g.allforce(); o.allforce()
+    assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
