@@ -1,0 +1,324 @@
+"""Benchmark of the MDynaMix step on GB300.
+
+Workload (one GPU): 32,768 flexible SPC-FW waters, 98,304 atoms, cubic box
+99.336 A at 1.0 g/cm3, double time step 0.2/2 fs (NFREQ 10), Nose-Hoover NVT
+300 K, R_cutoff 12 A, R_short 5 A, Ewald alpha 0.25/A with |n| <= 20 per axis
+(16,700 k-vectors), neighbour lists refreshed every 10 long steps, seeded
+jittered lattice start.  A step is one long step (DOUBLE, mdstep.f:324-436).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Our arm: the FP64 drop-in (value) and the mixed-precision path (``mixed``)
+run the same workload; both numbers go on one JSON line with the mixed path's
+force error against FP64.  ``e2e`` drives the C ABI with pinned host buffers:
+every step uploads positions and momenta and downloads them again.
+Reference arm (--impl reference): the CPU restatement of the reference's
+routines (oracle/), all host threads, timed on the same workload.
+Under torchrun each rank runs its own replica (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s mixed vs FP64 on GB300 at ≤1e-5 force err; p50/p99 job latency"
+UNIT = "atom-steps/s"
+WORKLOAD = dict(workload="SPC-FW water 32768 molecules (98304 atoms), DOUBLE 0.2/2 fs, "
+                         "NVT 300 K, Rc 12 A, Ewald alpha 0.25/A |n|<=20",
+                atoms=98304, nkv=16700, nfreq=10, ichnb=10, rcut=12.0, rshort=5.0,
+                l2="working set > L2 (long rows 266 MB, phase tables 98 MB per step)",
+                list_mode="reference (list at Rc, refresh every 10 long steps)")
+
+# Algorithmic work per unit of each kernel group (frozen).
+OPS_PAIR = 80            # per listed pair evaluation
+OPS_EW_SFAC = 11         # per (k, atom) term, structure-factor pass
+OPS_EW_FORCE = 10        # per (k, atom) term, force pass
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "_work", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except OSError:
+            rows = []
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[4 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def make_system():
+    from mdynamix_gb300 import system as S
+    s = S.System(S.spcfw_water())
+    st = S.make_configuration(s, seed=1, jitter=0.05)
+    return s, st
+
+
+def roofline_of(timers, counts, mbsh, mbln, nkv, n, peak64, peak32, mixed):
+    """Dominant kernel group and its achieved throughput against the
+    measured FMA peak of the pipe it is bound by."""
+    ms = {k: v[0] for k, v in timers.items()}
+    top = max(ms, key=ms.get)
+    cnt = max(1, timers[top][1])
+    per_launch_s = ms[top] / cnt * 1e-3
+    work = {"pair_long": OPS_PAIR * mbln, "pair_short": OPS_PAIR * mbsh,
+            "ew_sfac": OPS_EW_SFAC * nkv * n, "ew_force": OPS_EW_FORCE * nkv * n}
+    if top in work:
+        achieved = work[top] / per_launch_s / 1e12
+        peak = peak32 if mixed else peak64
+        return top, {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": None, "kernel": top, "launches": cnt,
+                     "ms_per_launch": per_launch_s * 1e3,
+                     "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak)"}
+    return top, {"bound": "hbm", "achieved": None, "peak": None, "unit": "GB/s", "frac": None,
+                 "traffic": None, "kernel": top}
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    from mdynamix_gb300.mdx import ForcePath, probe_fma_peak
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    s, st = make_system()
+    n = s.nstot
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = ForcePath(s, precision=MDX_FP64 if prec == "fp64" else MDX_MIXED)
+        g.set_state(*st)
+        g.double(0)                       # prologue: CHCNB, GETCOM, SLFORCES, FFORCES
+        g.double_steps(args.warmup, 0, records=False)
+        stream = torch.cuda.ExternalStream(g.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        l0 = g.launches
+        with Clocks(local) as clk:
+            e0.record(stream)
+            g.double_steps(args.steps, args.warmup, records=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        launches = g.launches - l0
+        t = torch.tensor([ms], device="cuda")
+        if dist:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        # instrumented pass: per-group device time (CUDA events on the same stream)
+        g.set_timers(True)
+        g.timers()
+        g.double_steps(args.steps, args.warmup + args.steps, records=False)
+        tm = g.timers()
+        g.set_timers(False)
+        out[prec] = dict(ms=ms, launches=launches, timers=tm, clocks=clk.summary(), ctx=g)
+    # list sizes and force error at the shared start state
+    g64 = ForcePath(s, precision=MDX_FP64)
+    g32 = ForcePath(s, precision=MDX_MIXED)
+    for g in (g64, g32):
+        g.set_state(*st)
+        mbsh, mbln = g.chcnb()
+        g.getcom()
+        g.allforce()
+    f64, f32 = g64.forces(3), g32.forces(3)
+    ferr = float(np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum()))
+    ferr_max = float(np.abs(f32 - f64).max() / np.abs(f64).max())
+    # e2e through the C ABI with pinned host buffers
+    g = out["fp64"]["ctx"]
+    pinned = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(6)]
+    (x, y, z, vx, vy, vz), th = g.get_state()
+    for a, b in zip(pinned, (x, y, z, vx, vy, vz)):
+        a[:] = b
+    ke = max(2, min(args.steps, 10))
+    mstep = 2 * args.steps + args.warmup
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(ke):
+        g.set_state(*pinned, thermo=th)
+        rec = g.double_steps(1, mstep + k, records=True)
+        (xx, yy, zz, uu, vv, ww), th = g.get_state()
+        for a, b in zip(pinned, (xx, yy, zz, uu, vv, ww)):
+            a[:] = b
+    e2e_s = (time.perf_counter() - t0) / ke
+    peak64 = probe_fma_peak(True)
+    peak32 = probe_fma_peak(False)
+    from mdynamix_gb300.abi import MdxStepRecord
+    import ctypes
+    return dict(rec_bytes=ctypes.sizeof(MdxStepRecord), out=out, n=n, mbsh=mbsh, mbln=mbln, ferr=ferr, ferr_max=ferr_max,
+                e2e_s=e2e_s, e2e_steps=ke, peak64=peak64, peak32=peak32, dist=dist,
+                nkv=s.kvector_count())
+
+
+def cpu_baseline(s, st, threads, budget_s=40.0):
+    """The oracle (restated reference routines) on the same workload:
+    one CHCNB and one long step, list build amortised over ICHNB steps."""
+    import oracle
+    o = oracle.Oracle(s, threads=threads)
+    o.set_state(*st)
+    t0 = time.perf_counter(); o.chcnb(); t_list = time.perf_counter() - t0
+    o.getcom(); o.slforces(); o.fforces()
+    t0 = time.perf_counter(); o.double_steps(1, 0); t_step = time.perf_counter() - t0
+    per = t_step + t_list / s.spec.ichnb
+    return {"value": s.nstot / per, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"1 long step ({t_step:.2f} s) + 1 CHCNB ({t_list:.2f} s) / ICHNB "
+                      f"on the full 98304-atom workload, C restatement -O2 OpenMP"}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    s, st = make_system()
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(s, threads=threads)
+    o.set_state(*st)
+    t0 = time.perf_counter(); o.chcnb(); t_list = time.perf_counter() - t0
+    o.getcom(); o.slforces(); o.fforces()
+    w = min(args.warmup, 1)
+    if w:
+        o.double_steps(w, 0)
+    # bounded sample: at most ~3 minutes of timed CPU work
+    t0 = time.perf_counter(); o.double_steps(1, w); t1 = time.perf_counter() - t0
+    k = max(1, min(args.steps - 1, int(150.0 / max(t1, 1e-3))))
+    t0 = time.perf_counter(); o.double_steps(k, w + 1); tk = time.perf_counter() - t0
+    steps = k + 1
+    per = (t1 + tk) / steps + t_list / s.spec.ichnb
+    v = s.nstot / per
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": w, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism="cpu threads"), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{steps} DOUBLE long steps of the full workload + "
+                                       f"CHCNB ({t_list:.1f} s) amortised over ICHNB=10; "
+                                       f"C restatement of the reference routines, OpenMP"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    r = run_gpu(args, rank, world, local)
+    if rank != 0:
+        if r["dist"]:
+            r["dist"].destroy_process_group()
+        return
+    n = r["n"]
+    o64, o32 = r["out"]["fp64"], r["out"]["mixed"]
+    v64 = world * n * args.steps / (o64["ms"] * 1e-3)
+    v32 = world * n * args.steps / (o32["ms"] * 1e-3)
+    top, roof = roofline_of(o64["timers"], None, r["mbsh"], r["mbln"], r["nkv"], n,
+                            r["peak64"], r["peak32"], mixed=False)
+    top32, roof32 = roofline_of(o32["timers"], None, r["mbsh"], r["mbln"], r["nkv"], n,
+                                r["peak64"], r["peak32"], mixed=True)
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        s, st = make_system()
+        cpu = cpu_baseline(s, st, os.cpu_count() or 1)
+    dt_fs = 2.0
+    line = {
+        "metric": METRIC, "value": v64, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": o64["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(WORKLOAD, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "ns_per_day": v64 / n * dt_fs * 1e-6 * 86400,
+        "mixed": {"value": v32, "unit": UNIT, "ms_per_step": o32["ms"] / args.steps,
+                  "dtype": "f32 pair/bonded/Ewald products, i64 fixed-point force sums, "
+                           "f64 S(k)/reductions/update",
+                  "speedup_vs_fp64": v32 / v64, "force_err_rms": r["ferr"],
+                  "force_err_max_rel": r["ferr_max"],
+                  "ns_per_day": v32 / n * dt_fs * 1e-6 * 86400,
+                  "roofline": roof32, "gpu_launches": o32["launches"],
+                  "clocks": o32["clocks"],
+                  "timers_ms": {k: round(v[0] / args.steps, 4) for k, v in o32["timers"].items()}},
+        "roofline": roof,
+        "timers_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in o64["timers"].items()},
+        "e2e": {"value": world * n / r["e2e_s"], "unit": UNIT,
+                "h2d_bytes_per_step": 6 * n * 8,
+                "d2h_bytes_per_step": 6 * n * 8 + r["rec_bytes"],
+                "steps": r["e2e_steps"]},
+        "gpu_launches": o64["launches"],
+        "clocks": o64["clocks"],
+        "cpu_baseline": cpu,
+        "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
+        "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},
+    }
+    print(json.dumps(line), flush=True)
+    if r["dist"]:
+        r["dist"].destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

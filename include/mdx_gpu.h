@@ -266,6 +266,33 @@ void *mdx_stream(mdx_ctx *ctx);
 int64_t mdx_launch_count(const mdx_ctx *ctx);
 int mdx_sync(mdx_ctx *ctx);
 
+/* Per-routine device timers, the GPU counterpart of the reference's CPU time
+ * table (/TIMESZ/ in common_inc.f:102-103, printed by GETAVR, aver.f:284-297).
+ * When on, CUDA events bracket each kernel group on the context's stream;
+ * mdx_get_timers synchronises, returns accumulated milliseconds and launch
+ * counts per group (arrays of MDX_NTIMERS) and clears them. */
+enum {
+  MDX_T_LIST = 0,     /* CHCNB                       (TIMEV) */
+  MDX_T_PAIR_SHORT,   /* LOCALF                      (TIMES) */
+  MDX_T_PAIR_LONG,    /* FORCES                      (TIMEL) */
+  MDX_T_EW_TABLES,    /* FURIR phase tables          (TIMEF) */
+  MDX_T_EW_SFAC,      /* FURIR structure factors     (TIMEF) */
+  MDX_T_EW_KTERMS,    /* FURIR per-k energy/virial   (TIMEF) */
+  MDX_T_EW_FORCE,     /* FURIR forces                (TIMEF) */
+  MDX_T_ETERMS,       /* ETERMS                      (TIMEE) */
+  MDX_T_BONDED,       /* GETBND/GETANG/GETTRS/STRBND (TIMEB..) */
+  MDX_T_MOVE,         /* kicks, drift, GETCOM, SHAKE, SCALING (TIMEG) */
+  MDX_T_OTHER,        /* zeroing, fixed-point folds, reductions */
+  MDX_NTIMERS
+};
+int mdx_set_timers(mdx_ctx *ctx, int on);
+int mdx_get_timers(mdx_ctx *ctx, double *ms, int64_t *count);
+
+/* Measured CUDA-core FMA throughput of the current device in TFLOP/s
+ * (fp64 != 0: FP64, else FP32); a roofline denominator, not a routine of the
+ * reference. */
+int mdx_probe_fma_peak(int fp64, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -431,6 +431,7 @@ __global__ void k_strbnd(WaterPar w, const dbl4 *__restrict__ pos, double bxl,
 }  // namespace
 
 int launch_bonded(mdx_ctx *ctx, int laver) {
+  MDX_TIMER(ctx, MDX_T_BONDED);
   DevData &d = ctx->dv;
   mdx_scalars *sc = d.sc;
   const bool mx = ctx->mixed();

@@ -512,12 +512,17 @@ int launch_furir(mdx_ctx *ctx) {
   const double cfur = 4.0 * PI_REF * ctx->p.coulf / vol;
   const Chunk *chunks = reinterpret_cast<const Chunk *>(d.kchunks);
   const int nchunk = d.nchunk;
-  k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
-      d.n, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
-      d.tabxf, d.tabyf, d.tabzf);
-  MDX_LAUNCHED(ctx);
+  {
+    MDX_TIMER(ctx, MDX_T_EW_TABLES);
+    k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
+        d.n, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
+        d.tabxf, d.tabyf, d.tabzf);
+    MDX_LAUNCHED(ctx);
+  }
   MDX_CUDA(cudaMemsetAsync(d.sk, 0, sizeof(double2) * d.nkv, ctx->stream));
   dim3 grid((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
+  {
+  MDX_TIMER(ctx, MDX_T_EW_SFAC);
   if (ctx->mixed()) {
     size_t sh = sizeof(float2) * TILE * (d.kx + d.ky + d.kz);
     k_sfac<float, float2><<<grid, 128, sh, ctx->stream>>>(
@@ -528,14 +533,19 @@ int launch_furir(mdx_ctx *ctx) {
         d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk);
   }
   MDX_LAUNCHED(ctx);
+  }
   double *qpe = d.red + 40;
   mdx_scalars *sc = d.sc;
   Dst6 dst{{qpe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
+  {
+  MDX_TIMER(ctx, MDX_T_EW_KTERMS);
   k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
       d.ncol, d.cols, d.sk, ibx, iby, ibz, alp2, cfur, d.wk, d.wkz, dst);
   MDX_LAUNCHED(ctx);
   k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
   MDX_LAUNCHED(ctx);
+  }
+  MDX_TIMER(ctx, MDX_T_EW_FORCE);
   if (ctx->mixed()) {
     k_rforce32<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
         d.n, d.ncol, d.cols, d.wk, d.wkz, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky,
@@ -550,6 +560,7 @@ int launch_furir(mdx_ctx *ctx) {
 }
 
 int launch_eterms(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_ETERMS);
   DevData &d = ctx->dv;
   if (ctx->p.lmnbl) return MDX_OK;
   SelfEnergy se;

@@ -814,6 +814,7 @@ int launch_getemp(mdx_ctx *ctx);
 
 // Scratch of the SCALING stages lives at a fixed place of the context.
 static ScalScratch *scratch(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   return reinterpret_cast<ScalScratch *>(ctx->dv.scal_scratch);
 }
 
@@ -871,6 +872,7 @@ static int scale_atoms(mdx_ctx *ctx, int mode) {
 // (same operation order as the reference: V*SCV, then V + HTSTEP*G);
 // *pending_vscale tells the caller.
 int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   const mdx_params &p = ctx->p;
   if (pending_vscale) *pending_vscale = false;
   if (ial == 3 && p.lnvt) {
@@ -930,12 +932,14 @@ int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
 }
 
 int launch_mstep1_rescale(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   RC(launch_getemp(ctx));
   RC(stage(ctx, ST_MSTEP1));
   return scale_atoms(ctx, 1);
 }
 
 int launch_zero_fast(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   k_zero_scalars<<<1, 64, 0, ctx->stream>>>(d.sc, 1, ctx->p.molint, ctx->d.ntypes);
   MDX_LAUNCHED(ctx);
@@ -948,6 +952,7 @@ int launch_zero_fast(mdx_ctx *ctx) {
 }
 
 int launch_zero_slow(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   k_zero_scalars<<<1, 64, 0, ctx->stream>>>(d.sc, 2, ctx->p.molint, ctx->d.ntypes);
   MDX_LAUNCHED(ctx);
@@ -960,6 +965,7 @@ int launch_zero_slow(mdx_ctx *ctx) {
 }
 
 int launch_fix_to_double(mdx_ctx *ctx, int which) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   const unsigned long long *f = which == 1 ? d.hfix : d.gfix;
   double *x = which == 1 ? d.hx : d.gx, *y = which == 1 ? d.hy : d.gy,
@@ -970,6 +976,7 @@ int launch_fix_to_double(mdx_ctx *ctx, int which) {
 }
 
 int launch_sclfrc(mdx_ctx *ctx, int nnn) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   if (!ctx->p.lscft) return MDX_OK;
   DevData &d = ctx->dv;
   const double fct = nnn == 1 ? ctx->p.ftscl * ctx->p.ftimes : ctx->p.ftscl;
@@ -982,6 +989,7 @@ int launch_sclfrc(mdx_ctx *ctx, int nnn) {
 }
 
 int launch_sum_forces(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   k_sum_forces<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.gx, d.gy, d.gz, d.hx,
                                                            d.hy, d.hz, d.fx, d.fy, d.fz);
@@ -990,6 +998,7 @@ int launch_sum_forces(mdx_ctx *ctx) {
 }
 
 int launch_getcom(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   DevData &d = ctx->dv;
   k_getcom<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z,
@@ -999,6 +1008,7 @@ int launch_getcom(mdx_ctx *ctx) {
 }
 
 int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   DevData &d = ctx->dv;
   const double *x = which == 1 ? d.hx : which == 2 ? d.gx : d.fx;
   const double *y = which == 1 ? d.hy : which == 2 ? d.gy : d.fy;
@@ -1011,6 +1021,7 @@ int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale) {
 }
 
 int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   DevData &d = ctx->dv;
   k_kick_drift<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.ainfo, move_const(ctx), htsteb, tsteb, prev, d.hx, d.hy, d.hz, d.massdi,
@@ -1020,6 +1031,7 @@ int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev) {
 }
 
 int launch_leapfrog_shake(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
   DevData &d = ctx->dv;
   k_leapfrog<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.ainfo, move_const(ctx), ctx->p.tstep, d.fx, d.fy, d.fz, d.massdi, d.vx,
@@ -1047,6 +1059,7 @@ int launch_leapfrog_shake(mdx_ctx *ctx) {
 }
 
 int launch_vira(mdx_ctx *ctx, int from_viran) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   if (from_viran)
     k_vira_from_viran<<<1, 1, 0, ctx->stream>>>(ctx->dv.th);
   else
@@ -1056,6 +1069,7 @@ int launch_vira(mdx_ctx *ctx, int from_viran) {
 }
 
 int launch_record(mdx_ctx *ctx, int slot, int mstep) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   k_record<<<1, 1, 0, ctx->stream>>>(ctx->dv.rec, slot, mstep, ctx->dv.sc, ctx->dv.th);
   MDX_LAUNCHED(ctx);
   return MDX_OK;

@@ -442,6 +442,12 @@ int mdx_close(mdx_ctx *ctx) {
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &sp : ctx->spans) {
+    cudaEventDestroy(sp.a);
+    cudaEventDestroy(sp.b);
+  }
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MDX_OK;
@@ -721,8 +727,9 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
   ctx->launches++;
   RC(launch_mirror_f32(ctx));
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  // lists and forces persist, as the reference's COMMON blocks do, until the
+  // caller asks for CHCNB / the force routines again
   ctx->have_state = true;
-  ctx->have_lists = false;
   return MDX_OK;
 }
 
@@ -936,6 +943,33 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
     ctx->launches++;
     cudaStreamSynchronize(ctx->stream);
     cudaFree(dq);
+  }
+  return MDX_OK;
+}
+
+int mdx_set_timers(mdx_ctx *ctx, int on) {
+  if (!ctx) return MDX_ERR_ARG;
+  ctx->timing = on != 0;
+  return MDX_OK;
+}
+
+int mdx_get_timers(mdx_ctx *ctx, double *ms, int64_t *count) {
+  if (!ctx) return MDX_ERR_ARG;
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (auto &sp : ctx->spans) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, sp.a, sp.b);
+    ctx->t_ms[sp.id] += t;
+    ctx->t_cnt[sp.id] += 1;
+    ctx->ev_pool.push_back(sp.a);
+    ctx->ev_pool.push_back(sp.b);
+  }
+  ctx->spans.clear();
+  for (int k = 0; k < MDX_NTIMERS; ++k) {
+    if (ms) ms[k] = ctx->t_ms[k];
+    if (count) count[k] = ctx->t_cnt[k];
+    ctx->t_ms[k] = 0.0;
+    ctx->t_cnt[k] = 0;
   }
   return MDX_OK;
 }

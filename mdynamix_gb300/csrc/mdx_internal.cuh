@@ -177,8 +177,49 @@ struct mdx_ctx {
   double list_rl2 = 0;  // squared list radius used by the last build
   FixScale fix{};
   int mbsh = 0, mbln = 0;
+  // device timers (mdx_set_timers)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Span {
+    int id;
+    cudaEvent_t a, b;
+  };
+  std::vector<Span> spans;
+  double t_ms[MDX_NTIMERS]{};
+  int64_t t_cnt[MDX_NTIMERS]{};
   bool mixed() const { return d.precision == MDX_MIXED; }
+  cudaEvent_t take_event() {
+    if (ev_pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = ev_pool.back();
+    ev_pool.pop_back();
+    return e;
+  }
 };
+
+// Brackets the launches of one scope with CUDA events when timers are on.
+struct TimerScope {
+  mdx_ctx *ctx;
+  int id;
+  cudaEvent_t a = nullptr;
+  TimerScope(mdx_ctx *c, int i) : ctx(c), id(i) {
+    if (ctx->timing) {
+      a = ctx->take_event();
+      cudaEventRecord(a, ctx->stream);
+    }
+  }
+  ~TimerScope() {
+    if (ctx->timing && a) {
+      cudaEvent_t b = ctx->take_event();
+      cudaEventRecord(b, ctx->stream);
+      ctx->spans.push_back({id, a, b});
+    }
+  }
+};
+#define MDX_TIMER(ctx, id) TimerScope mdx_timer_scope_(ctx, id)
 
 // --------------------------------------------------------------- helpers --
 #define MDX_CUDA(call)                                                      \

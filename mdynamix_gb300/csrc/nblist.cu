@@ -272,6 +272,7 @@ __global__ void k_halve_counts(mdx_scalars *sc) {
 }  // namespace
 
 int launch_mirror_f32(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   k_mirror<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, 1.0 / ctx->boxl,
@@ -281,6 +282,7 @@ int launch_mirror_f32(mdx_ctx *ctx) {
 }
 
 int launch_build_lists(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_LIST);
   DevData &d = ctx->dv;
   const double rl = ctx->p.rcut + ctx->p.rskin;
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,

@@ -526,10 +526,13 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
 
 }  // namespace
 
-int launch_localf(mdx_ctx *ctx, bool split) { return launch_pair(ctx, true, split); }
-int launch_forces_long(mdx_ctx *ctx, bool split) { return launch_pair(ctx, false, split); }
+int launch_localf(mdx_ctx *ctx, bool split) {
+  MDX_TIMER(ctx, MDX_T_PAIR_SHORT); return launch_pair(ctx, true, split); }
+int launch_forces_long(mdx_ctx *ctx, bool split) {
+  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair(ctx, false, split); }
 
 int launch_wir(mdx_ctx *ctx, int which) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   double *dst = which == 1 ? &d.sc->wirss : &d.sc->wirs;
   const double *fx = which == 1 ? d.hx : d.gx, *fy = which == 1 ? d.hy : d.gy,

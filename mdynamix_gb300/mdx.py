@@ -31,6 +31,19 @@ LIB_PATH = os.path.join(HERE, "_lib", "libmdxgpu.so")
 
 _lib = None
 
+TIMER_NAMES = ["list", "pair_short", "pair_long", "ew_tables", "ew_sfac", "ew_kterms",
+               "ew_force", "eterms", "bonded", "move", "other"]
+
+
+def probe_fma_peak(fp64: bool) -> float:
+    """Measured FMA throughput (TFLOP/s) of the current GPU."""
+    L = load()
+    v = C.c_double()
+    rc = L.mdx_probe_fma_peak(int(fp64), C.byref(v))
+    if rc != 0:
+        raise MdxError(rc, "probe failed")
+    return v.value
+
 
 class MdxError(RuntimeError):
     def __init__(self, code: int, msg: str):
@@ -74,6 +87,9 @@ def load():
     L.mdx_launch_count.restype = C.c_int64
     L.mdx_sync.argtypes = [P]
     L.mdx_version.restype = C.c_int
+    L.mdx_set_timers.argtypes = [P, C.c_int]
+    L.mdx_get_timers.argtypes = [P, F64P, C.POINTER(C.c_int64)]
+    L.mdx_probe_fma_peak.argtypes = [C.c_int, F64P]
     _lib = L
     return L
 
@@ -124,6 +140,18 @@ class ForcePath:
 
     def sync(self):
         self._check(self.L.mdx_sync(self.h))
+
+    def set_timers(self, on: bool = True):
+        self._check(self.L.mdx_set_timers(self.h, int(on)))
+
+    def timers(self) -> dict:
+        """Accumulated device milliseconds and launch counts per routine group
+        since the last call (the GPU counterpart of the reference's CPU time
+        table); clears them."""
+        ms = np.zeros(len(TIMER_NAMES))
+        cnt = np.zeros(len(TIMER_NAMES), dtype=np.int64)
+        self._check(self.L.mdx_get_timers(self.h, _fp(ms), cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        return {n: (float(ms[i]), int(cnt[i])) for i, n in enumerate(TIMER_NAMES)}
 
     # ---------------------------------------------------------------- data
     def set_params(self, params: MdxParams):

@@ -691,10 +691,10 @@ static inline void pair_params(const ox_state *st, int ISP0, int ISP, int JSP,
 }
 
 /* --------------------------------------------------------------- LOCALF */
-static void localf(ox_state *st) {
-  mdx_scalars *s = &st->s;
+static void localf_range(ox_state *st, mdx_scalars *s, double *hx, double *hy,
+                         double *hz, int i0, int i1) {
   const double ALPHAD = st->p.alphad;
-  for (int INP = 1; INP <= st->mbsh; ++INP) {
+  for (int INP = i0; INP <= i1; ++INP) {
     int ISP0 = st->nbs1[INP];
     int ISP = abs(ISP0);
     int JSP = st->nbs2[INP];
@@ -760,16 +760,64 @@ static void localf(ox_state *st) {
       }
       s->pe2 = s->pe2 + ESR;
     }
-    st->hx[ISP] = st->hx[ISP] + FORCE * DX;
-    st->hy[ISP] = st->hy[ISP] + FORCE * DY;
-    st->hz[ISP] = st->hz[ISP] + FORCE * DZ;
-    st->hx[JSP] = st->hx[JSP] - FORCE * DX;
-    st->hy[JSP] = st->hy[JSP] - FORCE * DY;
-    st->hz[JSP] = st->hz[JSP] - FORCE * DZ;
+    hx[ISP] = hx[ISP] + FORCE * DX;
+    hy[ISP] = hy[ISP] + FORCE * DY;
+    hz[ISP] = hz[ISP] + FORCE * DZ;
+    hx[JSP] = hx[JSP] - FORCE * DX;
+    hy[JSP] = hy[JSP] - FORCE * DY;
+    hz[JSP] = hz[JSP] - FORCE * DZ;
     s->virfx = s->virfx + FORCE * (DX * DX);
     s->virfy = s->virfy + FORCE * (DY * DY);
     s->virfz = s->virfz + FORCE * (DZ * DZ);
   }
+}
+
+/* Sum of thread-private accumulators of a parallel pair sweep (CPU baseline
+ * runs only; the checker runs single-threaded in the reference's order). */
+static void add_scalars(mdx_scalars *d, const mdx_scalars *a) {
+  d->pe1 += a->pe1; d->pels1 += a->pels1; d->pe2 += a->pe2; d->pels2 += a->pels2;
+  d->vir1 += a->vir1; d->vir2 += a->vir2;
+  d->virx += a->virx; d->viry += a->viry; d->virz += a->virz;
+  d->virfx += a->virfx; d->virfy += a->virfy; d->virfz += a->virfz;
+  for (int k = 0; k < MDX_NTPP; ++k) { d->pote1[k] += a->pote1[k]; d->potl1[k] += a->potl1[k]; }
+  for (int k = 0; k < MDX_NTPS; ++k) { d->pes141[k] += a->pes141[k]; d->psr141[k] += a->psr141[k]; }
+}
+
+typedef void (*pair_range_fn)(ox_state *, mdx_scalars *, double *, double *,
+                              double *, int, int);
+
+static void pair_sweep(ox_state *st, pair_range_fn fn, int npairs, double *fx,
+                       double *fy, double *fz) {
+  const int nth = st->nthreads;
+  if (nth <= 1 || npairs < 10000) {
+    fn(st, &st->s, fx, fy, fz, 1, npairs);
+    return;
+  }
+  const int n = st->nstot;
+  double *buf = (double *)xcalloc((size_t)nth * 3 * (n + 1), sizeof(double));
+  mdx_scalars *ss = (mdx_scalars *)xcalloc((size_t)nth, sizeof(mdx_scalars));
+#pragma omp parallel num_threads(nth)
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    int i0 = 1 + (int)((long)npairs * t / nth), i1 = (int)((long)npairs * (t + 1) / nth);
+    double *bx = buf + (size_t)t * 3 * (n + 1);
+    fn(st, &ss[t], bx, bx + (n + 1), bx + 2 * (n + 1), i0, i1);
+  }
+  for (int t = 0; t < nth; ++t) {
+    double *bx = buf + (size_t)t * 3 * (n + 1), *by = bx + (n + 1), *bz = by + (n + 1);
+    for (int i = 1; i <= n; ++i) { fx[i] += bx[i]; fy[i] += by[i]; fz[i] += bz[i]; }
+    add_scalars(&st->s, &ss[t]);
+  }
+  free(buf);
+  free(ss);
+}
+
+static void localf(ox_state *st) {
+  mdx_scalars *s = &st->s;
+  pair_sweep(st, localf_range, st->mbsh, st->hx, st->hy, st->hz);
   for (int N = 1; N <= st->nstot; ++N) {
     int M = st->nnum[N];
     s->wirss = s->wirss - st->hx[N] * (st->sx[N] - st->X[M]) -
@@ -779,10 +827,10 @@ static void localf(ox_state *st) {
 }
 
 /* --------------------------------------------------------------- FORCES */
-static void forces_long(ox_state *st) {
-  mdx_scalars *s = &st->s;
+static void forces_range(ox_state *st, mdx_scalars *s, double *gx, double *gy,
+                         double *gz, int i0, int i1) {
   const double ALPHAD = st->p.alphad;
-  for (int INP = 1; INP <= st->mbln; ++INP) {
+  for (int INP = i0; INP <= i1; ++INP) {
     int ISP0 = st->nbl1[INP];
     int JSP = st->nbl2[INP];
     int ISP = abs(ISP0);
@@ -848,13 +896,17 @@ static void forces_long(ox_state *st) {
       s->viry = s->viry + FORCE * (DY * DY);
       s->virz = s->virz + FORCE * (DZ * DZ);
     }
-    st->gx[ISP] = st->gx[ISP] + FORCE * DX;
-    st->gy[ISP] = st->gy[ISP] + FORCE * DY;
-    st->gz[ISP] = st->gz[ISP] + FORCE * DZ;
-    st->gx[JSP] = st->gx[JSP] - FORCE * DX;
-    st->gy[JSP] = st->gy[JSP] - FORCE * DY;
-    st->gz[JSP] = st->gz[JSP] - FORCE * DZ;
+    gx[ISP] = gx[ISP] + FORCE * DX;
+    gy[ISP] = gy[ISP] + FORCE * DY;
+    gz[ISP] = gz[ISP] + FORCE * DZ;
+    gx[JSP] = gx[JSP] - FORCE * DX;
+    gy[JSP] = gy[JSP] - FORCE * DY;
+    gz[JSP] = gz[JSP] - FORCE * DZ;
   }
+}
+
+static void forces_long(ox_state *st) {
+  pair_sweep(st, forces_range, st->mbln, st->gx, st->gy, st->gz);
 }
 
 /* ---------------------------------------------------------------- INIFUR */
