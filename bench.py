@@ -144,6 +144,13 @@ def run_gpu(args, rank, world, local):
     s, st = make_system()
     n = s.nstot
     out = {}
+    if args.only:
+        g = ForcePath(s, precision=MDX_FP64 if args.only == "fp64" else MDX_MIXED)
+        g.set_state(*st)
+        g.double(0)
+        g.double_steps(args.warmup + args.steps, 0, records=False)
+        g.sync()
+        return None
     for prec in ("fp64", "mixed"):
         g = ForcePath(s, precision=MDX_FP64 if prec == "fp64" else MDX_MIXED)
         g.set_state(*st)
@@ -264,6 +271,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
+                    help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = env_rank()
@@ -271,6 +280,8 @@ def main():
         reference_arm(args, rank, world)
         return
     r = run_gpu(args, rank, world, local)
+    if r is None:
+        return
     if rank != 0:
         if r["dist"]:
             r["dist"].destroy_process_group()

@@ -12,13 +12,18 @@
 //   F_j    = sum_c [RXV_c, RYV_c] Im(T_j(c) U_j(c)),  Fz = Im(T_j(c) V_j(c))
 //   U_j(c) = sum_{nz} W_k Z_j(nz), V_j(c) = sum_{nz} RZV_k W_k Z_j(nz),
 //   W_k    = 2 AKC_k conj(S_k)
-// so each (k, atom) term costs one complex multiply-add per pass and no
-// transcendental.  Mathematically this is the reference's sum; in FP64 the
-// difference is rounding (recurrence error ~ |n| ulp).
+// so each (k, atom) term costs one complex multiply-add per pass (4 fused
+// multiply-adds) and no transcendental.  Mathematically this is the
+// reference's sum; in FP64 the difference is rounding (the recurrence adds
+// about |n| ulp).
+//
+// Tables are stored n-major (tab[n * N + atom]) so that a warp of atoms
+// reads one coalesced row per n.
 //
 // Mixed path: tables rounded to FP32 after an FP64 recurrence, products and
-// the per-slice sums in FP32, S(k) accumulated across slices in FP64, forces
-// accumulated per column in 64-bit fixed point.
+// the per-slice sums in FP32, S(k) accumulated across slices in FP64, W in
+// FP32 for the force pass, forces accumulated per column in 64-bit fixed
+// point.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -36,59 +41,52 @@ struct Chunk {
   int col, nz0, len, k0;
 };
 
-// complex helpers
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
-__device__ __forceinline__ double2 tab_get(const double2 *t, int n) {
-  double2 v = t[n < 0 ? -n : n];
-  if (n < 0) v.y = -v.y;
-  return v;
-}
-__device__ __forceinline__ float2 tab_getf(const float2 *t, int n) {
-  float2 v = t[n < 0 ? -n : n];
-  if (n < 0) v.y = -v.y;
+template <typename C2>
+__device__ __forceinline__ C2 conj_if(C2 v, bool neg) {
+  if (neg) v.y = -v.y;
   return v;
 }
 
-// Phase tables: thread per (atom, axis), FP64 recurrence from one sincos.
+// Phase tables: thread per (axis, atom), FP64 recurrence from one sincos.
 __global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
                          double iby, double ibz, int kx, int ky, int kz,
                          double2 *__restrict__ tx, double2 *__restrict__ ty,
                          double2 *__restrict__ tz, float2 *__restrict__ txf,
                          float2 *__restrict__ tyf, float2 *__restrict__ tzf) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 3 * n) return;
-  int i = t / 3, a = t - 3 * i;
-  dbl4 p = pos[i];
-  double x = a == 0 ? p.x * ibx : a == 1 ? p.y * iby : p.z * ibz;
-  double th = 2.0 * PI_REF * x;
+  const int a = t / n, i = t - a * n;
+  const dbl4 p = pos[i];
+  const double x = a == 0 ? p.x * ibx : a == 1 ? p.y * iby : p.z * ibz;
   double s, c;
-  sincos(th, &s, &c);
+  sincos(2.0 * PI_REF * x, &s, &c);
   const double2 e = make_double2(c, s);
   const int len = a == 0 ? kx : a == 1 ? ky : kz;
-  const size_t off = (size_t)i * len;
   const double q = a == 0 ? p.w : 1.0;
   double2 v = make_double2(1.0, 0.0);
   if (txf) {  // mixed path: FP64 recurrence, FP32 table
-    float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + off;
+    float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
     for (int k = 0; k < len; ++k) {
-      dst[k] = make_float2((float)(q * v.x), (float)(q * v.y));
+      dst[(size_t)k * n] = make_float2((float)(q * v.x), (float)(q * v.y));
       v = cmul(v, e);
     }
   } else {
-    double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + off;
+    double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + i;
     for (int k = 0; k < len; ++k) {
-      dst[k] = make_double2(q * v.x, q * v.y);
+      dst[(size_t)k * n] = make_double2(q * v.x, q * v.y);
       v = cmul(v, e);
     }
   }
 }
 
-// S(k): thread per chunk (column, up to CH consecutive nz), block.y = slice.
+// S(k): thread per chunk (column, up to CH consecutive nz), block.y = slice
+// of atoms staged TILE at a time in shared memory.
 template <typename R, typename C2>
 __global__ void __launch_bounds__(128) k_sfac(
     int n, int nchunk, const Chunk *__restrict__ chunks,
@@ -96,7 +94,7 @@ __global__ void __launch_bounds__(128) k_sfac(
     const C2 *__restrict__ ty, const C2 *__restrict__ tz, int kx, int ky, int kz,
     double2 *__restrict__ sk) {
   extern __shared__ unsigned char smem_raw[];
-  C2 *sx = reinterpret_cast<C2 *>(smem_raw);
+  C2 *sx = reinterpret_cast<C2 *>(smem_raw);  // [atom][n]
   C2 *sy = sx + TILE * kx;
   C2 *sz = sy + TILE * ky;
   const int ch = blockIdx.x * blockDim.x + threadIdx.x;
@@ -107,32 +105,43 @@ __global__ void __launch_bounds__(128) k_sfac(
     cc = chunks[ch];
     col = cols[cc.col];
   }
+  const int ny = col.ny < 0 ? -col.ny : col.ny;
+  const bool nyneg = col.ny < 0;
   R sr[CH], si[CH];
 #pragma unroll
   for (int t = 0; t < CH; ++t) sr[t] = si[t] = R(0);
   for (int base = a0; base < a1; base += TILE) {
     const int m = min(TILE, a1 - base);
     __syncthreads();
-    for (int k = threadIdx.x; k < m * kx; k += blockDim.x) sx[k] = tx[(size_t)base * kx + k];
-    for (int k = threadIdx.x; k < m * ky; k += blockDim.x) sy[k] = ty[(size_t)base * ky + k];
-    for (int k = threadIdx.x; k < m * kz; k += blockDim.x) sz[k] = tz[(size_t)base * kz + k];
+    for (int k = threadIdx.x; k < m * kx; k += blockDim.x) {
+      const int nn = k / m, j = k - nn * m;
+      sx[j * kx + nn] = tx[(size_t)nn * n + base + j];
+    }
+    for (int k = threadIdx.x; k < m * ky; k += blockDim.x) {
+      const int nn = k / m, j = k - nn * m;
+      sy[j * ky + nn] = ty[(size_t)nn * n + base + j];
+    }
+    for (int k = threadIdx.x; k < m * kz; k += blockDim.x) {
+      const int nn = k / m, j = k - nn * m;
+      sz[j * kz + nn] = tz[(size_t)nn * n + base + j];
+    }
     __syncthreads();
     if (ch < nchunk) {
       for (int j = 0; j < m; ++j) {
-        C2 X = sx[j * kx + col.nx];
-        int ny = col.ny;
-        C2 Y = sy[j * ky + (ny < 0 ? -ny : ny)];
-        if (ny < 0) Y.y = -Y.y;
-        const R tr = X.x * Y.x - X.y * Y.y, ti = X.x * Y.y + X.y * Y.x;
+        const C2 X = sx[j * kx + col.nx];
+        const C2 Y = conj_if(sy[j * ky + ny], nyneg);
+        const R tr = fma(X.x, Y.x, -X.y * Y.y), ti = fma(X.x, Y.y, X.y * Y.x);
         const C2 *zr = sz + j * kz;
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
           if (t < cc.len) {
-            int nz = cc.nz0 + t;
-            C2 Z = zr[nz < 0 ? -nz : nz];
-            R zy = nz < 0 ? -Z.y : Z.y;
-            sr[t] += tr * Z.x - ti * zy;
-            si[t] += tr * zy + ti * Z.x;
+            const int nz = cc.nz0 + t;
+            const C2 Z = zr[nz < 0 ? -nz : nz];
+            const R zy = nz < 0 ? -Z.y : Z.y;
+            sr[t] = fma(tr, Z.x, sr[t]);
+            sr[t] = fma(-ti, zy, sr[t]);
+            si[t] = fma(tr, zy, si[t]);
+            si[t] = fma(ti, Z.x, si[t]);
           }
         }
       }
@@ -150,21 +159,28 @@ __global__ void __launch_bounds__(128) k_sfac(
 
 // Per k: energy and virial terms (forces.f:1316-1331), W_k and RZV W_k.
 __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
-                         const double2 *__restrict__ sk, double ibx, double iby,
-                         double ibz, double alp2, double cfur,
+                         const double2 *__restrict__ sk, double bx, double by,
+                         double bz, double alp2, double cfur,
                          double2 *__restrict__ wk, double2 *__restrict__ wkz,
+                         float2 *__restrict__ wkf, float2 *__restrict__ wkzf,
+                         double2 *__restrict__ colrv, float2 *__restrict__ colrvf,
                          Dst6 dst) {
   double acc[4] = {0, 0, 0, 0};
   const double twopi = 2.0 * PI_REF;
   for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
     const KCol col = cols[c];
     const int len = col.nzhi - col.nzlo + 1;
+    if (threadIdx.x == 0) {
+      const double rx = (twopi * col.nx) / bx, ry = (twopi * col.ny) / by;
+      colrv[c] = make_double2(rx, ry);
+      colrvf[c] = make_float2((float)rx, (float)ry);
+    }
     for (int t = threadIdx.x; t < len; t += blockDim.x) {
       const int k = col.koff + t;
       const int nz = col.nzlo + t;
-      const double RXV = (twopi * col.nx) * ibx;
-      const double RYV = (twopi * col.ny) * iby;
-      const double RZV = (twopi * nz) * ibz;
+      const double RXV = (twopi * col.nx) / bx;
+      const double RYV = (twopi * col.ny) / by;
+      const double RZV = (twopi * nz) / bz;
       const double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
       const double2 S = sk[k];
       const double SCS = S.x, SSN = S.y;
@@ -177,8 +193,14 @@ __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
       acc[3] -= (RZV * RZV) * AKV * S2;
       const double AK2 = 2.0 * AKC;
       const double2 W = make_double2(AK2 * SCS, -AK2 * SSN);
-      wk[k] = W;
-      wkz[k] = make_double2(RZV * W.x, RZV * W.y);
+      const double2 Wz = make_double2(RZV * W.x, RZV * W.y);
+      if (wkf) {
+        wkf[k] = make_float2((float)W.x, (float)W.y);
+        wkzf[k] = make_float2((float)Wz.x, (float)Wz.y);
+      } else {
+        wk[k] = W;
+        wkz[k] = Wz;
+      }
     }
   }
   block_add<4>(acc, dst.p);
@@ -195,36 +217,68 @@ __global__ void k_qpe_fold(mdx_scalars *sc, double *qpe) {
   *qpe = 0.0;
 }
 
-// Forces: thread per atom, all columns.
+// U += W conj(Z) (nz < 0, Z stored for |nz|) or U += W Z, both with two FMAs
+// per component.
+template <typename R, typename C2>
+__device__ __forceinline__ void cmac(R &ux, R &uy, const C2 w, const C2 z, bool neg) {
+  if (neg) {
+    ux = fma(w.x, z.x, ux);
+    ux = fma(w.y, z.y, ux);
+    uy = fma(w.y, z.x, uy);
+    uy = fma(-w.x, z.y, uy);
+  } else {
+    ux = fma(w.x, z.x, ux);
+    ux = fma(-w.y, z.y, ux);
+    uy = fma(w.x, z.y, uy);
+    uy = fma(w.y, z.x, uy);
+  }
+}
+
+// Forces: thread per atom, all columns; the nz loop is split at 0 so the
+// conjugation is a compile-time choice in each half.
+template <typename R, typename C2>
+__device__ __forceinline__ void column_sums(const C2 *__restrict__ Z, int n,
+                                            const C2 *__restrict__ w,
+                                            const C2 *__restrict__ wz,
+                                            const KCol &col, R &ux, R &uy,
+                                            R &vx, R &vy) {
+  int nz = col.nzlo, k = col.koff;
+  const int neg_end = min(col.nzhi, -1);
+  for (; nz <= neg_end; ++nz, ++k) {
+    const C2 z = Z[(size_t)(-nz) * n];
+    const C2 a = w[k], b = wz[k];
+    cmac<R, C2>(ux, uy, a, z, true);
+    cmac<R, C2>(vx, vy, b, z, true);
+  }
+  for (; nz <= col.nzhi; ++nz, ++k) {
+    const C2 z = Z[(size_t)nz * n];
+    const C2 a = w[k], b = wz[k];
+    cmac<R, C2>(ux, uy, a, z, false);
+    cmac<R, C2>(vx, vy, b, z, false);
+  }
+}
+
 __global__ void __launch_bounds__(128) k_rforce64(
     int n, int ncol, const KCol *__restrict__ cols,
     const double2 *__restrict__ wk, const double2 *__restrict__ wkz,
     const double2 *__restrict__ tx, const double2 *__restrict__ ty,
-    const double2 *__restrict__ tz, int kx, int ky, int kz, double ibx,
-    double iby, double *__restrict__ gx, double *__restrict__ gy,
-    double *__restrict__ gz) {
+    const double2 *__restrict__ tz, const double2 *__restrict__ colrv,
+    double *__restrict__ gx, double *__restrict__ gy, double *__restrict__ gz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double twopi = 2.0 * PI_REF;
-  const double2 *X = tx + (size_t)i * kx, *Y = ty + (size_t)i * ky,
-                *Z = tz + (size_t)i * kz;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int c = 0; c < ncol; ++c) {
     const KCol col = cols[c];
-    double2 U = make_double2(0.0, 0.0), V = make_double2(0.0, 0.0);
-    for (int nz = col.nzlo, k = col.koff; nz <= col.nzhi; ++nz, ++k) {
-      const double2 Zv = tab_get(Z, nz);
-      const double2 w = __ldg(&wk[k]), wz = __ldg(&wkz[k]);
-      U.x += w.x * Zv.x - w.y * Zv.y;
-      U.y += w.x * Zv.y + w.y * Zv.x;
-      V.x += wz.x * Zv.x - wz.y * Zv.y;
-      V.y += wz.x * Zv.y + wz.y * Zv.x;
-    }
-    const double2 T = cmul(X[col.nx], tab_get(Y, col.ny));
-    const double imTU = T.x * U.y + T.y * U.x;
-    const double imTV = T.x * V.y + T.y * V.x;
-    fx += ((twopi * col.nx) * ibx) * imTU;
-    fy += ((twopi * col.ny) * iby) * imTU;
+    double ux = 0., uy = 0., vx = 0., vy = 0.;
+    column_sums<double, double2>(tz + i, n, wk, wkz, col, ux, uy, vx, vy);
+    const int ny = col.ny < 0 ? -col.ny : col.ny;
+    const double2 T = cmul(tx[(size_t)col.nx * n + i],
+                           conj_if(ty[(size_t)ny * n + i], col.ny < 0));
+    const double imTU = fma(T.x, uy, T.y * ux);
+    const double imTV = fma(T.x, vy, T.y * vx);
+    const double2 rv = colrv[c];
+    fx = fma(rv.x, imTU, fx);
+    fy = fma(rv.y, imTU, fy);
     fz += imTV;
   }
   gx[i] += fx;
@@ -234,35 +288,27 @@ __global__ void __launch_bounds__(128) k_rforce64(
 
 __global__ void __launch_bounds__(128) k_rforce32(
     int n, int ncol, const KCol *__restrict__ cols,
-    const double2 *__restrict__ wk, const double2 *__restrict__ wkz,
+    const float2 *__restrict__ wk, const float2 *__restrict__ wkz,
     const float2 *__restrict__ tx, const float2 *__restrict__ ty,
-    const float2 *__restrict__ tz, int kx, int ky, int kz, double ibx,
-    double iby, FixScale fsc, unsigned long long *__restrict__ gfix) {
+    const float2 *__restrict__ tz, const float2 *__restrict__ colrv, FixScale fsc,
+    unsigned long long *__restrict__ gfix) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float twopi = (float)(2.0 * PI_REF);
-  const float2 *X = tx + (size_t)i * kx, *Y = ty + (size_t)i * ky,
-               *Z = tz + (size_t)i * kz;
   const float sc = (float)fsc.scale;
   long long ax = 0, ay = 0, az = 0;
   for (int c = 0; c < ncol; ++c) {
     const KCol col = cols[c];
-    float2 U = make_float2(0.f, 0.f), V = make_float2(0.f, 0.f);
-    for (int nz = col.nzlo, k = col.koff; nz <= col.nzhi; ++nz, ++k) {
-      const float2 Zv = tab_getf(Z, nz);
-      const double2 wd = __ldg(&wk[k]), wzd = __ldg(&wkz[k]);
-      const float2 w = make_float2((float)wd.x, (float)wd.y);
-      const float2 wz = make_float2((float)wzd.x, (float)wzd.y);
-      U.x += w.x * Zv.x - w.y * Zv.y;
-      U.y += w.x * Zv.y + w.y * Zv.x;
-      V.x += wz.x * Zv.x - wz.y * Zv.y;
-      V.y += wz.x * Zv.y + wz.y * Zv.x;
-    }
-    const float2 T = cmulf(X[col.nx], tab_getf(Y, col.ny));
-    const float imTU = T.x * U.y + T.y * U.x;
-    const float imTV = T.x * V.y + T.y * V.x;
-    ax += __float2ll_rn((float)((twopi * col.nx) * ibx) * imTU * sc);
-    ay += __float2ll_rn((float)((twopi * col.ny) * iby) * imTU * sc);
+    float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f;
+    column_sums<float, float2>(tz + i, n, wk, wkz, col, ux, uy, vx, vy);
+    const int ny = col.ny < 0 ? -col.ny : col.ny;
+    const float2 T = cmulf(tx[(size_t)col.nx * n + i],
+                           conj_if(ty[(size_t)ny * n + i], col.ny < 0));
+    const float imTU = fmaf(T.x, uy, T.y * ux);
+    const float imTV = fmaf(T.x, vy, T.y * vx);
+    // per-column partials go to 64-bit fixed point (order independent)
+    const float2 rv = colrv[c];
+    ax += __float2ll_rn(rv.x * imTU * sc);
+    ay += __float2ll_rn(rv.y * imTU * sc);
     az += __float2ll_rn(imTV * sc);
   }
   gfix[i] += (unsigned long long)ax;
@@ -319,8 +365,7 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
                          const int4 *__restrict__ ainfo,
                          const int *__restrict__ nnbb,
                          const int *__restrict__ inbb, int nbdmax,
-                         const int *__restrict__ mol_first,
-                         const int *__restrict__ mol_nat, TypeConst tc,
+                         const int *__restrict__ mol_first, TypeConst tc,
                          double coulf, double alphad, double bx, double by,
                          double bz, double *gx, double *gy, double *gz,
                          unsigned long long *gfix, double fscale, Dst6 dst,
@@ -345,8 +390,7 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
       }
     } else {
       // EE molecule: every intramolecular pair JSM < ISM (forces.f:1585-1594)
-      const int m = ai.y;
-      const int f = mol_first[m];
+      const int f = mol_first[ai.y];
       for (int jsp = f; jsp < isp; ++jsp)
         eterms_pair(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc,
                     acc, spee_sh, gx, gy, gz, gfix, n, fscale);
@@ -376,6 +420,7 @@ int host_inifur(mdx_ctx *ctx) {
     return MDX_ERR_UNSUPPORTED;
   }
   DevData &d = ctx->dv;
+  ctx->drop_graphs();  // k-set buffers are reallocated below
   const double alphad = ctx->p.alphad;
   const double ALP2 = alphad * alphad;
   const double CUTK2 = 4.0 * ALP2 * ctx->p.fexp;
@@ -384,7 +429,6 @@ int host_inifur(mdx_ctx *ctx) {
   const int KMAX = (int)(CUTK * ctx->boxl / TWOPI + 1);
   const int KMAY = (int)(CUTK * ctx->boyl / TWOPI + 1);
   const int KMAZ = (int)(CUTK * ctx->bozl / TWOPI + 1);
-  // presence map of (nx, ny, nz) in the reference's k-set
   const int NY = 2 * KMAY + 1, NZ = 2 * KMAZ + 1;
   std::vector<unsigned char> in((size_t)(KMAX + 1) * NY * NZ, 0);
   int nkv = 0;
@@ -463,9 +507,15 @@ int host_inifur(mdx_ctx *ctx) {
     }
   }
   if (d.sk) cudaFree(d.sk);
-  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * 3 * (size_t)std::max(1, nkv)));
-  d.wk = d.sk + nkv;
-  d.wkz = d.wk + nkv;
+  const size_t nk = (size_t)std::max(1, nkv);
+  const size_t nc = std::max<size_t>(1, cols.size());
+  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (4 * nk + 2 * nc)));
+  d.wk = d.sk + nk;
+  d.wkz = d.wk + nk;
+  d.wkf = reinterpret_cast<float2 *>(d.wkz + nk);
+  d.wkzf = d.wkf + nk;
+  d.colrv = d.wkz + 2 * nk;
+  d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
   // self-energy (forces.f:1426-1447)
   const double ABC = alphad / std::sqrt(PI_REF);
   ctx->spei = 0.0;
@@ -512,6 +562,7 @@ int launch_furir(mdx_ctx *ctx) {
   const double cfur = 4.0 * PI_REF * ctx->p.coulf / vol;
   const Chunk *chunks = reinterpret_cast<const Chunk *>(d.kchunks);
   const int nchunk = d.nchunk;
+  const bool mx = ctx->mixed();
   {
     MDX_TIMER(ctx, MDX_T_EW_TABLES);
     k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
@@ -520,40 +571,41 @@ int launch_furir(mdx_ctx *ctx) {
     MDX_LAUNCHED(ctx);
   }
   MDX_CUDA(cudaMemsetAsync(d.sk, 0, sizeof(double2) * d.nkv, ctx->stream));
-  dim3 grid((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
   {
-  MDX_TIMER(ctx, MDX_T_EW_SFAC);
-  if (ctx->mixed()) {
-    size_t sh = sizeof(float2) * TILE * (d.kx + d.ky + d.kz);
-    k_sfac<float, float2><<<grid, 128, sh, ctx->stream>>>(
-        d.n, nchunk, chunks, d.cols, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky, d.kz, d.sk);
-  } else {
-    size_t sh = sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
-    k_sfac<double, double2><<<grid, 128, sh, ctx->stream>>>(
-        d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk);
-  }
-  MDX_LAUNCHED(ctx);
+    MDX_TIMER(ctx, MDX_T_EW_SFAC);
+    dim3 grid((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
+    if (mx) {
+      size_t sh = sizeof(float2) * TILE * (d.kx + d.ky + d.kz);
+      k_sfac<float, float2><<<grid, 128, sh, ctx->stream>>>(
+          d.n, nchunk, chunks, d.cols, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky, d.kz, d.sk);
+    } else {
+      size_t sh = sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
+      k_sfac<double, double2><<<grid, 128, sh, ctx->stream>>>(
+          d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk);
+    }
+    MDX_LAUNCHED(ctx);
   }
   double *qpe = d.red + 40;
   mdx_scalars *sc = d.sc;
-  Dst6 dst{{qpe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
   {
-  MDX_TIMER(ctx, MDX_T_EW_KTERMS);
-  k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-      d.ncol, d.cols, d.sk, ibx, iby, ibz, alp2, cfur, d.wk, d.wkz, dst);
-  MDX_LAUNCHED(ctx);
-  k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
-  MDX_LAUNCHED(ctx);
+    MDX_TIMER(ctx, MDX_T_EW_KTERMS);
+    Dst6 dst{{qpe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
+    k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
+        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk, d.wkz,
+        mx ? d.wkf : nullptr, mx ? d.wkzf : nullptr, d.colrv, d.colrvf, dst);
+    MDX_LAUNCHED(ctx);
+    k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
+    MDX_LAUNCHED(ctx);
   }
   MDX_TIMER(ctx, MDX_T_EW_FORCE);
-  if (ctx->mixed()) {
+  if (mx) {
     k_rforce32<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wk, d.wkz, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky,
-        d.kz, ibx, iby, ctx->fix, d.gfix);
+        d.n, d.ncol, d.cols, d.wkf, d.wkzf, d.tabxf, d.tabyf, d.tabzf, d.colrvf,
+        ctx->fix, d.gfix);
   } else {
     k_rforce64<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wk, d.wkz, d.tabx, d.taby, d.tabz, d.kx, d.ky,
-        d.kz, ibx, iby, d.gx, d.gy, d.gz);
+        d.n, d.ncol, d.cols, d.wk, d.wkz, d.tabx, d.taby, d.tabz, d.colrv, d.gx, d.gy,
+        d.gz);
   }
   MDX_LAUNCHED(ctx);
   return MDX_OK;
@@ -571,10 +623,9 @@ int launch_eterms(mdx_ctx *ctx) {
   mdx_scalars *sc = d.sc;
   Dst6 dst{{&sc->spe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
   k_eterms<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-      d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, d.mol_nat,
-      ctx->tc, ctx->p.coulf, ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl,
-      d.gx, d.gy, d.gz, ctx->mixed() ? d.gfix : nullptr, ctx->fix.scale, dst,
-      sc->spee);
+      d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc,
+      ctx->p.coulf, ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy,
+      d.gz, ctx->mixed() ? d.gfix : nullptr, ctx->fix.scale, dst, sc->spee);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -778,7 +778,15 @@ __global__ void k_vira_zero(mdx_thermo *th) {
 
 // ------------------------------------------------------------------ record
 __global__ void k_record(mdx_step_record *rec, int slot, int mstep,
-                         const mdx_scalars *s, const mdx_thermo *th) {
+                         const mdx_scalars *s, const mdx_thermo *th, int *ctr,
+                         int cap) {
+  if (ctr) {  // graph replay: slot and step number come from device counters
+    slot = ctr[0];
+    mstep = ctr[1];
+    ctr[0] = slot + 1;
+    ctr[1] = mstep + 1;
+    if (slot >= cap) return;
+  }
   mdx_step_record &r = rec[slot];
   r.mstep = mstep;
   r.mbsh = s->mbsh;
@@ -1070,7 +1078,10 @@ int launch_vira(mdx_ctx *ctx, int from_viran) {
 
 int launch_record(mdx_ctx *ctx, int slot, int mstep) {
   MDX_TIMER(ctx, MDX_T_OTHER);
-  k_record<<<1, 1, 0, ctx->stream>>>(ctx->dv.rec, slot, mstep, ctx->dv.sc, ctx->dv.th);
+  // slot < 0: take slot and step number from the device counters
+  int *ctr = slot < 0 ? ctx->dv.shake_iter + 16 : nullptr;
+  k_record<<<1, 1, 0, ctx->stream>>>(ctx->dv.rec, slot, mstep, ctx->dv.sc, ctx->dv.th, ctr,
+                                     ctx->dv.rec_cap);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

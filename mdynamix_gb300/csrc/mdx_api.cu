@@ -257,7 +257,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
   RC(launch_kick(ctx, 2, HTSTEP, false));
   RC(launch_scaling(ctx, 2, nullptr));
   if (p.lnpt) RC(sync_box_from_device(ctx));
-  if (slot >= 0) RC(launch_record(ctx, slot, mstep));
+  if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters
   return MDX_OK;
 }
 
@@ -272,7 +272,7 @@ int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
   RC(launch_getcom(ctx));
   if (mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
   RC(do_allforce(ctx, false));
-  if (slot >= 0) RC(launch_record(ctx, slot, mstep));
+  if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters
   return MDX_OK;
 }
 
@@ -292,12 +292,50 @@ int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
     return MDX_ERR_STATE;
   }
   if (rec) RC(ensure_records(ctx, nsteps));
+  // CUDA-graph replay of whole long steps: DOUBLE at constant volume has a
+  // fixed launch sequence, with or without the mid-step list rebuild.
+  const bool graphs = dbl && !ctx->p.lnpt && !ctx->timing && ctx->use_graphs;
+  if (graphs && rec) {
+    int c0[2] = {0, mstep0 + 1};
+    MDX_CUDA(cudaMemcpyAsync(ctx->dv.shake_iter + 16, c0, sizeof c0, cudaMemcpyHostToDevice,
+                             ctx->stream));
+    MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
   for (int s = 1; s <= nsteps; ++s) {
     const int mstep = mstep0 + s;
-    if (dbl)
-      RC(double_step(ctx, mstep, rec ? s - 1 : -1));
-    else
-      RC(sultan_step(ctx, mstep, rec ? s - 1 : -1));
+    if (graphs) {
+      const int g = (mstep % ctx->p.ichnb == 0 ? 1 : 0) + (rec ? 2 : 0);
+      if (!ctx->gexec[g]) {
+        const int64_t l0 = ctx->launches;
+        MDX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = double_step(ctx, mstep, rec ? -1 : -2);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc) {
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+        if (e != cudaSuccess) {
+          ctx->err = std::string("graph capture: ") + cudaGetErrorString(e);
+          return MDX_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&ctx->gexec[g], graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+          ctx->gexec[g] = nullptr;
+          ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+          return MDX_ERR_CUDA;
+        }
+        ctx->glaunches[g] = ctx->launches - l0;
+        ctx->launches = l0;
+      }
+      MDX_CUDA(cudaGraphLaunch(ctx->gexec[g], ctx->stream));
+      ctx->launches += ctx->glaunches[g];
+    } else if (dbl) {
+      RC(double_step(ctx, mstep, rec ? s - 1 : -2));
+    } else {
+      RC(sultan_step(ctx, mstep, rec ? s - 1 : -2));
+    }
   }
   RC(check_err(ctx));
   if (rec) {
@@ -353,6 +391,10 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
     ctx->d.cap_long *= 2;
   }
   cudaGetDevice(&ctx->device);
+  {
+    const char *g = getenv("MDX_GRAPHS");
+    if (g && g[0] == '0') ctx->use_graphs = false;
+  }
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return MDX_ERR_CUDA;
@@ -443,6 +485,7 @@ int mdx_close(mdx_ctx *ctx) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->drop_graphs();
   for (auto &sp : ctx->spans) {
     cudaEventDestroy(sp.a);
     cudaEventDestroy(sp.b);
@@ -660,6 +703,7 @@ int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
       p->rcut + p->rskin > 0.5 * std::min(p->boxl, std::min(p->boyl, p->bozl))) {
     // the reference allows it (single image per pair); so does the list build
   }
+  ctx->drop_graphs();  // kernel arguments baked into the step graphs change
   ctx->p = *p;
   ctx->pc.coulf = p->coulf;
   ctx->pc.alphad = p->alphad;
@@ -935,6 +979,7 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
   ctx->p.raex = bee * (1. - std::pow(ec, pw2));
   ctx->p.ec_me = ec;
   ctx->pc.raex = ctx->p.raex;
+  ctx->drop_graphs();
   if (ctx->have_state) {
     double *dq = nullptr;
     RC(dmalloc(ctx, &dq, d.n));

@@ -134,6 +134,9 @@ struct DevData {
   float2 *tabxf, *tabyf, *tabzf;
   double2 *sk;                  // structure factors, column order
   double2 *wk, *wkz;            // AK2*conj(S), kz*AK2*conj(S)
+  float2 *wkf, *wkzf;           // FP32 copies for the mixed force pass
+  double2 *colrv;               // per column (RXV, RYV) at the current box
+  float2 *colrvf;
   double *kscal;                // per-k scratch of the energy/virial kernel
   // scalars and state blocks
   mdx_scalars *sc;
@@ -176,6 +179,17 @@ struct mdx_ctx {
   CellGrid grid{};
   double list_rl2 = 0;  // squared list radius used by the last build
   FixScale fix{};
+  // CUDA graphs of one long step: [rebuild?] + 2 * [records?]
+  cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t glaunches[4] = {0, 0, 0, 0};
+  bool use_graphs = true;
+  void drop_graphs() {
+    for (auto &g : gexec)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
   int mbsh = 0, mbln = 0;
   // device timers (mdx_set_timers)
   bool timing = false;

@@ -298,6 +298,7 @@ int launch_build_lists(mdx_ctx *ctx) {
   g.cz = ctx->bozl / g.nz;
   g.ncell = g.nx * g.ny * g.nz;
   if (g.ncell != ctx->grid.ncell) {
+    ctx->drop_graphs();
     if (d.cell_cnt) cudaFree(d.cell_cnt);
     if (d.cell_start) cudaFree(d.cell_start);
     MDX_CUDA(cudaMalloc(&d.cell_cnt, sizeof(int) * (g.ncell + 1) * 2));

@@ -163,3 +163,20 @@ def test_set_lambda_matches_oracle():
     g.chcnb(); o.chcnb()
     g.allforce(); o.allforce()
     assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
+
+
+def test_graph_replay_matches_eager(monkeypatch):
+    """Long steps replayed from captured CUDA graphs give the same state and
+    records as eager launches (mixed path: bit for bit)."""
+    s, st = CASES["spcfw"]()
+    runs = []
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("MDX_GRAPHS", graphs)
+        g = ForcePath(s, precision=MDX_MIXED)
+        g.set_state(*st)
+        rec = g.double(12)
+        (x, y, z, *_), th = g.get_state()
+        runs.append((np.stack([x, y, z]), [r.temp for r in rec], [r.mstep for r in rec]))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert runs[0][1] == runs[1][1]
+    assert runs[0][2] == list(range(1, 13))
