@@ -115,7 +115,7 @@ __global__ void k_getbnd(int nrbt, const int *__restrict__ ibi,
       acc[4] = (double)(FORB * (BZ * BZ));
     }
   }
-  block_add<5>(acc, dst.p);
+  block_add<5>(acc, dst);
   if (laver && nrbb <= 256) {
     for (int k = threadIdx.x; k < nrbb; k += blockDim.x) {
       if (sbr[k] != 0.0) atomicAdd(&br[k], sbr[k]);
@@ -187,7 +187,7 @@ __global__ void k_getang(int nrat, const int *__restrict__ iai,
       acc[3] = (double)(-AZ * FAZ - BZ * FBZ);
     }
   }
-  block_add<4>(acc, dst.p);
+  block_add<4>(acc, dst);
   if (laver && nraa <= 256) {
     for (int k = threadIdx.x; k < nraa; k += blockDim.x) {
       if (sar[k] != 0.0) atomicAdd(&ar[k], sar[k]);
@@ -332,7 +332,7 @@ __global__ void k_gettrs(int nrrt, const int *__restrict__ iti,
       }
     }
   }
-  block_add<4>(acc, dst.p);
+  block_add<4>(acc, dst);
 }
 
 struct WaterPar {
@@ -419,10 +419,11 @@ __global__ void k_strbnd(WaterPar w, const dbl4 *__restrict__ pos, double bxl,
       acc[4] = (double)VIZ;
     }
   }
-  block_add<5>(acc, dst.p);
+  block_add<5>(acc, dst);
   if (laver) {
-    double *d6[6] = {&br[w.i1], &br[w.i1 + 1], &br[w.i1 + 2],
-                     &be[w.i1], &be[w.i1 + 1], &be[w.i1 + 2]};
+    // second reduction: its own partials region and counter
+    Dst6 d6{{&br[w.i1], &br[w.i1 + 1], &br[w.i1 + 2], &be[w.i1], &be[w.i1 + 1], &be[w.i1 + 2]},
+            dst.part ? dst.part + (size_t)gridDim.x * 8 : nullptr, dst.ctr ? dst.ctr + 1 : nullptr};
     double v6[6] = {brs[0], brs[1], brs[2], bes[0], bes[1], bes[2]};
     block_add<6>(v6, d6);
   }
@@ -468,7 +469,7 @@ int launch_bonded(mdx_ctx *ctx, int laver) {
     w.ro2 = ctx->h_ro[i1 + 1];
     w.aadd = w.aaa * w.ro1;
     w.bbdd = w.bbb * w.ro2;
-    Dst6 dst{{&sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz, nullptr}};
+    Dst6 dst = dst6(ctx, (w.nmol + T - 1) / T, 14, &sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz);
     if (mx)
       k_strbnd<float><<<(w.nmol + T - 1) / T, T, 0, ctx->stream>>>(w, d.pos, bx, by, bz, o, dst, laver, d.br, d.be);
     else
@@ -476,7 +477,7 @@ int launch_bonded(mdx_ctx *ctx, int laver) {
     MDX_LAUNCHED(ctx);
   }
   if (d.nrbt > 0) {
-    Dst6 dst{{&sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz, nullptr}};
+    Dst6 dst = dst6(ctx, (d.nrbt + T - 1) / T, 5, &sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz);
 #define GB(R)                                                                          \
   k_getbnd<R><<<(d.nrbt + T - 1) / T, T, 0, ctx->stream>>>(                            \
       d.nrbt, d.ibi, d.jbj, d.ibuk, d.bid, d.brb, d.bfb, d.bdb, d.bro, d.pos, d.ainfo, \
@@ -486,7 +487,7 @@ int launch_bonded(mdx_ctx *ctx, int laver) {
     MDX_LAUNCHED(ctx);
   }
   if (d.nrat > 0) {
-    Dst6 dst{{&sc->pint, &sc->virfx, &sc->virfy, &sc->virfz, nullptr, nullptr}};
+    Dst6 dst = dst6(ctx, (d.nrat + T - 1) / T, 4, &sc->pint, &sc->virfx, &sc->virfy, &sc->virfz);
 #define GA(R)                                                                          \
   k_getang<R><<<(d.nrat + T - 1) / T, T, 0, ctx->stream>>>(                            \
       d.nrat, d.iai, d.jaj, d.kak, d.iauk, d.ara, d.afa, d.pos, d.ainfo, ctx->tc,      \
@@ -496,7 +497,7 @@ int launch_bonded(mdx_ctx *ctx, int laver) {
     MDX_LAUNCHED(ctx);
   }
   if (d.nrrt > 0) {
-    Dst6 dst{{&sc->pint, &sc->virfx, &sc->virfy, &sc->virfz, nullptr, nullptr}};
+    Dst6 dst = dst6(ctx, (d.nrrt + T - 1) / T, 4, &sc->pint, &sc->virfx, &sc->virfy, &sc->virfz);
     TorsTab tt{d.titors, d.tnmul, d.tft, d.trt, d.tft1, d.tft2, d.tft3, d.tft4, d.tft5};
 #define GT(R)                                                                          \
   k_gettrs<R><<<(d.nrrt + T - 1) / T, T, 0, ctx->stream>>>(                            \

@@ -36,6 +36,7 @@ constexpr double PI_REF = 3.1415926536;  // common_inc.f:31
 constexpr int CH = 8;                    // nz per chunk of the S(k) kernel
 constexpr int SLICE = 512;               // atoms per slice of the S(k) kernel
 constexpr int TILE = 32;                 // atoms staged in shared memory
+constexpr size_t SFAC_SMEM_MAX = 227 * 1024;
 
 struct Chunk {
   int col, nz0, len, k0;
@@ -67,19 +68,25 @@ __global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
   double s, c;
   sincos(2.0 * PI_REF * x, &s, &c);
   const double2 e = make_double2(c, s);
-  const int len = a == 0 ? kx : a == 1 ? ky : kz;
+  // x and y tables hold n = 0..K; the z table holds n = -K..K (conjugates
+  // stored) at index n + K, so the inner loops need no sign test
+  const int kzo = (kz - 1) / 2;
+  const int len = a == 0 ? kx : a == 1 ? ky : kzo + 1;
+  const int off = a == 2 ? kzo : 0;
   const double q = a == 0 ? p.w : 1.0;
   double2 v = make_double2(1.0, 0.0);
   if (txf) {  // mixed path: FP64 recurrence, FP32 table
     float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
     for (int k = 0; k < len; ++k) {
-      dst[(size_t)k * n] = make_float2((float)(q * v.x), (float)(q * v.y));
+      dst[(size_t)(off + k) * n] = make_float2((float)(q * v.x), (float)(q * v.y));
+      if (a == 2) dst[(size_t)(off - k) * n] = make_float2((float)v.x, (float)-v.y);
       v = cmul(v, e);
     }
   } else {
     double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + i;
     for (int k = 0; k < len; ++k) {
-      dst[(size_t)k * n] = make_double2(q * v.x, q * v.y);
+      dst[(size_t)(off + k) * n] = make_double2(q * v.x, q * v.y);
+      if (a == 2) dst[(size_t)(off - k) * n] = make_double2(v.x, -v.y);
       v = cmul(v, e);
     }
   }
@@ -92,7 +99,7 @@ __global__ void __launch_bounds__(128) k_sfac(
     int n, int nchunk, const Chunk *__restrict__ chunks,
     const KCol *__restrict__ cols, const C2 *__restrict__ tx,
     const C2 *__restrict__ ty, const C2 *__restrict__ tz, int kx, int ky, int kz,
-    double2 *__restrict__ sk) {
+    double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
   extern __shared__ unsigned char smem_raw[];
   C2 *sx = reinterpret_cast<C2 *>(smem_raw);  // [atom][n]
   C2 *sy = sx + TILE * kx;
@@ -107,6 +114,7 @@ __global__ void __launch_bounds__(128) k_sfac(
   }
   const int ny = col.ny < 0 ? -col.ny : col.ny;
   const bool nyneg = col.ny < 0;
+  const int kzo = (kz - 1) / 2;
   R sr[CH], si[CH];
 #pragma unroll
   for (int t = 0; t < CH; ++t) sr[t] = si[t] = R(0);
@@ -135,12 +143,10 @@ __global__ void __launch_bounds__(128) k_sfac(
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
           if (t < cc.len) {
-            const int nz = cc.nz0 + t;
-            const C2 Z = zr[nz < 0 ? -nz : nz];
-            const R zy = nz < 0 ? -Z.y : Z.y;
+            const C2 Z = zr[cc.nz0 + t + kzo];
             sr[t] = fma(tr, Z.x, sr[t]);
-            sr[t] = fma(-ti, zy, sr[t]);
-            si[t] = fma(tr, zy, si[t]);
+            sr[t] = fma(-ti, Z.y, sr[t]);
+            si[t] = fma(tr, Z.y, si[t]);
             si[t] = fma(ti, Z.x, si[t]);
           }
         }
@@ -151,18 +157,35 @@ __global__ void __launch_bounds__(128) k_sfac(
 #pragma unroll
     for (int t = 0; t < CH; ++t)
       if (t < cc.len) {
-        atomicAdd(&sk[cc.k0 + t].x, (double)sr[t]);
-        atomicAdd(&sk[cc.k0 + t].y, (double)si[t]);
+        if (part) {  // slice partial, summed in slice order by k_sfac_sum
+          part[(size_t)blockIdx.y * nkv + cc.k0 + t] = make_double2((double)sr[t], (double)si[t]);
+        } else {
+          atomicAdd(&sk[cc.k0 + t].x, (double)sr[t]);
+          atomicAdd(&sk[cc.k0 + t].y, (double)si[t]);
+        }
       }
   }
+}
+
+// S(k) = sum of the slice partials in slice order (deterministic).
+__global__ void k_sfac_sum(int nkv, int nslice, const double2 *__restrict__ part,
+                           double2 *__restrict__ sk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nkv) return;
+  double x = 0.0, y = 0.0;
+  for (int s = 0; s < nslice; ++s) {
+    const double2 v = part[(size_t)s * nkv + k];
+    x += v.x;
+    y += v.y;
+  }
+  sk[k] = make_double2(x, y);
 }
 
 // Per k: energy and virial terms (forces.f:1316-1331), W_k and RZV W_k.
 __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
                          const double2 *__restrict__ sk, double bx, double by,
                          double bz, double alp2, double cfur,
-                         double2 *__restrict__ wk, double2 *__restrict__ wkz,
-                         float2 *__restrict__ wkf, float2 *__restrict__ wkzf,
+                         dbl4 *__restrict__ wk, float4 *__restrict__ wkf,
                          double2 *__restrict__ colrv, float2 *__restrict__ colrvf,
                          Dst6 dst) {
   double acc[4] = {0, 0, 0, 0};
@@ -192,18 +215,18 @@ __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
       acc[2] -= (RYV * RYV) * AKV * S2;
       acc[3] -= (RZV * RZV) * AKV * S2;
       const double AK2 = 2.0 * AKC;
-      const double2 W = make_double2(AK2 * SCS, -AK2 * SSN);
-      const double2 Wz = make_double2(RZV * W.x, RZV * W.y);
-      if (wkf) {
-        wkf[k] = make_float2((float)W.x, (float)W.y);
-        wkzf[k] = make_float2((float)Wz.x, (float)Wz.y);
-      } else {
+      dbl4 W;
+      W.x = AK2 * SCS;
+      W.y = -AK2 * SSN;
+      W.z = RZV * W.x;
+      W.w = RZV * W.y;
+      if (wkf)
+        wkf[k] = make_float4((float)W.x, (float)W.y, (float)W.z, (float)W.w);
+      else
         wk[k] = W;
-        wkz[k] = Wz;
-      }
     }
   }
-  block_add<4>(acc, dst.p);
+  block_add<4>(acc, dst);
 }
 
 // QPE into PELS1 and the three virial projections (forces.f:1333-1336).
@@ -217,103 +240,124 @@ __global__ void k_qpe_fold(mdx_scalars *sc, double *qpe) {
   *qpe = 0.0;
 }
 
-// U += W conj(Z) (nz < 0, Z stored for |nz|) or U += W Z, both with two FMAs
-// per component.
-template <typename R, typename C2>
-__device__ __forceinline__ void cmac(R &ux, R &uy, const C2 w, const C2 z, bool neg) {
-  if (neg) {
-    ux = fma(w.x, z.x, ux);
-    ux = fma(w.y, z.y, ux);
-    uy = fma(w.y, z.x, uy);
-    uy = fma(-w.x, z.y, uy);
-  } else {
-    ux = fma(w.x, z.x, ux);
-    ux = fma(-w.y, z.y, ux);
-    uy = fma(w.x, z.y, uy);
-    uy = fma(w.y, z.x, uy);
-  }
-}
-
-// Forces: thread per atom, all columns; the nz loop is split at 0 so the
-// conjugation is a compile-time choice in each half.
-template <typename R, typename C2>
+// Column sums U = sum_nz W_k Z(nz), V = sum_nz RZV_k W_k Z(nz) over the
+// signed z table (Z points at row nz = 0 of this atom).  wk holds
+// (Re W, Im W, Re RZV W, Im RZV W) per k.
+template <typename R, typename W4, typename C2>
 __device__ __forceinline__ void column_sums(const C2 *__restrict__ Z, int n,
-                                            const C2 *__restrict__ w,
-                                            const C2 *__restrict__ wz,
+                                            const W4 *__restrict__ wk,
                                             const KCol &col, R &ux, R &uy,
                                             R &vx, R &vy) {
-  int nz = col.nzlo, k = col.koff;
-  const int neg_end = min(col.nzhi, -1);
-  for (; nz <= neg_end; ++nz, ++k) {
-    const C2 z = Z[(size_t)(-nz) * n];
-    const C2 a = w[k], b = wz[k];
-    cmac<R, C2>(ux, uy, a, z, true);
-    cmac<R, C2>(vx, vy, b, z, true);
-  }
-  for (; nz <= col.nzhi; ++nz, ++k) {
-    const C2 z = Z[(size_t)nz * n];
-    const C2 a = w[k], b = wz[k];
-    cmac<R, C2>(ux, uy, a, z, false);
-    cmac<R, C2>(vx, vy, b, z, false);
+  const C2 *z = Z + (long long)col.nzlo * n;
+  const W4 *w = wk + col.koff;
+  const int len = col.nzhi - col.nzlo + 1;
+#pragma unroll 4
+  for (int t = 0; t < len; ++t) {
+    const C2 zz = z[(long long)t * n];
+    const W4 a = w[t];
+    ux = fma(a.x, zz.x, ux);
+    ux = fma(-a.y, zz.y, ux);
+    uy = fma(a.x, zz.y, uy);
+    uy = fma(a.y, zz.x, uy);
+    vx = fma(a.z, zz.x, vx);
+    vx = fma(-a.w, zz.y, vx);
+    vy = fma(a.z, zz.y, vy);
+    vy = fma(a.w, zz.x, vy);
   }
 }
 
-__global__ void __launch_bounds__(128) k_rforce64(
-    int n, int ncol, const KCol *__restrict__ cols,
-    const double2 *__restrict__ wk, const double2 *__restrict__ wkz,
+// Force passes: a block is RF_ATOMS atoms x RF_PARTS column parts (one warp
+// per part); part p takes columns p, p + RF_PARTS, ... and the parts are
+// added in part order through shared memory, so the sum is deterministic.
+constexpr int RF_ATOMS = 32;
+constexpr int RF_PARTS = 4;
+
+__global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
+    int n, int ncol, const KCol *__restrict__ cols, const dbl4 *__restrict__ wk,
     const double2 *__restrict__ tx, const double2 *__restrict__ ty,
-    const double2 *__restrict__ tz, const double2 *__restrict__ colrv,
+    const double2 *__restrict__ tz, int kzo, const double2 *__restrict__ colrv,
     double *__restrict__ gx, double *__restrict__ gy, double *__restrict__ gz) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  __shared__ double red[3][RF_PARTS][RF_ATOMS];
+  const int lane = threadIdx.x % RF_ATOMS, part = threadIdx.x / RF_ATOMS;
+  const int i = blockIdx.x * RF_ATOMS + lane;
   double fx = 0.0, fy = 0.0, fz = 0.0;
-  for (int c = 0; c < ncol; ++c) {
-    const KCol col = cols[c];
-    double ux = 0., uy = 0., vx = 0., vy = 0.;
-    column_sums<double, double2>(tz + i, n, wk, wkz, col, ux, uy, vx, vy);
-    const int ny = col.ny < 0 ? -col.ny : col.ny;
-    const double2 T = cmul(tx[(size_t)col.nx * n + i],
-                           conj_if(ty[(size_t)ny * n + i], col.ny < 0));
-    const double imTU = fma(T.x, uy, T.y * ux);
-    const double imTV = fma(T.x, vy, T.y * vx);
-    const double2 rv = colrv[c];
-    fx = fma(rv.x, imTU, fx);
-    fy = fma(rv.y, imTU, fy);
-    fz += imTV;
+  if (i < n) {
+    const double2 *Z = tz + (size_t)kzo * n + i;
+    for (int c = part; c < ncol; c += RF_PARTS) {
+      const KCol col = cols[c];
+      double ux = 0., uy = 0., vx = 0., vy = 0.;
+      column_sums<double, dbl4, double2>(Z, n, wk, col, ux, uy, vx, vy);
+      const int ny = col.ny < 0 ? -col.ny : col.ny;
+      const double2 T = cmul(tx[(size_t)col.nx * n + i],
+                             conj_if(ty[(size_t)ny * n + i], col.ny < 0));
+      const double imTU = fma(T.x, uy, T.y * ux);
+      const double imTV = fma(T.x, vy, T.y * vx);
+      const double2 rv = colrv[c];
+      fx = fma(rv.x, imTU, fx);
+      fy = fma(rv.y, imTU, fy);
+      fz += imTV;
+    }
   }
-  gx[i] += fx;
-  gy[i] += fy;
-  gz[i] += fz;
+  red[0][part][lane] = fx;
+  red[1][part][lane] = fy;
+  red[2][part][lane] = fz;
+  __syncthreads();
+  if (part == 0 && i < n) {
+#pragma unroll
+    for (int p = 1; p < RF_PARTS; ++p) {
+      fx += red[0][p][lane];
+      fy += red[1][p][lane];
+      fz += red[2][p][lane];
+    }
+    gx[i] += fx;
+    gy[i] += fy;
+    gz[i] += fz;
+  }
 }
 
-__global__ void __launch_bounds__(128) k_rforce32(
-    int n, int ncol, const KCol *__restrict__ cols,
-    const float2 *__restrict__ wk, const float2 *__restrict__ wkz,
+__global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce32(
+    int n, int ncol, const KCol *__restrict__ cols, const float4 *__restrict__ wk,
     const float2 *__restrict__ tx, const float2 *__restrict__ ty,
-    const float2 *__restrict__ tz, const float2 *__restrict__ colrv, FixScale fsc,
-    unsigned long long *__restrict__ gfix) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float sc = (float)fsc.scale;
+    const float2 *__restrict__ tz, int kzo, const float2 *__restrict__ colrv,
+    FixScale fsc, unsigned long long *__restrict__ gfix) {
+  __shared__ long long red[3][RF_PARTS][RF_ATOMS];
+  const int lane = threadIdx.x % RF_ATOMS, part = threadIdx.x / RF_ATOMS;
+  const int i = blockIdx.x * RF_ATOMS + lane;
+  const float sc = fsc.scalef;
   long long ax = 0, ay = 0, az = 0;
-  for (int c = 0; c < ncol; ++c) {
-    const KCol col = cols[c];
-    float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f;
-    column_sums<float, float2>(tz + i, n, wk, wkz, col, ux, uy, vx, vy);
-    const int ny = col.ny < 0 ? -col.ny : col.ny;
-    const float2 T = cmulf(tx[(size_t)col.nx * n + i],
-                           conj_if(ty[(size_t)ny * n + i], col.ny < 0));
-    const float imTU = fmaf(T.x, uy, T.y * ux);
-    const float imTV = fmaf(T.x, vy, T.y * vx);
-    // per-column partials go to 64-bit fixed point (order independent)
-    const float2 rv = colrv[c];
-    ax += __float2ll_rn(rv.x * imTU * sc);
-    ay += __float2ll_rn(rv.y * imTU * sc);
-    az += __float2ll_rn(imTV * sc);
+  if (i < n) {
+    const float2 *Z = tz + (size_t)kzo * n + i;
+    for (int c = part; c < ncol; c += RF_PARTS) {
+      const KCol col = cols[c];
+      float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f;
+      column_sums<float, float4, float2>(Z, n, wk, col, ux, uy, vx, vy);
+      const int ny = col.ny < 0 ? -col.ny : col.ny;
+      const float2 T = cmulf(tx[(size_t)col.nx * n + i],
+                             conj_if(ty[(size_t)ny * n + i], col.ny < 0));
+      const float imTU = fmaf(T.x, uy, T.y * ux);
+      const float imTV = fmaf(T.x, vy, T.y * vx);
+      // per-column partials go to 64-bit fixed point (order independent)
+      const float2 rv = colrv[c];
+      ax += f2ll_rn(rv.x * imTU * sc);
+      ay += f2ll_rn(rv.y * imTU * sc);
+      az += f2ll_rn(imTV * sc);
+    }
   }
-  gfix[i] += (unsigned long long)ax;
-  gfix[n + i] += (unsigned long long)ay;
-  gfix[2 * n + i] += (unsigned long long)az;
+  red[0][part][lane] = ax;
+  red[1][part][lane] = ay;
+  red[2][part][lane] = az;
+  __syncthreads();
+  if (part == 0 && i < n) {
+#pragma unroll
+    for (int p = 1; p < RF_PARTS; ++p) {
+      ax += red[0][p][lane];
+      ay += red[1][p][lane];
+      az += red[2][p][lane];
+    }
+    gfix[i] += (unsigned long long)ax;
+    gfix[n + i] += (unsigned long long)ay;
+    gfix[2 * n + i] += (unsigned long long)az;
+  }
 }
 
 // ETERMS (forces.f:1482-1676): thread per atom ISP over its bound partners
@@ -396,7 +440,7 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
                     acc, spee_sh, gx, gy, gz, gfix, n, fscale);
     }
   }
-  block_add<4>(acc, dst.p);
+  block_add<4>(acc, dst);
   if (threadIdx.x < MDX_NT && spee_sh[threadIdx.x] != 0.0)
     atomicAdd(&spee[threadIdx.x], spee_sh[threadIdx.x]);
 }
@@ -472,7 +516,7 @@ int host_inifur(mdx_ctx *ctx) {
         chunks.push_back(Chunk{c, z0, std::min(CH, hi - z0 + 1), koff + (z0 - lo)});
       koff += cnt;
     }
-  const int kx = KMAX + 1, ky = KMAY + 1, kz = KMAZ + 1;
+  const int kx = KMAX + 1, ky = KMAY + 1, kz = 2 * KMAZ + 1;
   const bool realloc_tables = kx != d.kx || ky != d.ky || kz != d.kz;
   d.kx = kx;
   d.ky = ky;
@@ -490,6 +534,20 @@ int host_inifur(mdx_ctx *ctx) {
   MDX_CUDA(cudaMemcpy(d.kchunks, chunks.data(), sizeof(Chunk) * chunks.size(),
                       cudaMemcpyHostToDevice));
   d.nchunk = (int)chunks.size();
+  // shared-memory tile of the S(k) kernel: TILE atoms x all table rows
+  const size_t sh = (ctx->mixed() ? sizeof(float2) : sizeof(double2)) * TILE * (kx + ky + kz);
+  if (sh > SFAC_SMEM_MAX) {
+    ctx->err = "reciprocal k-set too large for the structure-factor tile";
+    return MDX_ERR_UNSUPPORTED;
+  }
+  if (sh > 48 * 1024) {
+    if (ctx->mixed())
+      MDX_CUDA(cudaFuncSetAttribute(k_sfac<float, float2>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+    else
+      MDX_CUDA(cudaFuncSetAttribute(k_sfac<double, double2>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  }
   if (realloc_tables) {
     cudaFree(d.tabx);
     cudaFree(d.tabxf);
@@ -508,14 +566,22 @@ int host_inifur(mdx_ctx *ctx) {
   }
   if (d.sk) cudaFree(d.sk);
   const size_t nk = (size_t)std::max(1, nkv);
+  const size_t nkp = (nk + 1) & ~(size_t)1;  // keeps wk 32-byte aligned
   const size_t nc = std::max<size_t>(1, cols.size());
-  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (4 * nk + 2 * nc)));
-  d.wk = d.sk + nk;
-  d.wkz = d.wk + nk;
-  d.wkf = reinterpret_cast<float2 *>(d.wkz + nk);
-  d.wkzf = d.wkf + nk;
-  d.colrv = d.wkz + 2 * nk;
+  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (nkp + 3 * nk + 2 * nc)));
+  d.wk = reinterpret_cast<dbl4 *>(d.sk + nkp);
+  d.wkf = reinterpret_cast<float4 *>(d.wk + nk);
+  d.colrv = reinterpret_cast<double2 *>(d.wkf + nk);
   d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
+  // per-slice partials of S(k), summed in slice order
+  if (d.sk_part) cudaFree(d.sk_part);
+  d.sk_part = nullptr;
+  const size_t nslice = ((size_t)d.n + SLICE - 1) / SLICE;
+  if (cudaMalloc(reinterpret_cast<void **>(&d.sk_part), sizeof(double2) * nslice * nk) !=
+      cudaSuccess) {
+    d.sk_part = nullptr;  // falls back to atomic slice sums
+    cudaGetLastError();
+  }
   // self-energy (forces.f:1426-1447)
   const double ABC = alphad / std::sqrt(PI_REF);
   ctx->spei = 0.0;
@@ -574,38 +640,45 @@ int launch_furir(mdx_ctx *ctx) {
   {
     MDX_TIMER(ctx, MDX_T_EW_SFAC);
     dim3 grid((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
+    const size_t sh = (mx ? sizeof(float2) : sizeof(double2)) * TILE * (d.kx + d.ky + d.kz);
     if (mx) {
-      size_t sh = sizeof(float2) * TILE * (d.kx + d.ky + d.kz);
       k_sfac<float, float2><<<grid, 128, sh, ctx->stream>>>(
-          d.n, nchunk, chunks, d.cols, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky, d.kz, d.sk);
+          d.n, nchunk, chunks, d.cols, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky, d.kz, d.sk,
+          d.sk_part, d.nkv);
     } else {
-      size_t sh = sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
       k_sfac<double, double2><<<grid, 128, sh, ctx->stream>>>(
-          d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk);
+          d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk,
+          d.sk_part, d.nkv);
     }
     MDX_LAUNCHED(ctx);
+    if (d.sk_part) {
+      k_sfac_sum<<<(d.nkv + 255) / 256, 256, 0, ctx->stream>>>(d.nkv, (int)grid.y,
+                                                                d.sk_part, d.sk);
+      MDX_LAUNCHED(ctx);
+    }
   }
   double *qpe = d.red + 40;
   mdx_scalars *sc = d.sc;
   {
     MDX_TIMER(ctx, MDX_T_EW_KTERMS);
-    Dst6 dst{{qpe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
+    Dst6 dst = dst6(ctx, std::min(d.ncol, 1024), 4, qpe, &sc->virx, &sc->viry, &sc->virz);
     k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk, d.wkz,
-        mx ? d.wkf : nullptr, mx ? d.wkzf : nullptr, d.colrv, d.colrvf, dst);
+        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk,
+        mx ? d.wkf : nullptr, d.colrv, d.colrvf, dst);
     MDX_LAUNCHED(ctx);
     k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
     MDX_LAUNCHED(ctx);
   }
   MDX_TIMER(ctx, MDX_T_EW_FORCE);
+  const int kzo = (d.kz - 1) / 2;
+  const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
   if (mx) {
-    k_rforce32<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wkf, d.wkzf, d.tabxf, d.tabyf, d.tabzf, d.colrvf,
-        ctx->fix, d.gfix);
+    k_rforce32<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
+        d.n, d.ncol, d.cols, d.wkf, d.tabxf, d.tabyf, d.tabzf, kzo, d.colrvf, ctx->fix,
+        d.gfix);
   } else {
-    k_rforce64<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wk, d.wkz, d.tabx, d.taby, d.tabz, d.colrv, d.gx, d.gy,
-        d.gz);
+    k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
+        d.n, d.ncol, d.cols, d.wk, d.tabx, d.taby, d.tabz, kzo, d.colrv, d.gx, d.gy, d.gz);
   }
   MDX_LAUNCHED(ctx);
   return MDX_OK;
@@ -621,7 +694,7 @@ int launch_eterms(mdx_ctx *ctx) {
   k_eterms_init<<<1, 1, 0, ctx->stream>>>(d.sc, se, ctx->d.ntypes);
   MDX_LAUNCHED(ctx);
   mdx_scalars *sc = d.sc;
-  Dst6 dst{{&sc->spe, &sc->virx, &sc->viry, &sc->virz, nullptr, nullptr}};
+  Dst6 dst = dst6(ctx, (d.n + 127) / 128, 4, &sc->spe, &sc->virx, &sc->viry, &sc->virz);
   k_eterms<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
       d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc,
       ctx->p.coulf, ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy,

@@ -221,7 +221,8 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
                          int ntypes, const double *__restrict__ massdi,
                          const double *__restrict__ vx,
                          const double *__restrict__ vy,
-                         const double *__restrict__ vz, double *ekacc) {
+                         const double *__restrict__ vz, double *ekacc,
+                         double *part, unsigned *ctr) {
   double e[MDX_NT + 4];
 #pragma unroll
   for (int k = 0; k < MDX_NT + 4; ++k) e[k] = 0.0;
@@ -242,19 +243,10 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
     for (int k = 0; k < MDX_NT; ++k)
       if (k == t) e[k] += 0.5 * VSC;
   }
-  // block reduction of MDX_NT+4 values
-  __shared__ double sh[32][MDX_NT + 4];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double *dst[MDX_NT + 4];
 #pragma unroll
-  for (int k = 0; k < MDX_NT + 4; ++k) e[k] = warp_sum(e[k]);
-  if (lane == 0)
-    for (int k = 0; k < MDX_NT + 4; ++k) sh[wid][k] = e[k];
-  __syncthreads();
-  if (threadIdx.x < MDX_NT + 4) {
-    double s = 0.0;
-    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
-    if (threadIdx.x < ntypes || threadIdx.x >= MDX_NT) atomicAdd(&ekacc[threadIdx.x], s);
-  }
+  for (int k = 0; k < MDX_NT + 4; ++k) dst[k] = (k < ntypes || k >= MDX_NT) ? ekacc + k : nullptr;
+  block_add_core<MDX_NT + 4>(e, dst, part, ctr);
 }
 
 // Device scratch of SCALING between stages.
@@ -666,7 +658,7 @@ __global__ void k_shejk(int nop, const int *__restrict__ mol_first,
                         const double *__restrict__ oy,
                         const double *__restrict__ oz, double *fx, double *fy,
                         double *fz, double bx, double by, double bz,
-                        mdx_thermo *th, int *err) {
+                        mdx_thermo *th, int *err, Dst6 vdst) {
   double vir[3] = {0, 0, 0};
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   int iter_out = 0;
@@ -758,8 +750,7 @@ __global__ void k_shejk(int nop, const int *__restrict__ mol_first,
       }
     }
   }
-  double *dst[3] = {&th->viran[0], &th->viran[1], &th->viran[2]};
-  block_add<3>(vir, dst);
+  block_add<3>(vir, vdst);
   if (iter_out > 0) atomicMax(&th->shake_iter_max, iter_out);
 }
 
@@ -856,7 +847,8 @@ static int stage(mdx_ctx *ctx, int st) {
 int launch_getemp(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   k_getemp<<<160, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), ctx->d.ntypes,
-                                         d.massdi, d.vx, d.vy, d.vz, scratch(ctx)->ekacc);
+                                         d.massdi, d.vx, d.vy, d.vz, scratch(ctx)->ekacc,
+                                         d.red_part, d.red_ctr);
   MDX_LAUNCHED(ctx);
   return stage(ctx, ST_GETEMP);
 }
@@ -1060,7 +1052,8 @@ int launch_leapfrog_shake(mdx_ctx *ctx) {
     k_shejk<<<(d.nop + 63) / 64, 64, 0, ctx->stream>>>(
         d.nop, d.mol_first, d.mol_nat, d.mol_type, move_const(ctx), sk, d.bib, d.bjb,
         d.bid, d.brb, d.massdi, d.pos, d.vx, d.vy, d.vz, d.ox, d.oy, d.oz, d.fx, d.fy,
-        d.fz, ctx->boxl, ctx->boyl, ctx->bozl, d.th, d.err);
+        d.fz, ctx->boxl, ctx->boyl, ctx->bozl, d.th, d.err,
+        dst6(ctx, (d.nop + 63) / 64, 3, &d.th->viran[0], &d.th->viran[1], &d.th->viran[2]));
     MDX_LAUNCHED(ctx);
   }
   return MDX_OK;

@@ -162,6 +162,8 @@ void set_fix_scales(mdx_ctx *ctx) {
   ctx->fix.inv = 1.0 / fs;
   ctx->fix.escale = es;
   ctx->fix.einv = 1.0 / es;
+  ctx->fix.scalef = (float)fs;
+  ctx->fix.escalef = (float)es;
 }
 
 int require(mdx_ctx *ctx, bool topo, bool par, bool state) {
@@ -178,7 +180,7 @@ int do_fforces(mdx_ctx *ctx, int laver, bool split) {
   RC(launch_zero_fast(ctx));
   if (ctx->mixed()) RC(launch_mirror_f32(ctx));
   RC(launch_localf(ctx, split));
-  if (!ctx->mixed()) RC(launch_wir(ctx, 1));
+  RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
   RC(launch_bonded(ctx, laver));
   if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
   RC(launch_sclfrc(ctx, 1));
@@ -213,7 +215,7 @@ int do_allforce(mdx_ctx *ctx, bool split) {
   RC(launch_zero_slow(ctx));
   if (ctx->mixed()) RC(launch_mirror_f32(ctx));
   RC(launch_localf(ctx, split));
-  if (!ctx->mixed()) RC(launch_wir(ctx, 1));
+  RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
   RC(launch_bonded(ctx, split ? 1 : 0));
   if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
   RC(do_slow_parts(ctx, split));
@@ -439,6 +441,9 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
   AL(d.err, 4);
   AL(d.shake_iter, 32);
   AL(d.red, 512);
+  AL(d.red_part, (size_t)1 << 21);
+  AL(d.red_ctr, 8);
+  d.red_cap = (size_t)1 << 21;
   if (!rc) {
     unsigned char *ss = nullptr;
     rc = dmalloc(ctx, &ss, scal_scratch_bytes());
@@ -481,7 +486,8 @@ int mdx_close(mdx_ctx *ctx) {
                   d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.tabx, d.tabxf, d.sk, d.sc, d.th,
-                  d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d};
+                  d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
+                  d.red_part, d.red_ctr, d.sk_part};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -521,6 +527,8 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
     tc.ipot[k] = t->ipot[k];
     tc.c14el[k] = t->c14el[k];
     tc.c14lj[k] = t->c14lj[k];
+    tc.c14elf[k] = (float)t->c14el[k];
+    tc.c14ljf[k] = (float)t->c14lj[k];
     for (int j = 0; j < nt; ++j) tc.mdx[k][j] = t->mdx[(size_t)k + (size_t)j * t->ld_mdx] - 1;
     ctx->nspec[k] = t->nspec[k];
     ctx->nsits[k] = t->nsits[k];

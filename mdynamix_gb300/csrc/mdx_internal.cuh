@@ -55,6 +55,8 @@ struct TypeConst {
   int ipot[MDX_NT];
   double c14el[MDX_NT];
   double c14lj[MDX_NT];
+  float c14elf[MDX_NT];
+  float c14ljf[MDX_NT];
   int mdx[MDX_NT][MDX_NT];  // 0-based type pair index
 };
 
@@ -82,11 +84,15 @@ struct KCol {
 struct FixScale {
   double scale, inv;    // forces
   double escale, einv;  // energies and virials
+  float scalef, escalef;  // the same scales as FP32 (powers of two: exact)
 };
 
-// Destination pointers of a block reduction, passed by value to kernels.
+// Destination pointers of a block reduction, passed by value to kernels,
+// with the partials buffer and counter of the deterministic reduction.
 struct Dst6 {
   double *p[6];
+  double *part;
+  unsigned *ctr;
 };
 
 struct DevData {
@@ -126,15 +132,15 @@ struct DevData {
   double *br, *be, *ar, *ae, *tr, *te;
   // SHAKE (per type: first bond record, bond count)
   // Ewald
-  int nkv, ncol, kx, ky, kz;  // kx,ky,kz: table lengths (max |n| + 1)
+  int nkv, ncol, kx, ky, kz;  // table rows: kx = KMAX+1, ky = KMAY+1, kz = 2 KMAZ+1
   KCol *cols;
   void *kchunks;                // column chunks of the S(k) kernel
   int nchunk;
-  double2 *tabx, *taby, *tabz;  // [atom][n]
+  double2 *tabx, *taby, *tabz;  // [n][atom]; z rows are n = -KMAZ..KMAZ
   float2 *tabxf, *tabyf, *tabzf;
   double2 *sk;                  // structure factors, column order
-  double2 *wk, *wkz;            // AK2*conj(S), kz*AK2*conj(S)
-  float2 *wkf, *wkzf;           // FP32 copies for the mixed force pass
+  dbl4 *wk;                     // (W, RZV W) per k, W = AK2*conj(S)
+  float4 *wkf;                  // FP32 copy for the mixed force pass
   double2 *colrv;               // per column (RXV, RYV) at the current box
   float2 *colrvf;
   double *kscal;                // per-k scratch of the energy/virial kernel
@@ -148,6 +154,11 @@ struct DevData {
   double *red;       // reduction scratch
   void *scal_scratch;  // SCALING stage scratch (integrate.cu)
   int *nspec_d;        // NSPEC per type
+  double *red_part;    // per-block partials of the deterministic reductions
+  unsigned *red_ctr;
+  size_t red_cap;      // doubles in red_part
+  double2 *sk_part;    // per-slice S(k) partials (deterministic slice sum)
+  size_t sk_part_cap;
 };
 
 struct mdx_ctx {
@@ -213,6 +224,20 @@ struct mdx_ctx {
     return e;
   }
 };
+
+// Reduction destinations for a launch of nblocks blocks reducing nv values:
+// deterministic (partials + ordered sum) whenever the partials buffer is
+// large enough.
+inline Dst6 dst6(const mdx_ctx *ctx, size_t nblocks, int nv, double *a,
+                 double *b = nullptr, double *c = nullptr, double *d = nullptr,
+                 double *e = nullptr, double *f = nullptr) {
+  Dst6 r{{a, b, c, d, e, f}, nullptr, nullptr};
+  if (ctx->dv.red_part && nblocks * (size_t)nv <= ctx->dv.red_cap) {
+    r.part = ctx->dv.red_part;
+    r.ctr = ctx->dv.red_ctr;
+  }
+  return r;
+}
 
 // Brackets the launches of one scope with CUDA events when timers are on.
 struct TimerScope {
@@ -292,11 +317,19 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
-// Block-wide sum of NV doubles into dst with one atomicAdd per value per
-// block.  All threads of the block must call it.
+// Block-wide sum of NV doubles added to *dst[k] (null pointers skipped).  All
+// threads of the block must call it.
+//
+// With a partials buffer the result is deterministic: every block stores its
+// totals at part[block * NV + k], and the last block to finish (counted on
+// *ctr) sums the partials in block order and adds once to dst, then resets
+// the counter for the next launch on the stream.  Without one, each block
+// adds with atomicAdd (order-dependent in the last bit).
 template <int NV>
-__device__ __forceinline__ void block_add(double (&v)[NV], double *const *dst) {
+__device__ __forceinline__ void block_add_core(double (&v)[NV], double *const *dst,
+                                               double *part, unsigned *ctr) {
   __shared__ double sh[32][NV];
+  __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -306,15 +339,57 @@ __device__ __forceinline__ void block_add(double (&v)[NV], double *const *dst) {
     for (int k = 0; k < NV; ++k) sh[wid][k] = v[k];
   }
   __syncthreads();
+  const unsigned nblk = gridDim.x * gridDim.y;
+  const unsigned blin = blockIdx.y * gridDim.x + blockIdx.x;
   if (wid == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       double t = lane < nw ? sh[lane][k] : 0.0;
       t = warp_sum(t);
-      if (lane == 0 && dst[k]) atomicAdd(dst[k], t);
+      if (lane == 0) {
+        if (part)
+          part[(size_t)blin * NV + k] = t;
+        else if (dst[k])
+          atomicAdd(dst[k], t);
+      }
+    }
+    if (part && lane == 0) {
+      __threadfence();
+      last = atomicAdd(ctr, 1u) == nblk - 1;
     }
   }
   __syncthreads();
+  if (part && last && wid == 0) {
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0.0;
+      for (unsigned b = lane; b < nblk; b += 32) t += __ldcg(&part[(size_t)b * NV + k]);
+      t = warp_sum(t);
+      if (lane == 0 && dst[k]) *dst[k] += t;
+    }
+    if (lane == 0) *ctr = 0u;
+  }
+  __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ void block_add(double (&v)[NV], const Dst6 &d) {
+  block_add_core<NV>(v, d.p, d.part, d.ctr);
+}
+
+// Round-to-nearest float -> 64-bit integer from FP32 and 32-bit conversions
+// only (on this GPU the 64-bit conversion instructions issue on the narrow
+// FP64 pipe).  |y| = hi * 2^32 + lo with hi = floor(|y| 2^-32); the
+// subtraction is exact because lo is made of the low mantissa bits of |y|.
+// Equal to __float2ll_rn(y) for |y| < 2^63.
+__device__ __forceinline__ long long f2ll_rn(float y) {
+  const float a = fabsf(y);
+  const float hf = floorf(a * 2.3283064365386963e-10f);
+  const unsigned hi = __float2uint_rz(hf);
+  const unsigned lo = __float2uint_rn(fmaf(-hf, 4294967296.0f, a));
+  const long long r = (long long)(((unsigned long long)hi << 32) + lo);
+  return y < 0.f ? -r : r;
 }
 
 // Fixed-point force accumulation of the mixed path: two's complement in an

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) k_pair64(
       atomicAdd(&fz[i], fiz);
     }
   }
-  block_add<6>(acc, dst.p);
+  block_add<6>(acc, dst);
   if (SPLIT) {
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x)
@@ -204,7 +204,7 @@ __global__ void k_wir(int n, const dbl4 *__restrict__ pos,
                       const int4 *__restrict__ ainfo, const double *__restrict__ X,
                       const double *__restrict__ Y, const double *__restrict__ Z,
                       const double *__restrict__ fx, const double *__restrict__ fy,
-                      const double *__restrict__ fz, double *dst) {
+                      const double *__restrict__ fz, Dst6 dst) {
   double w[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -212,8 +212,27 @@ __global__ void k_wir(int n, const dbl4 *__restrict__ pos,
     const int m = ainfo[i].y;
     w[0] = w[0] - fx[i] * (p.x - X[m]) - fy[i] * (p.y - Y[m]) - fz[i] * (p.z - Z[m]);
   }
-  double *d[1] = {dst};
-  block_add<1>(w, d);
+  block_add<1>(w, dst);
+}
+
+// WIRSS on the mixed path: the short-row sweep has just stored the pair
+// forces as fixed point; the bonded terms have not been added yet.
+__global__ void k_wir_fix(int n, const dbl4 *__restrict__ pos,
+                          const int4 *__restrict__ ainfo, const double *__restrict__ X,
+                          const double *__restrict__ Y, const double *__restrict__ Z,
+                          const unsigned long long *__restrict__ f, double inv,
+                          Dst6 dst) {
+  double w[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const dbl4 p = pos[i];
+    const int m = ainfo[i].y;
+    const double fx = (double)(long long)f[i] * inv;
+    const double fy = (double)(long long)f[n + i] * inv;
+    const double fz = (double)(long long)f[2 * n + i] * inv;
+    w[0] = w[0] - fx * (p.x - X[m]) - fy * (p.y - Y[m]) - fz * (p.z - Z[m]);
+  }
+  block_add<1>(w, dst);
 }
 
 // ---------------------------------------------------------------- mixed ---
@@ -267,9 +286,9 @@ __global__ void __launch_bounds__(256) k_pair32(
       float QIJ, A6, B12, RAE = 0.f;
       if (same) {
         if (is14) {
-          QIJ = qsi * qsitef[j] * coulf * (float)tc.c14el[ti];
-          A6 = __ldg(&tb.a614f[tix]) * (float)tc.c14lj[ti];
-          B12 = __ldg(&tb.b1214f[tix]) * (float)tc.c14lj[ti];
+          QIJ = qsi * qsitef[j] * coulf * tc.c14elf[ti];
+          A6 = __ldg(&tb.a614f[tix]) * tc.c14ljf[ti];
+          B12 = __ldg(&tb.b1214f[tix]) * tc.c14ljf[ti];
         } else {
           QIJ = qsi * qsitef[j] * coulf;
           A6 = __ldg(&tb.a60f[tix]);
@@ -361,9 +380,10 @@ __global__ void __launch_bounds__(256) k_pair32(
       fza += FORCE * DZ;
     }
     // forces: lane partials -> fixed point -> integer warp sum -> one store
-    long long qx = __float2ll_rn(fxa * (float)fsc.scale);
-    long long qy = __float2ll_rn(fya * (float)fsc.scale);
-    long long qz = __float2ll_rn(fza * (float)fsc.scale);
+    // (no 64-bit conversion instruction: those issue on the FP64 pipe)
+    long long qx = f2ll_rn(fxa * fsc.scalef);
+    long long qy = f2ll_rn(fya * fsc.scalef);
+    long long qz = f2ll_rn(fza * fsc.scalef);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       qx += __shfl_xor_sync(0xffffffffu, qx, o);
@@ -374,20 +394,11 @@ __global__ void __launch_bounds__(256) k_pair32(
       ffix[i] = (unsigned long long)qx;
       ffix[n + i] = (unsigned long long)qy;
       ffix[2 * n + i] = (unsigned long long)qz;
-      if (SHORT) {
-        // WIRSS needs the pair force on the atom (forces.f:991-995)
-        const dbl4 p = pos[i];
-        const double inv = fsc.inv;
-        const double w = -(double)qx * inv * (p.x - X[mi]) -
-                         (double)qy * inv * (p.y - Y[mi]) -
-                         (double)qz * inv * (p.z - Z[mi]);
-        tot[P_WIR] = __double2ll_rn(w * escale);
-      }
     }
 #pragma unroll
     for (int k = 0; k < P_WIR; ++k) {
       float t = warp_sumf(a[k]);
-      if (lane == 0) tot[k] = __float2ll_rn(t * (float)escale);
+      if (lane == 0) tot[k] = f2ll_rn(t * fsc.escalef);
     }
   }
   // block sum of the integer slots, one atomic per slot per block
@@ -482,8 +493,8 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
   if (!ctx->mixed()) {
     double *fx = shrt ? d.hx : d.gx, *fy = shrt ? d.hy : d.gy, *fz = shrt ? d.hz : d.gz;
     mdx_scalars *sc = d.sc;
-    Dst6 ddst = shrt ? Dst6{{&sc->pels2, &sc->pe2, &sc->vir2, &sc->virfx, &sc->virfy, &sc->virfz}}
-                     : Dst6{{&sc->pels1, &sc->pe1, &sc->vir1, &sc->virx, &sc->viry, &sc->virz}};
+    Dst6 ddst = shrt ? dst6(ctx, grid, 6, &sc->pels2, &sc->pe2, &sc->vir2, &sc->virfx, &sc->virfy, &sc->virfz)
+                     : dst6(ctx, grid, 6, &sc->pels1, &sc->pe1, &sc->vir1, &sc->virx, &sc->viry, &sc->virz);
 #define LP64(S, P)                                                                \
   k_pair64<S, P><<<grid, T, 0, ctx->stream>>>(                                    \
       d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
@@ -535,9 +546,16 @@ int launch_wir(mdx_ctx *ctx, int which) {
   MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   double *dst = which == 1 ? &d.sc->wirss : &d.sc->wirs;
+  if (which == 1 && ctx->mixed()) {
+    k_wir_fix<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, d.hfix,
+                                            ctx->fix.inv, dst6(ctx, 160, 1, dst));
+    MDX_LAUNCHED(ctx);
+    return MDX_OK;
+  }
   const double *fx = which == 1 ? d.hx : d.gx, *fy = which == 1 ? d.hy : d.gy,
                *fz = which == 1 ? d.hz : d.gz;
-  k_wir<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz, dst);
+  k_wir<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz,
+                                      dst6(ctx, 160, 1, dst));
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
