@@ -41,8 +41,8 @@ WORKLOAD = dict(workload="SPC-FW water 32768 molecules (98304 atoms), DOUBLE 0.2
 
 # Algorithmic work per unit of each kernel group (frozen).
 OPS_PAIR = 80            # per listed pair evaluation
-OPS_EW_SFAC = 11         # per (k, atom) term, structure-factor pass
-OPS_EW_FORCE = 10        # per (k, atom) term, force pass
+OPS_EW_SFAC = 8          # per (k, atom) term, structure-factor pass (4 FMA)
+OPS_EW_FORCE = 16        # per (k, atom) term, force pass (8 FMA)
 
 
 def env_rank():

@@ -54,6 +54,21 @@ __device__ __forceinline__ C2 conj_if(C2 v, bool neg) {
   return v;
 }
 
+// Asynchronous global -> shared copies (8 bytes), grouped per staged tile.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait1() {
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait0() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Phase tables: thread per (axis, atom), FP64 recurrence from one sincos.
 __global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
                          double iby, double ibz, int kx, int ky, int kz,
@@ -107,7 +122,7 @@ __global__ void __launch_bounds__(128) k_sfac(
   const int ch = blockIdx.x * blockDim.x + threadIdx.x;
   const int a0 = blockIdx.y * SLICE, a1 = min(n, a0 + SLICE);
   Chunk cc{0, 0, 0, 0};
-  KCol col{0, 0, 0, 0, 0};
+  KCol col{0, 0, 0, 0, 0, 0};
   if (ch < nchunk) {
     cc = chunks[ch];
     col = cols[cc.col];
@@ -167,6 +182,126 @@ __global__ void __launch_bounds__(128) k_sfac(
   }
 }
 
+// Mixed S(k) pass.  A work item is (column group, window of SCH nz starting
+// at t0 within the group's range); a thread accumulates 4 columns x SCH nz in
+// FP32 registers over one slice of atoms, staged TILE at a time in shared
+// memory as one row per atom: X(0..KMAX), Y(0..KMAY), Z(-KMAZ..KMAZ) and SCH
+// zeros (windows past KMAZ and padding columns read zeros).  Tiles are double
+// buffered: the next tile's cp.async copies run under this tile's FMAs.  Items are sorted
+// by absolute nz window so the lanes of a warp mostly read the same z entries
+// (shared-memory broadcast).  The slice length is chosen on the host so the
+// grid is one full wave of resident blocks.
+constexpr int SCH = 8;
+struct SItem {
+  int g, t0;
+};
+
+__global__ void __launch_bounds__(128, 3) k_sfac32(
+    int n, int nitem, const SItem *__restrict__ items, const KGroup *__restrict__ groups,
+    const KCol *__restrict__ cols, const float2 *__restrict__ tab, int kx, int ky, int kz,
+    int slice, double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
+  // tab: the X, Y and Z tables back to back, row r at tab + r * n
+  extern __shared__ float2 srow[];  // [2][TILE][kx + ky + kz + SCH], double buffer
+  const int zpad = kx + ky + kz;    // first zero entry of a row
+  const int rowlen = zpad + SCH;
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a0 = blockIdx.y * slice, a1 = min(n, a0 + slice);
+  const bool active = it < nitem;
+  int xo[KGRP], yo[KGRP];
+  unsigned ysg[KGRP];  // sign bit flips Im Y for ny < 0
+  int zo = 0;
+  {
+    const SItem si = active ? items[it] : SItem{0, 0};
+    const KGroup &G = groups[si.g];
+#pragma unroll
+    for (int c = 0; c < KGRP; ++c) {
+      const int ci = active ? G.col[c] : -1;
+      const KCol col = ci >= 0 ? cols[ci] : KCol{0, 0, 0, 0, 0, 0};
+      xo[c] = ci >= 0 ? col.nx : zpad;  // padding column: X = 0
+      yo[c] = kx + (col.ny < 0 ? -col.ny : col.ny);
+      ysg[c] = col.ny < 0 ? 0x80000000u : 0u;
+    }
+    zo = kx + ky + (kz - 1) / 2 + G.nzlo + si.t0;
+  }
+  float ar[KGRP][SCH], ai[KGRP][SCH];
+#pragma unroll
+  for (int c = 0; c < KGRP; ++c)
+#pragma unroll
+    for (int s = 0; s < SCH; ++s) ar[c][s] = ai[c][s] = 0.f;
+  const int bufsz = TILE * rowlen;
+  for (int k = threadIdx.x; k < 2 * TILE * SCH; k += blockDim.x)
+    srow[(k / SCH) * rowlen + zpad + k % SCH] = make_float2(0.f, 0.f);
+  // stage a tile of atoms asynchronously (cp.async, one group per tile)
+  auto stage = [&](int buf, int base) {
+    const int m = min(TILE, a1 - base);
+    float2 *dst = srow + buf * bufsz;
+    for (int k = threadIdx.x; k < m * zpad; k += blockDim.x) {
+      const int r = k / m, j = k - r * m;
+      cp_async8(dst + j * rowlen + r, tab + (size_t)r * n + base + j);
+    }
+  };
+  if (a0 < a1) stage(0, a0);
+  cp_async_commit();
+  int t = 0;
+  for (int base = a0; base < a1; base += TILE, ++t) {
+    if (base + TILE < a1) stage((t + 1) & 1, base + TILE);
+    cp_async_commit();
+    cp_async_wait1();
+    __syncthreads();
+    const int m = min(TILE, a1 - base);
+    if (active) {
+#pragma unroll 1
+      for (int j = 0; j < m; ++j) {
+        const float2 *row = srow + (t & 1) * bufsz + j * rowlen;
+        float tr[KGRP], ti[KGRP];
+#pragma unroll
+        for (int c = 0; c < KGRP; ++c) {
+          const float2 X = row[xo[c]];
+          const float2 Y = row[yo[c]];
+          const float yy = __uint_as_float(__float_as_uint(Y.y) ^ ysg[c]);
+          tr[c] = fmaf(X.x, Y.x, -X.y * yy);
+          ti[c] = fmaf(X.x, yy, X.y * Y.x);
+        }
+        const float2 *zr = row + zo;
+#pragma unroll
+        for (int s = 0; s < SCH; ++s) {
+          const float2 Z = zr[s];
+#pragma unroll
+          for (int c = 0; c < KGRP; ++c) {
+            ar[c][s] = fmaf(tr[c], Z.x, ar[c][s]);
+            ar[c][s] = fmaf(-ti[c], Z.y, ar[c][s]);
+            ai[c][s] = fmaf(tr[c], Z.y, ai[c][s]);
+            ai[c][s] = fmaf(ti[c], Z.x, ai[c][s]);
+          }
+        }
+      }
+    }
+    __syncthreads();  // buffer (t & 1) is restaged two tiles later
+  }
+  cp_async_wait0();
+  if (!active) return;
+  const SItem si = items[it];
+  const KGroup &G = groups[si.g];
+  const int len = min(SCH, G.len - si.t0);
+#pragma unroll
+  for (int c = 0; c < KGRP; ++c) {
+    const int ci = G.col[c];
+    if (ci < 0) continue;
+    const int k0 = cols[ci].koff + si.t0;
+#pragma unroll
+    for (int s = 0; s < SCH; ++s)
+      if (s < len) {
+        const double2 v = make_double2((double)ar[c][s], (double)ai[c][s]);
+        if (part) {  // slice partial, summed in slice order by k_sfac_sum
+          part[(size_t)blockIdx.y * nkv + k0 + s] = v;
+        } else {
+          atomicAdd(&sk[k0 + s].x, v.x);
+          atomicAdd(&sk[k0 + s].y, v.y);
+        }
+      }
+  }
+}
+
 // S(k) = sum of the slice partials in slice order (deterministic).
 __global__ void k_sfac_sum(int nkv, int nslice, const double2 *__restrict__ part,
                            double2 *__restrict__ sk) {
@@ -221,7 +356,7 @@ __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
       W.z = RZV * W.x;
       W.w = RZV * W.y;
       if (wkf)
-        wkf[k] = make_float4((float)W.x, (float)W.y, (float)W.z, (float)W.w);
+        wkf[col.wpos + KGRP * t] = make_float4((float)W.x, (float)W.y, (float)W.z, (float)W.w);
       else
         wk[k] = W;
     }
@@ -315,48 +450,105 @@ __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
   }
 }
 
-__global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce32(
-    int n, int ncol, const KCol *__restrict__ cols, const float4 *__restrict__ wk,
-    const float2 *__restrict__ tx, const float2 *__restrict__ ty,
-    const float2 *__restrict__ tz, int kzo, const float2 *__restrict__ colrv,
-    FixScale fsc, unsigned long long *__restrict__ gfix) {
-  __shared__ long long red[3][RF_PARTS][RF_ATOMS];
-  const int lane = threadIdx.x % RF_ATOMS, part = threadIdx.x / RF_ATOMS;
-  const int i = blockIdx.x * RF_ATOMS + lane;
+// Mixed force pass over column groups.  A block holds RF_APT x 32 atoms (a
+// thread takes atoms lane and lane + 32) and RF_PARTS warps that share the
+// groups out (group p, p + RF_PARTS, ...).  The block's X, Y and Z table rows
+// are staged in shared memory ([row][atom], conflict-free); per nz and atom
+// one z load, and per nz four warp-uniform W loads feed 32 FMAs per atom.
+constexpr int RF_APT = 2;
+constexpr int RF_BATOMS = 32 * RF_APT;
+
+__global__ void __launch_bounds__(32 * RF_PARTS) k_rforce32(
+    int n, int ngroup, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
+    const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
+    const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
+  // tab: the X, Y and Z tables back to back, row r at tab + r * n
+  extern __shared__ float2 srf[];  // [kx + ky + kz][RF_BATOMS]
+  __shared__ long long red[3][RF_PARTS][RF_BATOMS];
+  const int lane = threadIdx.x % 32, part = threadIdx.x / 32;
+  const int i0 = blockIdx.x * RF_BATOMS;
+  const int nrow = kx + ky + kz;
+  for (int k = threadIdx.x; k < nrow * RF_BATOMS; k += blockDim.x) {
+    const int r = k / RF_BATOMS, j = k - r * RF_BATOMS;
+    srf[k] = i0 + j < n ? tab[(size_t)r * n + i0 + j] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
   const float sc = fsc.scalef;
-  long long ax = 0, ay = 0, az = 0;
-  if (i < n) {
-    const float2 *Z = tz + (size_t)kzo * n + i;
-    for (int c = part; c < ncol; c += RF_PARTS) {
-      const KCol col = cols[c];
-      float ux = 0.f, uy = 0.f, vx = 0.f, vy = 0.f;
-      column_sums<float, float4, float2>(Z, n, wk, col, ux, uy, vx, vy);
+  long long ax[RF_APT], ay[RF_APT], az[RF_APT];
+#pragma unroll
+  for (int q = 0; q < RF_APT; ++q) ax[q] = ay[q] = az[q] = 0;
+  const float2 *X = srf + lane;
+  const float2 *Y = X + kx * RF_BATOMS;
+  const float2 *Z = Y + (ky + (kz - 1) / 2) * RF_BATOMS;  // row nz = 0
+  for (int g = part; g < ngroup; g += RF_PARTS) {
+    const KGroup G = groups[g];
+    float u[RF_APT][KGRP][2], v[RF_APT][KGRP][2];
+#pragma unroll
+    for (int q = 0; q < RF_APT; ++q)
+#pragma unroll
+      for (int c = 0; c < KGRP; ++c) u[q][c][0] = u[q][c][1] = v[q][c][0] = v[q][c][1] = 0.f;
+    const float2 *z = Z + G.nzlo * RF_BATOMS;
+    const float4 *w = wg + (size_t)KGRP * G.woff;
+#pragma unroll 2
+    for (int t = 0; t < G.len; ++t) {
+      float2 zz[RF_APT];
+#pragma unroll
+      for (int q = 0; q < RF_APT; ++q) zz[q] = z[t * RF_BATOMS + 32 * q];
+#pragma unroll
+      for (int c = 0; c < KGRP; ++c) {
+        const float4 a = w[KGRP * t + c];
+#pragma unroll
+        for (int q = 0; q < RF_APT; ++q) {
+          u[q][c][0] = fmaf(a.x, zz[q].x, u[q][c][0]);
+          u[q][c][0] = fmaf(-a.y, zz[q].y, u[q][c][0]);
+          u[q][c][1] = fmaf(a.x, zz[q].y, u[q][c][1]);
+          u[q][c][1] = fmaf(a.y, zz[q].x, u[q][c][1]);
+          v[q][c][0] = fmaf(a.z, zz[q].x, v[q][c][0]);
+          v[q][c][0] = fmaf(-a.w, zz[q].y, v[q][c][0]);
+          v[q][c][1] = fmaf(a.z, zz[q].y, v[q][c][1]);
+          v[q][c][1] = fmaf(a.w, zz[q].x, v[q][c][1]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < KGRP; ++c) {
+      if (G.col[c] < 0) continue;
+      const KCol col = cols[G.col[c]];
       const int ny = col.ny < 0 ? -col.ny : col.ny;
-      const float2 T = cmulf(tx[(size_t)col.nx * n + i],
-                             conj_if(ty[(size_t)ny * n + i], col.ny < 0));
-      const float imTU = fmaf(T.x, uy, T.y * ux);
-      const float imTV = fmaf(T.x, vy, T.y * vx);
-      // per-column partials go to 64-bit fixed point (order independent)
-      const float2 rv = colrv[c];
-      ax += f2ll_rn(rv.x * imTU * sc);
-      ay += f2ll_rn(rv.y * imTU * sc);
-      az += f2ll_rn(imTV * sc);
+      const float2 rv = colrv[G.col[c]];
+#pragma unroll
+      for (int q = 0; q < RF_APT; ++q) {
+        const float2 T = cmulf(X[col.nx * RF_BATOMS + 32 * q],
+                               conj_if(Y[ny * RF_BATOMS + 32 * q], col.ny < 0));
+        const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
+        const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
+        // per-column partials go to 64-bit fixed point (order independent)
+        ax[q] += f2ll_rn(rv.x * imTU * sc);
+        ay[q] += f2ll_rn(rv.y * imTU * sc);
+        az[q] += f2ll_rn(imTV * sc);
+      }
     }
   }
-  red[0][part][lane] = ax;
-  red[1][part][lane] = ay;
-  red[2][part][lane] = az;
-  __syncthreads();
-  if (part == 0 && i < n) {
 #pragma unroll
-    for (int p = 1; p < RF_PARTS; ++p) {
-      ax += red[0][p][lane];
-      ay += red[1][p][lane];
-      az += red[2][p][lane];
+  for (int q = 0; q < RF_APT; ++q) {
+    red[0][part][lane + 32 * q] = ax[q];
+    red[1][part][lane + 32 * q] = ay[q];
+    red[2][part][lane + 32 * q] = az[q];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < RF_BATOMS; j += blockDim.x) {
+    const int i = i0 + j;
+    if (i >= n) continue;
+    long long sx = 0, sy = 0, sz = 0;
+#pragma unroll
+    for (int p = 0; p < RF_PARTS; ++p) {
+      sx += red[0][p][j];
+      sy += red[1][p][j];
+      sz += red[2][p][j];
     }
-    gfix[i] += (unsigned long long)ax;
-    gfix[n + i] += (unsigned long long)ay;
-    gfix[2 * n + i] += (unsigned long long)az;
+    gfix[i] += (unsigned long long)sx;
+    gfix[n + i] += (unsigned long long)sy;
+    gfix[2 * n + i] += (unsigned long long)sz;
   }
 }
 
@@ -511,11 +703,41 @@ int host_inifur(mdx_ctx *ctx) {
         return MDX_ERR_UNSUPPORTED;
       }
       const int c = (int)cols.size();
-      cols.push_back(KCol{ix, iy, lo, hi, koff});
+      cols.push_back(KCol{ix, iy, lo, hi, koff, 0});
       for (int z0 = lo; z0 <= hi; z0 += CH)
         chunks.push_back(Chunk{c, z0, std::min(CH, hi - z0 + 1), koff + (z0 - lo)});
       koff += cnt;
     }
+  // column groups of the mixed force pass: columns sorted by nz range (then
+  // by column index), four at a time, the last group of a range padded
+  std::vector<int> order(cols.size());
+  for (size_t c = 0; c < cols.size(); ++c) order[c] = (int)c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return cols[a].nzlo != cols[b].nzlo ? cols[a].nzlo < cols[b].nzlo
+                                        : cols[a].nzhi < cols[b].nzhi;
+  });
+  std::vector<KGroup> groups;
+  int woff = 0;
+  for (size_t p = 0; p < order.size();) {
+    const KCol &c0 = cols[order[p]];
+    KGroup g{c0.nzlo, c0.nzhi - c0.nzlo + 1, woff, 0, {-1, -1, -1, -1}};
+    for (int s = 0; s < KGRP && p < order.size(); ++s) {
+      const KCol &cs = cols[order[p]];
+      if (cs.nzlo != c0.nzlo || cs.nzhi != c0.nzhi) break;
+      g.col[s] = order[p];
+      cols[order[p]].wpos = KGRP * woff + s;
+      ++p;
+    }
+    woff += g.len;
+    groups.push_back(g);
+  }
+  const size_t nwg = (size_t)KGRP * std::max(1, woff);
+  std::vector<SItem> items;
+  for (size_t g = 0; g < groups.size(); ++g)
+    for (int t0 = 0; t0 < groups[g].len; t0 += SCH) items.push_back(SItem{(int)g, t0});
+  std::stable_sort(items.begin(), items.end(), [&](const SItem &a, const SItem &b) {
+    return groups[a.g].nzlo + a.t0 < groups[b.g].nzlo + b.t0;
+  });
   const int kx = KMAX + 1, ky = KMAY + 1, kz = 2 * KMAZ + 1;
   const bool realloc_tables = kx != d.kx || ky != d.ky || kz != d.kz;
   d.kx = kx;
@@ -526,27 +748,63 @@ int host_inifur(mdx_ctx *ctx) {
   ctx->nkv = nkv;
   if (d.cols) cudaFree(d.cols);
   if (d.kchunks) cudaFree(d.kchunks);
+  if (d.kgroups) cudaFree(d.kgroups);
+  if (d.sitems) cudaFree(d.sitems);
   d.cols = nullptr;
   d.kchunks = nullptr;
+  d.kgroups = nullptr;
+  d.sitems = nullptr;
+  MDX_CUDA(cudaMalloc(&d.sitems, sizeof(SItem) * std::max<size_t>(1, items.size())));
+  MDX_CUDA(cudaMemcpy(d.sitems, items.data(), sizeof(SItem) * items.size(),
+                      cudaMemcpyHostToDevice));
+  d.nsitem = (int)items.size();
+  MDX_CUDA(cudaMalloc(&d.kgroups, sizeof(KGroup) * std::max<size_t>(1, groups.size())));
+  MDX_CUDA(cudaMemcpy(d.kgroups, groups.data(), sizeof(KGroup) * groups.size(),
+                      cudaMemcpyHostToDevice));
+  d.ngroup = (int)groups.size();
   MDX_CUDA(cudaMalloc(&d.cols, sizeof(KCol) * std::max<size_t>(1, cols.size())));
   MDX_CUDA(cudaMalloc(&d.kchunks, sizeof(Chunk) * std::max<size_t>(1, chunks.size())));
   MDX_CUDA(cudaMemcpy(d.cols, cols.data(), sizeof(KCol) * cols.size(), cudaMemcpyHostToDevice));
   MDX_CUDA(cudaMemcpy(d.kchunks, chunks.data(), sizeof(Chunk) * chunks.size(),
                       cudaMemcpyHostToDevice));
   d.nchunk = (int)chunks.size();
-  // shared-memory tile of the S(k) kernel: TILE atoms x all table rows
-  const size_t sh = (ctx->mixed() ? sizeof(float2) : sizeof(double2)) * TILE * (kx + ky + kz);
+  // shared-memory tile of the S(k) kernels: TILE atoms x all table rows
+  const size_t sh = ctx->mixed() ? 2 * sizeof(float2) * TILE * (kx + ky + kz + SCH)
+                                 : sizeof(double2) * TILE * (kx + ky + kz);
   if (sh > SFAC_SMEM_MAX) {
     ctx->err = "reciprocal k-set too large for the structure-factor tile";
     return MDX_ERR_UNSUPPORTED;
   }
-  if (sh > 48 * 1024) {
-    if (ctx->mixed())
-      MDX_CUDA(cudaFuncSetAttribute(k_sfac<float, float2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
-    else
-      MDX_CUDA(cudaFuncSetAttribute(k_sfac<double, double2>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  // the dynamic shared memory of the mixed force pass plus its static
+  // reduction buffer must also fit
+  const size_t shr = sizeof(float2) * RF_BATOMS * (kx + ky + kz);
+  if (ctx->mixed() && shr + sizeof(long long) * 3 * RF_PARTS * RF_BATOMS > SFAC_SMEM_MAX) {
+    ctx->err = "reciprocal k-set too large for the force-pass tile";
+    return MDX_ERR_UNSUPPORTED;
+  }
+  // opt in to more than 48 KB of shared memory (set every time: cheap)
+  if (ctx->mixed()) {
+    MDX_CUDA(cudaFuncSetAttribute(k_rforce32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)shr));
+    MDX_CUDA(cudaFuncSetAttribute(k_sfac32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sh));
+  } else {
+    MDX_CUDA(cudaFuncSetAttribute(k_sfac<double, double2>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  }
+  // mixed S(k): slices sized so the grid is one wave of resident blocks
+  size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
+  if (ctx->mixed()) {
+    int nsm = 0, dev = 0, per_sm = 0;
+    MDX_CUDA(cudaGetDevice(&dev));
+    MDX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sfac32, 128, sh));
+    const int nib = std::max(1, ((int)items.size() + 127) / 128);
+    int ns = std::max(1, std::max(1, per_sm) * nsm / nib);
+    ns = std::min(ns, std::max(1, d.n / 128));  // at least 128 atoms a slice
+    d.sfac_slice = (d.n + ns - 1) / ns;
+    d.sfac_nslice = (d.n + d.sfac_slice - 1) / d.sfac_slice;
+    nslice_max = std::max(nslice_max, (size_t)d.sfac_nslice);
   }
   if (realloc_tables) {
     cudaFree(d.tabx);
@@ -568,16 +826,17 @@ int host_inifur(mdx_ctx *ctx) {
   const size_t nk = (size_t)std::max(1, nkv);
   const size_t nkp = (nk + 1) & ~(size_t)1;  // keeps wk 32-byte aligned
   const size_t nc = std::max<size_t>(1, cols.size());
-  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (nkp + 3 * nk + 2 * nc)));
+  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (nkp + 2 * nk + nwg + 2 * nc)));
   d.wk = reinterpret_cast<dbl4 *>(d.sk + nkp);
   d.wkf = reinterpret_cast<float4 *>(d.wk + nk);
-  d.colrv = reinterpret_cast<double2 *>(d.wkf + nk);
+  // padding slots of the grouped W stay zero; k_kterms writes the others
+  MDX_CUDA(cudaMemset(d.wkf, 0, sizeof(float4) * nwg));
+  d.colrv = reinterpret_cast<double2 *>(d.wkf + nwg);
   d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
   // per-slice partials of S(k), summed in slice order
   if (d.sk_part) cudaFree(d.sk_part);
   d.sk_part = nullptr;
-  const size_t nslice = ((size_t)d.n + SLICE - 1) / SLICE;
-  if (cudaMalloc(reinterpret_cast<void **>(&d.sk_part), sizeof(double2) * nslice * nk) !=
+  if (cudaMalloc(reinterpret_cast<void **>(&d.sk_part), sizeof(double2) * nslice_max * nk) !=
       cudaSuccess) {
     d.sk_part = nullptr;  // falls back to atomic slice sums
     cudaGetLastError();
@@ -639,13 +898,16 @@ int launch_furir(mdx_ctx *ctx) {
   MDX_CUDA(cudaMemsetAsync(d.sk, 0, sizeof(double2) * d.nkv, ctx->stream));
   {
     MDX_TIMER(ctx, MDX_T_EW_SFAC);
-    dim3 grid((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
-    const size_t sh = (mx ? sizeof(float2) : sizeof(double2)) * TILE * (d.kx + d.ky + d.kz);
+    const size_t sh = mx ? 2 * sizeof(float2) * TILE * (d.kx + d.ky + d.kz + SCH)
+                         : sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
+    dim3 grid;
     if (mx) {
-      k_sfac<float, float2><<<grid, 128, sh, ctx->stream>>>(
-          d.n, nchunk, chunks, d.cols, d.tabxf, d.tabyf, d.tabzf, d.kx, d.ky, d.kz, d.sk,
-          d.sk_part, d.nkv);
+      grid = dim3((d.nsitem + 127) / 128, d.sfac_nslice);
+      k_sfac32<<<grid, 128, sh, ctx->stream>>>(
+          d.n, d.nsitem, reinterpret_cast<const SItem *>(d.sitems), d.kgroups, d.cols,
+          d.tabxf, d.kx, d.ky, d.kz, d.sfac_slice, d.sk, d.sk_part, d.nkv);
     } else {
+      grid = dim3((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
       k_sfac<double, double2><<<grid, 128, sh, ctx->stream>>>(
           d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk,
           d.sk_part, d.nkv);
@@ -673,9 +935,10 @@ int launch_furir(mdx_ctx *ctx) {
   const int kzo = (d.kz - 1) / 2;
   const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
   if (mx) {
-    k_rforce32<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wkf, d.tabxf, d.tabyf, d.tabzf, kzo, d.colrvf, ctx->fix,
-        d.gfix);
+    const size_t shr = sizeof(float2) * RF_BATOMS * (d.kx + d.ky + d.kz);
+    k_rforce32<<<(d.n + RF_BATOMS - 1) / RF_BATOMS, 32 * RF_PARTS, shr, ctx->stream>>>(
+        d.n, d.ngroup, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf,
+        ctx->fix, d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
         d.n, d.ncol, d.cols, d.wk, d.tabx, d.taby, d.tabz, kzo, d.colrv, d.gx, d.gy, d.gz);

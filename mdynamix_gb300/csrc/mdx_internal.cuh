@@ -77,6 +77,16 @@ struct CellGrid {
 struct KCol {
   int nx, ny, nzlo, nzhi;  // integer k components (rectangular cell)
   int koff;                // first k of the column in the column-ordered list
+  int wpos;                // slot of (nz = nzlo) in the grouped W array
+};
+
+// Four columns with the same nz range, for the mixed force pass: their W
+// values are interleaved (wg[4 (woff + t) + slot]) so one z-table load feeds
+// four columns.  col[s] < 0 marks a padding slot (W = 0).
+constexpr int KGRP = 4;
+struct KGroup {
+  int nzlo, len, woff, pad;
+  int col[KGRP];
 };
 
 // Scratch for fixed-point accumulation of the mixed path: forces are stored
@@ -140,7 +150,12 @@ struct DevData {
   float2 *tabxf, *tabyf, *tabzf;
   double2 *sk;                  // structure factors, column order
   dbl4 *wk;                     // (W, RZV W) per k, W = AK2*conj(S)
-  float4 *wkf;                  // FP32 copy for the mixed force pass
+  float4 *wkf;                  // FP32 copy for the mixed force pass, grouped
+  KGroup *kgroups;              // column groups of the mixed force pass
+  int ngroup;
+  void *sitems;                 // work items of the mixed S(k) pass
+  int nsitem;
+  int sfac_slice, sfac_nslice;  // atoms per slice and slices of that pass
   double2 *colrv;               // per column (RXV, RYV) at the current box
   float2 *colrvf;
   double *kscal;                // per-k scratch of the energy/virial kernel

@@ -1,45 +1,70 @@
 // probe.cu -- measured CUDA-core FMA throughput (FP64 and FP32) of the
 // device, used as the roofline denominator of the FP64 / FP32 pipe-bound
-// kernels.  Eight independent FMA chains per thread, all SMs busy, timed with
-// CUDA events; results are written out so nothing is optimised away.
+// kernels.  Independent FMA chains per thread (8 or 16), 2 to 8 blocks of 256
+// threads per SM, each configuration timed with CUDA events (best of three
+// launches of roughly 10-20 ms); the best configuration is reported.  Results
+// are written out so nothing is optimised away.
 #include "mdx_internal.cuh"
 
 namespace {
 
-template <typename T>
+template <typename T, int NCH>
 __global__ void __launch_bounds__(256) k_fma(int iters, T b, T c, T *out) {
-  T a0 = (T)threadIdx.x, a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
-  T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+  T a[NCH];
+#pragma unroll
+  for (int k = 0; k < NCH; ++k) a[k] = (T)(threadIdx.x + k);
   for (int i = 0; i < iters; ++i) {
-    a0 = a0 * b + c; a1 = a1 * b + c; a2 = a2 * b + c; a3 = a3 * b + c;
-    a4 = a4 * b + c; a5 = a5 * b + c; a6 = a6 * b + c; a7 = a7 * b + c;
+#pragma unroll
+    for (int k = 0; k < NCH; ++k) a[k] = fma(a[k], b, c);
   }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  T s = T(0);
+#pragma unroll
+  for (int k = 0; k < NCH; ++k) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-template <typename T>
-double run(int iters) {
+// One configuration (NCH chains per thread, bps blocks of 256 per SM), best
+// of three timed launches.
+template <typename T, int NCH>
+double run_cfg(int iters, int bps) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = sms * 8, threads = 256;
+  const int blocks = sms * bps, threads = 256;
   T *out = nullptr;
   if (cudaMalloc(&out, sizeof(T) * blocks * threads) != cudaSuccess) return -1.0;
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  k_fma<T><<<blocks, threads>>>(iters / 8, (T)0.999999, (T)1e-7, out);  // warm up
-  cudaEventRecord(a);
-  k_fma<T><<<blocks, threads>>>(iters, (T)0.999999, (T)1e-7, out);
-  cudaEventRecord(b);
-  cudaEventSynchronize(b);
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, a, b);
+  k_fma<T, NCH><<<blocks, threads>>>(iters / 8, (T)0.999999, (T)1e-7, out);  // warm up
+  float ms = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(a);
+    k_fma<T, NCH><<<blocks, threads>>>(iters, (T)0.999999, (T)1e-7, out);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    ms = t < ms ? t : ms;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(out);
-  const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  const double flops = 2.0 * NCH * (double)iters * blocks * threads;
   return flops / (ms * 1e-3) / 1e12;
+}
+
+// The best of a few occupancy / chain-count configurations.
+template <typename T>
+double run(int iters) {
+  double best = -1.0;
+  const int bps[3] = {2, 4, 8};
+  for (int k = 0; k < 3; ++k) {
+    best = fmax(best, run_cfg<T, 8>(iters * 8 / bps[k], bps[k]));
+    best = fmax(best, run_cfg<T, 16>(iters * 4 / bps[k], bps[k]));
+  }
+  return best;
 }
 
 }  // namespace
