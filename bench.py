@@ -39,10 +39,23 @@ WORKLOAD = dict(workload="SPC-FW water 32768 molecules (98304 atoms), DOUBLE 0.2
                 l2="working set > L2 (long rows 266 MB, phase tables 98 MB per step)",
                 list_mode="reference (list at Rc, refresh every 10 long steps)")
 
-# Algorithmic work per unit of each kernel group (frozen).
-OPS_PAIR = 80            # per listed pair evaluation
-OPS_EW_SFAC = 8          # per (k, atom) term, structure-factor pass (4 FMA)
-OPS_EW_FORCE = 16        # per (k, atom) term, force pass (8 FMA)
+# Algorithmic work per unit of each kernel group (frozen constants; an add,
+# sub or mul counts 1, an FMA 2, sqrt / reciprocal / exp / sin / cos 1 each).
+OPS_PAIR = 80            # per listed pair evaluated (forces.f:1071-1198)
+OPS_EW_TERM = 21         # per (k, atom) term, both reciprocal passes (forces.f:1286-1331)
+OPS_EW_K = 20            # per k-vector (energy, virial, W)
+
+# DRAM bytes per long step of the dominant group, from ncu captures of
+# `python bench.py --only {fp64,mixed} --steps 2 --warmup 3`
+# (dram__bytes_read.sum + dram__bytes_write.sum of every launch of the
+# group's kernels in one long step).  None where not captured.
+# fp64 ewald: k_tables 76.2 + k_sfac 165.5 + k_sfac_sum 51.3 + k_kterms 0.4
+#             + k_rforce64 133.4;  mixed: 8.2 + 68.7 + 24.3 + 0.4 + 71.1
+# fp64 pair: 10 x 30.7 (short) + 153.1 (long); mixed: 10 x 36.4 + 280.9
+TRAFFIC_MB = {
+    ("fp64", "ewald"): 426.8, ("mixed", "ewald"): 172.7,
+    ("fp64", "pair"): 460.4, ("mixed", "pair"): 644.6,
+}
 
 
 def env_rank():
@@ -105,25 +118,33 @@ def make_system():
     return s, st
 
 
-def roofline_of(timers, counts, mbsh, mbln, nkv, n, peak64, peak32, mixed):
-    """Dominant kernel group and its achieved throughput against the
-    measured FMA peak of the pipe it is bound by."""
-    ms = {k: v[0] for k, v in timers.items()}
-    top = max(ms, key=ms.get)
-    cnt = max(1, timers[top][1])
-    per_launch_s = ms[top] / cnt * 1e-3
-    work = {"pair_long": OPS_PAIR * mbln, "pair_short": OPS_PAIR * mbsh,
-            "ew_sfac": OPS_EW_SFAC * nkv * n, "ew_force": OPS_EW_FORCE * nkv * n}
-    if top in work:
-        achieved = work[top] / per_launch_s / 1e12
-        peak = peak32 if mixed else peak64
-        return top, {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": None, "kernel": top, "launches": cnt,
-                     "ms_per_launch": per_launch_s * 1e3,
-                     "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak)"}
-    return top, {"bound": "hbm", "achieved": None, "peak": None, "unit": "GB/s", "frac": None,
-                 "traffic": None, "kernel": top}
+def roofline_of(timers, mbsh, mbln, nfreq, nkv, n, peak64, peak32, prec, nsteps):
+    """Roofline of the dominant kernel group of one long step: reciprocal
+    Ewald (phase tables, S(k), per-k terms, forces) or the real-space pair
+    loops (NFREQ short-list passes + one long-list pass).  Ops per long step
+    from the frozen per-unit constants; time from the device timers (CUDA
+    events on the launching stream) of the instrumented pass, per long
+    step; peak = measured FMA throughput of the pipe the path computes on."""
+    ms = {k: v[0] / nsteps for k, v in timers.items()}
+    groups = {
+        "ewald": (ms["ew_tables"] + ms["ew_sfac"] + ms["ew_kterms"] + ms["ew_force"],
+                  OPS_EW_TERM * nkv * n + OPS_EW_K * nkv,
+                  "k_tables + k_sfac + k_sfac_sum + k_kterms + k_rforce"),
+        "pair": (ms["pair_short"] + ms["pair_long"], OPS_PAIR * (nfreq * mbsh + mbln),
+                 "k_pair (short list x NFREQ, long list x 1)"),
+    }
+    top = max(groups, key=lambda g: groups[g][0])
+    t_ms, ops, kernels = groups[top]
+    achieved = ops / (t_ms * 1e-3) / 1e12
+    peak = peak64 if prec == "fp64" else peak32
+    tr = TRAFFIC_MB.get((prec, top))
+    share = t_ms / sum(ms.values())
+    return {"bound": "fp64" if prec == "fp64" else "fp32", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "traffic": tr * 1e6 if tr is not None else None,
+            "kernel": f"{top}: {kernels}", "ms_per_long_step": t_ms, "share_of_step": share,
+            "ops_per_long_step": ops,
+            "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak, of measured)"}
 
 
 def run_gpu(args, rank, world, local):
@@ -214,7 +235,7 @@ def run_gpu(args, rank, world, local):
     import ctypes
     return dict(rec_bytes=ctypes.sizeof(MdxStepRecord), out=out, n=n, mbsh=mbsh, mbln=mbln, ferr=ferr, ferr_max=ferr_max,
                 e2e_s=e2e_s, e2e_steps=ke, peak64=peak64, peak32=peak32, dist=dist,
-                nkv=s.kvector_count())
+                nkv=s.kvector_count(), nfreq=s.spec.nfreq)
 
 
 def cpu_baseline(s, st, threads, budget_s=40.0):
@@ -290,10 +311,11 @@ def main():
     o64, o32 = r["out"]["fp64"], r["out"]["mixed"]
     v64 = world * n * args.steps / (o64["ms"] * 1e-3)
     v32 = world * n * args.steps / (o32["ms"] * 1e-3)
-    top, roof = roofline_of(o64["timers"], None, r["mbsh"], r["mbln"], r["nkv"], n,
-                            r["peak64"], r["peak32"], mixed=False)
-    top32, roof32 = roofline_of(o32["timers"], None, r["mbsh"], r["mbln"], r["nkv"], n,
-                                r["peak64"], r["peak32"], mixed=True)
+    nfreq = r["nfreq"]
+    roof = roofline_of(o64["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
+                       r["peak64"], r["peak32"], "fp64", args.steps)
+    roof32 = roofline_of(o32["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
+                         r["peak64"], r["peak32"], "mixed", args.steps)
     cpu = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()

@@ -451,20 +451,35 @@ __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
 }
 
 // Mixed force pass over column groups.  A block holds RF_APT x 32 atoms (a
-// thread takes atoms lane and lane + 32) and RF_PARTS warps that share the
-// groups out (group p, p + RF_PARTS, ...).  The block's X, Y and Z table rows
-// are staged in shared memory ([row][atom], conflict-free); per nz and atom
-// one z load, and per nz four warp-uniform W loads feed 32 FMAs per atom.
+// thread takes atoms lane and lane + 32) and RF_PARTS warps; warp p takes the
+// contiguous group range [parts.g[p], parts.g[p+1]) whose W records are
+// contiguous too.  The block's X, Y and Z table rows are staged in shared
+// memory ([row][atom], conflict-free).  Each warp streams its W records
+// through a two-batch shared-memory ring with cp.async (RF_WB records a
+// batch, one 16-byte copy per lane), so W latency hides under the FMAs of
+// the previous batch.  Per nz and atom one z load; per nz four broadcast W
+// loads feed 32 FMAs per atom.
 constexpr int RF_APT = 2;
 constexpr int RF_BATOMS = 32 * RF_APT;
+constexpr int RF_WB = 32 / KGRP;  // W records per batch (one float4 per lane)
+struct RfParts {
+  int g[RF_PARTS + 1];
+};
+static_assert(RF_PARTS + 1 <= 8, "DevData::rf_parts holds 8 entries");
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 
 __global__ void __launch_bounds__(32 * RF_PARTS) k_rforce32(
-    int n, int ngroup, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
+    int n, RfParts parts, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
     const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
     const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
   // tab: the X, Y and Z tables back to back, row r at tab + r * n
   extern __shared__ float2 srf[];  // [kx + ky + kz][RF_BATOMS]
   __shared__ long long red[3][RF_PARTS][RF_BATOMS];
+  __shared__ float4 ring[RF_PARTS][2][RF_WB * KGRP];
   const int lane = threadIdx.x % 32, part = threadIdx.x / 32;
   const int i0 = blockIdx.x * RF_BATOMS;
   const int nrow = kx + ky + kz;
@@ -480,54 +495,76 @@ __global__ void __launch_bounds__(32 * RF_PARTS) k_rforce32(
   const float2 *X = srf + lane;
   const float2 *Y = X + kx * RF_BATOMS;
   const float2 *Z = Y + (ky + (kz - 1) / 2) * RF_BATOMS;  // row nz = 0
-  for (int g = part; g < ngroup; g += RF_PARTS) {
-    const KGroup G = groups[g];
-    float u[RF_APT][KGRP][2], v[RF_APT][KGRP][2];
+  const int gs = parts.g[part], ge = parts.g[part + 1];
+  if (gs < ge) {
+    const int rs = groups[gs].woff;
+    const int re = groups[ge - 1].woff + groups[ge - 1].len;
+    float4 *wr = &ring[part][0][0];
+    // lane copies component lane % KGRP of record (batch start + lane / KGRP)
+    auto issue = [&](int buf, int rec0) {
+      const int rec = rec0 + lane / KGRP;
+      if (rec < re) cp_async16(wr + buf * RF_WB * KGRP + lane, wg + (size_t)KGRP * rec + lane % KGRP);
+    };
+    issue(0, rs);
+    cp_async_commit();
+    int r = rs, next = rs + RF_WB;
+    for (int g = gs; g < ge; ++g) {
+      const KGroup G = groups[g];
+      float u[RF_APT][KGRP][2], v[RF_APT][KGRP][2];
 #pragma unroll
-    for (int q = 0; q < RF_APT; ++q)
+      for (int q = 0; q < RF_APT; ++q)
 #pragma unroll
-      for (int c = 0; c < KGRP; ++c) u[q][c][0] = u[q][c][1] = v[q][c][0] = v[q][c][1] = 0.f;
-    const float2 *z = Z + G.nzlo * RF_BATOMS;
-    const float4 *w = wg + (size_t)KGRP * G.woff;
-#pragma unroll 2
-    for (int t = 0; t < G.len; ++t) {
-      float2 zz[RF_APT];
+        for (int c = 0; c < KGRP; ++c) u[q][c][0] = u[q][c][1] = v[q][c][0] = v[q][c][1] = 0.f;
+      const float2 *z = Z + G.nzlo * RF_BATOMS;
+      for (int t = 0; t < G.len; ++t, ++r) {
+        const int q8 = r - rs;
+        if (q8 % RF_WB == 0) {  // batch boundary: this batch landed, prefetch the next
+          cp_async_wait0();
+          __syncwarp();
+          if (next < re) issue((q8 / RF_WB + 1) & 1, next);
+          cp_async_commit();
+          next += RF_WB;
+        }
+        const float4 *w = wr + (((q8 / RF_WB) & 1) * RF_WB + q8 % RF_WB) * KGRP;
+        float2 zz[RF_APT];
 #pragma unroll
-      for (int q = 0; q < RF_APT; ++q) zz[q] = z[t * RF_BATOMS + 32 * q];
+        for (int q = 0; q < RF_APT; ++q) zz[q] = z[t * RF_BATOMS + 32 * q];
+#pragma unroll
+        for (int c = 0; c < KGRP; ++c) {
+          const float4 a = w[c];
+#pragma unroll
+          for (int q = 0; q < RF_APT; ++q) {
+            u[q][c][0] = fmaf(a.x, zz[q].x, u[q][c][0]);
+            u[q][c][0] = fmaf(-a.y, zz[q].y, u[q][c][0]);
+            u[q][c][1] = fmaf(a.x, zz[q].y, u[q][c][1]);
+            u[q][c][1] = fmaf(a.y, zz[q].x, u[q][c][1]);
+            v[q][c][0] = fmaf(a.z, zz[q].x, v[q][c][0]);
+            v[q][c][0] = fmaf(-a.w, zz[q].y, v[q][c][0]);
+            v[q][c][1] = fmaf(a.z, zz[q].y, v[q][c][1]);
+            v[q][c][1] = fmaf(a.w, zz[q].x, v[q][c][1]);
+          }
+        }
+      }
 #pragma unroll
       for (int c = 0; c < KGRP; ++c) {
-        const float4 a = w[KGRP * t + c];
+        if (G.col[c] < 0) continue;
+        const KCol col = cols[G.col[c]];
+        const int ny = col.ny < 0 ? -col.ny : col.ny;
+        const float2 rv = colrv[G.col[c]];
 #pragma unroll
         for (int q = 0; q < RF_APT; ++q) {
-          u[q][c][0] = fmaf(a.x, zz[q].x, u[q][c][0]);
-          u[q][c][0] = fmaf(-a.y, zz[q].y, u[q][c][0]);
-          u[q][c][1] = fmaf(a.x, zz[q].y, u[q][c][1]);
-          u[q][c][1] = fmaf(a.y, zz[q].x, u[q][c][1]);
-          v[q][c][0] = fmaf(a.z, zz[q].x, v[q][c][0]);
-          v[q][c][0] = fmaf(-a.w, zz[q].y, v[q][c][0]);
-          v[q][c][1] = fmaf(a.z, zz[q].y, v[q][c][1]);
-          v[q][c][1] = fmaf(a.w, zz[q].x, v[q][c][1]);
+          const float2 T = cmulf(X[col.nx * RF_BATOMS + 32 * q],
+                                 conj_if(Y[ny * RF_BATOMS + 32 * q], col.ny < 0));
+          const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
+          const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
+          // per-column partials go to 64-bit fixed point (order independent)
+          ax[q] += f2ll_rn(rv.x * imTU * sc);
+          ay[q] += f2ll_rn(rv.y * imTU * sc);
+          az[q] += f2ll_rn(imTV * sc);
         }
       }
     }
-#pragma unroll
-    for (int c = 0; c < KGRP; ++c) {
-      if (G.col[c] < 0) continue;
-      const KCol col = cols[G.col[c]];
-      const int ny = col.ny < 0 ? -col.ny : col.ny;
-      const float2 rv = colrv[G.col[c]];
-#pragma unroll
-      for (int q = 0; q < RF_APT; ++q) {
-        const float2 T = cmulf(X[col.nx * RF_BATOMS + 32 * q],
-                               conj_if(Y[ny * RF_BATOMS + 32 * q], col.ny < 0));
-        const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
-        const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
-        // per-column partials go to 64-bit fixed point (order independent)
-        ax[q] += f2ll_rn(rv.x * imTU * sc);
-        ay[q] += f2ll_rn(rv.y * imTU * sc);
-        az[q] += f2ll_rn(imTV * sc);
-      }
-    }
+    cp_async_wait0();
   }
 #pragma unroll
   for (int q = 0; q < RF_APT; ++q) {
@@ -732,6 +769,18 @@ int host_inifur(mdx_ctx *ctx) {
     groups.push_back(g);
   }
   const size_t nwg = (size_t)KGRP * std::max(1, woff);
+  // contiguous group ranges of the mixed force pass's warps, balanced by
+  // W records (woff is cumulative in group order)
+  {
+    int g = 0;
+    d.rf_parts[0] = 0;
+    for (int p = 1; p < RF_PARTS; ++p) {
+      const long long target = (long long)woff * p / RF_PARTS;
+      while (g < (int)groups.size() && groups[g].woff < target) ++g;
+      d.rf_parts[p] = g;
+    }
+    d.rf_parts[RF_PARTS] = (int)groups.size();
+  }
   std::vector<SItem> items;
   for (size_t g = 0; g < groups.size(); ++g)
     for (int t0 = 0; t0 < groups[g].len; t0 += SCH) items.push_back(SItem{(int)g, t0});
@@ -778,7 +827,9 @@ int host_inifur(mdx_ctx *ctx) {
   // the dynamic shared memory of the mixed force pass plus its static
   // reduction buffer must also fit
   const size_t shr = sizeof(float2) * RF_BATOMS * (kx + ky + kz);
-  if (ctx->mixed() && shr + sizeof(long long) * 3 * RF_PARTS * RF_BATOMS > SFAC_SMEM_MAX) {
+  if (ctx->mixed() && shr + sizeof(long long) * 3 * RF_PARTS * RF_BATOMS +
+                             sizeof(float4) * RF_PARTS * 2 * RF_WB * KGRP >
+                         SFAC_SMEM_MAX) {
     ctx->err = "reciprocal k-set too large for the force-pass tile";
     return MDX_ERR_UNSUPPORTED;
   }
@@ -936,9 +987,11 @@ int launch_furir(mdx_ctx *ctx) {
   const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
   if (mx) {
     const size_t shr = sizeof(float2) * RF_BATOMS * (d.kx + d.ky + d.kz);
+    RfParts parts;
+    for (int p = 0; p <= RF_PARTS; ++p) parts.g[p] = d.rf_parts[p];
     k_rforce32<<<(d.n + RF_BATOMS - 1) / RF_BATOMS, 32 * RF_PARTS, shr, ctx->stream>>>(
-        d.n, d.ngroup, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf,
-        ctx->fix, d.gfix);
+        d.n, parts, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
+        d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
         d.n, d.ncol, d.cols, d.wk, d.tabx, d.taby, d.tabz, kzo, d.colrv, d.gx, d.gy, d.gz);

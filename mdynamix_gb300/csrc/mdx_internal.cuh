@@ -156,6 +156,7 @@ struct DevData {
   void *sitems;                 // work items of the mixed S(k) pass
   int nsitem;
   int sfac_slice, sfac_nslice;  // atoms per slice and slices of that pass
+  int rf_parts[8];              // group ranges of the mixed force pass's warps
   double2 *colrv;               // per column (RXV, RYV) at the current box
   float2 *colrvf;
   double *kscal;                // per-k scratch of the energy/virial kernel
