@@ -7,6 +7,7 @@ library is a plain C ABI (include/mdx_gpu.h).
 from __future__ import annotations
 
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -19,7 +20,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libmdxgpu.so")
 BUILD = os.path.join(ROOT, "_build")
 SOURCES = ["mdx_api.cu", "integrate.cu", "bonded.cu", "ewald.cu", "pair.cu", "nblist.cu",
-           "probe.cu"]
+           "probe.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
@@ -45,6 +46,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     cc = nvcc()
+    # objects of another host architecture (a copied tree) are rebuilt
+    stamp = os.path.join(BUILD, "HOST_ARCH")
+    arch = platform.machine()
+    if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
+        force = True
     jobs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
@@ -65,6 +71,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
     if force or jobs or not os.path.exists(LIB):
         run([cc, *ARCH, "-shared", "-o", LIB, *objs])
+    with open(stamp, "w") as fh:
+        fh.write(arch + "\n")
     return LIB
 
 
