@@ -256,6 +256,25 @@ int mdx_sultan(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot,
 int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0,
                      mdx_step_record *rec);
 
+/* SLFORCES without device allocation.  No counterpart in the reference (its
+ * FURIR uses static COMMON arrays; this library's mdx_slforces keeps the S(k)
+ * partial sums in a device buffer it allocates with the k-set).  For callers
+ * that must not allocate device memory during a run: a host loop that has
+ * handed its HBM budget to many resident contexts and cannot have a call
+ * fail or fragment memory half way, or one that cannot afford cudaMalloc's /
+ * cudaFree's implicit device-wide synchronisation, which stalls every other
+ * stream on the GPU.  Same kernels and results as mdx_slforces, with the S(k)
+ * scratch in one static device array of MDX_SK_STATIC_BYTES per device.
+ * Returns MDX_ERR_UNSUPPORTED when slices x k-vectors x 16 bytes exceed it,
+ * MDX_ERR_STATE when the k-set is not built yet or the box left its 5 %
+ * window (a new k-set allocates: call mdx_inifur), or when timers are on.
+ * The first call on a device sets up the scratch address; make it before any
+ * stream capture.  Calls whose kernels overlap on the device (other
+ * contexts, other streams or threads) share the scratch and race: serialise
+ * them. */
+#define MDX_SK_STATIC_BYTES (4u << 20)
+int mdx_slforces_static(mdx_ctx *ctx, mdx_scalars *out);
+
 /* expanded-ensemble scaling (RECINT) */
 int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,
                    double bee);

@@ -910,6 +910,11 @@ int host_inifur(mdx_ctx *ctx) {
   return MDX_OK;
 }
 
+int sfac_slices(const mdx_ctx *ctx) {
+  const DevData &d = ctx->dv;
+  return ctx->mixed() ? d.sfac_nslice : (d.n + SLICE - 1) / SLICE;
+}
+
 int launch_furir(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   if (ctx->p.alphad <= 0.0) return MDX_OK;

@@ -435,6 +435,12 @@ int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 int host_inifur(mdx_ctx *ctx);
 int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
+int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
+// mdx_api.cu, for the allocation-free entry point in noalloc.cu
+int api_require(mdx_ctx *ctx, bool topo, bool par, bool state);
+int api_check_err(mdx_ctx *ctx);
+int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out);
+int api_do_slforces(mdx_ctx *ctx, bool split);
 // integrate.cu
 int launch_zero_fast(mdx_ctx *ctx);
 int launch_zero_slow(mdx_ctx *ctx);

@@ -78,6 +78,7 @@ def load():
     L.mdx_fforces.argtypes = [P, C.c_int, C.POINTER(MdxScalars)]
     L.mdx_slforces.argtypes = [P, C.POINTER(MdxScalars)]
     L.mdx_allforce.argtypes = [P, C.POINTER(MdxScalars)]
+    L.mdx_slforces_static.argtypes = [P, C.POINTER(MdxScalars)]
     for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
         getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
     L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
