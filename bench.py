@@ -238,6 +238,35 @@ def run_gpu(args, rank, world, local):
                 nkv=s.kvector_count(), nfreq=s.spec.nfreq)
 
 
+def serving_leg(args):
+    """Continuous batching of solvation jobs (a bounded sample of the
+    256-job stream): Poisson arrivals, 5 coupling states per job, admission
+    by slots and HBM budget, p50/p99 latency from arrival to completion."""
+    from mdynamix_gb300 import serve
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    out = {}
+    jobs = serve.solvation_stream(args.serve_jobs, rate=args.serve_rate, seed=11,
+                                  steps_per_state=args.serve_steps)
+    preps = [serve.prepare(j) for j in jobs]          # request preprocessing (host)
+    warm = serve.Server(precision=MDX_MIXED, slots=4)  # first-use costs (module load)
+    warm.run([serve.prepare(serve.JobSpec("warm", jobs[0].spec, steps_per_state=2))])
+    for name, prec in (("mixed", MDX_MIXED), ("fp64", MDX_FP64)):
+        srv = serve.Server(precision=prec, slots=args.serve_slots)
+        t0 = time.perf_counter()
+        res = srv.run(preps)
+        wall = time.perf_counter() - t0
+        st = serve.latency_stats(res, wall)
+        st["peak_resident_jobs"] = srv.peak_resident
+        out[name] = st
+    atoms = [p.system.nstot for p in preps]
+    out["sample"] = (f"{len(preps)} jobs of {min(atoms)}-{max(atoms)} atoms (one solute in water), "
+                     f"Poisson arrivals at {args.serve_rate}/s, 5 coupling states x "
+                     f"{args.serve_steps} DOUBLE long steps per job, up to {args.serve_slots} "
+                     f"resident; latency = completion - arrival")
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    return out
+
+
 def cpu_baseline(s, st, threads, budget_s=40.0):
     """The oracle (restated reference routines) on the same workload:
     one CHCNB and one long step, list build amortised over ICHNB steps."""
@@ -292,6 +321,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--serve-jobs", type=int, default=32, help="serving leg sample (0 = off)")
+    ap.add_argument("--serve-steps", type=int, default=20, help="long steps per coupling state")
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
+    ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
@@ -316,6 +349,7 @@ def main():
                        r["peak64"], r["peak32"], "fp64", args.steps)
     roof32 = roofline_of(o32["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
                          r["peak64"], r["peak32"], "mixed", args.steps)
+    serving = serving_leg(args) if args.serve_jobs > 0 else None
     cpu = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()
@@ -344,6 +378,7 @@ def main():
                 "steps": r["e2e_steps"]},
         "gpu_launches": o64["launches"],
         "clocks": o64["clocks"],
+        "serving": serving,
         "cpu_baseline": cpu,
         "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
         "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},

@@ -38,6 +38,7 @@
 #ifndef MDX_GPU_H
 #define MDX_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -255,6 +256,24 @@ int mdx_sultan(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot,
                mdx_step_record *rec);
 int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0,
                      mdx_step_record *rec);
+
+/* Asynchronous DOUBLE for a host loop that drives many contexts at once
+ * (no counterpart in the reference, whose step loop is synchronous).
+ * mdx_double_enqueue puts nsteps long steps (mdstep.f:324-436) on the
+ * context's stream, optionally preceded by DOUBLE's prologue (CHCNB, GETCOM,
+ * SLFORCES, FFORCES; mdstep.f:296-310), and returns without waiting; steps
+ * are replayed from captured CUDA graphs, so constant volume and timers off
+ * are required (MDX_ERR_STATE otherwise).  mdx_poll sets *done = 1 once all
+ * enqueued work has finished and then returns its error status, exactly as
+ * mdx_double would; *done = 0 while work is in flight.  mdx_device_memory
+ * reports the device's free and total bytes (cudaMemGetInfo), for admission
+ * by memory budget. */
+int mdx_double_enqueue(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, int32_t prologue);
+int mdx_poll(mdx_ctx *ctx, int32_t *done);
+int mdx_device_memory(size_t *free_bytes, size_t *total_bytes);
+/* Diagnostic: the CUDA runtime error recorded for the calling thread and not
+ * yet consumed (0 = none), without clearing it. */
+int mdx_pending_cuda_error(void);
 
 /* SLFORCES without device allocation.  No counterpart in the reference (its
  * FURIR uses static COMMON arrays; this library's mdx_slforces keeps the S(k)

@@ -26,6 +26,7 @@
 // point.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "mdx_internal.cuh"
@@ -683,6 +684,18 @@ __global__ void k_eterms_init(mdx_scalars *sc, SelfEnergy se, int ntypes) {
   for (int t = 0; t < MDX_NT; ++t) sc->spee[t] = t < ntypes ? se.speei[t] : 0.0;
 }
 
+std::mutex g_smem_mu;
+
+template <typename K>
+cudaError_t raise_smem_limit(K kernel, size_t bytes) {
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 }  // namespace
 
 // INIFUR: the reference's k-set (forces.f:1366-1424) regrouped in columns,
@@ -795,24 +808,24 @@ int host_inifur(mdx_ctx *ctx) {
   d.nkv = nkv;
   d.ncol = (int)cols.size();
   ctx->nkv = nkv;
-  if (d.cols) cudaFree(d.cols);
-  if (d.kchunks) cudaFree(d.kchunks);
-  if (d.kgroups) cudaFree(d.kgroups);
-  if (d.sitems) cudaFree(d.sitems);
+  ctx_free(ctx, d.cols);
+  ctx_free(ctx, d.kchunks);
+  ctx_free(ctx, d.kgroups);
+  ctx_free(ctx, d.sitems);
   d.cols = nullptr;
   d.kchunks = nullptr;
   d.kgroups = nullptr;
   d.sitems = nullptr;
-  MDX_CUDA(cudaMalloc(&d.sitems, sizeof(SItem) * std::max<size_t>(1, items.size())));
+  MDX_CUDA(ctx_alloc(ctx, &d.sitems, sizeof(SItem) * std::max<size_t>(1, items.size())));
   MDX_CUDA(cudaMemcpy(d.sitems, items.data(), sizeof(SItem) * items.size(),
                       cudaMemcpyHostToDevice));
   d.nsitem = (int)items.size();
-  MDX_CUDA(cudaMalloc(&d.kgroups, sizeof(KGroup) * std::max<size_t>(1, groups.size())));
+  MDX_CUDA(ctx_alloc(ctx, &d.kgroups, sizeof(KGroup) * std::max<size_t>(1, groups.size())));
   MDX_CUDA(cudaMemcpy(d.kgroups, groups.data(), sizeof(KGroup) * groups.size(),
                       cudaMemcpyHostToDevice));
   d.ngroup = (int)groups.size();
-  MDX_CUDA(cudaMalloc(&d.cols, sizeof(KCol) * std::max<size_t>(1, cols.size())));
-  MDX_CUDA(cudaMalloc(&d.kchunks, sizeof(Chunk) * std::max<size_t>(1, chunks.size())));
+  MDX_CUDA(ctx_alloc(ctx, &d.cols, sizeof(KCol) * std::max<size_t>(1, cols.size())));
+  MDX_CUDA(ctx_alloc(ctx, &d.kchunks, sizeof(Chunk) * std::max<size_t>(1, chunks.size())));
   MDX_CUDA(cudaMemcpy(d.cols, cols.data(), sizeof(KCol) * cols.size(), cudaMemcpyHostToDevice));
   MDX_CUDA(cudaMemcpy(d.kchunks, chunks.data(), sizeof(Chunk) * chunks.size(),
                       cudaMemcpyHostToDevice));
@@ -833,15 +846,13 @@ int host_inifur(mdx_ctx *ctx) {
     ctx->err = "reciprocal k-set too large for the force-pass tile";
     return MDX_ERR_UNSUPPORTED;
   }
-  // opt in to more than 48 KB of shared memory (set every time: cheap)
+  // the dynamic shared-memory limit of a kernel is process-wide, shared by
+  // every context: only ever raise it
   if (ctx->mixed()) {
-    MDX_CUDA(cudaFuncSetAttribute(k_rforce32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)shr));
-    MDX_CUDA(cudaFuncSetAttribute(k_sfac32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sh));
+    MDX_CUDA(raise_smem_limit(k_rforce32, shr));
+    MDX_CUDA(raise_smem_limit(k_sfac32, sh));
   } else {
-    MDX_CUDA(cudaFuncSetAttribute(k_sfac<double, double2>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+    MDX_CUDA(raise_smem_limit(k_sfac<double, double2>, sh));
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
@@ -858,26 +869,26 @@ int host_inifur(mdx_ctx *ctx) {
     nslice_max = std::max(nslice_max, (size_t)d.sfac_nslice);
   }
   if (realloc_tables) {
-    cudaFree(d.tabx);
-    cudaFree(d.tabxf);
+    ctx_free(ctx, d.tabx);
+    ctx_free(ctx, d.tabxf);
     d.tabx = d.taby = d.tabz = nullptr;
     d.tabxf = d.tabyf = d.tabzf = nullptr;
     const size_t per = (size_t)kx + ky + kz;
     if (ctx->mixed()) {
-      MDX_CUDA(cudaMalloc(&d.tabxf, sizeof(float2) * per * d.n));
+      MDX_CUDA(ctx_alloc(ctx, &d.tabxf, sizeof(float2) * per * d.n));
       d.tabyf = d.tabxf + (size_t)kx * d.n;
       d.tabzf = d.tabyf + (size_t)ky * d.n;
     } else {
-      MDX_CUDA(cudaMalloc(&d.tabx, sizeof(double2) * per * d.n));
+      MDX_CUDA(ctx_alloc(ctx, &d.tabx, sizeof(double2) * per * d.n));
       d.taby = d.tabx + (size_t)kx * d.n;
       d.tabz = d.taby + (size_t)ky * d.n;
     }
   }
-  if (d.sk) cudaFree(d.sk);
+  ctx_free(ctx, d.sk);
   const size_t nk = (size_t)std::max(1, nkv);
   const size_t nkp = (nk + 1) & ~(size_t)1;  // keeps wk 32-byte aligned
   const size_t nc = std::max<size_t>(1, cols.size());
-  MDX_CUDA(cudaMalloc(&d.sk, sizeof(double2) * (nkp + 2 * nk + nwg + 2 * nc)));
+  MDX_CUDA(ctx_alloc(ctx, &d.sk, sizeof(double2) * (nkp + 2 * nk + nwg + 2 * nc)));
   d.wk = reinterpret_cast<dbl4 *>(d.sk + nkp);
   d.wkf = reinterpret_cast<float4 *>(d.wk + nk);
   // padding slots of the grouped W stay zero; k_kterms writes the others
@@ -885,9 +896,9 @@ int host_inifur(mdx_ctx *ctx) {
   d.colrv = reinterpret_cast<double2 *>(d.wkf + nwg);
   d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
   // per-slice partials of S(k), summed in slice order
-  if (d.sk_part) cudaFree(d.sk_part);
+  ctx_free(ctx, d.sk_part);
   d.sk_part = nullptr;
-  if (cudaMalloc(reinterpret_cast<void **>(&d.sk_part), sizeof(double2) * nslice_max * nk) !=
+  if (ctx_alloc(ctx, &d.sk_part, sizeof(double2) * nslice_max * nk) !=
       cudaSuccess) {
     d.sk_part = nullptr;  // falls back to atomic slice sums
     cudaGetLastError();

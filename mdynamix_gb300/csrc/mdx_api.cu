@@ -34,12 +34,17 @@ template <typename T>
 int dmalloc(mdx_ctx *ctx, T **p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * n);
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), sizeof(T) * n, ctx->stream);
   if (e != cudaSuccess) {
-    ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    ctx->err = std::string("cudaMallocAsync: ") + cudaGetErrorString(e);
     return MDX_ERR_NOMEM;
   }
-  cudaMemset(*p, 0, sizeof(T) * n);
+  cudaMemsetAsync(*p, 0, sizeof(T) * n, ctx->stream);
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("allocation: ") + cudaGetErrorString(e);
+    return MDX_ERR_CUDA;
+  }
   return MDX_OK;
 }
 
@@ -280,9 +285,42 @@ int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
 
 int ensure_records(mdx_ctx *ctx, int n) {
   if (n <= ctx->dv.rec_cap) return MDX_OK;
-  if (ctx->dv.rec) cudaFree(ctx->dv.rec);
+  ctx_free(ctx, ctx->dv.rec);
   RC(dmalloc(ctx, &ctx->dv.rec, (size_t)n));
   ctx->dv.rec_cap = n;
+  return MDX_OK;
+}
+
+// One DOUBLE long step replayed from its captured graph (captured on first
+// use; four variants: list rebuild or not x records or not).
+int graph_step(mdx_ctx *ctx, int mstep, bool rec) {
+  const int g = (mstep % ctx->p.ichnb == 0 ? 1 : 0) + (rec ? 2 : 0);
+  if (!ctx->gexec[g]) {
+    const int64_t l0 = ctx->launches;
+    MDX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = double_step(ctx, mstep, rec ? -1 : -2);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) {
+      ctx->err = std::string("graph capture: ") + cudaGetErrorString(e);
+      return MDX_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&ctx->gexec[g], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      ctx->gexec[g] = nullptr;
+      ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+      return MDX_ERR_CUDA;
+    }
+    ctx->glaunches[g] = ctx->launches - l0;
+    ctx->launches = l0;
+  }
+  MDX_CUDA(cudaGraphLaunch(ctx->gexec[g], ctx->stream));
+  ctx->launches += ctx->glaunches[g];
   return MDX_OK;
 }
 
@@ -306,33 +344,7 @@ int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
   for (int s = 1; s <= nsteps; ++s) {
     const int mstep = mstep0 + s;
     if (graphs) {
-      const int g = (mstep % ctx->p.ichnb == 0 ? 1 : 0) + (rec ? 2 : 0);
-      if (!ctx->gexec[g]) {
-        const int64_t l0 = ctx->launches;
-        MDX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = double_step(ctx, mstep, rec ? -1 : -2);
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-        if (rc) {
-          if (graph) cudaGraphDestroy(graph);
-          return rc;
-        }
-        if (e != cudaSuccess) {
-          ctx->err = std::string("graph capture: ") + cudaGetErrorString(e);
-          return MDX_ERR_CUDA;
-        }
-        e = cudaGraphInstantiate(&ctx->gexec[g], graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) {
-          ctx->gexec[g] = nullptr;
-          ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e);
-          return MDX_ERR_CUDA;
-        }
-        ctx->glaunches[g] = ctx->launches - l0;
-        ctx->launches = l0;
-      }
-      MDX_CUDA(cudaGraphLaunch(ctx->gexec[g], ctx->stream));
-      ctx->launches += ctx->glaunches[g];
+      RC(graph_step(ctx, mstep, rec != nullptr));
     } else if (dbl) {
       RC(double_step(ctx, mstep, rec ? s - 1 : -2));
     } else {
@@ -488,9 +500,10 @@ int mdx_close(mdx_ctx *ctx) {
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
                   d.red_part, d.red_ctr, d.sk_part};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->stream) {
+    for (void *p : ptrs) ctx_free(ctx, p);
+    cudaStreamSynchronize(ctx->stream);
+  }
   ctx->drop_graphs();
   for (auto &sp : ctx->spans) {
     cudaEventDestroy(sp.a);
@@ -749,8 +762,8 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
                                                          tmp + 3 * n, d.pos);
     ctx->launches++;
   }
+  ctx_free(ctx, tmp);
   cudaStreamSynchronize(ctx->stream);
-  cudaFree(tmp);
   if (rc) return rc;
   RC(upload(ctx, d.vx, vx, n));
   RC(upload(ctx, d.vy, vy, n));
@@ -801,7 +814,7 @@ int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
     if (sx) cudaMemcpy(sx, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost);
     if (sy) cudaMemcpy(sy, tmp + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
     if (sz) cudaMemcpy(sz, tmp + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    cudaFree(tmp);
+    ctx_free(ctx, tmp);
   }
   if (vx) MDX_CUDA(cudaMemcpy(vx, d.vx, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (vy) MDX_CUDA(cudaMemcpy(vy, d.vy, sizeof(double) * n, cudaMemcpyDeviceToHost));
@@ -923,6 +936,52 @@ int mdx_double(mdx_ctx *ctx, int32_t nsteps, int32_t nsttot, mdx_step_record *re
   return run_steps(ctx, true, nsteps, nsttot, rec);
 }
 
+int mdx_double_enqueue(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, int32_t prologue) {
+  if (!ctx || nsteps < 0) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  if (ctx->p.lnpt || ctx->timing || !ctx->use_graphs) {
+    ctx->err = "enqueued steps need graph replay: constant volume, timers off";
+    return MDX_ERR_STATE;
+  }
+  if (prologue) {  // DOUBLE's prologue, mdstep.f:296-310
+    RC(launch_vira(ctx, 0));
+    RC(launch_build_lists(ctx));
+    RC(launch_getcom(ctx));
+    RC(do_slforces(ctx, false));
+    RC(do_fforces(ctx, 1, false));
+  } else if (!ctx->have_lists) {
+    ctx->err = "neighbour lists not built (enqueue with the prologue first)";
+    return MDX_ERR_STATE;
+  }
+  for (int s = 1; s <= nsteps; ++s) RC(graph_step(ctx, mstep0 + s, false));
+  return MDX_OK;
+}
+
+int mdx_poll(mdx_ctx *ctx, int32_t *done) {
+  if (!ctx || !done) return MDX_ERR_ARG;
+  const cudaError_t e = cudaStreamQuery(ctx->stream);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return MDX_OK;
+  }
+  if (e != cudaSuccess) {
+    ctx->err = std::string("stream: ") + cudaGetErrorString(e);
+    return MDX_ERR_CUDA;
+  }
+  *done = 1;
+  return check_err(ctx);
+}
+
+int mdx_pending_cuda_error(void) { return (int)cudaPeekAtLastError(); }
+
+int mdx_device_memory(size_t *free_bytes, size_t *total_bytes) {
+  size_t f = 0, t = 0;
+  if (cudaMemGetInfo(&f, &t) != cudaSuccess) return MDX_ERR_CUDA;
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return MDX_OK;
+}
+
 int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, mdx_step_record *rec) {
   if (!ctx || nsteps < 0) return MDX_ERR_ARG;
   return run_steps(ctx, false, nsteps, mstep0, rec);
@@ -994,8 +1053,8 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
     RC(upload(ctx, dq, ctx->h_q.data(), d.n));
     k_set_q<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, dq, d.pos);
     ctx->launches++;
+    ctx_free(ctx, dq);
     cudaStreamSynchronize(ctx->stream);
-    cudaFree(dq);
   }
   return MDX_OK;
 }

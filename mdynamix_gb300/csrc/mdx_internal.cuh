@@ -422,6 +422,24 @@ __device__ __forceinline__ void fix_addf(unsigned long long *a, float v,
   atomicAdd(a, (unsigned long long)q);
 }
 
+// Device memory of a context is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the context's stream): freeing never synchronises the
+// whole device, so contexts can open and close while others run.  An
+// allocation is followed by a sync of the context's own stream, so host-side
+// copies into it may follow at once.
+inline cudaError_t ctx_alloc(mdx_ctx *ctx, void **p, size_t bytes) {
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return e;
+}
+template <typename T>
+inline cudaError_t ctx_alloc(mdx_ctx *ctx, T **p, size_t bytes) {
+  return ctx_alloc(ctx, reinterpret_cast<void **>(p), bytes);
+}
+inline void ctx_free(mdx_ctx *ctx, void *p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
 // ---------------------------------------------------------- host launchers
 // nblist.cu
 int launch_build_lists(mdx_ctx *ctx);

@@ -299,10 +299,10 @@ int launch_build_lists(mdx_ctx *ctx) {
   g.ncell = g.nx * g.ny * g.nz;
   if (g.ncell != ctx->grid.ncell) {
     ctx->drop_graphs();
-    if (d.cell_cnt) cudaFree(d.cell_cnt);
-    if (d.cell_start) cudaFree(d.cell_start);
-    MDX_CUDA(cudaMalloc(&d.cell_cnt, sizeof(int) * (g.ncell + 1) * 2));
-    MDX_CUDA(cudaMalloc(&d.cell_start, sizeof(int) * (g.ncell + 1)));
+    ctx_free(ctx, d.cell_cnt);
+    ctx_free(ctx, d.cell_start);
+    MDX_CUDA(ctx_alloc(ctx, &d.cell_cnt, sizeof(int) * (g.ncell + 1) * 2));
+    MDX_CUDA(ctx_alloc(ctx, &d.cell_start, sizeof(int) * (g.ncell + 1)));
   }
   ctx->grid = g;
   ctx->list_rl2 = rl * rl;

@@ -4,7 +4,7 @@
 // mdx_slforces evaluates the slow forces with buffers the context owns; the
 // one scratch buffer of that path, the per-slice partial sums of the Ewald
 // structure factors S(k) (written by k_sfac / k_sfac32, summed in slice order
-// by k_sfac_sum), lives in a cudaMalloc'd block that INIFUR sizes.  This entry
+// by k_sfac_sum), lives in a device block allocated with the k-set.  This entry
 // point runs the same kernels with that scratch taken from a file-scope
 // static device array instead, and refuses (never allocates) whenever the
 // path would need device memory it does not already have:

@@ -79,6 +79,9 @@ def load():
     L.mdx_slforces.argtypes = [P, C.POINTER(MdxScalars)]
     L.mdx_allforce.argtypes = [P, C.POINTER(MdxScalars)]
     L.mdx_slforces_static.argtypes = [P, C.POINTER(MdxScalars)]
+    L.mdx_double_enqueue.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
+    L.mdx_poll.argtypes = [P, I32P]
+    L.mdx_device_memory.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
         getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
     L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -93,6 +96,15 @@ def load():
     L.mdx_probe_fma_peak.argtypes = [C.c_int, F64P]
     _lib = L
     return L
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    L = load()
+    f, t = C.c_size_t(), C.c_size_t()
+    if L.mdx_device_memory(C.byref(f), C.byref(t)) != 0:
+        raise MdxError(2, "cudaMemGetInfo failed")
+    return f.value, t.value
 
 
 def _fp(a):
@@ -228,6 +240,16 @@ class ForcePath:
 
     def sultan_steps(self, nsteps: int, mstep0: int, records: bool = True):
         return self._run("mdx_sultan_steps", nsteps, mstep0, records)
+
+    def enqueue_double(self, nsteps: int, mstep0: int = 0, prologue: bool = False):
+        """Queue nsteps DOUBLE long steps (and the prologue) without waiting."""
+        self._check(self.L.mdx_double_enqueue(self.h, nsteps, mstep0, int(prologue)))
+
+    def poll(self) -> bool:
+        """True once the queued work has finished (errors raise MdxError)."""
+        d = C.c_int32()
+        self._check(self.L.mdx_poll(self.h, C.byref(d)))
+        return bool(d.value)
 
     def set_lambda(self, ec: float, pw1: float = 1.0, pw2: float = 1.0 / 3.0, bee: float = 3.0):
         self._check(self.L.mdx_set_lambda(self.h, ec, pw1, pw2, bee))

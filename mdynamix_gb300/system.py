@@ -796,6 +796,45 @@ def _random_rotation(rng: np.random.Generator) -> np.ndarray:
         [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
 
 
+def _lattice_with_room(rng, nside: int, nop: int, big: List[int]) -> np.ndarray:
+    """Lattice cell per molecule, leaving the neighbour cells of molecules
+    with more than three sites empty as far as the spare cells allow (first
+    the 6 face neighbours of every such molecule, then the other 20), so a
+    solute does not start inside its neighbours."""
+    ncell = nside ** 3
+    spare = ncell - nop
+    order = rng.permutation(ncell)
+    taken = np.zeros(ncell, dtype=bool)
+    blocked = np.zeros(ncell, dtype=bool)
+    cell_of = np.full(nop, -1, dtype=np.int64)
+
+    def idx(i, j, k):
+        return ((i % nside) * nside + (j % nside)) * nside + (k % nside)
+
+    faces = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+    rest = [(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)
+            if (a, b, c) != (0, 0, 0) and (a, b, c) not in faces]
+    pos = 0
+    for m in big:
+        while taken[order[pos]] or blocked[order[pos]]:
+            pos += 1
+        c = order[pos]
+        taken[c] = True
+        cell_of[m] = c
+    for shell in (faces, rest):
+        for m in big:
+            c = cell_of[m]
+            i, j, k = c // (nside * nside), (c // nside) % nside, c % nside
+            for d in shell:
+                nb = idx(i + d[0], j + d[1], k + d[2])
+                if not taken[nb] and not blocked[nb] and blocked.sum() < spare:
+                    blocked[nb] = True
+    free = [c for c in order if not taken[c] and not blocked[c]]
+    others = [m for m in range(nop) if cell_of[m] < 0]
+    cell_of[others] = free[:len(others)]
+    return cell_of
+
+
 def make_configuration(s: System, seed: int = 1, jitter: float = 0.3,
                        order: Optional[np.ndarray] = None):
     """Seeded start: molecular centres on a jittered simple-cubic lattice
@@ -807,8 +846,13 @@ def make_configuration(s: System, seed: int = 1, jitter: float = 0.3,
     nside = int(math.ceil(nop ** (1.0 / 3.0) - 1e-9))
     cells = np.array([(i, j, k) for i in range(nside) for j in range(nside) for k in range(nside)],
                      dtype=np.float64)
-    perm = rng.permutation(len(cells))[:nop]
-    cells = cells[perm]
+    mtype = np.repeat(np.arange(s.ntypes), s.nspec[:s.ntypes])
+    big = [int(m) for m in np.nonzero(s.nsits[mtype] > 3)[0]]
+    if big and len(cells) > nop:
+        cells = cells[_lattice_with_room(rng, nside, nop, big)]
+    else:
+        perm = rng.permutation(len(cells))[:nop]
+        cells = cells[perm]
     box = np.array([s.boxl, s.boyl, s.bozl])
     a = box / nside
     com = (cells + 0.5) * a - 0.5 * box
@@ -865,3 +909,15 @@ def spcfw_water(nwater: int = 32768, nmax: int = 20, alpha_per_a: float = 0.25,
                    nfreq=steps_nfreq, rcut=rcut, rshort=5.0,
                    alpha=alpha_per_a * rcut, fexp=fexp, ichnb=10, shake=False,
                    nvt=(300.0, 30.0), trtemp=300.0)
+
+
+SOLUTES = ("CH3OH", "C2H5OH", "CH3CN", "dmso", "Li+", "Na+", "Cl-")
+
+
+def solvation_job(solute: str, nwater: int, rcut: float = 9.0) -> RunSpec:
+    """One solute (the expanded-ensemble type, EE_type 1) in flexible SPC
+    water (H2O, fSPC) at 1.0 g/cm3: Rcut 9, Ewald A = 2.8, B = 9 (input.f
+    defaults), double time step 0.2/2 fs, Nose-Hoover 298 K / 30 fs."""
+    return RunSpec(molecules=[(solute, 1), ("H2O", nwater)], density=1.0, dt_fs=2.0,
+                   nfreq=10, rcut=rcut, rshort=5.0, alpha=2.8, fexp=9.0, ichnb=10,
+                   nvt=(298.0, 30.0), trtemp=298.0, iee_type=1)
