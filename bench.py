@@ -267,6 +267,53 @@ def serving_leg(args):
     return out
 
 
+def pimd_leg(args):
+    """Path-integral water: 256 SPC-FW x 32 bead replicas (24,576 bead
+    atoms), dt 0.25 fs, bead thermostats; a bounded sample of long steps per
+    precision, and the mixed path's force error against FP64 after the
+    preparation."""
+    import torch
+    from mdynamix_gb300 import system as S
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    from mdynamix_gb300.mdx import PimdPath
+    s = S.System(S.pimd_water(nwater=256, nbeads=32))
+    states = S.pimd_beads(s, seed=5)
+    out = {}
+    paths = {}
+    for name, prec in (("mixed", MDX_MIXED), ("fp64", MDX_FP64)):
+        pp = PimdPath(s, states, precision=prec)
+        pp.run(args.pimd_warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        recs = pp.steps(args.pimd_steps, args.pimd_warmup)
+        dt = time.perf_counter() - t0
+        atoms = s.nstot * s.spec.nbeads
+        out[name] = {"atom_steps_per_s": atoms * args.pimd_steps / dt,
+                     "ms_per_step": dt / args.pimd_steps * 1e3,
+                     "temp_last": recs[-1].temp, "qek_last": recs[-1].qek}
+        paths[name] = pp
+    # force error of the mixed path on identical bead coordinates
+    g64 = PimdPath(s, states, precision=MDX_FP64)
+    g32 = PimdPath(s, states, precision=MDX_MIXED)
+    g64.run(0)
+    g32.run(0)
+    num = den = 0.0
+    for a, b in zip(g32.beads, g64.beads):
+        fa = a.forces(1) + a.forces(2)
+        fb = b.forces(1) + b.forces(2)
+        num += float(((fa - fb) ** 2).sum())
+        den += float((fb ** 2).sum())
+    out["force_err_rms_mixed_vs_fp64"] = math.sqrt(num / den)
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    out["sample"] = (f"256 SPC-FW waters x 32 beads (24576 bead atoms), Rc 9 A, alpha 0.35/A, "
+                     f"dt 0.25 fs, PI_thermo 300 K / 5 fs / chains of 4; {args.pimd_warmup} "
+                     f"steps with the preparation, then {args.pimd_steps} timed long steps "
+                     f"(host wall clock around synchronised calls)")
+    for pp in list(paths.values()) + [g64, g32]:
+        pp.close()
+    return out
+
+
 def cpu_baseline(s, st, threads, budget_s=40.0):
     """The oracle (restated reference routines) on the same workload:
     one CHCNB and one long step, list build amortised over ICHNB steps."""
@@ -325,6 +372,8 @@ def main():
     ap.add_argument("--serve-steps", type=int, default=20, help="long steps per coupling state")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
     ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--pimd-steps", type=int, default=20, help="PIMD leg timed steps (0 = off)")
+    ap.add_argument("--pimd-warmup", type=int, default=3)
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
@@ -350,6 +399,7 @@ def main():
     roof32 = roofline_of(o32["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
                          r["peak64"], r["peak32"], "mixed", args.steps)
     serving = serving_leg(args) if args.serve_jobs > 0 else None
+    pimd = pimd_leg(args) if args.pimd_steps > 0 else None
     cpu = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()
@@ -379,6 +429,7 @@ def main():
         "gpu_launches": o64["launches"],
         "clocks": o64["clocks"],
         "serving": serving,
+        "pimd": pimd,
         "cpu_baseline": cpu,
         "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
         "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},

@@ -298,6 +298,49 @@ int mdx_slforces_static(mdx_ctx *ctx, mdx_scalars *out);
 int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,
                    double bee);
 
+/* Path-integral MD (pimd.f): NBEADS contexts, one per bead replica of the
+ * same system (same topology and parameters, states uploaded), advanced
+ * together.  The reference runs one bead per MPI rank (input.f:643-659) and
+ * couples them every short step by ring springs (PIFORCES, pimd.f:321-395;
+ * neighbour-bead coordinates travel as REAL*4, pimd.f:450-486, and are used
+ * rounded to single precision here too) and by per-atom Nose-Hoover chains
+ * on the bead kinetic energy summed over beads (BEADNOSE, pimd.f:402-444);
+ * forces of each bead are divided by NBEADS.  Here all beads stay on one
+ * GPU; each long step is one CUDA graph whose per-bead work runs on the
+ * beads' own streams concurrently, joined for the two cross-bead kernels.
+ * Bead thermostats only (PI_thermo): a bead context with LNVT or LNPT set is
+ * rejected (MDX_ERR_UNSUPPORTED). */
+typedef struct {
+  int32_t nbeads;   /* NBEADS (PIMD keyword)                          */
+  int32_t jnh;      /* JNH bead thermostats per atom (PI_thermo)       */
+  double beadfac;   /* BEADFAC, setup.f:696                            */
+  double conveq;    /* CONVEQ,  setup.f:700                            */
+  double dqqt;      /* DQQT,    main.f:413                             */
+  double fnh;       /* FNH,     main.f:415                             */
+} mdx_pimd_params;
+
+/* One record per long step of the bead ensemble (pimd.f:225-241 quantities). */
+typedef struct {
+  int32_t mstep;
+  double qek;       /* QEK = QEKS/NFREQ: ring-spring energy (pimd.f:229)  */
+  double virpi;     /* VIRPI summed over beads                           */
+  double pe;        /* PE1+PE2+PELS1+PELS2+SPE+PINT summed over beads     */
+  double tke;       /* TKE summed over beads                             */
+  double temp;      /* TEMP averaged over beads                          */
+} mdx_pimd_record;
+
+typedef struct mdx_pimd mdx_pimd;
+int mdx_pimd_open(mdx_ctx *const *beads, const mdx_pimd_params *par, mdx_pimd **out);
+int mdx_pimd_close(mdx_pimd *pi);
+/* PIMD (pimd.f:18-316): the preparation 1.2 (CHCNB, GETCOM, SLFORCES,
+ * FFORCES, /NBEADS, PIFORCES) then nsteps long steps; records optional. */
+int mdx_pimd_run(mdx_pimd *pi, int32_t nsteps, int32_t nsttot, mdx_pimd_record *rec);
+/* nsteps more long steps without the preparation. */
+int mdx_pimd_steps(mdx_pimd *pi, int32_t nsteps, int32_t mstep0, mdx_pimd_record *rec);
+/* THERMO(NSTOT, JNH), column-major, in and out. */
+int mdx_pimd_get_thermo(mdx_pimd *pi, double *thermo);
+int mdx_pimd_set_thermo(mdx_pimd *pi, const double *thermo);
+
 /* measurement helpers: the stream the context launches on, and a count of
  * the kernels it has launched since open */
 void *mdx_stream(mdx_ctx *ctx);

@@ -126,6 +126,19 @@ class MdxStepRecord(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MdxPimdParams(C.Structure):
+    _fields_ = [("nbeads", C.c_int32), ("jnh", C.c_int32), ("beadfac", C.c_double),
+                ("conveq", C.c_double), ("dqqt", C.c_double), ("fnh", C.c_double)]
+
+
+class MdxPimdRecord(C.Structure):
+    _fields_ = [("mstep", C.c_int32)] + [(n, C.c_double) for n in (
+        "qek", "virpi", "pe", "tke", "temp")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def records_to_dicts(recs) -> List[dict]:
     return [r.as_dict() for r in recs]
 

@@ -1095,10 +1095,12 @@ int mdx_sync(mdx_ctx *ctx) {
 
 }  // extern "C"
 
-// Linkage for noalloc.cu (the helpers above have internal linkage).
+// Linkage for noalloc.cu and pimd.cu (the helpers above have internal
+// linkage).
 int api_require(mdx_ctx *ctx, bool topo, bool par, bool state) {
   return require(ctx, topo, par, state);
 }
 int api_check_err(mdx_ctx *ctx) { return check_err(ctx); }
 int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out) { return copy_scalars(ctx, out); }
 int api_do_slforces(mdx_ctx *ctx, bool split) { return do_slforces(ctx, split); }
+int api_do_fforces(mdx_ctx *ctx, int laver, bool split) { return do_fforces(ctx, laver, split); }

@@ -459,6 +459,7 @@ int api_require(mdx_ctx *ctx, bool topo, bool par, bool state);
 int api_check_err(mdx_ctx *ctx);
 int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out);
 int api_do_slforces(mdx_ctx *ctx, bool split);
+int api_do_fforces(mdx_ctx *ctx, int laver, bool split);
 // integrate.cu
 int launch_zero_fast(mdx_ctx *ctx);
 int launch_zero_slow(mdx_ctx *ctx);
@@ -468,5 +469,8 @@ int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
 int launch_getcom(mdx_ctx *ctx);
 int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev);
 int launch_record(mdx_ctx *ctx, int slot, int mstep);
+int launch_getemp(mdx_ctx *ctx);
+int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
+int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);

@@ -284,7 +284,9 @@ int launch_mirror_f32(mdx_ctx *ctx) {
 int launch_build_lists(mdx_ctx *ctx) {
   MDX_TIMER(ctx, MDX_T_LIST);
   DevData &d = ctx->dv;
-  const double rl = ctx->p.rcut + ctx->p.rskin;
+  // CHCNB puts every pair within SHORT in the short list even when SHORT
+  // exceeds the cutoff (forces.f:1964-1976), so the search radius covers both
+  const double rl = std::max(ctx->p.rcut + ctx->p.rskin, ctx->p.rshort);
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
          0.5 * ctx->bozl};
   CellGrid g;

@@ -94,6 +94,13 @@ def load():
     L.mdx_set_timers.argtypes = [P, C.c_int]
     L.mdx_get_timers.argtypes = [P, F64P, C.POINTER(C.c_int64)]
     L.mdx_probe_fma_peak.argtypes = [C.c_int, F64P]
+    from .abi import MdxPimdParams, MdxPimdRecord
+    L.mdx_pimd_open.argtypes = [C.POINTER(P), C.POINTER(MdxPimdParams), C.POINTER(P)]
+    L.mdx_pimd_close.argtypes = [P]
+    L.mdx_pimd_run.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxPimdRecord)]
+    L.mdx_pimd_steps.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxPimdRecord)]
+    L.mdx_pimd_get_thermo.argtypes = [P, F64P]
+    L.mdx_pimd_set_thermo.argtypes = [P, F64P]
     _lib = L
     return L
 
@@ -256,3 +263,63 @@ class ForcePath:
 
 
 __all__ = ["ForcePath", "MdxError", "load", "MDX_FP64", "MDX_MIXED"]
+
+
+class PimdPath:
+    """Path-integral MD: one ForcePath per bead replica, advanced together
+    (PIMD, pimd.f:18-316) by the library's bead coupling."""
+
+    def __init__(self, system, states, precision: int = MDX_FP64, **caps):
+        from .system import pimd_params
+        from .abi import MdxPimdRecord
+        self.L = load()
+        self.system = system
+        self.pp = pimd_params(system)
+        self.beads = []
+        for st in states:
+            g = ForcePath(system, precision=precision, **caps)
+            g.set_state(*st)
+            self.beads.append(g)
+        hs = (C.c_void_p * len(self.beads))(*[b.h.value for b in self.beads])
+        h = C.c_void_p()
+        rc = self.L.mdx_pimd_open(hs, C.byref(self.pp), C.byref(h))
+        if rc != 0:
+            raise MdxError(rc, self.L.mdx_last_error(self.beads[0].h).decode())
+        self.h = h
+        self._Rec = MdxPimdRecord
+
+    def _run(self, fn, nsteps, start):
+        recs = (self._Rec * max(1, nsteps))()
+        rc = getattr(self.L, fn)(self.h, nsteps, start, recs)
+        if rc != 0:
+            raise MdxError(rc, "PIMD: " + " / ".join(
+                self.L.mdx_last_error(b.h).decode() for b in self.beads[:1]))
+        return [recs[i] for i in range(nsteps)]
+
+    def run(self, nsteps: int, nsttot: int = 0):
+        return self._run("mdx_pimd_run", nsteps, nsttot)
+
+    def steps(self, nsteps: int, mstep0: int):
+        return self._run("mdx_pimd_steps", nsteps, mstep0)
+
+    def thermo(self) -> np.ndarray:
+        t = np.zeros(self.system.nstot * self.pp.jnh)
+        if self.L.mdx_pimd_get_thermo(self.h, _fp(t)) != 0:
+            raise MdxError(2, "PIMD thermo download")
+        return t
+
+    def states(self):
+        return [b.get_state()[0] for b in self.beads]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mdx_pimd_close(self.h)
+            self.h = None
+        for b in self.beads:
+            b.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -303,6 +303,8 @@ class RunSpec:
     cut_forces: Optional[float] = None             # Cut_forces FTSCL
     rskin: float = 0.0                             # list skin (build mode)
     iee_type: Optional[int] = None                 # EE_type (1-based)
+    nbeads: int = 1                                # PIMD NBEADS (bead masses MASS/NBEADS)
+    pi_thermo: Optional[Tuple[float, int]] = None  # PI_thermo BTAU (fs), JNH (TRTEMP: trtemp)
 
 
 class System:
@@ -431,7 +433,7 @@ class System:
         self.site_eps = np.concatenate([[s["eps"] for s in t["sites"]] for t in self.types])
         self.site_r = np.concatenate([np.array(t["r"]) for t in self.types], axis=0)
         self.site_type = np.concatenate([[i + 1] * len(t["sites"]) for i, t in enumerate(self.types)]).astype(np.int32)
-        nb = 1  # NBEADS
+        nb = self.spec.nbeads  # NBEADS (setup.f:149)
         self.massd_site = self.site_mass / (nb * self.factm * self.unitm)
         n = self.nstot
         self.itype = np.zeros(n, dtype=np.int32)
@@ -921,3 +923,42 @@ def solvation_job(solute: str, nwater: int, rcut: float = 9.0) -> RunSpec:
     return RunSpec(molecules=[(solute, 1), ("H2O", nwater)], density=1.0, dt_fs=2.0,
                    nfreq=10, rcut=rcut, rshort=5.0, alpha=2.8, fexp=9.0, ichnb=10,
                    nvt=(298.0, 30.0), trtemp=298.0, iee_type=1)
+
+
+def pimd_params(s: System):
+    """BEADFAC, CONVEQ (setup.f:696-700), DQQT, FNH (main.f:413-415) of a
+    spec with nbeads > 1 and pi_thermo = (BTAU fs, JNH)."""
+    from .abi import MdxPimdParams
+    sp = s.spec
+    P = sp.nbeads
+    btau, jnh = sp.pi_thermo
+    beadfac = 0.5e-3 * P * (BOLTZ * sp.trtemp / HPLANK) ** 2 * s.unitl ** 2 / (s.unite * AVSNO)
+    dqqt = (s.unitt * 1.0e15 / btau) ** 2
+    return MdxPimdParams(nbeads=P, jnh=int(jnh), beadfac=beadfac,
+                         conveq=s.enerf * s.tempf / P, dqqt=dqqt, fnh=dqqt / (3.0 * P))
+
+
+def pimd_beads(s: System, seed: int = 1, sigma_h: float = 0.1):
+    """Bead starts: the classical start of make_configuration, each bead
+    displaced by a seeded Gaussian of width sigma_h * sqrt(m_H / m) A per
+    axis, with its own Maxwell momenta (bead masses) at TRTEMP."""
+    P = s.spec.nbeads
+    base = make_configuration(s, seed=seed, jitter=0.05)
+    rng = np.random.default_rng(seed + 7777)
+    m = s.site_mass[s.nsite - 1]
+    sig = sigma_h * np.sqrt(1.008 / m)
+    states = []
+    for b in range(P):
+        mom = make_configuration(s, seed=seed + 1 + b, jitter=0.05)[3:]
+        d = rng.normal(size=(3, s.nstot)) * sig
+        states.append((base[0] + d[0], base[1] + d[1], base[2] + d[2]) + tuple(mom))
+    return states
+
+
+def pimd_water(nwater: int = 256, nbeads: int = 32) -> RunSpec:
+    """Flexible SPC-FW water as bead replicas: 300 K, Rcut 9, Ewald A 3.15,
+    B 13.27 (alpha 0.35/A, |n| <= 8), dt 0.25 fs without double time step,
+    PI_thermo 300 K, 5 fs, chains of 4."""
+    return RunSpec(molecules=[("SPC-FW", nwater)], density=1.0, dt_fs=0.25, nfreq=1,
+                   rcut=9.0, rshort=5.0, alpha=3.15, fexp=13.27, ichnb=10, nvt=None,
+                   trtemp=300.0, nbeads=nbeads, pi_thermo=(5.0, 4))

@@ -56,6 +56,9 @@ def lib():
         for n in ("ox_double", "ox_double_steps", "ox_sultan", "ox_sultan_steps"):
             getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
         L.ox_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
+        from mdynamix_gb300.abi import MdxPimdParams, MdxPimdRecord
+        L.ox_pimd_steps.argtypes = [C.POINTER(P), C.POINTER(MdxPimdParams), F64P, C.c_int32,
+                                    C.c_int32, C.c_int, C.POINTER(MdxPimdRecord)]
     return _lib
 
 
@@ -185,3 +188,39 @@ class Oracle:
 
     def set_lambda(self, ec, pw1=1.0, pw2=1.0 / 3.0, bee=3.0):
         self._check(self.L.ox_set_lambda(self.h, ec, pw1, pw2, bee))
+
+
+class OraclePimd:
+    """PIMD over bead replicas with the restated pimd.f (PIFORCES, BEADNOSE,
+    the PIMD loop); one Oracle per bead."""
+
+    def __init__(self, system, states, threads: int = 1):
+        from mdynamix_gb300.system import pimd_params
+        self.system = system
+        self.pp = pimd_params(system)
+        self.beads = []
+        for st in states:
+            o = Oracle(system, threads=threads)
+            o.set_state(*st)
+            self.beads.append(o)
+        self.thermo = np.zeros(system.nstot * self.pp.jnh)
+        self.L = lib()
+
+    def _steps(self, nsteps, mstep0, prologue):
+        from mdynamix_gb300.abi import MdxPimdRecord
+        hs = (C.c_void_p * len(self.beads))(*[b.h.value for b in self.beads])
+        recs = (MdxPimdRecord * max(1, nsteps))()
+        rc = self.L.ox_pimd_steps(hs, C.byref(self.pp), _fp(self.thermo), nsteps, mstep0,
+                                  int(prologue), recs)
+        if rc != 0:
+            self.beads[0]._check(rc)
+        return [recs[i] for i in range(nsteps)]
+
+    def run(self, nsteps, nsttot=0):
+        return self._steps(nsteps, nsttot, True)
+
+    def steps(self, nsteps, mstep0):
+        return self._steps(nsteps, mstep0, False)
+
+    def states(self):
+        return [b.get_state()[0] for b in self.beads]

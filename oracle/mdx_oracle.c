@@ -2284,3 +2284,181 @@ int ox_set_lambda(ox_state *st, double ec, double pw1, double pw2,
   st->p.ec_me = ec;
   return MDX_OK;
 }
+
+/* ------------------------------------------------------------------ PIMD */
+/* PIFORCES (pimd.f:321-395) for every bead: harmonic springs to the beads
+ * below (JBEAD-1, received first, PI_SENDCOORD(1)) and above (JBEAD+1),
+ * whose coordinates arrive as REAL*4 (pimd.f:450-486).  Adds to HX/HY/HZ,
+ * VIRFX/Y/Z; returns QEK = 0.5 * sum over beads (the MPI_ALLREDUCE,
+ * pimd.f:383-385) and each bead's VIRPI. */
+static double piforces(ox_state *const *b, int P, const mdx_pimd_params *pp,
+                       double *virpi) {
+  double qsum = 0.;
+  for (int jb = 0; jb < P; ++jb) {
+    ox_state *st = b[jb];
+    double QEK = 0.;
+    for (int dir = 0; dir < 2; ++dir) {
+      const ox_state *o = b[dir == 0 ? (jb + P - 1) % P : (jb + 1) % P];
+      double VIRPI = 0.;
+      for (int I = 1; I <= st->nstot; ++I) {
+        int IS = st->nsite[I];
+        double BX = st->sx[I] - (double)(float)o->sx[I];
+        double BY = st->sy[I] - (double)(float)o->sy[I];
+        double BZ = st->sz[I] - (double)(float)o->sz[I];
+        pbc(st, &BX, &BY, &BZ);
+        double BSQ = BX * BX + BY * BY + BZ * BZ;
+        double BBB = sqrt(BSQ);
+        double R1I = 1.0 / BBB;
+        double DBND = BBB * pp->beadfac * st->mass[IS];
+        double EBDD = DBND * BBB;
+        double FORB = -2.0 * DBND * R1I;
+        st->hx[I] = st->hx[I] + BX * FORB;
+        st->hy[I] = st->hy[I] + BY * FORB;
+        st->hz[I] = st->hz[I] + BZ * FORB;
+        QEK = QEK + EBDD;
+        if (dir == 0) {
+          VIRPI = VIRPI + FORB * BSQ;
+          st->s.virfx = st->s.virfx + FORB * (BX * BX) * P;
+          st->s.virfy = st->s.virfy + FORB * (BY * BY) * P;
+          st->s.virfz = st->s.virfz + FORB * (BZ * BZ) * P;
+        }
+      }
+      if (dir == 0) virpi[jb] = VIRPI;
+    }
+    qsum = qsum + QEK;
+  }
+  return 0.5 * qsum;
+}
+
+/* BEADNOSE (pimd.f:402-444): per atom, the kinetic energy summed over
+ * beads drives a Nose-Hoover chain of length JNH shared by the atom's beads;
+ * every bead's momentum of that atom is scaled by SCV. */
+static void beadnose(ox_state *const *b, int P, const mdx_pimd_params *pp,
+                     double *thermo) {
+  const ox_state *s0 = b[0];
+  const int n = s0->nstot, JNH = pp->jnh;
+  const double TSTEB = s0->p.tsteb, TRTEMP = s0->p.trtemp;
+  for (int I = 1; I <= n; ++I) {
+    double FEK = 0.;
+    for (int jb = 0; jb < P; ++jb) {
+      const ox_state *st = b[jb];
+      FEK = FEK + 0.5 * (st->vx[I] * st->vx[I] + st->vy[I] * st->vy[I] +
+                         st->vz[I] * st->vz[I]) * st->massdi[I];
+    }
+    double *T = thermo + (I - 1); /* THERMO(I, J) at T[(J-1) * n] */
+    double ATEMP = FEK * pp->conveq;
+    double DKE = ATEMP / TRTEMP - 1.0;
+    T[0] = T[0] + DKE * pp->dqqt * TSTEB;
+    for (int J = 2; J <= JNH; ++J) {
+      T[(size_t)(J - 1) * n] = T[(size_t)(J - 1) * n] +
+                               (T[(size_t)(J - 2) * n] * T[(size_t)(J - 2) * n] - pp->fnh) * TSTEB;
+      T[(size_t)(J - 2) * n] = T[(size_t)(J - 2) * n] * (1. - T[(size_t)(J - 1) * n] * TSTEB);
+    }
+    double SCV = 1. - T[0] * TSTEB;
+    for (int jb = 0; jb < P; ++jb) {
+      ox_state *st = b[jb];
+      st->vx[I] = st->vx[I] * SCV;
+      st->vy[I] = st->vy[I] * SCV;
+      st->vz[I] = st->vz[I] * SCV;
+    }
+  }
+}
+
+static void scale_forces(ox_state *st, int P, int slow) {
+  for (int I = 1; I <= st->nstot; ++I) {
+    if (slow) {
+      st->gx[I] = st->gx[I] / P;
+      st->gy[I] = st->gy[I] / P;
+      st->gz[I] = st->gz[I] / P;
+    }
+    st->hx[I] = st->hx[I] / P;
+    st->hy[I] = st->hy[I] / P;
+    st->hz[I] = st->hz[I] / P;
+  }
+}
+
+int ox_pimd_steps(ox_state *const *b, const mdx_pimd_params *pp, double *thermo,
+                  int32_t nsteps, int32_t mstep0, int prologue, mdx_pimd_record *rec) {
+  int rc;
+  const int P = pp->nbeads;
+  if (P < 2 || pp->jnh < 1) return MDX_ERR_ARG;
+  ox_state *s0 = b[0];
+  if (s0->p.lnvt || s0->p.lnpt) {
+    snprintf(s0->msg, sizeof s0->msg, "PIMD with NVT/NPT scaling is not built");
+    return MDX_ERR_UNSUPPORTED;
+  }
+  double *virpi = (double *)xcalloc((size_t)P, sizeof(double));
+  const int NFREQ = s0->p.nfreq, NFREQ2 = NFREQ / 2 + 1;
+  const double HTSTEP = 0.5 * s0->p.tstep, TSTEB = s0->p.tsteb, HTSTEB = 0.5 * s0->p.tsteb;
+  if (prologue) { /* 1.2 (pimd.f:48-72) */
+    for (int jb = 0; jb < P; ++jb) {
+      ox_state *st = b[jb];
+      st->th.vira[0] = st->th.vira[1] = st->th.vira[2] = 0.;
+      if ((rc = ox_chcnb(st, NULL, NULL))) goto out;
+      ox_getcom(st);
+      if ((rc = ox_slforces(st, NULL))) goto out;
+      ox_fforces(st, 0, NULL);
+      scale_forces(st, P, 1);
+    }
+    piforces(b, P, pp, virpi);
+  }
+  for (int NSTEP = 1; NSTEP <= nsteps; ++NSTEP) {
+    const int MSTEP = mstep0 + NSTEP;
+    double QEKS = 0.;
+    for (int jb = 0; jb < P; ++jb) { /* PI_SCALING(1): GETEMP only (no NVT/NPT) */
+      if ((rc = getemp(b[jb]))) goto out;
+      kick(b[jb], b[jb]->gx, b[jb]->gy, b[jb]->gz, HTSTEP);
+    }
+    for (int NSTEB = 1; NSTEB <= NFREQ; ++NSTEB) {
+      for (int jb = 0; jb < P; ++jb) kick(b[jb], b[jb]->hx, b[jb]->hy, b[jb]->hz, HTSTEB);
+      beadnose(b, P, pp, thermo);
+      for (int jb = 0; jb < P; ++jb) {
+        ox_state *st = b[jb];
+        for (int I = 1; I <= st->nstot; ++I)
+          if (st->lmove[st->itype[I]]) {
+            st->sx[I] = st->vx[I] * TSTEB * st->massdi[I] + st->sx[I];
+            st->sy[I] = st->vy[I] * TSTEB * st->massdi[I] + st->sy[I];
+            st->sz[I] = st->vz[I] * TSTEB * st->massdi[I] + st->sz[I];
+          }
+        ox_getcom(st);
+        if (NSTEB == NFREQ2 && MSTEP % st->p.ichnb == 0)
+          if ((rc = ox_chcnb(st, NULL, NULL))) goto out;
+        if (NSTEB == NFREQ) {
+          if ((rc = ox_slforces(st, NULL))) goto out;
+          ox_fforces(st, 1, NULL);
+          scale_forces(st, P, 1);
+        } else {
+          ox_fforces(st, 0, NULL);
+          scale_forces(st, P, 0);
+        }
+      }
+      QEKS = QEKS + piforces(b, P, pp, virpi);
+      for (int jb = 0; jb < P; ++jb) {
+        kick(b[jb], b[jb]->hx, b[jb]->hy, b[jb]->hz, HTSTEB);
+        if ((rc = getemp(b[jb]))) goto out;
+      }
+    }
+    for (int jb = 0; jb < P; ++jb) {
+      kick(b[jb], b[jb]->gx, b[jb]->gy, b[jb]->gz, HTSTEP);
+      if ((rc = getemp(b[jb]))) goto out; /* PI_SCALING(2) */
+    }
+    if (rec) {
+      mdx_pimd_record *r = &rec[NSTEP - 1];
+      memset(r, 0, sizeof *r);
+      r->mstep = MSTEP;
+      r->qek = QEKS / NFREQ;
+      for (int jb = 0; jb < P; ++jb) {
+        const mdx_scalars *s = &b[jb]->s;
+        r->virpi += virpi[jb];
+        r->pe += s->pe1 + s->pe2 + s->pels1 + s->pels2 + s->spe + s->pint;
+        r->tke += b[jb]->th.tke;
+        r->temp += b[jb]->th.temp;
+      }
+      r->temp /= P;
+    }
+  }
+  rc = MDX_OK;
+out:
+  free(virpi);
+  return rc;
+}

@@ -12,8 +12,17 @@ pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-10      # relative, forces / energies / virials (FP64 drop-in bar)
 MIXED_TOL = 1e-5      # relative RMS force error of the mixed path
 
+def _short_beyond_cut():
+    # R_short above R_cutoff: CHCNB still files every pair within SHORT in
+    # the short list (forces.f:1964-1976)
+    spec = systems.spcfw(n=125, ions=0, rcut=5.5)
+    spec.rshort = 6.0
+    return systems.build(spec)
+
+
 CASES = {
     "spce_ions": lambda: systems.build(systems.spce_ions()),
+    "short_beyond_cut": _short_beyond_cut,
     "spcfw": lambda: systems.build(systems.spcfw()),
     "organics": lambda: systems.build(systems.organics()),
 }
