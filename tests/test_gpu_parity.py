@@ -108,6 +108,50 @@ def test_sultan_shake_fp64():
         assert abs(a.pels1 - b.pels1) <= 1e-8 * abs(b.pels1)
 
 
+def _npt_pair(spec):
+    s, st = systems.build(spec)
+    g = ForcePath(s)
+    o = oracle.Oracle(s)
+    g.set_state(*st)
+    o.set_state(*st)
+    return g, o
+
+
+def _check_npt(g, o, rg, ro):
+    (gx, gy, gz, *_), tg = g.get_state()
+    (ox, oy, oz, *_), to = o.get_state()
+    dpos = max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max())
+    assert dpos < 1e-9
+    for a, b in zip(rg, ro):
+        for n in ("boxl", "boyl", "bozl", "vol", "scl", "sc", "tryck", "temp", "pels1"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-8 * max(abs(getattr(b, n)), 1e-12), n
+    assert ro[-1].vol != ro[0].vol  # the barostat moved the box
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_sultan_npt_fp64(aniso):
+    """SULTAN + SHEJK with SCALING(3): Nose-Hoover NPT, isotropic or per axis
+    (mdstep.f:534-1093)."""
+    spec = systems.spce_ions()
+    spec.nvt = (300.0, 30.0)
+    spec.npt = (1.0, 500.0)
+    spec.anisotropic = aniso
+    g, o = _npt_pair(spec)
+    rg, ro = g.sultan(5), o.sultan(5)
+    _check_npt(g, o, rg, ro)
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_double_npt_fp64(aniso):
+    """DOUBLE with SCALING(1)/(2) in NPT (box rescaled every long step)."""
+    spec = systems.spcfw()
+    spec.npt = (1.0, 500.0)
+    spec.anisotropic = aniso
+    g, o = _npt_pair(spec)
+    rg, ro = g.double(3), o.double(3)
+    _check_npt(g, o, rg, ro)
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_mixed_force_error(name):
     s, st = CASES[name]()
