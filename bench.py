@@ -314,6 +314,52 @@ def pimd_leg(args):
     return out
 
 
+def bilayer_leg(args):
+    """DMPC bilayer in SPC water (98 lipids, 3655 waters), anisotropic NPT
+    with SHAKE (SULTAN): mixed-path force, energy and virial errors against
+    FP64 on the same configuration, and a bounded sample of long steps per
+    precision."""
+    import torch
+    from mdynamix_gb300 import system as S
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    from mdynamix_gb300.mdx import ForcePath
+    s = S.System(S.dmpc_bilayer())
+    st = S.bilayer_configuration(s, seed=1)
+    out = {}
+    sc = {}
+    f = {}
+    for name, prec in (("fp64", MDX_FP64), ("mixed", MDX_MIXED)):
+        g = ForcePath(s, precision=prec)
+        g.set_state(*st)
+        g.chcnb()
+        g.getcom()
+        sc[name] = g.allforce()
+        f[name] = g.forces(3)
+        g.sultan(args.bilayer_warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.sultan_steps(args.bilayer_steps, args.bilayer_warmup)
+        dt = time.perf_counter() - t0
+        out[name] = {"atom_steps_per_s": s.nstot * args.bilayer_steps / dt,
+                     "ms_per_step": dt / args.bilayer_steps * 1e3}
+        g.close()
+    a, b = f["mixed"], f["fp64"]
+    err = {"force_rms": float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))}
+    for n in ("pe1", "pe2", "pels1", "pels2", "spe", "pint"):
+        x, y = getattr(sc["mixed"], n), getattr(sc["fp64"], n)
+        err[n] = abs(x - y) / max(abs(y), 1e-300)
+    vm = sc["mixed"].vir1 + sc["mixed"].vir2 + sc["mixed"].virb
+    vf = sc["fp64"].vir1 + sc["fp64"].vir2 + sc["fp64"].virb
+    err["virial"] = abs(vm - vf) / abs(vf)
+    out["mixed_vs_fp64_rel_err"] = err
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    out["sample"] = (f"{s.nspec[0]} DMPC + {s.nspec[1]} SPC ({s.nstot} atoms), box "
+                     f"{s.boxl:.0f}x{s.boyl:.0f}x{s.bozl:.0f} A, Rc 12, Ewald 3.12/9.72, SHAKE, "
+                     f"anisotropic NPT 303 K / 1 bar, dt 2 fs; {args.bilayer_warmup} + "
+                     f"{args.bilayer_steps} timed SULTAN steps (host clock, synchronised)")
+    return out
+
+
 def cpu_baseline(s, st, threads, budget_s=40.0):
     """The oracle (restated reference routines) on the same workload:
     one CHCNB and one long step, list build amortised over ICHNB steps."""
@@ -374,6 +420,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--pimd-steps", type=int, default=20, help="PIMD leg timed steps (0 = off)")
     ap.add_argument("--pimd-warmup", type=int, default=3)
+    ap.add_argument("--bilayer-steps", type=int, default=10, help="bilayer leg timed steps (0 = off)")
+    ap.add_argument("--bilayer-warmup", type=int, default=3)
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
@@ -400,6 +448,7 @@ def main():
                          r["peak64"], r["peak32"], "mixed", args.steps)
     serving = serving_leg(args) if args.serve_jobs > 0 else None
     pimd = pimd_leg(args) if args.pimd_steps > 0 else None
+    bilayer = bilayer_leg(args) if args.bilayer_steps > 0 else None
     cpu = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()
@@ -430,6 +479,7 @@ def main():
         "clocks": o64["clocks"],
         "serving": serving,
         "pimd": pimd,
+        "bilayer": bilayer,
         "cpu_baseline": cpu,
         "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
         "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},

@@ -20,8 +20,19 @@ def _short_beyond_cut():
     return systems.build(spec)
 
 
+def _bilayer_patch():
+    # one DMPC per leaflet (118 atoms: bonds, angles, torsions, 1-4 pairs,
+    # SHAKE on a 118-atom molecule) in SPC water
+    from mdynamix_gb300 import system as S
+    spec = S.dmpc_bilayer(nside=1, nwater=500, box=(20.0, 20.0, 60.0), rcut=9.0,
+                          alpha=2.8, fexp=9.0)
+    s = S.System(spec)
+    return s, S.bilayer_configuration(s, seed=2)
+
+
 CASES = {
     "spce_ions": lambda: systems.build(systems.spce_ions()),
+    "bilayer_patch": _bilayer_patch,
     "short_beyond_cut": _short_beyond_cut,
     "spcfw": lambda: systems.build(systems.spcfw()),
     "organics": lambda: systems.build(systems.organics()),
@@ -139,6 +150,19 @@ def test_sultan_npt_fp64(aniso):
     g, o = _npt_pair(spec)
     rg, ro = g.sultan(5), o.sultan(5)
     _check_npt(g, o, rg, ro)
+
+
+def test_sultan_npt_bilayer_fp64():
+    """Lipid bilayer patch: SULTAN + SHEJK (118-atom molecule) with the
+    anisotropic barostat."""
+    s, st = _bilayer_patch()
+    g = ForcePath(s)
+    o = oracle.Oracle(s)
+    g.set_state(*st)
+    o.set_state(*st)
+    rg, ro = g.sultan(3), o.sultan(3)
+    _check_npt(g, o, rg, ro)
+    assert [r.shake_iter for r in rg] == [r.shake_iter for r in ro]
 
 
 @pytest.mark.parametrize("aniso", [False, True])
