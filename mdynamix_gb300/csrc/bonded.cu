@@ -60,7 +60,127 @@ __device__ __forceinline__ void avg_add(double *sh, double *gl, int m, int nrec,
     atomicAdd(&gl[m], v);
 }
 
+// Non-atomic add for a thread that owns every atom it touches (the
+// molecule-local kernel); the same per-term rounding as add_force.
 template <typename R>
+__device__ __forceinline__ void add_force_own(const BondOut &o, int i, R fx, R fy, R fz) {
+  if (o.hfix) {
+    o.hfix[i] += (unsigned long long)__double2ll_rn((double)fx * o.fscale);
+    o.hfix[o.n + i] += (unsigned long long)__double2ll_rn((double)fy * o.fscale);
+    o.hfix[2 * o.n + i] += (unsigned long long)__double2ll_rn((double)fz * o.fscale);
+  } else {
+    o.hx[i] += (double)fx;
+    o.hy[i] += (double)fy;
+    o.hz[i] += (double)fz;
+  }
+}
+
+// One bond (GETBND forces.f:140-196): harmonic, or Morse for ID = 1 within
+// 2 REQ.  acc: PINT VIRB VIRFX VIRFY VIRFZ; *bd, *eb: length and energy.
+template <typename R, bool OWN>
+__device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, int J, int M,
+                                          const int *__restrict__ bid,
+                                          const double *__restrict__ rb,
+                                          const double *__restrict__ fb,
+                                          const double *__restrict__ db,
+                                          const double *__restrict__ ro, int lmove,
+                                          double bx, double by, double bz,
+                                          const BondOut &o, double *acc, R *bd, R *eb) {
+  double BXd, BYd, BZd;
+  vec(pos, J, I, bx, by, bz, BXd, BYd, BZd);
+  const R BX = (R)BXd, BY = (R)BYd, BZ = (R)BZd;
+  const R REQ = (R)rb[M];
+  const R BSQ = BX * BX + BY * BY + BZ * BZ;
+  const R BD = sqrt(BSQ);
+  const R R1I = R(1) / BD;
+  const R BBB = BD - REQ;
+  R EBDD, FORB;
+  if (bid[M] != 1 || BBB > REQ) {
+    const R DBND = BBB * (R)fb[M];
+    EBDD = DBND * BBB;
+    FORB = R(-2) * DBND * R1I;
+  } else {
+    const R DDIS = (R)db[M], ROH = (R)ro[M];
+    const R EXM = exp(-ROH * BBB);
+    const R EXMP = R(1) - EXM;
+    EBDD = DDIS * (EXMP * EXMP);
+    FORB = R(-2) * DDIS * ROH * EXM * EXMP * R1I;
+  }
+  acc[0] += (double)EBDD;
+  *bd = BD;
+  *eb = EBDD;
+  if (lmove) {
+    if (OWN) {
+      add_force_own<R>(o, I, -BX * FORB, -BY * FORB, -BZ * FORB);
+      add_force_own<R>(o, J, BX * FORB, BY * FORB, BZ * FORB);
+    } else {
+      add_force<R>(o, I, -BX * FORB, -BY * FORB, -BZ * FORB);
+      add_force<R>(o, J, BX * FORB, BY * FORB, BZ * FORB);
+    }
+    acc[1] += (double)(FORB * BSQ);
+    acc[2] += (double)(FORB * (BX * BX));
+    acc[3] += (double)(FORB * (BY * BY));
+    acc[4] += (double)(FORB * (BZ * BZ));
+  }
+}
+
+// One angle (GETANG forces.f:230-303), harmonic in theta.
+// acc: PINT VIRB(unused) VIRFX VIRFY VIRFZ; *alf, *ea: angle and energy.
+template <typename R, bool OWN>
+__device__ __forceinline__ void angle_term(const dbl4 *__restrict__ pos, int I, int J, int K,
+                                           int M, const double *__restrict__ ra,
+                                           const double *__restrict__ fa, int lmove,
+                                           double bx, double by, double bz,
+                                           const BondOut &o, double *acc, R *alf, R *ea) {
+  const R FCN = (R)fa[M], AEQ = (R)ra[M];
+  double ax, ay, az, bxv, byv, bzv;
+  vec(pos, I, J, bx, by, bz, ax, ay, az);
+  vec(pos, K, J, bx, by, bz, bxv, byv, bzv);
+  const R AX = (R)ax, AY = (R)ay, AZ = (R)az;
+  const R BX = (R)bxv, BY = (R)byv, BZ = (R)bzv;
+  const R ASQ = AX * AX + AY * AY + AZ * AZ;
+  const R ASQI = R(1) / ASQ;
+  const R BSQ = BX * BX + BY * BY + BZ * BZ;
+  const R BSQI = R(1) / BSQ;
+  const R AB = sqrt(ASQ * BSQ);
+  const R ABI = R(1) / AB;
+  R COSA = AX * BX + AY * BY + AZ * BZ;
+  COSA = COSA * ABI;
+  COSA = fmin(COSA, R(1));
+  COSA = fmax(COSA, R(-1));
+  const R ALF = acos(COSA);
+  const R SINA = sin(ALF);
+  const R SINAI = R(1) / SINA;
+  const R DALF = ALF - AEQ;
+  const R ABC = DALF * FCN;
+  const R EANG = ABC * DALF;
+  acc[0] += (double)EANG;
+  *alf = ALF;
+  *ea = EANG;
+  if (lmove) {
+    const R SAB = R(-2) * ABC * SINAI;
+    const R CAB = SAB * COSA;
+    const R FAB = SAB * ABI;
+    const R FAA = CAB * ASQI;
+    const R FBB = CAB * BSQI;
+    const R FAX = FAB * BX - FAA * AX, FAY = FAB * BY - FAA * AY, FAZ = FAB * BZ - FAA * AZ;
+    const R FBX = FAB * AX - FBB * BX, FBY = FAB * AY - FBB * BY, FBZ = FAB * AZ - FBB * BZ;
+    if (OWN) {
+      add_force_own<R>(o, I, -FAX, -FAY, -FAZ);
+      add_force_own<R>(o, J, FAX + FBX, FAY + FBY, FAZ + FBZ);
+      add_force_own<R>(o, K, -FBX, -FBY, -FBZ);
+    } else {
+      add_force<R>(o, I, -FAX, -FAY, -FAZ);
+      add_force<R>(o, J, FAX + FBX, FAY + FBY, FAZ + FBZ);
+      add_force<R>(o, K, -FBX, -FBY, -FBZ);
+    }
+    acc[2] += (double)(-AX * FAX - BX * FBX);
+    acc[3] += (double)(-AY * FAY - BY * FBY);
+    acc[4] += (double)(-AZ * FAZ - BZ * FBZ);
+  }
+}
+
+template <typename R, bool ENER>
 __global__ void k_getbnd(int nrbt, const int *__restrict__ ibi,
                          const int *__restrict__ jbj, const int *__restrict__ ibuk,
                          const int *__restrict__ bid, const double *__restrict__ rb,
@@ -80,43 +200,18 @@ __global__ void k_getbnd(int nrbt, const int *__restrict__ ibi,
   if (N < nrbt) {
     const int I = ibi[N], J = jbj[N], M = ibuk[N];
     const int ityp = ainfo[I].x;
-    double BXd, BYd, BZd;
-    vec(pos, J, I, bx, by, bz, BXd, BYd, BZd);
-    const R BX = (R)BXd, BY = (R)BYd, BZ = (R)BZd;
-    const R REQ = (R)rb[M];
-    const R BSQ = BX * BX + BY * BY + BZ * BZ;
-    const R BD = sqrt(BSQ);
-    const R R1I = R(1) / BD;
-    const R BBB = BD - REQ;
-    R EBDD, FORB;
-    if (bid[M] != 1 || BBB > REQ) {
-      const R DBND = BBB * (R)fb[M];
-      EBDD = DBND * BBB;
-      FORB = R(-2) * DBND * R1I;
-    } else {
-      const R DDIS = (R)db[M], ROH = (R)ro[M];
-      const R EXM = exp(-ROH * BBB);
-      const R EXMP = R(1) - EXM;
-      EBDD = DDIS * (EXMP * EXMP);
-      FORB = R(-2) * DDIS * ROH * EXM * EXMP * R1I;
-    }
-    acc[0] = (double)EBDD;
+    R BD, EB;
+    bond_term<R, false>(pos, I, J, M, bid, rb, fb, db, ro, tc.lmove[ityp], bx, by, bz, o,
+                        acc, &BD, &EB);
     if (laver) {
       const double fnspi = 1.0 / (double)nspec[ityp];
       avg_add(sbr, br, M, nrbb, (double)BD * fnspi);
-      avg_add(sbe, be, M, nrbb, (double)EBDD * fnspi);
-    }
-    if (tc.lmove[ityp]) {
-      add_force<R>(o, I, -BX * FORB, -BY * FORB, -BZ * FORB);
-      add_force<R>(o, J, BX * FORB, BY * FORB, BZ * FORB);
-      acc[1] = (double)(FORB * BSQ);
-      acc[2] = (double)(FORB * (BX * BX));
-      acc[3] = (double)(FORB * (BY * BY));
-      acc[4] = (double)(FORB * (BZ * BZ));
+      avg_add(sbe, be, M, nrbb, (double)EB * fnspi);
     }
   }
-  block_add<5>(acc, dst);
+  if (ENER) block_add<5>(acc, dst);
   if (laver && nrbb <= 256) {
+    __syncthreads();
     for (int k = threadIdx.x; k < nrbb; k += blockDim.x) {
       if (sbr[k] != 0.0) atomicAdd(&br[k], sbr[k]);
       if (sbe[k] != 0.0) atomicAdd(&be[k], sbe[k]);
@@ -124,7 +219,7 @@ __global__ void k_getbnd(int nrbt, const int *__restrict__ ibi,
   }
 }
 
-template <typename R>
+template <typename R, bool ENER>
 __global__ void k_getang(int nrat, const int *__restrict__ iai,
                          const int *__restrict__ jaj, const int *__restrict__ kak,
                          const int *__restrict__ iauk, const double *__restrict__ ra,
@@ -138,61 +233,96 @@ __global__ void k_getang(int nrat, const int *__restrict__ iai,
     for (int k = threadIdx.x; k < 256; k += blockDim.x) sar[k] = sae[k] = 0.0;
     __syncthreads();
   }
-  double acc[4] = {0, 0, 0, 0};  // PINT VIRFX VIRFY VIRFZ
+  double acc[5] = {0, 0, 0, 0, 0};  // PINT (VIRB) VIRFX VIRFY VIRFZ
   const int N = blockIdx.x * blockDim.x + threadIdx.x;
   if (N < nrat) {
     const int I = iai[N], J = jaj[N], K = kak[N], M = iauk[N];
     const int ityp = ainfo[I].x;
-    const R FCN = (R)fa[M], AEQ = (R)ra[M];
-    double ax, ay, az, bxv, byv, bzv;
-    vec(pos, I, J, bx, by, bz, ax, ay, az);
-    vec(pos, K, J, bx, by, bz, bxv, byv, bzv);
-    const R AX = (R)ax, AY = (R)ay, AZ = (R)az;
-    const R BX = (R)bxv, BY = (R)byv, BZ = (R)bzv;
-    const R ASQ = AX * AX + AY * AY + AZ * AZ;
-    const R ASQI = R(1) / ASQ;
-    const R BSQ = BX * BX + BY * BY + BZ * BZ;
-    const R BSQI = R(1) / BSQ;
-    const R AB = sqrt(ASQ * BSQ);
-    const R ABI = R(1) / AB;
-    R COSA = AX * BX + AY * BY + AZ * BZ;
-    COSA = COSA * ABI;
-    COSA = fmin(COSA, R(1));
-    COSA = fmax(COSA, R(-1));
-    const R ALF = acos(COSA);
-    const R SINA = sin(ALF);
-    const R SINAI = R(1) / SINA;
-    const R DALF = ALF - AEQ;
-    const R ABC = DALF * FCN;
-    const R EANG = ABC * DALF;
-    acc[0] = (double)EANG;
+    R ALF, EA;
+    angle_term<R, false>(pos, I, J, K, M, ra, fa, tc.lmove[ityp], bx, by, bz, o, acc, &ALF,
+                         &EA);
     if (laver) {
       const double fnspi = 1.0 / (double)nspec[ityp];
       avg_add(sar, ar, M, nraa, (double)ALF * fnspi);
-      avg_add(sae, ae, M, nraa, (double)EANG * fnspi);
-    }
-    if (tc.lmove[ityp]) {
-      const R SAB = R(-2) * ABC * SINAI;
-      const R CAB = SAB * COSA;
-      const R FAB = SAB * ABI;
-      const R FAA = CAB * ASQI;
-      const R FBB = CAB * BSQI;
-      const R FAX = FAB * BX - FAA * AX, FAY = FAB * BY - FAA * AY, FAZ = FAB * BZ - FAA * AZ;
-      const R FBX = FAB * AX - FBB * BX, FBY = FAB * AY - FBB * BY, FBZ = FAB * AZ - FBB * BZ;
-      add_force<R>(o, I, -FAX, -FAY, -FAZ);
-      add_force<R>(o, J, FAX + FBX, FAY + FBY, FAZ + FBZ);
-      add_force<R>(o, K, -FBX, -FBY, -FBZ);
-      acc[1] = (double)(-AX * FAX - BX * FBX);
-      acc[2] = (double)(-AY * FAY - BY * FBY);
-      acc[3] = (double)(-AZ * FAZ - BZ * FBZ);
+      avg_add(sae, ae, M, nraa, (double)EA * fnspi);
     }
   }
-  block_add<4>(acc, dst);
+  if (ENER) {
+    double a4[4] = {acc[0], acc[2], acc[3], acc[4]};
+    block_add<4>(a4, dst);
+  }
   if (laver && nraa <= 256) {
+    __syncthreads();
     for (int k = threadIdx.x; k < nraa; k += blockDim.x) {
       if (sar[k] != 0.0) atomicAdd(&ar[k], sar[k]);
       if (sae[k] != 0.0) atomicAdd(&ae[k], sae[k]);
     }
+  }
+}
+
+// Bonds and angles of small molecule types, one thread per molecule: every
+// atom a thread touches belongs to its molecule, so forces are added
+// without atomics (same per-term rounding, so the sums are identical).
+template <typename R, bool ENER>
+__global__ void __launch_bounds__(128) k_molbonded(
+    int ntpl, const MolTpl *__restrict__ tpl, const int *__restrict__ bid,
+    const double *__restrict__ rb, const double *__restrict__ fb,
+    const double *__restrict__ db, const double *__restrict__ ro,
+    const double *__restrict__ ra, const double *__restrict__ fa,
+    const dbl4 *__restrict__ pos, TypeConst tc, const int *__restrict__ nspec, double bx,
+    double by, double bz, BondOut o, Dst6 dst, int nrbb, int nraa, int laver, double *br,
+    double *be, double *ar, double *ae) {
+  __shared__ double sav[4][256];  // BR BE AR AE per record (laver)
+  if (laver) {
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x) sav[k / 256][k % 256] = 0.0;
+    __syncthreads();
+  }
+  double acc[5] = {0, 0, 0, 0, 0};  // PINT VIRB VIRFX VIRFY VIRFZ
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = 0;
+  while (t < ntpl && g >= tpl[t].nmol) {
+    g -= tpl[t].nmol;
+    ++t;
+  }
+  if (t < ntpl) {
+    const MolTpl &T = tpl[t];
+    const int base = T.first + g * T.nsit;
+    const int lmove = tc.lmove[T.type];
+    const double fnspi = 1.0 / (double)nspec[T.type];
+    for (int b = 0; b < T.nb; ++b) {
+      const int M = T.bm[b];
+      R BD, EB;
+      bond_term<R, true>(pos, base + T.bi[b], base + T.bj[b], M, bid, rb, fb, db, ro, lmove,
+                         bx, by, bz, o, acc, &BD, &EB);
+      if (laver) {
+        avg_add(sav[0], br, M, nrbb, (double)BD * fnspi);
+        avg_add(sav[1], be, M, nrbb, (double)EB * fnspi);
+      }
+    }
+    for (int a = 0; a < T.na; ++a) {
+      const int M = T.am[a];
+      R ALF, EA;
+      angle_term<R, true>(pos, base + T.ai[a], base + T.aj[a], base + T.ak[a], M, ra, fa,
+                          lmove, bx, by, bz, o, acc, &ALF, &EA);
+      if (laver) {
+        avg_add(sav[2], ar, M, nraa, (double)ALF * fnspi);
+        avg_add(sav[3], ae, M, nraa, (double)EA * fnspi);
+      }
+    }
+  }
+  if (ENER) block_add<5>(acc, dst);
+  if (laver) {
+    __syncthreads();
+    if (nrbb <= 256)
+      for (int k = threadIdx.x; k < nrbb; k += blockDim.x) {
+        if (sav[0][k] != 0.0) atomicAdd(&br[k], sav[0][k]);
+        if (sav[1][k] != 0.0) atomicAdd(&be[k], sav[1][k]);
+      }
+    if (nraa <= 256)
+      for (int k = threadIdx.x; k < nraa; k += blockDim.x) {
+        if (sav[2][k] != 0.0) atomicAdd(&ar[k], sav[2][k]);
+        if (sav[3][k] != 0.0) atomicAdd(&ae[k], sav[3][k]);
+      }
   }
 }
 
@@ -431,7 +561,7 @@ __global__ void k_strbnd(WaterPar w, const dbl4 *__restrict__ pos, double bxl,
 
 }  // namespace
 
-int launch_bonded(mdx_ctx *ctx, int laver) {
+int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
   MDX_TIMER(ctx, MDX_T_BONDED);
   DevData &d = ctx->dv;
   mdx_scalars *sc = d.sc;
@@ -476,23 +606,46 @@ int launch_bonded(mdx_ctx *ctx, int laver) {
       k_strbnd<double><<<(w.nmol + T - 1) / T, T, 0, ctx->stream>>>(w, d.pos, bx, by, bz, o, dst, laver, d.br, d.be);
     MDX_LAUNCHED(ctx);
   }
+  if (d.ntpl > 0) {
+    const int nb = (d.ntpl_mol + T - 1) / T;
+    Dst6 dst = dst6(ctx, nb, 5, &sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz);
+#define GM(R, E)                                                                       \
+  k_molbonded<R, E><<<nb, T, 0, ctx->stream>>>(                                         \
+      d.ntpl, d.moltpl, d.bid, d.brb, d.bfb, d.bdb, d.bro, d.ara, d.afa, d.pos, ctx->tc, \
+      nspec, bx, by, bz, o, dst, d.nrbb, d.nraa, laver, d.br, d.be, d.ar, d.ae)
+    if (mx) {
+      if (ener) GM(float, true); else GM(float, false);
+    } else {
+      if (ener) GM(double, true); else GM(double, false);
+    }
+#undef GM
+    MDX_LAUNCHED(ctx);
+  }
   if (d.nrbt > 0) {
     Dst6 dst = dst6(ctx, (d.nrbt + T - 1) / T, 5, &sc->pint, &sc->virb, &sc->virfx, &sc->virfy, &sc->virfz);
-#define GB(R)                                                                          \
-  k_getbnd<R><<<(d.nrbt + T - 1) / T, T, 0, ctx->stream>>>(                            \
+#define GB(R, E)                                                                       \
+  k_getbnd<R, E><<<(d.nrbt + T - 1) / T, T, 0, ctx->stream>>>(                         \
       d.nrbt, d.ibi, d.jbj, d.ibuk, d.bid, d.brb, d.bfb, d.bdb, d.bro, d.pos, d.ainfo, \
       ctx->tc, nspec, bx, by, bz, o, dst, d.nrbb, laver, d.br, d.be)
-    if (mx) GB(float); else GB(double);
+    if (mx) {
+      if (ener) GB(float, true); else GB(float, false);
+    } else {
+      if (ener) GB(double, true); else GB(double, false);
+    }
 #undef GB
     MDX_LAUNCHED(ctx);
   }
   if (d.nrat > 0) {
     Dst6 dst = dst6(ctx, (d.nrat + T - 1) / T, 4, &sc->pint, &sc->virfx, &sc->virfy, &sc->virfz);
-#define GA(R)                                                                          \
-  k_getang<R><<<(d.nrat + T - 1) / T, T, 0, ctx->stream>>>(                            \
+#define GA(R, E)                                                                       \
+  k_getang<R, E><<<(d.nrat + T - 1) / T, T, 0, ctx->stream>>>(                         \
       d.nrat, d.iai, d.jaj, d.kak, d.iauk, d.ara, d.afa, d.pos, d.ainfo, ctx->tc,      \
       nspec, bx, by, bz, o, dst, d.nraa, laver, d.ar, d.ae)
-    if (mx) GA(float); else GA(double);
+    if (mx) {
+      if (ener) GA(float, true); else GA(float, false);
+    } else {
+      if (ener) GA(double, true); else GA(double, false);
+    }
 #undef GA
     MDX_LAUNCHED(ctx);
   }

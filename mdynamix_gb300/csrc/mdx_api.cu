@@ -20,7 +20,7 @@ int launch_leapfrog_shake(mdx_ctx *ctx);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 size_t scal_scratch_bytes();
 // bonded.cu
-int launch_bonded(mdx_ctx *ctx, int laver);
+int launch_bonded(mdx_ctx *ctx, int laver, bool ener = true);
 
 namespace {
 
@@ -181,12 +181,15 @@ int require(mdx_ctx *ctx, bool topo, bool par, bool state) {
 }
 
 // ---------------------------------------------------------------- forces
-int do_fforces(mdx_ctx *ctx, int laver, bool split) {
+// ener = false: an intermediate short step of DOUBLE, whose fast energies
+// and virials the next FFORCES zeroes before anything reads them; the pair
+// sweep then computes forces only.
+int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true) {
   RC(launch_zero_fast(ctx));
   if (ctx->mixed()) RC(launch_mirror_f32(ctx));
-  RC(launch_localf(ctx, split));
-  RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
-  RC(launch_bonded(ctx, laver));
+  RC(launch_localf(ctx, split, ener));
+  if (ener) RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
+  RC(launch_bonded(ctx, laver, ener));
   if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
   RC(launch_sclfrc(ctx, 1));
   return MDX_OK;
@@ -257,7 +260,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
       RC(do_slforces(ctx, false));
       RC(do_fforces(ctx, 0, false));
     } else {
-      RC(do_fforces(ctx, 0, false));
+      RC(do_fforces(ctx, 0, false, false));
     }
   }
   RC(launch_kick(ctx, 1, HTSTEB, false));
@@ -492,7 +495,7 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
 int mdx_close(mdx_ctx *ctx) {
   if (!ctx) return MDX_OK;
   DevData &d = ctx->dv;
-  void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.vx, d.massdi, d.amass, d.qsite,
+  void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.stab, d.pinfo, d.moltpl, d.vx, d.massdi, d.amass, d.qsite,
                   d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
                   d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
                   d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f,
@@ -512,6 +515,120 @@ int mdx_close(mdx_ctx *ctx) {
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
+  return MDX_OK;
+}
+
+// Bonds and angles of small molecule types (at most ML_MAXS sites, no
+// STRBND water potential, no torsions, the same terms in every molecule, in
+// BNDLST's per-molecule order) become one template per type for the
+// molecule-local kernel; every other instance stays in the lists.
+static int split_bonded(mdx_ctx *ctx, const mdx_topo *t) {
+  DevData &d = ctx->dv;
+  const int nt = ctx->d.ntypes, nb_all = ctx->d.nrbt, na_all = ctx->d.nrat;
+  std::vector<char> ok(nt, 0);
+  std::vector<MolTpl> tpl(nt);
+  std::vector<int> first(nt), nsit(nt);
+  for (int k = 0; k < nt; ++k) {
+    first[k] = t->isaddr[k];
+    nsit[k] = t->nsits[k];
+    ok[k] = t->nsits[k] <= ML_MAXS && t->ipot[k] != 1 && t->ipot[k] != 2 && t->nspec[k] > 0;
+    MolTpl &m = tpl[k];
+    std::memset(&m, 0, sizeof m);
+    m.first = first[k];
+    m.nmol = t->nspec[k];
+    m.nsit = nsit[k];
+    m.type = k;
+  }
+  auto typ = [&](int atom0) { return t->itype[atom0] - 1; };
+  for (int N = 0; N < ctx->d.nrrt; ++N) ok[typ(t->iti[N] - 1)] = 0;
+  // templates from each type's first molecule
+  for (int N = 0; N < nb_all; ++N) {
+    const int I = t->ibi[N] - 1, J = t->jbj[N] - 1, k = typ(I);
+    if (!ok[k] || I - first[k] >= nsit[k]) continue;
+    MolTpl &m = tpl[k];
+    if (m.nb == ML_MAXB || J - first[k] >= nsit[k] || J < first[k]) { ok[k] = 0; continue; }
+    m.bi[m.nb] = (unsigned char)(I - first[k]);
+    m.bj[m.nb] = (unsigned char)(J - first[k]);
+    m.bm[m.nb] = (short)(t->ibuk[N] - 1);
+    ++m.nb;
+  }
+  for (int N = 0; N < na_all; ++N) {
+    const int I = t->iai[N] - 1, J = t->jaj[N] - 1, K = t->kak[N] - 1, k = typ(I);
+    if (!ok[k] || I - first[k] >= nsit[k]) continue;
+    MolTpl &m = tpl[k];
+    if (m.na == ML_MAXA || J < first[k] || K < first[k] || J - first[k] >= nsit[k] ||
+        K - first[k] >= nsit[k]) { ok[k] = 0; continue; }
+    m.ai[m.na] = (unsigned char)(I - first[k]);
+    m.aj[m.na] = (unsigned char)(J - first[k]);
+    m.ak[m.na] = (unsigned char)(K - first[k]);
+    m.am[m.na] = (short)(t->iauk[N] - 1);
+    ++m.na;
+  }
+  // every molecule must repeat its type's template in order
+  std::vector<int> seen(nt, 0);
+  for (int N = 0; N < nb_all; ++N) {
+    const int I = t->ibi[N] - 1, k = typ(I);
+    if (!ok[k]) continue;
+    const MolTpl &m = tpl[k];
+    const int q = seen[k]++, b = m.nb ? q % m.nb : 0, base = first[k] + (m.nb ? q / m.nb : 0) * nsit[k];
+    if (!m.nb || I != base + m.bi[b] || t->jbj[N] - 1 != base + m.bj[b] || t->ibuk[N] - 1 != m.bm[b])
+      ok[k] = 0;
+  }
+  for (int k = 0; k < nt; ++k)
+    if (ok[k] && seen[k] != tpl[k].nb * tpl[k].nmol) ok[k] = 0;
+  std::fill(seen.begin(), seen.end(), 0);
+  for (int N = 0; N < na_all; ++N) {
+    const int I = t->iai[N] - 1, k = typ(I);
+    if (!ok[k]) continue;
+    const MolTpl &m = tpl[k];
+    const int q = seen[k]++, a = m.na ? q % m.na : 0, base = first[k] + (m.na ? q / m.na : 0) * nsit[k];
+    if (!m.na || I != base + m.ai[a] || t->jaj[N] - 1 != base + m.aj[a] ||
+        t->kak[N] - 1 != base + m.ak[a] || t->iauk[N] - 1 != m.am[a])
+      ok[k] = 0;
+  }
+  for (int k = 0; k < nt; ++k)
+    if (ok[k] && seen[k] != tpl[k].na * tpl[k].nmol) ok[k] = 0;
+  // templates in use and the remaining instance lists
+  std::vector<MolTpl> use;
+  for (int k = 0; k < nt; ++k)
+    if (ok[k] && (tpl[k].nb || tpl[k].na)) use.push_back(tpl[k]);
+    else ok[k] = 0;
+  std::vector<int> bi, bj, bm, ai, aj, ak, am;
+  for (int N = 0; N < nb_all; ++N)
+    if (!ok[typ(t->ibi[N] - 1)]) {
+      bi.push_back(t->ibi[N] - 1);
+      bj.push_back(t->jbj[N] - 1);
+      bm.push_back(t->ibuk[N] - 1);
+    }
+  for (int N = 0; N < na_all; ++N)
+    if (!ok[typ(t->iai[N] - 1)]) {
+      ai.push_back(t->iai[N] - 1);
+      aj.push_back(t->jaj[N] - 1);
+      ak.push_back(t->kak[N] - 1);
+      am.push_back(t->iauk[N] - 1);
+    }
+  d.nrbt = (int)bi.size();
+  d.nrat = (int)ai.size();
+  if (d.nrbt) {
+    RC(upload(ctx, d.ibi, bi.data(), d.nrbt));
+    RC(upload(ctx, d.jbj, bj.data(), d.nrbt));
+    RC(upload(ctx, d.ibuk, bm.data(), d.nrbt));
+  }
+  if (d.nrat) {
+    RC(upload(ctx, d.iai, ai.data(), d.nrat));
+    RC(upload(ctx, d.jaj, aj.data(), d.nrat));
+    RC(upload(ctx, d.kak, ak.data(), d.nrat));
+    RC(upload(ctx, d.iauk, am.data(), d.nrat));
+  }
+  ctx_free(ctx, d.moltpl);
+  d.moltpl = nullptr;
+  d.ntpl = (int)use.size();
+  d.ntpl_mol = 0;
+  for (const MolTpl &m : use) d.ntpl_mol += m.nmol;
+  if (d.ntpl) {
+    RC(dmalloc(ctx, &d.moltpl, use.size()));
+    RC(upload(ctx, d.moltpl, use.data(), use.size()));
+  }
   return MDX_OK;
 }
 
@@ -570,6 +687,18 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
   RC(upload(ctx, d.qsite, qsite.data(), n));
   RC(upload(ctx, d.qsitef, qsitef.data(), n));
   ctx->h_q.assign(t->q, t->q + n);
+  if (ctx->mixed()) {
+    if (ns >= (1 << MDX_SITE_BITS) || d.nop >= (1 << (32 - MDX_SITE_BITS))) {
+      ctx->err = "mixed path: at most 8191 sites and 524287 molecules";
+      return MDX_ERR_UNSUPPORTED;
+    }
+    std::vector<int> pinfo(n);
+    for (int i = 0; i < n; ++i)
+      pinfo[i] = (int)(((unsigned)(t->nnum[i] - 1) << MDX_SITE_BITS) | (unsigned)(t->nsite[i] - 1));
+    RC(dmalloc(ctx, &d.pinfo, n));
+    RC(dmalloc(ctx, &d.stab, (size_t)ns));
+    RC(upload(ctx, d.pinfo, pinfo.data(), n));
+  }
   // molecules: atoms are contiguous per molecule, molecules per type
   std::vector<int> mf(d.nop, -1), mn(d.nop, 0), mt(d.nop, 0);
   for (int i = 0; i < n; ++i) {
@@ -670,22 +799,9 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
   RC(upload(ctx, d.bfb, t->fb, d.nrbb));
   RC(upload(ctx, d.bdb, t->db, d.nrbb));
   RC(upload(ctx, d.bro, t->ro, d.nrbb));
-  if (d.nrbt) {
-    auto a = m1(t->ibi, d.nrbt), b = m1(t->jbj, d.nrbt), c = m1(t->ibuk, d.nrbt);
-    RC(upload(ctx, d.ibi, a.data(), d.nrbt));
-    RC(upload(ctx, d.jbj, b.data(), d.nrbt));
-    RC(upload(ctx, d.ibuk, c.data(), d.nrbt));
-  }
   RC(upload(ctx, d.ara, t->ra, d.nraa));
   RC(upload(ctx, d.afa, t->fa, d.nraa));
-  if (d.nrat) {
-    auto a = m1(t->iai, d.nrat), b = m1(t->jaj, d.nrat), c = m1(t->kak, d.nrat),
-         e = m1(t->iauk, d.nrat);
-    RC(upload(ctx, d.iai, a.data(), d.nrat));
-    RC(upload(ctx, d.jaj, b.data(), d.nrat));
-    RC(upload(ctx, d.kak, c.data(), d.nrat));
-    RC(upload(ctx, d.iauk, e.data(), d.nrat));
-  }
+  RC(split_bonded(ctx, t));
   RC(upload(ctx, d.titors, t->itors, d.nrtt));
   RC(upload(ctx, d.tnmul, t->nmul, d.nrtt));
   RC(upload(ctx, d.tft, t->ft, d.nrtt));
@@ -705,6 +821,7 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
     RC(upload(ctx, d.ituk, f.data(), d.nrrt));
   }
   RC(upload(ctx, d.nspec_d, t->nspec, nt));
+  if (ctx->mixed()) RC(upload_site_table(ctx));
   ctx->have_topo = true;
   return MDX_OK;
 }
@@ -1056,6 +1173,7 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
     ctx_free(ctx, dq);
     cudaStreamSynchronize(ctx->stream);
   }
+  if (ctx->mixed()) RC(upload_site_table(ctx));
   return MDX_OK;
 }
 
@@ -1094,6 +1212,38 @@ int mdx_sync(mdx_ctx *ctx) {
 }
 
 }  // extern "C"
+
+// Site table of the mixed pair kernels: per site the EE-scaled charge Q (the
+// same for every atom of a site: RECINT scales by molecule type,
+// mdee.f:119-127), the raw CHARGE, the LJ type and the molecule type.
+static float int_bits(int v) {
+  float f;
+  std::memcpy(&f, &v, sizeof f);
+  return f;
+}
+
+int upload_site_table(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  const int n = d.n, ns = ctx->d.nsites;
+  std::vector<float4> st(ns);
+  std::vector<char> seen(ns, 0);
+  for (int i = 0; i < n; ++i) {
+    const int site = ctx->h_nsite[i] - 1;
+    const float q = (float)ctx->h_q[i];
+    if (seen[site] && st[site].x != q) {
+      ctx->err = "mixed path: atoms of one site carry different charges";
+      return MDX_ERR_UNSUPPORTED;
+    }
+    seen[site] = 1;
+    st[site] = make_float4(q, (float)ctx->h_charge[site],
+                           int_bits(ctx->h_inbt[site] - 1),
+                           int_bits(ctx->h_itype[i] - 1));
+  }
+  for (int s = 0; s < ns; ++s)
+    if (!seen[s]) st[s] = make_float4(0.f, (float)ctx->h_charge[s], int_bits(ctx->h_inbt[s] - 1),
+                                      int_bits(0));
+  return upload(ctx, d.stab, st.data(), (size_t)ns);
+}
 
 // Linkage for noalloc.cu and pimd.cu (the helpers above have internal
 // linkage).

@@ -80,6 +80,19 @@ struct KCol {
   int wpos;                // slot of (nz = nzlo) in the grouped W array
 };
 
+// Bonds and angles of one small molecule type, atoms as offsets within the
+// molecule, for the molecule-local bonded kernel.
+constexpr int ML_MAXS = 8, ML_MAXB = 16, ML_MAXA = 24;
+struct MolTpl {
+  int first, nmol, nsit, nb, na, type;
+  unsigned char bi[ML_MAXB], bj[ML_MAXB];
+  short bm[ML_MAXB];
+  unsigned char ai[ML_MAXA], aj[ML_MAXA], ak[ML_MAXA];
+  short am[ML_MAXA];
+};
+
+constexpr int MDX_SITE_BITS = 13;  // sites < 8192, molecules < 2^19 (mixed path)
+
 // Four columns with the same nz range, for the mixed force pass: their W
 // values are interleaved (wg[4 (woff + t) + slot]) so one z-table load feeds
 // four columns.  col[s] < 0 marks a padding slot (W = 0).
@@ -151,6 +164,14 @@ struct DevData {
   double2 *sk;                  // structure factors, column order
   dbl4 *wk;                     // (W, RZV W) per k, W = AK2*conj(S)
   float4 *wkf;                  // FP32 copy for the mixed force pass, grouped
+  // mixed pair path: posi.w = (molecule << MDX_SITE_BITS) | site, and per
+  // site {Q (EE-scaled), CHARGE, LJ type, molecule type} as float4 bits
+  float4 *stab;
+  int *pinfo;
+  // small molecule types handled per molecule (bonds, angles); the instance
+  // lists ibi.. / iai.. then hold only the other types' terms
+  MolTpl *moltpl;
+  int ntpl, ntpl_mol;
   KGroup *kgroups;              // column groups of the mixed force pass
   int ngroup;
   void *sitems;                 // work items of the mixed S(k) pass
@@ -446,7 +467,7 @@ int launch_build_lists(mdx_ctx *ctx);
 int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
 // pair.cu
-int launch_localf(mdx_ctx *ctx, bool split);
+int launch_localf(mdx_ctx *ctx, bool split, bool ener = true);
 int launch_forces_long(mdx_ctx *ctx, bool split);
 int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 // ewald.cu
@@ -474,3 +495,4 @@ int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);
+int upload_site_table(mdx_ctx *ctx);  // mdx_api.cu: stab from the current charges

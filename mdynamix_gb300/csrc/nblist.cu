@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(BLK) k_build(
 // fixed-point coordinates: round(x / L * 2^32) kept modulo 2^32.
 __global__ void k_mirror(int n, const dbl4 *__restrict__ pos,
                          float4 *__restrict__ posf, int4 *__restrict__ posi,
-                         double ibx, double iby, double ibz) {
+                         const int *__restrict__ pinfo, double ibx, double iby,
+                         double ibz) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   dbl4 p = pos[i];
@@ -239,8 +240,7 @@ __global__ void k_mirror(int n, const dbl4 *__restrict__ pos,
     long long zi = __double2ll_rn(p.z * ibz * two32);
     posi[i] = make_int4((int)(unsigned)(unsigned long long)xi,
                         (int)(unsigned)(unsigned long long)yi,
-                        (int)(unsigned)(unsigned long long)zi,
-                        __float_as_int((float)p.w));
+                        (int)(unsigned)(unsigned long long)zi, pinfo[i]);
   }
 }
 
@@ -275,7 +275,7 @@ int launch_mirror_f32(mdx_ctx *ctx) {
   MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   k_mirror<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
-      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, 1.0 / ctx->boxl,
+      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
       1.0 / ctx->boyl, 1.0 / ctx->bozl);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
@@ -313,7 +313,7 @@ int launch_build_lists(mdx_ctx *ctx) {
                            ctx->stream));
   const int T = 256;
   k_mirror<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
-      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, 1.0 / ctx->boxl,
+      d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
       1.0 / ctx->boyl, 1.0 / ctx->bozl);
   MDX_LAUNCHED(ctx);
   k_cell_count<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(d.n, d.pos, b, g,

@@ -48,7 +48,7 @@ __device__ __forceinline__ float ewald_erfc_polyf(float ttt, float exp2a) {
 }
 
 // ---------------------------------------------------------------- FP64 ---
-template <bool SHORT, bool SPLIT>
+template <bool SHORT, bool SPLIT, bool ENER>
 __global__ void __launch_bounds__(256) k_pair64(
     int n, const dbl4 *__restrict__ pos, const int4 *__restrict__ ainfo,
     const double *__restrict__ qsite, const int *__restrict__ cnt,
@@ -124,10 +124,10 @@ __global__ void __launch_bounds__(256) k_pair64(
         EES = EE1;
         if (SHORT) {
           FORCE = QIJ * (1. / (R1E * R1E * R1E) + pc.rff2);
-          acc[P_VIR] += QIJ * (1.5 * pc.rff2 / (R1E * R1E) - pc.rff);
+          if (ENER) acc[P_VIR] += QIJ * (1.5 * pc.rff2 / (R1E * R1E) - pc.rff);
         } else {
           FORCE = QIJ * (1.0 / ((R1E * R1E) * R1) + pc.rff2);
-          acc[P_VIR] += QIJ * (1.5 * pc.rff2 * RR - pc.rff);
+          if (ENER) acc[P_VIR] += QIJ * (1.5 * pc.rff2 * RR - pc.rff);
         }
       } else {
         const double ALPHAR = pc.alphad * R1;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(256) k_pair64(
         if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], EE1);
         else atomicAdd(&s_split[mtr], EE1);
       }
-      acc[P_EES] += EES;
+      if (ENER) acc[P_EES] += EES;
       if (B12 != 0.0) {
         const double R2I = R1EI * R1EI;
         const double R6I = R2I * R2I * R2I;
@@ -153,25 +153,25 @@ __global__ void __launch_bounds__(256) k_pair64(
           if (SHORT) {
             if (tc.lmove[ti]) {
               if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], ESR);
-              acc[P_VIR] += FSR * R1;
+              if (ENER) acc[P_VIR] += FSR * R1;
             } else {
               ESR = 0.0;
               FORCE = 0.0;
             }
           } else {
-            if (tc.lmove[ti]) acc[P_VIR] += FSR * R1;
+            if (ENER && tc.lmove[ti]) acc[P_VIR] += FSR * R1;
             if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], ESR);
           }
         } else {
           if (SPLIT) atomicAdd(&s_split[MDX_NTPP + mtr], ESR);
-          acc[P_VIR] += FSR * R1;
+          if (ENER) acc[P_VIR] += FSR * R1;
         }
-        acc[P_ESR] += ESR;
+        if (ENER) acc[P_ESR] += ESR;
       }
       if (SHORT || !same || tc.lmove[ti]) {
-        acc[3] += FORCE * (DX * DX);
-        acc[4] += FORCE * (DY * DY);
-        acc[5] += FORCE * (DZ * DZ);
+        if (ENER) acc[3] += FORCE * (DX * DX);
+        if (ENER) acc[4] += FORCE * (DY * DY);
+        if (ENER) acc[5] += FORCE * (DZ * DZ);
       }
       const double gxv = FORCE * DX, gyv = FORCE * DY, gzv = FORCE * DZ;
       fix += gxv;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) k_pair64(
       atomicAdd(&fz[i], fiz);
     }
   }
-  block_add<6>(acc, dst);
+  if (ENER) block_add<6>(acc, dst);
   if (SPLIT) {
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x)
@@ -240,10 +240,9 @@ __device__ __forceinline__ float idiff(int a, int b, float s) {
   return (float)(int)((unsigned)a - (unsigned)b) * s;
 }
 
-template <bool SHORT, bool SPLIT>
+template <bool SHORT, bool SPLIT, bool ENER>
 __global__ void __launch_bounds__(256) k_pair32(
-    int n, const int4 *__restrict__ posi, const dbl4 *__restrict__ pos,
-    const int4 *__restrict__ ainfo, const float *__restrict__ qsitef,
+    int n, const int4 *__restrict__ posi, const float4 *__restrict__ stab,
     const int *__restrict__ cnt, const int *__restrict__ idx, int cap,
     PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
     FixScale fsc, unsigned long long *__restrict__ ffix,
@@ -261,11 +260,15 @@ __global__ void __launch_bounds__(256) k_pair32(
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
   if (i < n) {
+    // one 16-byte record per atom: fixed-point x, y, z and (molecule, site);
+    // charges and types come from the per-site table (L1-resident)
+    constexpr unsigned SITE_MASK = (1u << MDX_SITE_BITS) - 1u;
     const int4 pi = posi[i];
-    const int4 ai = ainfo[i];
-    const int ti = ai.x, mi = ai.y, ni = ai.z;
-    const float qi = __int_as_float(pi.w);
-    const float qsi = qsitef[i];
+    const float4 sti = __ldg(&stab[(unsigned)pi.w & SITE_MASK]);
+    const unsigned mi = (unsigned)pi.w >> MDX_SITE_BITS;
+    const int ti = __float_as_int(sti.w), ni = __float_as_int(sti.z);
+    const float qi = sti.x;
+    const float qsi = sti.y;
     const float coulf = (float)pc.coulf, alphad = (float)pc.alphad;
     const float raex = (float)pc.raex;
     const int c = cnt[i];
@@ -274,28 +277,34 @@ __global__ void __launch_bounds__(256) k_pair32(
 #pragma unroll
     for (int k = 0; k < P_NSLOT; ++k) a[k] = 0.f;
     const int *row = idx + (size_t)i * cap;
+    // the next entry's index and record are loaded while this one computes
+    int v = lane < c ? row[lane] : 0;
+    int4 pj = posi[v & 0x7fffffff];
     for (int k = lane; k < c; k += 32) {
-      const int v = row[k];
+      int vn = 0;
+      int4 pjn = pj;
+      if (k + 32 < c) {
+        vn = row[k + 32];
+        pjn = posi[vn & 0x7fffffff];
+      }
       const bool is14 = SHORT && v < 0;
-      const int j = v & 0x7fffffff;
-      const int4 pj = posi[j];
-      const int4 aj = ainfo[j];
-      const int tj = aj.x, nj = aj.z;
-      const bool same = aj.y == mi;
+      const float4 stj = __ldg(&stab[(unsigned)pj.w & SITE_MASK]);
+      const int tj = __float_as_int(stj.w), nj = __float_as_int(stj.z);
+      const bool same = ((unsigned)pj.w >> MDX_SITE_BITS) == mi;
       const int tix = ni * pc.nnbt + nj;
       float QIJ, A6, B12, RAE = 0.f;
       if (same) {
         if (is14) {
-          QIJ = qsi * qsitef[j] * coulf * tc.c14elf[ti];
+          QIJ = qsi * stj.y * coulf * tc.c14elf[ti];
           A6 = __ldg(&tb.a614f[tix]) * tc.c14ljf[ti];
           B12 = __ldg(&tb.b1214f[tix]) * tc.c14ljf[ti];
         } else {
-          QIJ = qsi * qsitef[j] * coulf;
+          QIJ = qsi * stj.y * coulf;
           A6 = __ldg(&tb.a60f[tix]);
           B12 = __ldg(&tb.b120f[tix]);
         }
       } else {
-        QIJ = qi * __int_as_float(pj.w) * coulf;
+        QIJ = qi * stj.x * coulf;
         A6 = __ldg(&tb.a6f[tix]);
         B12 = __ldg(&tb.b12f[tix]);
         if (pc.lmdee) RAE = (tc.iee[ti] * tc.iee[tj] == 0) ? raex : 0.f;
@@ -319,10 +328,10 @@ __global__ void __launch_bounds__(256) k_pair32(
         EES = EE1;
         if (SHORT) {
           FORCE = QIJ * (R1EI * R1EI * R1EI + rff2);
-          a[P_VIR] += QIJ * (1.5f * rff2 * R1EI * R1EI - rff);
+          if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * R1EI * R1EI - rff);
         } else {
           FORCE = QIJ * (R1EI * R1EI * R1I + rff2);
-          a[P_VIR] += QIJ * (1.5f * rff2 * RR - rff);
+          if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * RR - rff);
         }
       } else {
         const float ALPHAR = alphad * R1;
@@ -338,8 +347,11 @@ __global__ void __launch_bounds__(256) k_pair32(
         if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], (double)EE1);
         else atomicAdd(&s_split[mtr], (double)EE1);
       }
-      if (same) a[P_EE_SAME] += EE1; else a[P_EE_DIFF] += EE1;
-      a[P_EES] += EES;
+      if (ENER) {
+        if (same) a[P_EE_SAME] += EE1;
+        else a[P_EE_DIFF] += EE1;
+      }
+      if (ENER) a[P_EES] += EES;
       if (B12 != 0.f) {
         const float R2I = R1EI * R1EI;
         const float R6I = R2I * R2I * R2I;
@@ -350,34 +362,36 @@ __global__ void __launch_bounds__(256) k_pair32(
         if (same) {
           if (SHORT) {
             if (tc.lmove[ti]) {
-              a[P_VIR] += FSR * R1;
+              if (ENER) a[P_VIR] += FSR * R1;
             } else {
               ESR = 0.f;
               FORCE = 0.f;
               count_esr_split = false;
             }
           } else {
-            if (tc.lmove[ti]) a[P_VIR] += FSR * R1;
+            if (ENER && tc.lmove[ti]) a[P_VIR] += FSR * R1;
           }
           if (count_esr_split) {
-            a[P_ESR_SAME] += ESR;
+            if (ENER) a[P_ESR_SAME] += ESR;
             if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], (double)ESR);
           }
         } else {
-          a[P_ESR_DIFF] += ESR;
+          if (ENER) a[P_ESR_DIFF] += ESR;
           if (SPLIT) atomicAdd(&s_split[MDX_NTPP + tc.mdx[ti][tj]], (double)ESR);
-          a[P_VIR] += FSR * R1;
+          if (ENER) a[P_VIR] += FSR * R1;
         }
-        a[P_ESR] += ESR;
+        if (ENER) a[P_ESR] += ESR;
       }
       if (SHORT || !same || tc.lmove[ti]) {
-        a[P_VX] += FORCE * (DX * DX);
-        a[P_VY] += FORCE * (DY * DY);
-        a[P_VZ] += FORCE * (DZ * DZ);
+        if (ENER) a[P_VX] += FORCE * (DX * DX);
+        if (ENER) a[P_VY] += FORCE * (DY * DY);
+        if (ENER) a[P_VZ] += FORCE * (DZ * DZ);
       }
       fxa += FORCE * DX;
       fya += FORCE * DY;
       fza += FORCE * DZ;
+      v = vn;
+      pj = pjn;
     }
     // forces: lane partials -> fixed point -> integer warp sum -> one store
     // (no 64-bit conversion instruction: those issue on the FP64 pipe)
@@ -395,12 +409,15 @@ __global__ void __launch_bounds__(256) k_pair32(
       ffix[n + i] = (unsigned long long)qy;
       ffix[2 * n + i] = (unsigned long long)qz;
     }
+    if (ENER) {
 #pragma unroll
-    for (int k = 0; k < P_WIR; ++k) {
-      float t = warp_sumf(a[k]);
-      if (lane == 0) tot[k] = f2ll_rn(t * fsc.escalef);
+      for (int k = 0; k < P_WIR; ++k) {
+        float t = warp_sumf(a[k]);
+        if (lane == 0) tot[k] = f2ll_rn(t * fsc.escalef);
+      }
     }
   }
+  if (!ENER) return;  // forces only: no energy or virial slots
   // block sum of the integer slots, one atomic per slot per block
   __shared__ long long sh[8][P_NSLOT];
   const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -482,7 +499,10 @@ PairTables tables(const DevData &d) {
                     d.a6f,  d.b12f,  d.a60f,  d.b120f,  d.a614f, d.b1214f};
 }
 
-int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
+// ener = false: forces only (an intermediate short step of DOUBLE, whose fast
+// energies and virials are zeroed again by the next FFORCES before anything
+// reads them, forces.f:36-49).
+int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   DevData &d = ctx->dv;
   const int T = 256, WPB = T / 32;
   const int grid = (d.n + WPB - 1) / WPB;
@@ -496,13 +516,16 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
     Dst6 ddst = shrt ? dst6(ctx, grid, 6, &sc->pels2, &sc->pe2, &sc->vir2, &sc->virfx, &sc->virfy, &sc->virfz)
                      : dst6(ctx, grid, 6, &sc->pels1, &sc->pe1, &sc->vir1, &sc->virx, &sc->viry, &sc->virz);
 #define LP64(S, P)                                                                \
-  k_pair64<S, P><<<grid, T, 0, ctx->stream>>>(                                    \
+  if (ener) k_pair64<S, P, true><<<grid, T, 0, ctx->stream>>>(                    \
+      d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
+      ctx->boxl, ctx->boyl, ctx->bozl, fx, fy, fz, ddst, split_buf);              \
+  else k_pair64<S, P, false><<<grid, T, 0, ctx->stream>>>(                        \
       d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
       ctx->boxl, ctx->boyl, ctx->bozl, fx, fy, fz, ddst, split_buf)
     if (shrt) {
-      if (split) LP64(true, true); else LP64(true, false);
+      if (split) { LP64(true, true); } else { LP64(true, false); }
     } else {
-      if (split) LP64(false, true); else LP64(false, false);
+      if (split) { LP64(false, true); } else { LP64(false, false); }
     }
 #undef LP64
     MDX_LAUNCHED(ctx);
@@ -513,20 +536,26 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
 #define LP32(S, P)                                                                \
-  k_pair32<S, P><<<grid, T, 0, ctx->stream>>>(                                    \
-      d.n, d.posi, d.pos, d.ainfo, d.qsitef, cnt, idx, cap, tables(d),            \
+  if (ener) k_pair32<S, P, true><<<grid, T, 0, ctx->stream>>>(                    \
+      d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
+      ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
+      d.Y, d.Z, escale, slots, split_buf);                                        \
+  else k_pair32<S, P, false><<<grid, T, 0, ctx->stream>>>(                        \
+      d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf)
     if (shrt) {
-      if (split) LP32(true, true); else LP32(true, false);
+      if (split) { LP32(true, true); } else { LP32(true, false); }
     } else {
-      if (split) LP32(false, true); else LP32(false, false);
+      if (split) { LP32(false, true); } else { LP32(false, false); }
     }
 #undef LP32
     MDX_LAUNCHED(ctx);
-    k_fold_slots<<<1, 1, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
-                                            ctx->d.ntypes, split ? 1 : 0);
-    MDX_LAUNCHED(ctx);
+    if (ener) {
+      k_fold_slots<<<1, 1, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
+                                              ctx->d.ntypes, split ? 1 : 0);
+      MDX_LAUNCHED(ctx);
+    }
   }
   if (split) {
     k_fold_split<<<1, 64, 0, ctx->stream>>>(split_buf, d.sc);
@@ -537,10 +566,10 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split) {
 
 }  // namespace
 
-int launch_localf(mdx_ctx *ctx, bool split) {
-  MDX_TIMER(ctx, MDX_T_PAIR_SHORT); return launch_pair(ctx, true, split); }
+int launch_localf(mdx_ctx *ctx, bool split, bool ener) {
+  MDX_TIMER(ctx, MDX_T_PAIR_SHORT); return launch_pair(ctx, true, split, ener); }
 int launch_forces_long(mdx_ctx *ctx, bool split) {
-  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair(ctx, false, split); }
+  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair(ctx, false, split, true); }
 
 int launch_wir(mdx_ctx *ctx, int which) {
   MDX_TIMER(ctx, MDX_T_OTHER);
