@@ -473,29 +473,33 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-__global__ void __launch_bounds__(32 * RF_PARTS) k_rforce32(
+__global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
     int n, RfParts parts, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
     const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
     const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * n
-  extern __shared__ float2 srf[];  // [kx + ky + kz][RF_BATOMS]
+  // tab: the X, Y and Z tables back to back, row r at tab + r * n.  The Z
+  // rows (read every nz) are staged in shared memory; X and Y (read once per
+  // column) come through L1/L2, which keeps the block's shared memory small
+  // enough for more resident warps.
+  extern __shared__ float2 srf[];  // [kz][RF_BATOMS]
   __shared__ long long red[3][RF_PARTS][RF_BATOMS];
   __shared__ float4 ring[RF_PARTS][2][RF_WB * KGRP];
   const int lane = threadIdx.x % 32, part = threadIdx.x / 32;
   const int i0 = blockIdx.x * RF_BATOMS;
-  const int nrow = kx + ky + kz;
-  for (int k = threadIdx.x; k < nrow * RF_BATOMS; k += blockDim.x) {
+  const float2 *tz = tab + (size_t)(kx + ky) * n;
+  for (int k = threadIdx.x; k < kz * RF_BATOMS; k += blockDim.x) {
     const int r = k / RF_BATOMS, j = k - r * RF_BATOMS;
-    srf[k] = i0 + j < n ? tab[(size_t)r * n + i0 + j] : make_float2(0.f, 0.f);
+    srf[k] = i0 + j < n ? tz[(size_t)r * n + i0 + j] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   const float sc = fsc.scalef;
   long long ax[RF_APT], ay[RF_APT], az[RF_APT];
 #pragma unroll
   for (int q = 0; q < RF_APT; ++q) ax[q] = ay[q] = az[q] = 0;
-  const float2 *X = srf + lane;
-  const float2 *Y = X + kx * RF_BATOMS;
-  const float2 *Z = Y + (ky + (kz - 1) / 2) * RF_BATOMS;  // row nz = 0
+  int iq[RF_APT];  // this thread's atoms, clamped for the table reads
+#pragma unroll
+  for (int q = 0; q < RF_APT; ++q) iq[q] = min(i0 + lane + 32 * q, n - 1);
+  const float2 *Z = srf + lane + ((kz - 1) / 2) * RF_BATOMS;  // row nz = 0
   const int gs = parts.g[part], ge = parts.g[part + 1];
   if (gs < ge) {
     const int rs = groups[gs].woff;
@@ -554,8 +558,8 @@ __global__ void __launch_bounds__(32 * RF_PARTS) k_rforce32(
         const float2 rv = colrv[G.col[c]];
 #pragma unroll
         for (int q = 0; q < RF_APT; ++q) {
-          const float2 T = cmulf(X[col.nx * RF_BATOMS + 32 * q],
-                                 conj_if(Y[ny * RF_BATOMS + 32 * q], col.ny < 0));
+          const float2 T = cmulf(__ldg(&tab[(size_t)col.nx * n + iq[q]]),
+                                 conj_if(__ldg(&tab[(size_t)(kx + ny) * n + iq[q]]), col.ny < 0));
           const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
           const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
           // per-column partials go to 64-bit fixed point (order independent)
@@ -839,7 +843,7 @@ int host_inifur(mdx_ctx *ctx) {
   }
   // the dynamic shared memory of the mixed force pass plus its static
   // reduction buffer must also fit
-  const size_t shr = sizeof(float2) * RF_BATOMS * (kx + ky + kz);
+  const size_t shr = sizeof(float2) * RF_BATOMS * kz;
   if (ctx->mixed() && shr + sizeof(long long) * 3 * RF_PARTS * RF_BATOMS +
                              sizeof(float4) * RF_PARTS * 2 * RF_WB * KGRP >
                          SFAC_SMEM_MAX) {
@@ -1002,7 +1006,7 @@ int launch_furir(mdx_ctx *ctx) {
   const int kzo = (d.kz - 1) / 2;
   const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
   if (mx) {
-    const size_t shr = sizeof(float2) * RF_BATOMS * (d.kx + d.ky + d.kz);
+    const size_t shr = sizeof(float2) * RF_BATOMS * d.kz;
     RfParts parts;
     for (int p = 0; p <= RF_PARTS; ++p) parts.g[p] = d.rf_parts[p];
     k_rforce32<<<(d.n + RF_BATOMS - 1) / RF_BATOMS, 32 * RF_PARTS, shr, ctx->stream>>>(
