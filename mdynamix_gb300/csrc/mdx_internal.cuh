@@ -378,34 +378,34 @@ __device__ __forceinline__ void block_add_core(double (&v)[NV], double *const *d
   __syncthreads();
   const unsigned nblk = gridDim.x * gridDim.y;
   const unsigned blin = blockIdx.y * gridDim.x + blockIdx.x;
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double t = lane < nw ? sh[lane][k] : 0.0;
-      t = warp_sum(t);
-      if (lane == 0) {
-        if (part)
-          part[(size_t)blin * NV + k] = t;
-        else if (dst[k])
-          atomicAdd(dst[k], t);
+  // the block's total of value k is formed by warp k % nw (the same sums in
+  // the same order as one warp doing all of them, NV times shorter)
+  for (int k = wid; k < NV; k += nw) {
+    double t = lane < nw ? sh[lane][k] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) {
+      if (part) {
+        part[(size_t)blin * NV + k] = t;
+        __threadfence();
+      } else if (dst[k]) {
+        atomicAdd(dst[k], t);
       }
     }
-    if (part && lane == 0) {
-      __threadfence();
-      last = atomicAdd(ctr, 1u) == nblk - 1;
-    }
   }
-  __syncthreads();
-  if (part && last && wid == 0) {
-    __threadfence();
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double t = 0.0;
-      for (unsigned b = lane; b < nblk; b += 32) t += __ldcg(&part[(size_t)b * NV + k]);
-      t = warp_sum(t);
-      if (lane == 0 && dst[k]) *dst[k] += t;
+  if (part) {
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ctr, 1u) == nblk - 1;
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      for (int k = wid; k < NV; k += nw) {
+        double t = 0.0;
+        for (unsigned b = lane; b < nblk; b += 32) t += __ldcg(&part[(size_t)b * NV + k]);
+        t = warp_sum(t);
+        if (lane == 0 && dst[k]) *dst[k] += t;
+      }
+      if (threadIdx.x == 0) *ctr = 0u;
     }
-    if (lane == 0) *ctr = 0u;
   }
   __syncthreads();
 }

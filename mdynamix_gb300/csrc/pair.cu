@@ -105,8 +105,10 @@ __global__ void __launch_bounds__(256) k_pair64(
       double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
       pbc_rect(DX, DY, DZ, bx, by, bz, hbx, hby, hbzt);
       const double RR = DX * DX + DY * DY + DZ * DZ;
-      const double R1 = sqrt(RR);
-      const double R1I = 1. / R1;
+      // one reciprocal square root instead of a square root and a division
+      // (within an ulp of DSQRT and 1/R1)
+      const double R1I = rsqrt(RR);
+      const double R1 = RR * R1I;
       const double R1E = R1 + RAE;
       const double R1EI = RAE == 0.0 ? R1I : 1. / R1E;
       double EE1, EES, FORCE;
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(256) k_pair32(
       const float RR = DX * DX + DY * DY + DZ * DZ;
       const float R1I = rsqrtf(RR);
       const float R1 = RR * R1I;
-      const float R1EI = RAE == 0.f ? R1I : 1.f / (R1 + RAE);
+      const float R1EI = RAE == 0.f ? R1I : __fdividef(1.f, R1 + RAE);
       const float R1E = R1 + RAE;
       float EE1, EES, FORCE;
       if (is14 || (same && tc.iee[ti] == 0)) {
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(256) k_pair32(
         }
       } else {
         const float ALPHAR = alphad * R1;
-        const float TTT = __frcp_rn(1.f + (float)MDX_B1 * ALPHAR);
+        const float TTT = __fdividef(1.f, 1.f + (float)MDX_B1 * ALPHAR);
         const float EXP2A = __expf(-(ALPHAR * ALPHAR));
         const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
         EE1 = QIJ * R1EI;
