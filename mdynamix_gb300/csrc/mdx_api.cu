@@ -447,7 +447,9 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
   AL(d.ox, 3 * n);
   AL(d.ns_cnt, n);
   AL(d.nl_cnt, n);
-  AL(d.ns_idx, n * d.cap_s);
+  // mixed short rows are tiled by 32 atoms (list_slot): whole tiles stored
+  const size_t nrow = dims->precision == MDX_MIXED ? (n + 31) / 32 * 32 : n;
+  AL(d.ns_idx, nrow * d.cap_s);
   AL(d.nl_idx, n * d.cap_l);
   AL(d.atom_cell, n);
   AL(d.cell_list, n);

@@ -91,7 +91,16 @@ struct MolTpl {
   short am[ML_MAXA];
 };
 
-constexpr int MDX_SITE_BITS = 13;  // sites < 8192, molecules < 2^19 (mixed path)
+constexpr int MDX_SITE_BITS = 13;
+
+// Slot of entry k of atom i's neighbour row.  Rows back to back (a warp walks
+// one row) except the mixed path's short list ("tiled"): 32 atoms' rows
+// interleaved, entry k of the 32 atoms of a tile adjacent, so a thread per
+// atom reads its row with coalesced loads.  Tiled storage holds
+// ceil(n / 32) * 32 rows.
+__host__ __device__ __forceinline__ size_t list_slot(int i, int k, int cap, bool tiled) {
+  return tiled ? ((size_t)(i >> 5) * cap + k) * 32 + (i & 31) : (size_t)i * cap + k;
+}  // sites < 8192, molecules < 2^19 (mixed path)
 
 // Four columns with the same nz range, for the mixed force pass: their W
 // values are interleaved (wg[4 (woff + t) + slot]) so one z-table load feeds

@@ -200,10 +200,10 @@ __global__ void __launch_bounds__(BLK) k_build(
           if (kind == 1 || kind == 3) {
             int k = ns + __popc(ms & lower);
             if (k < cap_s)
-              ns_idx[(size_t)i * cap_s + k] = j | (kind == 3 ? (int)0x80000000 : 0);
+              ns_idx[list_slot(i, k, cap_s, full)] = j | (kind == 3 ? (int)0x80000000 : 0);
           } else if (kind == 2) {
             int k = nl + __popc(ml & lower);
-            if (k < cap_l) nl_idx[(size_t)i * cap_l + k] = j;
+            if (k < cap_l) nl_idx[list_slot(i, k, cap_l, false)] = j;
           }
           ns += __popc(ms);
           nl += __popc(ml);
@@ -357,7 +357,9 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l) {
   DevData &d = ctx->dv;
   const int n = d.n;
-  std::vector<int> cs(n), cl(n), rs((size_t)n * d.cap_s), rl((size_t)n * d.cap_l);
+  const bool tiled = ctx->mixed();
+  const size_t nrow = tiled ? ((size_t)n + 31) / 32 * 32 : (size_t)n;
+  std::vector<int> cs(n), cl(n), rs(nrow * d.cap_s), rl((size_t)n * d.cap_l);
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
   MDX_CUDA(cudaMemcpy(cs.data(), d.ns_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
   MDX_CUDA(cudaMemcpy(cl.data(), d.nl_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
@@ -369,14 +371,15 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
     const int I = i + 1;
     for (int pass = 0; pass < 2; ++pass) {
       const int cnt = pass == 0 ? cs[i] : cl[i];
-      const int *src = pass == 0 ? &rs[(size_t)i * d.cap_s] : &rl[(size_t)i * d.cap_l];
       row.clear();
       for (int k = 0; k < cnt; ++k) {
+        const int src_k = pass == 0 ? rs[list_slot(i, k, d.cap_s, tiled)]
+                                    : rl[list_slot(i, k, d.cap_l, false)];
         // the mixed path keeps full rows (each pair in both atoms' rows);
         // the reference list holds the owner's copy only
-        const int j = src[k] & 0x7fffffff;
+        const int j = src_k & 0x7fffffff;
         const bool own = ((i - j) & 1) == 0 ? (j < i) : (j > i);
-        if (own) row.push_back(src[k]);
+        if (own) row.push_back(src_k);
       }
       std::sort(row.begin(), row.end(), [I](int a, int b) {
         int ja = (a & 0x7fffffff) + 1, jb = (b & 0x7fffffff) + 1;

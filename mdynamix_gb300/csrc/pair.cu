@@ -256,11 +256,19 @@ __global__ void __launch_bounds__(256) k_pair32(
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
     __syncthreads();
   }
+  // short rows (about 50 entries): thread per owner atom over its tiled row
+  // (list_slot), entry k of the warp's 32 atoms in one 128-byte line; long
+  // rows (several hundred entries): warp per owner atom, lanes stride the row
   const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int i = SHORT ? blockIdx.x * blockDim.x + threadIdx.x
+                      : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int k0 = SHORT ? 0 : lane, kstep = SHORT ? 1 : 32;
   long long tot[P_NSLOT];
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
+  float a[P_NSLOT];
+#pragma unroll
+  for (int k = 0; k < P_NSLOT; ++k) a[k] = 0.f;
   if (i < n) {
     // one 16-byte record per atom: fixed-point x, y, z and (molecule, site);
     // charges and types come from the per-site table (L1-resident)
@@ -275,18 +283,16 @@ __global__ void __launch_bounds__(256) k_pair32(
     const float raex = (float)pc.raex;
     const int c = cnt[i];
     float fxa = 0.f, fya = 0.f, fza = 0.f;
-    float a[P_NSLOT];
-#pragma unroll
-    for (int k = 0; k < P_NSLOT; ++k) a[k] = 0.f;
-    const int *row = idx + (size_t)i * cap;
+    const int *row = idx + list_slot(i, 0, cap, SHORT);
+    const int rs = SHORT ? 32 : 1;  // stride of consecutive entries
     // the next entry's index and record are loaded while this one computes
-    int v = lane < c ? row[lane] : 0;
+    int v = k0 < c ? row[(size_t)k0 * rs] : 0;
     int4 pj = posi[v & 0x7fffffff];
-    for (int k = lane; k < c; k += 32) {
+    for (int k = k0; k < c; k += kstep) {
       int vn = 0;
       int4 pjn = pj;
-      if (k + 32 < c) {
-        vn = row[k + 32];
+      if (k + kstep < c) {
+        vn = row[(size_t)(k + kstep) * rs];
         pjn = posi[vn & 0x7fffffff];
       }
       const bool is14 = SHORT && v < 0;
@@ -395,28 +401,30 @@ __global__ void __launch_bounds__(256) k_pair32(
       v = vn;
       pj = pjn;
     }
-    // forces: lane partials -> fixed point -> integer warp sum -> one store
+    // forces: lane partials -> fixed point (-> integer warp sum) -> one store
     // (no 64-bit conversion instruction: those issue on the FP64 pipe)
     long long qx = f2ll_rn(fxa * fsc.scalef);
     long long qy = f2ll_rn(fya * fsc.scalef);
     long long qz = f2ll_rn(fza * fsc.scalef);
+    if (!SHORT) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      qx += __shfl_xor_sync(0xffffffffu, qx, o);
-      qy += __shfl_xor_sync(0xffffffffu, qy, o);
-      qz += __shfl_xor_sync(0xffffffffu, qz, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        qx += __shfl_xor_sync(0xffffffffu, qx, o);
+        qy += __shfl_xor_sync(0xffffffffu, qy, o);
+        qz += __shfl_xor_sync(0xffffffffu, qz, o);
+      }
     }
-    if (lane == 0) {
+    if (SHORT || lane == 0) {
       ffix[i] = (unsigned long long)qx;
       ffix[n + i] = (unsigned long long)qy;
       ffix[2 * n + i] = (unsigned long long)qz;
     }
-    if (ENER) {
+  }
+  if (ENER) {
 #pragma unroll
-      for (int k = 0; k < P_WIR; ++k) {
-        float t = warp_sumf(a[k]);
-        if (lane == 0) tot[k] = f2ll_rn(t * fsc.escalef);
-      }
+    for (int k = 0; k < P_WIR; ++k) {
+      float t = warp_sumf(a[k]);
+      if (lane == 0) tot[k] = f2ll_rn(t * fsc.escalef);
     }
   }
   if (!ENER) return;  // forces only: no energy or virial slots
@@ -537,12 +545,13 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
+    const int grid32 = shrt ? (d.n + T - 1) / T : grid;  // short: thread per atom
 #define LP32(S, P)                                                                \
-  if (ener) k_pair32<S, P, true><<<grid, T, 0, ctx->stream>>>(                    \
+  if (ener) k_pair32<S, P, true><<<grid32, T, 0, ctx->stream>>>(                  \
       d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf);                                        \
-  else k_pair32<S, P, false><<<grid, T, 0, ctx->stream>>>(                        \
+  else k_pair32<S, P, false><<<grid32, T, 0, ctx->stream>>>(                      \
       d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf)
