@@ -42,7 +42,11 @@ WORKLOAD = dict(workload="SPC-FW water 32768 molecules (98304 atoms), DOUBLE 0.2
 # Algorithmic work per unit of each kernel group (frozen constants; an add,
 # sub or mul counts 1, an FMA 2, sqrt / reciprocal / exp / sin / cos 1 each).
 OPS_PAIR = 80            # per listed pair evaluated (forces.f:1071-1198)
-OPS_EW_TERM = 21         # per (k, atom) term, both reciprocal passes (forces.f:1286-1331)
+# Reciprocal Ewald (forces.f:1286-1331) as the GPU passes walk the k-set:
+# columns of fixed (nx, ny), each nz = +p and -p taken together.
+OPS_EW_PAIR = 24         # per (paired record, atom): S(k) 4 FMA + forces 8 FMA
+OPS_EW_COL = 23          # per (column, atom): X Y twice, Im(T U), Im(T V), F
+OPS_EW_ROW = 8           # per (phase-table row, atom): recurrence step + charge
 OPS_EW_K = 20            # per k-vector (energy, virial, W)
 
 # DRAM bytes per long step of the dominant group, from ncu captures of
@@ -118,7 +122,7 @@ def make_system():
     return s, st
 
 
-def roofline_of(timers, mbsh, mbln, nfreq, nkv, n, peak64, peak32, prec, nsteps):
+def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps):
     """Roofline of the dominant kernel group of one long step: reciprocal
     Ewald (phase tables, S(k), per-k terms, forces) or the real-space pair
     loops (NFREQ short-list passes + one long-list pass).  Ops per long step
@@ -126,9 +130,11 @@ def roofline_of(timers, mbsh, mbln, nfreq, nkv, n, peak64, peak32, prec, nsteps)
     events on the launching stream) of the instrumented pass, per long
     step; peak = measured FMA throughput of the pipe the path computes on."""
     ms = {k: v[0] / nsteps for k, v in timers.items()}
+    nkv, ncol, npair, rows = kset
     groups = {
         "ewald": (ms["ew_tables"] + ms["ew_sfac"] + ms["ew_kterms"] + ms["ew_force"],
-                  OPS_EW_TERM * nkv * n + OPS_EW_K * nkv,
+                  (OPS_EW_PAIR * npair + OPS_EW_COL * ncol + OPS_EW_ROW * rows) * n
+                  + OPS_EW_K * nkv,
                   "k_tables + k_sfac + k_sfac_sum + k_kterms + k_rforce"),
         "pair": (ms["pair_short"] + ms["pair_long"], OPS_PAIR * (nfreq * mbsh + mbln),
                  "k_pair (short list x NFREQ, long list x 1)"),
@@ -235,7 +241,7 @@ def run_gpu(args, rank, world, local):
     import ctypes
     return dict(rec_bytes=ctypes.sizeof(MdxStepRecord), out=out, n=n, mbsh=mbsh, mbln=mbln, ferr=ferr, ferr_max=ferr_max,
                 e2e_s=e2e_s, e2e_steps=ke, peak64=peak64, peak32=peak32, dist=dist,
-                nkv=s.kvector_count(), nfreq=s.spec.nfreq)
+                kset=(s.kvector_count(),) + s.kcolumn_counts(), nfreq=s.spec.nfreq)
 
 
 def serving_leg(args):
@@ -442,9 +448,9 @@ def main():
     v64 = world * n * args.steps / (o64["ms"] * 1e-3)
     v32 = world * n * args.steps / (o32["ms"] * 1e-3)
     nfreq = r["nfreq"]
-    roof = roofline_of(o64["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
+    roof = roofline_of(o64["timers"], r["mbsh"], r["mbln"], nfreq, r["kset"], n,
                        r["peak64"], r["peak32"], "fp64", args.steps)
-    roof32 = roofline_of(o32["timers"], r["mbsh"], r["mbln"], nfreq, r["nkv"], n,
+    roof32 = roofline_of(o32["timers"], r["mbsh"], r["mbln"], nfreq, r["kset"], n,
                          r["peak64"], r["peak32"], "mixed", args.steps)
     serving = serving_leg(args) if args.serve_jobs > 0 else None
     pimd = pimd_leg(args) if args.pimd_steps > 0 else None

@@ -12,10 +12,16 @@
 //   F_j    = sum_c [RXV_c, RYV_c] Im(T_j(c) U_j(c)),  Fz = Im(T_j(c) V_j(c))
 //   U_j(c) = sum_{nz} W_k Z_j(nz), V_j(c) = sum_{nz} RZV_k W_k Z_j(nz),
 //   W_k    = 2 AKC_k conj(S_k)
-// so each (k, atom) term costs one complex multiply-add per pass (4 fused
-// multiply-adds) and no transcendental.  Mathematically this is the
-// reference's sum; in FP64 the difference is rounding (the recurrence adds
-// about |n| ulp).
+// with no transcendental per (k, atom) term.  INIFUR's k-set is symmetric
+// in nz within each column (apart from the k = (0, 0, nz > 0) column), and
+// Z_j(-n) = conj(Z_j(n)), so both passes take nz = +p and -p together:
+//   S(c, +p) = (A1 - A2, A3 + A4),  S(c, -p) = (A1 + A2, A4 - A3)
+//   with A1 = sum T.re a, A2 = sum T.im b, A3 = sum T.re b, A4 = sum T.im a,
+//   Z_j(p) = a + i b  (4 fused multiply-adds per atom for two k),
+//   U += P a + i M b,  P = W(+p) + W(-p),  M = W(+p) - W(-p)  (and V with
+//   RZV W), 4 fused multiply-adds per atom for two k.
+// Mathematically this is the reference's sum; in FP64 the difference is
+// rounding (the recurrence adds about |n| ulp).
 //
 // Tables are stored n-major (tab[n * N + atom]) so that a warp of atoms
 // reads one coalesced row per n.
@@ -84,56 +90,71 @@ __global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
   double s, c;
   sincos(2.0 * PI_REF * x, &s, &c);
   const double2 e = make_double2(c, s);
-  // x and y tables hold n = 0..K; the z table holds n = -K..K (conjugates
-  // stored) at index n + K, so the inner loops need no sign test
-  const int kzo = (kz - 1) / 2;
-  const int len = a == 0 ? kx : a == 1 ? ky : kzo + 1;
-  const int off = a == 2 ? kzo : 0;
+  // rows n = 0..K (negative n are the conjugates, never stored)
+  const int len = a == 0 ? kx : a == 1 ? ky : kz;
   const double q = a == 0 ? p.w : 1.0;
   double2 v = make_double2(1.0, 0.0);
   if (txf) {  // mixed path: FP64 recurrence, FP32 table
     float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
     for (int k = 0; k < len; ++k) {
-      dst[(size_t)(off + k) * n] = make_float2((float)(q * v.x), (float)(q * v.y));
-      if (a == 2) dst[(size_t)(off - k) * n] = make_float2((float)v.x, (float)-v.y);
+      dst[(size_t)k * n] = make_float2((float)(q * v.x), (float)(q * v.y));
       v = cmul(v, e);
     }
   } else {
     double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + i;
     for (int k = 0; k < len; ++k) {
-      dst[(size_t)(off + k) * n] = make_double2(q * v.x, q * v.y);
-      if (a == 2) dst[(size_t)(off - k) * n] = make_double2(v.x, -v.y);
+      dst[(size_t)k * n] = make_double2(q * v.x, q * v.y);
       v = cmul(v, e);
     }
   }
 }
 
-// S(k): thread per chunk (column, up to CH consecutive nz), block.y = slice
-// of atoms staged TILE at a time in shared memory.
-template <typename R, typename C2>
+// Write one paired accumulator as S(c, +p) and S(c, -p) (each only if the
+// k-vector exists): slice partial (summed in slice order by k_sfac_sum) or
+// atomic.
+__device__ __forceinline__ void sfac_out(const KCol &col, int p, double A1, double A2,
+                                         double A3, double A4, double2 *part, double2 *sk) {
+  const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
+  const double2 vp = make_double2(A1 - A2, A3 + A4), vm = make_double2(A1 + A2, A4 - A3);
+  if (part) {
+    if (kp >= 0) part[kp] = vp;
+    if (km >= 0) part[km] = vm;
+  } else {
+    if (kp >= 0) {
+      atomicAdd(&sk[kp].x, vp.x);
+      atomicAdd(&sk[kp].y, vp.y);
+    }
+    if (km >= 0) {
+      atomicAdd(&sk[km].x, vm.x);
+      atomicAdd(&sk[km].y, vm.y);
+    }
+  }
+}
+
+// FP64 S(k): thread per chunk (column, CH consecutive p from p0), block.y =
+// slice of SLICE atoms staged TILE at a time in shared memory.
 __global__ void __launch_bounds__(128) k_sfac(
     int n, int nchunk, const Chunk *__restrict__ chunks,
-    const KCol *__restrict__ cols, const C2 *__restrict__ tx,
-    const C2 *__restrict__ ty, const C2 *__restrict__ tz, int kx, int ky, int kz,
-    double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
+    const KCol *__restrict__ cols, const double2 *__restrict__ tx,
+    const double2 *__restrict__ ty, const double2 *__restrict__ tz, int kx, int ky,
+    int kz, double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
   extern __shared__ unsigned char smem_raw[];
-  C2 *sx = reinterpret_cast<C2 *>(smem_raw);  // [atom][n]
-  C2 *sy = sx + TILE * kx;
-  C2 *sz = sy + TILE * ky;
+  double2 *sx = reinterpret_cast<double2 *>(smem_raw);  // [atom][n]
+  double2 *sy = sx + TILE * kx;
+  double2 *sz = sy + TILE * ky;
   const int ch = blockIdx.x * blockDim.x + threadIdx.x;
   const int a0 = blockIdx.y * SLICE, a1 = min(n, a0 + SLICE);
   Chunk cc{0, 0, 0, 0};
-  KCol col{0, 0, 0, 0, 0, 0};
+  KCol col{0, 0, 0, 0, 0, 0, 0, 0};
   if (ch < nchunk) {
     cc = chunks[ch];
     col = cols[cc.col];
   }
   const int ny = col.ny < 0 ? -col.ny : col.ny;
   const bool nyneg = col.ny < 0;
-  const int kzo = (kz - 1) / 2;
-  R sr[CH], si[CH];
+  double A[CH][4];
 #pragma unroll
-  for (int t = 0; t < CH; ++t) sr[t] = si[t] = R(0);
+  for (int t = 0; t < CH; ++t) A[t][0] = A[t][1] = A[t][2] = A[t][3] = 0.0;
   for (int base = a0; base < a1; base += TILE) {
     const int m = min(TILE, a1 - base);
     __syncthreads();
@@ -152,47 +173,41 @@ __global__ void __launch_bounds__(128) k_sfac(
     __syncthreads();
     if (ch < nchunk) {
       for (int j = 0; j < m; ++j) {
-        const C2 X = sx[j * kx + col.nx];
-        const C2 Y = conj_if(sy[j * ky + ny], nyneg);
-        const R tr = fma(X.x, Y.x, -X.y * Y.y), ti = fma(X.x, Y.y, X.y * Y.x);
-        const C2 *zr = sz + j * kz;
+        const double2 X = sx[j * kx + col.nx];
+        const double2 Y = conj_if(sy[j * ky + ny], nyneg);
+        const double tr = fma(X.x, Y.x, -X.y * Y.y), ti = fma(X.x, Y.y, X.y * Y.x);
+        const double2 *zr = sz + j * kz + cc.nz0;
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
           if (t < cc.len) {
-            const C2 Z = zr[cc.nz0 + t + kzo];
-            sr[t] = fma(tr, Z.x, sr[t]);
-            sr[t] = fma(-ti, Z.y, sr[t]);
-            si[t] = fma(tr, Z.y, si[t]);
-            si[t] = fma(ti, Z.x, si[t]);
+            const double2 Z = zr[t];
+            A[t][0] = fma(tr, Z.x, A[t][0]);
+            A[t][1] = fma(ti, Z.y, A[t][1]);
+            A[t][2] = fma(tr, Z.y, A[t][2]);
+            A[t][3] = fma(ti, Z.x, A[t][3]);
           }
         }
       }
     }
   }
   if (ch < nchunk) {
+    double2 *pp = part ? part + (size_t)blockIdx.y * nkv : nullptr;
 #pragma unroll
     for (int t = 0; t < CH; ++t)
-      if (t < cc.len) {
-        if (part) {  // slice partial, summed in slice order by k_sfac_sum
-          part[(size_t)blockIdx.y * nkv + cc.k0 + t] = make_double2((double)sr[t], (double)si[t]);
-        } else {
-          atomicAdd(&sk[cc.k0 + t].x, (double)sr[t]);
-          atomicAdd(&sk[cc.k0 + t].y, (double)si[t]);
-        }
-      }
+      if (t < cc.len) sfac_out(col, cc.nz0 + t, A[t][0], A[t][1], A[t][2], A[t][3], pp, sk);
   }
 }
 
-// Mixed S(k) pass.  A work item is (column group, window of SCH nz starting
-// at t0 within the group's range); a thread accumulates 4 columns x SCH nz in
+// Mixed S(k) pass.  A work item is (column group, window of SCH values of p
+// from p0); a thread accumulates 4 columns x SCH paired sums (A1..A4) in
 // FP32 registers over one slice of atoms, staged TILE at a time in shared
-// memory as one row per atom: X(0..KMAX), Y(0..KMAY), Z(-KMAZ..KMAZ) and SCH
-// zeros (windows past KMAZ and padding columns read zeros).  Tiles are double
-// buffered: the next tile's cp.async copies run under this tile's FMAs.  Items are sorted
-// by absolute nz window so the lanes of a warp mostly read the same z entries
-// (shared-memory broadcast).  The slice length is chosen on the host so the
-// grid is one full wave of resident blocks.
-constexpr int SCH = 8;
+// memory as one row per atom: X(0..KMAX), Y(0..KMAY), Z(0..KMAZ) and SCH
+// zeros (windows past KMAZ and padding columns read zeros).  Tiles are
+// double buffered: the next tile's cp.async copies run under this tile's
+// FMAs.  Items are sorted by p0 so the lanes of a warp mostly read the same
+// z entries (shared-memory broadcast).  The slice length is chosen on the
+// host so the grid is one full wave of resident blocks.
+constexpr int SCH = 4;
 struct SItem {
   int g, t0;
 };
@@ -217,18 +232,18 @@ __global__ void __launch_bounds__(128, 3) k_sfac32(
 #pragma unroll
     for (int c = 0; c < KGRP; ++c) {
       const int ci = active ? G.col[c] : -1;
-      const KCol col = ci >= 0 ? cols[ci] : KCol{0, 0, 0, 0, 0, 0};
+      const KCol col = ci >= 0 ? cols[ci] : KCol{0, 0, 0, 0, 0, 0, 0, 0};
       xo[c] = ci >= 0 ? col.nx : zpad;  // padding column: X = 0
       yo[c] = kx + (col.ny < 0 ? -col.ny : col.ny);
       ysg[c] = col.ny < 0 ? 0x80000000u : 0u;
     }
-    zo = kx + ky + (kz - 1) / 2 + G.nzlo + si.t0;
+    zo = kx + ky + si.t0;
   }
-  float ar[KGRP][SCH], ai[KGRP][SCH];
+  float A[KGRP][SCH][4];
 #pragma unroll
   for (int c = 0; c < KGRP; ++c)
 #pragma unroll
-    for (int s = 0; s < SCH; ++s) ar[c][s] = ai[c][s] = 0.f;
+    for (int s = 0; s < SCH; ++s) A[c][s][0] = A[c][s][1] = A[c][s][2] = A[c][s][3] = 0.f;
   const int bufsz = TILE * rowlen;
   for (int k = threadIdx.x; k < 2 * TILE * SCH; k += blockDim.x)
     srow[(k / SCH) * rowlen + zpad + k % SCH] = make_float2(0.f, 0.f);
@@ -269,10 +284,10 @@ __global__ void __launch_bounds__(128, 3) k_sfac32(
           const float2 Z = zr[s];
 #pragma unroll
           for (int c = 0; c < KGRP; ++c) {
-            ar[c][s] = fmaf(tr[c], Z.x, ar[c][s]);
-            ar[c][s] = fmaf(-ti[c], Z.y, ar[c][s]);
-            ai[c][s] = fmaf(tr[c], Z.y, ai[c][s]);
-            ai[c][s] = fmaf(ti[c], Z.x, ai[c][s]);
+            A[c][s][0] = fmaf(tr[c], Z.x, A[c][s][0]);
+            A[c][s][1] = fmaf(ti[c], Z.y, A[c][s][1]);
+            A[c][s][2] = fmaf(tr[c], Z.y, A[c][s][2]);
+            A[c][s][3] = fmaf(ti[c], Z.x, A[c][s][3]);
           }
         }
       }
@@ -283,23 +298,17 @@ __global__ void __launch_bounds__(128, 3) k_sfac32(
   if (!active) return;
   const SItem si = items[it];
   const KGroup &G = groups[si.g];
-  const int len = min(SCH, G.len - si.t0);
+  double2 *pp = part ? part + (size_t)blockIdx.y * nkv : nullptr;
 #pragma unroll
   for (int c = 0; c < KGRP; ++c) {
     const int ci = G.col[c];
     if (ci < 0) continue;
-    const int k0 = cols[ci].koff + si.t0;
+    const KCol col = cols[ci];
 #pragma unroll
     for (int s = 0; s < SCH; ++s)
-      if (s < len) {
-        const double2 v = make_double2((double)ar[c][s], (double)ai[c][s]);
-        if (part) {  // slice partial, summed in slice order by k_sfac_sum
-          part[(size_t)blockIdx.y * nkv + k0 + s] = v;
-        } else {
-          atomicAdd(&sk[k0 + s].x, v.x);
-          atomicAdd(&sk[k0 + s].y, v.y);
-        }
-      }
+      if (si.t0 + s <= G.m)
+        sfac_out(col, si.t0 + s, (double)A[c][s][0], (double)A[c][s][1], (double)A[c][s][2],
+                 (double)A[c][s][3], pp, sk);
   }
 }
 
@@ -321,7 +330,7 @@ __global__ void k_sfac_sum(int nkv, int nslice, const double2 *__restrict__ part
 __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
                          const double2 *__restrict__ sk, double bx, double by,
                          double bz, double alp2, double cfur,
-                         dbl4 *__restrict__ wk, float4 *__restrict__ wkf,
+                         dbl4 *__restrict__ wk,
                          double2 *__restrict__ colrv, float2 *__restrict__ colrvf,
                          Dst6 dst) {
   double acc[4] = {0, 0, 0, 0};
@@ -356,13 +365,46 @@ __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
       W.y = -AK2 * SSN;
       W.z = RZV * W.x;
       W.w = RZV * W.y;
-      if (wkf)
-        wkf[col.wpos + KGRP * t] = make_float4((float)W.x, (float)W.y, (float)W.z, (float)W.w);
-      else
-        wk[k] = W;
+      wk[k] = W;
     }
   }
   block_add<4>(acc, dst);
+}
+
+// Paired W per (column, p): P = W(+p) + W(-p), M = W(+p) - W(-p) for U, the
+// same of RZV W for V (a missing k counts as W = 0; p = 0 gives P = W(0),
+// M = 0).  FP64: wp64[2 (poff + p) + {0, 1}] = {P_U, M_U}, {P_V, M_V};
+// mixed: the group-interleaved FP32 records of KGroup.
+__global__ void k_wpairs(int ncol, const KCol *__restrict__ cols, const dbl4 *__restrict__ wk,
+                         dbl4 *__restrict__ wp64, float4 *__restrict__ wp32) {
+  for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
+    const KCol col = cols[c];
+    for (int p = threadIdx.x; p <= col.m; p += blockDim.x) {
+      const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
+      dbl4 a, b;
+      a.x = a.y = a.z = a.w = 0.0;
+      b = a;
+      if (kp >= 0) a = wk[kp];
+      if (km >= 0) b = wk[km];
+      dbl4 u, v;  // {P, M} of W, of RZV W
+      u.x = a.x + b.x;
+      u.y = a.y + b.y;
+      u.z = a.x - b.x;
+      u.w = a.y - b.y;
+      v.x = a.z + b.z;
+      v.y = a.w + b.w;
+      v.z = a.z - b.z;
+      v.w = a.w - b.w;
+      if (wp32) {
+        float4 *r = wp32 + col.wpos + 8 * (size_t)p;  // wpos = 8 woff + 2 slot
+        r[0] = make_float4((float)u.x, (float)u.y, (float)u.z, (float)u.w);
+        r[1] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+      } else {
+        wp64[2 * (size_t)(col.poff + p)] = u;
+        wp64[2 * (size_t)(col.poff + p) + 1] = v;
+      }
+    }
+  }
 }
 
 // QPE into PELS1 and the three virial projections (forces.f:1333-1336).
@@ -376,53 +418,42 @@ __global__ void k_qpe_fold(mdx_scalars *sc, double *qpe) {
   *qpe = 0.0;
 }
 
-// Column sums U = sum_nz W_k Z(nz), V = sum_nz RZV_k W_k Z(nz) over the
-// signed z table (Z points at row nz = 0 of this atom).  wk holds
-// (Re W, Im W, Re RZV W, Im RZV W) per k.
-template <typename R, typename W4, typename C2>
-__device__ __forceinline__ void column_sums(const C2 *__restrict__ Z, int n,
-                                            const W4 *__restrict__ wk,
-                                            const KCol &col, R &ux, R &uy,
-                                            R &vx, R &vy) {
-  const C2 *z = Z + (long long)col.nzlo * n;
-  const W4 *w = wk + col.koff;
-  const int len = col.nzhi - col.nzlo + 1;
-#pragma unroll 4
-  for (int t = 0; t < len; ++t) {
-    const C2 zz = z[(long long)t * n];
-    const W4 a = w[t];
-    ux = fma(a.x, zz.x, ux);
-    ux = fma(-a.y, zz.y, ux);
-    uy = fma(a.x, zz.y, uy);
-    uy = fma(a.y, zz.x, uy);
-    vx = fma(a.z, zz.x, vx);
-    vx = fma(-a.w, zz.y, vx);
-    vy = fma(a.z, zz.y, vy);
-    vy = fma(a.w, zz.x, vy);
-  }
-}
-
 // Force passes: a block is RF_ATOMS atoms x RF_PARTS column parts (one warp
 // per part); part p takes columns p, p + RF_PARTS, ... and the parts are
 // added in part order through shared memory, so the sum is deterministic.
 constexpr int RF_ATOMS = 32;
 constexpr int RF_PARTS = 4;
 
+// FP64 force pass: U = sum_p P_U a + i M_U b over p = 0..m of each column
+// (Z(p) = a + i b), V the same with P_V, M_V; then F += rv Im(T U), Im(T V).
 __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
-    int n, int ncol, const KCol *__restrict__ cols, const dbl4 *__restrict__ wk,
+    int n, int ncol, const KCol *__restrict__ cols, const dbl4 *__restrict__ wp,
     const double2 *__restrict__ tx, const double2 *__restrict__ ty,
-    const double2 *__restrict__ tz, int kzo, const double2 *__restrict__ colrv,
+    const double2 *__restrict__ tz, const double2 *__restrict__ colrv,
     double *__restrict__ gx, double *__restrict__ gy, double *__restrict__ gz) {
   __shared__ double red[3][RF_PARTS][RF_ATOMS];
   const int lane = threadIdx.x % RF_ATOMS, part = threadIdx.x / RF_ATOMS;
   const int i = blockIdx.x * RF_ATOMS + lane;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (i < n) {
-    const double2 *Z = tz + (size_t)kzo * n + i;
+    const double2 *Z = tz + i;
     for (int c = part; c < ncol; c += RF_PARTS) {
       const KCol col = cols[c];
       double ux = 0., uy = 0., vx = 0., vy = 0.;
-      column_sums<double, dbl4, double2>(Z, n, wk, col, ux, uy, vx, vy);
+      const dbl4 *w = wp + 2 * (size_t)col.poff;
+#pragma unroll 4
+      for (int p = 0; p <= col.m; ++p) {
+        const double2 z = Z[(size_t)p * n];
+        const dbl4 u = w[2 * p], v = w[2 * p + 1];
+        ux = fma(u.x, z.x, ux);
+        ux = fma(-u.w, z.y, ux);
+        uy = fma(u.y, z.x, uy);
+        uy = fma(u.z, z.y, uy);
+        vx = fma(v.x, z.x, vx);
+        vx = fma(-v.w, z.y, vx);
+        vy = fma(v.y, z.x, vy);
+        vy = fma(v.z, z.y, vy);
+      }
       const int ny = col.ny < 0 ? -col.ny : col.ny;
       const double2 T = cmul(tx[(size_t)col.nx * n + i],
                              conj_if(ty[(size_t)ny * n + i], col.ny < 0));
@@ -453,16 +484,18 @@ __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
 
 // Mixed force pass over column groups.  A block holds RF_APT x 32 atoms (a
 // thread takes atoms lane and lane + 32) and RF_PARTS warps; warp p takes the
-// contiguous group range [parts.g[p], parts.g[p+1]) whose W records are
-// contiguous too.  The block's X, Y and Z table rows are staged in shared
-// memory ([row][atom], conflict-free).  Each warp streams its W records
-// through a two-batch shared-memory ring with cp.async (RF_WB records a
-// batch, one 16-byte copy per lane), so W latency hides under the FMAs of
-// the previous batch.  Per nz and atom one z load; per nz four broadcast W
-// loads feed 32 FMAs per atom.
+// contiguous group range [parts.g[p], parts.g[p+1]) whose paired-W records
+// are contiguous too.  The block's Z rows (p = 0..KMAZ) are staged in shared
+// memory ([row][atom], conflict-free); X and Y (read once per column) come
+// through L1/L2.  Each warp streams its records through a two-batch
+// shared-memory ring with cp.async (RF_WB records of 8 float4 a batch, one
+// 16-byte copy per lane), so W latency hides under the FMAs of the previous
+// batch.  Per p and atom one z load; per p eight broadcast loads feed 32 FMAs
+// per atom covering 8 k-vectors.
 constexpr int RF_APT = 2;
 constexpr int RF_BATOMS = 32 * RF_APT;
-constexpr int RF_WB = 32 / KGRP;  // W records per batch (one float4 per lane)
+constexpr int RF_REC = 2 * KGRP;  // float4 per record (4 columns x {U, V})
+constexpr int RF_WB = 32 / RF_REC;  // records per batch (one float4 per lane)
 struct RfParts {
   int g[RF_PARTS + 1];
 };
@@ -477,13 +510,10 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
     int n, RfParts parts, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
     const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
     const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * n.  The Z
-  // rows (read every nz) are staged in shared memory; X and Y (read once per
-  // column) come through L1/L2, which keeps the block's shared memory small
-  // enough for more resident warps.
+  // tab: the X, Y and Z tables back to back, row r at tab + r * n
   extern __shared__ float2 srf[];  // [kz][RF_BATOMS]
   __shared__ long long red[3][RF_PARTS][RF_BATOMS];
-  __shared__ float4 ring[RF_PARTS][2][RF_WB * KGRP];
+  __shared__ float4 ring[RF_PARTS][2][RF_WB * RF_REC];
   const int lane = threadIdx.x % 32, part = threadIdx.x / 32;
   const int i0 = blockIdx.x * RF_BATOMS;
   const float2 *tz = tab + (size_t)(kx + ky) * n;
@@ -499,16 +529,17 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
   int iq[RF_APT];  // this thread's atoms, clamped for the table reads
 #pragma unroll
   for (int q = 0; q < RF_APT; ++q) iq[q] = min(i0 + lane + 32 * q, n - 1);
-  const float2 *Z = srf + lane + ((kz - 1) / 2) * RF_BATOMS;  // row nz = 0
+  const float2 *Z = srf + lane;  // row p = 0
   const int gs = parts.g[part], ge = parts.g[part + 1];
   if (gs < ge) {
     const int rs = groups[gs].woff;
     const int re = groups[ge - 1].woff + groups[ge - 1].len;
     float4 *wr = &ring[part][0][0];
-    // lane copies component lane % KGRP of record (batch start + lane / KGRP)
+    // lane copies float4 lane % RF_REC of record (batch start + lane / RF_REC)
     auto issue = [&](int buf, int rec0) {
-      const int rec = rec0 + lane / KGRP;
-      if (rec < re) cp_async16(wr + buf * RF_WB * KGRP + lane, wg + (size_t)KGRP * rec + lane % KGRP);
+      const int rec = rec0 + lane / RF_REC;
+      if (rec < re)
+        cp_async16(wr + buf * RF_WB * RF_REC + lane, wg + (size_t)RF_REC * rec + lane % RF_REC);
     };
     issue(0, rs);
     cp_async_commit();
@@ -520,33 +551,32 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
       for (int q = 0; q < RF_APT; ++q)
 #pragma unroll
         for (int c = 0; c < KGRP; ++c) u[q][c][0] = u[q][c][1] = v[q][c][0] = v[q][c][1] = 0.f;
-      const float2 *z = Z + G.nzlo * RF_BATOMS;
-      for (int t = 0; t < G.len; ++t, ++r) {
-        const int q8 = r - rs;
-        if (q8 % RF_WB == 0) {  // batch boundary: this batch landed, prefetch the next
+      for (int p = 0; p < G.len; ++p, ++r) {
+        const int qb = r - rs;
+        if (qb % RF_WB == 0) {  // batch boundary: this batch landed, prefetch the next
           cp_async_wait0();
           __syncwarp();
-          if (next < re) issue((q8 / RF_WB + 1) & 1, next);
+          if (next < re) issue((qb / RF_WB + 1) & 1, next);
           cp_async_commit();
           next += RF_WB;
         }
-        const float4 *w = wr + (((q8 / RF_WB) & 1) * RF_WB + q8 % RF_WB) * KGRP;
+        const float4 *w = wr + (((qb / RF_WB) & 1) * RF_WB + qb % RF_WB) * RF_REC;
         float2 zz[RF_APT];
 #pragma unroll
-        for (int q = 0; q < RF_APT; ++q) zz[q] = z[t * RF_BATOMS + 32 * q];
+        for (int q = 0; q < RF_APT; ++q) zz[q] = Z[p * RF_BATOMS + 32 * q];
 #pragma unroll
         for (int c = 0; c < KGRP; ++c) {
-          const float4 a = w[c];
+          const float4 pu = w[2 * c], pv = w[2 * c + 1];  // {P.re, P.im, M.re, M.im}
 #pragma unroll
           for (int q = 0; q < RF_APT; ++q) {
-            u[q][c][0] = fmaf(a.x, zz[q].x, u[q][c][0]);
-            u[q][c][0] = fmaf(-a.y, zz[q].y, u[q][c][0]);
-            u[q][c][1] = fmaf(a.x, zz[q].y, u[q][c][1]);
-            u[q][c][1] = fmaf(a.y, zz[q].x, u[q][c][1]);
-            v[q][c][0] = fmaf(a.z, zz[q].x, v[q][c][0]);
-            v[q][c][0] = fmaf(-a.w, zz[q].y, v[q][c][0]);
-            v[q][c][1] = fmaf(a.z, zz[q].y, v[q][c][1]);
-            v[q][c][1] = fmaf(a.w, zz[q].x, v[q][c][1]);
+            u[q][c][0] = fmaf(pu.x, zz[q].x, u[q][c][0]);
+            u[q][c][0] = fmaf(-pu.w, zz[q].y, u[q][c][0]);
+            u[q][c][1] = fmaf(pu.y, zz[q].x, u[q][c][1]);
+            u[q][c][1] = fmaf(pu.z, zz[q].y, u[q][c][1]);
+            v[q][c][0] = fmaf(pv.x, zz[q].x, v[q][c][0]);
+            v[q][c][0] = fmaf(-pv.w, zz[q].y, v[q][c][0]);
+            v[q][c][1] = fmaf(pv.y, zz[q].x, v[q][c][1]);
+            v[q][c][1] = fmaf(pv.z, zz[q].y, v[q][c][1]);
           }
         }
       }
@@ -741,7 +771,7 @@ int host_inifur(mdx_ctx *ctx) {
   }
   std::vector<KCol> cols;
   std::vector<Chunk> chunks;
-  int koff = 0;
+  int koff = 0, poff = 0;
   for (int ix = 0; ix <= KMAX; ++ix)
     for (int iy = -KMAY; iy <= KMAY; ++iy) {
       int lo = 1 << 30, hi = -(1 << 30), cnt = 0;
@@ -757,35 +787,32 @@ int host_inifur(mdx_ctx *ctx) {
         return MDX_ERR_UNSUPPORTED;
       }
       const int c = (int)cols.size();
-      cols.push_back(KCol{ix, iy, lo, hi, koff, 0});
-      for (int z0 = lo; z0 <= hi; z0 += CH)
-        chunks.push_back(Chunk{c, z0, std::min(CH, hi - z0 + 1), koff + (z0 - lo)});
+      const int m = std::max(std::abs(lo), std::abs(hi));
+      cols.push_back(KCol{ix, iy, lo, hi, koff, 0, m, poff});
+      for (int p0 = 0; p0 <= m; p0 += CH)
+        chunks.push_back(Chunk{c, p0, std::min(CH, m - p0 + 1), 0});
       koff += cnt;
+      poff += m + 1;
     }
-  // column groups of the mixed force pass: columns sorted by nz range (then
-  // by column index), four at a time, the last group of a range padded
+  // column groups of the mixed passes: columns sorted by m (then by column
+  // index), four at a time, the last group of an m padded
   std::vector<int> order(cols.size());
   for (size_t c = 0; c < cols.size(); ++c) order[c] = (int)c;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return cols[a].nzlo != cols[b].nzlo ? cols[a].nzlo < cols[b].nzlo
-                                        : cols[a].nzhi < cols[b].nzhi;
-  });
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return cols[a].m < cols[b].m; });
   std::vector<KGroup> groups;
   int woff = 0;
   for (size_t p = 0; p < order.size();) {
-    const KCol &c0 = cols[order[p]];
-    KGroup g{c0.nzlo, c0.nzhi - c0.nzlo + 1, woff, 0, {-1, -1, -1, -1}};
-    for (int s = 0; s < KGRP && p < order.size(); ++s) {
-      const KCol &cs = cols[order[p]];
-      if (cs.nzlo != c0.nzlo || cs.nzhi != c0.nzhi) break;
+    const int m = cols[order[p]].m;
+    KGroup g{m, m + 1, woff, 0, {-1, -1, -1, -1}};
+    for (int s = 0; s < KGRP && p < order.size() && cols[order[p]].m == m; ++s, ++p) {
       g.col[s] = order[p];
-      cols[order[p]].wpos = KGRP * woff + s;
-      ++p;
+      cols[order[p]].wpos = RF_REC * woff + 2 * s;
     }
     woff += g.len;
     groups.push_back(g);
   }
-  const size_t nwg = (size_t)KGRP * std::max(1, woff);
+  const size_t nwg = (size_t)RF_REC * std::max(1, woff);
   // contiguous group ranges of the mixed force pass's warps, balanced by
   // W records (woff is cumulative in group order)
   {
@@ -801,10 +828,9 @@ int host_inifur(mdx_ctx *ctx) {
   std::vector<SItem> items;
   for (size_t g = 0; g < groups.size(); ++g)
     for (int t0 = 0; t0 < groups[g].len; t0 += SCH) items.push_back(SItem{(int)g, t0});
-  std::stable_sort(items.begin(), items.end(), [&](const SItem &a, const SItem &b) {
-    return groups[a.g].nzlo + a.t0 < groups[b.g].nzlo + b.t0;
-  });
-  const int kx = KMAX + 1, ky = KMAY + 1, kz = 2 * KMAZ + 1;
+  std::stable_sort(items.begin(), items.end(),
+                   [](const SItem &a, const SItem &b) { return a.t0 < b.t0; });
+  const int kx = KMAX + 1, ky = KMAY + 1, kz = KMAZ + 1;
   const bool realloc_tables = kx != d.kx || ky != d.ky || kz != d.kz;
   d.kx = kx;
   d.ky = ky;
@@ -845,7 +871,7 @@ int host_inifur(mdx_ctx *ctx) {
   // reduction buffer must also fit
   const size_t shr = sizeof(float2) * RF_BATOMS * kz;
   if (ctx->mixed() && shr + sizeof(long long) * 3 * RF_PARTS * RF_BATOMS +
-                             sizeof(float4) * RF_PARTS * 2 * RF_WB * KGRP >
+                             sizeof(float4) * RF_PARTS * 2 * RF_WB * RF_REC >
                          SFAC_SMEM_MAX) {
     ctx->err = "reciprocal k-set too large for the force-pass tile";
     return MDX_ERR_UNSUPPORTED;
@@ -856,7 +882,7 @@ int host_inifur(mdx_ctx *ctx) {
     MDX_CUDA(raise_smem_limit(k_rforce32, shr));
     MDX_CUDA(raise_smem_limit(k_sfac32, sh));
   } else {
-    MDX_CUDA(raise_smem_limit(k_sfac<double, double2>, sh));
+    MDX_CUDA(raise_smem_limit(k_sfac, sh));
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
@@ -892,12 +918,16 @@ int host_inifur(mdx_ctx *ctx) {
   const size_t nk = (size_t)std::max(1, nkv);
   const size_t nkp = (nk + 1) & ~(size_t)1;  // keeps wk 32-byte aligned
   const size_t nc = std::max<size_t>(1, cols.size());
-  MDX_CUDA(ctx_alloc(ctx, &d.sk, sizeof(double2) * (nkp + 2 * nk + nwg + 2 * nc)));
+  const size_t np64 = ctx->mixed() ? 0 : 2 * (size_t)poff;  // dbl4 records
+  const size_t np32 = ctx->mixed() ? nwg : 0;                // float4 records
+  MDX_CUDA(ctx_alloc(ctx, &d.sk,
+                     sizeof(double2) * (nkp + 2 * nk + 2 * np64 + np32 + 2 * nc)));
   d.wk = reinterpret_cast<dbl4 *>(d.sk + nkp);
-  d.wkf = reinterpret_cast<float4 *>(d.wk + nk);
-  // padding slots of the grouped W stay zero; k_kterms writes the others
-  MDX_CUDA(cudaMemset(d.wkf, 0, sizeof(float4) * nwg));
-  d.colrv = reinterpret_cast<double2 *>(d.wkf + nwg);
+  d.wp64 = d.wk + nk;
+  d.wkf = reinterpret_cast<float4 *>(d.wp64 + np64);
+  // padding slots of the grouped W stay zero; k_wpairs writes the others
+  if (np32) MDX_CUDA(cudaMemset(d.wkf, 0, sizeof(float4) * np32));
+  d.colrv = reinterpret_cast<double2 *>(d.wkf + np32);
   d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
   // per-slice partials of S(k), summed in slice order
   ctx_free(ctx, d.sk_part);
@@ -979,7 +1009,7 @@ int launch_furir(mdx_ctx *ctx) {
           d.tabxf, d.kx, d.ky, d.kz, d.sfac_slice, d.sk, d.sk_part, d.nkv);
     } else {
       grid = dim3((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
-      k_sfac<double, double2><<<grid, 128, sh, ctx->stream>>>(
+      k_sfac<<<grid, 128, sh, ctx->stream>>>(
           d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk,
           d.sk_part, d.nkv);
     }
@@ -996,14 +1026,16 @@ int launch_furir(mdx_ctx *ctx) {
     MDX_TIMER(ctx, MDX_T_EW_KTERMS);
     Dst6 dst = dst6(ctx, std::min(d.ncol, 1024), 4, qpe, &sc->virx, &sc->viry, &sc->virz);
     k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk,
-        mx ? d.wkf : nullptr, d.colrv, d.colrvf, dst);
+        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk, d.colrv,
+        d.colrvf, dst);
+    MDX_LAUNCHED(ctx);
+    k_wpairs<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
+        d.ncol, d.cols, d.wk, mx ? nullptr : d.wp64, mx ? d.wkf : nullptr);
     MDX_LAUNCHED(ctx);
     k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
     MDX_LAUNCHED(ctx);
   }
   MDX_TIMER(ctx, MDX_T_EW_FORCE);
-  const int kzo = (d.kz - 1) / 2;
   const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
   if (mx) {
     const size_t shr = sizeof(float2) * RF_BATOMS * d.kz;
@@ -1014,7 +1046,7 @@ int launch_furir(mdx_ctx *ctx) {
         d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
-        d.n, d.ncol, d.cols, d.wk, d.tabx, d.taby, d.tabz, kzo, d.colrv, d.gx, d.gy, d.gz);
+        d.n, d.ncol, d.cols, d.wp64, d.tabx, d.taby, d.tabz, d.colrv, d.gx, d.gy, d.gz);
   }
   MDX_LAUNCHED(ctx);
   return MDX_OK;

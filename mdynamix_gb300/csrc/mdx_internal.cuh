@@ -77,8 +77,15 @@ struct CellGrid {
 struct KCol {
   int nx, ny, nzlo, nzhi;  // integer k components (rectangular cell)
   int koff;                // first k of the column in the column-ordered list
-  int wpos;                // slot of (nz = nzlo) in the grouped W array
+  int wpos;                // mixed: slot of (group, p = 0) in the paired W array
+  int m;                   // max |nz|: the column pairs nz = +p and -p, p = 0..m
+  int poff;                // FP64: first paired-W record of the column
 };
+
+// k index of (column, nz), -1 outside the column's range.
+__host__ __device__ __forceinline__ int kcol_k(const KCol &c, int nz) {
+  return nz < c.nzlo || nz > c.nzhi ? -1 : c.koff + (nz - c.nzlo);
+}
 
 // Bonds and angles of one small molecule type, atoms as offsets within the
 // molecule, for the molecule-local bonded kernel.
@@ -102,12 +109,14 @@ __host__ __device__ __forceinline__ size_t list_slot(int i, int k, int cap, bool
   return tiled ? ((size_t)(i >> 5) * cap + k) * 32 + (i & 31) : (size_t)i * cap + k;
 }  // sites < 8192, molecules < 2^19 (mixed path)
 
-// Four columns with the same nz range, for the mixed force pass: their W
-// values are interleaved (wg[4 (woff + t) + slot]) so one z-table load feeds
-// four columns.  col[s] < 0 marks a padding slot (W = 0).
+// Four columns with the same m = max |nz|, for the mixed Ewald passes.  The
+// force pass reads, per p = 0..m, one record of 8 float4: for each column
+// slot s, {P_U, M_U} then {P_V, M_V} (paired W, see k_wpairs) at
+// wg[8 (woff + p) + 2 s + half]; one z-table load feeds four columns and
+// both signs of nz.  col[s] < 0 marks a padding slot (W = 0).
 constexpr int KGRP = 4;
 struct KGroup {
-  int nzlo, len, woff, pad;
+  int m, len, woff, pad;  // len = m + 1 records
   int col[KGRP];
 };
 
@@ -164,15 +173,16 @@ struct DevData {
   double *br, *be, *ar, *ae, *tr, *te;
   // SHAKE (per type: first bond record, bond count)
   // Ewald
-  int nkv, ncol, kx, ky, kz;  // table rows: kx = KMAX+1, ky = KMAY+1, kz = 2 KMAZ+1
+  int nkv, ncol, kx, ky, kz;  // table rows: n = 0..KMAX, 0..KMAY, 0..KMAZ
   KCol *cols;
   void *kchunks;                // column chunks of the S(k) kernel
   int nchunk;
-  double2 *tabx, *taby, *tabz;  // [n][atom]; z rows are n = -KMAZ..KMAZ
+  double2 *tabx, *taby, *tabz;  // [n][atom], n >= 0 (negative n: conjugates)
   float2 *tabxf, *tabyf, *tabzf;
   double2 *sk;                  // structure factors, column order
   dbl4 *wk;                     // (W, RZV W) per k, W = AK2*conj(S)
-  float4 *wkf;                  // FP32 copy for the mixed force pass, grouped
+  dbl4 *wp64;                   // FP64 paired W: 2 per (column, p), at poff + p
+  float4 *wkf;                  // mixed paired W, grouped (KGroup)
   // mixed pair path: posi.w = (molecule << MDX_SITE_BITS) | site, and per
   // site {Q (EE-scaled), CHARGE, LJ type, molecule type} as float4 bits
   float4 *stab;

@@ -277,6 +277,33 @@ def kvector_count(alphad: float, fexp: float, boxl: float, boyl: float,
     return n
 
 
+def kcolumn_counts(alphad: float, fexp: float, boxl: float, boyl: float,
+                   bozl: float) -> Tuple[int, int, int]:
+    """(columns, paired records, table rows) of the rectangular-cell k-set
+    INIFUR keeps (forces.f:1356-1412) as the GPU passes walk it: a column is
+    one (nx, ny) with its contiguous nz range, a paired record one p = 0..m,
+    m = max |nz|, covering nz = +p and -p; rows = (KMAX+1) + (KMAY+1) +
+    (KMAZ+1) phase-table rows per atom."""
+    twopi = 2.0 * PI
+    cutk2 = 4.0 * alphad ** 2 * fexp
+    cutk = math.sqrt(cutk2)
+    kmax = int(cutk * boxl / twopi + 1)
+    kmay = int(cutk * boyl / twopi + 1)
+    kmaz = int(cutk * bozl / twopi + 1)
+    cols = {}
+    for ikz in range(-kmaz, kmaz + 1):
+        for ikx in range(0, kmax + 1):
+            ky1 = (0 if ikz > 0 else 1) if ikx == 0 else -kmay
+            for iky in range(ky1, kmay + 1):
+                rk2 = ((twopi * ikx / boxl) ** 2 + (twopi * iky / boyl) ** 2
+                       + (twopi * ikz / bozl) ** 2)
+                if rk2 <= cutk2:
+                    m = cols.get((ikx, iky), 0)
+                    cols[(ikx, iky)] = max(m, abs(ikz))
+    npair = sum(m + 1 for m in cols.values())
+    return len(cols), npair, kmax + kmay + kmaz + 3
+
+
 # ---------------------------------------------------------------- spec ----
 @dataclass
 class RunSpec:
@@ -747,6 +774,9 @@ class System:
     # --------------------------------------------------------- helpers ---
     def kvector_count(self) -> int:
         return kvector_count(self.alphad, self.fexp, self.boxl, self.boyl, self.bozl)
+
+    def kcolumn_counts(self) -> Tuple[int, int, int]:
+        return kcolumn_counts(self.alphad, self.fexp, self.boxl, self.boyl, self.bozl)
 
     def summary(self) -> dict:
         return dict(nstot=self.nstot, nop=self.nop, ntypes=self.ntypes, nnbt=self.nnbt,
