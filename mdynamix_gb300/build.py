@@ -20,7 +20,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libmdxgpu.so")
 BUILD = os.path.join(ROOT, "_build")
 SOURCES = ["mdx_api.cu", "integrate.cu", "bonded.cu", "ewald.cu", "pair.cu", "nblist.cu",
-           "probe.cu", "noalloc.cu", "pimd.cu"]
+           "probe.cu", "noalloc.cu", "pimd.cu", "ewald_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
@@ -37,7 +37,7 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    deps = [src, os.path.join(CSRC, "mdx_internal.cuh"),
+    deps = [src, os.path.join(CSRC, "mdx_internal.cuh"), os.path.join(CSRC, "tc_ptx.cuh"),
             os.path.join(ROOT, "include", "mdx_gpu.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 

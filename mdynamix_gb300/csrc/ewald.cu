@@ -32,6 +32,7 @@
 // point.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -483,9 +484,12 @@ __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
 }
 
 // Mixed force pass over column groups.  A block holds RF_APT x 32 atoms (a
-// thread takes atoms lane and lane + 32) and RF_PARTS warps; warp p takes the
-// contiguous group range [parts.g[p], parts.g[p+1]) whose paired-W records
-// are contiguous too.  The block's Z rows (p = 0..KMAZ) are staged in shared
+// thread takes atoms lane and lane + 32) and RF_PARTS warps; the groups are
+// cut into nsplit x RF_PARTS contiguous ranges (parts[], balanced by W
+// records) and warp w of block (tile, s) takes range s RF_PARTS + w, whose
+// paired-W records are contiguous too.  nsplit > 1 spreads one atom tile
+// over several blocks so the grid fills the last wave of resident blocks;
+// their fixed-point partials meet in integer atomics (order independent).  The block's Z rows (p = 0..KMAZ) are staged in shared
 // memory ([row][atom], conflict-free); X and Y (read once per column) come
 // through L1/L2.  Each warp streams its records through a two-batch
 // shared-memory ring with cp.async (RF_WB records of 8 float4 a batch, one
@@ -496,10 +500,6 @@ constexpr int RF_APT = 2;
 constexpr int RF_BATOMS = 32 * RF_APT;
 constexpr int RF_REC = 2 * KGRP;  // float4 per record (4 columns x {U, V})
 constexpr int RF_WB = 32 / RF_REC;  // records per batch (one float4 per lane)
-struct RfParts {
-  int g[RF_PARTS + 1];
-};
-static_assert(RF_PARTS + 1 <= 8, "DevData::rf_parts holds 8 entries");
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -507,7 +507,8 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 }
 
 __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
-    int n, RfParts parts, const KGroup *__restrict__ groups, const KCol *__restrict__ cols,
+    int n, const int *__restrict__ parts, const KGroup *__restrict__ groups,
+    const KCol *__restrict__ cols,
     const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
     const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
   // tab: the X, Y and Z tables back to back, row r at tab + r * n
@@ -522,15 +523,19 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
     srf[k] = i0 + j < n ? tz[(size_t)r * n + i0 + j] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const float sc = fsc.scalef;
-  long long ax[RF_APT], ay[RF_APT], az[RF_APT];
+  // per atom and axis: the group sums (4 columns, FP32) accumulated with
+  // Kahan compensation (fs, fc), fixed order -> deterministic
+  float fs[RF_APT][3], fc[RF_APT][3];
 #pragma unroll
-  for (int q = 0; q < RF_APT; ++q) ax[q] = ay[q] = az[q] = 0;
+  for (int q = 0; q < RF_APT; ++q)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) fs[q][a] = fc[q][a] = 0.f;
   int iq[RF_APT];  // this thread's atoms, clamped for the table reads
 #pragma unroll
   for (int q = 0; q < RF_APT; ++q) iq[q] = min(i0 + lane + 32 * q, n - 1);
   const float2 *Z = srf + lane;  // row p = 0
-  const int gs = parts.g[part], ge = parts.g[part + 1];
+  const int gs = parts[blockIdx.y * RF_PARTS + part];
+  const int ge = parts[blockIdx.y * RF_PARTS + part + 1];
   if (gs < ge) {
     const int rs = groups[gs].woff;
     const int re = groups[ge - 1].woff + groups[ge - 1].len;
@@ -580,6 +585,9 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
           }
         }
       }
+      float gs[RF_APT][3];
+#pragma unroll
+      for (int q = 0; q < RF_APT; ++q) gs[q][0] = gs[q][1] = gs[q][2] = 0.f;
 #pragma unroll
       for (int c = 0; c < KGRP; ++c) {
         if (G.col[c] < 0) continue;
@@ -592,21 +600,30 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
                                  conj_if(__ldg(&tab[(size_t)(kx + ny) * n + iq[q]]), col.ny < 0));
           const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
           const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
-          // per-column partials go to 64-bit fixed point (order independent)
-          ax[q] += f2ll_rn(rv.x * imTU * sc);
-          ay[q] += f2ll_rn(rv.y * imTU * sc);
-          az[q] += f2ll_rn(imTV * sc);
+          gs[q][0] = fmaf(rv.x, imTU, gs[q][0]);
+          gs[q][1] = fmaf(rv.y, imTU, gs[q][1]);
+          gs[q][2] += imTV;
         }
       }
+#pragma unroll
+      for (int q = 0; q < RF_APT; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float y = gs[q][a] - fc[q][a];
+          const float t = fs[q][a] + y;
+          fc[q][a] = (t - fs[q][a]) - y;
+          fs[q][a] = t;
+        }
     }
     cp_async_wait0();
   }
+  // to 64-bit fixed point (scale a power of two: exact products)
+  const float sc = fsc.scalef;
 #pragma unroll
-  for (int q = 0; q < RF_APT; ++q) {
-    red[0][part][lane + 32 * q] = ax[q];
-    red[1][part][lane + 32 * q] = ay[q];
-    red[2][part][lane + 32 * q] = az[q];
-  }
+  for (int q = 0; q < RF_APT; ++q)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      red[a][part][lane + 32 * q] = f2ll_rn(fs[q][a] * sc) - f2ll_rn(fc[q][a] * sc);
   __syncthreads();
   for (int j = threadIdx.x; j < RF_BATOMS; j += blockDim.x) {
     const int i = i0 + j;
@@ -618,9 +635,15 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
       sy += red[1][p][j];
       sz += red[2][p][j];
     }
-    gfix[i] += (unsigned long long)sx;
-    gfix[n + i] += (unsigned long long)sy;
-    gfix[2 * n + i] += (unsigned long long)sz;
+    if (gridDim.y == 1) {
+      gfix[i] += (unsigned long long)sx;
+      gfix[n + i] += (unsigned long long)sy;
+      gfix[2 * n + i] += (unsigned long long)sz;
+    } else {
+      atomicAdd(&gfix[i], (unsigned long long)sx);
+      atomicAdd(&gfix[n + i], (unsigned long long)sy);
+      atomicAdd(&gfix[2 * n + i], (unsigned long long)sz);
+    }
   }
 }
 
@@ -718,10 +741,11 @@ __global__ void k_eterms_init(mdx_scalars *sc, SelfEnergy se, int ntypes) {
   for (int t = 0; t < MDX_NT; ++t) sc->spee[t] = t < ntypes ? se.speei[t] : 0.0;
 }
 
-std::mutex g_smem_mu;
 
-template <typename K>
-cudaError_t raise_smem_limit(K kernel, size_t bytes) {
+}  // namespace
+
+std::mutex g_smem_mu;
+cudaError_t raise_smem_limit_fn(const void *kernel, size_t bytes) {
   std::lock_guard<std::mutex> lock(g_smem_mu);
   cudaFuncAttributes a;
   cudaError_t e = cudaFuncGetAttributes(&a, kernel);
@@ -729,8 +753,6 @@ cudaError_t raise_smem_limit(K kernel, size_t bytes) {
   if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-
-}  // namespace
 
 // INIFUR: the reference's k-set (forces.f:1366-1424) regrouped in columns,
 // and the self-energy SPEEI/SPEI (forces.f:1426-1447).
@@ -813,18 +835,6 @@ int host_inifur(mdx_ctx *ctx) {
     groups.push_back(g);
   }
   const size_t nwg = (size_t)RF_REC * std::max(1, woff);
-  // contiguous group ranges of the mixed force pass's warps, balanced by
-  // W records (woff is cumulative in group order)
-  {
-    int g = 0;
-    d.rf_parts[0] = 0;
-    for (int p = 1; p < RF_PARTS; ++p) {
-      const long long target = (long long)woff * p / RF_PARTS;
-      while (g < (int)groups.size() && groups[g].woff < target) ++g;
-      d.rf_parts[p] = g;
-    }
-    d.rf_parts[RF_PARTS] = (int)groups.size();
-  }
   std::vector<SItem> items;
   for (size_t g = 0; g < groups.size(); ++g)
     for (int t0 = 0; t0 < groups[g].len; t0 += SCH) items.push_back(SItem{(int)g, t0});
@@ -883,6 +893,51 @@ int host_inifur(mdx_ctx *ctx) {
     MDX_CUDA(raise_smem_limit(k_sfac32, sh));
   } else {
     MDX_CUDA(raise_smem_limit(k_sfac, sh));
+  }
+  // mixed force pass: blocks per atom tile (nsplit) so that the grid ends
+  // close to a whole number of waves, then contiguous group ranges per warp,
+  // balanced by W records (woff is cumulative in group order)
+  if (ctx->mixed()) {
+    int nsm = 0, dev = 0, per_sm = 0;
+    MDX_CUDA(cudaGetDevice(&dev));
+    MDX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rforce32,
+                                                             32 * RF_PARTS, shr));
+    const double slots = (double)std::max(1, per_sm) * nsm;
+    const double tiles = (double)((d.n + RF_BATOMS - 1) / RF_BATOMS);
+    int best = 1;
+    double best_eff = 0.0;
+    for (int s = 1; s <= 8; ++s) {
+      const double w = tiles * s / slots;
+      const double eff = w / std::ceil(w);
+      if (eff > best_eff + 0.02) {  // a larger split must gain clearly
+        best_eff = eff;
+        best = s;
+      }
+    }
+    d.rf_nsplit = best;
+    const int np = best * RF_PARTS;
+    std::vector<int> parts(np + 1);
+    int g = 0;
+    parts[0] = 0;
+    for (int p = 1; p < np; ++p) {
+      const long long target = (long long)woff * p / np;
+      while (g < (int)groups.size() && groups[g].woff < target) ++g;
+      parts[p] = g;
+    }
+    parts[np] = (int)groups.size();
+    ctx_free(ctx, d.rf_part);
+    d.rf_part = nullptr;
+    MDX_CUDA(ctx_alloc(ctx, &d.rf_part, sizeof(int) * parts.size()));
+    MDX_CUDA(cudaMemcpy(d.rf_part, parts.data(), sizeof(int) * parts.size(),
+                        cudaMemcpyHostToDevice));
+  }
+  // tensor-core force pass (mixed), unless MDX_EWALD_TC=0 or K is too large
+  // for its shared-memory tiles; the CUDA-core pass above stays set up
+  if (ctx->mixed()) {
+    const char *env = std::getenv("MDX_EWALD_TC");
+    d.tc_on = false;
+    if (!(env && env[0] == '0') && !tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
@@ -1029,20 +1084,23 @@ int launch_furir(mdx_ctx *ctx) {
         d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk, d.colrv,
         d.colrvf, dst);
     MDX_LAUNCHED(ctx);
-    k_wpairs<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-        d.ncol, d.cols, d.wk, mx ? nullptr : d.wp64, mx ? d.wkf : nullptr);
-    MDX_LAUNCHED(ctx);
+    if (!(mx && d.tc_on)) {
+      k_wpairs<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
+          d.ncol, d.cols, d.wk, mx ? nullptr : d.wp64, mx ? d.wkf : nullptr);
+      MDX_LAUNCHED(ctx);
+    }
     k_qpe_fold<<<1, 1, 0, ctx->stream>>>(sc, qpe);
     MDX_LAUNCHED(ctx);
   }
   MDX_TIMER(ctx, MDX_T_EW_FORCE);
   const int rblocks = (d.n + RF_ATOMS - 1) / RF_ATOMS;
-  if (mx) {
+  if (mx && d.tc_on) {
+    return tc_force_launch(ctx);
+  } else if (mx) {
     const size_t shr = sizeof(float2) * RF_BATOMS * d.kz;
-    RfParts parts;
-    for (int p = 0; p <= RF_PARTS; ++p) parts.g[p] = d.rf_parts[p];
-    k_rforce32<<<(d.n + RF_BATOMS - 1) / RF_BATOMS, 32 * RF_PARTS, shr, ctx->stream>>>(
-        d.n, parts, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
+    const dim3 grid((d.n + RF_BATOMS - 1) / RF_BATOMS, d.rf_nsplit);
+    k_rforce32<<<grid, 32 * RF_PARTS, shr, ctx->stream>>>(
+        d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
         d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(

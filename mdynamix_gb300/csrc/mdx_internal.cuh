@@ -45,6 +45,7 @@ enum : int {
   DERR_NPT = 16,
   DERR_TEMP = 32,
   DERR_CELL = 64,
+  DERR_TIMEOUT = 128,  // a bounded device wait (tensor-core pipeline) ran out
 };
 
 // Per-type constants passed by value to kernels.
@@ -196,7 +197,15 @@ struct DevData {
   void *sitems;                 // work items of the mixed S(k) pass
   int nsitem;
   int sfac_slice, sfac_nslice;  // atoms per slice and slices of that pass
-  int rf_parts[8];              // group ranges of the mixed force pass's warps
+  // mixed tensor-core force pass: column slots (sorted by m, -1 = padding)
+  // and K-steps per tile of 32 columns; B tiles (hi, lo) rebuilt per step
+  bool tc_on;
+  int *tc_slot, *tc_ks;
+  float *tc_w;
+  float4 *tc_meta;  // per slot {nx, ny, rv} for the epilogue
+  int tc_ntile, tc_kp;
+  int *rf_part;                 // group ranges of the mixed force pass's warps
+  int rf_nsplit;                // blocks per atom tile of that pass
   double2 *colrv;               // per column (RXV, RYV) at the current box
   float2 *colrvf;
   double *kscal;                // per-k scratch of the energy/virial kernel
@@ -494,6 +503,15 @@ int host_inifur(mdx_ctx *ctx);
 int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
+bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz);
+int tc_force_launch(mdx_ctx *ctx);
+// Dynamic shared-memory limit of a kernel: process-wide, shared by every
+// context, so it is only ever raised (under a lock).
+cudaError_t raise_smem_limit_fn(const void *kernel, size_t bytes);
+template <typename K>
+cudaError_t raise_smem_limit(K kernel, size_t bytes) {
+  return raise_smem_limit_fn(reinterpret_cast<const void *>(kernel), bytes);
+}
 // mdx_api.cu, for the allocation-free entry point in noalloc.cu
 int api_require(mdx_ctx *ctx, bool topo, bool par, bool state);
 int api_check_err(mdx_ctx *ctx);

@@ -194,6 +194,34 @@ def test_mixed_force_error(name):
         assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * abs(getattr(a, n)) + 1e-9, n
 
 
+@pytest.mark.parametrize("name", ["spce_ions", "spcfw", "bilayer_patch"])
+def test_mixed_ewald_tensor_core_pass(name, monkeypatch):
+    """The tensor-core reciprocal force pass (3 x TF32 products) and the
+    CUDA-core FP32 pass agree with the FP64 path to the mixed bar, and with
+    each other well inside it."""
+    s, st = CASES[name]()
+    g64 = ForcePath(s, precision=MDX_FP64)
+    out = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("MDX_EWALD_TC", tc)
+        g = ForcePath(s, precision=MDX_MIXED)
+        g.set_state(*st)
+        g.chcnb()
+        g.getcom()
+        g.allforce()
+        out[tc] = g.forces(3)
+        g.close()
+    g64.set_state(*st)
+    g64.chcnb()
+    g64.getcom()
+    g64.allforce()
+    f64 = g64.forces(3)
+    nrm = np.sqrt((f64 ** 2).sum())
+    for tc, f in out.items():
+        assert np.sqrt(((f - f64) ** 2).sum()) / nrm < MIXED_TOL, tc
+    assert np.sqrt(((out["1"] - out["0"]) ** 2).sum()) / nrm < 2e-6
+
+
 def test_mixed_deterministic():
     s, st = CASES["spcfw"]()
     outs = []
