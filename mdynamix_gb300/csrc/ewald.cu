@@ -78,7 +78,7 @@ __device__ __forceinline__ void cp_async_wait0() {
 }
 
 // Phase tables: thread per (axis, atom), FP64 recurrence from one sincos.
-__global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
+__global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ibx,
                          double iby, double ibz, int kx, int ky, int kz,
                          double2 *__restrict__ tx, double2 *__restrict__ ty,
                          double2 *__restrict__ tz, float2 *__restrict__ txf,
@@ -95,10 +95,10 @@ __global__ void k_tables(int n, const dbl4 *__restrict__ pos, double ibx,
   const int len = a == 0 ? kx : a == 1 ? ky : kz;
   const double q = a == 0 ? p.w : 1.0;
   double2 v = make_double2(1.0, 0.0);
-  if (txf) {  // mixed path: FP64 recurrence, FP32 table
+  if (txf) {  // mixed path: FP64 recurrence, FP32 table (row stride ldn)
     float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
     for (int k = 0; k < len; ++k) {
-      dst[(size_t)k * n] = make_float2((float)(q * v.x), (float)(q * v.y));
+      dst[(size_t)k * ldn] = make_float2((float)(q * v.x), (float)(q * v.y));
       v = cmul(v, e);
     }
   } else {
@@ -215,9 +215,9 @@ struct SItem {
 
 __global__ void __launch_bounds__(128, 3) k_sfac32(
     int n, int nitem, const SItem *__restrict__ items, const KGroup *__restrict__ groups,
-    const KCol *__restrict__ cols, const float2 *__restrict__ tab, int kx, int ky, int kz,
-    int slice, double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * n
+    const KCol *__restrict__ cols, const float2 *__restrict__ tab, int ldn, int kx, int ky,
+    int kz, int slice, double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
+  // tab: the X, Y and Z tables back to back, row r at tab + r * ldn
   extern __shared__ float2 srow[];  // [2][TILE][kx + ky + kz + SCH], double buffer
   const int zpad = kx + ky + kz;    // first zero entry of a row
   const int rowlen = zpad + SCH;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(128, 3) k_sfac32(
     float2 *dst = srow + buf * bufsz;
     for (int k = threadIdx.x; k < m * zpad; k += blockDim.x) {
       const int r = k / m, j = k - r * m;
-      cp_async8(dst + j * rowlen + r, tab + (size_t)r * n + base + j);
+      cp_async8(dst + j * rowlen + r, tab + (size_t)r * ldn + base + j);
     }
   };
   if (a0 < a1) stage(0, a0);
@@ -509,18 +509,19 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
     int n, const int *__restrict__ parts, const KGroup *__restrict__ groups,
     const KCol *__restrict__ cols,
-    const float4 *__restrict__ wg, const float2 *__restrict__ tab, int kx, int ky, int kz,
-    const float2 *__restrict__ colrv, FixScale fsc, unsigned long long *__restrict__ gfix) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * n
+    const float4 *__restrict__ wg, const float2 *__restrict__ tab, int ldn, int kx, int ky,
+    int kz, const float2 *__restrict__ colrv, FixScale fsc,
+    unsigned long long *__restrict__ gfix) {
+  // tab: the X, Y and Z tables back to back, row r at tab + r * ldn
   extern __shared__ float2 srf[];  // [kz][RF_BATOMS]
   __shared__ long long red[3][RF_PARTS][RF_BATOMS];
   __shared__ float4 ring[RF_PARTS][2][RF_WB * RF_REC];
   const int lane = threadIdx.x % 32, part = threadIdx.x / 32;
   const int i0 = blockIdx.x * RF_BATOMS;
-  const float2 *tz = tab + (size_t)(kx + ky) * n;
+  const float2 *tz = tab + (size_t)(kx + ky) * ldn;
   for (int k = threadIdx.x; k < kz * RF_BATOMS; k += blockDim.x) {
     const int r = k / RF_BATOMS, j = k - r * RF_BATOMS;
-    srf[k] = i0 + j < n ? tz[(size_t)r * n + i0 + j] : make_float2(0.f, 0.f);
+    srf[k] = i0 + j < n ? tz[(size_t)r * ldn + i0 + j] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   // per atom and axis: the group sums (4 columns, FP32) accumulated with
@@ -596,8 +597,8 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
         const float2 rv = colrv[G.col[c]];
 #pragma unroll
         for (int q = 0; q < RF_APT; ++q) {
-          const float2 T = cmulf(__ldg(&tab[(size_t)col.nx * n + iq[q]]),
-                                 conj_if(__ldg(&tab[(size_t)(kx + ny) * n + iq[q]]), col.ny < 0));
+          const float2 T = cmulf(__ldg(&tab[(size_t)col.nx * ldn + iq[q]]),
+                                 conj_if(__ldg(&tab[(size_t)(kx + ny) * ldn + iq[q]]), col.ny < 0));
           const float imTU = fmaf(T.x, u[q][c][1], T.y * u[q][c][0]);
           const float imTV = fmaf(T.x, v[q][c][1], T.y * v[q][c][0]);
           gs[q][0] = fmaf(rv.x, imTU, gs[q][0]);
@@ -841,6 +842,7 @@ int host_inifur(mdx_ctx *ctx) {
   std::stable_sort(items.begin(), items.end(),
                    [](const SItem &a, const SItem &b) { return a.t0 < b.t0; });
   const int kx = KMAX + 1, ky = KMAY + 1, kz = KMAZ + 1;
+  d.ldn = ((d.n + 127) / 128) * 128;  // row stride of the FP32 tables
   const bool realloc_tables = kx != d.kx || ky != d.ky || kz != d.kz;
   d.kx = kx;
   d.ky = ky;
@@ -936,8 +938,11 @@ int host_inifur(mdx_ctx *ctx) {
   // for its shared-memory tiles; the CUDA-core pass above stays set up
   if (ctx->mixed()) {
     const char *env = std::getenv("MDX_EWALD_TC");
-    d.tc_on = false;
-    if (!(env && env[0] == '0') && !tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
+    d.tc_on = d.tcs_on = false;
+    if (!(env && env[0] == '0')) {
+      if (!tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
+      if (!tc_sfac_setup(ctx, cols)) cudaGetLastError();
+    }
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
@@ -960,9 +965,12 @@ int host_inifur(mdx_ctx *ctx) {
     d.tabxf = d.tabyf = d.tabzf = nullptr;
     const size_t per = (size_t)kx + ky + kz;
     if (ctx->mixed()) {
-      MDX_CUDA(ctx_alloc(ctx, &d.tabxf, sizeof(float2) * per * d.n));
-      d.tabyf = d.tabxf + (size_t)kx * d.n;
-      d.tabzf = d.tabyf + (size_t)ky * d.n;
+      // rows padded to ldn atoms (zero past n): row starts stay 1 KB aligned
+      // for the bulk copies of the tensor-core passes
+      MDX_CUDA(ctx_alloc(ctx, &d.tabxf, sizeof(float2) * per * d.ldn));
+      MDX_CUDA(cudaMemset(d.tabxf, 0, sizeof(float2) * per * d.ldn));
+      d.tabyf = d.tabxf + (size_t)kx * d.ldn;
+      d.tabzf = d.tabyf + (size_t)ky * d.ldn;
     } else {
       MDX_CUDA(ctx_alloc(ctx, &d.tabx, sizeof(double2) * per * d.n));
       d.taby = d.tabx + (size_t)kx * d.n;
@@ -1047,9 +1055,10 @@ int launch_furir(mdx_ctx *ctx) {
   {
     MDX_TIMER(ctx, MDX_T_EW_TABLES);
     k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
-        d.n, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
+        d.n, d.ldn, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
         d.tabxf, d.tabyf, d.tabzf);
     MDX_LAUNCHED(ctx);
+    if (mx && (rc = tc_zimages_launch(ctx))) return rc;
   }
   MDX_CUDA(cudaMemsetAsync(d.sk, 0, sizeof(double2) * d.nkv, ctx->stream));
   {
@@ -1057,19 +1066,23 @@ int launch_furir(mdx_ctx *ctx) {
     const size_t sh = mx ? 2 * sizeof(float2) * TILE * (d.kx + d.ky + d.kz + SCH)
                          : sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
     dim3 grid;
-    if (mx) {
-      grid = dim3((d.nsitem + 127) / 128, d.sfac_nslice);
-      k_sfac32<<<grid, 128, sh, ctx->stream>>>(
-          d.n, d.nsitem, reinterpret_cast<const SItem *>(d.sitems), d.kgroups, d.cols,
-          d.tabxf, d.kx, d.ky, d.kz, d.sfac_slice, d.sk, d.sk_part, d.nkv);
+    if (mx && d.tcs_on) {
+      if ((rc = tc_sfac_launch(ctx))) return rc;
     } else {
-      grid = dim3((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
-      k_sfac<<<grid, 128, sh, ctx->stream>>>(
-          d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk,
-          d.sk_part, d.nkv);
+      if (mx) {
+        grid = dim3((d.nsitem + 127) / 128, d.sfac_nslice);
+        k_sfac32<<<grid, 128, sh, ctx->stream>>>(
+            d.n, d.nsitem, reinterpret_cast<const SItem *>(d.sitems), d.kgroups, d.cols,
+            d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.sfac_slice, d.sk, d.sk_part, d.nkv);
+      } else {
+        grid = dim3((nchunk + 127) / 128, (d.n + SLICE - 1) / SLICE);
+        k_sfac<<<grid, 128, sh, ctx->stream>>>(
+            d.n, nchunk, chunks, d.cols, d.tabx, d.taby, d.tabz, d.kx, d.ky, d.kz, d.sk,
+            d.sk_part, d.nkv);
+      }
+      MDX_LAUNCHED(ctx);
     }
-    MDX_LAUNCHED(ctx);
-    if (d.sk_part) {
+    if (d.sk_part && !(mx && d.tcs_on)) {
       k_sfac_sum<<<(d.nkv + 255) / 256, 256, 0, ctx->stream>>>(d.nkv, (int)grid.y,
                                                                 d.sk_part, d.sk);
       MDX_LAUNCHED(ctx);
@@ -1100,7 +1113,7 @@ int launch_furir(mdx_ctx *ctx) {
     const size_t shr = sizeof(float2) * RF_BATOMS * d.kz;
     const dim3 grid((d.n + RF_BATOMS - 1) / RF_BATOMS, d.rf_nsplit);
     k_rforce32<<<grid, 32 * RF_PARTS, shr, ctx->stream>>>(
-        d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
+        d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
         d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(

@@ -1,28 +1,32 @@
-// ewald_tc.cu -- mixed-precision reciprocal Ewald force pass on the tensor
-// cores (FURIR's force loop, forces.f:1286-1314).
+// ewald_tc.cu -- mixed-precision reciprocal Ewald on the tensor cores: the
+// structure factors and the force pass of FURIR (forces.f:1286-1314).
 //
-// With Z_j(p) = a + i b (p = 0..KMAZ) and the paired W of each column
-// (P = W(+p) + W(-p), M = W(+p) - W(-p)), the per-atom column sums
-//   U.re = sum_p P.re a - M.im b,   U.im = sum_p P.im a + M.re b
-// (and V the same with RZV W) are one real matrix product
-//   D[atom][4 c + t] = sum_k A[atom][k] B[4 c + t][k],
-//   A[atom][2p] = a, A[atom][2p+1] = b,  K = 2 (KMAZ + 1) rounded up to 8,
-// so the whole force pass is an (atoms x K) x (K x 4 ncol) GEMM followed by
-// F_j += sum_c rv_c Im(T_j(c) U_j(c)), Fz += Im(T_j(c) V_j(c)).
+// With per-atom phase tables X_j(nx) (charge included), Y_j(ny), Z_j(p) =
+// a + i b (p = 0..KMAZ) and the k-set in columns (nx, ny) whose nz = +p and
+// -p are taken together (Z_j(-p) = conj Z_j(p)):
 //
-// The GEMM runs as TF32 tcgen05 MMAs (M = 128 atoms, N = 128 = 32 columns,
-// K = 8 per instruction) with FP32 accumulators in tensor memory.  Each
-// operand is split into two TF32 parts, x = hi + lo, and three products
-// hi*hi + hi*lo + lo*hi keep close to FP32 accuracy (the dropped lo*lo term
-// is 2^-22 relative).  Columns are sorted by m = max |nz| (descending) so a
-// tile of 32 columns only runs the K-steps its largest m needs.
+// * S(k): with T_j(c) = X_j(nx) Y_j(ny), the four sums of a (column, p) pair
+//     A1 = sum T.re a, A2 = sum T.im b, A3 = sum T.re b, A4 = sum T.im a
+//   are the entries of D = A B^T, A[2c + e][j] = (T.re, T.im)_j(c),
+//   B[2p + e][j] = (a, b)_j(p), K running over atoms; then
+//   S(c, +p) = (A1 - A2, A3 + A4), S(c, -p) = (A1 + A2, A4 - A3).
+// * forces: with the paired W of each column (P = W(+p) + W(-p),
+//   M = W(+p) - W(-p)), U.re = sum_p P.re a - M.im b, U.im = sum_p P.im a +
+//   M.re b (V the same with RZV W) are D[j][4c + t] = sum_k A[j][k] B[4c+t][k]
+//   with A[j][2p] = a, A[j][2p + 1] = b (K = 2 (KMAZ + 1) rounded up to 8);
+//   then F_j += sum_c rv_c Im(T_j(c) U_j(c)), Fz += Im(T_j(c) V_j(c)).
 //
-// A CTA owns 128 atoms: it stages their Z rows (hi and lo) once, then walks
-// the column tiles with two shared-memory B buffers and two tensor-memory
-// accumulators: MMA(t + 1) runs while the CTA's four warps read tile t's
-// accumulator (tcgen05.ld) and fold it into the forces.  The B tiles (hi and
-// lo, already in the MMA's core-matrix order) are built once per step by
-// k_wtiles from the per-k W values.
+// Both GEMMs run as TF32 tcgen05 MMAs (M = 128, K = 8 per instruction) into
+// FP32 accumulators in tensor memory.  Each operand is split into two TF32
+// parts, x = hi + lo, and three products hi*hi + hi*lo + lo*hi keep close to
+// FP32 accuracy (the dropped lo*lo term is 2^-22 relative).  The Z operands
+// of both passes are written once per step (k_zimages) as images in the
+// MMA's core-matrix order, so the passes bring them in with bulk copies; the
+// X and Y rows of their atoms come in as one tiled TMA box of the tables
+// (the FP32 tables have a row stride of ldn atoms, a multiple of 128, zero
+// past n).
+#include <cuda.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -31,22 +35,72 @@
 
 namespace {
 
-constexpr int TC_M = 128;         // atoms per CTA (MMA M)
-constexpr int TC_N = 128;         // accumulator columns per tile (32 k-columns)
+constexpr int TC_M = 128;          // atoms per CTA of the force pass (MMA M)
+constexpr int TC_N = 128;          // accumulator columns per tile (32 k-columns)
 constexpr int TC_COLS = TC_N / 4;  // k-columns per tile
+constexpr int TC_THREADS = 256;    // force pass: 8 warps, two per lane quarter
 constexpr uint32_t TC_POLLS = 1u << 20;  // bounded mbarrier waits
 
-// Byte offset of element (row r, k) in a K-major, unswizzled tile of kp
-// columns: core matrix (r / 8, k / 4) of 128 bytes, SBO = 32 kp, LBO = 128.
+// Force-pass operand layout: element (row r, k) of a K-major, unswizzled tile
+// of kp columns sits in core matrix (r / 8, k / 4) of 128 bytes: SBO = 32 kp,
+// LBO = 128.
 __host__ __device__ __forceinline__ uint32_t core_off(int r, int k, int kp) {
   return (uint32_t)((((r >> 3) * (kp >> 2) + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
 }
 
-// B tiles of one step: thread per (tile, row r, 4 consecutive k).  Row r of
-// tile t is column slot[32 t + r / 4], component r % 4 (U.re, U.im, V.re,
-// V.im); k = 2p takes the a-coefficient, k = 2p + 1 the b-coefficient.  The
-// threads with r % 4 = 0 and k = 0 also write the slot's epilogue record
-// {nx, ny (int bits; nx = -1 for padding), rv.x, rv.y}.
+// S-pass operand layout: 32 atoms (K) per chunk, core matrices along K
+// 144 bytes apart (128 + 16 spreads the shared-memory banks), SBO = 8 x 144.
+constexpr int SK_ROWS = 128;  // rows of an M-tile (64 columns x re/im)
+constexpr int SK_CH = 32;     // atoms per chunk (K of one stage)
+constexpr int SK_LBO = 144;
+constexpr int SK_SBO = 8 * SK_LBO;
+constexpr uint32_t SK_APART = (SK_ROWS / 8) * SK_SBO;  // bytes of one A part
+constexpr int SK_GCH = 32;  // chunks per partial sum written out (1024 atoms)
+
+__host__ __device__ __forceinline__ uint32_t sk_off(int row, int q) {  // (row, atom quad)
+  return (uint32_t)((row >> 3) * SK_SBO + q * SK_LBO + ((row & 7) << 4));
+}
+__host__ __device__ __forceinline__ uint32_t sk_bpart(int np) {  // bytes of one B part
+  return (uint32_t)(np / 8) * SK_SBO;
+}
+
+// Z images of one step: thread per (p, atom), atoms up to ldn (rows past n
+// are zero in the table).  zf: force-pass A operand, per 128-atom tile
+// [hi | lo] of 128 x kp; zs: S-pass B operand, per 32-atom chunk [hi | lo]
+// of np x 32.  Entries with p >= kz stay zero (set once at allocation).
+__global__ void k_zimages(int ldn, int kz, int kp, int np, const float2 *__restrict__ tz,
+                          unsigned char *__restrict__ zf, unsigned char *__restrict__ zs) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)kz * ldn) return;
+  const int p = (int)(t / ldn), i = (int)(t - (size_t)p * ldn);
+  const float2 z = tz[t];
+  float ah, al, bh, bl;
+  tc::tf32_split(z.x, ah, al);
+  tc::tf32_split(z.y, bh, bl);
+  if (zf) {
+    unsigned char *base = zf + (size_t)(i >> 7) * 1024 * kp;
+    const uint32_t o = core_off(i & 127, 2 * p, kp);  // k = 2p and 2p + 1: adjacent
+    *reinterpret_cast<float2 *>(base + o) = make_float2(ah, bh);
+    *reinterpret_cast<float2 *>(base + 512 * kp + o) = make_float2(al, bl);
+  }
+  if (zs) {
+    const uint32_t bp = sk_bpart(np);
+    unsigned char *base = zs + (size_t)(i >> 5) * 2 * bp;
+    const int j = i & 31;
+    const uint32_t o0 = sk_off(2 * p, j >> 2) + 4 * (j & 3);
+    const uint32_t o1 = sk_off(2 * p + 1, j >> 2) + 4 * (j & 3);
+    *reinterpret_cast<float *>(base + o0) = ah;
+    *reinterpret_cast<float *>(base + o1) = bh;
+    *reinterpret_cast<float *>(base + bp + o0) = al;
+    *reinterpret_cast<float *>(base + bp + o1) = bl;
+  }
+}
+
+// B tiles of the force pass, one step: thread per (tile, row r, 4
+// consecutive k).  Row r of tile t is column slot[32 t + r / 4], component
+// r % 4 (U.re, U.im, V.re, V.im); k = 2p takes the a-coefficient, k = 2p + 1
+// the b-coefficient.  The threads with r % 4 = 0 and k = 0 also write the
+// slot's epilogue record {nx, ny (int bits; nx = -1 for padding), rv.x, rv.y}.
 __global__ void k_wtiles(int ntile, int kp, const int *__restrict__ slot,
                          const KCol *__restrict__ cols, const dbl4 *__restrict__ wk,
                          const float2 *__restrict__ colrv, float *__restrict__ tw,
@@ -97,21 +151,26 @@ __global__ void k_wtiles(int ntile, int kp, const int *__restrict__ slot,
   *reinterpret_cast<float4 *>(base + tsz) = lo;
 }
 
-// Force pass: one CTA of 4 warps per 128 atoms.  Shared memory (1024-byte
-// aligned): A hi | A lo | B0 hi | B0 lo | B1 hi | B1 lo | X, Y rows of the
-// CTA's atoms ([row][atom], float2).  Thread 0 issues the bulk copies of the
-// B tiles (one tile ahead of the MMAs) and the MMAs; all four warps read the
-// accumulators.  Barriers: bfull[b] (B tile landed in buffer b), mdone[b]
-// (MMAs into accumulator b done, so B buffer b is free again).
-__global__ void __launch_bounds__(128, 1) k_rforce_tc(
-    int n, int ntile, int kp, const int *__restrict__ tile_ks, const float4 *__restrict__ meta,
-    const float4 *__restrict__ tw, const float2 *__restrict__ tab, int kx, int ky, int kz,
-    FixScale fsc, unsigned long long *__restrict__ gfix, int *__restrict__ err) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * n
+// Force pass: one CTA of 8 warps per 128 atoms.  Shared memory (1024-byte
+// aligned): A hi | A lo (the tile's Z image) | B0 hi | B0 lo | B1 hi | B1 lo |
+// X, Y rows of the CTA's atoms ([row][atom], float2).  Thread 0 issues the
+// bulk copies (A, X, Y once; B one tile ahead of the MMAs) and the MMAs.
+// Warps w and w + 4 read the same accumulator lanes (32 (w % 4) ..) and
+// split each tile's 32 columns between them.  Barriers: abar (A, X, Y
+// landed), bfull[b] (B tile landed in buffer b), mdone[b] (MMAs into
+// accumulator b done, so B buffer b is free again).
+__global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
+    int n, int ldn, int ntile, int kp, const int *__restrict__ tile_ks,
+    const float4 *__restrict__ meta, const float4 *__restrict__ tw,
+    const unsigned char *__restrict__ zimg, const __grid_constant__ CUtensorMap tmxy, int kx,
+    int ky, FixScale fsc, unsigned long long *__restrict__ gfix, int *__restrict__ err) {
+  // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 TC_M x (kx + ky)
   extern __shared__ unsigned char dsm_raw[];
-  __shared__ __align__(8) unsigned long long bfull[2], mdone[2];
+  __shared__ __align__(8) unsigned long long abar, bfull[2], mdone[2];
   __shared__ uint32_t tmem_base_sh;
+  __shared__ float red[6][TC_M];  // second-half partials (sum, compensation)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2;
   const int i0 = blockIdx.x * TC_M;
   const uint32_t raw = tc::smem_addr(dsm_raw);
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
@@ -119,20 +178,22 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
   const uint32_t sbase = raw + pad;
   const uint32_t part = (uint32_t)TC_M * kp * 4;  // bytes of one hi or lo tile
   const uint32_t sA = sbase, sB = sbase + 2 * part;
-  float2 *sxy = reinterpret_cast<float2 *>(dsm + 6 * (size_t)part);  // [kx + ky][TC_M]
+  const float2 *sxy = reinterpret_cast<const float2 *>(dsm + 6 * (size_t)part);  // [kx+ky][128]
+  const int kxy = kx + ky;
 
   if (warp == 0) {
     tc::tmem_alloc(tc::smem_addr(&tmem_base_sh), 2 * TC_N);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
+    tc::mbar_init(tc::smem_addr(&abar), 1);
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(tc::smem_addr(&bfull[b]), 1);
       tc::mbar_init(tc::smem_addr(&mdone[b]), 1);
     }
     tc::mbar_init_fence();
   }
-  __syncthreads();  // barriers initialised before the first copy arrives on them
+  __syncthreads();  // barriers initialised before any copy arrives on them
   // B tile t -> buffer b: one bulk copy of both parts (2 part bytes)
   auto copy_b = [&](int t, int b) {
     const uint32_t bar = tc::smem_addr(&bfull[b]);
@@ -140,41 +201,16 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
     tc::bulk_g2s(sB + (uint32_t)b * 2 * part, tw + (size_t)t * (2 * part / 16), 2 * part, bar);
   };
   if (tid == 0) {
+    const uint32_t bar = tc::smem_addr(&abar);
+    tc::mbar_arrive_expect_tx(bar, 2 * part + (uint32_t)kxy * TC_M * 8);
+    tc::bulk_g2s(sA, zimg + (size_t)blockIdx.x * 2 * part, 2 * part, bar);
+    tc::tma_load_2d(sA + 6 * part, &tmxy, 2 * i0, 0, bar);
     if (ntile > 0) copy_b(0, 0);
     if (ntile > 1) copy_b(1, 1);
   }
-  // A: this CTA's Z rows, hi and lo parts (rows past n are zero)
-  {
-    const int i = i0 + tid;
-    const float2 *tz = tab + (size_t)(kx + ky) * n;
-    for (int kc = 0; kc < (kp >> 2); ++kc) {
-      float z[4];
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const int p = 2 * kc + e;
-        float2 v = make_float2(0.f, 0.f);
-        if (i < n && p < kz) v = tz[(size_t)p * n + i];
-        z[2 * e] = v.x;
-        z[2 * e + 1] = v.y;
-      }
-      float4 hi, lo;
-      tc::tf32_split(z[0], hi.x, lo.x);
-      tc::tf32_split(z[1], hi.y, lo.y);
-      tc::tf32_split(z[2], hi.z, lo.z);
-      tc::tf32_split(z[3], hi.w, lo.w);
-      const uint32_t o = core_off(tid, 4 * kc, kp);
-      *reinterpret_cast<float4 *>(dsm + o) = hi;
-      *reinterpret_cast<float4 *>(dsm + part + o) = lo;
-    }
-  }
-  // X and Y rows of the CTA's atoms (clamped past n; those rows are unused)
-  for (int k = tid; k < (kx + ky) * TC_M; k += blockDim.x) {
-    const int r = k / TC_M, a = k - r * TC_M;
-    sxy[k] = tab[(size_t)r * n + min(i0 + a, n - 1)];
-  }
+  bool ok = tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS);
   const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
   const uint32_t lbo = 128, sbo = 32u * kp;
-  bool ok = true;
   auto issue = [&](int t, int b, uint32_t tbase) {
     if (!tc::mbar_wait(tc::smem_addr(&bfull[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS)) ok = false;
     tc::fence_after_sync();
@@ -192,15 +228,14 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
     tc::mma_commit(tc::smem_addr(&mdone[b]));
   };
 
-  tc::fence_proxy_async();  // A visible to the tensor cores
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = tmem_base_sh;
   if (tid == 0 && ntile > 0) issue(0, 0, tbase);
 
-  const int i = i0 + 32 * warp + lane;
-  const float2 *xa = sxy + 32 * warp + lane;  // this thread's atom, row 0
+  const int row = 32 * quarter + lane;  // this thread's atom within the tile
+  const float2 *xa = sxy + row;         // its X, Y rows
   float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
   for (int t = 0; t < ntile; ++t) {
     const int b = t & 1;
@@ -215,11 +250,11 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
       issue(t + 1, b ^ 1, tbase);
     }
     __syncwarp();  // warp 0 converged again before the warp-wide tcgen05.ld
-    // epilogue of tile t: 4 chunks of 8 columns (32 accumulator columns)
+    // epilogue of tile t: this warp's 2 chunks of 8 columns
     float gs[3] = {0.f, 0.f, 0.f};
-    for (int h = 0; h < TC_N / 32; ++h) {
+    for (int h = 2 * half; h < 2 * half + 2; ++h) {
       float v[32];
-      tc::tmem_ld32(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * TC_N + 32 * h), v);
+      tc::tmem_ld32(tbase + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * TC_N + 32 * h), v);
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const float4 mt = __ldg(&meta[t * TC_COLS + 8 * h + j]);  // nx, ny, rv
@@ -245,7 +280,14 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
       fs[a] = s;
     }
   }
-  __syncthreads();  // every tensor-memory read is done
+  if (half == 1) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      red[a][row] = fs[a];
+      red[3 + a][row] = fc[a];
+    }
+  }
+  __syncthreads();  // every tensor-memory read is done; halves meet
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tbase, 2 * TC_N);
@@ -254,27 +296,250 @@ __global__ void __launch_bounds__(128, 1) k_rforce_tc(
     atomicOr(err, DERR_TIMEOUT);
     return;
   }
-  if (i < n) {
+  const int i = i0 + row;
+  if (half == 0 && i < n) {
     const float sc = fsc.scalef;
-    gfix[i] += (unsigned long long)(f2ll_rn(fs[0] * sc) - f2ll_rn(fc[0] * sc));
-    gfix[n + i] += (unsigned long long)(f2ll_rn(fs[1] * sc) - f2ll_rn(fc[1] * sc));
-    gfix[2 * n + i] += (unsigned long long)(f2ll_rn(fs[2] * sc) - f2ll_rn(fc[2] * sc));
+    long long q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)  // fixed point, integer sums: order independent
+      q[a] = f2ll_rn(fs[a] * sc) - f2ll_rn(fc[a] * sc) + f2ll_rn(red[a][row] * sc) -
+             f2ll_rn(red[3 + a][row] * sc);
+    gfix[i] += (unsigned long long)q[0];
+    gfix[n + i] += (unsigned long long)q[1];
+    gfix[2 * n + i] += (unsigned long long)q[2];
   }
 }
 
-// Shared memory of the force pass: operands plus the X, Y rows, at least
-// 80 KB so that no more than two CTAs (2 x 256 tensor-memory columns) share
-// an SM.
+// Shared memory of the force pass: A, two B buffers, the X and Y rows.
 size_t tc_smem_bytes(int kp, int kxy) {
-  return std::max<size_t>(80 * 1024, 1024 + 6 * (size_t)TC_M * kp * 4 +
-                                         (size_t)kxy * TC_M * sizeof(float2));
+  return 1024 + 6 * (size_t)TC_M * kp * 4 + (size_t)kxy * TC_M * sizeof(float2);
+}
+
+__device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, float a, float b,
+                                         float c, float d) {
+  float4 h, l;
+  tc::tf32_split(a, h.x, l.x);
+  tc::tf32_split(b, h.y, l.y);
+  tc::tf32_split(c, h.z, l.z);
+  tc::tf32_split(d, h.w, l.w);
+  *reinterpret_cast<float4 *>(hi) = h;
+  *reinterpret_cast<float4 *>(lo) = l;
+}
+
+// S-pass: a CTA (8 warps, one per SM) takes an M-tile of 64 columns (128
+// rows) and a slice of atoms (a multiple of 32), np <= 64.  Per chunk of 32
+// atoms, thread 0 brings in the chunk's X and Y rows and its Z image (the B
+// operand) with bulk copies, SK_NB chunks ahead; all threads form T = X Y for
+// the tile's columns into the A operand (two buffers); thread 0 issues the
+// MMAs.  Tensor memory: two regions of 64 columns; group g of SK_GCH chunks
+// accumulates in region g % 2 and is written out as partial gps * slice + g
+// while group g + 1 runs.  Barriers: full[s] (X, Y rows and Z image of the
+// chunk in stage s landed), mdone[s] (MMAs of the chunk in stage s done),
+// gdone[r] (the group in region r done).
+constexpr int SK_NB = 4;         // copy stages (chunks in flight)
+constexpr int SK_THREADS = 256;  // 512 A items per chunk: 2 per thread
+
+__global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
+    int n, int ncol, int np, int slice, int gps, const KCol *__restrict__ cols,
+    const __grid_constant__ CUtensorMap tmxy, const unsigned char *__restrict__ zimg, int kx,
+    int ky, float *__restrict__ part, int *__restrict__ err) {
+  // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 SK_CH x (kx + ky)
+  extern __shared__ unsigned char dsm_raw[];
+  __shared__ __align__(8) unsigned long long full[SK_NB], mdone[SK_NB], gdone[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int2 cxy[SK_ROWS / 2];  // (nx, ny) of the tile's columns (nx < 0: none)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, ntm = gridDim.x;
+  const int a0 = blockIdx.y * slice, a1 = min(n, a0 + slice);
+  const uint32_t raw = tc::smem_addr(dsm_raw);
+  const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+  unsigned char *dsm = dsm_raw + pad;
+  const uint32_t sbase = raw + pad;
+  const uint32_t bpart = sk_bpart(np);
+  const int kxy = kx + ky;
+  const uint32_t xysz = (uint32_t)kxy * SK_CH * 8;  // X, Y rows of one chunk
+  // A0 (hi, lo) | A1 (hi, lo) | SK_NB x B (hi, lo) | SK_NB x X, Y rows [kxy][32]
+  const uint32_t oB = 4 * SK_APART, oX = oB + SK_NB * 2 * bpart;
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_addr(&tmem_base_sh), 128);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int s = 0; s < SK_NB; ++s) {
+      tc::mbar_init(tc::smem_addr(&full[s]), 1);
+      tc::mbar_init(tc::smem_addr(&mdone[s]), 1);
+    }
+    tc::mbar_init(tc::smem_addr(&gdone[0]), 1);
+    tc::mbar_init(tc::smem_addr(&gdone[1]), 1);
+    tc::mbar_init_fence();
+  }
+  if (tid < SK_ROWS / 2) {
+    const int c = mt * (SK_ROWS / 2) + tid;
+    int2 v = make_int2(-1, 0);
+    if (c < ncol) v = make_int2(cols[c].nx, cols[c].ny);
+    cxy[tid] = v;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = tmem_base_sh;
+  const uint32_t idesc = tc::idesc_tf32(SK_ROWS, np);
+  const int nchunk = (a1 - a0 + SK_CH - 1) / SK_CH;
+  const int ngroup = (nchunk + SK_GCH - 1) / SK_GCH;
+  bool ok = true;
+  // X, Y rows and Z image of chunk c into stage c % SK_NB (thread 0)
+  auto copy_in = [&](int c) {
+    const int s = c % SK_NB;
+    const uint32_t bar = tc::smem_addr(&full[s]);
+    const int j0 = a0 + c * SK_CH;
+    tc::mbar_arrive_expect_tx(bar, xysz + 2 * bpart);
+    tc::tma_load_2d(sbase + oX + (uint32_t)s * xysz, &tmxy, 2 * j0, 0, bar);
+    tc::bulk_g2s(sbase + oB + (uint32_t)s * 2 * bpart,
+                 zimg + (size_t)(a0 / SK_CH + c) * 2 * bpart, 2 * bpart, bar);
+  };
+  auto wait_mma = [&](int c) {  // MMAs of chunk c done
+    if (!tc::mbar_wait(tc::smem_addr(&mdone[c % SK_NB]), (uint32_t)(c / SK_NB) & 1u, TC_POLLS))
+      ok = false;
+  };
+  // write out the accumulator of group g (region g % 2) as partial
+  // gps * blockIdx.y + g: D row 32 (warp % 4) + lane, np columns; warps
+  // w and w + 4 take halves of the columns
+  auto flush = [&](int g) {
+    if (!tc::mbar_wait(tc::smem_addr(&gdone[g & 1]), (uint32_t)(g >> 1) & 1u, TC_POLLS))
+      ok = false;
+    tc::fence_after_sync();
+    __syncwarp();
+    const int q4 = warp & 3, hh = warp >> 2;
+    const int row = 32 * q4 + lane;
+    float *dst = part + (((size_t)(gps * blockIdx.y + g) * ntm + mt) * SK_ROWS + row) * np;
+    const int h = 32 * hh;  // np <= 64: columns [0, 32) and [32, 64)
+    if (h < np) {
+      float v[32];
+      tc::tmem_ld32(tbase + ((uint32_t)(32 * q4) << 16) + (uint32_t)(64 * (g & 1) + h), v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (h + j < np) dst[h + j] = v[j];
+    }
+    tc::fence_before_sync();
+  };
+
+  if (tid == 0)
+    for (int c = 0; c < min(nchunk, SK_NB - 1); ++c) copy_in(c);
+  int gf = 0;  // next group to write out
+  for (int c = 0; c < nchunk; ++c) {
+    const int s = c % SK_NB, b = c & 1;
+    unsigned char *sa = dsm + (size_t)b * 2 * SK_APART;
+    const float2 *sxy = reinterpret_cast<const float2 *>(dsm + oX + (size_t)s * xysz);
+    if (c >= 2) wait_mma(c - 2);  // A buffer b free
+    if (!tc::mbar_wait(tc::smem_addr(&full[s]), (uint32_t)(c / SK_NB) & 1u, TC_POLLS)) ok = false;
+    // A rows 2 cl (T.re) and 2 cl + 1 (T.im): 64 columns x 8 atom quads
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int it = tid + SK_THREADS * k, cl = it >> 3, q = it & 7;
+      const int2 xy = cxy[cl];
+      float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
+      if (xy.x >= 0) {
+        const bool neg = xy.y < 0;
+        const float4 *X = reinterpret_cast<const float4 *>(sxy + xy.x * SK_CH + 4 * q);
+        const float4 *Y =
+            reinterpret_cast<const float4 *>(sxy + (kx + (neg ? -xy.y : xy.y)) * SK_CH + 4 * q);
+        const float4 x01 = X[0], x23 = X[1], y01 = Y[0], y23 = Y[1];
+        const float xr[4] = {x01.x, x01.z, x23.x, x23.z}, xi[4] = {x01.y, x01.w, x23.y, x23.w};
+        const float yr[4] = {y01.x, y01.z, y23.x, y23.z};
+        float yi[4] = {y01.y, y01.w, y23.y, y23.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (neg) yi[u] = -yi[u];
+          re[u] = fmaf(xr[u], yr[u], -xi[u] * yi[u]);
+          im[u] = fmaf(xr[u], yi[u], xi[u] * yr[u]);
+        }
+      }
+      const uint32_t o0 = sk_off(2 * cl, q), o1 = sk_off(2 * cl + 1, q);
+      st_split(sa + o0, sa + SK_APART + o0, re[0], re[1], re[2], re[3]);
+      st_split(sa + o1, sa + SK_APART + o1, im[0], im[1], im[2], im[3]);
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();  // A(c) written; X, Y of chunk c read by everyone
+    if (tid == 0) {
+      tc::fence_after_sync();
+      // stage (c + SK_NB - 1) % SK_NB last held chunk c - 1: its X, Y rows
+      // were read before this barrier, its Z image once MMA(c - 1) is done
+      if (c + SK_NB - 1 < nchunk) {
+        if (c >= 1) wait_mma(c - 1);
+        copy_in(c + SK_NB - 1);
+      }
+      tc::fence_after_sync();
+      const int g = c / SK_GCH, cg = c - g * SK_GCH;
+      const uint32_t d = tbase + (uint32_t)(64 * (g & 1));
+      const uint32_t ah = sbase + (uint32_t)b * 2 * SK_APART, al = ah + SK_APART;
+      const uint32_t bh = sbase + oB + (uint32_t)s * 2 * bpart, bl = bh + bpart;
+      for (int k = 0; k < SK_CH / 8; ++k) {
+        const uint32_t ko = (uint32_t)k * 2 * SK_LBO;  // 8 atoms = two core matrices
+        const uint64_t dah = tc::sdesc(ah + ko, SK_LBO, SK_SBO);
+        const uint64_t dal = tc::sdesc(al + ko, SK_LBO, SK_SBO);
+        const uint64_t dbh = tc::sdesc(bh + ko, SK_LBO, SK_SBO);
+        const uint64_t dbl = tc::sdesc(bl + ko, SK_LBO, SK_SBO);
+        tc::mma_tf32(d, dah, dbh, idesc, (cg > 0 || k > 0) ? 1u : 0u);
+        tc::mma_tf32(d, dah, dbl, idesc, 1u);
+        tc::mma_tf32(d, dal, dbh, idesc, 1u);
+      }
+      tc::mma_commit(tc::smem_addr(&mdone[s]));
+      if (cg == SK_GCH - 1 || c == nchunk - 1) tc::mma_commit(tc::smem_addr(&gdone[g & 1]));
+    }
+    __syncwarp();
+    // the previous group is written out one chunk into the next one (its
+    // region is reused two groups later, after this CTA's barriers)
+    if (c - (c / SK_GCH) * SK_GCH == 1 && gf < c / SK_GCH) flush(gf++);
+  }
+  while (gf < ngroup) flush(gf++);
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tbase, 128);
+  }
+  if (!ok && tid == 0) atomicOr(err, DERR_TIMEOUT);
+}
+
+// S(k) from the partials: thread per (column, p <= m), partials added in
+// FP64 in a fixed order (deterministic).
+__global__ void k_sfac_tc_sum(int ncol, int np, int npart, int ntm, const KCol *__restrict__ cols,
+                              const int *__restrict__ cp0, const float *__restrict__ part,
+                              double2 *__restrict__ sk) {
+  // cp0[c] = first (column, p) item of column c; cp0[ncol] = items
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cp0[ncol]) return;
+  int lo = 0, hi = ncol;  // column of item t: cp0[c] <= t < cp0[c + 1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (cp0[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  const int c = lo, p = t - cp0[c];
+  const int mt = c / (SK_ROWS / 2), r = 2 * (c % (SK_ROWS / 2));
+  double A1 = 0.0, A2 = 0.0, A3 = 0.0, A4 = 0.0;
+  for (int s = 0; s < npart; ++s) {
+    const float *d = part + ((size_t)s * ntm + mt) * SK_ROWS * np;
+    A1 += (double)d[(size_t)r * np + 2 * p];
+    A3 += (double)d[(size_t)r * np + 2 * p + 1];
+    A4 += (double)d[(size_t)(r + 1) * np + 2 * p];
+    A2 += (double)d[(size_t)(r + 1) * np + 2 * p + 1];
+  }
+  const KCol col = cols[c];
+  const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
+  if (kp >= 0) sk[kp] = make_double2(A1 - A2, A3 + A4);
+  if (km >= 0) sk[km] = make_double2(A1 + A2, A4 - A3);
+}
+
+size_t sk_smem_bytes(int np, int kxy) {
+  return 1024 + 4 * (size_t)SK_APART + SK_NB * (2 * (size_t)sk_bpart(np) + (size_t)kxy * SK_CH * 8);
 }
 
 }  // namespace
 
 // Column order and tile table of the tensor-core force pass (host, from the
-// k-set columns).  Returns false when the pass does not apply (K too large
-// for the shared-memory tiles).
+// k-set columns) and its Z image.  Returns false when the pass does not
+// apply (its shared-memory tiles do not fit).
 bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
   DevData &d = ctx->dv;
   const int kp = ((2 * (kmaz + 1) + 7) / 8) * 8;
@@ -295,24 +560,143 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
   ctx_free(ctx, d.tc_slot);
   ctx_free(ctx, d.tc_w);
   ctx_free(ctx, d.tc_meta);
+  ctx_free(ctx, d.tc_zimg);
   d.tc_slot = nullptr;
   d.tc_w = nullptr;
   d.tc_meta = nullptr;
+  d.tc_zimg = nullptr;
+  const size_t zbytes = (size_t)(d.ldn / TC_M) * 1024 * kp;
   if (ctx_alloc(ctx, &d.tc_slot, sizeof(int) * (slot.size() + ks.size())) != cudaSuccess ||
       ctx_alloc(ctx, &d.tc_w, sizeof(float) * (size_t)ntile * 2 * TC_N * kp) != cudaSuccess ||
-      ctx_alloc(ctx, &d.tc_meta, sizeof(float4) * slot.size()) != cudaSuccess)
+      ctx_alloc(ctx, &d.tc_meta, sizeof(float4) * slot.size()) != cudaSuccess ||
+      ctx_alloc(ctx, &d.tc_zimg, zbytes) != cudaSuccess)
     return false;
   d.tc_ks = d.tc_slot + slot.size();
   if (cudaMemcpy(d.tc_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       cudaMemcpy(d.tc_ks, ks.data(), sizeof(int) * ks.size(), cudaMemcpyHostToDevice) !=
-          cudaSuccess)
+          cudaSuccess ||
+      cudaMemset(d.tc_zimg, 0, zbytes) != cudaSuccess)  // K columns past 2 kz stay zero
     return false;
   if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy)) != cudaSuccess) return false;
   d.tc_ntile = ntile;
   d.tc_kp = kp;
   d.tc_on = true;
   return true;
+}
+
+// Tables of the tensor-core S(k) pass: M-tiles, slices (about one wave of one
+// CTA per SM), partial buffer, item offsets, Z image.  Returns false when it
+// does not apply.
+bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
+  DevData &d = ctx->dv;
+  d.tcs_on = false;
+  const int np = ((2 * d.kz + 15) / 16) * 16;
+  const int kxy = d.kx + d.ky;
+  if (np > 64 || sk_smem_bytes(np, kxy) > 227 * 1024) return false;
+  const int ncol = (int)cols.size();
+  const int ntm = (ncol + SK_ROWS / 2 - 1) / (SK_ROWS / 2);
+  int nsm = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return false;
+  int ns = std::max(1, nsm / std::max(1, ntm));
+  int slice = (d.n + ns - 1) / ns;
+  slice = std::max(SK_CH, ((slice + SK_CH - 1) / SK_CH) * SK_CH);
+  ns = (d.n + slice - 1) / slice;
+  const int gps = (slice / SK_CH + SK_GCH - 1) / SK_GCH;  // partials per slice
+  std::vector<int> cp0(ncol + 1, 0);
+  for (int c = 0; c < ncol; ++c) cp0[c + 1] = cp0[c] + cols[c].m + 1;
+  ctx_free(ctx, d.tcs_part);
+  ctx_free(ctx, d.tcs_cp0);
+  ctx_free(ctx, d.tcs_zimg);
+  d.tcs_part = nullptr;
+  d.tcs_cp0 = nullptr;
+  d.tcs_zimg = nullptr;
+  const size_t pbytes = sizeof(float) * (size_t)ns * gps * ntm * SK_ROWS * np;
+  const size_t zbytes = (size_t)(d.ldn / SK_CH) * 2 * sk_bpart(np);
+  if (ctx_alloc(ctx, &d.tcs_part, pbytes) != cudaSuccess ||
+      ctx_alloc(ctx, &d.tcs_cp0, sizeof(int) * cp0.size()) != cudaSuccess ||
+      ctx_alloc(ctx, &d.tcs_zimg, zbytes) != cudaSuccess)
+    return false;
+  if (cudaMemcpy(d.tcs_cp0, cp0.data(), sizeof(int) * cp0.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      // partials past the last slice's atoms are never written: they stay zero;
+      // image rows 2p, 2p + 1 with p >= kz too
+      cudaMemset(d.tcs_part, 0, pbytes) != cudaSuccess ||
+      cudaMemset(d.tcs_zimg, 0, zbytes) != cudaSuccess)
+    return false;
+  if (raise_smem_limit(k_sfac_tc, sk_smem_bytes(np, kxy)) != cudaSuccess) return false;
+  d.tcs_np = np;
+  d.tcs_ntm = ntm;
+  d.tcs_nslice = ns;
+  d.tcs_slice = slice;
+  d.tcs_items = cp0[ncol];
+  d.tcs_gps = gps;
+  d.tcs_on = true;
+  return true;
+}
+
+// Tensor map of the FP32 tables: a [kx + ky + kz][2 ldn] float tensor, box
+// of box_atoms atoms (2 box_atoms floats, 8 to 1024 bytes) x (kx + ky) rows.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static int encode_xy_map(mdx_ctx *ctx, CUtensorMap *m, int box_atoms) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p) {
+      ctx->err = "cuTensorMapEncodeTiled is not available";
+      return MDX_ERR_CUDA;
+    }
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  const DevData &d = ctx->dv;
+  const cuuint64_t dim[2] = {(cuuint64_t)2 * d.ldn, (cuuint64_t)(d.kx + d.ky + d.kz)};
+  const cuuint64_t stride[1] = {(cuuint64_t)2 * d.ldn * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)(2 * box_atoms), (cuuint32_t)(d.kx + d.ky)};
+  const cuuint32_t estr[2] = {1, 1};
+  if (fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, d.tabxf, dim, stride, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+    ctx->err = "cuTensorMapEncodeTiled rejected the phase-table map";
+    return MDX_ERR_CUDA;
+  }
+  return MDX_OK;
+}
+
+// Z images of this step (after the phase tables), for whichever tensor-core
+// pass is on.
+int tc_zimages_launch(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  if (!d.tc_on && !d.tcs_on) return MDX_OK;
+  const size_t nth = (size_t)d.kz * d.ldn;
+  k_zimages<<<(unsigned)((nth + 255) / 256), 256, 0, ctx->stream>>>(
+      d.ldn, d.kz, d.tc_kp, d.tcs_np, d.tabzf, d.tc_on ? d.tc_zimg : nullptr,
+      d.tcs_on ? d.tcs_zimg : nullptr);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int tc_sfac_launch(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  CUtensorMap tm;
+  int rc = encode_xy_map(ctx, &tm, SK_CH);
+  if (rc) return rc;
+  k_sfac_tc<<<dim3(d.tcs_ntm, d.tcs_nslice), SK_THREADS, sk_smem_bytes(d.tcs_np, d.kx + d.ky),
+              ctx->stream>>>(d.n, d.ncol, d.tcs_np, d.tcs_slice, d.tcs_gps, d.cols, tm,
+                             d.tcs_zimg, d.kx, d.ky, d.tcs_part, d.err);
+  MDX_LAUNCHED(ctx);
+  k_sfac_tc_sum<<<(d.tcs_items + 127) / 128, 128, 0, ctx->stream>>>(
+      d.ncol, d.tcs_np, d.tcs_nslice * d.tcs_gps, d.tcs_ntm, d.cols, d.tcs_cp0, d.tcs_part,
+      d.sk);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
 }
 
 // One step's tensor-core force pass: B tiles from W, then the GEMM + fold.
@@ -323,10 +707,13 @@ int tc_force_launch(mdx_ctx *ctx) {
   k_wtiles<<<(nth + 255) / 256, 256, 0, ctx->stream>>>(d.tc_ntile, d.tc_kp, d.tc_slot, d.cols,
                                                        d.wk, d.colrvf, d.tc_w, d.tc_meta);
   MDX_LAUNCHED(ctx);
-  k_rforce_tc<<<(d.n + TC_M - 1) / TC_M, 128, tc_smem_bytes(d.tc_kp, d.kx + d.ky),
-                ctx->stream>>>(d.n, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
-                               reinterpret_cast<const float4 *>(d.tc_w), d.tabxf, d.kx, d.ky,
-                               d.kz, ctx->fix, d.gfix, d.err);
+  CUtensorMap tm;
+  int rc = encode_xy_map(ctx, &tm, TC_M);
+  if (rc) return rc;
+  k_rforce_tc<<<(d.n + TC_M - 1) / TC_M, TC_THREADS, tc_smem_bytes(d.tc_kp, d.kx + d.ky),
+                ctx->stream>>>(d.n, d.ldn, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
+                               reinterpret_cast<const float4 *>(d.tc_w), d.tc_zimg, tm, d.kx,
+                               d.ky, ctx->fix, d.gfix, d.err);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

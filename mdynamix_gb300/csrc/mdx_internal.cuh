@@ -175,6 +175,7 @@ struct DevData {
   // SHAKE (per type: first bond record, bond count)
   // Ewald
   int nkv, ncol, kx, ky, kz;  // table rows: n = 0..KMAX, 0..KMAY, 0..KMAZ
+  int ldn;                      // row stride (atoms) of the FP32 tables, n rounded up to 128
   KCol *cols;
   void *kchunks;                // column chunks of the S(k) kernel
   int nchunk;
@@ -203,7 +204,14 @@ struct DevData {
   int *tc_slot, *tc_ks;
   float *tc_w;
   float4 *tc_meta;  // per slot {nx, ny, rv} for the epilogue
+  unsigned char *tc_zimg;  // Z image (A operand), per 128-atom tile
   int tc_ntile, tc_kp;
+  // mixed tensor-core S(k) pass: slice partials (FP32) and (column, p) items
+  bool tcs_on;
+  float *tcs_part;
+  int *tcs_cp0;
+  unsigned char *tcs_zimg;  // Z image (B operand), per 32-atom chunk
+  int tcs_np, tcs_ntm, tcs_nslice, tcs_slice, tcs_items, tcs_gps;
   int *rf_part;                 // group ranges of the mixed force pass's warps
   int rf_nsplit;                // blocks per atom tile of that pass
   double2 *colrv;               // per column (RXV, RYV) at the current box
@@ -504,6 +512,9 @@ int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
 bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz);
+bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols);
+int tc_sfac_launch(mdx_ctx *ctx);
+int tc_zimages_launch(mdx_ctx *ctx);
 int tc_force_launch(mdx_ctx *ctx);
 // Dynamic shared-memory limit of a kernel: process-wide, shared by every
 // context, so it is only ever raised (under a lock).

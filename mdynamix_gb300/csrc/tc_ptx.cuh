@@ -109,6 +109,19 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst_smem, const void *src, uin
       : "memory");
 }
 
+// Tiled 2-D TMA load of one box of a tensor map (a __grid_constant__ kernel
+// parameter) at element coordinates (x, y) into shared memory, completion
+// reported as transactions on the mbarrier.  x times the element size must
+// be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst_smem, const void *tmap, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst_smem),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
 // D[tmem] (+)= A[smem] x B[smem]^T, M x N x 8 TF32, issued by one thread.
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
                                          uint32_t idesc, uint32_t accumulate) {
