@@ -38,7 +38,6 @@ namespace {
 constexpr int TC_M = 128;          // atoms per CTA of the force pass (MMA M)
 constexpr int TC_N = 128;          // accumulator columns per tile (32 k-columns)
 constexpr int TC_COLS = TC_N / 4;  // k-columns per tile
-constexpr int TC_THREADS = 256;    // force pass: 8 warps, two per lane quarter
 constexpr uint32_t TC_POLLS = 1u << 20;  // bounded mbarrier waits
 
 // Force-pass operand layout: element (row r, k) of a K-major, unswizzled tile
@@ -151,35 +150,48 @@ __global__ void k_wtiles(int ntile, int kp, const int *__restrict__ slot,
   *reinterpret_cast<float4 *>(base + tsz) = lo;
 }
 
-// Force pass: one CTA of 8 warps per 128 atoms.  Shared memory (1024-byte
-// aligned): A hi | A lo (the tile's Z image) | B0 hi | B0 lo | B1 hi | B1 lo |
-// X, Y rows of the CTA's atoms ([row][atom], float2).  Thread 0 issues the
-// bulk copies (A, X, Y once; B one tile ahead of the MMAs) and the MMAs.
-// Warps w and w + 4 read the same accumulator lanes (32 (w % 4) ..) and
-// split each tile's 32 columns between them.  Barriers: abar (A, X, Y
-// landed), bfull[b] (B tile landed in buffer b), mdone[b] (MMAs into
-// accumulator b done, so B buffer b is free again).
+// Force pass: one CTA per 128 atoms, warp-specialised.  Warp 8 (lane 0) is
+// the producer: bulk copies (once: the tile's Z image, its X and Y rows as
+// one TMA box, the epilogue records of all column tiles; then each B tile)
+// and the MMAs.  Warps 0-7 are the epilogue: warps w and w + 4 read the
+// accumulator lanes 32 (w % 4) .. + 31 and split each tile's 32 columns
+// between them.  Shared memory (1024-byte aligned): A hi | A lo | B0 hi |
+// B0 lo | B1 hi | B1 lo | X, Y rows ([row][atom], float2) | records.
+// Barriers: abar (A, X, Y, records landed), bfull[b] (B tile in buffer b
+// landed), mdone[b] (MMAs into accumulator b done: B buffer b free,
+// accumulator b readable), afree[b] (the 8 epilogue warps are done with
+// accumulator b).
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
+constexpr int TC_REC_BYTES = TC_COLS * 16;  // 32 epilogue records of a tile
+
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
-    int n, int ldn, int ntile, int kp, const int *__restrict__ tile_ks,
-    const float4 *__restrict__ meta, const float4 *__restrict__ tw,
-    const unsigned char *__restrict__ zimg, const __grid_constant__ CUtensorMap tmxy, int kx,
-    int ky, FixScale fsc, unsigned long long *__restrict__ gfix, int *__restrict__ err) {
-  // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 TC_M x (kx + ky)
+    int n, int ntile, int kp, const int *__restrict__ tile_ks, const float4 *__restrict__ meta,
+    const unsigned char *__restrict__ tw, const unsigned char *__restrict__ zimg,
+    const __grid_constant__ CUtensorMap tmxy, int kx, int ky, FixScale fsc,
+    unsigned long long *__restrict__ gfix, int *__restrict__ err) {
+  // tw: per tile [B hi | B lo]; meta: per column slot {nx, ny, rv.x, rv.y};
+  // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 TC_M x
+  // (kx + ky)
   extern __shared__ unsigned char dsm_raw[];
-  __shared__ __align__(8) unsigned long long abar, bfull[2], mdone[2];
+  __shared__ __align__(8) unsigned long long abar, bfull[2], mdone[2], afree[2];
   __shared__ uint32_t tmem_base_sh;
   __shared__ float red[6][TC_M];  // second-half partials (sum, compensation)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
   const int i0 = blockIdx.x * TC_M;
   const uint32_t raw = tc::smem_addr(dsm_raw);
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
   unsigned char *dsm = dsm_raw + pad;
   const uint32_t sbase = raw + pad;
-  const uint32_t part = (uint32_t)TC_M * kp * 4;  // bytes of one hi or lo tile
-  const uint32_t sA = sbase, sB = sbase + 2 * part;
-  const float2 *sxy = reinterpret_cast<const float2 *>(dsm + 6 * (size_t)part);  // [kx+ky][128]
+  const uint32_t part = (uint32_t)TC_M * kp * 4;    // bytes of one hi or lo tile
+  const uint32_t btile = 2 * part;               // bytes of one B tile
   const int kxy = kx + ky;
+  const uint32_t sA = sbase, sB = sbase + 2 * part, oXY = 2 * part + 2 * btile;
+  const uint32_t oRec = oXY + (uint32_t)kxy * TC_M * 8;
 
   if (warp == 0) {
     tc::tmem_alloc(tc::smem_addr(&tmem_base_sh), 2 * TC_N);
@@ -190,129 +202,150 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(tc::smem_addr(&bfull[b]), 1);
       tc::mbar_init(tc::smem_addr(&mdone[b]), 1);
+      tc::mbar_init(tc::smem_addr(&afree[b]), TC_EPI_WARPS);
     }
     tc::mbar_init_fence();
   }
-  __syncthreads();  // barriers initialised before any copy arrives on them
-  // B tile t -> buffer b: one bulk copy of both parts (2 part bytes)
-  auto copy_b = [&](int t, int b) {
-    const uint32_t bar = tc::smem_addr(&bfull[b]);
-    tc::mbar_arrive_expect_tx(bar, 2 * part);
-    tc::bulk_g2s(sB + (uint32_t)b * 2 * part, tw + (size_t)t * (2 * part / 16), 2 * part, bar);
-  };
-  if (tid == 0) {
-    const uint32_t bar = tc::smem_addr(&abar);
-    tc::mbar_arrive_expect_tx(bar, 2 * part + (uint32_t)kxy * TC_M * 8);
-    tc::bulk_g2s(sA, zimg + (size_t)blockIdx.x * 2 * part, 2 * part, bar);
-    tc::tma_load_2d(sA + 6 * part, &tmxy, 2 * i0, 0, bar);
-    if (ntile > 0) copy_b(0, 0);
-    if (ntile > 1) copy_b(1, 1);
-  }
-  bool ok = tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS);
-  const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
-  const uint32_t lbo = 128, sbo = 32u * kp;
-  auto issue = [&](int t, int b, uint32_t tbase) {
-    if (!tc::mbar_wait(tc::smem_addr(&bfull[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS)) ok = false;
-    tc::fence_after_sync();
-    const int ks = tile_ks[t];
-    const uint32_t d = tbase + (uint32_t)(b * TC_N);
-    const uint32_t bh = sB + (uint32_t)b * 2 * part, bl = bh + part;
-    for (int s = 0; s < ks; ++s) {
-      const uint32_t ko = (uint32_t)s * 256;  // 8 TF32 = two core matrices along K
-      const uint64_t ah = tc::sdesc(sA + ko, lbo, sbo), al = tc::sdesc(sA + part + ko, lbo, sbo);
-      const uint64_t bhd = tc::sdesc(bh + ko, lbo, sbo), bld = tc::sdesc(bl + ko, lbo, sbo);
-      tc::mma_tf32(d, ah, bhd, idesc, s > 0 ? 1u : 0u);
-      tc::mma_tf32(d, ah, bld, idesc, 1u);
-      tc::mma_tf32(d, al, bhd, idesc, 1u);
-    }
-    tc::mma_commit(tc::smem_addr(&mdone[b]));
-  };
-
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = tmem_base_sh;
-  if (tid == 0 && ntile > 0) issue(0, 0, tbase);
+  bool ok = true;
 
-  const int row = 32 * quarter + lane;  // this thread's atom within the tile
-  const float2 *xa = sxy + row;         // its X, Y rows
-  float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
-  for (int t = 0; t < ntile; ++t) {
-    const int b = t & 1;
-    // MMA(t) done: accumulator b ready, B buffer b free for tile t + 2
-    if (!tc::mbar_wait(tc::smem_addr(&mdone[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS)) ok = false;
-    tc::fence_after_sync();
-    if (tid == 0 && t + 2 < ntile) copy_b(t + 2, b);
-    tc::fence_before_sync();
-    __syncthreads();  // epilogue(t - 1) done: accumulator b ^ 1 free
-    if (tid == 0 && t + 1 < ntile) {
-      tc::fence_after_sync();
-      issue(t + 1, b ^ 1, tbase);
-    }
-    __syncwarp();  // warp 0 converged again before the warp-wide tcgen05.ld
-    // epilogue of tile t: this warp's 2 chunks of 8 columns
-    float gs[3] = {0.f, 0.f, 0.f};
-    for (int h = 2 * half; h < 2 * half + 2; ++h) {
-      float v[32];
-      tc::tmem_ld32(tbase + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * TC_N + 32 * h), v);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float4 mt = __ldg(&meta[t * TC_COLS + 8 * h + j]);  // nx, ny, rv
-        const int nx = __float_as_int(mt.x), nys = __float_as_int(mt.y);
-        if (nx < 0) continue;  // padding slot
-        const float2 X = xa[nx * TC_M];
-        float2 Y = xa[(kx + (nys < 0 ? -nys : nys)) * TC_M];
-        if (nys < 0) Y.y = -Y.y;
-        const float Tr = fmaf(X.x, Y.x, -X.y * Y.y), Ti = fmaf(X.x, Y.y, X.y * Y.x);
-        const float imTU = fmaf(Tr, v[4 * j + 1], Ti * v[4 * j]);
-        const float imTV = fmaf(Tr, v[4 * j + 3], Ti * v[4 * j + 2]);
-        gs[0] = fmaf(mt.z, imTU, gs[0]);
-        gs[1] = fmaf(mt.w, imTU, gs[1]);
-        gs[2] += imTV;
+  if (warp == TC_EPI_WARPS) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      auto copy_b = [&](int t, int b) {
+        const uint32_t bar = tc::smem_addr(&bfull[b]);
+        tc::mbar_arrive_expect_tx(bar, btile);
+        tc::bulk_g2s(sB + (uint32_t)b * btile, tw + (size_t)t * btile, btile, bar);
+      };
+      {
+        const uint32_t bar = tc::smem_addr(&abar);
+        const uint32_t recb = (uint32_t)ntile * TC_REC_BYTES;
+        tc::mbar_arrive_expect_tx(bar, 2 * part + (uint32_t)kxy * TC_M * 8 + recb);
+        tc::bulk_g2s(sA, zimg + (size_t)blockIdx.x * 2 * part, 2 * part, bar);
+        tc::tma_load_2d(sbase + oXY, &tmxy, 2 * i0, 0, bar);
+        if (recb) tc::bulk_g2s(sbase + oRec, meta, recb, bar);
+      }
+      if (ntile > 0) copy_b(0, 0);
+      if (ntile > 1) copy_b(1, 1);
+      if (!tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS)) ok = false;
+      const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
+      const uint32_t lbo = 128, sbo = 32u * kp;
+      for (int t = 0; t < ntile; ++t) {
+        const int b = t & 1;
+        if (!tc::mbar_wait(tc::smem_addr(&bfull[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS))
+          ok = false;
+        if (t >= 2 && !tc::mbar_wait(tc::smem_addr(&afree[b]), (uint32_t)((t - 2) >> 1) & 1u,
+                                      TC_POLLS))
+          ok = false;
+        tc::fence_after_sync();
+        const int ks = tile_ks[t];
+        const uint32_t d = tbase + (uint32_t)(b * TC_N);
+        const uint32_t bh = sB + (uint32_t)b * btile, bl = bh + part;
+        for (int s = 0; s < ks; ++s) {
+          const uint32_t ko = (uint32_t)s * 256;  // 8 TF32 = two core matrices along K
+          const uint64_t ah = tc::sdesc(sA + ko, lbo, sbo);
+          const uint64_t al = tc::sdesc(sA + part + ko, lbo, sbo);
+          const uint64_t bhd = tc::sdesc(bh + ko, lbo, sbo), bld = tc::sdesc(bl + ko, lbo, sbo);
+          tc::mma_tf32(d, ah, bhd, idesc, s > 0 ? 1u : 0u);
+          tc::mma_tf32(d, ah, bld, idesc, 1u);
+          tc::mma_tf32(d, al, bhd, idesc, 1u);
+        }
+        tc::mma_commit(tc::smem_addr(&mdone[b]));
+        // B buffer b ^ 1 (tile t - 1) refilled with tile t + 1 once MMA(t - 1)
+        // is done; MMA(t) runs meanwhile
+        if (t >= 1 && t + 1 < ntile) {
+          if (!tc::mbar_wait(tc::smem_addr(&mdone[b ^ 1]), (uint32_t)((t - 1) >> 1) & 1u,
+                             TC_POLLS))
+            ok = false;
+          copy_b(t + 1, b ^ 1);
+        }
       }
     }
-    tc::fence_before_sync();
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = 32 * quarter + lane;  // this thread's atom within the tile
+    const float2 *xa = reinterpret_cast<const float2 *>(dsm + oXY) + row;  // X, Y rows
+    if (!tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS)) ok = false;
+    float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
+    for (int t = 0; t < ntile; ++t) {
+      const int b = t & 1;
+      if (!tc::mbar_wait(tc::smem_addr(&mdone[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS))
+        ok = false;
+      tc::fence_after_sync();
+      __syncwarp();
+      const float4 *rec = reinterpret_cast<const float4 *>(dsm + oRec) + t * TC_COLS;
+      float gs[3] = {0.f, 0.f, 0.f};
+      for (int h = 2 * half; h < 2 * half + 2; ++h) {
+        float v[32];
+        tc::tmem_ld32(tbase + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * TC_N + 32 * h),
+                      v);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {  // Kahan-compensated sum over tiles
-      const float y = gs[a] - fc[a];
-      const float s = fs[a] + y;
-      fc[a] = (s - fs[a]) - y;
-      fs[a] = s;
+        for (int j = 0; j < 8; ++j) {
+          const float4 mt = rec[8 * h + j];  // nx, ny (int bits), rv
+          const int nx = __float_as_int(mt.x), nys = __float_as_int(mt.y);
+          if (nx < 0) continue;  // padding slot
+          const float2 X = xa[nx * TC_M];
+          float2 Y = xa[(kx + (nys < 0 ? -nys : nys)) * TC_M];
+          if (nys < 0) Y.y = -Y.y;
+          const float Tr = fmaf(X.x, Y.x, -X.y * Y.y), Ti = fmaf(X.x, Y.y, X.y * Y.x);
+          const float imTU = fmaf(Tr, v[4 * j + 1], Ti * v[4 * j]);
+          const float imTV = fmaf(Tr, v[4 * j + 3], Ti * v[4 * j + 2]);
+          gs[0] = fmaf(mt.z, imTU, gs[0]);
+          gs[1] = fmaf(mt.w, imTU, gs[1]);
+          gs[2] += imTV;
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&afree[b]));
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {  // Kahan-compensated sum over tiles
+        const float y = gs[a] - fc[a];
+        const float s = fs[a] + y;
+        fc[a] = (s - fs[a]) - y;
+        fs[a] = s;
+      }
+    }
+    if (half == 1) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        red[a][row] = fs[a];
+        red[3 + a][row] = fc[a];
+      }
+    }
+    __syncwarp();
+    named_sync(1, 32 * TC_EPI_WARPS);  // epilogue warps only: halves meet
+    const int i = i0 + row;
+    if (half == 0 && i < n) {
+      const float sc = fsc.scalef;
+      long long q[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)  // fixed point, integer sums: order independent
+        q[a] = f2ll_rn(fs[a] * sc) - f2ll_rn(fc[a] * sc) + f2ll_rn(red[a][row] * sc) -
+               f2ll_rn(red[3 + a][row] * sc);
+      gfix[i] += (unsigned long long)q[0];
+      gfix[n + i] += (unsigned long long)q[1];
+      gfix[2 * n + i] += (unsigned long long)q[2];
     }
   }
-  if (half == 1) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      red[a][row] = fs[a];
-      red[3 + a][row] = fc[a];
-    }
-  }
-  __syncthreads();  // every tensor-memory read is done; halves meet
+  tc::fence_before_sync();
+  __syncthreads();  // every MMA waited for, every tensor-memory read done
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tbase, 2 * TC_N);
   }
-  if (!ok) {
-    atomicOr(err, DERR_TIMEOUT);
-    return;
-  }
-  const int i = i0 + row;
-  if (half == 0 && i < n) {
-    const float sc = fsc.scalef;
-    long long q[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)  // fixed point, integer sums: order independent
-      q[a] = f2ll_rn(fs[a] * sc) - f2ll_rn(fc[a] * sc) + f2ll_rn(red[a][row] * sc) -
-             f2ll_rn(red[3 + a][row] * sc);
-    gfix[i] += (unsigned long long)q[0];
-    gfix[n + i] += (unsigned long long)q[1];
-    gfix[2 * n + i] += (unsigned long long)q[2];
-  }
+  if (!ok) atomicOr(err, DERR_TIMEOUT);
 }
 
-// Shared memory of the force pass: A, two B buffers, the X and Y rows.
-size_t tc_smem_bytes(int kp, int kxy) {
-  return 1024 + 6 * (size_t)TC_M * kp * 4 + (size_t)kxy * TC_M * sizeof(float2);
+// Shared memory of the force pass: A, two B tiles, X and Y rows, records.
+size_t tc_smem_bytes(int kp, int kxy, int ntile) {
+  return 1024 + 6 * (size_t)TC_M * kp * 4 + (size_t)kxy * TC_M * sizeof(float2) +
+         (size_t)ntile * TC_REC_BYTES;
 }
 
 __device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, float a, float b,
@@ -326,18 +359,22 @@ __device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, f
   *reinterpret_cast<float4 *>(lo) = l;
 }
 
-// S-pass: a CTA (8 warps, one per SM) takes an M-tile of 64 columns (128
-// rows) and a slice of atoms (a multiple of 32), np <= 64.  Per chunk of 32
-// atoms, thread 0 brings in the chunk's X and Y rows and its Z image (the B
-// operand) with bulk copies, SK_NB chunks ahead; all threads form T = X Y for
-// the tile's columns into the A operand (two buffers); thread 0 issues the
-// MMAs.  Tensor memory: two regions of 64 columns; group g of SK_GCH chunks
-// accumulates in region g % 2 and is written out as partial gps * slice + g
-// while group g + 1 runs.  Barriers: full[s] (X, Y rows and Z image of the
-// chunk in stage s landed), mdone[s] (MMAs of the chunk in stage s done),
-// gdone[r] (the group in region r done).
-constexpr int SK_NB = 4;         // copy stages (chunks in flight)
-constexpr int SK_THREADS = 256;  // 512 A items per chunk: 2 per thread
+// S-pass, warp-specialised: a CTA (one per SM) takes an M-tile of 64 columns
+// (128 rows) and a slice of atoms (a multiple of 32), np <= 64.  Warp 8
+// (lane 0) is the producer: per chunk of 32 atoms it brings in the chunk's X
+// and Y rows (one TMA box) and its Z image (the B operand) SK_NB - 1 chunks
+// ahead, and issues the MMAs.  Warps 0-7 form T = X Y for the tile's columns
+// into the A operand (two buffers) and write out the accumulators.  Tensor
+// memory: two regions of 64 columns; group g of SK_GCH chunks accumulates in
+// region g % 2 and is written out as partial gps * slice + g while group
+// g + 1 runs.  Barriers: full[s] (X, Y rows and Z image of the chunk in
+// stage s landed), afull[b] (A of the chunk in buffer b written: 8 warp
+// arrivals), mdone[s] (MMAs of the chunk in stage s done), gdone[r] (the
+// group in region r done), rfree[r] (region r written out: 8 arrivals).
+constexpr int SK_NB = 4;  // copy stages (chunks in flight)
+constexpr int SK_GEN_WARPS = 8;
+constexpr int SK_THREADS = 32 * (SK_GEN_WARPS + 1);
+constexpr int SK_GEN = 32 * SK_GEN_WARPS;  // 512 A items per chunk: 2 per thread
 
 __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
     int n, int ncol, int np, int slice, int gps, const KCol *__restrict__ cols,
@@ -345,7 +382,8 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
     int ky, float *__restrict__ part, int *__restrict__ err) {
   // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 SK_CH x (kx + ky)
   extern __shared__ unsigned char dsm_raw[];
-  __shared__ __align__(8) unsigned long long full[SK_NB], mdone[SK_NB], gdone[2];
+  __shared__ __align__(8) unsigned long long full[SK_NB], mdone[SK_NB], afull[2], gdone[2],
+      rfree[2];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int2 cxy[SK_ROWS / 2];  // (nx, ny) of the tile's columns (nx < 0: none)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -369,8 +407,11 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
       tc::mbar_init(tc::smem_addr(&full[s]), 1);
       tc::mbar_init(tc::smem_addr(&mdone[s]), 1);
     }
-    tc::mbar_init(tc::smem_addr(&gdone[0]), 1);
-    tc::mbar_init(tc::smem_addr(&gdone[1]), 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(tc::smem_addr(&afull[b]), SK_GEN_WARPS);
+      tc::mbar_init(tc::smem_addr(&gdone[b]), 1);
+      tc::mbar_init(tc::smem_addr(&rfree[b]), SK_GEN_WARPS);
+    }
     tc::mbar_init_fence();
   }
   if (tid < SK_ROWS / 2) {
@@ -383,122 +424,129 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = tmem_base_sh;
-  const uint32_t idesc = tc::idesc_tf32(SK_ROWS, np);
   const int nchunk = (a1 - a0 + SK_CH - 1) / SK_CH;
   const int ngroup = (nchunk + SK_GCH - 1) / SK_GCH;
   bool ok = true;
-  // X, Y rows and Z image of chunk c into stage c % SK_NB (thread 0)
-  auto copy_in = [&](int c) {
-    const int s = c % SK_NB;
-    const uint32_t bar = tc::smem_addr(&full[s]);
-    const int j0 = a0 + c * SK_CH;
-    tc::mbar_arrive_expect_tx(bar, xysz + 2 * bpart);
-    tc::tma_load_2d(sbase + oX + (uint32_t)s * xysz, &tmxy, 2 * j0, 0, bar);
-    tc::bulk_g2s(sbase + oB + (uint32_t)s * 2 * bpart,
-                 zimg + (size_t)(a0 / SK_CH + c) * 2 * bpart, 2 * bpart, bar);
-  };
-  auto wait_mma = [&](int c) {  // MMAs of chunk c done
-    if (!tc::mbar_wait(tc::smem_addr(&mdone[c % SK_NB]), (uint32_t)(c / SK_NB) & 1u, TC_POLLS))
-      ok = false;
-  };
-  // write out the accumulator of group g (region g % 2) as partial
-  // gps * blockIdx.y + g: D row 32 (warp % 4) + lane, np columns; warps
-  // w and w + 4 take halves of the columns
-  auto flush = [&](int g) {
-    if (!tc::mbar_wait(tc::smem_addr(&gdone[g & 1]), (uint32_t)(g >> 1) & 1u, TC_POLLS))
-      ok = false;
-    tc::fence_after_sync();
-    __syncwarp();
-    const int q4 = warp & 3, hh = warp >> 2;
-    const int row = 32 * q4 + lane;
-    float *dst = part + (((size_t)(gps * blockIdx.y + g) * ntm + mt) * SK_ROWS + row) * np;
-    const int h = 32 * hh;  // np <= 64: columns [0, 32) and [32, 64)
-    if (h < np) {
-      float v[32];
-      tc::tmem_ld32(tbase + ((uint32_t)(32 * q4) << 16) + (uint32_t)(64 * (g & 1) + h), v);
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (h + j < np) dst[h + j] = v[j];
-    }
-    tc::fence_before_sync();
+  auto wait = [&](unsigned long long &bar, int phase) {
+    if (!tc::mbar_wait(tc::smem_addr(&bar), (uint32_t)phase & 1u, TC_POLLS)) ok = false;
   };
 
-  if (tid == 0)
-    for (int c = 0; c < min(nchunk, SK_NB - 1); ++c) copy_in(c);
-  int gf = 0;  // next group to write out
-  for (int c = 0; c < nchunk; ++c) {
-    const int s = c % SK_NB, b = c & 1;
-    unsigned char *sa = dsm + (size_t)b * 2 * SK_APART;
-    const float2 *sxy = reinterpret_cast<const float2 *>(dsm + oX + (size_t)s * xysz);
-    if (c >= 2) wait_mma(c - 2);  // A buffer b free
-    if (!tc::mbar_wait(tc::smem_addr(&full[s]), (uint32_t)(c / SK_NB) & 1u, TC_POLLS)) ok = false;
-    // A rows 2 cl (T.re) and 2 cl + 1 (T.im): 64 columns x 8 atom quads
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int it = tid + SK_THREADS * k, cl = it >> 3, q = it & 7;
-      const int2 xy = cxy[cl];
-      float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
-      if (xy.x >= 0) {
-        const bool neg = xy.y < 0;
-        const float4 *X = reinterpret_cast<const float4 *>(sxy + xy.x * SK_CH + 4 * q);
-        const float4 *Y =
-            reinterpret_cast<const float4 *>(sxy + (kx + (neg ? -xy.y : xy.y)) * SK_CH + 4 * q);
-        const float4 x01 = X[0], x23 = X[1], y01 = Y[0], y23 = Y[1];
-        const float xr[4] = {x01.x, x01.z, x23.x, x23.z}, xi[4] = {x01.y, x01.w, x23.y, x23.w};
-        const float yr[4] = {y01.x, y01.z, y23.x, y23.z};
-        float yi[4] = {y01.y, y01.w, y23.y, y23.w};
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          if (neg) yi[u] = -yi[u];
-          re[u] = fmaf(xr[u], yr[u], -xi[u] * yi[u]);
-          im[u] = fmaf(xr[u], yi[u], xi[u] * yr[u]);
+  if (warp == SK_GEN_WARPS) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      auto copy_in = [&](int c) {  // X, Y rows and Z image of chunk c -> stage c % SK_NB
+        const int s = c % SK_NB;
+        const uint32_t bar = tc::smem_addr(&full[s]);
+        tc::mbar_arrive_expect_tx(bar, xysz + 2 * bpart);
+        tc::tma_load_2d(sbase + oX + (uint32_t)s * xysz, &tmxy, 2 * (a0 + c * SK_CH), 0, bar);
+        tc::bulk_g2s(sbase + oB + (uint32_t)s * 2 * bpart,
+                     zimg + (size_t)(a0 / SK_CH + c) * 2 * bpart, 2 * bpart, bar);
+      };
+      for (int c = 0; c < min(nchunk, SK_NB - 1); ++c) copy_in(c);
+      const uint32_t idesc = tc::idesc_tf32(SK_ROWS, np);
+      for (int c = 0; c < nchunk; ++c) {
+        const int s = c % SK_NB, b = c & 1;
+        const int g = c / SK_GCH, cg = c - g * SK_GCH;
+        wait(afull[b], c >> 1);  // A(c) written (and X, Y of chunk c read)
+        wait(full[s], c / SK_NB);
+        if (cg == 0 && g >= 2) wait(rfree[g & 1], (g - 2) >> 1);  // region written out
+        tc::fence_after_sync();
+        const uint32_t d = tbase + (uint32_t)(64 * (g & 1));
+        const uint32_t ah = sbase + (uint32_t)b * 2 * SK_APART, al = ah + SK_APART;
+        const uint32_t bh = sbase + oB + (uint32_t)s * 2 * bpart, bl = bh + bpart;
+        for (int k = 0; k < SK_CH / 8; ++k) {
+          const uint32_t ko = (uint32_t)k * 2 * SK_LBO;  // 8 atoms = two core matrices
+          const uint64_t dah = tc::sdesc(ah + ko, SK_LBO, SK_SBO);
+          const uint64_t dal = tc::sdesc(al + ko, SK_LBO, SK_SBO);
+          const uint64_t dbh = tc::sdesc(bh + ko, SK_LBO, SK_SBO);
+          const uint64_t dbl = tc::sdesc(bl + ko, SK_LBO, SK_SBO);
+          tc::mma_tf32(d, dah, dbh, idesc, (cg > 0 || k > 0) ? 1u : 0u);
+          tc::mma_tf32(d, dah, dbl, idesc, 1u);
+          tc::mma_tf32(d, dal, dbh, idesc, 1u);
+        }
+        tc::mma_commit(tc::smem_addr(&mdone[s]));
+        if (cg == SK_GCH - 1 || c == nchunk - 1) tc::mma_commit(tc::smem_addr(&gdone[g & 1]));
+        // stage of chunk c - 1 refilled with chunk c + SK_NB - 1: its X, Y
+        // rows were read (afull), its Z image once MMA(c - 1) is done
+        if (c + SK_NB - 1 < nchunk) {
+          if (c >= 1) wait(mdone[(c - 1) % SK_NB], (c - 1) / SK_NB);
+          copy_in(c + SK_NB - 1);
         }
       }
-      const uint32_t o0 = sk_off(2 * cl, q), o1 = sk_off(2 * cl + 1, q);
-      st_split(sa + o0, sa + SK_APART + o0, re[0], re[1], re[2], re[3]);
-      st_split(sa + o1, sa + SK_APART + o1, im[0], im[1], im[2], im[3]);
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();  // A(c) written; X, Y of chunk c read by everyone
-    if (tid == 0) {
-      tc::fence_after_sync();
-      // stage (c + SK_NB - 1) % SK_NB last held chunk c - 1: its X, Y rows
-      // were read before this barrier, its Z image once MMA(c - 1) is done
-      if (c + SK_NB - 1 < nchunk) {
-        if (c >= 1) wait_mma(c - 1);
-        copy_in(c + SK_NB - 1);
-      }
-      tc::fence_after_sync();
-      const int g = c / SK_GCH, cg = c - g * SK_GCH;
-      const uint32_t d = tbase + (uint32_t)(64 * (g & 1));
-      const uint32_t ah = sbase + (uint32_t)b * 2 * SK_APART, al = ah + SK_APART;
-      const uint32_t bh = sbase + oB + (uint32_t)s * 2 * bpart, bl = bh + bpart;
-      for (int k = 0; k < SK_CH / 8; ++k) {
-        const uint32_t ko = (uint32_t)k * 2 * SK_LBO;  // 8 atoms = two core matrices
-        const uint64_t dah = tc::sdesc(ah + ko, SK_LBO, SK_SBO);
-        const uint64_t dal = tc::sdesc(al + ko, SK_LBO, SK_SBO);
-        const uint64_t dbh = tc::sdesc(bh + ko, SK_LBO, SK_SBO);
-        const uint64_t dbl = tc::sdesc(bl + ko, SK_LBO, SK_SBO);
-        tc::mma_tf32(d, dah, dbh, idesc, (cg > 0 || k > 0) ? 1u : 0u);
-        tc::mma_tf32(d, dah, dbl, idesc, 1u);
-        tc::mma_tf32(d, dal, dbh, idesc, 1u);
-      }
-      tc::mma_commit(tc::smem_addr(&mdone[s]));
-      if (cg == SK_GCH - 1 || c == nchunk - 1) tc::mma_commit(tc::smem_addr(&gdone[g & 1]));
     }
     __syncwarp();
-    // the previous group is written out one chunk into the next one (its
-    // region is reused two groups later, after this CTA's barriers)
-    if (c - (c / SK_GCH) * SK_GCH == 1 && gf < c / SK_GCH) flush(gf++);
+  } else {
+    // ------------------------------------------------------------ generators
+    // write out the accumulator of group g (region g % 2) as partial
+    // gps * blockIdx.y + g: D row 32 (warp % 4) + lane; warps w and w + 4
+    // take columns [0, 32) and [32, 64) (np <= 64)
+    auto flush = [&](int g) {
+      wait(gdone[g & 1], g >> 1);
+      tc::fence_after_sync();
+      __syncwarp();
+      const int q4 = warp & 3, h = 32 * (warp >> 2);
+      const int row = 32 * q4 + lane;
+      float *dst = part + (((size_t)(gps * blockIdx.y + g) * ntm + mt) * SK_ROWS + row) * np;
+      if (h < np) {
+        float v[32];
+        tc::tmem_ld32(tbase + ((uint32_t)(32 * q4) << 16) + (uint32_t)(64 * (g & 1) + h), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (h + j < np) dst[h + j] = v[j];
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&rfree[g & 1]));
+    };
+    int gf = 0;  // next group to write out
+    for (int c = 0; c < nchunk; ++c) {
+      const int s = c % SK_NB, b = c & 1;
+      unsigned char *sa = dsm + (size_t)b * 2 * SK_APART;
+      const float2 *sxy = reinterpret_cast<const float2 *>(dsm + oX + (size_t)s * xysz);
+      if (c >= 2) wait(mdone[(c - 2) % SK_NB], (c - 2) / SK_NB);  // A buffer b free
+      wait(full[s], c / SK_NB);
+      // A rows 2 cl (T.re) and 2 cl + 1 (T.im): 64 columns x 8 atom quads
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int it = tid + SK_GEN * k, cl = it >> 3, q = it & 7;
+        const int2 xy = cxy[cl];
+        float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
+        if (xy.x >= 0) {
+          const bool neg = xy.y < 0;
+          const float4 *X = reinterpret_cast<const float4 *>(sxy + xy.x * SK_CH + 4 * q);
+          const float4 *Y =
+              reinterpret_cast<const float4 *>(sxy + (kx + (neg ? -xy.y : xy.y)) * SK_CH + 4 * q);
+          const float4 x01 = X[0], x23 = X[1], y01 = Y[0], y23 = Y[1];
+          const float xr[4] = {x01.x, x01.z, x23.x, x23.z};
+          const float xi[4] = {x01.y, x01.w, x23.y, x23.w};
+          const float yr[4] = {y01.x, y01.z, y23.x, y23.z};
+          float yi[4] = {y01.y, y01.w, y23.y, y23.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (neg) yi[u] = -yi[u];
+            re[u] = fmaf(xr[u], yr[u], -xi[u] * yi[u]);
+            im[u] = fmaf(xr[u], yi[u], xi[u] * yr[u]);
+          }
+        }
+        const uint32_t o0 = sk_off(2 * cl, q), o1 = sk_off(2 * cl + 1, q);
+        st_split(sa + o0, sa + SK_APART + o0, re[0], re[1], re[2], re[3]);
+        st_split(sa + o1, sa + SK_APART + o1, im[0], im[1], im[2], im[3]);
+      }
+      tc::fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&afull[b]));
+      // the previous group is written out one chunk into the next one
+      if (c - (c / SK_GCH) * SK_GCH == 1 && gf < c / SK_GCH) flush(gf++);
+    }
+    while (gf < ngroup) flush(gf++);
   }
-  while (gf < ngroup) flush(gf++);
-  __syncthreads();
+  tc::fence_before_sync();
+  __syncthreads();  // every MMA waited for, every tensor-memory read done
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tbase, 128);
   }
-  if (!ok && tid == 0) atomicOr(err, DERR_TIMEOUT);
+  if (!ok) atomicOr(err, DERR_TIMEOUT);
 }
 
 // S(k) from the partials: thread per (column, p <= m), partials added in
@@ -545,12 +593,12 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
   const int kp = ((2 * (kmaz + 1) + 7) / 8) * 8;
   d.tc_on = false;
   const int kxy = d.kx + d.ky;
-  if (tc_smem_bytes(kp, kxy) > 227 * 1024) return false;
+  const int ntile = ((int)cols.size() + TC_COLS - 1) / TC_COLS;
+  if (tc_smem_bytes(kp, kxy, ntile) > 227 * 1024) return false;
   std::vector<int> order(cols.size());
   for (size_t c = 0; c < cols.size(); ++c) order[c] = (int)c;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return cols[a].m > cols[b].m; });
-  const int ntile = ((int)cols.size() + TC_COLS - 1) / TC_COLS;
   std::vector<int> slot((size_t)ntile * TC_COLS, -1), ks(ntile, 0);
   for (size_t s = 0; s < order.size(); ++s) slot[s] = order[s];
   for (int t = 0; t < ntile; ++t) {
@@ -578,7 +626,7 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
           cudaSuccess ||
       cudaMemset(d.tc_zimg, 0, zbytes) != cudaSuccess)  // K columns past 2 kz stay zero
     return false;
-  if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy)) != cudaSuccess) return false;
+  if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy, ntile)) != cudaSuccess) return false;
   d.tc_ntile = ntile;
   d.tc_kp = kp;
   d.tc_on = true;
@@ -710,10 +758,11 @@ int tc_force_launch(mdx_ctx *ctx) {
   CUtensorMap tm;
   int rc = encode_xy_map(ctx, &tm, TC_M);
   if (rc) return rc;
-  k_rforce_tc<<<(d.n + TC_M - 1) / TC_M, TC_THREADS, tc_smem_bytes(d.tc_kp, d.kx + d.ky),
-                ctx->stream>>>(d.n, d.ldn, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
-                               reinterpret_cast<const float4 *>(d.tc_w), d.tc_zimg, tm, d.kx,
-                               d.ky, ctx->fix, d.gfix, d.err);
+  k_rforce_tc<<<(d.n + TC_M - 1) / TC_M, TC_THREADS,
+                tc_smem_bytes(d.tc_kp, d.kx + d.ky, d.tc_ntile), ctx->stream>>>(
+      d.n, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
+      reinterpret_cast<const unsigned char *>(d.tc_w), d.tc_zimg, tm, d.kx, d.ky, ctx->fix,
+      d.gfix, d.err);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
