@@ -49,16 +49,19 @@ OPS_EW_COL = 23          # per (column, atom): X Y twice, Im(T U), Im(T V), F
 OPS_EW_ROW = 8           # per (phase-table row, atom): recurrence step + charge
 OPS_EW_K = 20            # per k-vector (energy, virial, W)
 
-# DRAM bytes per long step of the dominant group, from ncu captures of
+# DRAM bytes per long step of each group, from ncu captures of
 # `python bench.py --only {fp64,mixed} --steps 2 --warmup 3`
 # (dram__bytes_read.sum + dram__bytes_write.sum of every launch of the
-# group's kernels in one long step).  None where not captured.
-# fp64 ewald: k_tables 76.2 + k_sfac 165.5 + k_sfac_sum 51.3 + k_kterms 0.4
-#             + k_rforce64 133.4;  mixed: 8.2 + 68.7 + 24.3 + 0.4 + 71.1
-# fp64 pair: 10 x 30.7 (short) + 153.1 (long); mixed: 10 x 36.4 + 280.9
+# group's kernels in one long step, MB).
+# fp64 ewald: k_tables 43.4 + k_sfac 125.8 + k_sfac_sum 51.3 + k_kterms 0.3
+#             + k_wpairs 0.6 + k_rforce64 102.9
+# mixed ewald: k_tables 3.2 + k_zimages 62.7 + k_sfac_tc 78.3 + partial sums 22.9
+#              + k_kterms 0.3 + k_wtiles 0.6 + k_rforce_tc 75.8
+# fp64 pair: 9 x 30.7 (short, forces) + 30.7 (short, energies) + 152.9 (long)
+# mixed pair: 9 x 24.3 + 24.3 + 278.8
 TRAFFIC_MB = {
-    ("fp64", "ewald"): 426.8, ("mixed", "ewald"): 172.7,
-    ("fp64", "pair"): 460.4, ("mixed", "pair"): 644.6,
+    ("fp64", "ewald"): 324.3, ("mixed", "ewald"): 243.8,
+    ("fp64", "pair"): 460.7, ("mixed", "pair"): 522.0,
 }
 
 
@@ -131,11 +134,13 @@ def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps
     step; peak = measured FMA throughput of the pipe the path computes on."""
     ms = {k: v[0] / nsteps for k, v in timers.items()}
     nkv, ncol, npair, rows = kset
+    ew_kernels = ("k_tables + k_zimages + k_sfac_tc + partial sums + k_kterms + k_wtiles + "
+                  "k_rforce_tc (TF32 tensor cores)" if prec == "mixed" else
+                  "k_tables + k_sfac + k_sfac_sum + k_kterms + k_wpairs + k_rforce64")
     groups = {
         "ewald": (ms["ew_tables"] + ms["ew_sfac"] + ms["ew_kterms"] + ms["ew_force"],
                   (OPS_EW_PAIR * npair + OPS_EW_COL * ncol + OPS_EW_ROW * rows) * n
-                  + OPS_EW_K * nkv,
-                  "k_tables + k_sfac + k_sfac_sum + k_kterms + k_rforce"),
+                  + OPS_EW_K * nkv, ew_kernels),
         "pair": (ms["pair_short"] + ms["pair_long"], OPS_PAIR * (nfreq * mbsh + mbln),
                  "k_pair (short list x NFREQ, long list x 1)"),
     }
@@ -145,11 +150,15 @@ def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps
     peak = peak64 if prec == "fp64" else peak32
     tr = TRAFFIC_MB.get((prec, top))
     share = t_ms / sum(ms.values())
+    other = {g: {"ms_per_long_step": v[0], "ops_per_long_step": v[1],
+                 "achieved_tflops": v[1] / (v[0] * 1e-3) / 1e12,
+                 "traffic": (TRAFFIC_MB.get((prec, g)) or 0) * 1e6, "kernels": v[2]}
+             for g, v in groups.items()}
     return {"bound": "fp64" if prec == "fp64" else "fp32", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "traffic": tr * 1e6 if tr is not None else None,
             "kernel": f"{top}: {kernels}", "ms_per_long_step": t_ms, "share_of_step": share,
-            "ops_per_long_step": ops,
+            "ops_per_long_step": ops, "groups": other,
             "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak, of measured)"}
 
 

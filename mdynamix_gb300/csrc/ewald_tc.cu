@@ -153,15 +153,15 @@ __global__ void k_wtiles(int ntile, int kp, const int *__restrict__ slot,
 // Force pass: one CTA per 128 atoms, warp-specialised.  Warp 8 (lane 0) is
 // the producer: bulk copies (once: the tile's Z image, its X and Y rows as
 // one TMA box, the epilogue records of all column tiles; then each B tile)
-// and the MMAs.  Warps 0-7 are the epilogue: warps w and w + 4 read the
-// accumulator lanes 32 (w % 4) .. + 31 and split each tile's 32 columns
-// between them.  Shared memory (1024-byte aligned): A hi | A lo | B0 hi |
+// and the MMAs.  Warps 0-15 are the epilogue: warp w reads the accumulator
+// lanes 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31 of each tile (8 of
+// its k-columns).  Shared memory (1024-byte aligned): A hi | A lo | B0 hi |
 // B0 lo | B1 hi | B1 lo | X, Y rows ([row][atom], float2) | records.
 // Barriers: abar (A, X, Y, records landed), bfull[b] (B tile in buffer b
 // landed), mdone[b] (MMAs into accumulator b done: B buffer b free,
-// accumulator b readable), afree[b] (the 8 epilogue warps are done with
+// accumulator b readable), afree[b] (the 16 epilogue warps are done with
 // accumulator b).
-constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_EPI_WARPS = 16;
 constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
 constexpr int TC_REC_BYTES = TC_COLS * 16;  // 32 epilogue records of a tile
 
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
   extern __shared__ unsigned char dsm_raw[];
   __shared__ __align__(8) unsigned long long abar, bfull[2], mdone[2], afree[2];
   __shared__ uint32_t tmem_base_sh;
-  __shared__ float red[6][TC_M];  // second-half partials (sum, compensation)
+  __shared__ float red[3][6][TC_M];  // partials of column quarters 1-3 (sum, compensation)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = blockIdx.x * TC_M;
   const uint32_t raw = tc::smem_addr(dsm_raw);
@@ -267,8 +267,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
-    const int quarter = warp & 3, half = warp >> 2;
-    const int row = 32 * quarter + lane;  // this thread's atom within the tile
+    const int quarter = warp & 3, h = warp >> 2;  // lane quarter, column chunk
+    const int row = 32 * quarter + lane;          // this thread's atom within the tile
     const float2 *xa = reinterpret_cast<const float2 *>(dsm + oXY) + row;  // X, Y rows
     if (!tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS)) ok = false;
     float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
       __syncwarp();
       const float4 *rec = reinterpret_cast<const float4 *>(dsm + oRec) + t * TC_COLS;
       float gs[3] = {0.f, 0.f, 0.f};
-      for (int h = 2 * half; h < 2 * half + 2; ++h) {
+      {
         float v[32];
         tc::tmem_ld32(tbase + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * TC_N + 32 * h),
                       v);
@@ -311,23 +311,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
         fs[a] = s;
       }
     }
-    if (half == 1) {
+    if (h > 0) {
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        red[a][row] = fs[a];
-        red[3 + a][row] = fc[a];
+        red[h - 1][a][row] = fs[a];
+        red[h - 1][3 + a][row] = fc[a];
       }
     }
     __syncwarp();
-    named_sync(1, 32 * TC_EPI_WARPS);  // epilogue warps only: halves meet
+    named_sync(1, 32 * TC_EPI_WARPS);  // epilogue warps only: column quarters meet
     const int i = i0 + row;
-    if (half == 0 && i < n) {
+    if (h == 0 && i < n) {
       const float sc = fsc.scalef;
       long long q[3];
 #pragma unroll
-      for (int a = 0; a < 3; ++a)  // fixed point, integer sums: order independent
-        q[a] = f2ll_rn(fs[a] * sc) - f2ll_rn(fc[a] * sc) + f2ll_rn(red[a][row] * sc) -
-               f2ll_rn(red[3 + a][row] * sc);
+      for (int a = 0; a < 3; ++a) {  // fixed point, integer sums: order independent
+        q[a] = f2ll_rn(fs[a] * sc) - f2ll_rn(fc[a] * sc);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          q[a] += f2ll_rn(red[k][a][row] * sc) - f2ll_rn(red[k][3 + a][row] * sc);
+      }
       gfix[i] += (unsigned long long)q[0];
       gfix[n + i] += (unsigned long long)q[1];
       gfix[2 * n + i] += (unsigned long long)q[2];
@@ -351,43 +354,49 @@ size_t tc_smem_bytes(int kp, int kxy, int ntile) {
 __device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, float a, float b,
                                          float c, float d) {
   float4 h, l;
-  tc::tf32_split(a, h.x, l.x);
-  tc::tf32_split(b, h.y, l.y);
-  tc::tf32_split(c, h.z, l.z);
-  tc::tf32_split(d, h.w, l.w);
+  tc::tf32_split_fast(a, h.x, l.x);
+  tc::tf32_split_fast(b, h.y, l.y);
+  tc::tf32_split_fast(c, h.z, l.z);
+  tc::tf32_split_fast(d, h.w, l.w);
   *reinterpret_cast<float4 *>(hi) = h;
   *reinterpret_cast<float4 *>(lo) = l;
 }
 
-// S-pass, warp-specialised: a CTA (one per SM) takes an M-tile of 64 columns
-// (128 rows) and a slice of atoms (a multiple of 32), np <= 64.  Warp 8
-// (lane 0) is the producer: per chunk of 32 atoms it brings in the chunk's X
-// and Y rows (one TMA box) and its Z image (the B operand) SK_NB - 1 chunks
-// ahead, and issues the MMAs.  Warps 0-7 form T = X Y for the tile's columns
-// into the A operand (two buffers) and write out the accumulators.  Tensor
-// memory: two regions of 64 columns; group g of SK_GCH chunks accumulates in
-// region g % 2 and is written out as partial gps * slice + g while group
-// g + 1 runs.  Barriers: full[s] (X, Y rows and Z image of the chunk in
-// stage s landed), afull[b] (A of the chunk in buffer b written: 8 warp
-// arrivals), mdone[s] (MMAs of the chunk in stage s done), gdone[r] (the
-// group in region r done), rfree[r] (region r written out: 8 arrivals).
+// S-pass, warp-specialised: a CTA (one per SM) takes MT <= 4 M-tiles of 64
+// columns (128 rows each) and a slice of atoms (a multiple of 32), np <= 64.
+// Warp 16 (lane 0) is the producer: per chunk of 32 atoms it brings in the
+// chunk's X and Y rows (one TMA box) and its Z image (the B operand, shared
+// by the MT tiles) SK_NB - 1 chunks ahead, and issues the MMAs.  Warps 0-15
+// form T = X Y for one tile's columns at a time (a job = (chunk, tile)) into
+// the A operand (two buffers) and write out the accumulators.  Tensor
+// memory: two regions of 256 columns, tile m at column 64 m of a region;
+// group g of SK_GCH chunks accumulates in region g % 2 and is written out as
+// partial gps * slice + g while group g + 1 runs.  Barriers: full[s] (X, Y
+// rows and Z image of the chunk in stage s landed), afull[b] (A of the job
+// in buffer b written: 16 warp arrivals), adone[b] (MMAs of that job done),
+// sdone[s] (MMAs of the chunk in stage s done), gdone[r] (the group in
+// region r done), rfree[r] (region r written out: 16 arrivals).
 constexpr int SK_NB = 4;  // copy stages (chunks in flight)
-constexpr int SK_GEN_WARPS = 8;
+constexpr int SK_MT = 4;  // M-tiles per CTA at most
+constexpr int SK_GEN_WARPS = 16;
 constexpr int SK_THREADS = 32 * (SK_GEN_WARPS + 1);
-constexpr int SK_GEN = 32 * SK_GEN_WARPS;  // 512 A items per chunk: 2 per thread
+constexpr int SK_GEN = 32 * SK_GEN_WARPS;  // 512 A items per job: 1 per thread
+static_assert(SK_GEN == (SK_ROWS / 2) * (SK_CH / 4), "one A item per generator thread");
 
 __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
-    int n, int ncol, int np, int slice, int gps, const KCol *__restrict__ cols,
+    int n, int ncol, int ntm, int np, int slice, int gps, const KCol *__restrict__ cols,
     const __grid_constant__ CUtensorMap tmxy, const unsigned char *__restrict__ zimg, int kx,
     int ky, float *__restrict__ part, int *__restrict__ err) {
   // tmxy: the FP32 tables as a [row][2 ldn] float tensor, box 2 SK_CH x (kx + ky)
   extern __shared__ unsigned char dsm_raw[];
-  __shared__ __align__(8) unsigned long long full[SK_NB], mdone[SK_NB], afull[2], gdone[2],
-      rfree[2];
+  __shared__ __align__(8) unsigned long long full[SK_NB], sdone[SK_NB], afull[2], adone[2],
+      gdone[2], rfree[2];
   __shared__ uint32_t tmem_base_sh;
-  __shared__ int2 cxy[SK_ROWS / 2];  // (nx, ny) of the tile's columns (nx < 0: none)
+  __shared__ int2 cxy[SK_MT][SK_ROWS / 2];  // (nx, ny) of the tiles' columns (nx < 0: none)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int mt = blockIdx.x, ntm = gridDim.x;
+  // this CTA's tiles [mt0, mt0 + MT): the ntm tiles spread evenly over gridDim.x
+  const int mt0 = (int)((long long)blockIdx.x * ntm / gridDim.x);
+  const int MT = (int)((long long)(blockIdx.x + 1) * ntm / gridDim.x) - mt0;
   const int a0 = blockIdx.y * slice, a1 = min(n, a0 + slice);
   const uint32_t raw = tc::smem_addr(dsm_raw);
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
@@ -399,26 +408,27 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
   // A0 (hi, lo) | A1 (hi, lo) | SK_NB x B (hi, lo) | SK_NB x X, Y rows [kxy][32]
   const uint32_t oB = 4 * SK_APART, oX = oB + SK_NB * 2 * bpart;
   if (warp == 0) {
-    tc::tmem_alloc(tc::smem_addr(&tmem_base_sh), 128);
+    tc::tmem_alloc(tc::smem_addr(&tmem_base_sh), 512);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
     for (int s = 0; s < SK_NB; ++s) {
       tc::mbar_init(tc::smem_addr(&full[s]), 1);
-      tc::mbar_init(tc::smem_addr(&mdone[s]), 1);
+      tc::mbar_init(tc::smem_addr(&sdone[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(tc::smem_addr(&afull[b]), SK_GEN_WARPS);
+      tc::mbar_init(tc::smem_addr(&adone[b]), 1);
       tc::mbar_init(tc::smem_addr(&gdone[b]), 1);
       tc::mbar_init(tc::smem_addr(&rfree[b]), SK_GEN_WARPS);
     }
     tc::mbar_init_fence();
   }
-  if (tid < SK_ROWS / 2) {
-    const int c = mt * (SK_ROWS / 2) + tid;
+  for (int k = tid; k < SK_MT * (SK_ROWS / 2); k += blockDim.x) {
+    const int m = k / (SK_ROWS / 2), c = (mt0 + m) * (SK_ROWS / 2) + k % (SK_ROWS / 2);
     int2 v = make_int2(-1, 0);
-    if (c < ncol) v = make_int2(cols[c].nx, cols[c].ny);
-    cxy[tid] = v;
+    if (m < MT && c < ncol) v = make_int2(cols[c].nx, cols[c].ny);
+    cxy[m][k % (SK_ROWS / 2)] = v;
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -433,6 +443,7 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
 
   if (warp == SK_GEN_WARPS) {
     // ------------------------------------------------------------ producer
+    // (the warp's other lanes wait at the closing barrier)
     if (lane == 0) {
       auto copy_in = [&](int c) {  // X, Y rows and Z image of chunk c -> stage c % SK_NB
         const int s = c % SK_NB;
@@ -445,31 +456,36 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
       for (int c = 0; c < min(nchunk, SK_NB - 1); ++c) copy_in(c);
       const uint32_t idesc = tc::idesc_tf32(SK_ROWS, np);
       for (int c = 0; c < nchunk; ++c) {
-        const int s = c % SK_NB, b = c & 1;
+        const int s = c % SK_NB;
         const int g = c / SK_GCH, cg = c - g * SK_GCH;
-        wait(afull[b], c >> 1);  // A(c) written (and X, Y of chunk c read)
         wait(full[s], c / SK_NB);
         if (cg == 0 && g >= 2) wait(rfree[g & 1], (g - 2) >> 1);  // region written out
-        tc::fence_after_sync();
-        const uint32_t d = tbase + (uint32_t)(64 * (g & 1));
-        const uint32_t ah = sbase + (uint32_t)b * 2 * SK_APART, al = ah + SK_APART;
-        const uint32_t bh = sbase + oB + (uint32_t)s * 2 * bpart, bl = bh + bpart;
-        for (int k = 0; k < SK_CH / 8; ++k) {
-          const uint32_t ko = (uint32_t)k * 2 * SK_LBO;  // 8 atoms = two core matrices
-          const uint64_t dah = tc::sdesc(ah + ko, SK_LBO, SK_SBO);
-          const uint64_t dal = tc::sdesc(al + ko, SK_LBO, SK_SBO);
-          const uint64_t dbh = tc::sdesc(bh + ko, SK_LBO, SK_SBO);
-          const uint64_t dbl = tc::sdesc(bl + ko, SK_LBO, SK_SBO);
-          tc::mma_tf32(d, dah, dbh, idesc, (cg > 0 || k > 0) ? 1u : 0u);
-          tc::mma_tf32(d, dah, dbl, idesc, 1u);
-          tc::mma_tf32(d, dal, dbh, idesc, 1u);
+        for (int m = 0; m < MT; ++m) {
+          const int j = c * MT + m, b = j & 1;
+          wait(afull[b], j >> 1);  // A of job j written (X, Y of chunk c read)
+          tc::fence_after_sync();
+          const uint32_t d = tbase + (uint32_t)(256 * (g & 1) + 64 * m);
+          const uint32_t ah = sbase + (uint32_t)b * 2 * SK_APART, al = ah + SK_APART;
+          const uint32_t bh = sbase + oB + (uint32_t)s * 2 * bpart, bl = bh + bpart;
+          for (int k = 0; k < SK_CH / 8; ++k) {
+            const uint32_t ko = (uint32_t)k * 2 * SK_LBO;  // 8 atoms = two core matrices
+            const uint64_t dah = tc::sdesc(ah + ko, SK_LBO, SK_SBO);
+            const uint64_t dal = tc::sdesc(al + ko, SK_LBO, SK_SBO);
+            const uint64_t dbh = tc::sdesc(bh + ko, SK_LBO, SK_SBO);
+            const uint64_t dbl = tc::sdesc(bl + ko, SK_LBO, SK_SBO);
+            tc::mma_tf32(d, dah, dbh, idesc, (cg > 0 || k > 0) ? 1u : 0u);
+            tc::mma_tf32(d, dah, dbl, idesc, 1u);
+            tc::mma_tf32(d, dal, dbh, idesc, 1u);
+          }
+          tc::mma_commit(tc::smem_addr(&adone[b]));
         }
-        tc::mma_commit(tc::smem_addr(&mdone[s]));
+        tc::mma_commit(tc::smem_addr(&sdone[s]));
         if (cg == SK_GCH - 1 || c == nchunk - 1) tc::mma_commit(tc::smem_addr(&gdone[g & 1]));
         // stage of chunk c - 1 refilled with chunk c + SK_NB - 1: its X, Y
-        // rows were read (afull), its Z image once MMA(c - 1) is done
+        // rows were read (afull), its Z image once the MMAs of chunk c - 1
+        // are done
         if (c + SK_NB - 1 < nchunk) {
-          if (c >= 1) wait(mdone[(c - 1) % SK_NB], (c - 1) / SK_NB);
+          if (c >= 1) wait(sdone[(c - 1) % SK_NB], (c - 1) / SK_NB);
           copy_in(c + SK_NB - 1);
         }
       }
@@ -477,45 +493,50 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
     __syncwarp();
   } else {
     // ------------------------------------------------------------ generators
-    // write out the accumulator of group g (region g % 2) as partial
-    // gps * blockIdx.y + g: D row 32 (warp % 4) + lane; warps w and w + 4
-    // take columns [0, 32) and [32, 64) (np <= 64)
+    // write out the accumulators of group g (region g % 2) as partial
+    // gps * blockIdx.y + g: warp w reads lanes 32 (w % 4) .. of tile w / 4,
+    // np <= 64 columns
     auto flush = [&](int g) {
       wait(gdone[g & 1], g >> 1);
       tc::fence_after_sync();
       __syncwarp();
-      const int q4 = warp & 3, h = 32 * (warp >> 2);
+      const int q4 = warp & 3, m = warp >> 2;
       const int row = 32 * q4 + lane;
-      float *dst = part + (((size_t)(gps * blockIdx.y + g) * ntm + mt) * SK_ROWS + row) * np;
-      if (h < np) {
-        float v[32];
-        tc::tmem_ld32(tbase + ((uint32_t)(32 * q4) << 16) + (uint32_t)(64 * (g & 1) + h), v);
+      if (m < MT) {
+        float *dst = part + (((size_t)(gps * blockIdx.y + g) * ntm + mt0 + m) * SK_ROWS + row) * np;
+        for (int h = 0; h < np; h += 32) {
+          float v[32];
+          tc::tmem_ld32(tbase + ((uint32_t)(32 * q4) << 16) + (uint32_t)(256 * (g & 1) + 64 * m + h),
+                        v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (h + j < np) dst[h + j] = v[j];
+          for (int j = 0; j < 32; ++j)
+            if (h + j < np) dst[h + j] = v[j];
+        }
       }
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tc::smem_addr(&rfree[g & 1]));
     };
+    // this thread's A item: column cl of the job's tile, atom quad q ->
+    // rows 2 cl (T.re), 2 cl + 1 (T.im)
+    const int cl = tid >> 3, q = tid & 7;
+    const uint32_t o0 = sk_off(2 * cl, q), o1 = sk_off(2 * cl + 1, q);
     int gf = 0;  // next group to write out
     for (int c = 0; c < nchunk; ++c) {
-      const int s = c % SK_NB, b = c & 1;
-      unsigned char *sa = dsm + (size_t)b * 2 * SK_APART;
-      const float2 *sxy = reinterpret_cast<const float2 *>(dsm + oX + (size_t)s * xysz);
-      if (c >= 2) wait(mdone[(c - 2) % SK_NB], (c - 2) / SK_NB);  // A buffer b free
+      const int s = c % SK_NB;
+      const unsigned char *sxy = dsm + oX + (size_t)s * xysz;
       wait(full[s], c / SK_NB);
-      // A rows 2 cl (T.re) and 2 cl + 1 (T.im): 64 columns x 8 atom quads
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int it = tid + SK_GEN * k, cl = it >> 3, q = it & 7;
-        const int2 xy = cxy[cl];
+      for (int m = 0; m < MT; ++m) {
+        const int j = c * MT + m, b = j & 1;
+        unsigned char *sa = dsm + (size_t)b * 2 * SK_APART;
+        if (j >= 2) wait(adone[b], (j - 2) >> 1);  // A buffer b free
+        const int2 xy = cxy[m][cl];
         float re[4] = {0.f, 0.f, 0.f, 0.f}, im[4] = {0.f, 0.f, 0.f, 0.f};
         if (xy.x >= 0) {
           const bool neg = xy.y < 0;
-          const float4 *X = reinterpret_cast<const float4 *>(sxy + xy.x * SK_CH + 4 * q);
-          const float4 *Y =
-              reinterpret_cast<const float4 *>(sxy + (kx + (neg ? -xy.y : xy.y)) * SK_CH + 4 * q);
+          const float4 *X = reinterpret_cast<const float4 *>(sxy + (xy.x * SK_CH + 4 * q) * 8);
+          const float4 *Y = reinterpret_cast<const float4 *>(
+              sxy + ((kx + (neg ? -xy.y : xy.y)) * SK_CH + 4 * q) * 8);
           const float4 x01 = X[0], x23 = X[1], y01 = Y[0], y23 = Y[1];
           const float xr[4] = {x01.x, x01.z, x23.x, x23.z};
           const float xi[4] = {x01.y, x01.w, x23.y, x23.w};
@@ -528,13 +549,12 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
             im[u] = fmaf(xr[u], yi[u], xi[u] * yr[u]);
           }
         }
-        const uint32_t o0 = sk_off(2 * cl, q), o1 = sk_off(2 * cl + 1, q);
         st_split(sa + o0, sa + SK_APART + o0, re[0], re[1], re[2], re[3]);
         st_split(sa + o1, sa + SK_APART + o1, im[0], im[1], im[2], im[3]);
+        tc::fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_addr(&afull[b]));
       }
-      tc::fence_proxy_async();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(tc::smem_addr(&afull[b]));
       // the previous group is written out one chunk into the next one
       if (c - (c / SK_GCH) * SK_GCH == 1 && gf < c / SK_GCH) flush(gf++);
     }
@@ -544,16 +564,27 @@ __global__ void __launch_bounds__(SK_THREADS, 1) k_sfac_tc(
   __syncthreads();  // every MMA waited for, every tensor-memory read done
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tbase, 128);
+    tc::tmem_dealloc(tbase, 512);
   }
   if (!ok) atomicOr(err, DERR_TIMEOUT);
 }
 
-// S(k) from the partials: thread per (column, p <= m), partials added in
-// FP64 in a fixed order (deterministic).
-__global__ void k_sfac_tc_sum(int ncol, int np, int npart, int ntm, const KCol *__restrict__ cols,
-                              const int *__restrict__ cp0, const float *__restrict__ part,
-                              double2 *__restrict__ sk) {
+// Partials -> one FP64 block per M-tile: thread per element of the
+// [ntm][128][np] block, partials added in FP64 in a fixed order
+// (deterministic; coalesced over the elements).
+__global__ void k_sfac_tc_reduce(int nel, int npart, const float *__restrict__ part,
+                                 double *__restrict__ red) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  double a = 0.0;
+  for (int s = 0; s < npart; ++s) a += (double)part[(size_t)s * nel + e];
+  red[e] = a;
+}
+
+// S(k) from the reduced blocks: thread per (column, p <= m).
+__global__ void k_sfac_tc_form(int ncol, int np, const KCol *__restrict__ cols,
+                               const int *__restrict__ cp0, const double *__restrict__ red,
+                               double2 *__restrict__ sk) {
   // cp0[c] = first (column, p) item of column c; cp0[ncol] = items
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cp0[ncol]) return;
@@ -565,14 +596,9 @@ __global__ void k_sfac_tc_sum(int ncol, int np, int npart, int ntm, const KCol *
   }
   const int c = lo, p = t - cp0[c];
   const int mt = c / (SK_ROWS / 2), r = 2 * (c % (SK_ROWS / 2));
-  double A1 = 0.0, A2 = 0.0, A3 = 0.0, A4 = 0.0;
-  for (int s = 0; s < npart; ++s) {
-    const float *d = part + ((size_t)s * ntm + mt) * SK_ROWS * np;
-    A1 += (double)d[(size_t)r * np + 2 * p];
-    A3 += (double)d[(size_t)r * np + 2 * p + 1];
-    A4 += (double)d[(size_t)(r + 1) * np + 2 * p];
-    A2 += (double)d[(size_t)(r + 1) * np + 2 * p + 1];
-  }
+  const double *d = red + (size_t)mt * SK_ROWS * np;
+  const double A1 = d[(size_t)r * np + 2 * p], A3 = d[(size_t)r * np + 2 * p + 1];
+  const double A4 = d[(size_t)(r + 1) * np + 2 * p], A2 = d[(size_t)(r + 1) * np + 2 * p + 1];
   const KCol col = cols[c];
   const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
   if (kp >= 0) sk[kp] = make_double2(A1 - A2, A3 + A4);
@@ -633,8 +659,8 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
   return true;
 }
 
-// Tables of the tensor-core S(k) pass: M-tiles, slices (about one wave of one
-// CTA per SM), partial buffer, item offsets, Z image.  Returns false when it
+// Tables of the tensor-core S(k) pass: M-tiles (up to SK_MT per CTA), slices
+// (about one wave of one CTA per SM), partial buffer, item offsets, Z image.  Returns false when it
 // does not apply.
 bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   DevData &d = ctx->dv;
@@ -648,7 +674,8 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return false;
-  int ns = std::max(1, nsm / std::max(1, ntm));
+  const int ncg = (ntm + SK_MT - 1) / SK_MT;  // CTAs per slice (up to SK_MT tiles each)
+  int ns = std::max(1, nsm / ncg);
   int slice = (d.n + ns - 1) / ns;
   slice = std::max(SK_CH, ((slice + SK_CH - 1) / SK_CH) * SK_CH);
   ns = (d.n + slice - 1) / slice;
@@ -658,14 +685,17 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   ctx_free(ctx, d.tcs_part);
   ctx_free(ctx, d.tcs_cp0);
   ctx_free(ctx, d.tcs_zimg);
+  ctx_free(ctx, d.tcs_red);
   d.tcs_part = nullptr;
   d.tcs_cp0 = nullptr;
   d.tcs_zimg = nullptr;
+  d.tcs_red = nullptr;
   const size_t pbytes = sizeof(float) * (size_t)ns * gps * ntm * SK_ROWS * np;
   const size_t zbytes = (size_t)(d.ldn / SK_CH) * 2 * sk_bpart(np);
   if (ctx_alloc(ctx, &d.tcs_part, pbytes) != cudaSuccess ||
       ctx_alloc(ctx, &d.tcs_cp0, sizeof(int) * cp0.size()) != cudaSuccess ||
-      ctx_alloc(ctx, &d.tcs_zimg, zbytes) != cudaSuccess)
+      ctx_alloc(ctx, &d.tcs_zimg, zbytes) != cudaSuccess ||
+      ctx_alloc(ctx, &d.tcs_red, sizeof(double) * (size_t)ntm * SK_ROWS * np) != cudaSuccess)
     return false;
   if (cudaMemcpy(d.tcs_cp0, cp0.data(), sizeof(int) * cp0.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
@@ -681,6 +711,7 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   d.tcs_slice = slice;
   d.tcs_items = cp0[ncol];
   d.tcs_gps = gps;
+  d.tcs_ncg = ncg;
   d.tcs_on = true;
   return true;
 }
@@ -736,13 +767,16 @@ int tc_sfac_launch(mdx_ctx *ctx) {
   CUtensorMap tm;
   int rc = encode_xy_map(ctx, &tm, SK_CH);
   if (rc) return rc;
-  k_sfac_tc<<<dim3(d.tcs_ntm, d.tcs_nslice), SK_THREADS, sk_smem_bytes(d.tcs_np, d.kx + d.ky),
-              ctx->stream>>>(d.n, d.ncol, d.tcs_np, d.tcs_slice, d.tcs_gps, d.cols, tm,
+  k_sfac_tc<<<dim3(d.tcs_ncg, d.tcs_nslice), SK_THREADS, sk_smem_bytes(d.tcs_np, d.kx + d.ky),
+              ctx->stream>>>(d.n, d.ncol, d.tcs_ntm, d.tcs_np, d.tcs_slice, d.tcs_gps, d.cols, tm,
                              d.tcs_zimg, d.kx, d.ky, d.tcs_part, d.err);
   MDX_LAUNCHED(ctx);
-  k_sfac_tc_sum<<<(d.tcs_items + 127) / 128, 128, 0, ctx->stream>>>(
-      d.ncol, d.tcs_np, d.tcs_nslice * d.tcs_gps, d.tcs_ntm, d.cols, d.tcs_cp0, d.tcs_part,
-      d.sk);
+  const int nel = d.tcs_ntm * SK_ROWS * d.tcs_np;
+  k_sfac_tc_reduce<<<(nel + 255) / 256, 256, 0, ctx->stream>>>(nel, d.tcs_nslice * d.tcs_gps,
+                                                                d.tcs_part, d.tcs_red);
+  MDX_LAUNCHED(ctx);
+  k_sfac_tc_form<<<(d.tcs_items + 127) / 128, 128, 0, ctx->stream>>>(
+      d.ncol, d.tcs_np, d.cols, d.tcs_cp0, d.tcs_red, d.sk);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

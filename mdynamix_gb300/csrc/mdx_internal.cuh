@@ -211,7 +211,8 @@ struct DevData {
   float *tcs_part;
   int *tcs_cp0;
   unsigned char *tcs_zimg;  // Z image (B operand), per 32-atom chunk
-  int tcs_np, tcs_ntm, tcs_nslice, tcs_slice, tcs_items, tcs_gps;
+  double *tcs_red;          // partials reduced per M-tile (FP64)
+  int tcs_np, tcs_ntm, tcs_nslice, tcs_slice, tcs_items, tcs_gps, tcs_ncg;
   int *rf_part;                 // group ranges of the mixed force pass's warps
   int rf_nsplit;                // blocks per atom tile of that pass
   double2 *colrv;               // per column (RXV, RYV) at the current box

@@ -182,4 +182,11 @@ __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
   lo = tf32_rna(x - hi);
 }
 
+// Cheaper split for operands built in the MMA's inner loop: lo = x - hi is
+// exact and is left for the MMA to truncate to TF32 (|error| <= 2^-21 |x|).
+__device__ __forceinline__ void tf32_split_fast(float x, float &hi, float &lo) {
+  hi = tf32_rna(x);
+  lo = x - hi;
+}
+
 }  // namespace tc
