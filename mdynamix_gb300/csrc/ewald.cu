@@ -934,15 +934,18 @@ int host_inifur(mdx_ctx *ctx) {
     MDX_CUDA(cudaMemcpy(d.rf_part, parts.data(), sizeof(int) * parts.size(),
                         cudaMemcpyHostToDevice));
   }
-  // tensor-core force pass (mixed), unless MDX_EWALD_TC=0 or K is too large
-  // for its shared-memory tiles; the CUDA-core pass above stays set up
+  // mixed tensor-core passes (when their shared-memory tiles fit; the
+  // CUDA-core passes above stay set up).  MDX_EWALD_TC: 0 = none, 1 (the
+  // default) = force pass, 2 = force pass and S(k).  The S(k) GEMM
+  // accumulates each 1024-atom partial in the tensor memory's FP32, which
+  // biases |S(k)|^2: the reciprocal energy is off by about 3e-5 relative
+  // against 1e-8 for the FP32 FMA pass, so it is not the default.
   if (ctx->mixed()) {
     const char *env = std::getenv("MDX_EWALD_TC");
+    const int mode = env && env[0] >= '0' && env[0] <= '2' ? env[0] - '0' : 1;
     d.tc_on = d.tcs_on = false;
-    if (!(env && env[0] == '0')) {
-      if (!tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
-      if (!tc_sfac_setup(ctx, cols)) cudaGetLastError();
-    }
+    if (mode >= 1 && !tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
+    if (mode >= 2 && !tc_sfac_setup(ctx, cols)) cudaGetLastError();
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;

@@ -195,31 +195,37 @@ def test_mixed_force_error(name):
 
 
 @pytest.mark.parametrize("name", ["spce_ions", "spcfw", "bilayer_patch"])
-def test_mixed_ewald_tensor_core_pass(name, monkeypatch):
-    """The tensor-core reciprocal force pass (3 x TF32 products) and the
-    CUDA-core FP32 pass agree with the FP64 path to the mixed bar, and with
-    each other well inside it."""
+def test_mixed_ewald_tensor_core_passes(name, monkeypatch):
+    """Tensor-core reciprocal passes (3 x TF32 products) against the CUDA-core
+    FP32 passes and the FP64 path: MDX_EWALD_TC=1 (force pass, the default)
+    and 2 (force pass and S(k)) keep the forces within the mixed bar and
+    within 2e-6 of the FP32 passes; the default keeps the reciprocal energy
+    of the FP32 passes (S(k) is the same kernel); the tensor-core S(k) keeps
+    it within 1e-4."""
     s, st = CASES[name]()
-    g64 = ForcePath(s, precision=MDX_FP64)
-    out = {}
-    for tc in ("1", "0"):
+    out, en = {}, {}
+    for tc in ("0", "1", "2"):
         monkeypatch.setenv("MDX_EWALD_TC", tc)
         g = ForcePath(s, precision=MDX_MIXED)
         g.set_state(*st)
         g.chcnb()
         g.getcom()
-        g.allforce()
+        en[tc] = g.allforce().pels1
         out[tc] = g.forces(3)
         g.close()
+    g64 = ForcePath(s, precision=MDX_FP64)
     g64.set_state(*st)
     g64.chcnb()
     g64.getcom()
-    g64.allforce()
+    e64 = g64.allforce().pels1
     f64 = g64.forces(3)
     nrm = np.sqrt((f64 ** 2).sum())
     for tc, f in out.items():
         assert np.sqrt(((f - f64) ** 2).sum()) / nrm < MIXED_TOL, tc
-    assert np.sqrt(((out["1"] - out["0"]) ** 2).sum()) / nrm < 2e-6
+    for tc in ("1", "2"):
+        assert np.sqrt(((out[tc] - out["0"]) ** 2).sum()) / nrm < 2e-6, tc
+    assert en["1"] == en["0"]
+    assert abs(en["2"] - e64) <= 1e-4 * abs(e64)
 
 
 def test_mixed_deterministic():
