@@ -375,6 +375,54 @@ def bilayer_leg(args):
     return out
 
 
+def nve_run(prec, s, st, th, nsteps, mstep0):
+    """NVE DOUBLE long steps from a given state: per-step total energy
+    (PE1 + PE2 + PELS1 + PELS2 + SPE + PINT + TKE, as the reference's
+    output sums them) and kinetic energy."""
+    from mdynamix_gb300.mdx import ForcePath
+    g = ForcePath(s, precision=prec)
+    p = g.packed.params
+    p.lnvt = 0
+    g.set_params(p)
+    th.sc = 0.0
+    g.set_state(*st, thermo=th)
+    rec = g.double(nsteps, mstep0)
+    g.close()
+    e = np.array([r.pe1 + r.pe2 + r.pels1 + r.pels2 + r.spe + r.pint + r.tke for r in rec])
+    ke = np.array([r.tke for r in rec])
+    return e, ke
+
+
+def nve_leg(args):
+    """NVE energy conservation of both paths from the same equilibrated state
+    (1000 SPC-FW waters, DOUBLE 0.2/2 fs, Rc 9 A): linear drift of the total
+    energy and its RMS fluctuation, per atom, over the run."""
+    from mdynamix_gb300 import system as S
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    from mdynamix_gb300.mdx import ForcePath
+    spec = S.RunSpec(molecules=[("SPC-FW", 1000)], density=1.0, dt_fs=2.0, nfreq=10,
+                     rcut=9.0, rshort=5.0, alpha=2.8, fexp=12.0, ichnb=10, nvt=(300.0, 30.0))
+    s = S.System(spec)
+    st = S.make_configuration(s, seed=3, jitter=0.05)
+    g = ForcePath(s, precision=MDX_FP64)
+    g.set_state(*st)
+    g.double(args.nve_equil, records=False)
+    state, th = g.get_state()
+    g.close()
+    out = {}
+    t = np.arange(args.nve_steps) * s.spec.dt_fs * 1e-3  # ps
+    for name, prec in (("fp64", MDX_FP64), ("mixed", MDX_MIXED)):
+        e, ke = nve_run(prec, s, state, th, args.nve_steps, args.nve_equil)
+        slope = float(np.polyfit(t, e, 1)[0])
+        out[name] = {"drift_per_ps_over_ke_rms": slope / float(ke.std()),
+                     "etot_rms_over_ke_rms": float(e.std() / ke.std())}
+    out["units"] = ("linear drift of the total energy per ps and its RMS fluctuation, "
+                    "both divided by the RMS fluctuation of the kinetic energy")
+    out["sample"] = (f"{s.nstot} atoms, {args.nve_equil} NVT long steps, then "
+                     f"{args.nve_steps} NVE long steps (2 fs) per path from that state")
+    return out
+
+
 def cpu_baseline(s, st, threads, budget_s=40.0):
     """The oracle (restated reference routines) on the same workload:
     one CHCNB and one long step, list build amortised over ICHNB steps."""
@@ -437,6 +485,8 @@ def main():
     ap.add_argument("--pimd-warmup", type=int, default=3)
     ap.add_argument("--bilayer-steps", type=int, default=10, help="bilayer leg timed steps (0 = off)")
     ap.add_argument("--bilayer-warmup", type=int, default=3)
+    ap.add_argument("--nve-steps", type=int, default=500, help="NVE leg long steps (0 = off)")
+    ap.add_argument("--nve-equil", type=int, default=100)
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
@@ -464,6 +514,7 @@ def main():
     serving = serving_leg(args) if args.serve_jobs > 0 else None
     pimd = pimd_leg(args) if args.pimd_steps > 0 else None
     bilayer = bilayer_leg(args) if args.bilayer_steps > 0 else None
+    nve = nve_leg(args) if args.nve_steps > 0 else None
     cpu = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()
@@ -495,6 +546,7 @@ def main():
         "serving": serving,
         "pimd": pimd,
         "bilayer": bilayer,
+        "nve": nve,
         "cpu_baseline": cpu,
         "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
         "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},
