@@ -859,17 +859,17 @@ int host_inifur(mdx_ctx *ctx) {
   d.kgroups = nullptr;
   d.sitems = nullptr;
   MDX_CUDA(ctx_alloc(ctx, &d.sitems, sizeof(SItem) * std::max<size_t>(1, items.size())));
-  MDX_CUDA(cudaMemcpy(d.sitems, items.data(), sizeof(SItem) * items.size(),
+  MDX_CUDA(ctx_copy(ctx->stream, d.sitems, items.data(), sizeof(SItem) * items.size(),
                       cudaMemcpyHostToDevice));
   d.nsitem = (int)items.size();
   MDX_CUDA(ctx_alloc(ctx, &d.kgroups, sizeof(KGroup) * std::max<size_t>(1, groups.size())));
-  MDX_CUDA(cudaMemcpy(d.kgroups, groups.data(), sizeof(KGroup) * groups.size(),
+  MDX_CUDA(ctx_copy(ctx->stream, d.kgroups, groups.data(), sizeof(KGroup) * groups.size(),
                       cudaMemcpyHostToDevice));
   d.ngroup = (int)groups.size();
   MDX_CUDA(ctx_alloc(ctx, &d.cols, sizeof(KCol) * std::max<size_t>(1, cols.size())));
   MDX_CUDA(ctx_alloc(ctx, &d.kchunks, sizeof(Chunk) * std::max<size_t>(1, chunks.size())));
-  MDX_CUDA(cudaMemcpy(d.cols, cols.data(), sizeof(KCol) * cols.size(), cudaMemcpyHostToDevice));
-  MDX_CUDA(cudaMemcpy(d.kchunks, chunks.data(), sizeof(Chunk) * chunks.size(),
+  MDX_CUDA(ctx_copy(ctx->stream, d.cols, cols.data(), sizeof(KCol) * cols.size(), cudaMemcpyHostToDevice));
+  MDX_CUDA(ctx_copy(ctx->stream, d.kchunks, chunks.data(), sizeof(Chunk) * chunks.size(),
                       cudaMemcpyHostToDevice));
   d.nchunk = (int)chunks.size();
   // shared-memory tile of the S(k) kernels: TILE atoms x all table rows
@@ -931,7 +931,7 @@ int host_inifur(mdx_ctx *ctx) {
     ctx_free(ctx, d.rf_part);
     d.rf_part = nullptr;
     MDX_CUDA(ctx_alloc(ctx, &d.rf_part, sizeof(int) * parts.size()));
-    MDX_CUDA(cudaMemcpy(d.rf_part, parts.data(), sizeof(int) * parts.size(),
+    MDX_CUDA(ctx_copy(ctx->stream, d.rf_part, parts.data(), sizeof(int) * parts.size(),
                         cudaMemcpyHostToDevice));
   }
   // mixed tensor-core passes (when their shared-memory tiles fit; the
@@ -971,7 +971,7 @@ int host_inifur(mdx_ctx *ctx) {
       // rows padded to ldn atoms (zero past n): row starts stay 1 KB aligned
       // for the bulk copies of the tensor-core passes
       MDX_CUDA(ctx_alloc(ctx, &d.tabxf, sizeof(float2) * per * d.ldn));
-      MDX_CUDA(cudaMemset(d.tabxf, 0, sizeof(float2) * per * d.ldn));
+      MDX_CUDA(cudaMemsetAsync(d.tabxf, 0, sizeof(float2) * per * d.ldn, ctx->stream));
       d.tabyf = d.tabxf + (size_t)kx * d.ldn;
       d.tabzf = d.tabyf + (size_t)ky * d.ldn;
     } else {
@@ -992,7 +992,7 @@ int host_inifur(mdx_ctx *ctx) {
   d.wp64 = d.wk + nk;
   d.wkf = reinterpret_cast<float4 *>(d.wp64 + np64);
   // padding slots of the grouped W stay zero; k_wpairs writes the others
-  if (np32) MDX_CUDA(cudaMemset(d.wkf, 0, sizeof(float4) * np32));
+  if (np32) MDX_CUDA(cudaMemsetAsync(d.wkf, 0, sizeof(float4) * np32, ctx->stream));
   d.colrv = reinterpret_cast<double2 *>(d.wkf + np32);
   d.colrvf = reinterpret_cast<float2 *>(d.colrv + nc);
   // per-slice partials of S(k), summed in slice order

@@ -646,11 +646,11 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
       ctx_alloc(ctx, &d.tc_zimg, zbytes) != cudaSuccess)
     return false;
   d.tc_ks = d.tc_slot + slot.size();
-  if (cudaMemcpy(d.tc_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice) !=
+  if (ctx_copy(ctx->stream, d.tc_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
-      cudaMemcpy(d.tc_ks, ks.data(), sizeof(int) * ks.size(), cudaMemcpyHostToDevice) !=
+      ctx_copy(ctx->stream, d.tc_ks, ks.data(), sizeof(int) * ks.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
-      cudaMemset(d.tc_zimg, 0, zbytes) != cudaSuccess)  // K columns past 2 kz stay zero
+      cudaMemsetAsync(d.tc_zimg, 0, zbytes, ctx->stream) != cudaSuccess)  // K columns past 2 kz stay zero
     return false;
   if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy, ntile)) != cudaSuccess) return false;
   d.tc_ntile = ntile;
@@ -697,12 +697,12 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
       ctx_alloc(ctx, &d.tcs_zimg, zbytes) != cudaSuccess ||
       ctx_alloc(ctx, &d.tcs_red, sizeof(double) * (size_t)ntm * SK_ROWS * np) != cudaSuccess)
     return false;
-  if (cudaMemcpy(d.tcs_cp0, cp0.data(), sizeof(int) * cp0.size(), cudaMemcpyHostToDevice) !=
+  if (ctx_copy(ctx->stream, d.tcs_cp0, cp0.data(), sizeof(int) * cp0.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       // partials past the last slice's atoms are never written: they stay zero;
       // image rows 2p, 2p + 1 with p >= kz too
-      cudaMemset(d.tcs_part, 0, pbytes) != cudaSuccess ||
-      cudaMemset(d.tcs_zimg, 0, zbytes) != cudaSuccess)
+      cudaMemsetAsync(d.tcs_part, 0, pbytes, ctx->stream) != cudaSuccess ||
+      cudaMemsetAsync(d.tcs_zimg, 0, zbytes, ctx->stream) != cudaSuccess)
     return false;
   if (raise_smem_limit(k_sfac_tc, sk_smem_bytes(np, kxy)) != cudaSuccess) return false;
   d.tcs_np = np;

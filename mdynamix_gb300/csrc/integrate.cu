@@ -80,12 +80,16 @@ struct MolConst {
   double summas[MDX_NT];
 };
 
+// GETCOM (service.f:463-563); with posf set it also refreshes the FP32 and
+// fixed-point mirrors of the wrapped positions (what k_mirror writes), so a
+// short step needs no separate mirror pass.
 __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
                          const int *__restrict__ mol_nat,
                          const int *__restrict__ mol_type,
                          const double *__restrict__ amass, dbl4 *pos, double *X,
                          double *Y, double *Z, MolConst mc, double bx, double by,
-                         double bz) {
+                         double bz, float4 *__restrict__ posf, int4 *__restrict__ posi,
+                         const int *__restrict__ pinfo) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
@@ -106,22 +110,24 @@ __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
   X[m] = xw;
   Y[m] = yw;
   Z[m] = zw;
-  if (xw != x || yw != y || zw != z) {
-    for (int k = 0; k < na; ++k) {
-      dbl4 p = pos[f + k];
-      p.x = (p.x - x) + xw;
-      p.y = (p.y - y) + yw;
-      p.z = (p.z - z) + zw;
-      pos[f + k] = p;
-    }
-  } else {
-    // the reference rebuilds every coordinate as (S - X) + X (service.f:549-552)
-    for (int k = 0; k < na; ++k) {
-      dbl4 p = pos[f + k];
-      p.x = (p.x - x) + x;
-      p.y = (p.y - y) + y;
-      p.z = (p.z - z) + z;
-      pos[f + k] = p;
+  // the reference rebuilds every coordinate as (S - X) + Xw (service.f:549-552)
+  const double two32 = 4294967296.0, ibx = 1.0 / bx, iby = 1.0 / by, ibz = 1.0 / bz;
+  for (int k = 0; k < na; ++k) {
+    dbl4 p = pos[f + k];
+    p.x = (p.x - x) + xw;
+    p.y = (p.y - y) + yw;
+    p.z = (p.z - z) + zw;
+    pos[f + k] = p;
+    if (posf) {
+      posf[f + k] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+      if (posi) {
+        const long long xi = __double2ll_rn(p.x * ibx * two32);
+        const long long yi = __double2ll_rn(p.y * iby * two32);
+        const long long zi = __double2ll_rn(p.z * ibz * two32);
+        posi[f + k] = make_int4((int)(unsigned)(unsigned long long)xi,
+                                (int)(unsigned)(unsigned long long)yi,
+                                (int)(unsigned)(unsigned long long)zi, pinfo[f + k]);
+      }
     }
   }
 }
@@ -997,12 +1003,13 @@ int launch_sum_forces(mdx_ctx *ctx) {
   return MDX_OK;
 }
 
-int launch_getcom(mdx_ctx *ctx) {
+int launch_getcom(mdx_ctx *ctx, bool mirror) {
   MDX_TIMER(ctx, MDX_T_MOVE);
   DevData &d = ctx->dv;
   k_getcom<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z,
-      mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl);
+      mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl, mirror ? d.posf : nullptr,
+      mirror && ctx->mixed() ? d.posi : nullptr, d.pinfo);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

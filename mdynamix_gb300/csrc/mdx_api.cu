@@ -55,7 +55,7 @@ int upload(mdx_ctx *ctx, T *dst, const T *src, size_t n) {
     ctx->err = "null input array";
     return MDX_ERR_ARG;
   }
-  MDX_CUDA(cudaMemcpy(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+  MDX_CUDA(ctx_copy(ctx->stream, dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
   return MDX_OK;
 }
 
@@ -115,12 +115,12 @@ __global__ void k_set_q(int n, const double *q, dbl4 *pos) {
 int check_err(mdx_ctx *ctx) {
   int herr = 0;
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
-  MDX_CUDA(cudaMemcpy(&herr, ctx->dv.err, sizeof(int), cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, &herr, ctx->dv.err, sizeof(int), cudaMemcpyDeviceToHost));
   if (!herr) return MDX_OK;
-  MDX_CUDA(cudaMemset(ctx->dv.err, 0, sizeof(int)));
+  MDX_CUDA(cudaMemsetAsync(ctx->dv.err, 0, sizeof(int), ctx->stream));
   if (herr & (DERR_LIST_SHORT | DERR_LIST_LONG)) {
     int need[2] = {0, 0};
-    cudaMemcpy(need, ctx->dv.shake_iter + 4, sizeof(int) * 2, cudaMemcpyDeviceToHost);
+    ctx_copy(ctx->stream, need, ctx->dv.shake_iter + 4, sizeof(int) * 2, cudaMemcpyDeviceToHost);
     char b[256];
     snprintf(b, sizeof b,
              "neighbour list overfilled: short row needs %d (cap %d), long row "
@@ -156,7 +156,7 @@ int check_err(mdx_ctx *ctx) {
 
 int copy_scalars(mdx_ctx *ctx, mdx_scalars *out) {
   if (!out) return MDX_OK;
-  MDX_CUDA(cudaMemcpy(out, ctx->dv.sc, sizeof(mdx_scalars), cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, out, ctx->dv.sc, sizeof(mdx_scalars), cudaMemcpyDeviceToHost));
   out->nkv = ctx->nkv;
   return MDX_OK;
 }
@@ -187,10 +187,13 @@ int require(mdx_ctx *ctx, bool topo, bool par, bool state) {
 // ---------------------------------------------------------------- forces
 // ener = false: an intermediate short step of DOUBLE, whose fast energies
 // and virials the next FFORCES zeroes before anything reads them; the pair
-// sweep then computes forces only.
-int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true) {
-  RC(launch_zero_fast(ctx));
-  if (ctx->mixed()) RC(launch_mirror_f32(ctx));
+// sweep then computes forces only, and on the mixed path nothing needs
+// zeroing (the short sweep stores every atom's fixed-point force before the
+// bonded terms add to it).  mirrored: GETCOM has just refreshed the FP32 and
+// fixed-point mirrors of the positions.
+int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true, bool mirrored = false) {
+  if (ener || !ctx->mixed()) RC(launch_zero_fast(ctx));
+  if (ctx->mixed() && !mirrored) RC(launch_mirror_f32(ctx));
   RC(launch_localf(ctx, split, ener));
   if (ener) RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
   RC(launch_bonded(ctx, laver, ener));
@@ -199,9 +202,9 @@ int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true) {
   return MDX_OK;
 }
 
-int do_slow_parts(mdx_ctx *ctx, bool split) {
+int do_slow_parts(mdx_ctx *ctx, bool split, bool mirrored = false) {
   if (ctx->mixed()) {
-    RC(launch_mirror_f32(ctx));
+    if (!mirrored) RC(launch_mirror_f32(ctx));
     RC(launch_forces_long(ctx, split));  // stores G first
     RC(launch_furir(ctx));
     RC(launch_eterms(ctx));
@@ -214,9 +217,9 @@ int do_slow_parts(mdx_ctx *ctx, bool split) {
   return MDX_OK;
 }
 
-int do_slforces(mdx_ctx *ctx, bool split) {
+int do_slforces(mdx_ctx *ctx, bool split, bool mirrored = false) {
   RC(launch_zero_slow(ctx));
-  RC(do_slow_parts(ctx, split));
+  RC(do_slow_parts(ctx, split, mirrored));
   RC(launch_wir(ctx, 2));
   RC(launch_sclfrc(ctx, 2));
   return MDX_OK;
@@ -240,7 +243,7 @@ int do_allforce(mdx_ctx *ctx, bool split) {
 int sync_box_from_device(mdx_ctx *ctx) {
   double b[3];
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
-  MDX_CUDA(cudaMemcpy(b, &ctx->dv.th->boxl, sizeof b, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, b, &ctx->dv.th->boxl, sizeof b, cudaMemcpyDeviceToHost));
   ctx->boxl = b[0];
   ctx->boyl = b[1];
   ctx->bozl = b[2];
@@ -258,13 +261,13 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
   RC(launch_kick(ctx, 2, HTSTEP, pend));
   for (int s = 1; s <= NFREQ; ++s) {
     RC(launch_kick_drift(ctx, HTSTEB, TSTEB, s > 1 ? 1 : 0));
-    RC(launch_getcom(ctx));
+    RC(launch_getcom(ctx, true));  // positions stay put until the next drift
     if (s == NFREQ2 && mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
     if (s == NFREQ) {
-      RC(do_slforces(ctx, false));
-      RC(do_fforces(ctx, 0, false));
+      RC(do_slforces(ctx, false, true));
+      RC(do_fforces(ctx, 0, false, true, true));
     } else {
-      RC(do_fforces(ctx, 0, false, false));
+      RC(do_fforces(ctx, 0, false, false, true));
     }
   }
   RC(launch_kick(ctx, 1, HTSTEB, false));
@@ -360,7 +363,7 @@ int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
   }
   RC(check_err(ctx));
   if (rec) {
-    MDX_CUDA(cudaMemcpy(rec, ctx->dv.rec, sizeof(mdx_step_record) * nsteps,
+    MDX_CUDA(ctx_copy(ctx->stream, rec, ctx->dv.rec, sizeof(mdx_step_record) * nsteps,
                         cudaMemcpyDeviceToHost));
   }
   return MDX_OK;
@@ -934,15 +937,15 @@ int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
     k_get_pos<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.pos, tmp, tmp + n, tmp + 2 * n);
     ctx->launches++;
     cudaStreamSynchronize(ctx->stream);
-    if (sx) cudaMemcpy(sx, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    if (sy) cudaMemcpy(sy, tmp + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    if (sz) cudaMemcpy(sz, tmp + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (sx) ctx_copy(ctx->stream, sx, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (sy) ctx_copy(ctx->stream, sy, tmp + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (sz) ctx_copy(ctx->stream, sz, tmp + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
     ctx_free(ctx, tmp);
   }
-  if (vx) MDX_CUDA(cudaMemcpy(vx, d.vx, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  if (vy) MDX_CUDA(cudaMemcpy(vy, d.vy, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  if (vz) MDX_CUDA(cudaMemcpy(vz, d.vz, sizeof(double) * n, cudaMemcpyDeviceToHost));
-  if (th) MDX_CUDA(cudaMemcpy(th, d.th, sizeof(mdx_thermo), cudaMemcpyDeviceToHost));
+  if (vx) MDX_CUDA(ctx_copy(ctx->stream, vx, d.vx, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (vy) MDX_CUDA(ctx_copy(ctx->stream, vy, d.vy, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (vz) MDX_CUDA(ctx_copy(ctx->stream, vz, d.vz, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (th) MDX_CUDA(ctx_copy(ctx->stream, th, d.th, sizeof(mdx_thermo), cudaMemcpyDeviceToHost));
   return MDX_OK;
 }
 
@@ -953,9 +956,9 @@ int mdx_download_forces(mdx_ctx *ctx, int which, double *fx, double *fy, double 
   const double *y = which == 1 ? d.hy : which == 2 ? d.gy : d.fy;
   const double *z = which == 1 ? d.hz : which == 2 ? d.gz : d.fz;
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
-  MDX_CUDA(cudaMemcpy(fx, x, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(fy, y, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(fz, z, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, fx, x, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, fy, y, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, fz, z, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
   return MDX_OK;
 }
 
@@ -981,7 +984,7 @@ int mdx_chcnb(mdx_ctx *ctx, int32_t *mbsh, int32_t *mbln) {
   RC(launch_build_lists(ctx));
   RC(check_err(ctx));
   int c[2];
-  MDX_CUDA(cudaMemcpy(c, &ctx->dv.sc->mbsh, sizeof c, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, c, &ctx->dv.sc->mbsh, sizeof c, cudaMemcpyDeviceToHost));
   ctx->mbsh = c[0];
   ctx->mbln = c[1];
   if (mbsh) *mbsh = c[0];
@@ -1129,8 +1132,8 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
   const size_t nn = (size_t)nb * nb;
   std::vector<double> a6(nn), b12(nn);
   std::vector<float> a6f(nn), b12f(nn);
-  MDX_CUDA(cudaMemcpy(a6.data(), d.a6lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(b12.data(), d.b12lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, a6.data(), d.a6lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, b12.data(), d.b12lj, sizeof(double) * nn, cudaMemcpyDeviceToHost));
   ctx->spei = 0.0;
   for (int t = 0; t < nt; ++t) {
     const double ESCI = ctx->tc.iee[t] == 0 ? std::pow(ec, pw1) : 1.0;

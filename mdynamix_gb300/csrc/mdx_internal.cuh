@@ -490,6 +490,16 @@ inline cudaError_t ctx_alloc(mdx_ctx *ctx, void **p, size_t bytes) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return e;
 }
+// Copy on a context's stream and wait: ordered after the stream's kernels
+// (device-to-host reads see their results) and complete on return (host
+// buffers may go away).  The contexts' streams are non-blocking, so a plain
+// cudaMemcpy / cudaMemset on the legacy default stream would race with them.
+inline cudaError_t ctx_copy(cudaStream_t s, void *dst, const void *src, size_t bytes,
+                            cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
 template <typename T>
 inline cudaError_t ctx_alloc(mdx_ctx *ctx, T **p, size_t bytes) {
   return ctx_alloc(ctx, reinterpret_cast<void **>(p), bytes);
@@ -536,7 +546,7 @@ int launch_zero_slow(mdx_ctx *ctx);
 int launch_fix_to_double(mdx_ctx *ctx, int which);  // mixed: int64 -> G/H
 int launch_sclfrc(mdx_ctx *ctx, int nnn);
 int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
-int launch_getcom(mdx_ctx *ctx);
+int launch_getcom(mdx_ctx *ctx, bool mirror = false);  // mirror: refresh posf/posi too
 int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev);
 int launch_record(mdx_ctx *ctx, int slot, int mstep);
 int launch_getemp(mdx_ctx *ctx);

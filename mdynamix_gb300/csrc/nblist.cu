@@ -361,10 +361,10 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
   const size_t nrow = tiled ? ((size_t)n + 31) / 32 * 32 : (size_t)n;
   std::vector<int> cs(n), cl(n), rs(nrow * d.cap_s), rl((size_t)n * d.cap_l);
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));
-  MDX_CUDA(cudaMemcpy(cs.data(), d.ns_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(cl.data(), d.nl_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(rs.data(), d.ns_idx, sizeof(int) * rs.size(), cudaMemcpyDeviceToHost));
-  MDX_CUDA(cudaMemcpy(rl.data(), d.nl_idx, sizeof(int) * rl.size(), cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, cs.data(), d.ns_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, cl.data(), d.nl_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, rs.data(), d.ns_idx, sizeof(int) * rs.size(), cudaMemcpyDeviceToHost));
+  MDX_CUDA(ctx_copy(ctx->stream, rl.data(), d.nl_idx, sizeof(int) * rl.size(), cudaMemcpyDeviceToHost));
   long ks = 0, kl = 0;
   std::vector<int> row;
   for (int i = 0; i < n; ++i) {

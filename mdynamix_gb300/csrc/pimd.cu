@@ -345,7 +345,7 @@ int finish(mdx_pimd *pi, int32_t nsteps, mdx_pimd_record *rec) {
   PI_CUDA(cudaStreamSynchronize(pi->stream));
   for (int k = 0; k < pi->P; ++k) RC(bead_err(pi, k, api_check_err(pi->beads[k])));
   if (rec && nsteps > 0)
-    PI_CUDA(cudaMemcpy(rec, pi->rec, sizeof(mdx_pimd_record) * nsteps, cudaMemcpyDeviceToHost));
+    PI_CUDA(ctx_copy(pi->stream, rec, pi->rec, sizeof(mdx_pimd_record) * nsteps, cudaMemcpyDeviceToHost));
   return MDX_OK;
 }
 
@@ -426,8 +426,8 @@ int mdx_pimd_open(mdx_ctx *const *beads, const mdx_pimd_params *par, mdx_pimd **
       (rc = pi_alloc(pi, reinterpret_cast<void **>(&pi->rec_ctr), 2 * sizeof(int))))
     return fail(rc);
   if (cudaStreamSynchronize(pi->stream) != cudaSuccess ||
-      cudaMemcpy(pi->db, hb.data(), sizeof(PiBead) * pi->P, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(pi->smass, sm.data(), sizeof(double) * pi->n, cudaMemcpyHostToDevice) != cudaSuccess)
+      ctx_copy(pi->stream, pi->db, hb.data(), sizeof(PiBead) * pi->P, cudaMemcpyHostToDevice) != cudaSuccess ||
+      ctx_copy(pi->stream, pi->smass, sm.data(), sizeof(double) * pi->n, cudaMemcpyHostToDevice) != cudaSuccess)
     return fail(MDX_ERR_CUDA);
   *out = pi;
   return MDX_OK;
@@ -467,7 +467,7 @@ int mdx_pimd_steps(mdx_pimd *pi, int32_t nsteps, int32_t mstep0, mdx_pimd_record
 int mdx_pimd_get_thermo(mdx_pimd *pi, double *thermo) {
   if (!pi || !thermo) return MDX_ERR_ARG;
   if (cudaStreamSynchronize(pi->stream) != cudaSuccess ||
-      cudaMemcpy(thermo, pi->thermo, sizeof(double) * (size_t)pi->pp.jnh * pi->n,
+      ctx_copy(pi->stream, thermo, pi->thermo, sizeof(double) * (size_t)pi->pp.jnh * pi->n,
                  cudaMemcpyDeviceToHost) != cudaSuccess)
     return MDX_ERR_CUDA;
   return MDX_OK;
@@ -476,7 +476,7 @@ int mdx_pimd_get_thermo(mdx_pimd *pi, double *thermo) {
 int mdx_pimd_set_thermo(mdx_pimd *pi, const double *thermo) {
   if (!pi || !thermo) return MDX_ERR_ARG;
   if (cudaStreamSynchronize(pi->stream) != cudaSuccess ||
-      cudaMemcpy(pi->thermo, thermo, sizeof(double) * (size_t)pi->pp.jnh * pi->n,
+      ctx_copy(pi->stream, pi->thermo, thermo, sizeof(double) * (size_t)pi->pp.jnh * pi->n,
                  cudaMemcpyHostToDevice) != cudaSuccess)
     return MDX_ERR_CUDA;
   return MDX_OK;
