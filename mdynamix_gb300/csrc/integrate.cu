@@ -191,6 +191,94 @@ __global__ void k_kick_drift(int n, const int4 *__restrict__ ainfo, MoveConst mv
   pos[i] = p;
 }
 
+// One short step of DOUBLE's inner loop up to the fast forces, thread per
+// molecule: the kick and drift of k_kick_drift for each of its atoms
+// (mdstep.f:383-397), then GETCOM's centre of mass and wrap (service.f:
+// 463-563) and the position mirrors, all in the order the separate kernels
+// use.  hfix (mixed path): the previous short step's fast forces are read
+// as fixed point, so that step needs no fold to FP64.
+__global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
+                                 const int *__restrict__ mol_nat,
+                                 const int *__restrict__ mol_type,
+                                 const int4 *__restrict__ ainfo, MoveConst mv,
+                                 MolConst mc, double htsteb, double tsteb, int prev,
+                                 const double *__restrict__ hx, const double *__restrict__ hy,
+                                 const double *__restrict__ hz,
+                                 const unsigned long long *__restrict__ hfix, int n,
+                                 double inv, const double *__restrict__ massdi,
+                                 const double *__restrict__ amass, double *vx, double *vy,
+                                 double *vz, dbl4 *pos, double *X, double *Y, double *Z,
+                                 double bx, double by, double bz, float4 *__restrict__ posf,
+                                 int4 *__restrict__ posi, const int *__restrict__ pinfo) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nop) return;
+  const int f = mol_first[m], na = mol_nat[m];
+  double x = 0., y = 0., z = 0.;
+  for (int k = 0; k < na; ++k) {
+    const int i = f + k;
+    dbl4 p = pos[i];
+    if (mv.lmove[ainfo[i].x]) {
+      double u = vx[i], v = vy[i], w = vz[i];
+      double fx, fy, fz;
+      if (hfix) {
+        fx = (double)(long long)hfix[i] * inv;
+        fy = (double)(long long)hfix[n + i] * inv;
+        fz = (double)(long long)hfix[2 * n + i] * inv;
+      } else {
+        fx = hx[i];
+        fy = hy[i];
+        fz = hz[i];
+      }
+      if (prev) {
+        u = u + htsteb * fx;
+        v = v + htsteb * fy;
+        w = w + htsteb * fz;
+      }
+      u = u + htsteb * fx;
+      v = v + htsteb * fy;
+      w = w + htsteb * fz;
+      vx[i] = u;
+      vy[i] = v;
+      vz[i] = w;
+      const double mi = massdi[i];
+      p.x = u * tsteb * mi + p.x;
+      p.y = v * tsteb * mi + p.y;
+      p.z = w * tsteb * mi + p.z;
+    }
+    pos[i] = p;
+    const double ms = amass[i];
+    x = x + ms * p.x;
+    y = y + ms * p.y;
+    z = z + ms * p.z;
+  }
+  const double summ = mc.summas[mol_type[m]];
+  x = x / summ;
+  y = y / summ;
+  z = z / summ;
+  double xw = x, yw = y, zw = z;
+  pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  X[m] = xw;
+  Y[m] = yw;
+  Z[m] = zw;
+  const double two32 = 4294967296.0, ibx = 1.0 / bx, iby = 1.0 / by, ibz = 1.0 / bz;
+  for (int k = 0; k < na; ++k) {
+    dbl4 p = pos[f + k];
+    p.x = (p.x - x) + xw;
+    p.y = (p.y - y) + yw;
+    p.z = (p.z - z) + zw;
+    pos[f + k] = p;
+    posf[f + k] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+    if (posi) {
+      const long long xi = __double2ll_rn(p.x * ibx * two32);
+      const long long yi = __double2ll_rn(p.y * iby * two32);
+      const long long zi = __double2ll_rn(p.z * ibz * two32);
+      posi[f + k] = make_int4((int)(unsigned)(unsigned long long)xi,
+                              (int)(unsigned)(unsigned long long)yi,
+                              (int)(unsigned)(unsigned long long)zi, pinfo[f + k]);
+    }
+  }
+}
+
 // SULTAN 1.3.1-1.3.2.2 (mdstep.f:89-113): OX = SX, V += TSTEP F,
 // SX += TSTEP V MASSDI.
 __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
@@ -1033,6 +1121,18 @@ int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev) {
   k_kick_drift<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.ainfo, move_const(ctx), htsteb, tsteb, prev, d.hx, d.hy, d.hz, d.massdi,
       d.vx, d.vy, d.vz, d.pos);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, bool from_fix) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
+  DevData &d = ctx->dv;
+  k_kick_drift_com<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
+      d.nop, d.mol_first, d.mol_nat, d.mol_type, d.ainfo, move_const(ctx), mol_const(ctx),
+      htsteb, tsteb, prev, d.hx, d.hy, d.hz, from_fix ? d.hfix : nullptr, d.n, ctx->fix.inv,
+      d.massdi, d.amass, d.vx, d.vy, d.vz, d.pos, d.X, d.Y, d.Z, ctx->boxl, ctx->boyl,
+      ctx->bozl, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -191,13 +191,15 @@ int require(mdx_ctx *ctx, bool topo, bool par, bool state) {
 // zeroing (the short sweep stores every atom's fixed-point force before the
 // bonded terms add to it).  mirrored: GETCOM has just refreshed the FP32 and
 // fixed-point mirrors of the positions.
-int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true, bool mirrored = false) {
+int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true, bool mirrored = false,
+               bool fold = true) {
   if (ener || !ctx->mixed()) RC(launch_zero_fast(ctx));
   if (ctx->mixed() && !mirrored) RC(launch_mirror_f32(ctx));
   RC(launch_localf(ctx, split, ener));
   if (ener) RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
   RC(launch_bonded(ctx, laver, ener));
-  if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
+  // fold = false: the next step's kick reads the fixed-point forces itself
+  if (ctx->mixed() && fold) RC(launch_fix_to_double(ctx, 1));
   RC(launch_sclfrc(ctx, 1));
   return MDX_OK;
 }
@@ -259,15 +261,19 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
   RC(launch_scaling(ctx, 1, &pend));
   if (p.lnpt) RC(sync_box_from_device(ctx));
   RC(launch_kick(ctx, 2, HTSTEP, pend));
+  // mixed path, intermediate short steps: the fast forces stay in fixed
+  // point (no fold) unless SCLFRC needs them in FP64
+  const bool keep_fix = ctx->mixed() && !p.lscft;
   for (int s = 1; s <= NFREQ; ++s) {
-    RC(launch_kick_drift(ctx, HTSTEB, TSTEB, s > 1 ? 1 : 0));
-    RC(launch_getcom(ctx, true));  // positions stay put until the next drift
+    // kick, drift, GETCOM and the mirrors; positions then stay put until the
+    // next short step
+    RC(launch_kick_drift_com(ctx, HTSTEB, TSTEB, s > 1 ? 1 : 0, keep_fix && s > 1));
     if (s == NFREQ2 && mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
     if (s == NFREQ) {
       RC(do_slforces(ctx, false, true));
       RC(do_fforces(ctx, 0, false, true, true));
     } else {
-      RC(do_fforces(ctx, 0, false, false, true));
+      RC(do_fforces(ctx, 0, false, false, true, !keep_fix));
     }
   }
   RC(launch_kick(ctx, 1, HTSTEB, false));

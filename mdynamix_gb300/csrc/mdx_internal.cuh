@@ -547,6 +547,9 @@ int launch_fix_to_double(mdx_ctx *ctx, int which);  // mixed: int64 -> G/H
 int launch_sclfrc(mdx_ctx *ctx, int nnn);
 int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
 int launch_getcom(mdx_ctx *ctx, bool mirror = false);  // mirror: refresh posf/posi too
+// DOUBLE's kick + drift + GETCOM + mirrors in one pass (from_fix: fast
+// forces read as fixed point, mixed path)
+int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, bool from_fix);
 int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev);
 int launch_record(mdx_ctx *ctx, int slot, int mstep);
 int launch_getemp(mdx_ctx *ctx);
