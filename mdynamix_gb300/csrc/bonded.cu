@@ -4,8 +4,10 @@
 //   GETTRS forces.f:323-513  (AMBER, MM3 Tors1, Tors5, improper)
 //   STRBND forces.f:530-800  (flexible SPC water, IPOT 1/2)
 // One thread per term.  Bond vectors are formed in FP64 with the reference's
-// minimum image; the rest of the arithmetic runs in R (double on the FP64
-// path, float on the mixed path, whose forces go to 64-bit fixed point).
+// minimum image (vec_r can take them from the fixed-point positions instead;
+// launch_bonded leaves that off); the rest of the arithmetic runs in R
+// (double on the FP64 path, float on the mixed path, whose forces go to
+// 64-bit fixed point with FP32 operations only).
 // PINT, VIRB and VIRFX.. are block-reduced in FP64; the per-record averages
 // BR/BE, AR/AE, TR/TE are only formed when the caller asks for them.
 #include <cmath>
@@ -19,14 +21,26 @@ struct BondOut {
   unsigned long long *hfix;
   int n;
   double fscale;
+  float fscalef;      // the same power of two as FP32
+  const int4 *posi;   // mixed: fixed-point positions (bond vectors by integer wrap)
+  float sx, sy, sz;   // box / 2^32
 };
+
+// Fixed-point force term: R = float rounds v * 2^k with FP32 operations only
+// (the product is exact, so this equals the FP64 rounding of the same value;
+// 64-bit conversion instructions issue on the narrow FP64 pipe).
+template <typename R>
+__device__ __forceinline__ long long fix_term(const BondOut &o, R v) {
+  if (sizeof(R) == sizeof(float)) return f2ll_rn((float)v * o.fscalef);
+  return __double2ll_rn((double)v * o.fscale);
+}
 
 template <typename R>
 __device__ __forceinline__ void add_force(const BondOut &o, int i, R fx, R fy, R fz) {
   if (o.hfix) {
-    fix_add(&o.hfix[i], (double)fx, o.fscale);
-    fix_add(&o.hfix[o.n + i], (double)fy, o.fscale);
-    fix_add(&o.hfix[2 * o.n + i], (double)fz, o.fscale);
+    atomicAdd(&o.hfix[i], (unsigned long long)fix_term<R>(o, fx));
+    atomicAdd(&o.hfix[o.n + i], (unsigned long long)fix_term<R>(o, fy));
+    atomicAdd(&o.hfix[2 * o.n + i], (unsigned long long)fix_term<R>(o, fz));
   } else {
     atomicAdd(&o.hx[i], (double)fx);
     atomicAdd(&o.hy[i], (double)fy);
@@ -42,6 +56,26 @@ __device__ __forceinline__ void vec(const dbl4 *pos, int a, int b, double bx,
   y = pa.y - pb.y;
   z = pa.z - pb.z;
   pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+}
+
+// Bond vector a - b in R: FP64 minimum image of the FP64 positions, or on
+// the mixed path (float, posi set) the wrapped difference of the 32-bit
+// fixed-point positions (exact minimum image by integer wrap-around).
+template <typename R>
+__device__ __forceinline__ void vec_r(const dbl4 *pos, const BondOut &o, int a, int b, double bx,
+                                      double by, double bz, R &x, R &y, R &z) {
+  if (sizeof(R) == sizeof(float) && o.posi) {
+    const int4 pa = o.posi[a], pb = o.posi[b];
+    x = (R)((float)(int)((unsigned)pa.x - (unsigned)pb.x) * o.sx);
+    y = (R)((float)(int)((unsigned)pa.y - (unsigned)pb.y) * o.sy);
+    z = (R)((float)(int)((unsigned)pa.z - (unsigned)pb.z) * o.sz);
+  } else {
+    double xd, yd, zd;
+    vec(pos, a, b, bx, by, bz, xd, yd, zd);
+    x = (R)xd;
+    y = (R)yd;
+    z = (R)zd;
+  }
 }
 
 template <typename R>
@@ -65,9 +99,9 @@ __device__ __forceinline__ void avg_add(double *sh, double *gl, int m, int nrec,
 template <typename R>
 __device__ __forceinline__ void add_force_own(const BondOut &o, int i, R fx, R fy, R fz) {
   if (o.hfix) {
-    o.hfix[i] += (unsigned long long)__double2ll_rn((double)fx * o.fscale);
-    o.hfix[o.n + i] += (unsigned long long)__double2ll_rn((double)fy * o.fscale);
-    o.hfix[2 * o.n + i] += (unsigned long long)__double2ll_rn((double)fz * o.fscale);
+    o.hfix[i] += (unsigned long long)fix_term<R>(o, fx);
+    o.hfix[o.n + i] += (unsigned long long)fix_term<R>(o, fy);
+    o.hfix[2 * o.n + i] += (unsigned long long)fix_term<R>(o, fz);
   } else {
     o.hx[i] += (double)fx;
     o.hy[i] += (double)fy;
@@ -86,9 +120,8 @@ __device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, i
                                           const double *__restrict__ ro, int lmove,
                                           double bx, double by, double bz,
                                           const BondOut &o, double *acc, R *bd, R *eb) {
-  double BXd, BYd, BZd;
-  vec(pos, J, I, bx, by, bz, BXd, BYd, BZd);
-  const R BX = (R)BXd, BY = (R)BYd, BZ = (R)BZd;
+  R BX, BY, BZ;
+  vec_r<R>(pos, o, J, I, bx, by, bz, BX, BY, BZ);
   const R REQ = (R)rb[M];
   const R BSQ = BX * BX + BY * BY + BZ * BZ;
   const R BD = sqrt(BSQ);
@@ -133,11 +166,9 @@ __device__ __forceinline__ void angle_term(const dbl4 *__restrict__ pos, int I, 
                                            double bx, double by, double bz,
                                            const BondOut &o, double *acc, R *alf, R *ea) {
   const R FCN = (R)fa[M], AEQ = (R)ra[M];
-  double ax, ay, az, bxv, byv, bzv;
-  vec(pos, I, J, bx, by, bz, ax, ay, az);
-  vec(pos, K, J, bx, by, bz, bxv, byv, bzv);
-  const R AX = (R)ax, AY = (R)ay, AZ = (R)az;
-  const R BX = (R)bxv, BY = (R)byv, BZ = (R)bzv;
+  R AX, AY, AZ, BX, BY, BZ;
+  vec_r<R>(pos, o, I, J, bx, by, bz, AX, AY, AZ);
+  vec_r<R>(pos, o, K, J, bx, by, bz, BX, BY, BZ);
   const R ASQ = AX * AX + AY * AY + AZ * AZ;
   const R ASQI = R(1) / ASQ;
   const R BSQ = BX * BX + BY * BY + BZ * BZ;
@@ -566,7 +597,12 @@ int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
   DevData &d = ctx->dv;
   mdx_scalars *sc = d.sc;
   const bool mx = ctx->mixed();
-  BondOut o{d.hx, d.hy, d.hz, mx ? d.hfix : nullptr, d.n, ctx->fix.scale};
+  // bond vectors stay FP64 differences on both paths: the fixed-point ones
+  // cost the mixed path 40 % more force error (stiff bonds turn small
+  // length errors into large force errors) for 0.06 ms a long step
+  BondOut o{d.hx, d.hy, d.hz, mx ? d.hfix : nullptr, d.n, ctx->fix.scale, ctx->fix.scalef,
+            nullptr, (float)(ctx->boxl / 4294967296.0),
+            (float)(ctx->boyl / 4294967296.0), (float)(ctx->bozl / 4294967296.0)};
   const int T = 128;
   const double bx = ctx->boxl, by = ctx->boyl, bz = ctx->bozl;
   const int *nspec = d.nspec_d;
