@@ -311,15 +311,18 @@ __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
 // ------------------------------------------------------------------ GETEMP
 // ekin layout as the reference's EKIN: [0..ntypes-1] per type, then total,
 // VIRKX, VIRKY, VIRKZ.
+// NT >= ntypes: per-type sums carried (NT + 4 values reduced; the unused
+// types of ekacc are left alone).
+template <int NT>
 __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
                          int ntypes, const double *__restrict__ massdi,
                          const double *__restrict__ vx,
                          const double *__restrict__ vy,
                          const double *__restrict__ vz, double *ekacc,
                          double *part, unsigned *ctr) {
-  double e[MDX_NT + 4];
+  double e[NT + 4];
 #pragma unroll
-  for (int k = 0; k < MDX_NT + 4; ++k) e[k] = 0.0;
+  for (int k = 0; k < NT + 4; ++k) e[k] = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
     const int t = ainfo[i].x;
@@ -329,18 +332,20 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
     const double VVY = m * (vy[i] * vy[i]);
     const double VVZ = m * (vz[i] * vz[i]);
     const double VSC = VVX + VVY + VVZ;
-    e[MDX_NT + 1] += VVX;
-    e[MDX_NT + 2] += VVY;
-    e[MDX_NT + 3] += VVZ;
-    e[MDX_NT] += VSC;
+    e[NT + 1] += VVX;
+    e[NT + 2] += VVY;
+    e[NT + 3] += VVZ;
+    e[NT] += VSC;
 #pragma unroll
-    for (int k = 0; k < MDX_NT; ++k)
+    for (int k = 0; k < NT; ++k)
       if (k == t) e[k] += 0.5 * VSC;
   }
-  double *dst[MDX_NT + 4];
+  // value k < NT -> ekacc[k] (type k), NT + j -> ekacc[MDX_NT + j]
+  double *dst[NT + 4];
 #pragma unroll
-  for (int k = 0; k < MDX_NT + 4; ++k) dst[k] = (k < ntypes || k >= MDX_NT) ? ekacc + k : nullptr;
-  block_add_core<MDX_NT + 4>(e, dst, part, ctr);
+  for (int k = 0; k < NT + 4; ++k)
+    dst[k] = k < NT ? (k < ntypes ? ekacc + k : nullptr) : ekacc + MDX_NT + (k - NT);
+  block_add_core<NT + 4>(e, dst, part, ctr);
 }
 
 // Device scratch of SCALING between stages.
@@ -419,8 +424,8 @@ __device__ void reclen_dev(mdx_thermo *th, double sx, double sy, double sz) {
   th->vol = th->boxl * th->boyl * th->bozl;
 }
 
-__global__ void k_scal(int stage, ScalConst c, ScalScratch *ss, mdx_thermo *th,
-                       const mdx_scalars *s, int *err) {
+__device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_thermo *th,
+                           const mdx_scalars *s, int *err) {
   const double TSTEP = c.tstep, HTSTEP = c.htstep, FNST = c.fnst;
   const double DQT = c.dqt, DQP = c.dqp, RTP = c.rtp;
   const double VOL = th->vol;
@@ -655,6 +660,22 @@ __global__ void k_scal(int stage, ScalConst c, ScalScratch *ss, mdx_thermo *th,
       break;
     }
   }
+}
+
+__global__ void k_scal(int stage, ScalConst c, ScalScratch *ss, mdx_thermo *th,
+                       const mdx_scalars *s, int *err) {
+  scal_stage(stage, c, ss, th, s, err);
+}
+
+// Several consecutive SCALING stages in one launch (one thread, in order:
+// the same as one launch each).
+struct StageList {
+  int n;
+  int st[8];
+};
+__global__ void k_scal_list(StageList L, ScalConst c, ScalScratch *ss, mdx_thermo *th,
+                            const mdx_scalars *s, int *err) {
+  for (int k = 0; k < L.n; ++k) scal_stage(L.st[k], c, ss, th, s, err);
 }
 
 // Velocity (and position) scaling of the SCALING stages.
@@ -938,13 +959,42 @@ static int stage(mdx_ctx *ctx, int st) {
   return MDX_OK;
 }
 
-int launch_getemp(mdx_ctx *ctx) {
+// Queue of SCALING stages launched together; flushed before any kernel that
+// reads what they write (the per-atom scalings) or writes what they read.
+struct StageQ {
+  mdx_ctx *ctx;
+  StageList L{};
+  void push(int st) { L.st[L.n++] = st; }
+  int flush() {
+    if (!L.n) return MDX_OK;
+    k_scal_list<<<1, 1, 0, ctx->stream>>>(L, scal_const(ctx), scratch(ctx), ctx->dv.th,
+                                          ctx->dv.sc, ctx->dv.err);
+    MDX_LAUNCHED(ctx);
+    L.n = 0;
+    return MDX_OK;
+  }
+};
+
+// The kinetic-energy reduction of GETEMP; its fold is the ST_GETEMP stage.
+static int getemp_kernel(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
-  k_getemp<<<160, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), ctx->d.ntypes,
-                                         d.massdi, d.vx, d.vy, d.vz, scratch(ctx)->ekacc,
-                                         d.red_part, d.red_ctr);
+  const int nt = ctx->d.ntypes;
+#define GETEMP(NT)                                                                       \
+  k_getemp<NT><<<160, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), nt, d.massdi, \
+                                             d.vx, d.vy, d.vz, scratch(ctx)->ekacc,      \
+                                             d.red_part, d.red_ctr)
+  if (nt <= 1) GETEMP(1);
+  else if (nt <= 2) GETEMP(2);
+  else if (nt <= 4) GETEMP(4);
+  else GETEMP(MDX_NT);
+#undef GETEMP
   MDX_LAUNCHED(ctx);
-  return stage(ctx, ST_GETEMP);
+  return MDX_OK;
+}
+
+int launch_getemp(mdx_ctx *ctx) {
+  const int rc = getemp_kernel(ctx);
+  return rc ? rc : stage(ctx, ST_GETEMP);
 }
 
 static int scale_atoms(mdx_ctx *ctx, int mode) {
@@ -968,61 +1018,76 @@ static int scale_atoms(mdx_ctx *ctx, int mode) {
 int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
   MDX_TIMER(ctx, MDX_T_MOVE);
   const mdx_params &p = ctx->p;
+  StageQ q{ctx};
   if (pending_vscale) *pending_vscale = false;
   if (ial == 3 && p.lnvt) {
-    RC(stage(ctx, ST_3V));
+    q.push(ST_3V);
+    RC(q.flush());
     RC(scale_atoms(ctx, 0));
   }
-  RC(launch_getemp(ctx));
-  RC(stage(ctx, ST_PRESS));
+  RC(getemp_kernel(ctx));
+  q.push(ST_GETEMP);
+  q.push(ST_PRESS);
   if (ial == 1) {
     if (p.lnvt) {
-      RC(stage(ctx, ST_1A));
+      q.push(ST_1A);
       if (p.lnpt) {
+        RC(q.flush());
         RC(scale_atoms(ctx, 2));
-        RC(stage(ctx, ST_1RECLEN));
+        q.push(ST_1RECLEN);
       } else {
         // 3.4.3 calls GETEMP again on unchanged velocities: same values
-        RC(stage(ctx, ST_1NVT));
-        if (pending_vscale) *pending_vscale = true;
-        else RC(scale_atoms(ctx, 0));
+        q.push(ST_1NVT);
+        if (pending_vscale) {
+          *pending_vscale = true;
+        } else {
+          RC(q.flush());
+          RC(scale_atoms(ctx, 0));
+        }
       }
-      RC(stage(ctx, ST_EABS));
+      q.push(ST_EABS);
     }
   } else if (ial == 2) {
     if (p.lnvt) {
-      RC(stage(ctx, ST_2V));
+      q.push(ST_2V);
+      RC(q.flush());
       RC(scale_atoms(ctx, 0));
       if (p.lnpt) {
-        RC(stage(ctx, ST_2NPTV));
+        q.push(ST_2NPTV);
+        RC(q.flush());
         RC(scale_atoms(ctx, 3));
-        RC(launch_getemp(ctx));
-        RC(stage(ctx, ST_2SCL));
+        RC(getemp_kernel(ctx));
+        q.push(ST_GETEMP);
+        q.push(ST_2SCL);
       } else {
-        RC(launch_getemp(ctx));
+        RC(getemp_kernel(ctx));
+        q.push(ST_GETEMP);
       }
-      RC(stage(ctx, ST_2SC));
+      q.push(ST_2SC);
     }
   } else if (ial == 3) {
     if (p.lnvt) {
-      RC(stage(ctx, ST_3A));
+      q.push(ST_3A);
       if (p.lnpt) {
+        RC(q.flush());
         DevData &d = ctx->dv;
         k_com_scale<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
             d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, mol_const(ctx),
             move_const(ctx), scratch(ctx), d.vx, d.vy, d.vz, d.pos);
         MDX_LAUNCHED(ctx);
-        RC(stage(ctx, ST_3B));
+        q.push(ST_3B);
       }
-      RC(stage(ctx, ST_EABS));
+      q.push(ST_EABS);
     }
   }
   if (p.lsclt && (ial == 2 || ial == 3)) {
-    RC(stage(ctx, ST_SCLT));
+    q.push(ST_SCLT);
+    RC(q.flush());
     RC(scale_atoms(ctx, 0));
-    RC(launch_getemp(ctx));
+    RC(getemp_kernel(ctx));
+    q.push(ST_GETEMP);
   }
-  return MDX_OK;
+  return q.flush();
 }
 
 int launch_mstep1_rescale(mdx_ctx *ctx) {
