@@ -513,7 +513,7 @@ int mdx_close(mdx_ctx *ctx) {
   void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.stab, d.pinfo, d.moltpl, d.vx, d.massdi, d.amass, d.qsite,
                   d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
                   d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
-                  d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f,
+                  d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f, d.abf,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
@@ -741,6 +741,7 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
   if (!d.a6lj) {
     RC(dmalloc(ctx, &d.a6lj, 6 * nn));
     RC(dmalloc(ctx, &d.a6f, 6 * nn));
+    RC(dmalloc(ctx, &d.abf, 3 * nn));
   }
   d.b12lj = d.a6lj + nn; d.a6lj0 = d.b12lj + nn; d.b12lj0 = d.a6lj0 + nn;
   d.a6_14 = d.b12lj0 + nn; d.b12_14 = d.a6_14 + nn;
@@ -758,6 +759,7 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
       }
   RC(upload(ctx, d.a6lj, lj.data(), lj.size()));
   RC(upload(ctx, d.a6f, ljf.data(), ljf.size()));
+  RC(pack_lj_tables(ctx));
   ctx->h_a6lj0.assign(lj.begin() + 2 * nn, lj.begin() + 3 * nn);
   ctx->h_b12lj0.assign(lj.begin() + 3 * nn, lj.begin() + 4 * nn);
   ctx->h_inbt.assign(t->inbt, t->inbt + ns);
@@ -1175,6 +1177,7 @@ int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2, double bee) 
   RC(upload(ctx, d.b12lj, b12.data(), nn));
   RC(upload(ctx, d.a6f, a6f.data(), nn));
   RC(upload(ctx, d.b12f, b12f.data(), nn));
+  RC(pack_lj_tables(ctx));
   ctx->p.raex = bee * (1. - std::pow(ec, pw2));
   ctx->p.ec_me = ec;
   ctx->pc.raex = ctx->p.raex;

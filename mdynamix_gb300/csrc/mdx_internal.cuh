@@ -161,6 +161,7 @@ struct DevData {
   // LJ tables [i*nnbt + j]
   double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
+  float2 *abf;  // (A6, B12) FP32 pairs for the mixed sweeps: inter, intra, 1-4
   // bonded
   int nrbb, nraa, nrtt, nrbt, nrat, nrrt;
   int *bid, *bib, *bjb;
@@ -515,6 +516,7 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
 // pair.cu
 int launch_localf(mdx_ctx *ctx, bool split, bool ener = true);
+int pack_lj_tables(mdx_ctx *ctx);  // abf from the FP32 tables
 int launch_forces_long(mdx_ctx *ctx, bool split);
 int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 // ewald.cu

@@ -25,6 +25,8 @@ namespace {
 struct PairTables {
   const double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   const float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
+  const float2 *abf;  // (A6, B12) FP32 pairs: [kind][i*nnbt + j], kind 0 inter, 1 intra, 2 1-4
+  int nn;             // nnbt^2
 };
 
 // Output slots of one pair sweep.
@@ -281,6 +283,11 @@ __global__ void __launch_bounds__(256) k_pair32(
     const float qsi = sti.y;
     const float coulf = (float)pc.coulf, alphad = (float)pc.alphad;
     const float raex = (float)pc.raex;
+    // per-owner constants of the type tables, hoisted out of the row
+    const int eei = tc.iee[ti], lmovei = tc.lmove[ti];
+    const float c14e = tc.c14elf[ti], c14l = tc.c14ljf[ti];
+    const float qsc = qsi * coulf, qic = qi * coulf;
+    const float2 *abrow = tb.abf + ni * pc.nnbt;
     const int c = cnt[i];
     float fxa = 0.f, fya = 0.f, fza = 0.f;
     const int *row = idx + list_slot(i, 0, cap, SHORT);
@@ -299,23 +306,19 @@ __global__ void __launch_bounds__(256) k_pair32(
       const float4 stj = __ldg(&stab[(unsigned)pj.w & SITE_MASK]);
       const int tj = __float_as_int(stj.w), nj = __float_as_int(stj.z);
       const bool same = ((unsigned)pj.w >> MDX_SITE_BITS) == mi;
-      const int tix = ni * pc.nnbt + nj;
+      // one (A6, B12) load: inter-molecular, intra-molecular or 1-4 table
+      const int kind = same ? (is14 ? 2 : 1) : 0;
+      const float2 ab = __ldg(&abrow[kind * tb.nn + nj]);
       float QIJ, A6, B12, RAE = 0.f;
       if (same) {
-        if (is14) {
-          QIJ = qsi * stj.y * coulf * tc.c14elf[ti];
-          A6 = __ldg(&tb.a614f[tix]) * tc.c14ljf[ti];
-          B12 = __ldg(&tb.b1214f[tix]) * tc.c14ljf[ti];
-        } else {
-          QIJ = qsi * stj.y * coulf;
-          A6 = __ldg(&tb.a60f[tix]);
-          B12 = __ldg(&tb.b120f[tix]);
-        }
+        QIJ = is14 ? qsc * stj.y * c14e : qsc * stj.y;
+        A6 = is14 ? ab.x * c14l : ab.x;
+        B12 = is14 ? ab.y * c14l : ab.y;
       } else {
-        QIJ = qi * stj.x * coulf;
-        A6 = __ldg(&tb.a6f[tix]);
-        B12 = __ldg(&tb.b12f[tix]);
-        if (pc.lmdee) RAE = (tc.iee[ti] * tc.iee[tj] == 0) ? raex : 0.f;
+        QIJ = qic * stj.x;
+        A6 = ab.x;
+        B12 = ab.y;
+        if (pc.lmdee) RAE = (eei * tc.iee[tj] == 0) ? raex : 0.f;
       }
       const float DX = idiff(pi.x, pj.x, sx);
       const float DY = idiff(pi.y, pj.y, sy);
@@ -326,9 +329,9 @@ __global__ void __launch_bounds__(256) k_pair32(
       const float R1EI = RAE == 0.f ? R1I : __fdividef(1.f, R1 + RAE);
       const float R1E = R1 + RAE;
       float EE1, EES, FORCE;
-      if (is14 || (same && tc.iee[ti] == 0)) {
+      if (is14 || (same && eei == 0)) {
         EE1 = QIJ * R1I;
-        FORCE = tc.lmove[ti] ? EE1 * (R1I * R1I) : 0.f;
+        FORCE = lmovei ? EE1 * (R1I * R1I) : 0.f;
         EES = EE1;
       } else if (pc.lmnbl) {
         const float rff = (float)pc.rff, rff2 = (float)pc.rff2;
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(256) k_pair32(
         bool count_esr_split = true;
         if (same) {
           if (SHORT) {
-            if (tc.lmove[ti]) {
+            if (lmovei) {
               if (ENER) a[P_VIR] += FSR * R1;
             } else {
               ESR = 0.f;
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(256) k_pair32(
               count_esr_split = false;
             }
           } else {
-            if (ENER && tc.lmove[ti]) a[P_VIR] += FSR * R1;
+            if (ENER && lmovei) a[P_VIR] += FSR * R1;
           }
           if (count_esr_split) {
             if (ENER) a[P_ESR_SAME] += ESR;
@@ -390,7 +393,7 @@ __global__ void __launch_bounds__(256) k_pair32(
         }
         if (ENER) a[P_ESR] += ESR;
       }
-      if (SHORT || !same || tc.lmove[ti]) {
+      if (SHORT || !same || lmovei) {
         if (ENER) a[P_VX] += FORCE * (DX * DX);
         if (ENER) a[P_VY] += FORCE * (DY * DY);
         if (ENER) a[P_VZ] += FORCE * (DZ * DZ);
@@ -506,7 +509,17 @@ __global__ void k_fold_split(double *split, mdx_scalars *sc) {
 
 PairTables tables(const DevData &d) {
   return PairTables{d.a6lj, d.b12lj, d.a6lj0, d.b12lj0, d.a6_14, d.b12_14,
-                    d.a6f,  d.b12f,  d.a60f,  d.b120f,  d.a614f, d.b1214f};
+                    d.a6f,  d.b12f,  d.a60f,  d.b120f,  d.a614f, d.b1214f,
+                    d.abf,  d.nnbt * d.nnbt};
+}
+
+__global__ void k_pack_lj(int nn, const float *__restrict__ f, float2 *__restrict__ abf) {
+  // f: a6f, b12f, a60f, b120f, a614f, b1214f back to back (nn each)
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nn) return;
+  abf[k] = make_float2(f[k], f[nn + k]);
+  abf[nn + k] = make_float2(f[2 * nn + k], f[3 * nn + k]);
+  abf[2 * nn + k] = make_float2(f[4 * nn + k], f[5 * nn + k]);
 }
 
 // ener = false: forces only (an intermediate short step of DOUBLE, whose fast
@@ -576,6 +589,18 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
 }
 
 }  // namespace
+
+// The interleaved FP32 (A6, B12) tables of the mixed sweeps, from the FP32
+// tables (after the topology upload and every RECINT).
+int pack_lj_tables(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  const int nn = d.nnbt * d.nnbt;
+  if (!d.abf || nn <= 0) return MDX_OK;
+  k_pack_lj<<<(nn + 127) / 128, 128, 0, ctx->stream>>>(nn, d.a6f, d.abf);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
 
 int launch_localf(mdx_ctx *ctx, bool split, bool ener) {
   MDX_TIMER(ctx, MDX_T_PAIR_SHORT); return launch_pair(ctx, true, split, ener); }
