@@ -258,19 +258,21 @@ __global__ void __launch_bounds__(256) k_pair32(
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
     __syncthreads();
   }
-  // short rows (about 50 entries): thread per owner atom over its tiled row
-  // (list_slot), entry k of the warp's 32 atoms in one 128-byte line; long
-  // rows (several hundred entries): warp per owner atom, lanes stride the row
+  // short rows (about 50 entries): two threads per owner atom over its tiled
+  // row (list_slot; entry k of 32 atoms in one 128-byte line), even and odd
+  // entries; long rows (several hundred entries): warp per owner atom, lanes
+  // stride the row
   const int lane = threadIdx.x & 31;
-  const int i = SHORT ? blockIdx.x * blockDim.x + threadIdx.x
+  const int i = SHORT ? (blockIdx.x * blockDim.x + threadIdx.x) >> 1
                       : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int k0 = SHORT ? 0 : lane, kstep = SHORT ? 1 : 32;
+  const int k0 = SHORT ? (lane & 1) : lane, kstep = SHORT ? 2 : 32;
   long long tot[P_NSLOT];
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
   float a[P_NSLOT];
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) a[k] = 0.f;
+  long long qx = 0, qy = 0, qz = 0;
   if (i < n) {
     // one 16-byte record per atom: fixed-point x, y, z and (molecule, site);
     // charges and types come from the per-site table (L1-resident)
@@ -406,18 +408,28 @@ __global__ void __launch_bounds__(256) k_pair32(
     }
     // forces: lane partials -> fixed point (-> integer warp sum) -> one store
     // (no 64-bit conversion instruction: those issue on the FP64 pipe)
-    long long qx = f2ll_rn(fxa * fsc.scalef);
-    long long qy = f2ll_rn(fya * fsc.scalef);
-    long long qz = f2ll_rn(fza * fsc.scalef);
-    if (!SHORT) {
+    qx = f2ll_rn(fxa * fsc.scalef);
+    qy = f2ll_rn(fya * fsc.scalef);
+    qz = f2ll_rn(fza * fsc.scalef);
+    if (!SHORT) {  // the whole warp shares the owner: uniform branch
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         qx += __shfl_xor_sync(0xffffffffu, qx, o);
         qy += __shfl_xor_sync(0xffffffffu, qy, o);
         qz += __shfl_xor_sync(0xffffffffu, qz, o);
       }
+      if (lane == 0) {
+        ffix[i] = (unsigned long long)qx;
+        ffix[n + i] = (unsigned long long)qy;
+        ffix[2 * n + i] = (unsigned long long)qz;
+      }
     }
-    if (SHORT || lane == 0) {
+  }
+  if (SHORT) {  // the owner's two threads are adjacent lanes; every lane takes part
+    qx += __shfl_xor_sync(0xffffffffu, qx, 1);
+    qy += __shfl_xor_sync(0xffffffffu, qy, 1);
+    qz += __shfl_xor_sync(0xffffffffu, qz, 1);
+    if (i < n && (lane & 1) == 0) {
       ffix[i] = (unsigned long long)qx;
       ffix[n + i] = (unsigned long long)qy;
       ffix[2 * n + i] = (unsigned long long)qz;
@@ -558,7 +570,7 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
-    const int grid32 = shrt ? (d.n + T - 1) / T : grid;  // short: thread per atom
+    const int grid32 = shrt ? (2 * d.n + T - 1) / T : grid;  // short: 2 threads per atom
 #define LP32(S, P)                                                                \
   if (ener) k_pair32<S, P, true><<<grid32, T, 0, ctx->stream>>>(                  \
       d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
