@@ -143,13 +143,18 @@ __global__ void __launch_bounds__(BLK) k_build(
     const int *__restrict__ cell_list, double short2, double rl2, int cap_s,
     int cap_l, int *__restrict__ ns_cnt, int *__restrict__ nl_cnt,
     int *__restrict__ ns_idx, int *__restrict__ nl_idx, int *__restrict__ err,
-    int *__restrict__ need, int full) {
+    int *__restrict__ need, int full, const int4 *__restrict__ posi, float sxf, float syf,
+    float szf) {
+  // posi (mixed path): the prefilter takes the wrapped differences of the
+  // fixed-point positions and the molecule from their packed word, one
+  // 16-byte gather per candidate
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (BLK / 32) + (threadIdx.x >> 5);
   if (i >= n) return;
   const dbl4 pi = pos[i];
   const float4 pf = posf[i];
   const int imol = ainfo[i].y;
+  const int4 qi = posi ? posi[i] : make_int4(0, 0, 0, 0);
   const int c0 = atom_cell[i];
   const int cx0 = c0 % g.nx, cy0 = (c0 / g.nx) % g.ny, cz0 = c0 / (g.nx * g.ny);
   const float fbx = (float)b.bx, fby = (float)b.by, fbz = (float)b.bz;
@@ -174,14 +179,30 @@ __global__ void __launch_bounds__(BLK) k_build(
           if (base + lane < e) {
             j = cell_list[base + lane];
             if (j != i && (full || owns(i, j))) {
-              bool same = ainfo[j].y == imol;
+              int4 qj;
+              bool same;
+              if (posi) {
+                qj = posi[j];
+                same = ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS);
+              } else {
+                same = ainfo[j].y == imol;
+              }
               if (same) {
                 kind = classify_exact(i, j, true, pi, pos[j], b, short2, rl2,
                                       nnbb, inbb, nbdmax);
               } else {
-                float4 q = posf[j];
-                float dx = pf.x - q.x, dy = pf.y - q.y, dz = pf.z - q.z;
-                pbc_rectf(dx, dy, dz, fbx, fby, fbz, fhx, fhy, fhz);
+                float dx, dy, dz;
+                if (posi) {
+                  dx = (float)(int)((unsigned)qi.x - (unsigned)qj.x) * sxf;
+                  dy = (float)(int)((unsigned)qi.y - (unsigned)qj.y) * syf;
+                  dz = (float)(int)((unsigned)qi.z - (unsigned)qj.z) * szf;
+                } else {
+                  const float4 q = posf[j];
+                  dx = pf.x - q.x;
+                  dy = pf.y - q.y;
+                  dz = pf.z - q.z;
+                  pbc_rectf(dx, dy, dz, fbx, fby, fbz, fhx, fhy, fhz);
+                }
                 float d2 = dx * dx + dy * dy + dz * dz;
                 if (d2 > rl2f_hi) {
                   kind = 0;
@@ -336,7 +357,9 @@ int launch_build_lists(mdx_ctx *ctx) {
       d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,
       d.cell_start, d.cell_list, ctx->p.rshort * ctx->p.rshort, rl * rl,
       d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
-      ctx->mixed() ? 1 : 0);
+      ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,
+      (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),
+      (float)(ctx->bozl / 4294967296.0));
   MDX_LAUNCHED(ctx);
   MDX_CUDA(cudaMemsetAsync(&d.sc->mbsh, 0, sizeof(int) * 2, ctx->stream));
   k_count_totals<<<64, 256, 0, ctx->stream>>>(d.n, d.ns_cnt, d.nl_cnt, d.sc);
