@@ -105,6 +105,8 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start,
   }
 }
 
+constexpr int CELL_REACH = 1;  // list cells per list radius (2 measured slower: 125 thin cells)
+
 // Ownership of pair (i, j) in the strip loop: i owns it when (i-j) is even
 // and j < i, or (i-j) is odd and j > i (forces.f:1834, 2014).
 __device__ __forceinline__ bool owns(int i, int j) {
@@ -162,15 +164,16 @@ __global__ void __launch_bounds__(BLK) k_build(
   const float rl2f_hi = (float)(rl2 * (1.0 + 1e-4)), rl2f_lo = (float)(rl2 * (1.0 - 1e-4));
   const float s2f_hi = (float)(short2 * (1.0 + 1e-4)), s2f_lo = (float)(short2 * (1.0 - 1e-4));
   int ns = 0, nl = 0;
-  const int ox0 = g.nx >= 3 ? -1 : 0, ox1 = g.nx >= 3 ? 1 : g.nx - 1;
-  const int oy0 = g.ny >= 3 ? -1 : 0, oy1 = g.ny >= 3 ? 1 : g.ny - 1;
-  const int oz0 = g.nz >= 3 ? -1 : 0, oz1 = g.nz >= 3 ? 1 : g.nz - 1;
+  constexpr int R = CELL_REACH, W = 2 * CELL_REACH + 1;
+  const int ox0 = g.nx >= W ? -R : 0, ox1 = g.nx >= W ? R : g.nx - 1;
+  const int oy0 = g.ny >= W ? -R : 0, oy1 = g.ny >= W ? R : g.ny - 1;
+  const int oz0 = g.nz >= W ? -R : 0, oz1 = g.nz >= W ? R : g.nz - 1;
   for (int oz = oz0; oz <= oz1; ++oz)
     for (int oy = oy0; oy <= oy1; ++oy)
       for (int ox = ox0; ox <= ox1; ++ox) {
-        int cx = g.nx >= 3 ? (cx0 + ox + g.nx) % g.nx : ox;
-        int cy = g.ny >= 3 ? (cy0 + oy + g.ny) % g.ny : oy;
-        int cz = g.nz >= 3 ? (cz0 + oz + g.nz) % g.nz : oz;
+        int cx = g.nx >= W ? (cx0 + ox + g.nx) % g.nx : ox;
+        int cy = g.ny >= W ? (cy0 + oy + g.ny) % g.ny : oy;
+        int cz = g.nz >= W ? (cz0 + oz + g.nz) % g.nz : oz;
         int c = (cz * g.ny + cy) * g.nx + cx;
         int s = cell_start[c], e = cell_start[c + 1];
         for (int base = s; base < e; base += 32) {
@@ -311,11 +314,12 @@ int launch_build_lists(mdx_ctx *ctx) {
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
          0.5 * ctx->bozl};
   CellGrid g;
-  g.nx = std::max(1, (int)std::floor(ctx->boxl / rl));
-  g.ny = std::max(1, (int)std::floor(ctx->boyl / rl));
-  g.nz = std::max(1, (int)std::floor(ctx->bozl / rl));
-  // the stencil needs cells at least rl wide; below 3 cells a dimension is
-  // scanned whole
+  // cells at least rl / CELL_REACH wide, stencil +-CELL_REACH cells (a
+  // (2 R + 1)^3 stencil of thinner cells tests fewer far candidates than
+  // 27 cells of width rl); below 2 R + 1 cells a dimension is scanned whole
+  g.nx = std::max(1, (int)std::floor(CELL_REACH * ctx->boxl / rl));
+  g.ny = std::max(1, (int)std::floor(CELL_REACH * ctx->boyl / rl));
+  g.nz = std::max(1, (int)std::floor(CELL_REACH * ctx->bozl / rl));
   g.cx = ctx->boxl / g.nx;
   g.cy = ctx->boyl / g.ny;
   g.cz = ctx->bozl / g.nz;
