@@ -80,9 +80,10 @@ struct MolConst {
   double summas[MDX_NT];
 };
 
-// GETCOM (service.f:463-563); with posf set it also refreshes the FP32 and
-// fixed-point mirrors of the wrapped positions (what k_mirror writes), so a
-// short step needs no separate mirror pass.
+// GETCOM (service.f:463-563); with posi set it also refreshes the
+// fixed-point mirror of the wrapped positions (what k_mirror writes for the
+// sweeps), so a short step needs no separate mirror pass.  The FP32 mirror
+// posf only feeds the list build, which refreshes it itself.
 __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
                          const int *__restrict__ mol_nat,
                          const int *__restrict__ mol_type,
@@ -118,16 +119,13 @@ __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
     p.y = (p.y - y) + yw;
     p.z = (p.z - z) + zw;
     pos[f + k] = p;
-    if (posf) {
-      posf[f + k] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
-      if (posi) {
-        const long long xi = __double2ll_rn(p.x * ibx * two32);
-        const long long yi = __double2ll_rn(p.y * iby * two32);
-        const long long zi = __double2ll_rn(p.z * ibz * two32);
-        posi[f + k] = make_int4((int)(unsigned)(unsigned long long)xi,
-                                (int)(unsigned)(unsigned long long)yi,
-                                (int)(unsigned)(unsigned long long)zi, pinfo[f + k]);
-      }
+    if (posi) {
+      const long long xi = __double2ll_rn(p.x * ibx * two32);
+      const long long yi = __double2ll_rn(p.y * iby * two32);
+      const long long zi = __double2ll_rn(p.z * ibz * two32);
+      posi[f + k] = make_int4((int)(unsigned)(unsigned long long)xi,
+                              (int)(unsigned)(unsigned long long)yi,
+                              (int)(unsigned)(unsigned long long)zi, pinfo[f + k]);
     }
   }
 }
@@ -194,8 +192,8 @@ __global__ void k_kick_drift(int n, const int4 *__restrict__ ainfo, MoveConst mv
 // One short step of DOUBLE's inner loop up to the fast forces, thread per
 // molecule: the kick and drift of k_kick_drift for each of its atoms
 // (mdstep.f:383-397), then GETCOM's centre of mass and wrap (service.f:
-// 463-563) and the position mirrors, all in the order the separate kernels
-// use.  hfix (mixed path): the previous short step's fast forces are read
+// 463-563) and the fixed-point mirror, all in the order the separate
+// kernels use.  hfix (mixed path): the previous short step's fast forces are read
 // as fixed point, so that step needs no fold to FP64.
 __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
                                  const int *__restrict__ mol_nat,
@@ -267,7 +265,6 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
     p.y = (p.y - y) + yw;
     p.z = (p.z - z) + zw;
     pos[f + k] = p;
-    posf[f + k] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
     if (posi) {
       const long long xi = __double2ll_rn(p.x * ibx * two32);
       const long long yi = __double2ll_rn(p.y * iby * two32);
@@ -1161,7 +1158,7 @@ int launch_getcom(mdx_ctx *ctx, bool mirror) {
   DevData &d = ctx->dv;
   k_getcom<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z,
-      mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl, mirror ? d.posf : nullptr,
+      mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl, nullptr,
       mirror && ctx->mixed() ? d.posi : nullptr, d.pinfo);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
