@@ -55,12 +55,12 @@ OPS_EW_K = 20            # per k-vector (energy, virial, W)
 # group's kernels in one long step, MB).
 # fp64 ewald: k_tables 43.4 + k_sfac 125.8 + k_sfac_sum 51.3 + k_kterms 0.3
 #             + k_wpairs 0.6 + k_rforce64 102.9
-# mixed ewald: k_tables 3.2 + k_zimages 62.7 + k_sfac_tc 78.3 + partial sums 22.9
+# mixed ewald: k_tables 3.2 + k_zimages 17.9 + k_sfac32 52.6 + k_sfac_sum 24.3
 #              + k_kterms 0.3 + k_wtiles 0.6 + k_rforce_tc 75.8
 # fp64 pair: 9 x 30.7 (short, forces) + 30.7 (short, energies) + 152.9 (long)
 # mixed pair: 9 x 24.3 + 24.3 + 278.8
 TRAFFIC_MB = {
-    ("fp64", "ewald"): 324.3, ("mixed", "ewald"): 243.8,
+    ("fp64", "ewald"): 324.3, ("mixed", "ewald"): 174.7,
     ("fp64", "pair"): 460.7, ("mixed", "pair"): 522.0,
 }
 
@@ -134,7 +134,7 @@ def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps
     step; peak = measured FMA throughput of the pipe the path computes on."""
     ms = {k: v[0] / nsteps for k, v in timers.items()}
     nkv, ncol, npair, rows = kset
-    ew_kernels = ("k_tables + k_zimages + k_sfac_tc + partial sums + k_kterms + k_wtiles + "
+    ew_kernels = ("k_tables + k_zimages + k_sfac32 + k_sfac_sum + k_kterms + k_wtiles + "
                   "k_rforce_tc (TF32 tensor cores)" if prec == "mixed" else
                   "k_tables + k_sfac + k_sfac_sum + k_kterms + k_wpairs + k_rforce64")
     groups = {
