@@ -40,11 +40,17 @@ constexpr int TC_N = 128;          // accumulator columns per tile (32 k-columns
 constexpr int TC_COLS = TC_N / 4;  // k-columns per tile
 constexpr uint32_t TC_POLLS = 1u << 20;  // bounded mbarrier waits
 
-// Force-pass operand layout: element (row r, k) of a K-major, unswizzled tile
-// of kp columns sits in core matrix (r / 8, k / 4) of 128 bytes: SBO = 32 kp,
-// LBO = 128.
-__host__ __device__ __forceinline__ uint32_t core_off(int r, int k, int kp) {
-  return (uint32_t)((((r >> 3) * (kp >> 2) + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
+// Force-pass operand layout (128 rows, K-major, unswizzled), K-step major:
+// the 8 K of MMA step s = k / 8 fill 8 KB, [hi | lo] of 4 KB each, and
+// within a part core matrix (r / 8, k / 4) of 128 bytes sits at
+// ((k / 4) % 2) 2048 + (r / 8) 128: LBO (along K) = 2048, SBO (along M/N)
+// = 128.  A tile whose columns need ks steps is then its first ks x 8 KB.
+constexpr uint32_t TC_STEP = 8192;  // bytes of one K step (hi and lo)
+constexpr uint32_t TC_LO = 4096;    // lo part within a step
+constexpr uint32_t TC_LBO = 2048, TC_SBO = 128;
+__host__ __device__ __forceinline__ uint32_t core_off(int r, int k) {  // hi part
+  return (uint32_t)((k >> 3) * TC_STEP + ((k >> 2) & 1) * TC_LBO + (r >> 3) * TC_SBO +
+                    ((r & 7) << 4) + ((k & 3) << 2));
 }
 
 // S-pass operand layout: 32 atoms (K) per chunk, core matrices along K
@@ -65,7 +71,7 @@ __host__ __device__ __forceinline__ uint32_t sk_bpart(int np) {  // bytes of one
 
 // Z images of one step: thread per (p, atom), atoms up to ldn (rows past n
 // are zero in the table).  zf: force-pass A operand, per 128-atom tile
-// [hi | lo] of 128 x kp; zs: S-pass B operand, per 32-atom chunk [hi | lo]
+// kp / 8 K steps of [hi | lo]; zs: S-pass B operand, per 32-atom chunk [hi | lo]
 // of np x 32.  Entries with p >= kz stay zero (set once at allocation).
 __global__ void k_zimages(int ldn, int kz, int kp, int np, const float2 *__restrict__ tz,
                           unsigned char *__restrict__ zf, unsigned char *__restrict__ zs) {
@@ -78,9 +84,9 @@ __global__ void k_zimages(int ldn, int kz, int kp, int np, const float2 *__restr
   tc::tf32_split(z.y, bh, bl);
   if (zf) {
     unsigned char *base = zf + (size_t)(i >> 7) * 1024 * kp;
-    const uint32_t o = core_off(i & 127, 2 * p, kp);  // k = 2p and 2p + 1: adjacent
+    const uint32_t o = core_off(i & 127, 2 * p);  // k = 2p and 2p + 1: adjacent
     *reinterpret_cast<float2 *>(base + o) = make_float2(ah, bh);
-    *reinterpret_cast<float2 *>(base + 512 * kp + o) = make_float2(al, bl);
+    *reinterpret_cast<float2 *>(base + TC_LO + o) = make_float2(al, bl);
   }
   if (zs) {
     const uint32_t bp = sk_bpart(np);
@@ -144,19 +150,18 @@ __global__ void k_wtiles(int ntile, int kp, const int *__restrict__ slot,
   tc::tf32_split(v[1], hi.y, lo.y);
   tc::tf32_split(v[2], hi.z, lo.z);
   tc::tf32_split(v[3], hi.w, lo.w);
-  const size_t tsz = (size_t)TC_N * kp;  // floats per part
-  float *base = tw + (size_t)tile * 2 * tsz + core_off(r, 4 * kc, kp) / 4;
+  float *base = tw + (size_t)tile * 2 * TC_N * kp + core_off(r, 4 * kc) / 4;
   *reinterpret_cast<float4 *>(base) = hi;
-  *reinterpret_cast<float4 *>(base + tsz) = lo;
+  *reinterpret_cast<float4 *>(base + TC_LO / 4) = lo;
 }
 
-// Force pass: one CTA per 128 atoms, warp-specialised.  Warp 8 (lane 0) is
+// Force pass: one CTA per 128 atoms, warp-specialised.  Warp 16 (lane 0) is
 // the producer: bulk copies (once: the tile's Z image, its X and Y rows as
-// one TMA box, the epilogue records of all column tiles; then each B tile)
-// and the MMAs.  Warps 0-15 are the epilogue: warp w reads the accumulator
+// one TMA box, the epilogue records of all column tiles; then the first
+// ks K steps of each B tile) and the MMAs.  Warps 0-15 are the epilogue: warp w reads the accumulator
 // lanes 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31 of each tile (8 of
-// its k-columns).  Shared memory (1024-byte aligned): A hi | A lo | B0 hi |
-// B0 lo | B1 hi | B1 lo | X, Y rows ([row][atom], float2) | records.
+// its k-columns).  Shared memory (1024-byte aligned): A | B0 | B1 (K steps
+// of [hi | lo]) | X, Y rows ([row][atom], float2) | records.
 // Barriers: abar (A, X, Y, records landed), bfull[b] (B tile in buffer b
 // landed), mdone[b] (MMAs into accumulator b done: B buffer b free,
 // accumulator b readable), afree[b] (the 16 epilogue warps are done with
@@ -187,10 +192,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
   unsigned char *dsm = dsm_raw + pad;
   const uint32_t sbase = raw + pad;
-  const uint32_t part = (uint32_t)TC_M * kp * 4;    // bytes of one hi or lo tile
-  const uint32_t btile = 2 * part;               // bytes of one B tile
+  const uint32_t btile = (uint32_t)TC_M * kp * 8;  // bytes of one operand tile (hi, lo)
   const int kxy = kx + ky;
-  const uint32_t sA = sbase, sB = sbase + 2 * part, oXY = 2 * part + 2 * btile;
+  const uint32_t sA = sbase, sB = sbase + btile, oXY = 3 * btile;
   const uint32_t oRec = oXY + (uint32_t)kxy * TC_M * 8;
 
   if (warp == 0) {
@@ -215,16 +219,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
   if (warp == TC_EPI_WARPS) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      auto copy_b = [&](int t, int b) {
+      auto copy_b = [&](int t, int b) {  // the K steps tile t uses
         const uint32_t bar = tc::smem_addr(&bfull[b]);
-        tc::mbar_arrive_expect_tx(bar, btile);
-        tc::bulk_g2s(sB + (uint32_t)b * btile, tw + (size_t)t * btile, btile, bar);
+        const uint32_t bytes = (uint32_t)tile_ks[t] * TC_STEP;
+        tc::mbar_arrive_expect_tx(bar, bytes);
+        tc::bulk_g2s(sB + (uint32_t)b * btile, tw + (size_t)t * btile, bytes, bar);
       };
       {
         const uint32_t bar = tc::smem_addr(&abar);
         const uint32_t recb = (uint32_t)ntile * TC_REC_BYTES;
-        tc::mbar_arrive_expect_tx(bar, 2 * part + (uint32_t)kxy * TC_M * 8 + recb);
-        tc::bulk_g2s(sA, zimg + (size_t)blockIdx.x * 2 * part, 2 * part, bar);
+        tc::mbar_arrive_expect_tx(bar, btile + (uint32_t)kxy * TC_M * 8 + recb);
+        tc::bulk_g2s(sA, zimg + (size_t)blockIdx.x * btile, btile, bar);
         tc::tma_load_2d(sbase + oXY, &tmxy, 2 * i0, 0, bar);
         if (recb) tc::bulk_g2s(sbase + oRec, meta, recb, bar);
       }
@@ -232,7 +237,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
       if (ntile > 1) copy_b(1, 1);
       if (!tc::mbar_wait(tc::smem_addr(&abar), 0u, TC_POLLS)) ok = false;
       const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
-      const uint32_t lbo = 128, sbo = 32u * kp;
       for (int t = 0; t < ntile; ++t) {
         const int b = t & 1;
         if (!tc::mbar_wait(tc::smem_addr(&bfull[b]), (uint32_t)(t >> 1) & 1u, TC_POLLS))
@@ -243,12 +247,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rforce_tc(
         tc::fence_after_sync();
         const int ks = tile_ks[t];
         const uint32_t d = tbase + (uint32_t)(b * TC_N);
-        const uint32_t bh = sB + (uint32_t)b * btile, bl = bh + part;
+        const uint32_t bh = sB + (uint32_t)b * btile;
         for (int s = 0; s < ks; ++s) {
-          const uint32_t ko = (uint32_t)s * 256;  // 8 TF32 = two core matrices along K
-          const uint64_t ah = tc::sdesc(sA + ko, lbo, sbo);
-          const uint64_t al = tc::sdesc(sA + part + ko, lbo, sbo);
-          const uint64_t bhd = tc::sdesc(bh + ko, lbo, sbo), bld = tc::sdesc(bl + ko, lbo, sbo);
+          const uint32_t ko = (uint32_t)s * TC_STEP;  // 8 TF32 = two core matrices along K
+          const uint64_t ah = tc::sdesc(sA + ko, TC_LBO, TC_SBO);
+          const uint64_t al = tc::sdesc(sA + ko + TC_LO, TC_LBO, TC_SBO);
+          const uint64_t bhd = tc::sdesc(bh + ko, TC_LBO, TC_SBO);
+          const uint64_t bld = tc::sdesc(bh + ko + TC_LO, TC_LBO, TC_SBO);
           tc::mma_tf32(d, ah, bhd, idesc, s > 0 ? 1u : 0u);
           tc::mma_tf32(d, ah, bld, idesc, 1u);
           tc::mma_tf32(d, al, bhd, idesc, 1u);
@@ -796,7 +801,7 @@ int tc_force_launch(mdx_ctx *ctx) {
                 tc_smem_bytes(d.tc_kp, d.kx + d.ky, d.tc_ntile), ctx->stream>>>(
       d.n, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
       reinterpret_cast<const unsigned char *>(d.tc_w), d.tc_zimg, tm, d.kx, d.ky, ctx->fix,
-      d.gfix, d.err);
+      d.efix, d.err);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -36,14 +36,22 @@ __global__ void k_zero_scalars(mdx_scalars *sc, int which, int molint, int ntype
   }
 }
 
+// f2 (optional): a second fixed-point part, added as integers first.
 __global__ void k_fix_fold(int n, const unsigned long long *__restrict__ f,
-                           double inv, double *__restrict__ x,
-                           double *__restrict__ y, double *__restrict__ z) {
+                           const unsigned long long *__restrict__ f2, double inv,
+                           double *__restrict__ x, double *__restrict__ y,
+                           double *__restrict__ z) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  x[i] = (double)(long long)f[i] * inv;
-  y[i] = (double)(long long)f[n + i] * inv;
-  z[i] = (double)(long long)f[2 * n + i] * inv;
+  unsigned long long a = f[i], b = f[n + i], c = f[2 * n + i];
+  if (f2) {
+    a += f2[i];
+    b += f2[n + i];
+    c += f2[2 * n + i];
+  }
+  x[i] = (double)(long long)a * inv;
+  y[i] = (double)(long long)b * inv;
+  z[i] = (double)(long long)c * inv;
 }
 
 // SCLFRC (service.f:182-287)
@@ -78,6 +86,7 @@ __global__ void k_sum_forces(int n, const double *gx, const double *gy,
 // ----------------------------------------------------------------- GETCOM
 struct MolConst {
   double summas[MDX_NT];
+  double rsummas[MDX_NT];  // 1 / summas (mixed path's centre of mass)
 };
 
 // GETCOM (service.f:463-563); with posi set it also refreshes the
@@ -206,8 +215,11 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
                                  double inv, const double *__restrict__ massdi,
                                  const double *__restrict__ amass, double *vx, double *vy,
                                  double *vz, dbl4 *pos, double *X, double *Y, double *Z,
-                                 double bx, double by, double bz, float4 *__restrict__ posf,
+                                 double bx, double by, double bz, double3 ibs,
                                  int4 *__restrict__ posi, const int *__restrict__ pinfo) {
+  // ibs: 2^32 / box per axis (host-computed: no FP64 division per thread);
+  // posi set (mixed path): centre of mass by the reciprocal mass, the
+  // fixed-point mirror refreshed
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
@@ -249,30 +261,31 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
     y = y + ms * p.y;
     z = z + ms * p.z;
   }
-  const double summ = mc.summas[mol_type[m]];
-  x = x / summ;
-  y = y / summ;
-  z = z / summ;
+  if (posi) {
+    const double rs = mc.rsummas[mol_type[m]];
+    x = x * rs;
+    y = y * rs;
+    z = z * rs;
+  } else {
+    const double summ = mc.summas[mol_type[m]];
+    x = x / summ;
+    y = y / summ;
+    z = z / summ;
+  }
   double xw = x, yw = y, zw = z;
   pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
   X[m] = xw;
   Y[m] = yw;
   Z[m] = zw;
-  const double two32 = 4294967296.0, ibx = 1.0 / bx, iby = 1.0 / by, ibz = 1.0 / bz;
   for (int k = 0; k < na; ++k) {
     dbl4 p = pos[f + k];
     p.x = (p.x - x) + xw;
     p.y = (p.y - y) + yw;
     p.z = (p.z - z) + zw;
     pos[f + k] = p;
-    if (posi) {
-      const long long xi = __double2ll_rn(p.x * ibx * two32);
-      const long long yi = __double2ll_rn(p.y * iby * two32);
-      const long long zi = __double2ll_rn(p.z * ibz * two32);
-      posi[f + k] = make_int4((int)(unsigned)(unsigned long long)xi,
-                              (int)(unsigned)(unsigned long long)yi,
-                              (int)(unsigned)(unsigned long long)zi, pinfo[f + k]);
-    }
+    if (posi)
+      posi[f + k] = make_int4(fix32_rn(__dmul_rn(p.x, ibs.x)), fix32_rn(__dmul_rn(p.y, ibs.y)),
+                              fix32_rn(__dmul_rn(p.z, ibs.z)), pinfo[f + k]);
   }
 }
 
@@ -915,7 +928,10 @@ MoveConst move_const(mdx_ctx *ctx) {
 }
 MolConst mol_const(mdx_ctx *ctx) {
   MolConst m{};
-  for (int t = 0; t < MDX_NT; ++t) m.summas[t] = ctx->summas[t];
+  for (int t = 0; t < MDX_NT; ++t) {
+    m.summas[t] = ctx->summas[t];
+    m.rsummas[t] = ctx->summas[t] != 0.0 ? 1.0 / ctx->summas[t] : 0.0;
+  }
   return m;
 }
 
@@ -1114,6 +1130,7 @@ int launch_zero_slow(mdx_ctx *ctx) {
   MDX_LAUNCHED(ctx);
   if (ctx->mixed()) {
     MDX_CUDA(cudaMemsetAsync(d.gfix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
+    MDX_CUDA(cudaMemsetAsync(d.efix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
   } else {
     MDX_CUDA(cudaMemsetAsync(d.gx, 0, sizeof(double) * 3 * d.n, ctx->stream));
   }
@@ -1124,9 +1141,10 @@ int launch_fix_to_double(mdx_ctx *ctx, int which) {
   MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   const unsigned long long *f = which == 1 ? d.hfix : d.gfix;
+  const unsigned long long *f2 = which == 1 ? nullptr : d.efix;  // G = pair + Ewald parts
   double *x = which == 1 ? d.hx : d.gx, *y = which == 1 ? d.hy : d.gy,
          *z = which == 1 ? d.hz : d.gz;
-  k_fix_fold<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, f, ctx->fix.inv, x, y, z);
+  k_fix_fold<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, f, f2, ctx->fix.inv, x, y, z);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
@@ -1194,7 +1212,10 @@ int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, b
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.ainfo, move_const(ctx), mol_const(ctx),
       htsteb, tsteb, prev, d.hx, d.hy, d.hz, from_fix ? d.hfix : nullptr, d.n, ctx->fix.inv,
       d.massdi, d.amass, d.vx, d.vy, d.vz, d.pos, d.X, d.Y, d.Z, ctx->boxl, ctx->boyl,
-      ctx->bozl, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo);
+      ctx->bozl,
+      make_double3(4294967296.0 * (1.0 / ctx->boxl), 4294967296.0 * (1.0 / ctx->boyl),
+                   4294967296.0 * (1.0 / ctx->bozl)),
+      ctx->mixed() ? d.posi : nullptr, d.pinfo);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -154,6 +154,7 @@ struct DevData {
   double *gx, *gy, *gz, *hx, *hy, *hz, *fx, *fy, *fz;
   double *ox, *oy, *oz;
   unsigned long long *gfix, *hfix;  // 3n each, x then y then z
+  unsigned long long *efix;  // 3n: reciprocal Ewald + ETERMS part of G (mixed)
   // lists
   int cap_s, cap_l;
   int *ns_cnt, *nl_cnt, *ns_idx, *nl_idx;
@@ -243,6 +244,10 @@ struct mdx_ctx {
   PairConst pc{};
   DevData dv{};
   cudaStream_t stream = nullptr;
+  // mixed path: the reciprocal Ewald of the slow forces runs on `side`
+  // (higher priority) beside the long-list pair sweep on `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int device = 0;
   int64_t launches = 0;
   bool have_topo = false, have_params = false, have_state = false,
@@ -467,6 +472,15 @@ __device__ __forceinline__ long long f2ll_rn(float y) {
   return y < 0.f ? -r : r;
 }
 
+// Low 32 bits of round-to-nearest-even(t) for |t| < 2^51: adding 1.5 x 2^52
+// leaves the rounded integer in the low mantissa bits (the bias itself has
+// none there).  One FP64 add instead of a 64-bit conversion; equal to
+// (int)(unsigned long long)__double2ll_rn(t) in that range.  __dadd_rn keeps
+// the compiler from fusing the add with the product that forms t.
+__device__ __forceinline__ int fix32_rn(double t) {
+  return __double2loint(__dadd_rn(t, 6755399441055744.0));
+}
+
 // Fixed-point force accumulation of the mixed path: two's complement in an
 // unsigned 64-bit word, so that integer addition is associative and the sum
 // is independent of the order of contributions.
@@ -517,10 +531,13 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
 // pair.cu
 int launch_localf(mdx_ctx *ctx, bool split, bool ener = true);
 int pack_lj_tables(mdx_ctx *ctx);  // abf from the FP32 tables
-int launch_forces_long(mdx_ctx *ctx, bool split);
+// fold = false: the energy slots are folded later by launch_forces_long_fold
+int launch_forces_long(mdx_ctx *ctx, bool split, bool fold = true);
+int launch_forces_long_fold(mdx_ctx *ctx, bool split);
 int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 // ewald.cu
 int host_inifur(mdx_ctx *ctx);
+int furir_prepare(mdx_ctx *ctx);  // host side of FURIR: INIFUR on first use / box change
 int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
