@@ -1038,7 +1038,8 @@ int sfac_slices(const mdx_ctx *ctx) {
   return ctx->mixed() ? d.sfac_nslice : (d.n + SLICE - 1) / SLICE;
 }
 
-int furir_prepare(mdx_ctx *ctx) {
+int launch_furir(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
   if (ctx->p.alphad <= 0.0) return MDX_OK;
   const double FKTX = 1.05, FKTS = 0.95;
   int rc;
@@ -1058,14 +1059,6 @@ int furir_prepare(mdx_ctx *ctx) {
     ctx->bozlo = ctx->bozl;
     if ((rc = host_inifur(ctx))) return rc;
   }
-  return MDX_OK;
-}
-
-int launch_furir(mdx_ctx *ctx) {
-  DevData &d = ctx->dv;
-  if (ctx->p.alphad <= 0.0) return MDX_OK;
-  int rc = furir_prepare(ctx);
-  if (rc) return rc;
   if (d.nkv == 0 || (ctx->d.ntypes == 1 && ctx->nspec[0] == 1)) return MDX_OK;
   const double ibx = 1.0 / ctx->boxl, iby = 1.0 / ctx->boyl, ibz = 1.0 / ctx->bozl;
   const double vol = ctx->boxl * ctx->boyl * ctx->bozl;
@@ -1136,7 +1129,7 @@ int launch_furir(mdx_ctx *ctx) {
     const dim3 grid((d.n + RF_BATOMS - 1) / RF_BATOMS, d.rf_nsplit);
     k_rforce32<<<grid, 32 * RF_PARTS, shr, ctx->stream>>>(
         d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
-        d.efix);
+        d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
         d.n, d.ncol, d.cols, d.wp64, d.tabx, d.taby, d.tabz, d.colrv, d.gx, d.gy, d.gz);
@@ -1159,7 +1152,7 @@ int launch_eterms(mdx_ctx *ctx) {
   k_eterms<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
       d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc,
       ctx->p.coulf, ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy,
-      d.gz, ctx->mixed() ? d.efix : nullptr, ctx->fix.scale, dst, sc->spee);
+      d.gz, ctx->mixed() ? d.gfix : nullptr, ctx->fix.scale, dst, sc->spee);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -801,7 +801,7 @@ int tc_force_launch(mdx_ctx *ctx) {
                 tc_smem_bytes(d.tc_kp, d.kx + d.ky, d.tc_ntile), ctx->stream>>>(
       d.n, d.tc_ntile, d.tc_kp, d.tc_ks, d.tc_meta,
       reinterpret_cast<const unsigned char *>(d.tc_w), d.tc_zimg, tm, d.kx, d.ky, ctx->fix,
-      d.efix, d.err);
+      d.gfix, d.err);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -36,22 +36,14 @@ __global__ void k_zero_scalars(mdx_scalars *sc, int which, int molint, int ntype
   }
 }
 
-// f2 (optional): a second fixed-point part, added as integers first.
 __global__ void k_fix_fold(int n, const unsigned long long *__restrict__ f,
-                           const unsigned long long *__restrict__ f2, double inv,
-                           double *__restrict__ x, double *__restrict__ y,
-                           double *__restrict__ z) {
+                           double inv, double *__restrict__ x,
+                           double *__restrict__ y, double *__restrict__ z) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  unsigned long long a = f[i], b = f[n + i], c = f[2 * n + i];
-  if (f2) {
-    a += f2[i];
-    b += f2[n + i];
-    c += f2[2 * n + i];
-  }
-  x[i] = (double)(long long)a * inv;
-  y[i] = (double)(long long)b * inv;
-  z[i] = (double)(long long)c * inv;
+  x[i] = (double)(long long)f[i] * inv;
+  y[i] = (double)(long long)f[n + i] * inv;
+  z[i] = (double)(long long)f[2 * n + i] * inv;
 }
 
 // SCLFRC (service.f:182-287)
@@ -1130,7 +1122,6 @@ int launch_zero_slow(mdx_ctx *ctx) {
   MDX_LAUNCHED(ctx);
   if (ctx->mixed()) {
     MDX_CUDA(cudaMemsetAsync(d.gfix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
-    MDX_CUDA(cudaMemsetAsync(d.efix, 0, sizeof(unsigned long long) * 3 * d.n, ctx->stream));
   } else {
     MDX_CUDA(cudaMemsetAsync(d.gx, 0, sizeof(double) * 3 * d.n, ctx->stream));
   }
@@ -1141,10 +1132,9 @@ int launch_fix_to_double(mdx_ctx *ctx, int which) {
   MDX_TIMER(ctx, MDX_T_OTHER);
   DevData &d = ctx->dv;
   const unsigned long long *f = which == 1 ? d.hfix : d.gfix;
-  const unsigned long long *f2 = which == 1 ? nullptr : d.efix;  // G = pair + Ewald parts
   double *x = which == 1 ? d.hx : d.gx, *y = which == 1 ? d.hy : d.gy,
          *z = which == 1 ? d.hz : d.gz;
-  k_fix_fold<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, f, f2, ctx->fix.inv, x, y, z);
+  k_fix_fold<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, f, ctx->fix.inv, x, y, z);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

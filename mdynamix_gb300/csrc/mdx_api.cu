@@ -206,31 +206,10 @@ int do_fforces(mdx_ctx *ctx, int laver, bool split, bool ener = true, bool mirro
 
 int do_slow_parts(mdx_ctx *ctx, bool split, bool mirrored = false) {
   if (ctx->mixed()) {
-    // The long-list sweep stores the pair part of G (gfix); the reciprocal
-    // Ewald and ETERMS add theirs into efix on the side stream, concurrently
-    // (not while device timers are on).  Scalars they share (PELS1, the
-    // virial) are added in a fixed order: Ewald's, then the sweep's slots
-    // after the join, so results do not depend on the overlap.
     if (!mirrored) RC(launch_mirror_f32(ctx));
-    RC(furir_prepare(ctx));  // host work and its copies stay on the main stream
-    const bool fork = ctx->side && !ctx->timing;
-    cudaStream_t main = ctx->stream;
-    if (fork) {
-      MDX_CUDA(cudaEventRecord(ctx->ev_fork, main));
-      MDX_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-    }
-    RC(launch_forces_long(ctx, split, false));
-    if (fork) ctx->stream = ctx->side;
-    int rc = launch_furir(ctx);
-    if (!rc) rc = launch_eterms(ctx);
-    ctx->stream = main;
-    if (fork) {
-      // joined even after an error, so that a capture can end
-      MDX_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
-      MDX_CUDA(cudaStreamWaitEvent(main, ctx->ev_join, 0));
-    }
-    RC(rc);
-    RC(launch_forces_long_fold(ctx, split));
+    RC(launch_forces_long(ctx, split));  // stores G first
+    RC(launch_furir(ctx));
+    RC(launch_eterms(ctx));
     RC(launch_fix_to_double(ctx, 2));
   } else {
     RC(launch_furir(ctx));
@@ -450,17 +429,6 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
     delete ctx;
     return MDX_ERR_CUDA;
   }
-  if (dims->precision == MDX_MIXED) {
-    int lo = 0, hi = 0;
-    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
-        cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
-      ctx->err = "side stream or events";
-      mdx_close(ctx);
-      return MDX_ERR_CUDA;
-    }
-  }
   DevData &d = ctx->dv;
   const size_t n = dims->nstot;
   d.n = dims->nstot;
@@ -514,7 +482,6 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
   if (!rc && dims->precision == MDX_MIXED) {
     AL(d.gfix, 3 * n);
     AL(d.hfix, 3 * n);
-    AL(d.efix, 3 * n);
   }
 #undef AL
   if (rc) {
@@ -545,7 +512,7 @@ int mdx_close(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.stab, d.pinfo, d.moltpl, d.vx, d.massdi, d.amass, d.qsite,
                   d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
-                  d.gx, d.ox, d.gfix, d.hfix, d.efix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
+                  d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
                   d.cell_cnt, d.cell_start, d.cell_list, d.atom_cell, d.a6lj, d.a6f, d.abf,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
@@ -561,12 +528,6 @@ int mdx_close(mdx_ctx *ctx) {
     cudaEventDestroy(sp.b);
   }
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
-  if (ctx->side) {
-    cudaStreamSynchronize(ctx->side);
-    cudaStreamDestroy(ctx->side);
-  }
-  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MDX_OK;

@@ -154,7 +154,6 @@ struct DevData {
   double *gx, *gy, *gz, *hx, *hy, *hz, *fx, *fy, *fz;
   double *ox, *oy, *oz;
   unsigned long long *gfix, *hfix;  // 3n each, x then y then z
-  unsigned long long *efix;  // 3n: reciprocal Ewald + ETERMS part of G (mixed)
   // lists
   int cap_s, cap_l;
   int *ns_cnt, *nl_cnt, *ns_idx, *nl_idx;
@@ -244,10 +243,6 @@ struct mdx_ctx {
   PairConst pc{};
   DevData dv{};
   cudaStream_t stream = nullptr;
-  // mixed path: the reciprocal Ewald of the slow forces runs on `side`
-  // (higher priority) beside the long-list pair sweep on `stream`
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int device = 0;
   int64_t launches = 0;
   bool have_topo = false, have_params = false, have_state = false,
@@ -531,13 +526,10 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
 // pair.cu
 int launch_localf(mdx_ctx *ctx, bool split, bool ener = true);
 int pack_lj_tables(mdx_ctx *ctx);  // abf from the FP32 tables
-// fold = false: the energy slots are folded later by launch_forces_long_fold
-int launch_forces_long(mdx_ctx *ctx, bool split, bool fold = true);
-int launch_forces_long_fold(mdx_ctx *ctx, bool split);
+int launch_forces_long(mdx_ctx *ctx, bool split);
 int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 // ewald.cu
 int host_inifur(mdx_ctx *ctx);
-int furir_prepare(mdx_ctx *ctx);  // host side of FURIR: INIFUR on first use / box change
 int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums

@@ -537,10 +537,7 @@ __global__ void k_pack_lj(int nn, const float *__restrict__ f, float2 *__restric
 // ener = false: forces only (an intermediate short step of DOUBLE, whose fast
 // energies and virials are zeroed again by the next FFORCES before anything
 // reads them, forces.f:36-49).
-// fold = false: the integer slots and split sums stay for launch_pair_fold.
-int launch_pair_fold(mdx_ctx *ctx, bool shrt, bool split, bool ener);
-
-int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener, bool fold = true) {
+int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   DevData &d = ctx->dv;
   const int T = 256, WPB = T / 32;
   const int grid = (d.n + WPB - 1) / WPB;
@@ -590,20 +587,14 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener, bool fold = true
     }
 #undef LP32
     MDX_LAUNCHED(ctx);
-  }
-  return fold ? launch_pair_fold(ctx, shrt, split, ener) : MDX_OK;
-}
-
-int launch_pair_fold(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
-  DevData &d = ctx->dv;
-  if (ctx->mixed() && ener) {
-    k_fold_slots<<<1, 1, 0, ctx->stream>>>(reinterpret_cast<unsigned long long *>(d.red),
-                                            1.0 / ctx->fix.escale, d.sc, shrt ? 1 : 2,
-                                            ctx->d.ntypes, split ? 1 : 0);
-    MDX_LAUNCHED(ctx);
+    if (ener) {
+      k_fold_slots<<<1, 1, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
+                                              ctx->d.ntypes, split ? 1 : 0);
+      MDX_LAUNCHED(ctx);
+    }
   }
   if (split) {
-    k_fold_split<<<1, 64, 0, ctx->stream>>>(d.red + 64, d.sc);
+    k_fold_split<<<1, 64, 0, ctx->stream>>>(split_buf, d.sc);
     MDX_LAUNCHED(ctx);
   }
   return MDX_OK;
@@ -625,10 +616,8 @@ int pack_lj_tables(mdx_ctx *ctx) {
 
 int launch_localf(mdx_ctx *ctx, bool split, bool ener) {
   MDX_TIMER(ctx, MDX_T_PAIR_SHORT); return launch_pair(ctx, true, split, ener); }
-int launch_forces_long(mdx_ctx *ctx, bool split, bool fold) {
-  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair(ctx, false, split, true, fold); }
-int launch_forces_long_fold(mdx_ctx *ctx, bool split) {
-  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair_fold(ctx, false, split, true); }
+int launch_forces_long(mdx_ctx *ctx, bool split) {
+  MDX_TIMER(ctx, MDX_T_PAIR_LONG); return launch_pair(ctx, false, split, true); }
 
 int launch_wir(mdx_ctx *ctx, int which) {
   MDX_TIMER(ctx, MDX_T_OTHER);
