@@ -158,6 +158,7 @@ struct DevData {
   int cap_s, cap_l;
   int *ns_cnt, *nl_cnt, *ns_idx, *nl_idx;
   int *cell_cnt, *cell_start, *cell_list, *atom_cell;
+  int4 *cell_pos;  // per cell-sorted slot: the candidate record k_build reads
   // LJ tables [i*nnbt + j]
   double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;

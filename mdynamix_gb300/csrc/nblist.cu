@@ -105,6 +105,26 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start,
   }
 }
 
+// Candidate records in cell order, beside cell_list: the fixed-point
+// position and packed (molecule, site) word (mixed path), or the FP32
+// mirror's x, y, z bits and the molecule (FP64 path).  k_build then reads a
+// run of neighbour cells as one coalesced stream, with no gather through
+// the atom index.
+__global__ void k_cell_gather(int n, const int *__restrict__ list, const int4 *__restrict__ posi,
+                              const float4 *__restrict__ posf, const int4 *__restrict__ ainfo,
+                              int4 *__restrict__ cell_pos) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int j = list[k];
+  if (posi) {
+    cell_pos[k] = posi[j];
+  } else {
+    const float4 f = posf[j];
+    cell_pos[k] = make_int4(__float_as_int(f.x), __float_as_int(f.y), __float_as_int(f.z),
+                            ainfo[j].y);
+  }
+}
+
 constexpr int CELL_REACH = 1;  // list cells per list radius (2 measured slower: 125 thin cells)
 
 // Ownership of pair (i, j) in the strip loop: i owns it when (i-j) is even
@@ -142,7 +162,8 @@ __global__ void __launch_bounds__(BLK) k_build(
     const int4 *__restrict__ ainfo, const int *__restrict__ nnbb,
     const int *__restrict__ inbb, int nbdmax, BoxD b, CellGrid g,
     const int *__restrict__ atom_cell, const int *__restrict__ cell_start,
-    const int *__restrict__ cell_list, double short2, double rl2, int cap_s,
+    const int *__restrict__ cell_list, const int4 *__restrict__ cell_pos, double short2,
+    double rl2, int cap_s,
     int cap_l, int *__restrict__ ns_cnt, int *__restrict__ nl_cnt,
     int *__restrict__ ns_idx, int *__restrict__ nl_idx, int *__restrict__ err,
     int *__restrict__ need, int full, const int4 *__restrict__ posi, float sxf, float syf,
@@ -168,28 +189,34 @@ __global__ void __launch_bounds__(BLK) k_build(
   const int ox0 = g.nx >= W ? -R : 0, ox1 = g.nx >= W ? R : g.nx - 1;
   const int oy0 = g.ny >= W ? -R : 0, oy1 = g.ny >= W ? R : g.ny - 1;
   const int oz0 = g.nz >= W ? -R : 0, oz1 = g.nz >= W ? R : g.nz - 1;
+  auto wrapx = [&](int ox) { return g.nx >= W ? (cx0 + ox + g.nx) % g.nx : ox; };
   for (int oz = oz0; oz <= oz1; ++oz)
-    for (int oy = oy0; oy <= oy1; ++oy)
-      for (int ox = ox0; ox <= ox1; ++ox) {
-        int cx = g.nx >= W ? (cx0 + ox + g.nx) % g.nx : ox;
-        int cy = g.ny >= W ? (cy0 + oy + g.ny) % g.ny : oy;
-        int cz = g.nz >= W ? (cz0 + oz + g.nz) % g.nz : oz;
-        int c = (cz * g.ny + cy) * g.nx + cx;
-        int s = cell_start[c], e = cell_start[c + 1];
+    for (int oy = oy0; oy <= oy1; ++oy) {
+      const int cy = g.ny >= W ? (cy0 + oy + g.ny) % g.ny : oy;
+      const int cz = g.nz >= W ? (cz0 + oz + g.nz) % g.nz : oz;
+      const int crow = (cz * g.ny + cy) * g.nx;
+      // the row's stencil cells in stencil order, consecutive cells merged
+      // into one run of the cell-sorted arrays (the order of candidates is
+      // unchanged)
+      for (int ox = ox0; ox <= ox1;) {
+        const int cxa = wrapx(ox);
+        int cxb = cxa;
+        while (ox < ox1 && wrapx(ox + 1) == cxb + 1) {
+          ++ox;
+          ++cxb;
+        }
+        ++ox;
+        const int s = cell_start[crow + cxa], e = cell_start[crow + cxb + 1];
         for (int base = s; base < e; base += 32) {
           int kind = 0;
           int j = -1;
           if (base + lane < e) {
             j = cell_list[base + lane];
+            const int4 qj = cell_pos[base + lane];  // independent of the load of j
             if (j != i && (full || owns(i, j))) {
-              int4 qj;
-              bool same;
-              if (posi) {
-                qj = posi[j];
-                same = ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS);
-              } else {
-                same = ainfo[j].y == imol;
-              }
+              const bool same =
+                  posi ? ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS)
+                       : qj.w == imol;
               if (same) {
                 kind = classify_exact(i, j, true, pi, pos[j], b, short2, rl2,
                                       nnbb, inbb, nbdmax);
@@ -200,10 +227,9 @@ __global__ void __launch_bounds__(BLK) k_build(
                   dy = (float)(int)((unsigned)qi.y - (unsigned)qj.y) * syf;
                   dz = (float)(int)((unsigned)qi.z - (unsigned)qj.z) * szf;
                 } else {
-                  const float4 q = posf[j];
-                  dx = pf.x - q.x;
-                  dy = pf.y - q.y;
-                  dz = pf.z - q.z;
+                  dx = pf.x - __int_as_float(qj.x);
+                  dy = pf.y - __int_as_float(qj.y);
+                  dz = pf.z - __int_as_float(qj.z);
                   pbc_rectf(dx, dy, dz, fbx, fby, fbz, fhx, fhy, fhz);
                 }
                 float d2 = dx * dx + dy * dy + dz * dz;
@@ -233,6 +259,7 @@ __global__ void __launch_bounds__(BLK) k_build(
           nl += __popc(ml);
         }
       }
+    }
   if (lane == 0) {
     ns_cnt[i] = min(ns, cap_s);
     nl_cnt[i] = min(nl, cap_l);
@@ -354,12 +381,15 @@ int launch_build_lists(mdx_ctx *ctx) {
   k_cell_sort<<<(g.ncell + 7) / 8, 256, 0, ctx->stream>>>(g.ncell, d.cell_start,
                                                           d.cell_list);
   MDX_LAUNCHED(ctx);
+  k_cell_gather<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
+      d.n, d.cell_list, ctx->mixed() ? d.posi : nullptr, d.posf, d.ainfo, d.cell_pos);
+  MDX_LAUNCHED(ctx);
   int *need = d.shake_iter + 4;  // two ints of scratch after the SHAKE counter
   MDX_CUDA(cudaMemsetAsync(need, 0, sizeof(int) * 2, ctx->stream));
   const int BLK = 256;
   k_build<BLK><<<(d.n + BLK / 32 - 1) / (BLK / 32), BLK, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,
-      d.cell_start, d.cell_list, ctx->p.rshort * ctx->p.rshort, rl * rl,
+      d.cell_start, d.cell_list, d.cell_pos, ctx->p.rshort * ctx->p.rshort, rl * rl,
       d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
       ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,
       (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),
