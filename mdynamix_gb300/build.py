@@ -24,6 +24,11 @@ SOURCES = ["mdx_api.cu", "integrate.cu", "bonded.cu", "ewald.cu", "pair.cu", "nb
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
+# Per-file additions.  pair.cu: FP32 denormals flush to zero (the FP32 pair
+# terms are far from the denormal range), which drops the denormal handling
+# around the special-function instructions of the sweeps (measured 8 % on
+# the short sweep; no gain elsewhere).
+FILE_FLAGS = {"pair.cu": ["-ftz=true"]}
 
 
 def nvcc() -> str:
@@ -38,7 +43,7 @@ def _stale(obj: str, src: str) -> bool:
         return True
     t = os.path.getmtime(obj)
     deps = [src, os.path.join(CSRC, "mdx_internal.cuh"), os.path.join(CSRC, "tc_ptx.cuh"),
-            os.path.join(ROOT, "include", "mdx_gpu.h")]
+            os.path.join(ROOT, "include", "mdx_gpu.h"), os.path.abspath(__file__)]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -56,7 +61,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src = os.path.join(CSRC, s)
         obj = os.path.join(BUILD, s.replace(".cu", ".o"))
         if force or _stale(obj, src):
-            jobs.append([cc, *ARCH, *FLAGS, "-c", src, "-o", obj])
+            jobs.append([cc, *ARCH, *FLAGS, *FILE_FLAGS.get(s, []), "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

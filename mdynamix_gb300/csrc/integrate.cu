@@ -190,6 +190,8 @@ __global__ void k_kick_drift(int n, const int4 *__restrict__ ainfo, MoveConst mv
   pos[i] = p;
 }
 
+constexpr int KD_MAXA = 4;  // atoms per molecule of the register path below
+
 // One short step of DOUBLE's inner loop up to the fast forces, thread per
 // molecule: the kick and drift of k_kick_drift for each of its atoms
 // (mdstep.f:383-397), then GETCOM's centre of mass and wrap (service.f:
@@ -205,8 +207,10 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
                                  const double *__restrict__ hz,
                                  const unsigned long long *__restrict__ hfix, int n,
                                  double inv, const double *__restrict__ massdi,
-                                 const double *__restrict__ amass, double *vx, double *vy,
-                                 double *vz, dbl4 *pos, double *X, double *Y, double *Z,
+                                 const double *__restrict__ amass, double *__restrict__ vx,
+                                 double *__restrict__ vy, double *__restrict__ vz,
+                                 dbl4 *__restrict__ pos, double *__restrict__ X,
+                                 double *__restrict__ Y, double *__restrict__ Z,
                                  double bx, double by, double bz, double3 ibs,
                                  int4 *__restrict__ posi, const int *__restrict__ pinfo) {
   // ibs: 2^32 / box per axis (host-computed: no FP64 division per thread);
@@ -215,6 +219,74 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
+  if (posi && na <= KD_MAXA) {
+    // Mixed path, small molecules: the atoms stay in registers between the
+    // centre of mass and the wrap, each position is stored once, and the
+    // update takes fewer FP64 operations (the two half kicks of one force
+    // as one, 1/2^k folded into the kick factor, the drift factor TSTEB /
+    // m formed once per atom, coordinates rebuilt around the wrapped centre
+    // only when it moved).  The same update up to FP64 rounding.
+    const double hk = prev ? 2.0 * htsteb : htsteb, hkf = hk * inv;
+    dbl4 pr[KD_MAXA];
+    double x = 0., y = 0., z = 0.;
+#pragma unroll
+    for (int k = 0; k < KD_MAXA; ++k) {
+      if (k < na) {
+        const int i = f + k;
+        dbl4 p = pos[i];
+        if (mv.lmove[ainfo[i].x]) {
+          double u = vx[i], v = vy[i], w = vz[i];
+          if (hfix) {
+            u = fma((double)(long long)hfix[i], hkf, u);
+            v = fma((double)(long long)hfix[n + i], hkf, v);
+            w = fma((double)(long long)hfix[2 * n + i], hkf, w);
+          } else {
+            u = fma(hx[i], hk, u);
+            v = fma(hy[i], hk, v);
+            w = fma(hz[i], hk, w);
+          }
+          vx[i] = u;
+          vy[i] = v;
+          vz[i] = w;
+          const double tm = tsteb * massdi[i];
+          p.x = fma(u, tm, p.x);
+          p.y = fma(v, tm, p.y);
+          p.z = fma(w, tm, p.z);
+        }
+        pr[k] = p;
+        const double ms = amass[i];
+        x = fma(ms, p.x, x);
+        y = fma(ms, p.y, y);
+        z = fma(ms, p.z, z);
+      }
+    }
+    const double rs = mc.rsummas[mol_type[m]];
+    x = x * rs;
+    y = y * rs;
+    z = z * rs;
+    double xw = x, yw = y, zw = z;
+    pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+    X[m] = xw;
+    Y[m] = yw;
+    Z[m] = zw;
+    const bool moved = xw != x || yw != y || zw != z;
+#pragma unroll
+    for (int k = 0; k < KD_MAXA; ++k) {
+      if (k < na) {
+        dbl4 p = pr[k];
+        if (moved) {
+          p.x = (p.x - x) + xw;
+          p.y = (p.y - y) + yw;
+          p.z = (p.z - z) + zw;
+        }
+        pos[f + k] = p;
+        posi[f + k] =
+            make_int4(fix32_rn(__dmul_rn(p.x, ibs.x)), fix32_rn(__dmul_rn(p.y, ibs.y)),
+                      fix32_rn(__dmul_rn(p.z, ibs.z)), pinfo[f + k]);
+      }
+    }
+    return;
+  }
   double x = 0., y = 0., z = 0.;
   for (int k = 0; k < na; ++k) {
     const int i = f + k;
