@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(128, 3) k_sfac32(
     __syncthreads();
     const int m = min(TILE, a1 - base);
     if (active) {
-#pragma unroll 1
+#pragma unroll 2  // two atoms' loads in flight (measured 7 % faster than 1 and 4)
       for (int j = 0; j < m; ++j) {
         const float2 *row = srow + (t & 1) * bufsz + j * rowlen;
         float tr[KGRP], ti[KGRP];
