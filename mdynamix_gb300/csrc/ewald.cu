@@ -662,49 +662,58 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
 
 // ETERMS (forces.f:1482-1676): thread per atom ISP over its bound partners
 // JSP < ISP (normal types), or over all intramolecular pairs of EE types.
+// R = double: the FP64 path; R = float (mixed path, gfix set): the pair's
+// FP64 minimum-image vector rounded to FP32, the rest in FP32, forces to
+// 64-bit fixed point with FP32 operations only.  Energy and virial sums are
+// FP64 either way.
+template <typename R>
 __device__ __forceinline__ void eterms_pair(
     int isp, int jsp, int ityp, const dbl4 &pi, const dbl4 &pj, double coulf,
     double alphad, double bx, double by, double bz, const TypeConst &tc,
-    double *acc, double *spee_sh, double *gx, double *gy, double *gz,
-    unsigned long long *gfix, int n, double fscale) {
-  const double QIJ = coulf * pi.w * pj.w;
-  double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
-  pbc_rect(DX, DY, DZ, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
-  const double R2 = DX * DX + DY * DY + DZ * DZ;
-  const double R2I = 1.0 / R2;
-  const double R1 = sqrt(R2);
-  const double R1I = R1 * R2I;
-  const double ALPHAR = alphad * R1;
-  const double TTT = 1.0 / (1.0 + MDX_B1 * ALPHAR);
-  const double EXP2A = exp(-(ALPHAR * ALPHAR));
-  const double ERFC =
-      ((((MDX_A5 * TTT + MDX_A4) * TTT + MDX_A3) * TTT + MDX_A2) * TTT + MDX_A1) * TTT * EXP2A;
-  const double EES = QIJ * (ERFC - 1.0) * R1I;
-  acc[0] += EES;
-  atomicAdd(&spee_sh[ityp], EES);
+    double *acc, double *gx, double *gy, double *gz,
+    unsigned long long *gfix, int n, float fscalef) {
+  double DXd = pi.x - pj.x, DYd = pi.y - pj.y, DZd = pi.z - pj.z;
+  pbc_rect(DXd, DYd, DZd, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  const R QIJ = (R)(coulf * pi.w * pj.w);
+  const R DX = (R)DXd, DY = (R)DYd, DZ = (R)DZd;
+  const R R2 = DX * DX + DY * DY + DZ * DZ;
+  const R R2I = R(1) / R2;
+  const R R1 = sqrt(R2);
+  const R R1I = R1 * R2I;
+  const R ALPHAR = (R)alphad * R1;
+  const R TTT = R(1) / (R(1) + (R)MDX_B1 * ALPHAR);
+  const R EXP2A = exp(-(ALPHAR * ALPHAR));
+  const R ERFC = (((((R)MDX_A5 * TTT + (R)MDX_A4) * TTT + (R)MDX_A3) * TTT + (R)MDX_A2) * TTT +
+                  (R)MDX_A1) * TTT * EXP2A;
+  const R EES = QIJ * (ERFC - R(1)) * R1I;
+  acc[0] += (double)EES;
   if (tc.lmove[ityp]) {
-    const double FES = QIJ * ((MDX_TOTPI * ALPHAR * EXP2A + ERFC) - 1.0) * R1I * R2I;
+    const R FES = QIJ * (((R)MDX_TOTPI * ALPHAR * EXP2A + ERFC) - R(1)) * R1I * R2I;
+    const R FX = FES * DX, FY = FES * DY, FZ = FES * DZ;
     if (gfix) {
-      fix_add(&gfix[isp], FES * DX, fscale);
-      fix_add(&gfix[n + isp], FES * DY, fscale);
-      fix_add(&gfix[2 * n + isp], FES * DZ, fscale);
-      fix_add(&gfix[jsp], -FES * DX, fscale);
-      fix_add(&gfix[n + jsp], -FES * DY, fscale);
-      fix_add(&gfix[2 * n + jsp], -FES * DZ, fscale);
+      const long long qx = f2ll_rn((float)FX * fscalef), qy = f2ll_rn((float)FY * fscalef),
+                      qz = f2ll_rn((float)FZ * fscalef);
+      atomicAdd(&gfix[isp], (unsigned long long)qx);
+      atomicAdd(&gfix[n + isp], (unsigned long long)qy);
+      atomicAdd(&gfix[2 * n + isp], (unsigned long long)qz);
+      atomicAdd(&gfix[jsp], (unsigned long long)-qx);
+      atomicAdd(&gfix[n + jsp], (unsigned long long)-qy);
+      atomicAdd(&gfix[2 * n + jsp], (unsigned long long)-qz);
     } else {
-      atomicAdd(&gx[isp], FES * DX);
-      atomicAdd(&gy[isp], FES * DY);
-      atomicAdd(&gz[isp], FES * DZ);
-      atomicAdd(&gx[jsp], -FES * DX);
-      atomicAdd(&gy[jsp], -FES * DY);
-      atomicAdd(&gz[jsp], -FES * DZ);
+      atomicAdd(&gx[isp], (double)FX);
+      atomicAdd(&gy[isp], (double)FY);
+      atomicAdd(&gz[isp], (double)FZ);
+      atomicAdd(&gx[jsp], -(double)FX);
+      atomicAdd(&gy[jsp], -(double)FY);
+      atomicAdd(&gz[jsp], -(double)FZ);
     }
-    acc[1] += FES * (DX * DX);
-    acc[2] += FES * (DY * DY);
-    acc[3] += FES * (DZ * DZ);
+    acc[1] += (double)(FES * (DX * DX));
+    acc[2] += (double)(FES * (DY * DY));
+    acc[3] += (double)(FES * (DZ * DZ));
   }
 }
 
+template <typename R>
 __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
                          const int4 *__restrict__ ainfo,
                          const int *__restrict__ nnbb,
@@ -712,7 +721,7 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
                          const int *__restrict__ mol_first, TypeConst tc,
                          double coulf, double alphad, double bx, double by,
                          double bz, double *gx, double *gy, double *gz,
-                         unsigned long long *gfix, double fscale, Dst6 dst,
+                         unsigned long long *gfix, float fscalef, Dst6 dst,
                          double *spee) {
   __shared__ double spee_sh[MDX_NT];
   if (threadIdx.x < MDX_NT) spee_sh[threadIdx.x] = 0.0;
@@ -729,16 +738,19 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
         int jf = inbb[isp * nbdmax + k];
         int jsp = (jf < 0 ? -jf : jf) - 1;
         if (isp > jsp)
-          eterms_pair(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz,
-                      tc, acc, spee_sh, gx, gy, gz, gfix, n, fscale);
+          eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc, acc, gx,
+                         gy, gz, gfix, n, fscalef);
       }
     } else {
       // EE molecule: every intramolecular pair JSM < ISM (forces.f:1585-1594)
       const int f = mol_first[ai.y];
       for (int jsp = f; jsp < isp; ++jsp)
-        eterms_pair(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc,
-                    acc, spee_sh, gx, gy, gz, gfix, n, fscale);
+        eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc, acc, gx,
+                       gy, gz, gfix, n, fscalef);
     }
+    // SPEE of the atom's type: the thread's own sum (one shared atomic per
+    // thread, not per pair)
+    if (acc[0] != 0.0) atomicAdd(&spee_sh[ityp], acc[0]);
   }
   block_add<4>(acc, dst);
   if (threadIdx.x < MDX_NT && spee_sh[threadIdx.x] != 0.0)
@@ -1149,10 +1161,16 @@ int launch_eterms(mdx_ctx *ctx) {
   MDX_LAUNCHED(ctx);
   mdx_scalars *sc = d.sc;
   Dst6 dst = dst6(ctx, (d.n + 127) / 128, 4, &sc->spe, &sc->virx, &sc->viry, &sc->virz);
-  k_eterms<<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
-      d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc,
-      ctx->p.coulf, ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy,
-      d.gz, ctx->mixed() ? d.gfix : nullptr, ctx->fix.scale, dst, sc->spee);
+  if (ctx->mixed())
+    k_eterms<float><<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
+        d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc, ctx->p.coulf,
+        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy, d.gz, d.gfix,
+        ctx->fix.scalef, dst, sc->spee);
+  else
+    k_eterms<double><<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
+        d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc, ctx->p.coulf,
+        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy, d.gz, nullptr, 0.f, dst,
+        sc->spee);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
