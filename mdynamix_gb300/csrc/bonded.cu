@@ -24,6 +24,7 @@ struct BondOut {
   float fscalef;      // the same power of two as FP32
   const int4 *posi;   // mixed: fixed-point positions (bond vectors by integer wrap)
   float sx, sy, sz;   // box / 2^32
+  float limx, limy, limz;  // 0.99 x half box: below it no minimum-image shift
 };
 
 // Fixed-point force term: R = float rounds v * 2^k with FP32 operations only
@@ -69,6 +70,22 @@ __device__ __forceinline__ void vec_r(const dbl4 *pos, const BondOut &o, int a, 
     x = (R)((float)(int)((unsigned)pa.x - (unsigned)pb.x) * o.sx);
     y = (R)((float)(int)((unsigned)pa.y - (unsigned)pb.y) * o.sy);
     z = (R)((float)(int)((unsigned)pa.z - (unsigned)pb.z) * o.sz);
+  } else if (sizeof(R) == sizeof(float)) {
+    // FP64 difference rounded to FP32; the minimum-image test runs on the
+    // FP32 value against 0.99 x half box (bond vectors lie far inside it)
+    // and only a vector near or past it takes the FP64 test and shift:
+    // the same result as vec()
+    const dbl4 pa = pos[a], pb = pos[b];
+    double xd = pa.x - pb.x, yd = pa.y - pb.y, zd = pa.z - pb.z;
+    x = (R)xd;
+    y = (R)yd;
+    z = (R)zd;
+    if (fabsf((float)x) > o.limx || fabsf((float)y) > o.limy || fabsf((float)z) > o.limz) {
+      pbc_rect(xd, yd, zd, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      x = (R)xd;
+      y = (R)yd;
+      z = (R)zd;
+    }
   } else {
     double xd, yd, zd;
     vec(pos, a, b, bx, by, bz, xd, yd, zd);
@@ -319,7 +336,7 @@ __global__ void __launch_bounds__(128) k_molbonded(
     const MolTpl &T = tpl[t];
     const int base = T.first + g * T.nsit;
     const int lmove = tc.lmove[T.type];
-    const double fnspi = 1.0 / (double)nspec[T.type];
+    const double fnspi = laver ? 1.0 / (double)nspec[T.type] : 0.0;
     for (int b = 0; b < T.nb; ++b) {
       const int M = T.bm[b];
       R BD, EB;
@@ -602,7 +619,8 @@ int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
   // length errors into large force errors) for 0.06 ms a long step
   BondOut o{d.hx, d.hy, d.hz, mx ? d.hfix : nullptr, d.n, ctx->fix.scale, ctx->fix.scalef,
             nullptr, (float)(ctx->boxl / 4294967296.0),
-            (float)(ctx->boyl / 4294967296.0), (float)(ctx->bozl / 4294967296.0)};
+            (float)(ctx->boyl / 4294967296.0), (float)(ctx->bozl / 4294967296.0),
+            (float)(0.495 * ctx->boxl), (float)(0.495 * ctx->boyl), (float)(0.495 * ctx->bozl)};
   const int T = 128;
   const double bx = ctx->boxl, by = ctx->boyl, bz = ctx->bozl;
   const int *nspec = d.nspec_d;
