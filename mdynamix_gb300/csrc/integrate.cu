@@ -736,20 +736,39 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
   }
 }
 
-__global__ void k_scal(int stage, ScalConst c, ScalScratch *ss, mdx_thermo *th,
-                       const mdx_scalars *s, int *err) {
-  scal_stage(stage, c, ss, th, s, err);
-}
-
 // Several consecutive SCALING stages in one launch (one thread, in order:
 // the same as one launch each).
 struct StageList {
   int n;
   int st[8];
 };
+__device__ __forceinline__ void copy_words(void *dst, const void *src, int bytes) {
+  int *d = static_cast<int *>(dst);
+  const int *s = static_cast<const int *>(src);
+  for (int k = threadIdx.x; k < bytes / 4; k += blockDim.x) d[k] = s[k];
+}
+
+// The stages are one serial chain of scalar arithmetic; from global memory
+// each of its loads would be a round trip.  The block brings the scratch,
+// the thermostat state and the scalars into shared memory at once, thread 0
+// runs the stages there, and the block writes the first two back.
 __global__ void k_scal_list(StageList L, ScalConst c, ScalScratch *ss, mdx_thermo *th,
                             const mdx_scalars *s, int *err) {
-  for (int k = 0; k < L.n; ++k) scal_stage(L.st[k], c, ss, th, s, err);
+  __shared__ ScalScratch ss_s;
+  __shared__ mdx_thermo th_s;
+  __shared__ mdx_scalars s_s;
+  static_assert(sizeof(ScalScratch) % 4 == 0 && sizeof(mdx_thermo) % 4 == 0 &&
+                    sizeof(mdx_scalars) % 4 == 0,
+                "word copies");
+  copy_words(&ss_s, ss, sizeof(ScalScratch));
+  copy_words(&th_s, th, sizeof(mdx_thermo));
+  copy_words(&s_s, s, sizeof(mdx_scalars));
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < L.n; ++k) scal_stage(L.st[k], c, &ss_s, &th_s, &s_s, err);
+  __syncthreads();
+  copy_words(ss, &ss_s, sizeof(ScalScratch));
+  copy_words(th, &th_s, sizeof(mdx_thermo));
 }
 
 // Velocity (and position) scaling of the SCALING stages.
@@ -1030,8 +1049,11 @@ static ScalConst scal_const(mdx_ctx *ctx) {
 }
 
 static int stage(mdx_ctx *ctx, int st) {
-  k_scal<<<1, 1, 0, ctx->stream>>>(st, scal_const(ctx), scratch(ctx), ctx->dv.th,
-                                   ctx->dv.sc, ctx->dv.err);
+  StageList L{};
+  L.n = 1;
+  L.st[0] = st;
+  k_scal_list<<<1, 128, 0, ctx->stream>>>(L, scal_const(ctx), scratch(ctx), ctx->dv.th,
+                                            ctx->dv.sc, ctx->dv.err);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
@@ -1044,8 +1066,8 @@ struct StageQ {
   void push(int st) { L.st[L.n++] = st; }
   int flush() {
     if (!L.n) return MDX_OK;
-    k_scal_list<<<1, 1, 0, ctx->stream>>>(L, scal_const(ctx), scratch(ctx), ctx->dv.th,
-                                          ctx->dv.sc, ctx->dv.err);
+    k_scal_list<<<1, 128, 0, ctx->stream>>>(L, scal_const(ctx), scratch(ctx), ctx->dv.th,
+                                            ctx->dv.sc, ctx->dv.err);
     MDX_LAUNCHED(ctx);
     L.n = 0;
     return MDX_OK;
@@ -1057,7 +1079,7 @@ static int getemp_kernel(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   const int nt = ctx->d.ntypes;
 #define GETEMP(NT)                                                                       \
-  k_getemp<NT><<<160, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), nt, d.massdi, \
+  k_getemp<NT><<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), nt, d.massdi, \
                                              d.vx, d.vy, d.vz, scratch(ctx)->ekacc,      \
                                              d.red_part, d.red_ctr)
   if (nt <= 1) GETEMP(1);

@@ -421,6 +421,10 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
     ctx->d.cap_long *= 2;
   }
   cudaGetDevice(&ctx->device);
+  if (cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device) !=
+          cudaSuccess ||
+      ctx->nsm < 1)
+    ctx->nsm = 1;
   {
     const char *g = getenv("MDX_GRAPHS");
     if (g && g[0] == '0') ctx->use_graphs = false;

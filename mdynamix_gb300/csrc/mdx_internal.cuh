@@ -245,6 +245,7 @@ struct mdx_ctx {
   DevData dv{};
   cudaStream_t stream = nullptr;
   int device = 0;
+  int nsm = 1;  // SMs of the device: grid of the grid-stride reductions (one block each)
   int64_t launches = 0;
   bool have_topo = false, have_params = false, have_state = false,
        have_lists = false, have_com = false;

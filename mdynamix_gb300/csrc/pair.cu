@@ -629,15 +629,15 @@ int launch_wir(mdx_ctx *ctx, int which) {
   DevData &d = ctx->dv;
   double *dst = which == 1 ? &d.sc->wirss : &d.sc->wirs;
   if (which == 1 && ctx->mixed()) {
-    k_wir_fix<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, d.hfix,
-                                            ctx->fix.inv, dst6(ctx, 160, 1, dst));
+    k_wir_fix<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, d.hfix,
+                                                 ctx->fix.inv, dst6(ctx, ctx->nsm, 1, dst));
     MDX_LAUNCHED(ctx);
     return MDX_OK;
   }
   const double *fx = which == 1 ? d.hx : d.gx, *fy = which == 1 ? d.hy : d.gy,
                *fz = which == 1 ? d.hz : d.gz;
-  k_wir<<<160, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz,
-                                      dst6(ctx, 160, 1, dst));
+  k_wir<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz,
+                                           dst6(ctx, ctx->nsm, 1, dst));
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
