@@ -212,10 +212,11 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
                                  dbl4 *__restrict__ pos, double *__restrict__ X,
                                  double *__restrict__ Y, double *__restrict__ Z,
                                  double bx, double by, double bz, double3 ibs,
-                                 int4 *__restrict__ posi, const int *__restrict__ pinfo) {
+                                 int4 *__restrict__ posi, const int *__restrict__ pinfo,
+                                 int4 *__restrict__ posc, const int *__restrict__ slot_of) {
   // ibs: 2^32 / box per axis (host-computed: no FP64 division per thread);
   // posi set (mixed path): centre of mass by the reciprocal mass, the
-  // fixed-point mirror refreshed
+  // fixed-point mirror refreshed, and (posc set) its cell-order copy
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
@@ -280,9 +281,11 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
           p.z = (p.z - z) + zw;
         }
         pos[f + k] = p;
-        posi[f + k] =
+        const int4 q =
             make_int4(fix32_rn(__dmul_rn(p.x, ibs.x)), fix32_rn(__dmul_rn(p.y, ibs.y)),
                       fix32_rn(__dmul_rn(p.z, ibs.z)), pinfo[f + k]);
+        posi[f + k] = q;
+        if (posc) posc[slot_of[f + k]] = q;
       }
     }
     return;
@@ -347,9 +350,12 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
     p.y = (p.y - y) + yw;
     p.z = (p.z - z) + zw;
     pos[f + k] = p;
-    if (posi)
-      posi[f + k] = make_int4(fix32_rn(__dmul_rn(p.x, ibs.x)), fix32_rn(__dmul_rn(p.y, ibs.y)),
-                              fix32_rn(__dmul_rn(p.z, ibs.z)), pinfo[f + k]);
+    if (posi) {
+      const int4 q = make_int4(fix32_rn(__dmul_rn(p.x, ibs.x)), fix32_rn(__dmul_rn(p.y, ibs.y)),
+                               fix32_rn(__dmul_rn(p.z, ibs.z)), pinfo[f + k]);
+      posi[f + k] = q;
+      if (posc) posc[slot_of[f + k]] = q;
+    }
   }
 }
 
@@ -1263,7 +1269,7 @@ int launch_getcom(mdx_ctx *ctx, bool mirror) {
       mol_const(ctx), ctx->boxl, ctx->boyl, ctx->bozl, nullptr,
       mirror && ctx->mixed() ? d.posi : nullptr, d.pinfo);
   MDX_LAUNCHED(ctx);
-  return MDX_OK;
+  return mirror ? launch_cell_refresh(ctx) : MDX_OK;
 }
 
 int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale) {
@@ -1299,7 +1305,8 @@ int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, b
       ctx->bozl,
       make_double3(4294967296.0 * (1.0 / ctx->boxl), 4294967296.0 * (1.0 / ctx->boyl),
                    4294967296.0 * (1.0 / ctx->bozl)),
-      ctx->mixed() ? d.posi : nullptr, d.pinfo);
+      ctx->mixed() ? d.posi : nullptr, d.pinfo,
+      ctx->mixed() && ctx->have_lists ? d.cell_pos : nullptr, d.slot_of);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -471,6 +471,7 @@ int mdx_open(const mdx_dims *dims, mdx_ctx **out) {
   AL(d.atom_cell, n);
   AL(d.cell_list, n);
   AL(d.cell_pos, n);
+  AL(d.slot_of, n);
   AL(d.sc, 1);
   AL(d.th, 1);
   AL(d.err, 4);
@@ -518,7 +519,7 @@ int mdx_close(mdx_ctx *ctx) {
   void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.stab, d.pinfo, d.moltpl, d.vx, d.massdi, d.amass, d.qsite,
                   d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
                   d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
-                  d.cell_cnt, d.cell_start, d.cell_list, d.cell_pos, d.atom_cell, d.a6lj, d.a6f, d.abf,
+                  d.cell_cnt, d.cell_start, d.cell_list, d.cell_pos, d.slot_of, d.atom_cell, d.a6lj, d.a6f, d.abf,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,

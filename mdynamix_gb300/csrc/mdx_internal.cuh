@@ -158,7 +158,11 @@ struct DevData {
   int cap_s, cap_l;
   int *ns_cnt, *nl_cnt, *ns_idx, *nl_idx;
   int *cell_cnt, *cell_start, *cell_list, *atom_cell;
-  int4 *cell_pos;  // per cell-sorted slot: the candidate record k_build reads
+  // per cell-sorted slot: the candidate record k_build reads; on the mixed
+  // path also the neighbour records of the pair sweeps, whose lists hold
+  // slots (kept equal to posi[cell_list[slot]] by every posi writer)
+  int4 *cell_pos;
+  int *slot_of;  // mixed path: slot of atom i in the cell order of the last build
   // LJ tables [i*nnbt + j]
   double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
@@ -570,4 +574,5 @@ int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);
+int launch_cell_refresh(mdx_ctx *ctx);  // mixed: cell_pos from posi (after posi writers)
 int upload_site_table(mdx_ctx *ctx);  // mdx_api.cu: stab from the current charges

@@ -112,10 +112,11 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start,
 // the atom index.
 __global__ void k_cell_gather(int n, const int *__restrict__ list, const int4 *__restrict__ posi,
                               const float4 *__restrict__ posf, const int4 *__restrict__ ainfo,
-                              int4 *__restrict__ cell_pos) {
+                              int4 *__restrict__ cell_pos, int *__restrict__ slot_of) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int j = list[k];
+  if (slot_of) slot_of[j] = k;
   if (posi) {
     cell_pos[k] = posi[j];
   } else {
@@ -247,13 +248,15 @@ __global__ void __launch_bounds__(BLK) k_build(
           unsigned ms = __ballot_sync(0xffffffffu, kind == 1 || kind == 3);
           unsigned ml = __ballot_sync(0xffffffffu, kind == 2);
           unsigned lower = (1u << lane) - 1u;
+          // full rows (mixed path) hold the neighbour's cell-order slot
+          const int v = full ? base + lane : j;
           if (kind == 1 || kind == 3) {
             int k = ns + __popc(ms & lower);
             if (k < cap_s)
-              ns_idx[list_slot(i, k, cap_s, full)] = j | (kind == 3 ? (int)0x80000000 : 0);
+              ns_idx[list_slot(i, k, cap_s, full)] = v | (kind == 3 ? (int)0x80000000 : 0);
           } else if (kind == 2) {
             int k = nl + __popc(ml & lower);
-            if (k < cap_l) nl_idx[list_slot(i, k, cap_l, false)] = j;
+            if (k < cap_l) nl_idx[list_slot(i, k, cap_l, false)] = v;
           }
           ns += __popc(ms);
           nl += __popc(ml);
@@ -329,6 +332,15 @@ int launch_mirror_f32(mdx_ctx *ctx) {
       d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
       1.0 / ctx->boyl, 1.0 / ctx->bozl);
   MDX_LAUNCHED(ctx);
+  return launch_cell_refresh(ctx);
+}
+
+int launch_cell_refresh(mdx_ctx *ctx) {
+  if (!ctx->mixed() || !ctx->have_lists) return MDX_OK;
+  DevData &d = ctx->dv;
+  k_cell_gather<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
+      d.n, d.cell_list, d.posi, d.posf, d.ainfo, d.cell_pos, nullptr);
+  MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
 
@@ -382,7 +394,8 @@ int launch_build_lists(mdx_ctx *ctx) {
                                                           d.cell_list);
   MDX_LAUNCHED(ctx);
   k_cell_gather<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
-      d.n, d.cell_list, ctx->mixed() ? d.posi : nullptr, d.posf, d.ainfo, d.cell_pos);
+      d.n, d.cell_list, ctx->mixed() ? d.posi : nullptr, d.posf, d.ainfo, d.cell_pos,
+      ctx->mixed() ? d.slot_of : nullptr);
   MDX_LAUNCHED(ctx);
   int *need = d.shake_iter + 4;  // two ints of scratch after the SHAKE counter
   MDX_CUDA(cudaMemsetAsync(need, 0, sizeof(int) * 2, ctx->stream));
@@ -422,6 +435,12 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
   MDX_CUDA(ctx_copy(ctx->stream, cl.data(), d.nl_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost));
   MDX_CUDA(ctx_copy(ctx->stream, rs.data(), d.ns_idx, sizeof(int) * rs.size(), cudaMemcpyDeviceToHost));
   MDX_CUDA(ctx_copy(ctx->stream, rl.data(), d.nl_idx, sizeof(int) * rl.size(), cudaMemcpyDeviceToHost));
+  std::vector<int> slot_atom;  // mixed path: rows hold cell-order slots
+  if (tiled) {
+    slot_atom.resize(n);
+    MDX_CUDA(ctx_copy(ctx->stream, slot_atom.data(), d.cell_list, sizeof(int) * n,
+                      cudaMemcpyDeviceToHost));
+  }
   long ks = 0, kl = 0;
   std::vector<int> row;
   for (int i = 0; i < n; ++i) {
@@ -430,8 +449,9 @@ int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
       const int cnt = pass == 0 ? cs[i] : cl[i];
       row.clear();
       for (int k = 0; k < cnt; ++k) {
-        const int src_k = pass == 0 ? rs[list_slot(i, k, d.cap_s, tiled)]
-                                    : rl[list_slot(i, k, d.cap_l, false)];
+        int src_k = pass == 0 ? rs[list_slot(i, k, d.cap_s, tiled)]
+                              : rl[list_slot(i, k, d.cap_l, false)];
+        if (tiled) src_k = (src_k & (int)0x80000000) | slot_atom[src_k & 0x7fffffff];
         // the mixed path keeps full rows (each pair in both atoms' rows);
         // the reference list holds the owner's copy only
         const int j = src_k & 0x7fffffff;

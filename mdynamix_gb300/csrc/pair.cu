@@ -251,7 +251,8 @@ __device__ __forceinline__ float idiff(int a, int b, float s) {
 // measured 12 % faster than the uncapped 44-64 registers).
 template <bool SHORT, bool SPLIT, bool ENER>
 __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
-    int n, const int4 *__restrict__ posi, const float4 *__restrict__ stab,
+    int n, const int4 *__restrict__ posi, const int4 *__restrict__ posn,
+    const float4 *__restrict__ stab,
     const int *__restrict__ cnt, const int *__restrict__ idx, int cap,
     PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
     FixScale fsc, unsigned long long *__restrict__ ffix,
@@ -300,14 +301,16 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     const int *row = idx + list_slot(i, 0, cap, SHORT);
     const int rs = SHORT ? 32 : 1;  // stride of consecutive entries
     // the next entry's index and record are loaded while this one computes
+    // entries are cell-order slots of posn (the neighbours' records in the
+    // order of the cell grid: neighbours of one owner lie in a few runs)
     int v = k0 < c ? row[(size_t)k0 * rs] : 0;
-    int4 pj = posi[v & 0x7fffffff];
+    int4 pj = posn[v & 0x7fffffff];
     for (int k = k0; k < c; k += kstep) {
       int vn = 0;
       int4 pjn = pj;
       if (k + kstep < c) {
         vn = row[(size_t)(k + kstep) * rs];
-        pjn = posi[vn & 0x7fffffff];
+        pjn = posn[vn & 0x7fffffff];
       }
       const bool is14 = SHORT && v < 0;
       const float4 stj = __ldg(&stab[(unsigned)pj.w & SITE_MASK]);
@@ -578,11 +581,11 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const int grid32 = shrt ? (2 * d.n + T - 1) / T : grid;  // short: 2 threads per atom
 #define LP32(S, P)                                                                \
   if (ener) k_pair32<S, P, true><<<grid32, T, 0, ctx->stream>>>(                  \
-      d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
+      d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf);                                        \
   else k_pair32<S, P, false><<<grid32, T, 0, ctx->stream>>>(                      \
-      d.n, d.posi, d.stab, cnt, idx, cap, tables(d),                             \
+      d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf)
     if (shrt) {
