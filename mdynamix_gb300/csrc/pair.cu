@@ -241,6 +241,7 @@ __global__ void k_wir_fix(int n, const dbl4 *__restrict__ pos,
 
 // ---------------------------------------------------------------- mixed ---
 constexpr int PAIR32_BLOCKS = 6;  // resident blocks per SM the register cap aims at
+constexpr int SPO = 4;  // threads per owner atom of the short sweep (adjacent lanes; 4: 5 % faster than 2)
 
 __device__ __forceinline__ float idiff(int a, int b, float s) {
   return (float)(int)((unsigned)a - (unsigned)b) * s;
@@ -264,14 +265,14 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
     __syncthreads();
   }
-  // short rows (about 50 entries): two threads per owner atom over its tiled
+  // short rows (about 50 entries): SPO threads per owner atom over its tiled
   // row (list_slot; entry k of 32 atoms in one 128-byte line), even and odd
   // entries; long rows (several hundred entries): warp per owner atom, lanes
   // stride the row
   const int lane = threadIdx.x & 31;
-  const int i = SHORT ? (blockIdx.x * blockDim.x + threadIdx.x) >> 1
+  const int i = SHORT ? (blockIdx.x * blockDim.x + threadIdx.x) / SPO
                       : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int k0 = SHORT ? (lane & 1) : lane, kstep = SHORT ? 2 : 32;
+  const int k0 = SHORT ? lane % SPO : lane, kstep = SHORT ? SPO : 32;
   long long tot[P_NSLOT];
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
@@ -433,11 +434,14 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
       }
     }
   }
-  if (SHORT) {  // the owner's two threads are adjacent lanes; every lane takes part
-    qx += __shfl_xor_sync(0xffffffffu, qx, 1);
-    qy += __shfl_xor_sync(0xffffffffu, qy, 1);
-    qz += __shfl_xor_sync(0xffffffffu, qz, 1);
-    if (i < n && (lane & 1) == 0) {
+  if (SHORT) {  // the owner's threads are adjacent lanes; every lane takes part
+#pragma unroll
+    for (int o = 1; o < SPO; o <<= 1) {
+      qx += __shfl_xor_sync(0xffffffffu, qx, o);
+      qy += __shfl_xor_sync(0xffffffffu, qy, o);
+      qz += __shfl_xor_sync(0xffffffffu, qz, o);
+    }
+    if (i < n && lane % SPO == 0) {
       ffix[i] = (unsigned long long)qx;
       ffix[n + i] = (unsigned long long)qy;
       ffix[2 * n + i] = (unsigned long long)qz;
@@ -578,7 +582,7 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
-    const int grid32 = shrt ? (2 * d.n + T - 1) / T : grid;  // short: 2 threads per atom
+    const int grid32 = shrt ? (SPO * d.n + T - 1) / T : grid;  // short: SPO threads per atom
 #define LP32(S, P)                                                                \
   if (ener) k_pair32<S, P, true><<<grid32, T, 0, ctx->stream>>>(                  \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
