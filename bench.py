@@ -448,7 +448,7 @@ def reference_arm(args, rank, world):
     o.set_state(*st)
     t0 = time.perf_counter(); o.chcnb(); t_list = time.perf_counter() - t0
     o.getcom(); o.slforces(); o.fforces()
-    w = min(args.warmup, 1)
+    w = min(args.warmup, 3)  # warm-up long steps (2-3 s each on the CPU), at most three
     if w:
         o.double_steps(w, 0)
     # bounded sample: at most ~3 minutes of timed CPU work
