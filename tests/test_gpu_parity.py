@@ -106,6 +106,27 @@ def test_double_fp64(name):
             assert abs(getattr(a, n) - getattr(b, n)) <= 1e-8 * max(abs(getattr(b, n)), 1e-12), n
 
 
+def test_double_mixed_tracks_fp64():
+    """Mixed DOUBLE long steps stay on the FP64 trajectory: methanol and
+    ethanol (more than four atoms: the per-molecule update) and water (the
+    register path), a list rebuild inside the run (ICHNB 10); positions
+    within 1e-5 A after 11 long steps, energies within 1e-4."""
+    s, st = CASES["organics"]()
+    out = {}
+    for prec in (MDX_FP64, MDX_MIXED):
+        g = ForcePath(s, precision=prec)
+        g.set_state(*st)
+        rec = g.double(11)
+        (x, y, z, *_), _ = g.get_state()
+        out[prec] = (np.stack([x, y, z]), rec)
+        g.close()
+    dpos = np.abs(out[MDX_MIXED][0] - out[MDX_FP64][0]).max()
+    assert dpos < 1e-5, dpos
+    for a, b in zip(out[MDX_MIXED][1], out[MDX_FP64][1]):
+        for n in ("pe1", "pels1", "pe2", "pels2", "pint", "tke"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * max(abs(getattr(b, n)), 1e-9), n
+
+
 def test_sultan_shake_fp64():
     s, st, g, o = pair("spce_ions")
     rg = g.sultan(3)
