@@ -671,7 +671,7 @@ template <typename R>
 __device__ __forceinline__ void eterms_pair(
     int isp, int jsp, int ityp, const dbl4 &pi, const dbl4 &pj, double coulf,
     double alphad, double bx, double by, double bz, const TypeConst &tc,
-    double *acc, double *gx, double *gy, double *gz,
+    R *acc, double *gx, double *gy, double *gz,
     unsigned long long *gfix, int n, float fscalef) {
   double DXd = pi.x - pj.x, DYd = pi.y - pj.y, DZd = pi.z - pj.z;
   pbc_rect(DXd, DYd, DZd, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
@@ -687,7 +687,7 @@ __device__ __forceinline__ void eterms_pair(
   const R ERFC = (((((R)MDX_A5 * TTT + (R)MDX_A4) * TTT + (R)MDX_A3) * TTT + (R)MDX_A2) * TTT +
                   (R)MDX_A1) * TTT * EXP2A;
   const R EES = QIJ * (ERFC - R(1)) * R1I;
-  acc[0] += (double)EES;
+  acc[0] += EES;
   if (tc.lmove[ityp]) {
     const R FES = QIJ * (((R)MDX_TOTPI * ALPHAR * EXP2A + ERFC) - R(1)) * R1I * R2I;
     const R FX = FES * DX, FY = FES * DY, FZ = FES * DZ;
@@ -708,9 +708,9 @@ __device__ __forceinline__ void eterms_pair(
       atomicAdd(&gy[jsp], -(double)FY);
       atomicAdd(&gz[jsp], -(double)FZ);
     }
-    acc[1] += (double)(FES * (DX * DX));
-    acc[2] += (double)(FES * (DY * DY));
-    acc[3] += (double)(FES * (DZ * DZ));
+    acc[1] += FES * (DX * DX);
+    acc[2] += FES * (DY * DY);
+    acc[3] += FES * (DZ * DZ);
   }
 }
 
@@ -727,11 +727,13 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
   __shared__ double spee_sh[MDX_NT];
   if (threadIdx.x < MDX_NT) spee_sh[threadIdx.x] = 0.0;
   __syncthreads();
-  double acc[4] = {0, 0, 0, 0};
+  R acc[4] = {0, 0, 0, 0};  // a thread's few terms: FP32 sums on the mixed path
   const int isp = blockIdx.x * blockDim.x + threadIdx.x;
+  int typ = -1;
   if (isp < n) {
     const int4 ai = ainfo[isp];
     const int ityp = ai.x;
+    typ = ityp;
     const dbl4 pi = pos[isp];
     if (tc.iee[ityp] != 0) {
       const int nb = nnbb[isp];
@@ -751,9 +753,24 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
     }
     // SPEE of the atom's type: the thread's own sum (one shared atomic per
     // thread, not per pair)
-    if (acc[0] != 0.0) atomicAdd(&spee_sh[ityp], acc[0]);
+    if (sizeof(R) == sizeof(double) && acc[0] != R(0)) atomicAdd(&spee_sh[ityp], (double)acc[0]);
   }
-  block_add<4>(acc, dst);
+  if (sizeof(R) == sizeof(double)) {
+    double a[4] = {(double)acc[0], (double)acc[1], (double)acc[2], (double)acc[3]};
+    block_add<4>(a, dst);
+  } else {
+    // warp sums in FP32 (a few terms a lane), then the FP64 block sums; SPEE
+    // by warp when the warp's atoms share a type
+    const int lane = threadIdx.x & 31;
+    const int t0 = __shfl_sync(0xffffffffu, typ, 0);
+    const bool uni = __all_sync(0xffffffffu, typ == t0 || typ < 0);
+    if (!uni && typ >= 0 && acc[0] != R(0)) atomicAdd(&spee_sh[typ], (double)acc[0]);
+    double a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = (double)warp_sumf((float)acc[k]);
+    if (uni && lane == 0 && t0 >= 0 && a[0] != 0.0) atomicAdd(&spee_sh[t0], a[0]);
+    block_add_core<4, true>(a, dst.p, dst.part, dst.ctr);
+  }
   if (threadIdx.x < MDX_NT && spee_sh[threadIdx.x] != 0.0)
     atomicAdd(&spee[threadIdx.x], spee_sh[threadIdx.x]);
 }

@@ -406,15 +406,19 @@ __device__ __forceinline__ float warp_sumf(float v) {
 // *ctr) sums the partials in block order and adds once to dst, then resets
 // the counter for the next launch on the stream.  Without one, each block
 // adds with atomicAdd (order-dependent in the last bit).
-template <int NV>
+// WARP_DONE: the caller has already summed each value over its warp (lane 0
+// holds the warp totals), e.g. in FP32 for a few terms a thread.
+template <int NV, bool WARP_DONE = false>
 __device__ __forceinline__ void block_add_core(double (&v)[NV], double *const *dst,
                                                double *part, unsigned *ctr) {
   __shared__ double sh[32][NV];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
+  if (!WARP_DONE) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+    for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  }
   if (lane == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) sh[wid][k] = v[k];
