@@ -128,7 +128,7 @@ __device__ __forceinline__ void add_force_own(const BondOut &o, int i, R fx, R f
 
 // One bond (GETBND forces.f:140-196): harmonic, or Morse for ID = 1 within
 // 2 REQ.  acc: PINT VIRB VIRFX VIRFY VIRFZ; *bd, *eb: length and energy.
-template <typename R, bool OWN>
+template <typename R, bool OWN, typename A = double>
 __device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, int J, int M,
                                           const int *__restrict__ bid,
                                           const double *__restrict__ rb,
@@ -136,7 +136,7 @@ __device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, i
                                           const double *__restrict__ db,
                                           const double *__restrict__ ro, int lmove,
                                           double bx, double by, double bz,
-                                          const BondOut &o, double *acc, R *bd, R *eb) {
+                                          const BondOut &o, A *acc, R *bd, R *eb) {
   R BX, BY, BZ;
   vec_r<R>(pos, o, J, I, bx, by, bz, BX, BY, BZ);
   const R REQ = (R)rb[M];
@@ -156,7 +156,7 @@ __device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, i
     EBDD = DDIS * (EXMP * EXMP);
     FORB = R(-2) * DDIS * ROH * EXM * EXMP * R1I;
   }
-  acc[0] += (double)EBDD;
+  acc[0] += (A)EBDD;
   *bd = BD;
   *eb = EBDD;
   if (lmove) {
@@ -167,21 +167,21 @@ __device__ __forceinline__ void bond_term(const dbl4 *__restrict__ pos, int I, i
       add_force<R>(o, I, -BX * FORB, -BY * FORB, -BZ * FORB);
       add_force<R>(o, J, BX * FORB, BY * FORB, BZ * FORB);
     }
-    acc[1] += (double)(FORB * BSQ);
-    acc[2] += (double)(FORB * (BX * BX));
-    acc[3] += (double)(FORB * (BY * BY));
-    acc[4] += (double)(FORB * (BZ * BZ));
+    acc[1] += (A)(FORB * BSQ);
+    acc[2] += (A)(FORB * (BX * BX));
+    acc[3] += (A)(FORB * (BY * BY));
+    acc[4] += (A)(FORB * (BZ * BZ));
   }
 }
 
 // One angle (GETANG forces.f:230-303), harmonic in theta.
 // acc: PINT VIRB(unused) VIRFX VIRFY VIRFZ; *alf, *ea: angle and energy.
-template <typename R, bool OWN>
+template <typename R, bool OWN, typename A = double>
 __device__ __forceinline__ void angle_term(const dbl4 *__restrict__ pos, int I, int J, int K,
                                            int M, const double *__restrict__ ra,
                                            const double *__restrict__ fa, int lmove,
                                            double bx, double by, double bz,
-                                           const BondOut &o, double *acc, R *alf, R *ea) {
+                                           const BondOut &o, A *acc, R *alf, R *ea) {
   const R FCN = (R)fa[M], AEQ = (R)ra[M];
   R AX, AY, AZ, BX, BY, BZ;
   vec_r<R>(pos, o, I, J, bx, by, bz, AX, AY, AZ);
@@ -202,7 +202,7 @@ __device__ __forceinline__ void angle_term(const dbl4 *__restrict__ pos, int I, 
   const R DALF = ALF - AEQ;
   const R ABC = DALF * FCN;
   const R EANG = ABC * DALF;
-  acc[0] += (double)EANG;
+  acc[0] += (A)EANG;
   *alf = ALF;
   *ea = EANG;
   if (lmove) {
@@ -222,9 +222,9 @@ __device__ __forceinline__ void angle_term(const dbl4 *__restrict__ pos, int I, 
       add_force<R>(o, J, FAX + FBX, FAY + FBY, FAZ + FBZ);
       add_force<R>(o, K, -FBX, -FBY, -FBZ);
     }
-    acc[2] += (double)(-AX * FAX - BX * FBX);
-    acc[3] += (double)(-AY * FAY - BY * FBY);
-    acc[4] += (double)(-AZ * FAZ - BZ * FBZ);
+    acc[2] += (A)(-AX * FAX - BX * FBX);
+    acc[3] += (A)(-AY * FAY - BY * FBY);
+    acc[4] += (A)(-AZ * FAZ - BZ * FBZ);
   }
 }
 
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(128) k_molbonded(
     for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x) sav[k / 256][k % 256] = 0.0;
     __syncthreads();
   }
-  double acc[5] = {0, 0, 0, 0, 0};  // PINT VIRB VIRFX VIRFY VIRFZ
+  R acc[5] = {0, 0, 0, 0, 0};  // PINT VIRB VIRFX VIRFY VIRFZ (a molecule's few terms)
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int t = 0;
   while (t < ntpl && g >= tpl[t].nmol) {
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(128) k_molbonded(
     for (int b = 0; b < T.nb; ++b) {
       const int M = T.bm[b];
       R BD, EB;
-      bond_term<R, true>(pos, base + T.bi[b], base + T.bj[b], M, bid, rb, fb, db, ro, lmove,
+      bond_term<R, true, R>(pos, base + T.bi[b], base + T.bj[b], M, bid, rb, fb, db, ro, lmove,
                          bx, by, bz, o, acc, &BD, &EB);
       if (laver) {
         avg_add(sav[0], br, M, nrbb, (double)BD * fnspi);
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(128) k_molbonded(
     for (int a = 0; a < T.na; ++a) {
       const int M = T.am[a];
       R ALF, EA;
-      angle_term<R, true>(pos, base + T.ai[a], base + T.aj[a], base + T.ak[a], M, ra, fa,
+      angle_term<R, true, R>(pos, base + T.ai[a], base + T.aj[a], base + T.ak[a], M, ra, fa,
                           lmove, bx, by, bz, o, acc, &ALF, &EA);
       if (laver) {
         avg_add(sav[2], ar, M, nraa, (double)ALF * fnspi);
@@ -358,7 +358,18 @@ __global__ void __launch_bounds__(128) k_molbonded(
       }
     }
   }
-  if (ENER) block_add<5>(acc, dst);
+  if (ENER) {
+    double a[5];
+    if (sizeof(R) == sizeof(double)) {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) a[k] = (double)acc[k];
+      block_add<5>(a, dst);
+    } else {  // warp sums in FP32, then the FP64 block sums
+#pragma unroll
+      for (int k = 0; k < 5; ++k) a[k] = (double)warp_sumf((float)acc[k]);
+      block_add_core<5, true>(a, dst.p, dst.part, dst.ctr);
+    }
+  }
   if (laver) {
     __syncthreads();
     if (nrbb <= 256)

@@ -392,40 +392,51 @@ __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
 // ekin layout as the reference's EKIN: [0..ntypes-1] per type, then total,
 // VIRKX, VIRKY, VIRKZ.
 // NT >= ntypes: per-type sums carried (NT + 4 values reduced; the unused
-// types of ekacc are left alone).
-template <int NT>
+// types of ekacc are left alone).  R = float (mixed path): the per-atom
+// terms and the warp sums in FP32 (a few atoms a thread, 32 threads a warp),
+// the block and grid sums in FP64.
+template <int NT, typename R>
 __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
                          int ntypes, const double *__restrict__ massdi,
                          const double *__restrict__ vx,
                          const double *__restrict__ vy,
                          const double *__restrict__ vz, double *ekacc,
                          double *part, unsigned *ctr) {
-  double e[NT + 4];
+  R e[NT + 4];
 #pragma unroll
-  for (int k = 0; k < NT + 4; ++k) e[k] = 0.0;
+  for (int k = 0; k < NT + 4; ++k) e[k] = R(0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
     const int t = ainfo[i].x;
     if (!mv.lmove[t]) continue;
-    const double m = massdi[i];
-    const double VVX = m * (vx[i] * vx[i]);
-    const double VVY = m * (vy[i] * vy[i]);
-    const double VVZ = m * (vz[i] * vz[i]);
-    const double VSC = VVX + VVY + VVZ;
+    const R m = (R)massdi[i], ux = (R)vx[i], uy = (R)vy[i], uz = (R)vz[i];
+    const R VVX = m * (ux * ux);
+    const R VVY = m * (uy * uy);
+    const R VVZ = m * (uz * uz);
+    const R VSC = VVX + VVY + VVZ;
     e[NT + 1] += VVX;
     e[NT + 2] += VVY;
     e[NT + 3] += VVZ;
     e[NT] += VSC;
 #pragma unroll
     for (int k = 0; k < NT; ++k)
-      if (k == t) e[k] += 0.5 * VSC;
+      if (k == t) e[k] += R(0.5) * VSC;
   }
   // value k < NT -> ekacc[k] (type k), NT + j -> ekacc[MDX_NT + j]
   double *dst[NT + 4];
 #pragma unroll
   for (int k = 0; k < NT + 4; ++k)
     dst[k] = k < NT ? (k < ntypes ? ekacc + k : nullptr) : ekacc + MDX_NT + (k - NT);
-  block_add_core<NT + 4>(e, dst, part, ctr);
+  double ed[NT + 4];
+  if (sizeof(R) == sizeof(double)) {
+#pragma unroll
+    for (int k = 0; k < NT + 4; ++k) ed[k] = (double)e[k];
+    block_add_core<NT + 4>(ed, dst, part, ctr);
+  } else {
+#pragma unroll
+    for (int k = 0; k < NT + 4; ++k) ed[k] = (double)warp_sumf((float)e[k]);
+    block_add_core<NT + 4, true>(ed, dst, part, ctr);
+  }
 }
 
 // Device scratch of SCALING between stages.
@@ -1084,10 +1095,17 @@ struct StageQ {
 static int getemp_kernel(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   const int nt = ctx->d.ntypes;
-#define GETEMP(NT)                                                                       \
-  k_getemp<NT><<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), nt, d.massdi, \
-                                             d.vx, d.vy, d.vz, scratch(ctx)->ekacc,      \
-                                             d.red_part, d.red_ctr)
+#define GETEMP(NT)                                                                    \
+  do {                                                                                \
+    if (ctx->mixed())                                                                 \
+      k_getemp<NT, float><<<ctx->nsm, 256, 0, ctx->stream>>>(                         \
+          d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,              \
+          scratch(ctx)->ekacc, d.red_part, d.red_ctr);                                \
+    else                                                                              \
+      k_getemp<NT, double><<<ctx->nsm, 256, 0, ctx->stream>>>(                        \
+          d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,              \
+          scratch(ctx)->ekacc, d.red_part, d.red_ctr);                                \
+  } while (0)
   if (nt <= 1) GETEMP(1);
   else if (nt <= 2) GETEMP(2);
   else if (nt <= 4) GETEMP(4);
