@@ -82,10 +82,33 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
                          double iby, double ibz, int kx, int ky, int kz,
                          double2 *__restrict__ tx, double2 *__restrict__ ty,
                          double2 *__restrict__ tz, float2 *__restrict__ txf,
-                         float2 *__restrict__ tyf, float2 *__restrict__ tzf) {
+                         float2 *__restrict__ tyf, float2 *__restrict__ tzf,
+                         const int4 *__restrict__ posi) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 3 * n) return;
   const int a = t / n, i = t - a * n;
+  if (txf) {
+    // mixed path, FP32 table (row stride ldn): every entry from its own
+    // phase.  k times the 32-bit fixed-point coordinate is k x / L modulo
+    // one turn, exactly (integer wrap-around), a signed fraction of half a
+    // turn in units of 2^-31.  Its top 24 bits are exact in FP32 and go to
+    // sincospif; the low 8 bits (under 3.7e-7 rad) rotate the result to
+    // first order.  No recurrence, no FP64 work.
+    const int4 pq = posi[i];
+    const unsigned u = (unsigned)(a == 0 ? pq.x : a == 1 ? pq.y : pq.z);
+    const float qf = a == 0 ? (float)pos[i].w : 1.0f;
+    const int len = a == 0 ? kx : a == 1 ? ky : kz;
+    float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
+    for (int k = 0; k < len; ++k) {
+      const int ph = (int)((unsigned)k * u);
+      const int hi = ph & ~0xff, lo = ph - hi;
+      float s, c;
+      sincospif((float)hi * 4.656612873077393e-10f, &s, &c);  // 2^-31
+      const float d = (float)lo * 1.4629180792671596e-09f;    // pi 2^-31
+      dst[(size_t)k * ldn] = make_float2(qf * fmaf(-s, d, c), qf * fmaf(c, d, s));
+    }
+    return;
+  }
   const dbl4 p = pos[i];
   const double x = a == 0 ? p.x * ibx : a == 1 ? p.y * iby : p.z * ibz;
   double s, c;
@@ -95,30 +118,10 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
   const int len = a == 0 ? kx : a == 1 ? ky : kz;
   const double q = a == 0 ? p.w : 1.0;
   double2 v = make_double2(1.0, 0.0);
-  if (txf) {
-    // mixed path, FP32 table (row stride ldn): FP64 anchors e^{i 4m theta}
-    // from the FP64 recurrence, the three entries after each anchor as FP32
-    // products with e, e^2, e^3 (about 2 ulp of FP32 against the exact
-    // phase, a quarter of the FP64 work)
-    float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
-    const double2 e2 = cmul(e, e), e3 = cmul(e2, e), e4 = cmul(e2, e2);
-    const float2 f1 = make_float2((float)e.x, (float)e.y);
-    const float2 f2 = make_float2((float)e2.x, (float)e2.y);
-    const float2 f3 = make_float2((float)e3.x, (float)e3.y);
-    for (int k = 0; k < len; k += 4) {
-      const float2 an = make_float2((float)(q * v.x), (float)(q * v.y));
-      dst[(size_t)k * ldn] = an;
-      if (k + 1 < len) dst[(size_t)(k + 1) * ldn] = cmulf(an, f1);
-      if (k + 2 < len) dst[(size_t)(k + 2) * ldn] = cmulf(an, f2);
-      if (k + 3 < len) dst[(size_t)(k + 3) * ldn] = cmulf(an, f3);
-      v = cmul(v, e4);
-    }
-  } else {
-    double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + i;
-    for (int k = 0; k < len; ++k) {
-      dst[(size_t)k * n] = make_double2(q * v.x, q * v.y);
-      v = cmul(v, e);
-    }
+  double2 *dst = (a == 0 ? tx : a == 1 ? ty : tz) + i;
+  for (int k = 0; k < len; ++k) {
+    dst[(size_t)k * n] = make_double2(q * v.x, q * v.y);
+    v = cmul(v, e);
   }
 }
 
@@ -1101,7 +1104,7 @@ int launch_furir(mdx_ctx *ctx) {
     MDX_TIMER(ctx, MDX_T_EW_TABLES);
     k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
         d.n, d.ldn, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
-        d.tabxf, d.tabyf, d.tabzf);
+        d.tabxf, d.tabyf, d.tabzf, mx ? d.posi : nullptr);
     MDX_LAUNCHED(ctx);
     if (mx && (rc = tc_zimages_launch(ctx))) return rc;
   }
