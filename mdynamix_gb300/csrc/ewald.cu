@@ -126,7 +126,7 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
 }
 
 // Write one paired accumulator as S(c, +p) and S(c, -p) (each only if the
-// k-vector exists): slice partial (summed in slice order by k_sfac_sum) or
+// k-vector exists): slice partial (summed in a fixed order by k_sfac_sum) or
 // atomic.
 __device__ __forceinline__ void sfac_out(const KCol &col, int p, double A1, double A2,
                                          double A3, double A4, double2 *part, double2 *sk) {
@@ -330,17 +330,34 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
 }
 
 // S(k) = sum of the slice partials in slice order (deterministic).
-__global__ void k_sfac_sum(int nkv, int nslice, const double2 *__restrict__ part,
-                           double2 *__restrict__ sk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nkv) return;
+constexpr int SUM_K = 32, SUM_G = 8;  // k-vectors and slice groups of a block
+
+// S(k) = the sum of the slice partials: thread (k, g) adds slices g, g +
+// SUM_G, ... in order, then the groups are added in group order (a fixed
+// order: deterministic); reads are coalesced over k.
+__global__ void __launch_bounds__(SUM_K * SUM_G) k_sfac_sum(int nkv, int nslice,
+                                                         const double2 *__restrict__ part,
+                                                         double2 *__restrict__ sk) {
+  __shared__ double2 sh[SUM_G][SUM_K];
+  const int kl = threadIdx.x % SUM_K, g = threadIdx.x / SUM_K;
+  const int k = blockIdx.x * SUM_K + kl;
   double x = 0.0, y = 0.0;
-  for (int s = 0; s < nslice; ++s) {
-    const double2 v = part[(size_t)s * nkv + k];
-    x += v.x;
-    y += v.y;
+  if (k < nkv)
+    for (int s = g; s < nslice; s += SUM_G) {
+      const double2 v = part[(size_t)s * nkv + k];
+      x += v.x;
+      y += v.y;
+    }
+  sh[g][kl] = make_double2(x, y);
+  __syncthreads();
+  if (g == 0 && k < nkv) {
+#pragma unroll
+    for (int q = 1; q < SUM_G; ++q) {
+      x += sh[q][kl].x;
+      y += sh[q][kl].y;
+    }
+    sk[k] = make_double2(x, y);
   }
-  sk[k] = make_double2(x, y);
 }
 
 // Per k: energy and virial terms (forces.f:1316-1331), W_k and RZV W_k.
@@ -1131,7 +1148,7 @@ int launch_furir(mdx_ctx *ctx) {
       MDX_LAUNCHED(ctx);
     }
     if (d.sk_part && !(mx && d.tcs_on)) {
-      k_sfac_sum<<<(d.nkv + 255) / 256, 256, 0, ctx->stream>>>(d.nkv, (int)grid.y,
+      k_sfac_sum<<<(d.nkv + SUM_K - 1) / SUM_K, SUM_K * SUM_G, 0, ctx->stream>>>(d.nkv, (int)grid.y,
                                                                 d.sk_part, d.sk);
       MDX_LAUNCHED(ctx);
     }
