@@ -361,13 +361,12 @@ __global__ void __launch_bounds__(SUM_K * SUM_G) k_sfac_sum(int nkv, int nslice,
 }
 
 // Per k: energy and virial terms (forces.f:1316-1331), W_k and RZV W_k.
-__global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
-                         const double2 *__restrict__ sk, double bx, double by,
-                         double bz, double alp2, double cfur,
-                         dbl4 *__restrict__ wk,
-                         double2 *__restrict__ colrv, float2 *__restrict__ colrvf,
-                         Dst6 dst) {
-  double acc[4] = {0, 0, 0, 0};
+// Per-k constants of FURIR that depend on the box and alpha only (forces.f:
+// 1316-1331): AKC, (RXV^2, RYV^2, RZV^2) AKV and RZV, five doubles per k,
+// and the column's (RXV, RYV); rebuilt when the box or alpha changes.
+__global__ void k_kconst(int ncol, const KCol *__restrict__ cols, double bx, double by,
+                         double bz, double alp2, double cfur, double *__restrict__ kc,
+                         double2 *__restrict__ colrv, float2 *__restrict__ colrvf) {
   const double twopi = 2.0 * PI_REF;
   for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
     const KCol col = cols[c];
@@ -384,23 +383,41 @@ __global__ void k_kterms(int ncol, const KCol *__restrict__ cols,
       const double RYV = (twopi * col.ny) / by;
       const double RZV = (twopi * nz) / bz;
       const double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
-      const double2 S = sk[k];
-      const double SCS = S.x, SSN = S.y;
       const double AKC = cfur * exp(-0.25 * RK2 / alp2) / RK2;
-      const double S2 = SSN * SSN + SCS * SCS;
-      acc[0] += AKC * S2;
       const double AKV = 0.5 * AKC * (4. * alp2 + RK2) / (alp2 * RK2);
-      acc[1] -= (RXV * RXV) * AKV * S2;
-      acc[2] -= (RYV * RYV) * AKV * S2;
-      acc[3] -= (RZV * RZV) * AKV * S2;
-      const double AK2 = 2.0 * AKC;
-      dbl4 W;
-      W.x = AK2 * SCS;
-      W.y = -AK2 * SSN;
-      W.z = RZV * W.x;
-      W.w = RZV * W.y;
-      wk[k] = W;
+      double *q = kc + 5 * (size_t)k;
+      q[0] = AKC;
+      q[1] = (RXV * RXV) * AKV;
+      q[2] = (RYV * RYV) * AKV;
+      q[3] = (RZV * RZV) * AKV;
+      q[4] = RZV;
     }
+  }
+}
+
+// Per k: energy and virial terms (forces.f:1316-1331), W_k and RZV W_k, from
+// S(k) and the per-k constants (the same products as the reference's
+// expressions, in its order).
+__global__ void k_kterms(int nkv, const double2 *__restrict__ sk,
+                         const double *__restrict__ kc, dbl4 *__restrict__ wk, Dst6 dst) {
+  double acc[4] = {0, 0, 0, 0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nkv; k += gridDim.x * blockDim.x) {
+    const double2 S = sk[k];
+    const double SCS = S.x, SSN = S.y;
+    const double *q = kc + 5 * (size_t)k;
+    const double AKC = q[0];
+    const double S2 = SSN * SSN + SCS * SCS;
+    acc[0] += AKC * S2;
+    acc[1] -= q[1] * S2;
+    acc[2] -= q[2] * S2;
+    acc[3] -= q[3] * S2;
+    const double AK2 = 2.0 * AKC;
+    dbl4 W;
+    W.x = AK2 * SCS;
+    W.y = -AK2 * SSN;
+    W.z = q[4] * W.x;
+    W.w = q[4] * W.y;
+    wk[k] = W;
   }
   block_add<4>(acc, dst);
 }
@@ -1043,7 +1060,11 @@ int host_inifur(mdx_ctx *ctx) {
     }
   }
   ctx_free(ctx, d.sk);
+  ctx_free(ctx, d.kconst);
+  d.kconst = nullptr;
+  ctx->kc_box[0] = -1.0;  // per-k constants rebuilt at the next FURIR
   const size_t nk = (size_t)std::max(1, nkv);
+  MDX_CUDA(ctx_alloc(ctx, &d.kconst, sizeof(double) * 5 * nk));
   const size_t nkp = (nk + 1) & ~(size_t)1;  // keeps wk 32-byte aligned
   const size_t nc = std::max<size_t>(1, cols.size());
   const size_t np64 = ctx->mixed() ? 0 : 2 * (size_t)poff;  // dbl4 records
@@ -1157,10 +1178,21 @@ int launch_furir(mdx_ctx *ctx) {
   mdx_scalars *sc = d.sc;
   {
     MDX_TIMER(ctx, MDX_T_EW_KTERMS);
-    Dst6 dst = dst6(ctx, std::min(d.ncol, 1024), 4, qpe, &sc->virx, &sc->viry, &sc->virz);
-    k_kterms<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-        d.ncol, d.cols, d.sk, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.wk, d.colrv,
-        d.colrvf, dst);
+    if (ctx->kc_box[0] != ctx->boxl || ctx->kc_box[1] != ctx->boyl ||
+        ctx->kc_box[2] != ctx->bozl || ctx->kc_box[3] != alp2 || ctx->kc_box[4] != cfur) {
+      k_kconst<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
+          d.ncol, d.cols, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.kconst, d.colrv,
+          d.colrvf);
+      MDX_LAUNCHED(ctx);
+      ctx->kc_box[0] = ctx->boxl;
+      ctx->kc_box[1] = ctx->boyl;
+      ctx->kc_box[2] = ctx->bozl;
+      ctx->kc_box[3] = alp2;
+      ctx->kc_box[4] = cfur;
+    }
+    const int kb = std::max(1, std::min((d.nkv + 127) / 128, 2 * ctx->nsm));
+    Dst6 dst = dst6(ctx, kb, 4, qpe, &sc->virx, &sc->viry, &sc->virz);
+    k_kterms<<<kb, 128, 0, ctx->stream>>>(d.nkv, d.sk, d.kconst, d.wk, dst);
     MDX_LAUNCHED(ctx);
     if (!(mx && d.tc_on)) {
       k_wpairs<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(

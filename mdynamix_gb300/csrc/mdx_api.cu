@@ -521,7 +521,7 @@ int mdx_close(mdx_ctx *ctx) {
                   d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
                   d.cell_cnt, d.cell_start, d.cell_list, d.cell_pos, d.slot_of, d.atom_cell, d.a6lj, d.a6f, d.abf,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
-                  d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
+                  d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.kconst, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
                   d.red_part, d.red_ctr, d.sk_part};
   if (ctx->stream) {

@@ -189,6 +189,7 @@ struct DevData {
   float2 *tabxf, *tabyf, *tabzf;
   double2 *sk;                  // structure factors, column order
   dbl4 *wk;                     // (W, RZV W) per k, W = AK2*conj(S)
+  double *kconst;               // per k: AKC, RXV^2 AKV, RYV^2 AKV, RZV^2 AKV, RZV
   dbl4 *wp64;                   // FP64 paired W: 2 per (column, p), at poff + p
   float4 *wkf;                  // mixed paired W, grouped (KGroup)
   // mixed pair path: posi.w = (molecule << MDX_SITE_BITS) | site, and per
@@ -250,6 +251,7 @@ struct mdx_ctx {
   cudaStream_t stream = nullptr;
   int device = 0;
   int nsm = 1;  // SMs of the device: grid of the grid-stride reductions (one block each)
+  double kc_box[5] = {-1.0, 0.0, 0.0, 0.0, 0.0};  // box, alpha^2, CFUR of dv.kconst
   int64_t launches = 0;
   bool have_topo = false, have_params = false, have_state = false,
        have_lists = false, have_com = false;
