@@ -126,7 +126,7 @@ __global__ void k_cell_gather(int n, const int *__restrict__ list, const int4 *_
   }
 }
 
-constexpr int CELL_REACH = 1;  // list cells per list radius (2 measured slower: 125 thin cells)
+constexpr int CELL_REACH = 2;  // list cells per list radius (a row of 5 thin cells is one run)
 
 // Ownership of pair (i, j) in the strip loop: i owns it when (i-j) is even
 // and j < i, or (i-j) is odd and j > i (forces.f:1834, 2014).
