@@ -53,15 +53,15 @@ OPS_EW_K = 20            # per k-vector (energy, virial, W)
 # `python bench.py --only {fp64,mixed} --steps 2 --warmup 3`
 # (dram__bytes_read.sum + dram__bytes_write.sum of every launch of the
 # group's kernels in one long step, MB).
-# fp64 ewald: k_tables 43.4 + k_sfac 126.1 + k_sfac_sum 51.3 + k_kterms 0.3
-#             + k_wpairs 0.6 + k_rforce64 102.8
-# mixed ewald: k_tables 3.2 + k_zimages 18.0 + k_sfac32 53.3 + k_sfac_sum 32.3
-#              + k_kterms 0.3 + k_wtiles 0.6 + k_rforce_tc 75.4
+# fp64 ewald: k_tables 43.4 + k_sfac 126.0 + k_sfac_sum 51.3 + k_kterms 1.0
+#             + k_wpairs 0.6 + k_rforce64 102.9
+# mixed ewald: k_tables 4.7 + k_zimages 18.1 + k_sfac32 53.4 + k_sfac_sum 32.4
+#              + k_kterms 1.0 + k_wtiles 0.6 + k_rforce_tc 75.4
 # fp64 pair: 9 x 30.7 (short, forces) + 30.7 (short, energies) + 153.1 (long)
-# mixed pair: 9 x 25.9 + 25.9 + 280.5
+# mixed pair: 9 x 25.9 + 25.9 + 280.4
 TRAFFIC_MB = {
-    ("fp64", "ewald"): 324.6, ("mixed", "ewald"): 183.2,
-    ("fp64", "pair"): 460.1, ("mixed", "pair"): 539.4,
+    ("fp64", "ewald"): 325.2, ("mixed", "ewald"): 185.5,
+    ("fp64", "pair"): 459.9, ("mixed", "pair"): 539.4,
 }
 
 
