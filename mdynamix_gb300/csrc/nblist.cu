@@ -5,14 +5,20 @@
 // parity, J > I).  That rule fixes which atom owns each pair; it is kept here
 // so that every owner row holds about half of the atom's neighbours (load
 // balance for free) and so that the export reproduces the reference's lists
-// entry for entry.  Candidates come from the 27 (or fewer, for small boxes)
-// neighbouring cells; each candidate is classified with the reference's exact
+// entry for entry (the mixed path keeps full rows: both owners).  Cells are
+// at least half the list radius wide; candidates come from the 5 x 5 x 5 (or
+// fewer, for small boxes) neighbouring cells, a stencil row of consecutive
+// cells read as one run of the cell-ordered candidate records; each
+// candidate is classified with the reference's exact
 // FP64 arithmetic (minimum image, RR2 <= RSSQ, RR2 <= SHORT2, the 8 A bound
 // on the intramolecular bonded check, 1-4 pairs to the short list), after an
 // FP32 prefilter that only decides pairs far from every boundary.
 //
 // Rows: nl_idx[i*cap_l + k] (long), ns_idx[i*cap_s + k] (short; bit 31 marks
-// a 1-4 pair), counts in nl_cnt / ns_cnt.  Row order is deterministic.
+// a 1-4 pair; the mixed path tiles short rows by 32 owners), counts in
+// nl_cnt / ns_cnt.  Entries are atom numbers (FP64 path) or cell-order slots
+// of the neighbour records (mixed path; mdx_get_lists maps them back).  Row
+// order is deterministic.
 #include <algorithm>
 #include <cmath>
 
