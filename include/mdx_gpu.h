@@ -12,6 +12,8 @@
  *   mdx_slforces     <- SLFORCES               forces.f:55-73
  *   mdx_allforce     <- ALLFORCE               forces.f:77-100
  *   mdx_getcom       <- GETCOM                 service.f:463-563
+ *   mdx_getkin       <- GETKIN (no GETROT)     service.f:611-735
+ *   mdx_chkmom       <- CHKMOM                 service.f:1081-1125
  *   mdx_double       <- DOUBLE (whole body)    mdstep.f:281-530
  *   mdx_double_steps <- DOUBLE loop 2.3 only   mdstep.f:324-436
  *   mdx_sultan       <- SULTAN (whole body)    mdstep.f:29-260
@@ -243,6 +245,22 @@ int mdx_chcnb(mdx_ctx *ctx, int32_t *mbsh, int32_t *mbln);
 int mdx_get_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                   int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
 int mdx_getcom(mdx_ctx *ctx);
+/* GETKIN: translational, rotational and internal kinetic energies and
+ * temperatures from the current momenta and the molecule-relative site
+ * vectors of the last GETCOM.  summd[t] = SUMMAS(t) / (AVSNO 1000 UNITM
+ * NBEADS) for the ntypes types; enerf_tempf = ENERF TEMPF; fnop, fnstr,
+ * fnsti = FNOP, FNSTR, FNSTI (main.f:297-346).  The molecular orientation
+ * analysis (GETROT, LMOL1/LMOL2) is not part of it. */
+typedef struct mdx_kin {
+  double ektr, ekrot, ekint, tke; /* EKTR, EKROT, EKINT, TKE */
+  double ttr, trot, tint;         /* TTR, TROT, TINT */
+} mdx_kin;
+int mdx_getkin(mdx_ctx *ctx, const double *summd, double enerf_tempf, double fnop,
+               double fnstr, double fnsti, mdx_kin *out);
+/* CHKMOM: removes the total momentum (sumasd = TOTMAS / UNITM) and updates
+ * the temperature as GETEMP; dv (optional) receives the removed DVX, DVY,
+ * DVZ. */
+int mdx_chkmom(mdx_ctx *ctx, double sumasd, double *dv);
 int mdx_fforces(mdx_ctx *ctx, int laver, mdx_scalars *out);
 int mdx_slforces(mdx_ctx *ctx, mdx_scalars *out);
 int mdx_allforce(mdx_ctx *ctx, mdx_scalars *out);

@@ -126,6 +126,12 @@ class MdxStepRecord(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MdxKin(C.Structure):
+    """mdx_kin: GETKIN's kinetic energies and temperatures."""
+    _fields_ = [(n, C.c_double) for n in ("ektr", "ekrot", "ekint", "tke", "ttr", "trot",
+                                          "tint")]
+
+
 class MdxPimdParams(C.Structure):
     _fields_ = [("nbeads", C.c_int32), ("jnh", C.c_int32), ("beadfac", C.c_double),
                 ("conveq", C.c_double), ("dqqt", C.c_double), ("fnh", C.c_double)]

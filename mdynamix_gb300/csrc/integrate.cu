@@ -1026,6 +1026,137 @@ MoveConst move_const(mdx_ctx *ctx) {
   for (int t = 0; t < MDX_NT; ++t) m.lmove[t] = ctx->tc.lmove[t];
   return m;
 }
+// ------------------------------------------------------------- observables
+// INV3B3 (util.f:89-125): inverse of a 3 x 3 matrix by cofactors; ier 1 when
+// |DET| < 1e-6 |trace|^3, 2 when DET = 0 (inverse set to zero).
+__device__ __forceinline__ void inv3b3(const double *A, double *AI, int &ier) {
+  AI[0] = A[4] * A[8] - A[5] * A[7];
+  AI[1] = A[2] * A[7] - A[1] * A[8];
+  AI[2] = A[1] * A[5] - A[2] * A[4];
+  AI[3] = A[5] * A[6] - A[3] * A[8];
+  AI[4] = A[0] * A[8] - A[2] * A[6];
+  AI[5] = A[2] * A[3] - A[0] * A[5];
+  AI[6] = A[3] * A[7] - A[4] * A[6];
+  AI[7] = A[1] * A[6] - A[0] * A[7];
+  AI[8] = A[0] * A[4] - A[1] * A[3];
+  const double det = A[0] * AI[0] + A[3] * AI[1] + A[6] * AI[2];
+  const double spur = A[0] + A[4] + A[8];
+  ier = fabs(det) < 1.e-6 * fabs(spur * spur * spur) ? 1 : 0;
+  double r = 0.0;
+  if (fabs(det) > 0.0) {
+    r = 1.0 / det;
+  } else {
+    ier = 2;
+  }
+  for (int k = 0; k < 9; ++k) AI[k] = r * AI[k];
+}
+
+struct KinConst {
+  double summd[MDX_NT];  // SUMMAS / (AVSNO 1000 UNITM NBEADS)
+  double summas[MDX_NT];
+};
+
+// GETKIN (service.f:611-735), thread per molecule: linear momentum and
+// translational kinetic energy, the inertia tensor of the site vectors W
+// (site position minus the molecule's centre, as GETCOM leaves them) with
+// MASSD = 1 / MASSDI, the angular momentum of the site momenta relative to
+// the molecule's, and the rotational kinetic energy (the reference's
+// fallback when the tensor is singular); EKTR, EKROT, TKE block-summed.
+__global__ void k_getkin(int nop, const int *__restrict__ mol_first,
+                         const int *__restrict__ mol_nat, const int *__restrict__ mol_type,
+                         KinConst kc, const double *__restrict__ amass,
+                         const double *__restrict__ massdi, const double *__restrict__ vx,
+                         const double *__restrict__ vy, const double *__restrict__ vz,
+                         const dbl4 *__restrict__ pos, const double *__restrict__ X,
+                         const double *__restrict__ Y, const double *__restrict__ Z, Dst6 dst) {
+  double acc[3] = {0.0, 0.0, 0.0};  // EKTR EKROT TKE
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nop) {
+    const int f = mol_first[m], na = mol_nat[m], t = mol_type[m];
+    double PX = 0.0, PY = 0.0, PZ = 0.0, tke = 0.0;
+    double TOR[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, TORI[9];
+    for (int k = 0; k < na; ++k) {
+      const int i = f + k;
+      const double u = vx[i], v = vy[i], w = vz[i];
+      PX = PX + u;
+      PY = PY + v;
+      PZ = PZ + w;
+      tke = tke + 0.5 * (u * u + v * v + w * w) * massdi[i];
+      const dbl4 p = pos[i];
+      const double wx = p.x - X[m], wy = p.y - Y[m], wz = p.z - Z[m];
+      const double md = 1.0 / massdi[i];
+      TOR[0] = TOR[0] + md * (wy * wy + wz * wz);
+      TOR[4] = TOR[4] + md * (wx * wx + wz * wz);
+      TOR[8] = TOR[8] + md * (wx * wx + wy * wy);
+      TOR[1] = TOR[1] - md * wx * wy;
+      TOR[2] = TOR[2] - md * wx * wz;
+      TOR[5] = TOR[5] - md * wy * wz;
+    }
+    TOR[3] = TOR[1];
+    TOR[6] = TOR[2];
+    TOR[7] = TOR[5];
+    int ier;
+    inv3b3(TOR, TORI, ier);
+    acc[0] = 0.5 * (PX * PX + PY * PY + PZ * PZ) / kc.summd[t];
+    acc[2] = tke;
+    double RX = 0.0, RY = 0.0, RZ = 0.0;
+    for (int k = 0; k < na; ++k) {
+      const int i = f + k;
+      const double fac = amass[i] / kc.summas[t];
+      const double vtx = vx[i] - PX * fac, vty = vy[i] - PY * fac, vtz = vz[i] - PZ * fac;
+      const dbl4 p = pos[i];
+      const double wx = p.x - X[m], wy = p.y - Y[m], wz = p.z - Z[m];
+      RX = RX + (vty * wz - wy * vtz);
+      RY = RY + (vtz * wx - wz * vtx);
+      RZ = RZ + (vtx * wy - wx * vty);
+    }
+    if (ier == 0) {
+      acc[1] = 0.5 * (TORI[0] * RX * RX + (TORI[1] + TORI[3]) * RX * RY + TORI[4] * RY * RY +
+                      (TORI[2] + TORI[6]) * RX * RZ + TORI[8] * RZ * RZ +
+                      (TORI[5] + TORI[7]) * RY * RZ);
+    } else {
+      const double PP = RX * RX + RY * RY + RZ * RZ;
+      if (PP >= 1.e-50) {
+        double ROTM = 0.0;
+        for (int k = 0; k < na; ++k) {
+          const int i = f + k;
+          const dbl4 p = pos[i];
+          const double wx = p.x - X[m], wy = p.y - Y[m], wz = p.z - Z[m];
+          const double SS = wx * wx + wy * wy + wz * wz;
+          const double SP = wx * RX + wy * RY + wz * RZ;
+          ROTM = ROTM + (1.0 / massdi[i]) * (SS * PP - SP * SP);
+        }
+        acc[1] = ROTM >= 1.e-50 ? 0.5 * PP * PP / ROTM : 0.0;
+      }
+    }
+  }
+  block_add<3>(acc, dst);
+}
+
+// CHKMOM (service.f:1081-1125): total momentum of all atoms, then
+// V -= (P / SUMASD) / MASSDI.
+__global__ void k_mom_sum(int n, const double *__restrict__ vx, const double *__restrict__ vy,
+                          const double *__restrict__ vz, Dst6 dst) {
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    acc[0] += vx[i];
+    acc[1] += vy[i];
+    acc[2] += vz[i];
+  }
+  block_add<3>(acc, dst);
+}
+
+__global__ void k_mom_remove(int n, double sumasd, const double *__restrict__ pt,
+                             const double *__restrict__ massdi, double *vx, double *vy,
+                             double *vz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dvx = pt[0] / sumasd, dvy = pt[1] / sumasd, dvz = pt[2] / sumasd;
+  vx[i] = vx[i] - dvx / massdi[i];
+  vy[i] = vy[i] - dvy / massdi[i];
+  vz[i] = vz[i] - dvz / massdi[i];
+}
+
 MolConst mol_const(mdx_ctx *ctx) {
   MolConst m{};
   for (int t = 0; t < MDX_NT; ++t) {
@@ -1375,5 +1506,42 @@ int launch_record(mdx_ctx *ctx, int slot, int mstep) {
   k_record<<<1, 1, 0, ctx->stream>>>(ctx->dv.rec, slot, mstep, ctx->dv.sc, ctx->dv.th, ctr,
                                      ctx->dv.rec_cap);
   MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+// GETKIN on the device; out = EKTR, EKROT, TKE (summed in block order).
+int launch_getkin(mdx_ctx *ctx, const double *summd, double *out) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
+  DevData &d = ctx->dv;
+  KinConst kc{};
+  for (int t = 0; t < MDX_NT; ++t) {
+    kc.summd[t] = t < ctx->d.ntypes ? summd[t] : 1.0;
+    kc.summas[t] = ctx->summas[t] != 0.0 ? ctx->summas[t] : 1.0;
+  }
+  double *acc = d.red + 480;  // scratch of the observables
+  MDX_CUDA(cudaMemsetAsync(acc, 0, 3 * sizeof(double), ctx->stream));
+  const int nb = (d.nop + 127) / 128;
+  k_getkin<<<nb, 128, 0, ctx->stream>>>(d.nop, d.mol_first, d.mol_nat, d.mol_type, kc, d.amass,
+                                        d.massdi, d.vx, d.vy, d.vz, d.pos, d.X, d.Y, d.Z,
+                                        dst6(ctx, nb, 3, acc, acc + 1, acc + 2));
+  MDX_LAUNCHED(ctx);
+  MDX_CUDA(ctx_copy(ctx->stream, out, acc, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+  return MDX_OK;
+}
+
+// CHKMOM on the device; pt = the total momentum removed.
+int launch_chkmom(mdx_ctx *ctx, double sumasd, double *pt) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
+  DevData &d = ctx->dv;
+  double *acc = d.red + 484;
+  MDX_CUDA(cudaMemsetAsync(acc, 0, 3 * sizeof(double), ctx->stream));
+  k_mom_sum<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.vx, d.vy, d.vz,
+                                               dst6(ctx, ctx->nsm, 3, acc, acc + 1, acc + 2));
+  MDX_LAUNCHED(ctx);
+  k_mom_remove<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, sumasd, acc, d.massdi, d.vx,
+                                                           d.vy, d.vz);
+  MDX_LAUNCHED(ctx);
+  RC(launch_getemp(ctx));  // GETEMP of the corrected momenta (service.f:1116)
+  MDX_CUDA(ctx_copy(ctx->stream, pt, acc, 3 * sizeof(double), cudaMemcpyDeviceToHost));
   return MDX_OK;
 }

@@ -1023,6 +1023,47 @@ int mdx_getcom(mdx_ctx *ctx) {
   return check_err(ctx);
 }
 
+int mdx_getkin(mdx_ctx *ctx, const double *summd, double enerf_tempf, double fnop,
+               double fnstr, double fnsti, mdx_kin *out) {
+  if (!ctx || !summd || !out) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));  // the centres: state upload, GETCOM, every step
+  double s[3];
+  RC(launch_getkin(ctx, summd, s));
+  RC(check_err(ctx));
+  // the tail of GETKIN (service.f:706-722), on the host
+  mdx_kin k{};
+  k.ektr = s[0];
+  k.ekrot = s[1];
+  k.tke = s[2];
+  k.ekint = k.tke - k.ektr - k.ekrot;
+  k.ttr = fnop > 1.1 ? k.ektr * enerf_tempf / (fnop - 1.0) : k.ektr * enerf_tempf / fnop;
+  if (fnstr > 0.01) {
+    k.trot = 3. * k.ekrot * enerf_tempf / fnstr;
+  } else {
+    double temp = 0.0;
+    MDX_CUDA(ctx_copy(ctx->stream, &temp, &ctx->dv.th->temp, sizeof(double),
+                      cudaMemcpyDeviceToHost));
+    k.trot = temp;
+  }
+  k.tint = fnsti > 0.01 ? 3.0 * k.ekint * enerf_tempf / fnsti : 0.0;
+  *out = k;
+  return MDX_OK;
+}
+
+int mdx_chkmom(mdx_ctx *ctx, double sumasd, double *dv) {
+  if (!ctx || !(sumasd > 0.0)) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  double pt[3];
+  RC(launch_chkmom(ctx, sumasd, pt));
+  RC(check_err(ctx));
+  if (dv) {
+    dv[0] = pt[0] / sumasd;
+    dv[1] = pt[1] / sumasd;
+    dv[2] = pt[2] / sumasd;
+  }
+  return MDX_OK;
+}
+
 int mdx_fforces(mdx_ctx *ctx, int laver, mdx_scalars *out) {
   if (!ctx) return MDX_ERR_ARG;
   RC(require(ctx, true, true, true));

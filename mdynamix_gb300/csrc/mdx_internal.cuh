@@ -570,6 +570,8 @@ int launch_fix_to_double(mdx_ctx *ctx, int which);  // mixed: int64 -> G/H
 int launch_sclfrc(mdx_ctx *ctx, int nnn);
 int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
 int launch_getcom(mdx_ctx *ctx, bool mirror = false);  // mirror: refresh posf/posi too
+int launch_getkin(mdx_ctx *ctx, const double *summd, double *out);  // EKTR, EKROT, TKE
+int launch_chkmom(mdx_ctx *ctx, double sumasd, double *pt);        // removed momentum
 // DOUBLE's kick + drift + GETCOM + mirrors in one pass (from_fix: fast
 // forces read as fixed point, mixed path)
 int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, bool from_fix);

@@ -75,6 +75,9 @@ def load():
     L.mdx_chcnb.argtypes = [P, I32P, I32P]
     L.mdx_get_lists.argtypes = [P, I32P, I32P, C.c_int32, I32P, I32P, C.c_int32]
     L.mdx_getcom.argtypes = [P]
+    L.mdx_getkin.argtypes = [P, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double,
+                             C.c_double, C.c_void_p]
+    L.mdx_chkmom.argtypes = [P, C.c_double, C.POINTER(C.c_double)]
     L.mdx_fforces.argtypes = [P, C.c_int, C.POINTER(MdxScalars)]
     L.mdx_slforces.argtypes = [P, C.POINTER(MdxScalars)]
     L.mdx_allforce.argtypes = [P, C.POINTER(MdxScalars)]
@@ -215,6 +218,26 @@ class ForcePath:
 
     def getcom(self):
         self._check(self.L.mdx_getcom(self.h))
+
+    def getkin(self):
+        """GETKIN (service.f:611-735): EKTR, EKROT, EKINT, TKE, TTR, TROT, TINT
+        with the system's unit and degree-of-freedom constants."""
+        from mdynamix_gb300.abi import MdxKin
+        from mdynamix_gb300.system import kin_summd
+        s = self.system
+        summd = (C.c_double * max(1, s.ntypes))(*kin_summd(s))
+        k = MdxKin()
+        self._check(self.L.mdx_getkin(self.h, summd, s.enerf * s.tempf, s.fnop, s.fnstr,
+                                      s.fnsti, C.byref(k)))
+        return k
+
+    def chkmom(self):
+        """CHKMOM (service.f:1081-1125): removes the total momentum; returns
+        the removed (DVX, DVY, DVZ)."""
+        from mdynamix_gb300.system import kin_sumasd
+        dv = (C.c_double * 3)()
+        self._check(self.L.mdx_chkmom(self.h, kin_sumasd(self.system), dv))
+        return tuple(dv)
 
     def fforces(self, laver: bool = True) -> MdxScalars:
         s = MdxScalars()

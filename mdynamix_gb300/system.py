@@ -277,6 +277,17 @@ def kvector_count(alphad: float, fexp: float, boxl: float, boyl: float,
     return n
 
 
+def kin_summd(s) -> List[float]:
+    """GETKIN's molecular masses in internal units, SUMMAS / (AVSNO 1000
+    UNITM NBEADS) per type (service.f:619)."""
+    return [s.summas[t] / (AVSNO * 1000.0 * s.unitm * s.spec.nbeads) for t in range(s.ntypes)]
+
+
+def kin_sumasd(s) -> float:
+    """CHKMOM's total mass, TOTMAS / UNITM (service.f:1096)."""
+    return s.totmas / s.unitm
+
+
 def kcolumn_counts(alphad: float, fexp: float, boxl: float, boyl: float,
                    bozl: float) -> Tuple[int, int, int]:
     """(columns, paired records, table rows) of the rectangular-cell k-set
@@ -379,18 +390,29 @@ class System:
 
     # main.f:289-350
     def _degrees_of_freedom(self):
-        fnst = 0.0
+        """FNST (total), FTTR (translational), FNSTR (rotational) and FNSTI
+        (internal) degrees of freedom, main.f:297-350."""
+        fnst = fttr = fnstr = 0.0
         lma = True
         for t in range(self.ntypes):
             if self.lmove[t]:
                 fnst += 3 * self.nspec[t] * self.nsits[t]
+                fttr += 3 * self.nspec[t]
                 if self.lshejk and self.ishejk[t] > 0:
                     fnst -= self.nrcon[t] * self.nspec[t]
+                if self.nsits[t] == 2:
+                    fnstr += 2.0 * self.nspec[t]
+                if self.nsits[t] >= 3:
+                    fnstr += 3.0 * self.nspec[t]
             else:
                 lma = False
-        if lma and self.nop > 1:
+        self.fnsti = float(fnst - fttr - fnstr)
+        if lma and self.nop > 1 and self.spec.nbeads <= 1:
             fnst -= 3.0
+            fttr -= 3.0
         self.fnst = float(fnst)
+        self.fttr = float(fttr)
+        self.fnstr = float(fnstr)
 
     # setup.f:27-113
     def _units(self):

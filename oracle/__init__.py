@@ -50,6 +50,9 @@ def lib():
         L.ox_chcnb.argtypes = [P, I32P, I32P]
         L.ox_get_lists.argtypes = [P, I32P, I32P, C.c_int32, I32P, I32P, C.c_int32]
         L.ox_getcom.argtypes = [P]
+        L.ox_getkin.argtypes = [P, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double,
+                                C.c_double, C.POINTER(C.c_double)]
+        L.ox_chkmom.argtypes = [P, C.c_double, C.POINTER(C.c_double)]
         L.ox_fforces.argtypes = [P, C.c_int, C.POINTER(MdxScalars)]
         L.ox_slforces.argtypes = [P, C.POINTER(MdxScalars)]
         L.ox_allforce.argtypes = [P, C.POINTER(MdxScalars)]
@@ -149,6 +152,22 @@ class Oracle:
 
     def getcom(self):
         self._check(self.L.ox_getcom(self.h))
+
+    def getkin(self):
+        """GETKIN: [EKTR, EKROT, EKINT, TKE, TTR, TROT, TINT]."""
+        from mdynamix_gb300.system import kin_summd
+        s = self.system
+        summd = (C.c_double * max(1, s.ntypes))(*kin_summd(s))
+        out = (C.c_double * 7)()
+        self._check(self.L.ox_getkin(self.h, summd, s.enerf * s.tempf, s.fnop, s.fnstr,
+                                     s.fnsti, out))
+        return list(out)
+
+    def chkmom(self):
+        from mdynamix_gb300.system import kin_sumasd
+        dv = (C.c_double * 3)()
+        self._check(self.L.ox_chkmom(self.h, kin_sumasd(self.system), dv))
+        return tuple(dv)
 
     def fforces(self, laver=True):
         from mdynamix_gb300.abi import MdxScalars

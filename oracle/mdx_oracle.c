@@ -31,6 +31,8 @@
  *   sclfrc        SCLFRC    service.f:182-287
  *   zerofs        ZEROFS    service.f:397-453
  *   ox_getcom     GETCOM    service.f:463-563
+ *   ox_getkin     GETKIN    service.f:611-735 (no GETROT)
+ *   ox_chkmom     CHKMOM    service.f:1081-1125
  *   reclen        RECLEN    service.f:572-605
  *   getemp        GETEMP    service.f:35-117
  *   pbc           PBC       service.f:953-990
@@ -1625,6 +1627,137 @@ static int getemp(ox_state *st) {
       (th->temp > st->p.chktf * st->p.trtemp || th->temp <= st->p.trtemp / st->p.chktf)) {
     snprintf(st->msg, sizeof st->msg, "Temperature control stopped the program: T=%g", th->temp);
     return MDX_ERR_NAN;
+  }
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- INV3B3 */
+/* util.f:89-125: inverse by cofactors, IER 1 for a near-singular matrix,
+ * 2 for a singular one (inverse zero). */
+static void inv3b3(const double *A, double *AI, double *DET, int *IER) {
+  AI[1] = A[5] * A[9] - A[6] * A[8];
+  AI[2] = A[3] * A[8] - A[2] * A[9];
+  AI[3] = A[2] * A[6] - A[3] * A[5];
+  AI[4] = A[6] * A[7] - A[4] * A[9];
+  AI[5] = A[1] * A[9] - A[3] * A[7];
+  AI[6] = A[3] * A[4] - A[1] * A[6];
+  AI[7] = A[4] * A[8] - A[5] * A[7];
+  AI[8] = A[2] * A[7] - A[1] * A[8];
+  AI[9] = A[1] * A[5] - A[2] * A[4];
+  *DET = A[1] * AI[1] + A[4] * AI[2] + A[7] * AI[3];
+  double SPUR = A[1] + A[5] + A[9];
+  *IER = 0;
+  if (fabs(*DET) < 1.e-6 * fabs(SPUR * SPUR * SPUR)) *IER = 1;
+  double R;
+  if (fabs(*DET) > 0.0) {
+    R = 1.0 / *DET;
+  } else {
+    R = 0.0;
+    *IER = 2;
+  }
+  for (int k = 1; k <= 9; ++k) AI[k] = R * AI[k];
+}
+
+/* ---------------------------------------------------------------- GETKIN */
+/* service.f:611-735 without GETROT (LMOL1/LMOL2).  SUMMD comes in per type
+ * (SUMMAS/(AVSNO*1000*UNITM*NBEADS)); MASSD(IS) is taken as 1/MASSDI of the
+ * atom (within an ulp of the stored site mass); WX.. are the site vectors
+ * GETCOM left.  out: EKTR, EKROT, EKINT, TKE, TTR, TROT, TINT. */
+int ox_getkin(ox_state *st, const double *summd, double enerf_tempf, double fnop,
+              double fnstr, double fnsti, double *out) {
+  int N = 0;
+  double EKTR = 0., EKROT = 0., TKE = 0.;
+  for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+    double SUMMD = summd[ITYP - 1];
+    int NSS = st->nsits[ITYP];
+    int ISB = st->isadr[ITYP] + 1, ISE = st->isadr[ITYP + 1];
+    for (int J = 1; J <= st->nspec[ITYP]; ++J) {
+      double PXJ = 0., PYJ = 0., PZJ = 0.;
+      double TOR[10], TORI[10], DET;
+      int IER;
+      for (int k = 1; k <= 9; ++k) TOR[k] = 0.;
+      for (int IS = ISB; IS <= ISE; ++IS) {
+        N = N + 1;
+        PXJ = PXJ + st->vx[N];
+        PYJ = PYJ + st->vy[N];
+        PZJ = PZJ + st->vz[N];
+        TKE = TKE + 0.5 * (st->vx[N] * st->vx[N] + st->vy[N] * st->vy[N] +
+                           st->vz[N] * st->vz[N]) * st->massdi[N];
+        double MD = 1.0 / st->massdi[N];
+        double WX = st->wx[N], WY = st->wy[N], WZ = st->wz[N];
+        TOR[1] = TOR[1] + MD * (WY * WY + WZ * WZ);
+        TOR[5] = TOR[5] + MD * (WX * WX + WZ * WZ);
+        TOR[9] = TOR[9] + MD * (WX * WX + WY * WY);
+        TOR[2] = TOR[2] - MD * WX * WY;
+        TOR[3] = TOR[3] - MD * WX * WZ;
+        TOR[6] = TOR[6] - MD * WY * WZ;
+      }
+      TOR[4] = TOR[2];
+      TOR[7] = TOR[3];
+      TOR[8] = TOR[6];
+      inv3b3(TOR, TORI, &DET, &IER);
+      EKTR = EKTR + 0.5 * (PXJ * PXJ + PYJ * PYJ + PZJ * PZJ) / SUMMD;
+      double RXJ = 0., RYJ = 0., RZJ = 0.;
+      N = N - NSS;
+      for (int IS = ISB; IS <= ISE; ++IS) {
+        N = N + 1;
+        double FAC = st->mass[IS] / st->summas[ITYP];
+        double VTX = st->vx[N] - PXJ * FAC;
+        double VTY = st->vy[N] - PYJ * FAC;
+        double VTZ = st->vz[N] - PZJ * FAC;
+        RXJ = RXJ + (VTY * st->wz[N] - st->wy[N] * VTZ);
+        RYJ = RYJ + (VTZ * st->wx[N] - st->wz[N] * VTX);
+        RZJ = RZJ + (VTX * st->wy[N] - st->wx[N] * VTY);
+      }
+      double EROTM;
+      if (IER == 0) {
+        EROTM = 0.5 * (TORI[1] * RXJ * RXJ + (TORI[2] + TORI[4]) * RXJ * RYJ +
+                       TORI[5] * RYJ * RYJ + (TORI[3] + TORI[7]) * RXJ * RZJ +
+                       TORI[9] * RZJ * RZJ + (TORI[6] + TORI[8]) * RYJ * RZJ);
+      } else {
+        double ROTM = 0.;
+        double PP = RXJ * RXJ + RYJ * RYJ + RZJ * RZJ;
+        if (PP < 1.e-50) continue; /* go to 100 */
+        N = N - NSS;
+        for (int IS = ISB; IS <= ISE; ++IS) {
+          N = N + 1;
+          double SS = st->wx[N] * st->wx[N] + st->wy[N] * st->wy[N] + st->wz[N] * st->wz[N];
+          double SP = st->wx[N] * RXJ + st->wy[N] * RYJ + st->wz[N] * RZJ;
+          ROTM = ROTM + (1.0 / st->massdi[N]) * (SS * PP - SP * SP);
+        }
+        EROTM = ROTM >= 1.e-50 ? 0.5 * PP * PP / ROTM : 0.0;
+      }
+      EKROT = EKROT + EROTM;
+    }
+  }
+  double EKINT = TKE - EKTR - EKROT;
+  double TTR = fnop > 1.1 ? EKTR * enerf_tempf / (fnop - 1.0) : EKTR * enerf_tempf / fnop;
+  double TROT = fnstr > 0.01 ? 3. * EKROT * enerf_tempf / fnstr : st->th.temp;
+  double TINT = fnsti > 0.01 ? 3.0 * EKINT * enerf_tempf / fnsti : 0.;
+  out[0] = EKTR; out[1] = EKROT; out[2] = EKINT; out[3] = TKE;
+  out[4] = TTR; out[5] = TROT; out[6] = TINT;
+  return MDX_OK;
+}
+
+/* ---------------------------------------------------------------- CHKMOM */
+/* service.f:1081-1125 (one rank): remove the total momentum, GETEMP; dv:
+ * the removed DVX, DVY, DVZ. */
+int ox_chkmom(ox_state *st, double sumasd, double *dv) {
+  double PT[3] = {0., 0., 0.};
+  for (int I = 1; I <= st->nstot; ++I) {
+    PT[0] = PT[0] + st->vx[I];
+    PT[1] = PT[1] + st->vy[I];
+    PT[2] = PT[2] + st->vz[I];
+  }
+  double DVX = PT[0] / sumasd, DVY = PT[1] / sumasd, DVZ = PT[2] / sumasd;
+  for (int I = 1; I <= st->nstot; ++I) {
+    st->vx[I] = st->vx[I] - DVX / st->massdi[I];
+    st->vy[I] = st->vy[I] - DVY / st->massdi[I];
+    st->vz[I] = st->vz[I] - DVZ / st->massdi[I];
+  }
+  getemp(st);
+  if (dv) {
+    dv[0] = DVX; dv[1] = DVY; dv[2] = DVZ;
   }
   return MDX_OK;
 }

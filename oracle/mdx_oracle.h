@@ -43,6 +43,9 @@ int ox_chcnb(ox_state *st, int32_t *mbsh, int32_t *mbln);
 int ox_get_lists(ox_state *st, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
 int ox_getcom(ox_state *st);
+int ox_getkin(ox_state *st, const double *summd, double enerf_tempf, double fnop,
+              double fnstr, double fnsti, double *out);
+int ox_chkmom(ox_state *st, double sumasd, double *dv);
 int ox_fforces(ox_state *st, int laver, mdx_scalars *out);
 int ox_slforces(ox_state *st, mdx_scalars *out);
 int ox_allforce(ox_state *st, mdx_scalars *out);

@@ -232,3 +232,52 @@ def test_library_exports_every_declared_symbol():
     lib.mdx_strerror.restype = ctypes.c_char_p
     assert lib.mdx_strerror(3) == b"neighbour list overflow"
     assert lib.mdx_version() >= 1
+
+
+# ---------------------------------------------------- GETKIN / CHKMOM ----
+def _kin_setup(seed=4):
+    s, st = systems.build(systems.organics(nw=30))
+    m = 1.0 / s.massdi                    # internal masses per atom
+    mol = s.nnum - 1
+    x = np.stack(st[:3], axis=1)
+    mm = np.zeros(s.nop)
+    np.add.at(mm, mol, m)
+    com = np.zeros((s.nop, 3))
+    for k in range(3):
+        np.add.at(com[:, k], mol, m * x[:, k])
+    com /= mm[:, None]
+    return s, st, m, mol, x - com[mol], np.random.default_rng(seed)
+
+
+def test_getkin_splits_translation_and_rotation():
+    """GETKIN (service.f:611-735) in the oracle: momenta that translate each
+    molecule rigidly are all translational energy; momenta that rotate each
+    (non-linear) molecule rigidly about its centre are all rotational."""
+    s, st, m, mol, w, rng = _kin_setup()
+    o = oracle.Oracle(s)
+    V = rng.normal(size=(s.nop, 3))
+    p = m[:, None] * V[mol]
+    o.set_state(*st[:3], p[:, 0], p[:, 1], p[:, 2])
+    o.getcom()
+    ektr, ekrot, ekint, tke = o.getkin()[:4]
+    assert abs(ektr - tke) < 1e-10 * tke and abs(ekrot) < 1e-10 * tke
+    om = rng.normal(size=(s.nop, 3))
+    p = m[:, None] * np.cross(om[mol], w)
+    o.set_state(*st[:3], p[:, 0], p[:, 1], p[:, 2])
+    o.getcom()
+    ektr, ekrot, ekint, tke, ttr, trot, tint = o.getkin()
+    assert abs(ektr) < 1e-10 * tke
+    assert abs(ekrot - tke) < 1e-8 * tke and abs(ekint) < 1e-8 * tke
+    assert abs(trot - 3.0 * ekrot * s.enerf * s.tempf / s.fnstr) < 1e-12 * trot
+
+
+def test_chkmom_removes_total_momentum():
+    s, st, m, mol, w, rng = _kin_setup()
+    o = oracle.Oracle(s)
+    v = rng.normal(size=(s.nstot, 3))
+    o.set_state(*st[:3], v[:, 0], v[:, 1], v[:, 2])
+    dv = o.chkmom()
+    (_, _, _, vx, vy, vz), _ = o.get_state()
+    tot = np.array([vx.sum(), vy.sum(), vz.sum()])
+    assert np.abs(tot).max() < 1e-10 * np.abs(v).sum()
+    assert np.allclose(np.array(dv) * S.kin_sumasd(s), v.sum(axis=0), rtol=1e-12, atol=1e-12)

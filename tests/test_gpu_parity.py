@@ -127,6 +127,29 @@ def test_double_mixed_tracks_fp64():
             assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * max(abs(getattr(b, n)), 1e-9), n
 
 
+@pytest.mark.parametrize("name", ["organics", "spce_ions"])
+def test_getkin_chkmom_match_oracle(name):
+    """GETKIN (molecules of 1 to 9 sites: the singular-tensor and
+    single-atom branches too) and CHKMOM against the oracle."""
+    s, st, g, o = pair(name)
+    for x in (g, o):
+        x.getcom()
+    kg = g.getkin()
+    ko = o.getkin()
+    for n, v in zip(("ektr", "ekrot", "ekint", "tke", "ttr", "trot", "tint"), ko):
+        assert abs(getattr(kg, n) - v) <= 1e-10 * max(abs(v), abs(ko[3])), n
+    # a start with a net momentum (the seeded configuration has none)
+    v = [st[3] + 0.3 * np.abs(st[3]).mean(), st[4] - 0.2 * np.abs(st[4]).mean(), st[5]]
+    for x in (g, o):
+        x.set_state(*st[:3], *v)
+    dg, do = np.array(g.chkmom()), np.array(o.chkmom())
+    assert np.abs(dg - do).max() <= 1e-10 * np.abs(do).max()
+    (_, _, _, gx, gy, gz), tg = g.get_state()
+    (_, _, _, ox, oy, oz), to = o.get_state()
+    assert relmax(np.stack([gx, gy, gz]), np.stack([ox, oy, oz])) < 1e-12
+    assert abs(tg.temp - to.temp) <= 1e-10 * to.temp
+
+
 def test_sultan_shake_fp64():
     s, st, g, o = pair("spce_ions")
     rg = g.sultan(3)
