@@ -136,11 +136,15 @@ struct MoveConst {
   int lmove[MDX_NT];
 };
 
+// bx set: a second kick with h2 right after (the same values as two passes)
 __global__ void k_kick(int n, const int4 *__restrict__ ainfo, MoveConst mv,
                        double h, const double *__restrict__ ax,
                        const double *__restrict__ ay, const double *__restrict__ az,
                        double *vx, double *vy, double *vz,
-                       const double *__restrict__ vscale) {
+                       const double *__restrict__ vscale, double h2 = 0.0,
+                       const double *__restrict__ bx = nullptr,
+                       const double *__restrict__ by = nullptr,
+                       const double *__restrict__ bz = nullptr) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int t = ainfo[i].x;
@@ -152,9 +156,17 @@ __global__ void k_kick(int n, const int4 *__restrict__ ainfo, MoveConst mv,
     y = y * s;
     z = z * s;
   }
-  vx[i] = x + h * ax[i];
-  vy[i] = y + h * ay[i];
-  vz[i] = z + h * az[i];
+  x = x + h * ax[i];
+  y = y + h * ay[i];
+  z = z + h * az[i];
+  if (bx) {
+    x = x + h2 * bx[i];
+    y = y + h2 * by[i];
+    z = z + h2 * bz[i];
+  }
+  vx[i] = x;
+  vy[i] = y;
+  vz[i] = z;
 }
 
 // DOUBLE 2.3.5.3-2.3.5.4 (mdstep.f:366-373), optionally preceded by the
@@ -1430,6 +1442,25 @@ int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale) {
   k_kick<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.ainfo, move_const(ctx), h, x, y, z, d.vx, d.vy, d.vz,
       apply_vscale ? scratch(ctx)->vscale : nullptr);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+// Two kicks in one pass: forces `which1` with h1, then `which2` with h2.
+int launch_kick2(mdx_ctx *ctx, int which1, double h1, int which2, double h2) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
+  DevData &d = ctx->dv;
+  auto set = [&](int w, const double *&x, const double *&y, const double *&z) {
+    x = w == 1 ? d.hx : w == 2 ? d.gx : d.fx;
+    y = w == 1 ? d.hy : w == 2 ? d.gy : d.fy;
+    z = w == 1 ? d.hz : w == 2 ? d.gz : d.fz;
+  };
+  const double *ax, *ay, *az, *bx, *by, *bz;
+  set(which1, ax, ay, az);
+  set(which2, bx, by, bz);
+  k_kick<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.ainfo, move_const(ctx), h1, ax, ay,
+                                                     az, d.vx, d.vy, d.vz, nullptr, h2, bx, by,
+                                                     bz);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

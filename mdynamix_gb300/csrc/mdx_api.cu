@@ -276,8 +276,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
       RC(do_fforces(ctx, 0, false, false, true, !keep_fix));
     }
   }
-  RC(launch_kick(ctx, 1, HTSTEB, false));
-  RC(launch_kick(ctx, 2, HTSTEP, false));
+  RC(launch_kick2(ctx, 1, HTSTEB, 2, HTSTEP));  // the two closing half kicks, one pass
   RC(launch_scaling(ctx, 2, nullptr));
   if (p.lnpt) RC(sync_box_from_device(ctx));
   if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters

@@ -579,6 +579,7 @@ int launch_kick_drift(mdx_ctx *ctx, double htsteb, double tsteb, int prev);
 int launch_record(mdx_ctx *ctx, int slot, int mstep);
 int launch_getemp(mdx_ctx *ctx);
 int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
+int launch_kick2(mdx_ctx *ctx, int which1, double h1, int which2, double h2);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);

@@ -477,8 +477,8 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
 
 // Fold the integer slots of a mixed sweep into mdx_scalars (full rows count
 // each pair twice, hence the 1/2 on pair sums).
-__global__ void k_fold_slots(unsigned long long *slots, double einv,
-                             mdx_scalars *sc, int which, int ntypes,
+__global__ void k_fold_slots(unsigned long long *__restrict__ slots, double einv,
+                             mdx_scalars *__restrict__ sc, int which, int ntypes,
                              int split) {
   double v[P_NSLOT];
   for (int k = 0; k < P_NSLOT; ++k) {
