@@ -281,3 +281,27 @@ def test_chkmom_removes_total_momentum():
     tot = np.array([vx.sum(), vy.sum(), vz.sum()])
     assert np.abs(tot).max() < 1e-10 * np.abs(v).sum()
     assert np.allclose(np.array(dv) * S.kin_sumasd(s), v.sum(axis=0), rtol=1e-12, atol=1e-12)
+
+
+def test_fixed_point_phase_split():
+    """The mixed phase tables' arithmetic (ewald.cu k_tables): k times a
+    32-bit fixed-point coordinate is the phase modulo one turn exactly
+    (integer wrap-around); its top 24 bits are exact in FP32 and the low 8
+    bits rotate the result to first order.  Restated in numpy (FP32 where
+    the kernel rounds), it stays within 2e-7 of exp(2 pi i k x / L)."""
+    rng = np.random.default_rng(7)
+    u = rng.integers(0, 2 ** 32, size=4000, dtype=np.uint64)
+    for k in (1, 2, 7, 21):
+        ph = ((u * k) % 2 ** 32).astype(np.int64)
+        ph = np.where(ph >= 2 ** 31, ph - 2 ** 32, ph)          # signed fraction of half a turn
+        hi = ph & ~0xff
+        lo = ph - hi
+        x = np.float32(hi) * np.float32(2.0 ** -31)               # exact in FP32
+        s = np.sin(np.pi * x.astype(np.float64)).astype(np.float32)
+        c = np.cos(np.pi * x.astype(np.float64)).astype(np.float32)
+        d = np.float32(lo) * np.float32(np.pi * 2.0 ** -31)
+        re = c - s * d
+        im = s + c * d
+        exact = np.exp(2j * np.pi * ((u * k) % 2 ** 32).astype(np.float64) / 2 ** 32)
+        err = np.abs((re.astype(np.float64) + 1j * im.astype(np.float64)) - exact).max()
+        assert err < 2e-7, (k, err)
