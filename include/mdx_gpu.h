@@ -146,7 +146,13 @@ typedef struct {
   double fexp;               /* FEXP  (B): |k|^2 <= 4 alpha^2 B          */
   double rcut;               /* RCUT (RCUTT; RSSQ = RCUTT**2)            */
   double rshort;             /* SHORT                                    */
-  double rskin;              /* 0 = reference list; >0 list at rcut+skin */
+  double rskin;              /* 0: the reference's list (CHCNB every ICHNB
+                                long steps, pairs evaluated as listed);
+                                > 0: Verlet-skin mode, not in the reference:
+                                list radius RCUT + rskin, pairs beyond RCUT
+                                skipped at evaluation, rebuilt once an atom
+                                has moved rskin / 2 (ICHNB unused); constant
+                                volume only                               */
   double rff, rff2;          /* reaction-field constants                 */
   double tstep, tsteb;       /* TSTEP, TSTEB                             */
   int32_t nfreq;             /* NFREQ short steps per long step          */
@@ -202,6 +208,8 @@ typedef struct {
                                 a message and goes on (mdstep.f:1264-1269) */
   int32_t nscale;            /* forced velocity rescalings (NRTSC)        */
   int32_t npt_fail;          /* NPT "too strong fluctuations" count (ISKK) */
+  int32_t list_builds;       /* CHCNB builds done (counted on the device)  */
+  int32_t reserved;
 } mdx_thermo;
 
 /* One record per long step, filled on the device and copied back once. */

@@ -112,7 +112,7 @@ class MdxThermo(C.Structure):
         ("tryck", C.c_double), ("tryckm", C.c_double), ("tryckx", C.c_double),
         ("trycky", C.c_double), ("tryckz", C.c_double),
         ("shake_iter_max", C.c_int32), ("shake_fail", C.c_int32), ("nscale", C.c_int32),
-        ("npt_fail", C.c_int32)]
+        ("npt_fail", C.c_int32), ("list_builds", C.c_int32), ("reserved", C.c_int32)]
 
 
 class MdxStepRecord(C.Structure):

@@ -268,7 +268,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
     // kick, drift, GETCOM and the mirrors; positions then stay put until the
     // next short step
     RC(launch_kick_drift_com(ctx, HTSTEB, TSTEB, s > 1 ? 1 : 0, keep_fix && s > 1));
-    if (s == NFREQ2 && mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
+    if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
     if (s == NFREQ) {
       RC(do_slforces(ctx, false, true));
       RC(do_fforces(ctx, 0, false, true, true));
@@ -292,7 +292,7 @@ int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
   RC(launch_scaling(ctx, 3, nullptr));
   if (p.lnpt) RC(sync_box_from_device(ctx));
   RC(launch_getcom(ctx));
-  if (mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
+  RC(launch_list_update(ctx, mstep));
   RC(do_allforce(ctx, false));
   if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters
   return MDX_OK;
@@ -309,7 +309,8 @@ int ensure_records(mdx_ctx *ctx, int n) {
 // One DOUBLE long step replayed from its captured graph (captured on first
 // use; four variants: list rebuild or not x records or not).
 int graph_step(mdx_ctx *ctx, int mstep, bool rec) {
-  const int g = (mstep % ctx->p.ichnb == 0 ? 1 : 0) + (rec ? 2 : 0);
+  const bool list = list_update_every_step(ctx) || mstep % ctx->p.ichnb == 0;
+  const int g = (list ? 1 : 0) + (rec ? 2 : 0);
   if (!ctx->gexec[g]) {
     const int64_t l0 = ctx->launches;
     MDX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -518,7 +519,7 @@ int mdx_close(mdx_ctx *ctx) {
   void *ptrs[] = {d.pos, d.posf, d.posi, d.qsitef, d.stab, d.pinfo, d.moltpl, d.vx, d.massdi, d.amass, d.qsite,
                   d.ainfo, d.nnbb, d.inbb, d.mol_first, d.mol_nat, d.mol_type, d.X,
                   d.gx, d.ox, d.gfix, d.hfix, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx,
-                  d.cell_cnt, d.cell_start, d.cell_list, d.cell_pos, d.slot_of, d.atom_cell, d.a6lj, d.a6f, d.abf,
+                  d.cell_cnt, d.cell_start, d.cell_list, d.cell_pos, d.slot_of, d.pos_ref, d.atom_cell, d.a6lj, d.a6f, d.abf,
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.kconst, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
@@ -859,11 +860,26 @@ int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
     ctx->err = "bad box, cutoff, NFREQ or ICHNB";
     return MDX_ERR_ARG;
   }
-  if (2.0 * (p->rcut + p->rskin) > std::min(p->boxl, std::min(p->boyl, p->bozl)) + 1e-9 &&
+  if (p->rskin < 0.0 || (p->rskin > 0.0 && p->lnpt)) {
+    ctx->err = "Verlet skin: rskin >= 0, and constant volume only";
+    return p->rskin < 0.0 ? MDX_ERR_ARG : MDX_ERR_UNSUPPORTED;
+  }
+  if (p->rskin > 0.0 && p->lmnbl) {
+    ctx->err = "Verlet skin: not with the reaction-field molecular cutoff";
+    return MDX_ERR_UNSUPPORTED;
+  }
+  if (p->rskin > 0.0 &&
       p->rcut + p->rskin > 0.5 * std::min(p->boxl, std::min(p->boyl, p->bozl))) {
-    // the reference allows it (single image per pair); so does the list build
+    ctx->err = "Verlet skin: RCUT + skin must stay within half the box";
+    return MDX_ERR_ARG;
   }
   ctx->drop_graphs();  // kernel arguments baked into the step graphs change
+  if (ctx->have_params && p->rskin != ctx->p.rskin) {
+    // a new list mode: the next step needs a fresh CHCNB
+    ctx->have_lists = false;
+    ctx_free(ctx, ctx->dv.pos_ref);
+    ctx->dv.pos_ref = nullptr;
+  }
   ctx->p = *p;
   ctx->pc.coulf = p->coulf;
   ctx->pc.alphad = p->alphad;
@@ -873,6 +889,8 @@ int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
   ctx->pc.lmnbl = p->lmnbl;
   ctx->pc.lmdee = p->lmdee;
   ctx->pc.nnbt = ctx->d.nnbt;
+  ctx->pc.rc2 = p->rskin > 0.0 ? p->rcut * p->rcut : 1e300;
+  ctx->pc.rc2f = p->rskin > 0.0 ? (float)(p->rcut * p->rcut) : 3.0e38f;
   ctx->boxl = p->boxl;
   ctx->boyl = p->boyl;
   ctx->bozl = p->bozl;

@@ -65,6 +65,11 @@ struct TypeConst {
 struct PairConst {
   double coulf, alphad, raex, rff, rff2;
   int lmnbl, lmdee, nnbt;
+  // squared cutoff the long-row sweeps test each pair against: RCUT^2 in
+  // skin mode (rows reach RCUT + skin), above every distance otherwise (the
+  // reference evaluates every listed pair)
+  double rc2;
+  float rc2f;
 };
 
 // Cell grid used by the list build.
@@ -163,6 +168,7 @@ struct DevData {
   // slots (kept equal to posi[cell_list[slot]] by every posi writer)
   int4 *cell_pos;
   int *slot_of;  // mixed path: slot of atom i in the cell order of the last build
+  dbl4 *pos_ref; // skin mode: positions at the last build (displacement check)
   // LJ tables [i*nnbt + j]
   double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   float *a6f, *b12f, *a60f, *b120f, *a614f, *b1214f;
@@ -533,6 +539,8 @@ inline void ctx_free(mdx_ctx *ctx, void *p) {
 // ---------------------------------------------------------- host launchers
 // nblist.cu
 int launch_build_lists(mdx_ctx *ctx);
+int launch_list_update(mdx_ctx *ctx, int mstep);  // CHCNB when due (ICHNB or skin)
+bool list_update_every_step(const mdx_ctx *ctx);  // skin mode: the update is in every step
 int export_lists(mdx_ctx *ctx, int32_t *nbs1, int32_t *nbs2, int32_t cap_s,
                  int32_t *nbl1, int32_t *nbl2, int32_t cap_l);
 // pair.cu

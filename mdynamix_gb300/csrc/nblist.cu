@@ -30,6 +30,10 @@ struct BoxD {
   double bx, by, bz, hbx, hby, hbz;
 };
 
+// Skin mode: the list kernels of a step run only when the displacement check
+// of that step asked for a rebuild (gate == nullptr: always).
+__device__ __forceinline__ bool closed(const int *gate) { return gate && *gate == 0; }
+
 __device__ __forceinline__ int wrap_cell(double x, double L, double cw, int n) {
   double u = (x + 0.5 * L) / cw;
   int c = (int)floor(u);
@@ -40,9 +44,9 @@ __device__ __forceinline__ int wrap_cell(double x, double L, double cw, int n) {
 
 __global__ void k_cell_count(int n, const dbl4 *__restrict__ pos, BoxD b,
                              CellGrid g, int *__restrict__ cell_cnt,
-                             int *__restrict__ atom_cell) {
+                             int *__restrict__ atom_cell, const int *__restrict__ gate) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || closed(gate)) return;
   dbl4 p = pos[i];
   int cx = wrap_cell(p.x, b.bx, g.cx, g.nx);
   int cy = wrap_cell(p.y, b.by, g.cy, g.ny);
@@ -54,8 +58,10 @@ __global__ void k_cell_count(int n, const dbl4 *__restrict__ pos, BoxD b,
 
 // Single-block exclusive scan of the cell counts (ncell is small).
 __global__ void k_cell_scan(int ncell, const int *__restrict__ cnt,
-                            int *__restrict__ start, int *__restrict__ fill) {
+                            int *__restrict__ start, int *__restrict__ fill,
+                            const int *__restrict__ gate) {
   __shared__ int sh[1024];
+  if (closed(gate)) return;
   int carry = 0;
   for (int base = 0; base < ncell; base += 1024) {
     int i = base + threadIdx.x;
@@ -82,9 +88,9 @@ __global__ void k_cell_scan(int ncell, const int *__restrict__ cnt,
 __global__ void k_cell_scatter(int n, const int *__restrict__ atom_cell,
                                const int *__restrict__ start,
                                int *__restrict__ fill,
-                               int *__restrict__ list) {
+                               int *__restrict__ list, const int *__restrict__ gate) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || closed(gate)) return;
   int c = atom_cell[i];
   int k = atomicAdd(&fill[c], 1);
   list[start[c] + k] = i;
@@ -93,10 +99,10 @@ __global__ void k_cell_scatter(int n, const int *__restrict__ atom_cell,
 // Sort each cell's atoms by index (one warp per cell, odd-even transposition
 // over the small cell population) so that rows come out in a fixed order.
 __global__ void k_cell_sort(int ncell, const int *__restrict__ start,
-                            int *__restrict__ list) {
+                            int *__restrict__ list, const int *__restrict__ gate) {
   int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int lane = threadIdx.x & 31;
-  if (c >= ncell) return;
+  if (c >= ncell || closed(gate)) return;
   int b = start[c], e = start[c + 1], m = e - b;
   for (int pass = 0; pass < m; ++pass) {
     int par = pass & 1;
@@ -118,9 +124,10 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start,
 // the atom index.
 __global__ void k_cell_gather(int n, const int *__restrict__ list, const int4 *__restrict__ posi,
                               const float4 *__restrict__ posf, const int4 *__restrict__ ainfo,
-                              int4 *__restrict__ cell_pos, int *__restrict__ slot_of) {
+                              int4 *__restrict__ cell_pos, int *__restrict__ slot_of,
+                              const int *__restrict__ gate = nullptr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+  if (k >= n || closed(gate)) return;
   const int j = list[k];
   if (slot_of) slot_of[j] = k;
   if (posi) {
@@ -174,14 +181,15 @@ __global__ void __launch_bounds__(BLK) k_build(
     int cap_l, int *__restrict__ ns_cnt, int *__restrict__ nl_cnt,
     int *__restrict__ ns_idx, int *__restrict__ nl_idx, int *__restrict__ err,
     int *__restrict__ need, int full, const int4 *__restrict__ posi, float sxf, float syf,
-    float szf) {
+    float szf, dbl4 *__restrict__ pos_ref, const int *__restrict__ gate) {
   // posi (mixed path): the prefilter takes the wrapped differences of the
   // fixed-point positions and the molecule from their packed word, one
   // 16-byte gather per candidate
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (BLK / 32) + (threadIdx.x >> 5);
-  if (i >= n) return;
+  if (i >= n || closed(gate)) return;
   const dbl4 pi = pos[i];
+  if (pos_ref && lane == 0) pos_ref[i] = pi;  // skin mode: positions of this build
   const float4 pf = posf[i];
   const int imol = ainfo[i].y;
   const int4 qi = posi ? posi[i] : make_int4(0, 0, 0, 0);
@@ -288,9 +296,9 @@ __global__ void __launch_bounds__(BLK) k_build(
 __global__ void k_mirror(int n, const dbl4 *__restrict__ pos,
                          float4 *__restrict__ posf, int4 *__restrict__ posi,
                          const int *__restrict__ pinfo, double ibx, double iby,
-                         double ibz) {
+                         double ibz, const int *__restrict__ gate = nullptr) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || closed(gate)) return;
   dbl4 p = pos[i];
   posf[i] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
   if (posi) {
@@ -306,7 +314,10 @@ __global__ void k_mirror(int n, const dbl4 *__restrict__ pos,
 
 __global__ void k_count_totals(int n, const int *__restrict__ ns_cnt,
                                const int *__restrict__ nl_cnt,
-                               mdx_scalars *sc) {
+                               mdx_scalars *sc, int *__restrict__ builds,
+                               const int *__restrict__ gate) {
+  if (closed(gate)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(builds, 1);  // once per build
   int s = 0, l = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -324,10 +335,35 @@ __global__ void k_count_totals(int n, const int *__restrict__ ns_cnt,
   }
 }
 
-__global__ void k_halve_counts(mdx_scalars *sc) {
+__global__ void k_halve_counts(mdx_scalars *sc, const int *__restrict__ gate) {
+  if (closed(gate)) return;
   sc->mbsh /= 2;
   sc->mbln /= 2;
 }
+
+// Zero n ints when the gate is open (a memset that a skin-mode step skips).
+__global__ void k_zero_gated(int *__restrict__ p, int n, const int *__restrict__ gate) {
+  if (closed(gate)) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    p[k] = 0;
+}
+
+// Skin mode: opens the gate when some atom has moved more than half the skin
+// (minimum image) since the last build.  The gate word was zeroed just before.
+__global__ void k_skin_check(int n, const dbl4 *__restrict__ pos,
+                             const dbl4 *__restrict__ pos_ref, BoxD b, double h2,
+                             int *__restrict__ gate) {
+  bool far = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const dbl4 p = pos[i], r = pos_ref[i];
+    double dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
+    pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+    far |= dx * dx + dy * dy + dz * dz > h2;
+  }
+  if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) *gate = 1;
+}
+
+__global__ void k_gate_zero(int *__restrict__ gate) { *gate = 0; }
 
 }  // namespace
 
@@ -350,7 +386,10 @@ int launch_cell_refresh(mdx_ctx *ctx) {
   return MDX_OK;
 }
 
-int launch_build_lists(mdx_ctx *ctx) {
+// CHCNB.  gate != nullptr (skin mode, inside a step): every kernel of the
+// build runs only if the displacement check of this step opened the gate, so
+// a captured step graph holds the build whether or not it happens.
+static int build_lists(mdx_ctx *ctx, const int *gate) {
   MDX_TIMER(ctx, MDX_T_LIST);
   DevData &d = ctx->dv;
   // CHCNB puts every pair within SHORT in the short list even when SHORT
@@ -370,41 +409,54 @@ int launch_build_lists(mdx_ctx *ctx) {
   g.cz = ctx->bozl / g.nz;
   g.ncell = g.nx * g.ny * g.nz;
   if (g.ncell != ctx->grid.ncell) {
+    if (gate) {  // a gated build never allocates (the box is fixed in skin mode)
+      ctx->err = "skin mode: the cell grid changed inside a step";
+      return MDX_ERR_STATE;
+    }
     ctx->drop_graphs();
     ctx_free(ctx, d.cell_cnt);
     ctx_free(ctx, d.cell_start);
     MDX_CUDA(ctx_alloc(ctx, &d.cell_cnt, sizeof(int) * (g.ncell + 1) * 2));
     MDX_CUDA(ctx_alloc(ctx, &d.cell_start, sizeof(int) * (g.ncell + 1)));
   }
+  if (ctx->p.rskin > 0.0 && !d.pos_ref) {
+    if (gate) {
+      ctx->err = "skin mode: no list built before the step";
+      return MDX_ERR_STATE;
+    }
+    MDX_CUDA(ctx_alloc(ctx, &d.pos_ref, sizeof(dbl4) * (size_t)d.n));
+  }
+  dbl4 *pos_ref = ctx->p.rskin > 0.0 ? d.pos_ref : nullptr;
   ctx->grid = g;
   ctx->list_rl2 = rl * rl;
   int *fill = d.cell_cnt + (g.ncell + 1);
-  MDX_CUDA(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * (g.ncell + 1),
-                           ctx->stream));
   const int T = 256;
+  k_zero_gated<<<(g.ncell + 1 + T - 1) / T, T, 0, ctx->stream>>>(d.cell_cnt, g.ncell + 1, gate);
+  MDX_LAUNCHED(ctx);
   k_mirror<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
-      1.0 / ctx->boyl, 1.0 / ctx->bozl);
+      1.0 / ctx->boyl, 1.0 / ctx->bozl, gate);
   MDX_LAUNCHED(ctx);
   k_cell_count<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(d.n, d.pos, b, g,
                                                           d.cell_cnt,
-                                                          d.atom_cell);
+                                                          d.atom_cell, gate);
   MDX_LAUNCHED(ctx);
   k_cell_scan<<<1, 1024, 0, ctx->stream>>>(g.ncell, d.cell_cnt, d.cell_start,
-                                           fill);
+                                           fill, gate);
   MDX_LAUNCHED(ctx);
   k_cell_scatter<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
-      d.n, d.atom_cell, d.cell_start, fill, d.cell_list);
+      d.n, d.atom_cell, d.cell_start, fill, d.cell_list, gate);
   MDX_LAUNCHED(ctx);
   k_cell_sort<<<(g.ncell + 7) / 8, 256, 0, ctx->stream>>>(g.ncell, d.cell_start,
-                                                          d.cell_list);
+                                                          d.cell_list, gate);
   MDX_LAUNCHED(ctx);
   k_cell_gather<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
       d.n, d.cell_list, ctx->mixed() ? d.posi : nullptr, d.posf, d.ainfo, d.cell_pos,
-      ctx->mixed() ? d.slot_of : nullptr);
+      ctx->mixed() ? d.slot_of : nullptr, gate);
   MDX_LAUNCHED(ctx);
   int *need = d.shake_iter + 4;  // two ints of scratch after the SHAKE counter
-  MDX_CUDA(cudaMemsetAsync(need, 0, sizeof(int) * 2, ctx->stream));
+  k_zero_gated<<<1, 32, 0, ctx->stream>>>(need, 2, gate);
+  MDX_LAUNCHED(ctx);
   const int BLK = 256;
   k_build<BLK><<<(d.n + BLK / 32 - 1) / (BLK / 32), BLK, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,
@@ -412,17 +464,47 @@ int launch_build_lists(mdx_ctx *ctx) {
       d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
       ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,
       (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),
-      (float)(ctx->bozl / 4294967296.0));
+      (float)(ctx->bozl / 4294967296.0), pos_ref, gate);
   MDX_LAUNCHED(ctx);
-  MDX_CUDA(cudaMemsetAsync(&d.sc->mbsh, 0, sizeof(int) * 2, ctx->stream));
-  k_count_totals<<<64, 256, 0, ctx->stream>>>(d.n, d.ns_cnt, d.nl_cnt, d.sc);
+  k_zero_gated<<<1, 32, 0, ctx->stream>>>(&d.sc->mbsh, 2, gate);
+  MDX_LAUNCHED(ctx);
+  k_count_totals<<<64, 256, 0, ctx->stream>>>(d.n, d.ns_cnt, d.nl_cnt, d.sc,
+                                              &d.th->list_builds, gate);
   MDX_LAUNCHED(ctx);
   if (ctx->mixed()) {  // full rows count every pair twice
-    k_halve_counts<<<1, 1, 0, ctx->stream>>>(d.sc);
+    k_halve_counts<<<1, 1, 0, ctx->stream>>>(d.sc, gate);
     MDX_LAUNCHED(ctx);
   }
   ctx->have_lists = true;
   return MDX_OK;
+}
+
+int launch_build_lists(mdx_ctx *ctx) { return build_lists(ctx, nullptr); }
+
+bool list_update_every_step(const mdx_ctx *ctx) { return ctx->p.rskin > 0.0; }
+
+// The list update of long step mstep: CHCNB every ICHNB-th step (the
+// reference's rule), or in skin mode a rebuild whenever an atom has moved
+// more than half the skin since the last build, decided on the device.
+int launch_list_update(mdx_ctx *ctx, int mstep) {
+  if (ctx->p.rskin <= 0.0) return mstep % ctx->p.ichnb == 0 ? build_lists(ctx, nullptr) : MDX_OK;
+  DevData &d = ctx->dv;
+  if (!d.pos_ref) {
+    ctx->err = "skin mode: no list built before the step";
+    return MDX_ERR_STATE;
+  }
+  int *gate = d.shake_iter + 6;
+  BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
+         0.5 * ctx->bozl};
+  {
+    MDX_TIMER(ctx, MDX_T_LIST);
+    k_gate_zero<<<1, 1, 0, ctx->stream>>>(gate);
+    MDX_LAUNCHED(ctx);
+    k_skin_check<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.pos, d.pos_ref, b,
+                                                    0.25 * ctx->p.rskin * ctx->p.rskin, gate);
+    MDX_LAUNCHED(ctx);
+  }
+  return build_lists(ctx, gate);
 }
 
 // Reference layout and order of the lists (forces.f:1956-1957, 2127-2140):

@@ -107,6 +107,7 @@ __global__ void __launch_bounds__(256) k_pair64(
       double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
       pbc_rect(DX, DY, DZ, bx, by, bz, hbx, hby, hbzt);
       const double RR = DX * DX + DY * DY + DZ * DZ;
+      if (!SHORT && RR > pc.rc2) continue;  // skin mode: listed beyond RCUT
       // one reciprocal square root instead of a square root and a division
       // (within an ulp of DSQRT and 1/R1)
       const double R1I = rsqrt(RR);
@@ -335,83 +336,85 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
       const float DY = idiff(pi.y, pj.y, sy);
       const float DZ = idiff(pi.z, pj.z, sz);
       const float RR = DX * DX + DY * DY + DZ * DZ;
-      const float R1I = rsqrtf(RR);
-      const float R1 = RR * R1I;
-      const float R1EI = RAE == 0.f ? R1I : __fdividef(1.f, R1 + RAE);
-      const float R1E = R1 + RAE;
-      float EE1, EES, FORCE;
-      if (is14 || (same && eei == 0)) {
-        EE1 = QIJ * R1I;
-        FORCE = lmovei ? EE1 * (R1I * R1I) : 0.f;
-        EES = EE1;
-      } else if (pc.lmnbl) {
-        const float rff = (float)pc.rff, rff2 = (float)pc.rff2;
-        EE1 = QIJ * (1.f / R1E - 0.5f * rff2 * (R1E * R1E) + rff);
-        EES = EE1;
-        if (SHORT) {
-          FORCE = QIJ * (R1EI * R1EI * R1EI + rff2);
-          if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * R1EI * R1EI - rff);
-        } else {
-          FORCE = QIJ * (R1EI * R1EI * R1I + rff2);
-          if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * RR - rff);
-        }
-      } else {
-        const float ALPHAR = alphad * R1;
-        const float TTT = __fdividef(1.f, 1.f + (float)MDX_B1 * ALPHAR);
-        const float EXP2A = __expf(-(ALPHAR * ALPHAR));
-        const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
-        EE1 = QIJ * R1EI;
-        EES = EE1 * ERFCT;
-        FORCE = EE1 * ((float)MDX_TOTPI * alphad * EXP2A + ERFCT * R1EI) * R1I;
-      }
-      if (SPLIT) {
-        const int mtr = tc.mdx[ti][tj];
-        if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], (double)EE1);
-        else atomicAdd(&s_split[mtr], (double)EE1);
-      }
-      if (ENER) {
-        if (same) a[P_EE_SAME] += EE1;
-        else a[P_EE_DIFF] += EE1;
-      }
-      if (ENER) a[P_EES] += EES;
-      if (B12 != 0.f) {
-        const float R2I = R1EI * R1EI;
-        const float R6I = R2I * R2I * R2I;
-        float ESR = (A6 + B12 * R6I) * R6I;
-        const float FSR = (6.f * A6 + 12.f * B12 * R6I) * R6I * R1EI;
-        FORCE = FORCE + FSR * R1I;
-        bool count_esr_split = true;
-        if (same) {
+      if (SHORT || RR <= pc.rc2f) {  // skin mode: long-row pairs beyond RCUT skipped
+        const float R1I = rsqrtf(RR);
+        const float R1 = RR * R1I;
+        const float R1EI = RAE == 0.f ? R1I : __fdividef(1.f, R1 + RAE);
+        const float R1E = R1 + RAE;
+        float EE1, EES, FORCE;
+        if (is14 || (same && eei == 0)) {
+          EE1 = QIJ * R1I;
+          FORCE = lmovei ? EE1 * (R1I * R1I) : 0.f;
+          EES = EE1;
+        } else if (pc.lmnbl) {
+          const float rff = (float)pc.rff, rff2 = (float)pc.rff2;
+          EE1 = QIJ * (1.f / R1E - 0.5f * rff2 * (R1E * R1E) + rff);
+          EES = EE1;
           if (SHORT) {
-            if (lmovei) {
-              if (ENER) a[P_VIR] += FSR * R1;
+            FORCE = QIJ * (R1EI * R1EI * R1EI + rff2);
+            if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * R1EI * R1EI - rff);
+          } else {
+            FORCE = QIJ * (R1EI * R1EI * R1I + rff2);
+            if (ENER) a[P_VIR] += QIJ * (1.5f * rff2 * RR - rff);
+          }
+        } else {
+          const float ALPHAR = alphad * R1;
+          const float TTT = __fdividef(1.f, 1.f + (float)MDX_B1 * ALPHAR);
+          const float EXP2A = __expf(-(ALPHAR * ALPHAR));
+          const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
+          EE1 = QIJ * R1EI;
+          EES = EE1 * ERFCT;
+          FORCE = EE1 * ((float)MDX_TOTPI * alphad * EXP2A + ERFCT * R1EI) * R1I;
+        }
+        if (SPLIT) {
+          const int mtr = tc.mdx[ti][tj];
+          if (same) atomicAdd(&s_split[2 * MDX_NTPP + ti], (double)EE1);
+          else atomicAdd(&s_split[mtr], (double)EE1);
+        }
+        if (ENER) {
+          if (same) a[P_EE_SAME] += EE1;
+          else a[P_EE_DIFF] += EE1;
+        }
+        if (ENER) a[P_EES] += EES;
+        if (B12 != 0.f) {
+          const float R2I = R1EI * R1EI;
+          const float R6I = R2I * R2I * R2I;
+          float ESR = (A6 + B12 * R6I) * R6I;
+          const float FSR = (6.f * A6 + 12.f * B12 * R6I) * R6I * R1EI;
+          FORCE = FORCE + FSR * R1I;
+          bool count_esr_split = true;
+          if (same) {
+            if (SHORT) {
+              if (lmovei) {
+                if (ENER) a[P_VIR] += FSR * R1;
+              } else {
+                ESR = 0.f;
+                FORCE = 0.f;
+                count_esr_split = false;
+              }
             } else {
-              ESR = 0.f;
-              FORCE = 0.f;
-              count_esr_split = false;
+              if (ENER && lmovei) a[P_VIR] += FSR * R1;
+            }
+            if (count_esr_split) {
+              if (ENER) a[P_ESR_SAME] += ESR;
+              if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], (double)ESR);
             }
           } else {
-            if (ENER && lmovei) a[P_VIR] += FSR * R1;
+            if (ENER) a[P_ESR_DIFF] += ESR;
+            if (SPLIT) atomicAdd(&s_split[MDX_NTPP + tc.mdx[ti][tj]], (double)ESR);
+            if (ENER) a[P_VIR] += FSR * R1;
           }
-          if (count_esr_split) {
-            if (ENER) a[P_ESR_SAME] += ESR;
-            if (SPLIT) atomicAdd(&s_split[2 * MDX_NTPP + MDX_NT + ti], (double)ESR);
-          }
-        } else {
-          if (ENER) a[P_ESR_DIFF] += ESR;
-          if (SPLIT) atomicAdd(&s_split[MDX_NTPP + tc.mdx[ti][tj]], (double)ESR);
-          if (ENER) a[P_VIR] += FSR * R1;
+          if (ENER) a[P_ESR] += ESR;
         }
-        if (ENER) a[P_ESR] += ESR;
+        if (SHORT || !same || lmovei) {
+          if (ENER) a[P_VX] += FORCE * (DX * DX);
+          if (ENER) a[P_VY] += FORCE * (DY * DY);
+          if (ENER) a[P_VZ] += FORCE * (DZ * DZ);
+        }
+        fxa += FORCE * DX;
+        fya += FORCE * DY;
+        fza += FORCE * DZ;
       }
-      if (SHORT || !same || lmovei) {
-        if (ENER) a[P_VX] += FORCE * (DX * DX);
-        if (ENER) a[P_VY] += FORCE * (DY * DY);
-        if (ENER) a[P_VZ] += FORCE * (DZ * DZ);
-      }
-      fxa += FORCE * DX;
-      fya += FORCE * DY;
-      fza += FORCE * DZ;
       v = vn;
       pj = pjn;
     }

@@ -295,7 +295,7 @@ int long_step(mdx_pimd *pi, int mstep) {
   for (int s = 1; s <= NFREQ; ++s) {
     RC(fork(pi));
     EACH_BEAD(RC(launch_kick_drift(ctx, 0.0, TSTEB, 0)); RC(launch_getcom(ctx));
-              if (s == NFREQ2 && mstep % p.ichnb == 0) RC(launch_build_lists(ctx));
+              if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
               if (s == NFREQ) {
                 RC(api_do_slforces(ctx, false));
                 RC(api_do_fforces(ctx, 1, false));
@@ -321,7 +321,8 @@ int long_step(mdx_pimd *pi, int mstep) {
 }
 
 int graph_long_step(mdx_pimd *pi, int mstep) {
-  const int g = mstep % pi->beads[0]->p.ichnb == 0 ? 1 : 0;
+  mdx_ctx *c0 = pi->beads[0];
+  const int g = list_update_every_step(c0) || mstep % c0->p.ichnb == 0 ? 1 : 0;
   if (!pi->g[g]) {
     PI_CUDA(cudaStreamBeginCapture(pi->stream, cudaStreamCaptureModeThreadLocal));
     const int rc = long_step(pi, mstep);

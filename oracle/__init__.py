@@ -20,9 +20,9 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with oracle/Makefile (gcc, a few seconds)."""
-    if force or not os.path.exists(LIB):
-        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile the oracle with oracle/Makefile (gcc, a few seconds; make
+    skips it when the library is newer than its sources)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
     return LIB
 
 
@@ -135,7 +135,8 @@ class Oracle:
     def chcnb(self):
         a, b = C.c_int32(), C.c_int32()
         self._check(self.L.ox_chcnb(self.h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        self.chcnb_counts = (a.value, b.value)
+        return self.chcnb_counts
 
     def lists(self):
         from mdynamix_gb300.abi import I32P

@@ -90,6 +90,10 @@ struct ox_state {
   int lhex, loct;
   double *sx, *sy, *sz, *vx, *vy, *vz, *fx, *fy, *fz, *gx, *gy, *gz, *hx,
       *hy, *hz, *ox, *oy, *oz, *wx, *wy, *wz;
+  /* Verlet-skin list mode (not in the reference): squared list radius and
+   * the positions of the last list build; list builds counted */
+  double rlist2, *rsx, *rsy, *rsz;
+  int nbuild;
   double *X, *Y, *Z, *PX, *PY, *PZ;
   int mbsh, mbln;
   int *nbs1, *nbs2, *nbl1, *nbl2;
@@ -152,6 +156,8 @@ static void reclen(ox_state *st, double scx, double scy, double scz) {
   st->hboyl = 0.5 * st->boyl;
   st->hbozl = 0.5 * st->bozl;
   st->rssq = st->p.rcut * st->p.rcut;
+  st->rlist2 = st->p.rskin > 0. ? (st->p.rcut + st->p.rskin) * (st->p.rcut + st->p.rskin)
+                                : st->rssq;
   st->vol = st->boxl * st->boyl * st->bozl;
   if (st->p.icell == 1) st->vol = 0.5 * st->vol;
 }
@@ -314,7 +320,7 @@ int ox_open(const mdx_dims *d, const mdx_topo *t, const mdx_params *p,
   double **arr[] = {&st->sx, &st->sy, &st->sz, &st->vx, &st->vy, &st->vz,
                     &st->fx, &st->fy, &st->fz, &st->gx, &st->gy, &st->gz,
                     &st->hx, &st->hy, &st->hz, &st->ox, &st->oy, &st->oz,
-                    &st->wx, &st->wy, &st->wz};
+                    &st->wx, &st->wy, &st->wz, &st->rsx, &st->rsy, &st->rsz};
   for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); ++k)
     *arr[k] = (double *)xcalloc((size_t)n + 1, sizeof(double));
   double **marr[] = {&st->X, &st->Y, &st->Z, &st->PX, &st->PY, &st->PZ};
@@ -369,7 +375,7 @@ void ox_close(ox_state *st) {
                   st->jtj, st->ktk, st->ltl, st->ituk, st->sx, st->sy, st->sz,
                   st->vx, st->vy, st->vz, st->fx, st->fy, st->fz, st->gx,
                   st->gy, st->gz, st->hx, st->hy, st->hz, st->ox, st->oy,
-                  st->oz, st->wx, st->wy, st->wz, st->X, st->Y, st->Z, st->PX,
+                  st->oz, st->wx, st->wy, st->wz, st->rsx, st->rsy, st->rsz, st->X, st->Y, st->Z, st->PX,
                   st->PY, st->PZ, st->nbs1, st->nbs2, st->nbl1, st->nbl2,
                   st->rkx, st->rky, st->rkz, st->br, st->be, st->ar, st->ae,
                   st->tr, st->te};
@@ -395,6 +401,7 @@ int ox_set_state(ox_state *st, const double *sx, const double *sy,
     st->vy[i + 1] = vy[i];
     st->vz[i + 1] = vz[i];
   }
+  st->nbuild = th ? th->list_builds : 0;
   if (th) {
     double bl = st->boxl, by = st->boyl, bz = st->bozl;
     st->th = *th;
@@ -454,6 +461,7 @@ int ox_get_state(ox_state *st, double *sx, double *sy, double *sz, double *vx,
     if (vz) vz[i] = st->vz[i + 1];
   }
   sync_thermo_box(st);
+  st->th.list_builds = st->nbuild;
   if (th) *th = st->th;
   return MDX_OK;
 }
@@ -510,8 +518,27 @@ static inline int chcnb_pair(const ox_state *st, int I, int J, int imol) {
     }
   }
   if (RRM <= st->short2) return 1;
-  if (RRM <= st->rssq) return 2;
+  if (RRM <= st->rlist2) return 2; /* RSSQ in the reference; RCUT+skin in skin mode */
   return 0;
+}
+
+/* Skin mode (not in the reference): rebuild once some atom has moved more
+ * than half the skin (minimum image) since the last build. */
+static int skin_moved(ox_state *st) {
+  const double h2 = 0.25 * st->p.rskin * st->p.rskin;
+  for (int I = 1; I <= st->nstot; ++I) {
+    double DX = st->sx[I] - st->rsx[I], DY = st->sy[I] - st->rsy[I],
+           DZ = st->sz[I] - st->rsz[I];
+    pbc(st, &DX, &DY, &DZ);
+    if (DX * DX + DY * DY + DZ * DZ > h2) return 1;
+  }
+  return 0;
+}
+
+/* The list update of a step: every ICHNB-th step (reference), or when an
+ * atom has moved half the skin (skin mode). */
+static int list_due(ox_state *st, int MSTEP) {
+  return st->p.rskin > 0. ? skin_moved(st) : MSTEP % st->p.ichnb == 0;
 }
 
 int ox_chcnb(ox_state *st, int32_t *mbsh, int32_t *mbln) {
@@ -610,6 +637,12 @@ int ox_chcnb(ox_state *st, int32_t *mbsh, int32_t *mbln) {
   }
   st->mbsh = (int)(MBSH < capS ? MBSH : capS);
   st->mbln = (int)(MBLN < capL ? MBLN : capL);
+  for (int I = 1; I <= n; ++I) {
+    st->rsx[I] = st->sx[I];
+    st->rsy[I] = st->sy[I];
+    st->rsz[I] = st->sz[I];
+  }
+  st->nbuild++;
   if (mbsh) *mbsh = (int32_t)MBSH;
   if (mbln) *mbln = (int32_t)MBLN;
   if (MBSH > capS) {
@@ -846,6 +879,8 @@ static void forces_range(ox_state *st, mdx_scalars *s, double *gx, double *gy,
     double DZ = st->sz[ISP] - st->sz[JSP];
     pbc(st, &DX, &DY, &DZ);
     double RR = DX * DX + DY * DY + DZ * DZ;
+    /* skin mode: the list reaches RCUT + skin, pairs beyond RCUT are skipped */
+    if (st->p.rskin > 0. && RR > st->rssq) continue;
     double R1 = sqrt(RR);
     double R1I = 1. / R1;
     double R1E = R1 + RAE;
@@ -2290,7 +2325,7 @@ int ox_double_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
           st->sz[I] = st->vz[I] * TSTEB * st->massdi[I] + st->sz[I];
         }
       ox_getcom(st);
-      if (NSTEB == NFREQ2 && MSTEP % st->p.ichnb == 0)
+      if (NSTEB == NFREQ2 && list_due(st, MSTEP))
         if ((rc = ox_chcnb(st, NULL, NULL))) return rc;
       if (NSTEB == NFREQ) {
         if ((rc = ox_slforces(st, NULL))) return rc;
@@ -2361,7 +2396,7 @@ int ox_sultan_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
     for (int k = 0; k < 3; ++k) st->th.vira[k] = st->th.viran[k];
     if ((rc = scaling(st, 3))) goto out;
     ox_getcom(st);
-    if (MSTEP % st->p.ichnb == 0)
+    if (list_due(st, MSTEP))
       if ((rc = ox_chcnb(st, NULL, NULL))) goto out;
     if ((rc = ox_allforce(st, NULL))) goto out;
     if (rec) fill_record(st, MSTEP, &rec[NSTEP - 1]);
