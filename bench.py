@@ -24,6 +24,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -48,6 +49,11 @@ OPS_EW_PAIR = 24         # per (paired record, atom): S(k) 4 FMA + forces 8 FMA
 OPS_EW_COL = 23          # per (column, atom): X Y twice, Im(T U), Im(T V), F
 OPS_EW_ROW = 8           # per (phase-table row, atom): recurrence step + charge
 OPS_EW_K = 20            # per k-vector (energy, virial, W)
+# The same work in the scope table's frozen per-(k, atom) count (a per-k
+# loop: phase 5, sin + cos 2, q x 2, S accumulate 2, force 10) + 20 per k;
+# the paired-record passes above do about half the multiply-adds of that
+# loop, so this count reads higher for the same time.
+OPS_EW_FROZEN_KATOM = 21
 
 # DRAM bytes per long step of each group, from ncu captures of
 # `python bench.py --only {fp64,mixed} --steps 2 --warmup 3`
@@ -76,10 +82,10 @@ class Clocks:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "_work", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="mdx_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
@@ -105,6 +111,7 @@ class Clocks:
     def summary(self):
         try:
             rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+            os.unlink(self.path)
         except OSError:
             rows = []
         rows = [[c.strip() for c in r] for r in rows if len(r) >= 8]
@@ -154,11 +161,16 @@ def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps
                  "achieved_tflops": v[1] / (v[0] * 1e-3) / 1e12,
                  "traffic": (TRAFFIC_MB.get((prec, g)) or 0) * 1e6, "kernels": v[2]}
              for g, v in groups.items()}
+    frozen = OPS_EW_FROZEN_KATOM * nkv * n + OPS_EW_K * nkv if top == "ewald" else ops
     return {"bound": "fp64" if prec == "fp64" else "fp32", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "traffic": tr * 1e6 if tr is not None else None,
             "kernel": f"{top}: {kernels}", "ms_per_long_step": t_ms, "share_of_step": share,
-            "ops_per_long_step": ops, "groups": other,
+            "ops_per_long_step": ops,
+            "frozen": {"ops_per_long_step": frozen,
+                       "achieved": frozen / (t_ms * 1e-3) / 1e12,
+                       "frac": frozen / (t_ms * 1e-3) / 1e12 / peak if peak else None},
+            "groups": other,
             "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak, of measured)"}
 
 
@@ -215,7 +227,31 @@ def run_gpu(args, rank, world, local):
         g.double_steps(args.steps, args.warmup + args.steps, records=False)
         tm = g.timers()
         g.set_timers(False)
-        out[prec] = dict(ms=ms, launches=launches, timers=tm, clocks=clk.summary(), ctx=g)
+        out[prec] = dict(ms=ms, launches=launches, timers=tm, clocks=clk.summary(), ctx=g,
+                         path=g.path_info())
+    # the same workload with the 1.5 A Verlet skin (rows to 13.5 A, pairs
+    # beyond 12 A skipped, rebuilt after 0.75 A of travel)
+    skin = {}
+    if args.skin:
+        from mdynamix_gb300 import system as S
+        import dataclasses
+        s_skin = S.System(dataclasses.replace(s.spec, rskin=1.5))
+        for prec in ("fp64", "mixed"):
+            g = ForcePath(s_skin, precision=MDX_FP64 if prec == "fp64" else MDX_MIXED)
+            g.set_state(*st)
+            g.double(0)
+            g.double_steps(args.warmup, 0, records=False)
+            stream = torch.cuda.ExternalStream(g.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            _, th0 = g.get_state()
+            e0.record(stream)
+            g.double_steps(args.steps, args.warmup, records=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            _, th1 = g.get_state()
+            skin[prec] = dict(ms=e0.elapsed_time(e1), builds=th1.list_builds - th0.list_builds)
+            g.close()
     # list sizes and force error at the shared start state
     g64 = ForcePath(s, precision=MDX_FP64)
     g32 = ForcePath(s, precision=MDX_MIXED)
@@ -223,8 +259,9 @@ def run_gpu(args, rank, world, local):
         g.set_state(*st)
         mbsh, mbln = g.chcnb()
         g.getcom()
-        g.allforce()
+        g.last_allforce = g.allforce()
     f64, f32 = g64.forces(3), g32.forces(3)
+    g32.close()
     ferr = float(np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum()))
     ferr_max = float(np.abs(f32 - f64).max() / np.abs(f64).max())
     # e2e through the C ABI with pinned host buffers
@@ -248,9 +285,12 @@ def run_gpu(args, rank, world, local):
     peak32 = probe_fma_peak(False)
     from mdynamix_gb300.abi import MdxStepRecord
     import ctypes
+    for prec in ("fp64", "mixed"):
+        out[prec]["ctx"].close()
     return dict(rec_bytes=ctypes.sizeof(MdxStepRecord), out=out, n=n, mbsh=mbsh, mbln=mbln, ferr=ferr, ferr_max=ferr_max,
                 e2e_s=e2e_s, e2e_steps=ke, peak64=peak64, peak32=peak32, dist=dist,
-                kset=(s.kvector_count(),) + s.kcolumn_counts(), nfreq=s.spec.nfreq)
+                kset=(s.kvector_count(),) + s.kcolumn_counts(), nfreq=s.spec.nfreq, skin=skin,
+                g64=g64)
 
 
 def serving_leg(args):
@@ -435,19 +475,42 @@ def nve_leg(args):
     return out
 
 
-def cpu_baseline(s, st, threads, budget_s=40.0):
-    """The oracle (restated reference routines) on the same workload:
-    one CHCNB and one long step, list build amortised over ICHNB steps."""
+def cpu_baseline_and_parity(s, st, threads, g64):
+    """The oracle (restated reference routines) on the same workload: one
+    CHCNB and one long step, the list build amortised over ICHNB steps; and,
+    on the way, the parity check of the FP64 GPU path at this size: lists
+    bit for bit, ALLFORCE forces, energies and virials at the start state."""
     import oracle
     o = oracle.Oracle(s, threads=threads)
     o.set_state(*st)
-    t0 = time.perf_counter(); o.chcnb(); t_list = time.perf_counter() - t0
-    o.getcom(); o.slforces(); o.fforces()
+    t0 = time.perf_counter(); counts = o.chcnb(); t_list = time.perf_counter() - t0
+    par = {"lists_bit_exact": None}
+    if g64 is not None:
+        (gs1, gs2), (gl1, gl2) = g64.lists()
+        (os1, os2), (ol1, ol2) = o.lists()
+        par["lists_bit_exact"] = bool(
+            g64.counts == counts and np.array_equal(gs1, os1) and np.array_equal(gs2, os2)
+            and np.array_equal(gl1, ol1) and np.array_equal(gl2, ol2))
+        del gs1, gs2, gl1, gl2, os1, os2, ol1, ol2
+    o.getcom()
+    b = o.allforce()
+    if g64 is not None:
+        fo = o.forces(3)
+        fg = g64.forces(3)
+        a = g64.last_allforce
+        par["force_rel_max"] = float(np.abs(fg - fo).max() / np.abs(fo).max())
+        par["scalar_rel_max"] = float(max(
+            abs(getattr(a, n) - getattr(b, n)) / abs(getattr(b, n))
+            for n in ("pe1", "pels1", "pe2", "pels2", "spe", "pint", "vir1", "vir2", "virb",
+                      "virx", "viry", "virz", "wirs", "wirss") if getattr(b, n) != 0.0))
+        par["pairs"] = {"short": int(counts[0]), "long": int(counts[1])}
+        par["tolerance"] = 1e-10
     t0 = time.perf_counter(); o.double_steps(1, 0); t_step = time.perf_counter() - t0
     per = t_step + t_list / s.spec.ichnb
-    return {"value": s.nstot / per, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"1 long step ({t_step:.2f} s) + 1 CHCNB ({t_list:.2f} s) / ICHNB "
-                      f"on the full 98304-atom workload, C restatement -O2 OpenMP"}
+    cpu = {"value": s.nstot / per, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"1 long step ({t_step:.1f} s) + CHCNB ({t_list:.1f} s)/ICHNB, full "
+                     f"98304-atom workload, C restatement -O2 OpenMP"}
+    return cpu, par
 
 
 def reference_arm(args, rank, world):
@@ -482,13 +545,89 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _r(x, sig=4):
+    """Round floats (recursively) to sig significant digits for the line."""
+    if isinstance(x, float):
+        return float(f"{x:.{sig}g}") if math.isfinite(x) else x
+    if isinstance(x, dict):
+        return {k: _r(v, sig) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_r(v, sig) for v in x]
+    return x
+
+
+def extra_legs(args):
+    """Evidence runs printed as their own JSON lines (not part of the
+    default run): the plain-method case's NVE run and the reference
+    sample's statistics."""
+    import torch  # noqa: F401  (CUDA context first)
+    if "cfg1" in args.leg:
+        print(json.dumps({"leg": "cfg1_nve", **_r(cfg1_nve_leg(args))}), flush=True)
+    if "sample" in args.leg:
+        from tests.nacl776 import reference_averages, sample_run_averages
+        from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+        out = {"reference_4nacl_out": reference_averages()}
+        for name, prec in (("fp64", MDX_FP64), ("mixed", MDX_MIXED)):
+            t0 = time.perf_counter()
+            out[name] = sample_run_averages(prec)
+            out[name + "_wall_s"] = time.perf_counter() - t0
+        print(json.dumps({"leg": "sample_4nacl", **_r(out, 6)}), flush=True)
+
+
+def cfg1_nve_leg(args):
+    """512 rigid SPC/E + 4 Na+ + 4 Cl- (1544 atoms), SULTAN + SHEJK: SHAKE
+    iterations at TOLER 1e-8 taken literally and at 1.4e-4; energy
+    conservation over 1000 NVE steps (2 fs) after 1000 NVT steps from the
+    lattice start, FP64 and mixed."""
+    import dataclasses
+    from mdynamix_gb300 import system as S
+    from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+    from mdynamix_gb300.mdx import ForcePath
+    out = {}
+    for toler in (1e-8, 1.4e-4):
+        s = S.System(dataclasses.replace(S.spce_nacl_nve(), toler=toler, nvt=(300.0, 30.0)))
+        st = S.make_configuration(s, seed=1, jitter=0.05)
+        g = ForcePath(s)
+        g.set_state(*st)
+        g.sultan(args.cfg1_equil, records=False)
+        state, th = g.get_state()
+        g.close()
+        for name, prec in (("fp64", MDX_FP64), ("mixed", MDX_MIXED)):
+            g = ForcePath(s, precision=prec)
+            p = g.packed.params
+            p.lnvt = 0
+            g.set_params(p)
+            th.sc = 0.0
+            g.set_state(*state, thermo=th)
+            t0 = time.perf_counter()
+            rec = g.sultan(args.cfg1_steps, args.cfg1_equil)
+            wall = time.perf_counter() - t0
+            _, th_end = g.get_state()
+            g.close()
+            e = np.array([r.pe1 + r.pe2 + r.pels1 + r.pels2 + r.spe + r.pint + r.tke for r in rec])
+            ke = np.array([r.tke for r in rec])
+            t = np.arange(len(rec)) * 2e-3
+            its = [r.shake_iter for r in rec]
+            out[f"toler_{toler:g}_{name}"] = {
+                "drift_per_ps_over_ke_rms": float(np.polyfit(t, e, 1)[0] / ke.std()),
+                "etot_rms_over_ke_rms": float(e.std() / ke.std()),
+                "shake_iter_mean": float(np.mean(its)), "shake_iter_max": int(max(its)),
+                "molecules_past_maxit": int(th_end.shake_fail),
+                "temp_mean": float(np.mean([r.temp for r in rec])),
+                "atom_steps_per_s": s.nstot * len(rec) / wall}
+    out["sample"] = (f"{args.cfg1_equil} NVT (300 K, 30 fs) steps from the seeded lattice, "
+                     f"then {args.cfg1_steps} NVE steps per path; TOLER is squared by SHEJK")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and parity leg")
+    ap.add_argument("--no-skin", dest="skin", action="store_false", help="skip the skin-mode leg")
     ap.add_argument("--serve-jobs", type=int, default=32, help="serving leg sample (0 = off)")
     ap.add_argument("--serve-steps", type=int, default=20, help="long steps per coupling state")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
@@ -499,6 +638,11 @@ def main():
     ap.add_argument("--bilayer-warmup", type=int, default=3)
     ap.add_argument("--nve-steps", type=int, default=500, help="NVE leg long steps (0 = off)")
     ap.add_argument("--nve-equil", type=int, default=100)
+    ap.add_argument("--leg", nargs="*", default=[], choices=["cfg1", "sample"],
+                    help="evidence runs only (their own JSON lines, no headline line)")
+    ap.add_argument("--cfg1-steps", type=int, default=1000)
+    ap.add_argument("--cfg1-equil", type=int, default=1000)
+    ap.add_argument("--detail", default=None, help="also write the full results to this file")
     ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
                     help="profiling runs: one precision, no e2e/error legs, no JSON line")
     args = ap.parse_args()
@@ -506,6 +650,10 @@ def main():
     rank, world, local = env_rank()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.leg:
+        if rank == 0:
+            extra_legs(args)
         return
     r = run_gpu(args, rank, world, local)
     if r is None:
@@ -527,43 +675,76 @@ def main():
     pimd = pimd_leg(args) if args.pimd_steps > 0 else None
     bilayer = bilayer_leg(args) if args.bilayer_steps > 0 else None
     nve = nve_leg(args) if args.nve_steps > 0 else None
-    cpu = None
+    cpu = parity = None
     if world == 1 and not args.no_cpu:
         s, st = make_system()
-        cpu = cpu_baseline(s, st, os.cpu_count() or 1)
+        cpu, parity = cpu_baseline_and_parity(s, st, os.cpu_count() or 1, r["g64"])
+    r["g64"].close()
     dt_fs = 2.0
+    full = {"roofline": roof, "mixed_roofline": roof32, "serving": serving, "pimd": pimd,
+            "bilayer": bilayer, "nve": nve, "cpu_baseline": cpu, "parity": parity,
+            "timers_ms_fp64": {k: v[0] / args.steps for k, v in o64["timers"].items()},
+            "timers_ms_mixed": {k: v[0] / args.steps for k, v in o32["timers"].items()},
+            "skin": r["skin"]}
+    if args.detail:
+        with open(args.detail, "w") as fh:
+            json.dump(full, fh, indent=1)
+
+    def roof_short(x):
+        return {"bound": x["bound"], "achieved": x["achieved"], "peak": x["peak"],
+                "unit": x["unit"], "frac": x["frac"], "traffic": x["traffic"],
+                "kernel": x["kernel"].split(":")[0] + " group",
+                "frac_frozen_ops": x["frozen"]["frac"], "ms_per_step": x["ms_per_long_step"],
+                "share": x["share_of_step"]}
+
+    skin = None
+    if r["skin"]:
+        k64, k32 = r["skin"]["fp64"], r["skin"]["mixed"]
+        skin = {"rskin_A": 1.5,
+                "fp64": world * n * args.steps / (k64["ms"] * 1e-3),
+                "mixed": world * n * args.steps / (k32["ms"] * 1e-3),
+                "list_builds": [k64["builds"], k32["builds"]]}
     line = {
         "metric": METRIC, "value": v64, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": o64["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(WORKLOAD, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
         "ns_per_day": v64 / n * dt_fs * 1e-6 * 86400,
-        "mixed": {"value": v32, "unit": UNIT, "ms_per_step": o32["ms"] / args.steps,
-                  "dtype": "f32 pair/bonded/Ewald products, i64 fixed-point force sums, "
-                           "f64 S(k)/reductions/update",
+        "mixed": {"value": v32, "ms_per_step": o32["ms"] / args.steps,
                   "speedup_vs_fp64": v32 / v64, "force_err_rms": r["ferr"],
                   "force_err_max_rel": r["ferr_max"],
-                  "ns_per_day": v32 / n * dt_fs * 1e-6 * 86400,
-                  "roofline": roof32, "gpu_launches": o32["launches"],
-                  "clocks": o32["clocks"],
-                  "timers_ms": {k: round(v[0] / args.steps, 4) for k, v in o32["timers"].items()}},
-        "roofline": roof,
-        "timers_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in o64["timers"].items()},
+                  "dtype": "f32 pair/bonded/Ewald products; S(k) f32 per slice, f64 across "
+                           "slices; i64 fixed-point forces; f64 reductions and update",
+                  "path": o32["path"], "roofline": roof_short(roof32),
+                  "gpu_launches": o32["launches"], "clocks": o32["clocks"]},
+        "roofline": roof_short(roof),
         "e2e": {"value": world * n / r["e2e_s"], "unit": UNIT,
                 "h2d_bytes_per_step": 6 * n * 8,
-                "d2h_bytes_per_step": 6 * n * 8 + r["rec_bytes"],
-                "steps": r["e2e_steps"]},
+                "d2h_bytes_per_step": 6 * n * 8 + r["rec_bytes"]},
         "gpu_launches": o64["launches"],
         "clocks": o64["clocks"],
-        "serving": serving,
-        "pimd": pimd,
-        "bilayer": bilayer,
-        "nve": nve,
+        "parity": parity,
+        "skin": skin,
         "cpu_baseline": cpu,
-        "lists": {"mbsh": r["mbsh"], "mbln": r["mbln"]},
-        "peaks_tflops": {"fp64_fma_measured": r["peak64"], "fp32_fma_measured": r["peak32"]},
     }
-    print(json.dumps(line), flush=True)
+    if serving:
+        line["serving"] = {k: {"value": serving[k]["atom_steps_per_s"],
+                               "p50_s": serving[k]["p50_s"], "p99_s": serving[k]["p99_s"]}
+                           for k in ("mixed", "fp64")}
+        line["serving"]["speedup"] = serving["speedup_mixed_vs_fp64"]
+    if pimd:
+        line["pimd"] = {"mixed": pimd["mixed"]["atom_steps_per_s"],
+                        "fp64": pimd["fp64"]["atom_steps_per_s"],
+                        "speedup": pimd["speedup_mixed_vs_fp64"],
+                        "force_err_rms": pimd["force_err_rms_mixed_vs_fp64"]}
+    if bilayer:
+        line["bilayer"] = {"mixed": bilayer["mixed"]["atom_steps_per_s"],
+                           "fp64": bilayer["fp64"]["atom_steps_per_s"],
+                           "speedup": bilayer["speedup_mixed_vs_fp64"],
+                           "force_err_rms": bilayer["mixed_vs_fp64_rel_err"]["force_rms"]}
+    if nve:
+        line["nve"] = {k: nve[k]["drift_per_ps_over_ke_rms"] for k in ("fp64", "mixed")}
+    print(json.dumps(_r(line)), flush=True)
     if r["dist"]:
         r["dist"].destroy_process_group()
 

@@ -165,7 +165,8 @@ typedef struct {
   double trpres, trpresx, trpresy, trpresz;
   double dqt, dqp, rtp;      /* thermostat/barostat constants (main.f)   */
   double fnst, fnop;         /* FNST degrees of freedom, FNOP            */
-  double ftscl, ftimes;      /* SCLFRC level, FTIMES                     */
+  double ftscl, ftimes;      /* FTSCL = 1 / Cut_forces level (main.f:850),
+                                FTIMES                                  */
   double convet;             /* CONVET (setup.f:119)                     */
   double unitp;              /* UNITP                                    */
   double efact;              /* EFACT = 1.D3/AVSNO/UNITE (setup.f:395)   */
@@ -241,6 +242,22 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
                      const double *vz, const mdx_thermo *th);
 int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
                        double *vx, double *vy, double *vz, mdx_thermo *th);
+/* Asynchronous copy of the state for restart dumps and trajectory frames
+ * written off the step loop (RESTRT(2) restart.f:308-420 and TRACE
+ * restart.f:425-598 read SX/VX on the host; the reference stops its step
+ * loop to write them).  mdx_snapshot queues, on the context's stream and
+ * after the work already queued there, the copy of positions, momenta and
+ * (th != NULL) the thermostat/box state into the given host buffers, and
+ * returns at once; use page-locked buffers (a copy into pageable memory
+ * waits for the stream).  mdx_snapshot_wait(slot) blocks until that copy has
+ * landed and may be called from another host thread.  Slots 0 ..
+ * MDX_SNAPSHOT_SLOTS-1 let several snapshots be in flight; a slot's buffers
+ * must not be reused before its wait returns.  The first call allocates a
+ * device staging buffer and waits for the stream once. */
+#define MDX_SNAPSHOT_SLOTS 8
+int mdx_snapshot(mdx_ctx *ctx, int32_t slot, double *sx, double *sy, double *sz,
+                 double *vx, double *vy, double *vz, mdx_thermo *th);
+int mdx_snapshot_wait(mdx_ctx *ctx, int32_t slot);
 /* which: 1 = H (fast), 2 = G (slow), 3 = F = G + H */
 int mdx_download_forces(mdx_ctx *ctx, int which, double *fx, double *fy,
                         double *fz);
@@ -297,6 +314,25 @@ int mdx_sultan_steps(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0,
 int mdx_double_enqueue(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, int32_t prologue);
 int mdx_poll(mdx_ctx *ctx, int32_t *done);
 int mdx_device_memory(size_t *free_bytes, size_t *total_bytes);
+/* Diagnostic: bytes in use and reserved in the current device's default
+ * memory pool, from which contexts allocate (cudaMallocAsync). */
+int mdx_pool_usage(size_t *used_bytes, size_t *reserved_bytes);
+/* Which kernels the context runs, for reports next to measured numbers (no
+ * counterpart in the reference).  Valid once the k-set exists.
+ *  ewald_force_pass: 0 FP64 CUDA cores; 1 FP32 CUDA cores; 2 TF32 tensor
+ *                    cores, three products per operand pair.
+ *  ewald_sfac_pass:  0 FP64 per slice, slices summed in FP64; 1 FP32 FMAs
+ *                    per slice, slices summed in FP64; 2 TF32 tensor cores
+ *                    with FP32 partials of 1024 atoms summed in FP64.
+ *  sfac_ordered:     1 when slice partials are summed in slice order (the
+ *                    reciprocal sums are then reproducible run to run).
+ *  list_mode:        0 the reference's (CHCNB every ICHNB long steps);
+ *                    1 Verlet skin. */
+typedef struct {
+  int32_t precision, ewald_force_pass, ewald_sfac_pass, sfac_slices;
+  int32_t sfac_ordered, list_mode, graphs, nkv;
+} mdx_path_info;
+int mdx_get_path_info(const mdx_ctx *ctx, mdx_path_info *out);
 /* Diagnostic: the CUDA runtime error recorded for the calling thread and not
  * yet consumed (0 = none), without clearing it. */
 int mdx_pending_cuda_error(void);
@@ -314,11 +350,35 @@ int mdx_pending_cuda_error(void);
  * MDX_ERR_STATE when the k-set is not built yet or the box left its 5 %
  * window (a new k-set allocates: call mdx_inifur), or when timers are on.
  * The first call on a device sets up the scratch address; make it before any
- * stream capture.  Calls whose kernels overlap on the device (other
+ * stream capture.  Under CUDA's lazy module loading that first call also
+ * loads the module that holds the array, so it reserves the 4 MiB then and
+ * can fail with MDX_ERR_CUDA when the device is full; later calls cannot.
+ * The address is cached per device for the process: do not cudaDeviceReset
+ * between calls.  With the mixed path's tensor-core S(k) pass on
+ * (MDX_EWALD_TC=2) the pass needs no slice scratch and the size limit does
+ * not apply.  Calls whose kernels overlap on the device (other
  * contexts, other streams or threads) share the scratch and race: serialise
  * them. */
 #define MDX_SK_STATIC_BYTES (4u << 20)
 int mdx_slforces_static(mdx_ctx *ctx, mdx_scalars *out);
+
+/* GETAVR's per-term statistics (aver.f:45-100) from the device.  The bonded
+ * routines form, per bond / angle / torsion record, the average over the
+ * type's molecules of its length (angle, dihedral) and energy -- BR/BE,
+ * AR/AE, TR/TE (forces.f:181-182, 272-273, 446-447) -- at every FFORCES
+ * with LAVER here.  mdx_get_bonded_averages returns those of the last such
+ * evaluation (NRBB, NRBB, NRAA, NRAA, NRTT, NRTT values; any pointer may be
+ * NULL; internal units, angles in radians).  With mdx_set_averaging(ctx, 1)
+ * every long step of DOUBLE / SULTAN evaluates its last fast forces with
+ * LAVER and adds the values and their squares to device sums;
+ * mdx_get_bonded_sums copies them out (1 + 4 (NRBB + NRAA + NRTT) doubles:
+ * the sample count, the sums of BR, BE, AR, AE, TR, TE back to back, then
+ * the sums of their squares in the same order) and, with clear != 0,
+ * restarts them -- the host keeps no per-step work at IAVER = 1. */
+int mdx_get_bonded_averages(mdx_ctx *ctx, double *br, double *be, double *ar, double *ae,
+                            double *tr, double *te);
+int mdx_set_averaging(mdx_ctx *ctx, int on);
+int mdx_get_bonded_sums(mdx_ctx *ctx, double *sums, int32_t clear);
 
 /* expanded-ensemble scaling (RECINT) */
 int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,

@@ -126,6 +126,16 @@ class MdxStepRecord(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MdxPathInfo(C.Structure):
+    """mdx_path_info: which passes a context runs."""
+    _fields_ = [(n, C.c_int32) for n in ("precision", "ewald_force_pass", "ewald_sfac_pass",
+                                         "sfac_slices", "sfac_ordered", "list_mode", "graphs",
+                                         "nkv")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class MdxKin(C.Structure):
     """mdx_kin: GETKIN's kinetic energies and temperatures."""
     _fields_ = [(n, C.c_double) for n in ("ektr", "ekrot", "ekint", "tke", "ttr", "trot",
@@ -262,7 +272,7 @@ def params_of(s: System) -> MdxParams:
     par.rtp = s.rtp
     par.fnst = s.fnst
     par.fnop = s.fnop
-    par.ftscl = sp.cut_forces or 0.0
+    par.ftscl = 1.0 / sp.cut_forces if sp.cut_forces else 0.0  # FTSCL=1./FTSCL, main.f:850
     par.ftimes = s.ftimes
     par.convet = s.convet
     par.unitp = s.unitp

@@ -12,6 +12,8 @@
 // BR/BE, AR/AE, TR/TE are only formed when the caller asks for them.
 #include <cmath>
 
+#include <algorithm>
+
 #include "mdx_internal.cuh"
 
 namespace {
@@ -725,5 +727,47 @@ int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
 #undef GT
     MDX_LAUNCHED(ctx);
   }
+  return MDX_OK;
+}
+
+// GETAVR's per-term statistics (aver.f:45-100) accumulated on the device: the
+// per-record averages BR/BE (bonds), AR/AE (angles), TR/TE (torsions) that
+// the bonded kernels have just formed under LAVER are added, with their
+// squares, to running sums, one sample per long step.  Layout of sums:
+// [0] samples; then the values of BR, BE, AR, AE, TR, TE back to back
+// (nrbb, nrbb, nraa, nraa, nrtt, nrtt entries: L in all), then their squares.
+__global__ void k_acc_bonded(int nrbb, int nraa, int nrtt, const double *__restrict__ br,
+                             const double *__restrict__ be, const double *__restrict__ ar,
+                             const double *__restrict__ ae, const double *__restrict__ tr,
+                             const double *__restrict__ te, double *__restrict__ sums) {
+  const int L = 2 * (nrbb + nraa + nrtt);
+  if (blockIdx.x == 0 && threadIdx.x == 0) sums[0] += 1.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
+    int r = k;
+    const double *src;
+    if (r < nrbb) src = br;
+    else if ((r -= nrbb) < nrbb) src = be;
+    else if ((r -= nrbb) < nraa) src = ar;
+    else if ((r -= nraa) < nraa) src = ae;
+    else if ((r -= nraa) < nrtt) src = tr;
+    else { r -= nrtt; src = te; }
+    const double v = src[r];
+    sums[1 + k] += v;
+    sums[1 + L + k] += v * v;
+  }
+}
+
+int bonded_sums_len(const mdx_ctx *ctx) {
+  return 1 + 4 * (ctx->dv.nrbb + ctx->dv.nraa + ctx->dv.nrtt);
+}
+
+int launch_acc_bonded(mdx_ctx *ctx) {
+  MDX_TIMER(ctx, MDX_T_OTHER);
+  DevData &d = ctx->dv;
+  if (!d.avsum) return MDX_OK;
+  const int L = 2 * (d.nrbb + d.nraa + d.nrtt);
+  k_acc_bonded<<<std::max(1, (L + 255) / 256), 256, 0, ctx->stream>>>(
+      d.nrbb, d.nraa, d.nrtt, d.br, d.be, d.ar, d.ae, d.tr, d.te, d.avsum);
+  MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -1023,8 +1023,8 @@ int host_inifur(mdx_ctx *ctx) {
     const char *env = std::getenv("MDX_EWALD_TC");
     const int mode = env && env[0] >= '0' && env[0] <= '2' ? env[0] - '0' : 1;
     d.tc_on = d.tcs_on = false;
-    if (mode >= 1 && !tc_force_setup(ctx, cols, KMAZ)) cudaGetLastError();
-    if (mode >= 2 && !tc_sfac_setup(ctx, cols)) cudaGetLastError();
+    if (mode >= 1 && tc_force_setup(ctx, cols, KMAZ) < 0) return MDX_ERR_CUDA;
+    if (mode >= 2 && tc_sfac_setup(ctx, cols) < 0) return MDX_ERR_CUDA;
   }
   // mixed S(k): slices sized so the grid is one wave of resident blocks
   size_t nslice_max = ((size_t)d.n + SLICE - 1) / SLICE;
@@ -1081,10 +1081,12 @@ int host_inifur(mdx_ctx *ctx) {
   // per-slice partials of S(k), summed in slice order
   ctx_free(ctx, d.sk_part);
   d.sk_part = nullptr;
-  if (ctx_alloc(ctx, &d.sk_part, sizeof(double2) * nslice_max * nk) !=
-      cudaSuccess) {
-    d.sk_part = nullptr;  // falls back to atomic slice sums
+  if (ctx_alloc(ctx, &d.sk_part, sizeof(double2) * nslice_max * nk) != cudaSuccess) {
+    // the ordered slice sum is what makes S(k) reproducible: no fallback
+    d.sk_part = nullptr;
     cudaGetLastError();
+    ctx->err = "S(k) slice partials: device allocation failed";
+    return MDX_ERR_NOMEM;
   }
   // self-energy (forces.f:1426-1447)
   const double ABC = alphad / std::sqrt(PI_REF);

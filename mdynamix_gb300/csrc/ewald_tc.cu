@@ -619,13 +619,22 @@ size_t sk_smem_bytes(int np, int kxy) {
 // Column order and tile table of the tensor-core force pass (host, from the
 // k-set columns) and its Z image.  Returns false when the pass does not
 // apply (its shared-memory tiles do not fit).
-bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
+// A failed set-up step of a tensor-core pass is an error of the call (no
+// silent switch to another pass): the message names the step and the CUDA
+// error, which is consumed.
+static int tc_fail(mdx_ctx *ctx, const char *what) {
+  const cudaError_t e = cudaGetLastError();
+  ctx->err = std::string(what) + (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : "");
+  return -1;
+}
+
+int tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
   DevData &d = ctx->dv;
   const int kp = ((2 * (kmaz + 1) + 7) / 8) * 8;
   d.tc_on = false;
   const int kxy = d.kx + d.ky;
   const int ntile = ((int)cols.size() + TC_COLS - 1) / TC_COLS;
-  if (tc_smem_bytes(kp, kxy, ntile) > 227 * 1024) return false;
+  if (tc_smem_bytes(kp, kxy, ntile) > 227 * 1024) return 0;  // tiles do not fit: CUDA cores
   std::vector<int> order(cols.size());
   for (size_t c = 0; c < cols.size(); ++c) order[c] = (int)c;
   std::stable_sort(order.begin(), order.end(),
@@ -649,36 +658,37 @@ bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz) {
       ctx_alloc(ctx, &d.tc_w, sizeof(float) * (size_t)ntile * 2 * TC_N * kp) != cudaSuccess ||
       ctx_alloc(ctx, &d.tc_meta, sizeof(float4) * slot.size()) != cudaSuccess ||
       ctx_alloc(ctx, &d.tc_zimg, zbytes) != cudaSuccess)
-    return false;
+    return tc_fail(ctx, "tensor-core force pass: device allocation");
   d.tc_ks = d.tc_slot + slot.size();
   if (ctx_copy(ctx->stream, d.tc_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       ctx_copy(ctx->stream, d.tc_ks, ks.data(), sizeof(int) * ks.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       cudaMemsetAsync(d.tc_zimg, 0, zbytes, ctx->stream) != cudaSuccess)  // K columns past 2 kz stay zero
-    return false;
-  if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy, ntile)) != cudaSuccess) return false;
+    return tc_fail(ctx, "tensor-core force pass: table upload");
+  if (raise_smem_limit(k_rforce_tc, tc_smem_bytes(kp, kxy, ntile)) != cudaSuccess)
+    return tc_fail(ctx, "tensor-core force pass: shared-memory limit");
   d.tc_ntile = ntile;
   d.tc_kp = kp;
   d.tc_on = true;
-  return true;
+  return 1;
 }
 
 // Tables of the tensor-core S(k) pass: M-tiles (up to SK_MT per CTA), slices
 // (about one wave of one CTA per SM), partial buffer, item offsets, Z image.  Returns false when it
 // does not apply.
-bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
+int tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   DevData &d = ctx->dv;
   d.tcs_on = false;
   const int np = ((2 * d.kz + 15) / 16) * 16;
   const int kxy = d.kx + d.ky;
-  if (np > 64 || sk_smem_bytes(np, kxy) > 227 * 1024) return false;
+  if (np > 64 || sk_smem_bytes(np, kxy) > 227 * 1024) return 0;  // does not fit
   const int ncol = (int)cols.size();
   const int ntm = (ncol + SK_ROWS / 2 - 1) / (SK_ROWS / 2);
   int nsm = 0, dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return false;
+    return tc_fail(ctx, "tensor-core S(k): device query");
   const int ncg = (ntm + SK_MT - 1) / SK_MT;  // CTAs per slice (up to SK_MT tiles each)
   int ns = std::max(1, nsm / ncg);
   int slice = (d.n + ns - 1) / ns;
@@ -701,15 +711,16 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
       ctx_alloc(ctx, &d.tcs_cp0, sizeof(int) * cp0.size()) != cudaSuccess ||
       ctx_alloc(ctx, &d.tcs_zimg, zbytes) != cudaSuccess ||
       ctx_alloc(ctx, &d.tcs_red, sizeof(double) * (size_t)ntm * SK_ROWS * np) != cudaSuccess)
-    return false;
+    return tc_fail(ctx, "tensor-core S(k): device allocation");
   if (ctx_copy(ctx->stream, d.tcs_cp0, cp0.data(), sizeof(int) * cp0.size(), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       // partials past the last slice's atoms are never written: they stay zero;
       // image rows 2p, 2p + 1 with p >= kz too
       cudaMemsetAsync(d.tcs_part, 0, pbytes, ctx->stream) != cudaSuccess ||
       cudaMemsetAsync(d.tcs_zimg, 0, zbytes, ctx->stream) != cudaSuccess)
-    return false;
-  if (raise_smem_limit(k_sfac_tc, sk_smem_bytes(np, kxy)) != cudaSuccess) return false;
+    return tc_fail(ctx, "tensor-core S(k): table upload");
+  if (raise_smem_limit(k_sfac_tc, sk_smem_bytes(np, kxy)) != cudaSuccess)
+    return tc_fail(ctx, "tensor-core S(k): shared-memory limit");
   d.tcs_np = np;
   d.tcs_ntm = ntm;
   d.tcs_nslice = ns;
@@ -718,7 +729,7 @@ bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols) {
   d.tcs_gps = gps;
   d.tcs_ncg = ncg;
   d.tcs_on = true;
-  return true;
+  return 1;
 }
 
 // Tensor map of the FP32 tables: a [kx + ky + kz][2 ldn] float tensor, box

@@ -227,13 +227,13 @@ int do_slforces(mdx_ctx *ctx, bool split, bool mirrored = false) {
   return MDX_OK;
 }
 
-int do_allforce(mdx_ctx *ctx, bool split) {
+int do_allforce(mdx_ctx *ctx, bool split, bool laver = false) {
   RC(launch_zero_fast(ctx));
   RC(launch_zero_slow(ctx));
   if (ctx->mixed()) RC(launch_mirror_f32(ctx));
   RC(launch_localf(ctx, split));
   RC(launch_wir(ctx, 1));  // WIRSS from the pair forces, before the bonded terms
-  RC(launch_bonded(ctx, split ? 1 : 0));
+  RC(launch_bonded(ctx, split || laver ? 1 : 0));
   if (ctx->mixed()) RC(launch_fix_to_double(ctx, 1));
   RC(do_slow_parts(ctx, split));
   RC(launch_wir(ctx, 2));
@@ -271,7 +271,10 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
     if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
     if (s == NFREQ) {
       RC(do_slforces(ctx, false, true));
-      RC(do_fforces(ctx, 0, false, true, true));
+      // the bonded statistics of the step (GETBND..GETTRS form them at every
+      // FFORCES, forces.f:113-513) when averages are kept on the device
+      RC(do_fforces(ctx, ctx->averaging ? 1 : 0, false, true, true));
+      if (ctx->averaging) RC(launch_acc_bonded(ctx));
     } else {
       RC(do_fforces(ctx, 0, false, false, true, !keep_fix));
     }
@@ -293,7 +296,8 @@ int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
   if (p.lnpt) RC(sync_box_from_device(ctx));
   RC(launch_getcom(ctx));
   RC(launch_list_update(ctx, mstep));
-  RC(do_allforce(ctx, false));
+  RC(do_allforce(ctx, false, ctx->averaging));
+  if (ctx->averaging) RC(launch_acc_bonded(ctx));
   if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters
   return MDX_OK;
 }
@@ -523,12 +527,14 @@ int mdx_close(mdx_ctx *ctx) {
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.kconst, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
-                  d.red_part, d.red_ctr, d.sk_part};
+                  d.red_part, d.red_ctr, d.sk_part, d.snap, d.avsum};
   if (ctx->stream) {
     for (void *p : ptrs) ctx_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
   }
   ctx->drop_graphs();
+  for (auto e : ctx->snap_ev)
+    if (e) cudaEventDestroy(e);
   for (auto &sp : ctx->spans) {
     cudaEventDestroy(sp.a);
     cudaEventDestroy(sp.b);
@@ -980,6 +986,76 @@ int mdx_download_state(mdx_ctx *ctx, double *sx, double *sy, double *sz,
   return MDX_OK;
 }
 
+int mdx_snapshot(mdx_ctx *ctx, int32_t slot, double *sx, double *sy, double *sz,
+                 double *vx, double *vy, double *vz, mdx_thermo *th) {
+  if (!ctx || slot < 0 || slot >= MDX_SNAPSHOT_SLOTS || !sx || !sy || !sz || !vx || !vy ||
+      !vz)
+    return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  DevData &d = ctx->dv;
+  const size_t n = d.n;
+  if (!d.snap) RC(dmalloc(ctx, &d.snap, 3 * n));  // first call: waits for the stream once
+  if (!ctx->snap_ev[slot])
+    MDX_CUDA(cudaEventCreateWithFlags(&ctx->snap_ev[slot], cudaEventDisableTiming));
+  k_get_pos<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.pos, d.snap, d.snap + n,
+                                                       d.snap + 2 * n);
+  MDX_LAUNCHED(ctx);
+  double *dst[6] = {sx, sy, sz, vx, vy, vz};
+  const double *src[6] = {d.snap, d.snap + n, d.snap + 2 * n, d.vx, d.vy, d.vz};
+  for (int k = 0; k < 6; ++k)
+    MDX_CUDA(cudaMemcpyAsync(dst[k], src[k], sizeof(double) * n, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  if (th)
+    MDX_CUDA(cudaMemcpyAsync(th, d.th, sizeof(mdx_thermo), cudaMemcpyDeviceToHost, ctx->stream));
+  MDX_CUDA(cudaEventRecord(ctx->snap_ev[slot], ctx->stream));
+  return MDX_OK;
+}
+
+int mdx_snapshot_wait(mdx_ctx *ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot >= MDX_SNAPSHOT_SLOTS || !ctx->snap_ev[slot]) return MDX_ERR_ARG;
+  const cudaError_t e = cudaEventSynchronize(ctx->snap_ev[slot]);
+  return e == cudaSuccess ? MDX_OK : MDX_ERR_CUDA;
+}
+
+int mdx_get_bonded_averages(mdx_ctx *ctx, double *br, double *be, double *ar, double *ae,
+                            double *tr, double *te) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, false, false));
+  DevData &d = ctx->dv;
+  MDX_CUDA(cudaStreamSynchronize(ctx->stream));
+  double *dst[6] = {br, be, ar, ae, tr, te};
+  const double *src[6] = {d.br, d.be, d.ar, d.ae, d.tr, d.te};
+  const int len[6] = {d.nrbb, d.nrbb, d.nraa, d.nraa, d.nrtt, d.nrtt};
+  for (int k = 0; k < 6; ++k)
+    if (dst[k] && len[k] > 0)
+      MDX_CUDA(ctx_copy(ctx->stream, dst[k], src[k], sizeof(double) * len[k],
+                        cudaMemcpyDeviceToHost));
+  return MDX_OK;
+}
+
+int mdx_set_averaging(mdx_ctx *ctx, int on) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, false, false));
+  DevData &d = ctx->dv;
+  if (on && !d.avsum) RC(dmalloc(ctx, &d.avsum, (size_t)bonded_sums_len(ctx)));
+  if ((on != 0) != ctx->averaging) ctx->drop_graphs();  // the step's launches change
+  ctx->averaging = on != 0;
+  return MDX_OK;
+}
+
+int mdx_get_bonded_sums(mdx_ctx *ctx, double *sums, int32_t clear) {
+  if (!ctx || !sums) return MDX_ERR_ARG;
+  DevData &d = ctx->dv;
+  const int len = bonded_sums_len(ctx);
+  if (!d.avsum) {
+    std::fill(sums, sums + len, 0.0);
+    return MDX_OK;
+  }
+  MDX_CUDA(ctx_copy(ctx->stream, sums, d.avsum, sizeof(double) * len, cudaMemcpyDeviceToHost));
+  if (clear) MDX_CUDA(cudaMemsetAsync(d.avsum, 0, sizeof(double) * len, ctx->stream));
+  return MDX_OK;
+}
+
 int mdx_download_forces(mdx_ctx *ctx, int which, double *fx, double *fy, double *fz) {
   if (!ctx || !fx || !fy || !fz || which < 1 || which > 3) return MDX_ERR_ARG;
   DevData &d = ctx->dv;
@@ -1177,6 +1253,35 @@ int mdx_device_memory(size_t *free_bytes, size_t *total_bytes) {
   if (cudaMemGetInfo(&f, &t) != cudaSuccess) return MDX_ERR_CUDA;
   if (free_bytes) *free_bytes = f;
   if (total_bytes) *total_bytes = t;
+  return MDX_OK;
+}
+
+int mdx_get_path_info(const mdx_ctx *ctx, mdx_path_info *out) {
+  if (!ctx || !out) return MDX_ERR_ARG;
+  const DevData &d = ctx->dv;
+  const bool mx = ctx->mixed();
+  out->precision = ctx->d.precision;
+  out->ewald_force_pass = !mx ? 0 : d.tc_on ? 2 : 1;
+  out->ewald_sfac_pass = !mx ? 0 : d.tcs_on ? 2 : 1;
+  out->sfac_slices = ctx->furir_init ? sfac_slices(ctx) : 0;
+  out->sfac_ordered = (mx && d.tcs_on) || d.sk_part != nullptr ? 1 : 0;
+  out->list_mode = ctx->p.rskin > 0.0 ? 1 : 0;
+  out->graphs = ctx->use_graphs ? 1 : 0;
+  out->nkv = ctx->nkv;
+  return MDX_OK;
+}
+
+int mdx_pool_usage(size_t *used_bytes, size_t *reserved_bytes) {
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess)
+    return MDX_ERR_CUDA;
+  uint64_t u = 0, r = 0;
+  if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u) != cudaSuccess ||
+      cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r) != cudaSuccess)
+    return MDX_ERR_CUDA;
+  if (used_bytes) *used_bytes = (size_t)u;
+  if (reserved_bytes) *reserved_bytes = (size_t)r;
   return MDX_OK;
 }
 

@@ -245,6 +245,8 @@ struct DevData {
   unsigned *red_ctr;
   size_t red_cap;      // doubles in red_part
   double2 *sk_part;    // per-slice S(k) partials (deterministic slice sum)
+  double *snap;        // mdx_snapshot: positions unpacked for the copy out (3n)
+  double *avsum;       // mdx_set_averaging: running sums of the bonded statistics
   size_t sk_part_cap;
 };
 
@@ -283,6 +285,7 @@ struct mdx_ctx {
   cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t glaunches[4] = {0, 0, 0, 0};
   bool use_graphs = true;
+  bool averaging = false;  // mdx_set_averaging: LAVER forces + statistics every long step
   void drop_graphs() {
     for (auto &g : gexec)
       if (g) {
@@ -291,6 +294,7 @@ struct mdx_ctx {
       }
   }
   int mbsh = 0, mbln = 0;
+  cudaEvent_t snap_ev[MDX_SNAPSHOT_SLOTS] = {};  // completion of mdx_snapshot per slot
   // device timers (mdx_set_timers)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -553,8 +557,10 @@ int host_inifur(mdx_ctx *ctx);
 int launch_furir(mdx_ctx *ctx);
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
-bool tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz);
-bool tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols);
+// 1: set up; 0: the k-set's tiles do not fit (the CUDA-core pass runs);
+// -1: a CUDA error (ctx->err says which step)
+int tc_force_setup(mdx_ctx *ctx, const std::vector<KCol> &cols, int kmaz);
+int tc_sfac_setup(mdx_ctx *ctx, const std::vector<KCol> &cols);
 int tc_sfac_launch(mdx_ctx *ctx);
 int tc_zimages_launch(mdx_ctx *ctx);
 int tc_force_launch(mdx_ctx *ctx);
@@ -571,6 +577,9 @@ int api_check_err(mdx_ctx *ctx);
 int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out);
 int api_do_slforces(mdx_ctx *ctx, bool split);
 int api_do_fforces(mdx_ctx *ctx, int laver, bool split);
+// bonded.cu: running sums of the per-record bonded statistics
+int launch_acc_bonded(mdx_ctx *ctx);
+int bonded_sums_len(const mdx_ctx *ctx);
 // integrate.cu
 int launch_zero_fast(mdx_ctx *ctx);
 int launch_zero_slow(mdx_ctx *ctx);

@@ -13,7 +13,9 @@
 //    window in which FURIR keeps that k-set (forces.f:1251-1265), else
 //    MDX_ERR_STATE;
 //  - the partial sums (slices x k-vectors x 16 bytes) must fit in
-//    MDX_SK_STATIC_BYTES, else MDX_ERR_UNSUPPORTED;
+//    MDX_SK_STATIC_BYTES, else MDX_ERR_UNSUPPORTED (not checked, and the
+//    scratch not used, when the mixed path's tensor-core S(k) pass is on:
+//    that pass keeps its partials in buffers of the k-set);
 //  - device timers must be off (they create events), else MDX_ERR_STATE.
 // Nothing in the static scratch has to start at zero: every (slice, k)
 // partial is written by the S(k) kernel before k_sfac_sum reads it.
@@ -22,7 +24,12 @@
 // on it and corrupt each other's S(k).  Serialise such calls.
 // Set-up: the first call on a device looks up the scratch's device address
 // with cudaGetSymbolAddress, with that device current; make that first call
-// before any stream capture that is to contain later calls.
+// before any stream capture that is to contain later calls.  Under CUDA's
+// lazy module loading that first lookup is also what loads this file's
+// module and with it the 4 MiB array: the first call per device can still
+// fail for want of device memory (MDX_ERR_CUDA), later calls cannot.  The
+// cached address belongs to the device context of the process; after a
+// cudaDeviceReset it is stale, so do not reset a device between calls.
 #include <mutex>
 
 #include "mdx_internal.cuh"
@@ -94,8 +101,11 @@ extern "C" int mdx_slforces_static(mdx_ctx *ctx, mdx_scalars *out) {
         return MDX_ERR_STATE;
       }
   }
+  // the tensor-core S(k) pass (mixed path) keeps its partials in buffers of
+  // the k-set and never touches the slice scratch
+  const bool uses_scratch = !(ctx->mixed() && d.tcs_on);
   const size_t need = (size_t)sfac_slices(ctx) * (size_t)std::max(1, d.nkv) * sizeof(double2);
-  if (need > MDX_SK_STATIC_BYTES) {
+  if (uses_scratch && need > MDX_SK_STATIC_BYTES) {
     char b[200];
     snprintf(b, sizeof b,
              "mdx_slforces_static: S(k) partial sums need %zu bytes; the static scratch "
@@ -103,6 +113,11 @@ extern "C" int mdx_slforces_static(mdx_ctx *ctx, mdx_scalars *out) {
              need, (size_t)MDX_SK_STATIC_BYTES);
     ctx->err = b;
     return MDX_ERR_UNSUPPORTED;
+  }
+  if (!uses_scratch) {
+    RC(api_do_slforces(ctx, true));
+    RC(api_check_err(ctx));
+    return api_copy_scalars(ctx, out);
   }
   void *scratch = nullptr;
   RC(scratch_address(ctx, &scratch));

@@ -71,6 +71,12 @@ def load():
     L.mdx_upload_state.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P, C.POINTER(MdxThermo)]
     L.mdx_download_state.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P, C.POINTER(MdxThermo)]
     L.mdx_download_forces.argtypes = [P, C.c_int, F64P, F64P, F64P]
+    L.mdx_snapshot.argtypes = [P, C.c_int32, F64P, F64P, F64P, F64P, F64P, F64P,
+                               C.POINTER(MdxThermo)]
+    L.mdx_snapshot_wait.argtypes = [P, C.c_int32]
+    L.mdx_get_bonded_averages.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P]
+    L.mdx_set_averaging.argtypes = [P, C.c_int]
+    L.mdx_get_bonded_sums.argtypes = [P, F64P, C.c_int32]
     L.mdx_inifur.argtypes = [P, I32P]
     L.mdx_chcnb.argtypes = [P, I32P, I32P]
     L.mdx_get_lists.argtypes = [P, I32P, I32P, C.c_int32, I32P, I32P, C.c_int32]
@@ -85,6 +91,9 @@ def load():
     L.mdx_double_enqueue.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     L.mdx_poll.argtypes = [P, I32P]
     L.mdx_device_memory.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    L.mdx_pool_usage.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    from mdynamix_gb300.abi import MdxPathInfo
+    L.mdx_get_path_info.argtypes = [P, C.POINTER(MdxPathInfo)]
     for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
         getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
     L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -253,6 +262,47 @@ class ForcePath:
         s = MdxScalars()
         self._check(self.L.mdx_allforce(self.h, C.byref(s)))
         return s
+
+    def path_info(self) -> dict:
+        """Which Ewald passes, list mode and graph replay the context uses."""
+        from mdynamix_gb300.abi import MdxPathInfo
+        info = MdxPathInfo()
+        self._check(self.L.mdx_get_path_info(self.h, C.byref(info)))
+        return info.as_dict()
+
+    def bonded_averages(self) -> dict:
+        """BR, BE, AR, AE, TR, TE of the last FFORCES with LAVER: per bond,
+        angle and torsion record, its length (angle) and energy averaged over
+        the type's molecules (forces.f:181-182, 272-273, 446-447)."""
+        s = self.system
+        out = {k: np.zeros(max(1, n)) for k, n in (("br", s.nrbb), ("be", s.nrbb),
+                                                    ("ar", s.nraa), ("ae", s.nraa),
+                                                    ("tr", s.nrtt), ("te", s.nrtt))}
+        self._check(self.L.mdx_get_bonded_averages(self.h, *[_fp(out[k]) for k in
+                                                             ("br", "be", "ar", "ae", "tr", "te")]))
+        n = {"br": s.nrbb, "be": s.nrbb, "ar": s.nraa, "ae": s.nraa, "tr": s.nrtt, "te": s.nrtt}
+        return {k: v[:n[k]] for k, v in out.items()}
+
+    def set_averaging(self, on: bool = True):
+        """Keep GETAVR's bonded statistics on the device, one sample per long
+        step (mdx_set_averaging)."""
+        self._check(self.L.mdx_set_averaging(self.h, int(on)))
+
+    def bonded_sums(self, clear: bool = False):
+        """(samples, sums, sums of squares) of BR, BE, AR, AE, TR, TE, each a
+        dict of arrays per record."""
+        s = self.system
+        lens = [("br", s.nrbb), ("be", s.nrbb), ("ar", s.nraa), ("ae", s.nraa),
+                ("tr", s.nrtt), ("te", s.nrtt)]
+        L = sum(n for _, n in lens)
+        buf = np.zeros(1 + 2 * L)
+        self._check(self.L.mdx_get_bonded_sums(self.h, _fp(buf), int(clear)))
+        sums, sq, off = {}, {}, 1
+        for k, n in lens:
+            sums[k] = buf[off:off + n].copy()
+            sq[k] = buf[1 + L + off - 1:1 + L + off - 1 + n].copy()
+            off += n
+        return int(buf[0]), sums, sq
 
     def _run(self, fn, nsteps, start, records=True):
         recs = (MdxStepRecord * max(1, nsteps))() if records else None

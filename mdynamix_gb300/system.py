@@ -965,6 +965,44 @@ def spcfw_water(nwater: int = 32768, nmax: int = 20, alpha_per_a: float = 0.25,
                    nvt=(300.0, 30.0), trtemp=300.0)
 
 
+def nacl_sample(box=None) -> RunSpec:
+    """The reference's own example, sample/4nacl.in: 256 flexible SPC
+    waters (H2O, fSPC) + 4 Na+_SD + 4 Cl-_SD at 1.02 g/cm3, double time step
+    0.2/2 fs, Nose-Hoover 298 K / 30 fs, R_cutoff 10, R_short 5, Ewald A = 3,
+    B = 9, Neighbour_list 10, Cut_forces 1.  ``box``: the box of a restart
+    file (the reference takes BOXL.. from the restart, restart.f:167)."""
+    return RunSpec(molecules=[("H2O", 256), ("Na+_SD", 4), ("Cl-_SD", 4)], density=1.02,
+                   box=None if box is None else tuple(float(x) for x in box), dt_fs=2.0,
+                   nfreq=10, rcut=10.0, rshort=5.0, alpha=3.0, fexp=9.0, ichnb=10,
+                   nvt=(298.0, 30.0), trtemp=298.0, cut_forces=1.0)
+
+
+def lrc_per_pair(s: System):
+    """PELRC and VRLRC per molecule-type pair (ELRCLJ, forces.f:1684-1736),
+    at the current volume, indexed by MDX - 1."""
+    pel = np.zeros(NTPP)
+    vrl = np.zeros(NTPP)
+    rc = math.sqrt(s.rssq)
+    for it in range(s.ntypes):
+        for is_ in range(s.isadr[it] + 1, s.isadr[it + 1] + 1):
+            ist = s.inbt[is_ - 1] - 1
+            for jt in range(it, s.ntypes):
+                mt = s.mdx[it, jt]
+                f = float(s.nspec[it] * s.nspec[jt])
+                if it == jt:
+                    f = 0.5 * f
+                for js in range(s.isadr[jt] + 1, s.isadr[jt + 1] + 1):
+                    jst = s.inbt[js - 1] - 1
+                    b12, a6 = s.b12lj[ist, jst], s.a6lj[ist, jst]
+                    if b12 > 1e-50 and a6 < -1e-50:
+                        ep = a6 ** 2 / b12
+                        si3 = math.sqrt(-b12 / a6)
+                        x = si3 / rc ** 3
+                        pel[mt - 1] += ep * si3 * ((1.0 / 9.0) * x ** 3 - (1.0 / 3.0) * x) * f
+                        vrl[mt - 1] += ep * si3 * ((-4.0 / 3.0) * x ** 3 + 2.0 * x) * f
+    return 4.0 * PI * pel / s.vol, -4.0 * PI * vrl / s.vol
+
+
 SOLUTES = ("CH3OH", "C2H5OH", "CH3CN", "dmso", "Li+", "Na+", "Cl-")
 
 

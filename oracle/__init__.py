@@ -154,6 +154,16 @@ class Oracle:
     def getcom(self):
         self._check(self.L.ox_getcom(self.h))
 
+    def bonded_averages(self):
+        s = self.system
+        out = {k: np.zeros(max(1, n)) for k, n in (("br", s.nrbb), ("be", s.nrbb),
+                                                    ("ar", s.nraa), ("ae", s.nraa),
+                                                    ("tr", s.nrtt), ("te", s.nrtt))}
+        self._check(self.L.ox_get_bonded_averages(self.h, *[_fp(out[k]) for k in
+                                                           ("br", "be", "ar", "ae", "tr", "te")]))
+        n = {"br": s.nrbb, "be": s.nrbb, "ar": s.nraa, "ae": s.nraa, "tr": s.nrtt, "te": s.nrtt}
+        return {k: v[:n[k]] for k, v in out.items()}
+
     def getkin(self):
         """GETKIN: [EKTR, EKROT, EKINT, TKE, TTR, TROT, TINT]."""
         from mdynamix_gb300.system import kin_summd

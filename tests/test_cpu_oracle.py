@@ -57,11 +57,15 @@ def test_exclusions_water_and_methanol():
     assert any((r < 0).any() for r in rows)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/moldb"), reason="reference tree absent")
+MOLDB_DIR = os.environ.get("MDX_REFERENCE_MOLDB", "")
+
+
+@pytest.mark.skipif(not os.path.isdir(MOLDB_DIR),
+                    reason="set MDX_REFERENCE_MOLDB to the reference's moldb directory")
 def test_moldb_fixture_matches_mmol_files():
     db = S.load_moldb()
-    for name in ("SPC_E", "SPC-FW", "H2O", "CH3OH", "dmpc"):
-        with open(f"/root/reference/moldb/{name}.mmol", encoding="latin-1") as fh:
+    for name in ("SPC_E", "SPC-FW", "H2O", "CH3OH", "dmpc", "Na+_SD", "Cl-_SD"):
+        with open(os.path.join(MOLDB_DIR, f"{name}.mmol"), encoding="latin-1") as fh:
             parsed = S.parse_mmol(fh.read(), name)
         assert parsed == db[name]
 
@@ -201,8 +205,10 @@ def test_abi_struct_sizes_match_c():
 #include <stdio.h>
 #include <stddef.h>
 #include "mdx_gpu.h"
-int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_topo),
- sizeof(mdx_params), sizeof(mdx_scalars), sizeof(mdx_thermo), sizeof(mdx_step_record));return 0;}
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_topo),
+ sizeof(mdx_params), sizeof(mdx_scalars), sizeof(mdx_thermo), sizeof(mdx_step_record),
+ sizeof(mdx_kin), sizeof(mdx_pimd_params), sizeof(mdx_pimd_record), sizeof(mdx_path_info));
+ return 0;}
 '''
     tmp = os.path.join(ROOT, "_build")
     os.makedirs(tmp, exist_ok=True)
@@ -213,7 +219,9 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
     got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(t) for t in (abi.MdxDims, abi.MdxTopo, abi.MdxParams,
-                                       abi.MdxScalars, abi.MdxThermo, abi.MdxStepRecord)]
+                                       abi.MdxScalars, abi.MdxThermo, abi.MdxStepRecord,
+                                       abi.MdxKin, abi.MdxPimdParams, abi.MdxPimdRecord,
+                                       abi.MdxPathInfo)]
     assert got == want
 
 

@@ -1,0 +1,171 @@
+"""GPU against the oracle on the named configurations and on the torsion
+forms no moldb molecule uses.
+
+- The plain-method case as specified: 512 rigid SPC/E + 4 Na+ + 4 Cl-
+  (1,544 atoms, 25.04 A box), R_cutoff 10, Ewald 2.8 / 9.84, SULTAN + SHEJK
+  with TOLER 1e-8 taken literally (SHEJK squares it, mdstep.f:1119, so the
+  bond lengths must meet 1e-16 relative: MAXIT is reached) and with TOLER
+  1.4e-4 (about 1e-8 in length), NVE.
+- GETTRS's MM3 (ITORS 1, forces.f:401-414), cosine-power (ITORS 5,
+  forces.f:415-434) and improper (ITORS -1, forces.f:435-440) branches on a
+  copy of ethanol whose dihedrals are switched to those forms.
+"""
+import copy
+import dataclasses
+
+import numpy as np
+import pytest
+
+import oracle
+from mdynamix_gb300 import system as S
+from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+
+pytestmark = pytest.mark.gpu
+FP64_TOL = 1e-10
+
+
+def relmax(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def cfg1(toler=1e-8):
+    s = S.System(dataclasses.replace(S.spce_nacl_nve(), toler=toler))
+    return s, S.make_configuration(s, seed=1, jitter=0.05)
+
+
+def _pair(s, st):
+    from mdynamix_gb300.mdx import ForcePath
+    g, o = ForcePath(s), oracle.Oracle(s, threads=4)
+    g.set_state(*st)
+    o.set_state(*st)
+    return g, o
+
+
+def test_cfg1_lists_and_forces():
+    s, st = cfg1()
+    assert s.nstot == 1544
+    g, o = _pair(s, st)
+    assert g.chcnb() == o.chcnb()
+    (gs1, gs2), (gl1, gl2) = g.lists()
+    (os1, os2), (ol1, ol2) = o.lists()
+    assert np.array_equal(gs1, os1) and np.array_equal(gl1, ol1)
+    assert np.array_equal(gs2, os2) and np.array_equal(gl2, ol2)
+    g.getcom(); o.getcom()
+    a, b = g.allforce(), o.allforce()
+    assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
+    for n in ("pe1", "pels1", "pe2", "pels2", "spe", "vir1", "vir2", "virx", "wirs", "wirss"):
+        assert abs(getattr(a, n) - getattr(b, n)) <= FP64_TOL * abs(getattr(b, n)), n
+
+
+@pytest.mark.parametrize("toler", [1e-8, 1.4e-4])
+def test_cfg1_sultan_shake_tracks_oracle(toler):
+    """Three SULTAN steps: positions to 1e-9 A; the same SHAKE iteration
+    counts (MAXIT + 1 = 2001 for the literal tolerance, every molecule
+    reported as not converged, as mdstep.f:1264-1269 prints)."""
+    s, st = cfg1(toler)
+    g, o = _pair(s, st)
+    rg, ro = g.sultan(3), o.sultan(3)
+    (gx, gy, gz, *_), tg = g.get_state()
+    (ox, oy, oz, *_), to = o.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
+    assert [r.shake_iter for r in rg] == [r.shake_iter for r in ro]
+    if toler == 1e-8:
+        assert all(r.shake_iter == 2001 for r in rg)
+    else:
+        assert all(r.shake_iter < 200 for r in rg)
+    for a, b in zip(rg, ro):
+        assert abs(a.temp - b.temp) <= 1e-8 * b.temp
+        assert abs(a.pels1 - b.pels1) <= 1e-8 * abs(b.pels1)
+
+
+def test_cfg1_nve_conserves_energy_like_fp64():
+    """Rigid SPC/E, SHEJK at TOLER 1.4e-4: after 400 NVT steps from the
+    lattice start, 300 NVE steps; the total energy's RMS stays a small
+    fraction of the kinetic energy's on both paths, and the mixed path
+    conserves it like the FP64 path."""
+    from mdynamix_gb300.mdx import ForcePath
+    s = S.System(dataclasses.replace(S.spce_nacl_nve(), toler=1.4e-4, nvt=(300.0, 30.0)))
+    st = S.make_configuration(s, seed=1, jitter=0.05)
+    g = ForcePath(s)
+    g.set_state(*st)
+    g.sultan(400, records=False)
+    state, th = g.get_state()
+    g.close()
+    out = {}
+    for prec in (MDX_FP64, MDX_MIXED):
+        g = ForcePath(s, precision=prec)
+        p = g.packed.params
+        p.lnvt = 0
+        g.set_params(p)
+        th.sc = 0.0
+        g.set_state(*state, thermo=th)
+        rec = g.sultan(300, 400)
+        e = np.array([r.pe1 + r.pe2 + r.pels1 + r.pels2 + r.spe + r.pint + r.tke for r in rec])
+        ke = np.array([r.tke for r in rec])
+        out[prec] = float(e.std() / ke.std())
+        assert max(r.shake_iter for r in rec) < 2001
+        g.close()
+    assert out[MDX_FP64] < 0.2, out
+    assert out[MDX_MIXED] < 2.0 * out[MDX_FP64] + 0.02, out
+
+
+# ------------------------------------------------------------ torsions --
+def torsion_db():
+    """moldb with 'C2H5OH' whose eight dihedrals cycle through ITORS 0, 1,
+    5 and -1 (parameters in kJ/mol and degrees, as .mmol files give them)."""
+    db = copy.deepcopy(S.load_moldb())
+    forms = [
+        dict(itors=0, nmul=3, ft=0.67, rt=0.0),
+        dict(itors=1, ft1=1.3, ft2=-0.45, ft3=0.8),
+        dict(itors=5, ft=0.4, ft1=1.1, ft2=-0.7, ft3=0.35, ft4=0.2, ft5=-0.12, rt=15.0),
+        dict(itors=-1, ft=0.02, rt=60.0),
+    ]
+    for k, t in enumerate(db["C2H5OH"]["tors"]):
+        base = dict(ft=0.0, ft1=0.0, ft2=0.0, ft3=0.0, ft4=0.0, ft5=0.0, rt=0.0, nmul=0)
+        base.update(forms[k % 4])
+        t.update(base)
+    return db
+
+
+def torsion_system():
+    db = torsion_db()
+    spec = S.RunSpec(molecules=[("H2O", 100), ("C2H5OH", 6)], density=1.0, dt_fs=2.0,
+                     nfreq=10, rcut=7.0, rshort=5.0, alpha=2.0, fexp=9.0, ichnb=10,
+                     nvt=(298.0, 30.0), trtemp=298.0)
+    s = S.System(spec, moldb=db)
+    assert set(s.t_itors.tolist()) == {0, 1, 5, -1}
+    return s, S.make_configuration(s, seed=5, jitter=0.05)
+
+
+def test_torsion_forms_match_oracle():
+    s, st = torsion_system()
+    g, o = _pair(s, st)
+    g.chcnb(); o.chcnb()
+    g.getcom(); o.getcom()
+    a, b = g.fforces(True), o.fforces(True)
+    assert relmax(g.forces(1), o.forces(1)) < FP64_TOL
+    assert abs(a.pint - b.pint) <= FP64_TOL * abs(b.pint)
+    ag, ao = g.bonded_averages(), o.bonded_averages()
+    for k in ("tr", "te", "br", "be", "ar", "ae"):
+        assert relmax(ag[k], ao[k]) < FP64_TOL, k
+    # and along three DOUBLE long steps
+    g2, o2 = _pair(s, st)
+    g2.double(3), o2.double(3)
+    (gx, *_), _ = g2.get_state()
+    (ox, *_), _ = o2.get_state()
+    assert np.abs(gx - ox).max() < 1e-9
+
+
+def test_torsion_forms_mixed_error():
+    from mdynamix_gb300.mdx import ForcePath
+    s, st = torsion_system()
+    f = {}
+    for prec in (MDX_FP64, MDX_MIXED):
+        g = ForcePath(s, precision=prec)
+        g.set_state(*st)
+        g.chcnb()
+        g.getcom()
+        g.fforces(True)
+        f[prec] = g.forces(1)
+    rms = np.sqrt(((f[MDX_MIXED] - f[MDX_FP64]) ** 2).sum() / (f[MDX_FP64] ** 2).sum())
+    assert rms < 1e-5, rms
