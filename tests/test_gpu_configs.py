@@ -111,7 +111,7 @@ def test_cfg1_nve_conserves_energy_like_fp64():
 
 # ------------------------------------------------------------ torsions --
 def torsion_db():
-    """moldb with 'C2H5OH' whose eight dihedrals cycle through ITORS 0, 1,
+    """moldb with "C2H5OH" whose twelve dihedrals cycle through ITORS 0, 1,
     5 and -1 (parameters in kJ/mol and degrees, as .mmol files give them)."""
     db = copy.deepcopy(S.load_moldb())
     forms = [
@@ -129,12 +129,12 @@ def torsion_db():
 
 def torsion_system():
     db = torsion_db()
-    spec = S.RunSpec(molecules=[("H2O", 100), ("C2H5OH", 6)], density=1.0, dt_fs=2.0,
-                     nfreq=10, rcut=7.0, rshort=5.0, alpha=2.0, fexp=9.0, ichnb=10,
+    spec = S.RunSpec(molecules=[("H2O", 100), ("CH3OH", 3), ("C2H5OH", 2)], density=1.0,
+                     dt_fs=2.0, nfreq=10, rcut=7.0, rshort=5.0, alpha=2.0, fexp=9.0, ichnb=10,
                      nvt=(298.0, 30.0), trtemp=298.0)
     s = S.System(spec, moldb=db)
     assert set(s.t_itors.tolist()) == {0, 1, 5, -1}
-    return s, S.make_configuration(s, seed=5, jitter=0.05)
+    return s, S.make_configuration(s, seed=11, jitter=0.05)
 
 
 def test_torsion_forms_match_oracle():
