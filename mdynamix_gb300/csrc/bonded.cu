@@ -69,9 +69,9 @@ __device__ __forceinline__ void vec_r(const dbl4 *pos, const BondOut &o, int a, 
                                       double by, double bz, R &x, R &y, R &z) {
   if (sizeof(R) == sizeof(float) && o.posi) {
     const int4 pa = o.posi[a], pb = o.posi[b];
-    x = (R)((float)(int)((unsigned)pa.x - (unsigned)pb.x) * o.sx);
-    y = (R)((float)(int)((unsigned)pa.y - (unsigned)pb.y) * o.sy);
-    z = (R)((float)(int)((unsigned)pa.z - (unsigned)pb.z) * o.sz);
+    x = (R)fixdiff(pa.x, pb.x, o.sx);
+    y = (R)fixdiff(pa.y, pb.y, o.sy);
+    z = (R)fixdiff(pa.z, pb.z, o.sz);
   } else if (sizeof(R) == sizeof(float)) {
     // FP64 difference rounded to FP32; the minimum-image test runs on the
     // FP32 value against 0.99 x half box (bond vectors lie far inside it)

@@ -475,18 +475,43 @@ __device__ __forceinline__ void block_add(double (&v)[NV], const Dst6 &d) {
   block_add_core<NV>(v, d.p, d.part, d.ctr);
 }
 
-// Round-to-nearest float -> 64-bit integer from FP32 and 32-bit conversions
-// only (on this GPU the 64-bit conversion instructions issue on the narrow
-// FP64 pipe).  |y| = hi * 2^32 + lo with hi = floor(|y| 2^-32); the
-// subtraction is exact because lo is made of the low mantissa bits of |y|.
-// Equal to __float2ll_rn(y) for |y| < 2^63.
+// Round-to-nearest-even float -> 64-bit integer from the bits of y with
+// integer operations only: no conversion instruction (on this GPU those
+// issue on the narrow FP64 pipe).  |y| = M 2^e with the 24-bit significand
+// M; e >= 0 shifts left, -24 <= e < 0 shifts right and rounds half to even
+// on the dropped bits, smaller e gives 0.  Equal to __float2ll_rn(y) for
+// |y| < 2^63.
 __device__ __forceinline__ long long f2ll_rn(float y) {
-  const float a = fabsf(y);
-  const float hf = floorf(a * 2.3283064365386963e-10f);
-  const unsigned hi = __float2uint_rz(hf);
-  const unsigned lo = __float2uint_rn(fmaf(-hf, 4294967296.0f, a));
-  const long long r = (long long)(((unsigned long long)hi << 32) + lo);
-  return y < 0.f ? -r : r;
+  const unsigned b = __float_as_uint(y);
+  const int e = min((int)((b >> 23) & 0xffu) - 150, 39);
+  const unsigned m = (b & 0x7fffffu) | 0x800000u;
+  unsigned long long r = 0;
+  if (e >= 0) {
+    r = (unsigned long long)m << e;
+  } else if (e >= -24) {
+    const int s = -e;
+    const unsigned q = m >> s, rem = m & ((1u << s) - 1u), half = 1u << (s - 1);
+    r = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+  }
+  return (b >> 31) ? -(long long)r : (long long)r;
+}
+
+// (float)d rounded to nearest even, from integer and FP32 operations only
+// (no I2F conversion instruction, which issues on the narrow FP64 pipe
+// here): d = hi 2^16 + lo with hi = d >> 16 (arithmetic) and lo = d & 0xffff.
+// Each half is exact as the low significand bits of a float of fixed
+// exponent (1.5 2^23 + hi, 2^23 + lo) less that float, and one FMA forms
+// hi 2^16 + lo with a single rounding.
+__device__ __forceinline__ float i2f_rn(int d) {
+  const float hi = __int_as_float(0x4b400000 + (d >> 16)) - 12582912.0f;
+  const float lo = __int_as_float(0x4b000000 | (d & 0xffff)) - 8388608.0f;
+  return fmaf(hi, 65536.0f, lo);
+}
+
+// Wrapped difference a - b of two 32-bit fixed-point coordinates as FP32,
+// times the scale s (box length / 2^32): the minimum-image vector component.
+__device__ __forceinline__ float fixdiff(int a, int b, float s) {
+  return i2f_rn((int)((unsigned)a - (unsigned)b)) * s;
 }
 
 // Low 32 bits of round-to-nearest-even(t) for |t| < 2^51: adding 1.5 x 2^52

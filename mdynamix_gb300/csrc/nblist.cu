@@ -238,9 +238,9 @@ __global__ void __launch_bounds__(BLK) k_build(
               } else {
                 float dx, dy, dz;
                 if (posi) {
-                  dx = (float)(int)((unsigned)qi.x - (unsigned)qj.x) * sxf;
-                  dy = (float)(int)((unsigned)qi.y - (unsigned)qj.y) * syf;
-                  dz = (float)(int)((unsigned)qi.z - (unsigned)qj.z) * szf;
+                  dx = fixdiff(qi.x, qj.x, sxf);
+                  dy = fixdiff(qi.y, qj.y, syf);
+                  dz = fixdiff(qi.z, qj.z, szf);
                 } else {
                   dx = pf.x - __int_as_float(qj.x);
                   dy = pf.y - __int_as_float(qj.y);

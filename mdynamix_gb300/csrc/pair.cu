@@ -244,9 +244,7 @@ __global__ void k_wir_fix(int n, const dbl4 *__restrict__ pos,
 constexpr int PAIR32_BLOCKS = 6;  // resident blocks per SM the register cap aims at
 constexpr int SPO = 4;  // threads per owner atom of the short sweep (adjacent lanes; 4: 5 % faster than 2)
 
-__device__ __forceinline__ float idiff(int a, int b, float s) {
-  return (float)(int)((unsigned)a - (unsigned)b) * s;
-}
+__device__ __forceinline__ float idiff(int a, int b, float s) { return fixdiff(a, b, s); }
 
 // Register cap for occupancy: the sweeps wait on gathered neighbour records,
 // and more resident warps hide more of that (6 blocks of 256: 40 registers;
