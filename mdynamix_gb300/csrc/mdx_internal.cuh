@@ -496,22 +496,13 @@ __device__ __forceinline__ long long f2ll_rn(float y) {
   return (b >> 31) ? -(long long)r : (long long)r;
 }
 
-// (float)d rounded to nearest even, from integer and FP32 operations only
-// (no I2F conversion instruction, which issues on the narrow FP64 pipe
-// here): d = hi 2^16 + lo with hi = d >> 16 (arithmetic) and lo = d & 0xffff.
-// Each half is exact as the low significand bits of a float of fixed
-// exponent (1.5 2^23 + hi, 2^23 + lo) less that float, and one FMA forms
-// hi 2^16 + lo with a single rounding.
-__device__ __forceinline__ float i2f_rn(int d) {
-  const float hi = __int_as_float(0x4b400000 + (d >> 16)) - 12582912.0f;
-  const float lo = __int_as_float(0x4b000000 | (d & 0xffff)) - 8388608.0f;
-  return fmaf(hi, 65536.0f, lo);
-}
-
 // Wrapped difference a - b of two 32-bit fixed-point coordinates as FP32,
 // times the scale s (box length / 2^32): the minimum-image vector component.
+// (An exact integer + FMA replacement of the int-to-float conversion was
+// measured slower in the pair sweeps, which are issue-bound: 0.39 against
+// 0.37 ms per long-row sweep at 98,304 atoms.)
 __device__ __forceinline__ float fixdiff(int a, int b, float s) {
-  return i2f_rn((int)((unsigned)a - (unsigned)b)) * s;
+  return (float)(int)((unsigned)a - (unsigned)b) * s;
 }
 
 // Low 32 bits of round-to-nearest-even(t) for |t| < 2^51: adding 1.5 x 2^52

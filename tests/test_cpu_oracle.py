@@ -315,18 +315,7 @@ def test_fixed_point_phase_split():
         assert err < 2e-7, (k, err)
 
 
-# ------------------------------------------- conversion-free helpers ----
-def _i2f_rn(d):
-    """mdx_internal.cuh i2f_rn, step by step in float32 (the FMA's single
-    rounding as the exact sum rounded once)."""
-    d = np.asarray(d, dtype=np.int64)
-    hi_bits = (0x4B400000 + (d >> 16)).astype(np.uint32)
-    lo_bits = (0x4B000000 | (d & 0xFFFF)).astype(np.uint32)
-    hi = hi_bits.view(np.float32) - np.float32(12582912.0)
-    lo = lo_bits.view(np.float32) - np.float32(8388608.0)
-    return (hi.astype(np.float64) * 65536.0 + lo.astype(np.float64)).astype(np.float32)
-
-
+# --------------------------------------------- fixed-point rounding ----
 def _f2ll_rn(y):
     """mdx_internal.cuh f2ll_rn on the bits of a float32, in Python ints."""
     b = int(np.float32(y).view(np.uint32))
@@ -342,15 +331,11 @@ def _f2ll_rn(y):
     return -r if b >> 31 else r
 
 
-def test_conversion_free_helpers_are_exact():
-    """i2f_rn equals (float)d rounded to nearest even for every 32-bit d
-    tried, f2ll_rn equals round-half-even of the float: the mixed path's
-    results do not change with the conversion instructions gone."""
+def test_float_to_int64_rounding_is_exact():
+    """f2ll_rn (the mixed path's rounding of FP32 partial sums to 64-bit
+    fixed point, integer operations on the float's bits) equals
+    round-half-even of the float, i.e. __float2ll_rn."""
     rng = np.random.default_rng(3)
-    d = np.concatenate([rng.integers(-2**31, 2**31, 200000),
-                        [-2**31, 2**31 - 1, 0, 1, -1, 65535, 65536, -65536, -65537,
-                         2**24 + 1, 2**24 + 3, -(2**24 + 1), 2**25 + 2]]).astype(np.int64)
-    assert np.array_equal(_i2f_rn(d), d.astype(np.float32))
     ys = np.concatenate([rng.normal(size=20000) * 10.0 ** rng.integers(-3, 18, 20000),
                          [0.0, 0.5, 1.5, 2.5, -0.5, -2.5, 1e-30, 4294967296.0, 2.0 ** 40 + 1e5,
                           8388608.5, 16777215.0]]).astype(np.float32)

@@ -146,8 +146,11 @@ def test_torsion_forms_match_oracle():
     assert relmax(g.forces(1), o.forces(1)) < FP64_TOL
     assert abs(a.pint - b.pint) <= FP64_TOL * abs(b.pint)
     ag, ao = g.bonded_averages(), o.bonded_averages()
-    for k in ("tr", "te", "br", "be", "ar", "ae"):
+    for k in ("te", "br", "be", "ar", "ae"):
         assert relmax(ag[k], ao[k]) < FP64_TOL, k
+    # dihedrals near 180 degrees: acos amplifies the last bits of the cosine
+    # (d acos / d co -> infinity at co = -1), so the angles agree to 1e-8
+    assert relmax(ag["tr"], ao["tr"]) < 1e-8
     # and along three DOUBLE long steps
     g2, o2 = _pair(s, st)
     g2.double(3), o2.double(3)
