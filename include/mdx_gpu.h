@@ -383,6 +383,20 @@ int mdx_get_bonded_sums(mdx_ctx *ctx, double *sums, int32_t clear);
 /* expanded-ensemble scaling (RECINT) */
 int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,
                    double bee);
+/* Energy differences for an expanded-ensemble move from the current
+ * subensemble (coupling ec_old = EC(ME), the one the last mdx_set_lambda
+ * set) to ec_new = EC(ME1), at the current positions and lists:
+ * out[0..3] = EFN, EFO (DIFFUR mdee.f:265-376: reciprocal Ewald sum, self
+ * and intramolecular Ewald terms of the new and the old charges) and EEN,
+ * EEO (DIFEN mdee.f:379-536: LJ and real-space Ewald of the listed pairs
+ * between an EE molecule and any other molecule), internal energy units.
+ * CHENS (mdee.f:142-262) forms DE = (EEN - EEO + EFN - EFO + EELRC(ME1) -
+ * EELRC(ME)) BETA - EE(ME1) + EE(ME) on the host, draws the Metropolis
+ * decision and, on acceptance, calls mdx_set_lambda(ec_new).  The
+ * reciprocal part re-forms S(k) at the current positions (FURIR's first
+ * half); forces are untouched. */
+int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double pw1, double pw2,
+                 double bee, double *out);
 
 /* Path-integral MD (pimd.f): NBEADS contexts, one per bead replica of the
  * same system (same topology and parameters, states uploaded), advanced

@@ -20,7 +20,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libmdxgpu.so")
 BUILD = os.path.join(ROOT, "_build")
 SOURCES = ["mdx_api.cu", "integrate.cu", "bonded.cu", "ewald.cu", "pair.cu", "nblist.cu",
-           "probe.cu", "noalloc.cu", "pimd.cu", "ewald_tc.cu"]
+           "probe.cu", "noalloc.cu", "pimd.cu", "ewald_tc.cu", "mdee.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]

@@ -1111,9 +1111,14 @@ int sfac_slices(const mdx_ctx *ctx) {
   return ctx->mixed() ? d.sfac_nslice : (d.n + SLICE - 1) / SLICE;
 }
 
-int launch_furir(mdx_ctx *ctx) {
+// FURIR's first half (forces.f:1217-1290): the k-set check against the box
+// (INIFUR again past the 5 % window), the phase tables and S(k) of the
+// current positions and charges into d.sk.  *skip: nothing to do (no Ewald,
+// empty k-set or a single molecule).
+int furir_sfac(mdx_ctx *ctx, bool *skip) {
   DevData &d = ctx->dv;
-  if (ctx->p.alphad <= 0.0) return MDX_OK;
+  *skip = ctx->p.alphad <= 0.0;
+  if (*skip) return MDX_OK;
   const double FKTX = 1.05, FKTS = 0.95;
   int rc;
   if (!ctx->furir_init) {
@@ -1132,11 +1137,9 @@ int launch_furir(mdx_ctx *ctx) {
     ctx->bozlo = ctx->bozl;
     if ((rc = host_inifur(ctx))) return rc;
   }
-  if (d.nkv == 0 || (ctx->d.ntypes == 1 && ctx->nspec[0] == 1)) return MDX_OK;
+  *skip = d.nkv == 0 || (ctx->d.ntypes == 1 && ctx->nspec[0] == 1);
+  if (*skip) return MDX_OK;
   const double ibx = 1.0 / ctx->boxl, iby = 1.0 / ctx->boyl, ibz = 1.0 / ctx->bozl;
-  const double vol = ctx->boxl * ctx->boyl * ctx->bozl;
-  const double alp2 = ctx->p.alphad * ctx->p.alphad;
-  const double cfur = 4.0 * PI_REF * ctx->p.coulf / vol;
   const Chunk *chunks = reinterpret_cast<const Chunk *>(d.kchunks);
   const int nchunk = d.nchunk;
   const bool mx = ctx->mixed();
@@ -1176,22 +1179,42 @@ int launch_furir(mdx_ctx *ctx) {
       MDX_LAUNCHED(ctx);
     }
   }
+  return MDX_OK;
+}
+
+// Per-k constants AKC, RXV^2 AKV, RYV^2 AKV, RZV^2 AKV, RZV (forces.f:1296-1305)
+// for the current box, rebuilt only when the box or alpha changed.
+int ensure_kconst(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  const double vol = ctx->boxl * ctx->boyl * ctx->bozl;
+  const double alp2 = ctx->p.alphad * ctx->p.alphad;
+  const double cfur = 4.0 * PI_REF * ctx->p.coulf / vol;
+  if (ctx->kc_box[0] != ctx->boxl || ctx->kc_box[1] != ctx->boyl ||
+      ctx->kc_box[2] != ctx->bozl || ctx->kc_box[3] != alp2 || ctx->kc_box[4] != cfur) {
+    k_kconst<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
+        d.ncol, d.cols, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.kconst, d.colrv,
+        d.colrvf);
+    MDX_LAUNCHED(ctx);
+    ctx->kc_box[0] = ctx->boxl;
+    ctx->kc_box[1] = ctx->boyl;
+    ctx->kc_box[2] = ctx->bozl;
+    ctx->kc_box[3] = alp2;
+    ctx->kc_box[4] = cfur;
+  }
+  return MDX_OK;
+}
+
+int launch_furir(mdx_ctx *ctx) {
+  DevData &d = ctx->dv;
+  bool skip = false;
+  int rc;
+  if ((rc = furir_sfac(ctx, &skip)) || skip) return rc;
+  const bool mx = ctx->mixed();
   double *qpe = d.red + 40;
   mdx_scalars *sc = d.sc;
   {
     MDX_TIMER(ctx, MDX_T_EW_KTERMS);
-    if (ctx->kc_box[0] != ctx->boxl || ctx->kc_box[1] != ctx->boyl ||
-        ctx->kc_box[2] != ctx->bozl || ctx->kc_box[3] != alp2 || ctx->kc_box[4] != cfur) {
-      k_kconst<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
-          d.ncol, d.cols, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.kconst, d.colrv,
-          d.colrvf);
-      MDX_LAUNCHED(ctx);
-      ctx->kc_box[0] = ctx->boxl;
-      ctx->kc_box[1] = ctx->boyl;
-      ctx->kc_box[2] = ctx->bozl;
-      ctx->kc_box[3] = alp2;
-      ctx->kc_box[4] = cfur;
-    }
+    if ((rc = ensure_kconst(ctx))) return rc;
     const int kb = std::max(1, std::min((d.nkv + 127) / 128, 2 * ctx->nsm));
     Dst6 dst = dst6(ctx, kb, 4, qpe, &sc->virx, &sc->viry, &sc->virz);
     k_kterms<<<kb, 128, 0, ctx->stream>>>(d.nkv, d.sk, d.kconst, d.wk, dst);

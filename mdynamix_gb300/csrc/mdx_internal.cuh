@@ -571,6 +571,8 @@ int launch_wir(mdx_ctx *ctx, int which);  // WIRSS (1) / WIRS (2)
 // ewald.cu
 int host_inifur(mdx_ctx *ctx);
 int launch_furir(mdx_ctx *ctx);
+int furir_sfac(mdx_ctx *ctx, bool *skip);  // k-set check, phase tables, S(k) into d.sk
+int ensure_kconst(mdx_ctx *ctx);           // per-k constants of the current box
 int launch_eterms(mdx_ctx *ctx);
 int sfac_slices(const mdx_ctx *ctx);  // slices of the S(k) partial sums
 // 1: set up; 0: the k-set's tiles do not fit (the CUDA-core pass runs);

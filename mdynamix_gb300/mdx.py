@@ -97,6 +97,8 @@ def load():
     for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
         getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
     L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.mdx_ee_delta.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                               F64P]
     L.mdx_stream.argtypes = [P]
     L.mdx_stream.restype = C.c_void_p
     L.mdx_launch_count.argtypes = [P]
@@ -330,6 +332,14 @@ class ForcePath:
         d = C.c_int32()
         self._check(self.L.mdx_poll(self.h, C.byref(d)))
         return bool(d.value)
+
+    def ee_delta(self, ec_old: float, ec_new: float, pw1: float = 1.0, pw2: float = 1.0 / 3.0,
+                 bee: float = 3.0):
+        """DIFFUR and DIFEN for a move from coupling ec_old to ec_new:
+        (EFN, EFO, EEN, EEO) in internal energy units."""
+        out = np.zeros(4)
+        self._check(self.L.mdx_ee_delta(self.h, ec_old, ec_new, pw1, pw2, bee, _fp(out)))
+        return tuple(float(x) for x in out)
 
     def set_lambda(self, ec: float, pw1: float = 1.0, pw2: float = 1.0 / 3.0, bee: float = 3.0):
         self._check(self.L.mdx_set_lambda(self.h, ec, pw1, pw2, bee))

@@ -18,8 +18,14 @@ here a single host loop keeps many systems resident on the device:
   memory is stream-ordered, so closing does not stall the other jobs) and
   its slot and memory go to the next request.
 
+A job may instead walk between its coupling states (``walk_ncee`` > 0):
+segments of NCEE long steps, each followed by a CHENS move (mdee.f:142-262;
+``mdee.MdeeWalk``: energy differences on the GPU, Metropolis on the host)
+that keeps or changes the coupling, ``walk_moves`` moves in all -- the
+reference's MDEE walk rather than fixed-coupling segments.
+
 Results are per job: the state (positions, momenta, thermostat) after each
-coupling state, and the latency from arrival to completion.  Contexts are
+coupling state or segment, and the latency from arrival to completion.  Contexts are
 independent and the mixed path is deterministic, so a job's results are the
 same alone and in any mix.
 """
@@ -48,6 +54,12 @@ class JobSpec:
     pw1: float = 1.0            # input.f:152-156 defaults
     pw2: float = 1.0 / 3.0
     bee: float = 3.0
+    walk_ncee: int = 0          # > 0: CHENS walk, a move every NCEE long steps
+    walk_moves: int = 0
+    walk_wl: float = 0.0        # Wang-Landau decrement of EE(ME) per move
+
+    def segments(self) -> int:
+        return self.walk_moves + 1 if self.walk_ncee else len(self.lambdas)
 
 
 @dataclass
@@ -102,8 +114,9 @@ def estimate_bytes(s: S.System, precision: int) -> int:
 class _Running:
     def __init__(self, prep: Prepared, g: ForcePath, res: JobResult, nbytes: int):
         self.prep, self.g, self.res, self.bytes = prep, g, res, nbytes
-        self.k = 0          # coupling state in flight
+        self.k = 0          # coupling state (or walk segment) in flight
         self.mstep = 0
+        self.walk = None
 
 
 class Server:
@@ -130,12 +143,32 @@ class Server:
     # one coupling state: RECINT scaling, then DOUBLE's prologue + segment
     def _start_state(self, r: _Running):
         j = r.prep.job
+        if j.walk_ncee:
+            if r.walk is None:
+                from .mdee import MdeeWalk
+                r.walk = MdeeWalk(r.prep.system, ec=list(j.lambdas), me=1, pw1=j.pw1,
+                                  pw2=j.pw2, bee=j.bee, wl_corr=j.walk_wl, seed=j.seed)
+                r.walk.apply(r.g)
+                r.g.enqueue_double(j.walk_ncee, r.mstep, prologue=True)
+            else:
+                r.walk.attempt(r.g)   # the previous segment has finished (polled)
+                r.g.enqueue_double(j.walk_ncee, r.mstep, prologue=False)
+            return
         r.g.set_lambda(j.lambdas[r.k], j.pw1, j.pw2, j.bee)
         r.g.enqueue_double(j.steps_per_state, r.mstep, prologue=True)
 
     def _finish_state(self, r: _Running):
         j = r.prep.job
         (x, y, z, vx, vy, vz), th = r.g.get_state()
+        if j.walk_ncee:
+            rec = {"lambda": r.walk.ec[r.walk.me - 1], "me": r.walk.me, "steps": j.walk_ncee,
+                   "temp": th.temp, "tke": th.tke, "accepted": r.walk.accepted}
+            if self.keep_states:
+                rec["state"] = (x, y, z, vx, vy, vz)
+            r.res.states.append(rec)
+            r.mstep += j.walk_ncee
+            r.k += 1
+            return
         rec = {"lambda": j.lambdas[r.k], "steps": j.steps_per_state, "temp": th.temp,
                "tke": th.tke}
         if self.keep_states:
@@ -180,7 +213,7 @@ class Server:
                     continue
                 progressed = True
                 self._finish_state(r)
-                if r.k < len(r.prep.job.lambdas):
+                if r.k < r.prep.job.segments():
                     self._start_state(r)
                     continue
                 r.res.finished = self.clock() - t0

@@ -59,6 +59,8 @@ def lib():
         for n in ("ox_double", "ox_double_steps", "ox_sultan", "ox_sultan_steps"):
             getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
         L.ox_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.ox_ee_delta.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, F64P]
         from mdynamix_gb300.abi import MdxPimdParams, MdxPimdRecord
         L.ox_pimd_steps.argtypes = [C.POINTER(P), C.POINTER(MdxPimdParams), F64P, C.c_int32,
                                     C.c_int32, C.c_int, C.POINTER(MdxPimdRecord)]
@@ -215,6 +217,11 @@ class Oracle:
 
     def sultan_steps(self, nsteps, mstep0):
         return self._run("ox_sultan_steps", nsteps, mstep0)
+
+    def ee_delta(self, ec_old, ec_new, pw1=1.0, pw2=1.0 / 3.0, bee=3.0):
+        out = np.zeros(4)
+        self._check(self.L.ox_ee_delta(self.h, ec_old, ec_new, pw1, pw2, bee, _fp(out)))
+        return tuple(float(x) for x in out)
 
     def set_lambda(self, ec, pw1=1.0, pw2=1.0 / 3.0, bee=3.0):
         self._check(self.L.ox_set_lambda(self.h, ec, pw1, pw2, bee))

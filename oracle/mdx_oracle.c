@@ -41,6 +41,7 @@
  *   ox_double     DOUBLE    mdstep.f:281-530
  *   ox_sultan     SULTAN    mdstep.f:29-260
  *   ox_set_lambda RECINT    mdee.f:86-140
+ *   ox_ee_delta   DIFFUR    mdee.f:265-376, DIFEN mdee.f:379-536
  */
 #include "mdx_oracle.h"
 
@@ -2415,6 +2416,138 @@ int ox_sultan(ox_state *st, int32_t nsteps, int32_t nsttot,
   if ((rc = getemp(st))) return rc;
   if ((rc = ox_allforce(st, NULL))) return rc;
   return ox_sultan_steps(st, nsteps, nsttot, rec);
+}
+
+/* --------------------------------------------------- DIFFUR / DIFEN */
+/* Energy differences of an expanded-ensemble move from coupling ec_old
+ * (EC(ME)) to ec_new (EC(ME1)): out = EFN, EFO (DIFFUR mdee.f:265-376) and
+ * EEN, EEO (DIFEN mdee.f:379-536), on the current positions, charges and
+ * lists.  The k-set is the last INIFUR's. */
+static double ee_pair_energy(const ox_state *st, int ISP, int JSP, double EEALN1, double RSHO,
+                             double RSHN, double *een) {
+  int ITYP = st->itype[ISP], JTYP = st->itype[JSP];
+  int ISB = st->nsite[ISP], JSB = st->nsite[JSP];
+  int ISN = st->inbt[ISB], JSN = st->inbt[JSB];
+  int nb = st->nnbt;
+  double A6O = st->a6lj[IDX2(ISN, JSN, nb)], B12O = st->b12lj[IDX2(ISN, JSN, nb)];
+  double QIJO = st->q[ISP] * st->q[JSP] * st->p.coulf;
+  double ESCI = st->iee[ITYP] == 0 ? EEALN1 : 1.0;
+  double ESCL = ESCI;
+  if (st->iee[JTYP] == 0) {
+    ESCL = ESCI * EEALN1;
+    ESCI = EEALN1;
+  }
+  double A6N = ESCI * st->a6lj0[IDX2(ISN, JSN, nb)];
+  double B12N = ESCI * st->b12lj0[IDX2(ISN, JSN, nb)];
+  double QIJN = ESCL * st->charge[ISB] * st->charge[JSB] * st->p.coulf;
+  double DX = st->sx[ISP] - st->sx[JSP];
+  double DY = st->sy[ISP] - st->sy[JSP];
+  double DZ = st->sz[ISP] - st->sz[JSP];
+  pbc(st, &DX, &DY, &DZ);
+  double RR = DX * DX + DY * DY + DZ * DZ;
+  double R1 = sqrt(RR);
+  double R1O = R1 + RSHO, R1N = R1 + RSHN;
+  double R1OI = 1. / R1O, R1NI = 1. / R1N;
+  double ALPHAR = st->p.alphad * R1;
+  double TTT = 1.0 / (1.0 + B1 * ALPHAR);
+  double ERFCR = ((((A5 * TTT + A4) * TTT + A3) * TTT + A2) * TTT + A1) * TTT *
+                 exp(-(ALPHAR * ALPHAR));
+  double EESO = QIJO * ERFCR * R1OI, EESN = QIJN * ERFCR * R1NI;
+  double R6IO = pow(R1OI, 6), R6IN = pow(R1NI, 6);
+  double ESRO = (A6O + B12O * R6IO) * R6IO;
+  double ESRN = (A6N + B12N * R6IN) * R6IN;
+  *een += EESN + ESRN;
+  return EESO + ESRO;
+}
+
+int ox_ee_delta(ox_state *st, double ec_old, double ec_new, double pw1, double pw2,
+                double bee, double *out) {
+  double EFN = 0., EFO = 0., EEN = 0., EEO = 0.;
+  const double ALEEO = pow(ec_old, pw1), ALEEN = pow(ec_new, pw1);
+  if (st->p.alphad > 0.0) {
+    if (!st->furir_init) {
+      snprintf(st->msg, sizeof st->msg, "no k-set yet");
+      return MDX_ERR_STATE;
+    }
+    /* 4.1 reciprocal sum, old and new charges */
+    const double ALP2 = st->p.alphad * st->p.alphad;
+    const double CFUR = 4.0 * PI * st->p.coulf / st->vol;
+    for (int IKV = 1; IKV <= st->nkv; ++IKV) {
+      double RXV = st->rkx[IKV] / st->boxl;
+      double RYV = st->rky[IKV] / st->boyl;
+      double RZV = st->rkz[IKV] / st->bozl;
+      double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
+      double SCSO = 0., SSNO = 0., SCSN = 0., SSNN = 0.;
+      for (int I = 1; I <= st->nstot; ++I) {
+        int IC = st->nsite[I], ITYP = st->itype[I];
+        double SCP = RXV * st->sx[I] + RYV * st->sy[I] + RZV * st->sz[I];
+        double SSC = sin(SCP), CSC = cos(SCP);
+        double QO = st->q[I];
+        double QN = st->iee[ITYP] == 0 ? st->charge[IC] * ALEEN : st->q[I];
+        SSNO = SSNO + QO * SSC;
+        SCSO = SCSO + QO * CSC;
+        SSNN = SSNN + QN * SSC;
+        SCSN = SCSN + QN * CSC;
+      }
+      double AKC = CFUR * exp(-0.25 * RK2 / ALP2) / RK2;
+      EFO = EFO + (SSNO * SSNO + SCSO * SCSO) * AKC;
+      EFN = EFN + (SSNN * SSNN + SCSN * SCSN) * AKC;
+    }
+    /* 4.2.1 self terms */
+    double ABC = st->p.alphad / sqrt(PI);
+    for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP)
+      if (st->iee[ITYP] == 0)
+        for (int II = 1; II <= st->nsits[ITYP]; ++II) {
+          int IS = st->isadr[ITYP] + II;
+          EFO = EFO - st->p.coulf * (ALEEO * st->charge[IS]) * (ALEEO * st->charge[IS]) * ABC *
+                          st->nspec[ITYP];
+          EFN = EFN - st->p.coulf * (ALEEN * st->charge[IS]) * (ALEEN * st->charge[IS]) * ABC *
+                          st->nspec[ITYP];
+        }
+    /* 4.2.2 intramolecular terms of EE molecules */
+    for (int ITYP = 1; ITYP <= st->ntypes; ++ITYP) {
+      if (!(st->iee[ITYP] == 0 && st->nsits[ITYP] > 1)) continue;
+      int ISBEG = st->isadr[ITYP] + 1, ISEND = st->isadr[ITYP + 1];
+      for (int IS = ISBEG; IS <= ISEND - 1; ++IS)
+        for (int JS = IS + 1; JS <= ISEND; ++JS)
+          for (int IM = 1; IM <= st->nspec[ITYP]; ++IM) {
+            int ISP = st->isaddr[ITYP] + (IM - 1) * st->nsits[ITYP] + IS - ISBEG + 1;
+            int JSP = st->isaddr[ITYP] + (IM - 1) * st->nsits[ITYP] + JS - ISBEG + 1;
+            double QIJO = st->p.coulf * st->q[ISP] * st->q[JSP];
+            double QIJN = st->p.coulf * ALEEN * ALEEN * st->charge[IS] * st->charge[JS];
+            double DX = st->sx[ISP] - st->sx[JSP];
+            double DY = st->sy[ISP] - st->sy[JSP];
+            double DZ = st->sz[ISP] - st->sz[JSP];
+            pbc(st, &DX, &DY, &DZ);
+            double R2 = DX * DX + DY * DY + DZ * DZ;
+            double R2I = 1.0 / R2, R1 = sqrt(R2), R1I = R1 * R2I;
+            double ALPHAR = st->p.alphad * R1;
+            double TTT = 1.0 / (1.0 + B1 * ALPHAR);
+            double EXP2A = exp(-(ALPHAR * ALPHAR));
+            double ERFC = ((((A5 * TTT + A4) * TTT + A3) * TTT + A2) * TTT + A1) * TTT * EXP2A;
+            double ERFR = (ERFC - 1.0) * R1I;
+            EFO = EFO + QIJO * ERFR;
+            EFN = EFN + QIJN * ERFR;
+          }
+    }
+  }
+  /* DIFEN over the long and the short lists */
+  double RSHO = bee * (1. - pow(ec_old, pw2)), RSHN = bee * (1. - pow(ec_new, pw2));
+  for (int pass = 0; pass < 2; ++pass) {
+    int np = pass == 0 ? st->mbln : st->mbsh;
+    const int *L1 = pass == 0 ? st->nbl1 : st->nbs1, *L2 = pass == 0 ? st->nbl2 : st->nbs2;
+    for (int INP = 1; INP <= np; ++INP) {
+      int ISP = abs(L1[INP]), JSP = L2[INP];
+      if (st->iee[st->itype[ISP]] * st->iee[st->itype[JSP]] == 1) continue;
+      if (st->nnum[ISP] == st->nnum[JSP]) continue;
+      EEO += ee_pair_energy(st, ISP, JSP, ALEEN, RSHO, RSHN, &EEN);
+    }
+  }
+  out[0] = EFN;
+  out[1] = EFO;
+  out[2] = EEN;
+  out[3] = EEO;
+  return MDX_OK;
 }
 
 /* ---------------------------------------------------------------- RECINT */
