@@ -339,9 +339,13 @@ def pimd_leg(args):
         pp = PimdPath(s, states, precision=prec)
         pp.run(args.pimd_warmup)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        stream = torch.cuda.ExternalStream(pp.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         recs = pp.steps(args.pimd_steps, args.pimd_warmup)
-        dt = time.perf_counter() - t0
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) * 1e-3
         atoms = s.nstot * s.spec.nbeads
         out[name] = {"atom_steps_per_s": atoms * args.pimd_steps / dt,
                      "ms_per_step": dt / args.pimd_steps * 1e3,
@@ -363,7 +367,7 @@ def pimd_leg(args):
     out["sample"] = (f"256 SPC-FW waters x 32 beads (24576 bead atoms), Rc 9 A, alpha 0.35/A, "
                      f"dt 0.25 fs, PI_thermo 300 K / 5 fs / chains of 4; {args.pimd_warmup} "
                      f"steps with the preparation, then {args.pimd_steps} timed long steps "
-                     f"(host wall clock around synchronised calls)")
+                     f"(CUDA events on the bead ensemble's stream)")
     for pp in list(paths.values()) + [g64, g32]:
         pp.close()
     return out
@@ -392,9 +396,13 @@ def bilayer_leg(args):
         f[name] = g.forces(3)
         g.sultan(args.bilayer_warmup)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        g.sultan_steps(args.bilayer_steps, args.bilayer_warmup)
-        dt = time.perf_counter() - t0
+        stream = torch.cuda.ExternalStream(g.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.sultan_steps(args.bilayer_steps, args.bilayer_warmup, records=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) * 1e-3
         out[name] = {"atom_steps_per_s": s.nstot * args.bilayer_steps / dt,
                      "ms_per_step": dt / args.bilayer_steps * 1e3}
         g.close()
@@ -411,7 +419,7 @@ def bilayer_leg(args):
     out["sample"] = (f"{s.nspec[0]} DMPC + {s.nspec[1]} SPC ({s.nstot} atoms), box "
                      f"{s.boxl:.0f}x{s.boyl:.0f}x{s.bozl:.0f} A, Rc 12, Ewald 3.12/9.72, SHAKE, "
                      f"anisotropic NPT 303 K / 1 bar, dt 2 fs; {args.bilayer_warmup} + "
-                     f"{args.bilayer_steps} timed SULTAN steps (host clock, synchronised)")
+                     f"{args.bilayer_steps} timed SULTAN steps (CUDA events on the stream)")
     return out
 
 
@@ -563,6 +571,11 @@ def extra_legs(args):
     import torch  # noqa: F401  (CUDA context first)
     if "cfg1" in args.leg:
         print(json.dumps({"leg": "cfg1_nve", **_r(cfg1_nve_leg(args))}), flush=True)
+    if "serving" in args.leg:
+        a = argparse.Namespace(**vars(args))
+        a.serve_jobs, a.serve_steps, a.serve_slots = 256, 500, 256
+        out = serving_leg(a)
+        print(json.dumps({"leg": "serving_256x5x500", **_r(out)}), flush=True)
     if "sample" in args.leg:
         from tests.nacl776 import reference_averages, sample_run_averages
         from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
@@ -638,7 +651,7 @@ def main():
     ap.add_argument("--bilayer-warmup", type=int, default=3)
     ap.add_argument("--nve-steps", type=int, default=500, help="NVE leg long steps (0 = off)")
     ap.add_argument("--nve-equil", type=int, default=100)
-    ap.add_argument("--leg", nargs="*", default=[], choices=["cfg1", "sample"],
+    ap.add_argument("--leg", nargs="*", default=[], choices=["cfg1", "sample", "serving"],
                     help="evidence runs only (their own JSON lines, no headline line)")
     ap.add_argument("--cfg1-steps", type=int, default=1000)
     ap.add_argument("--cfg1-equil", type=int, default=1000)

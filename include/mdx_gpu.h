@@ -437,6 +437,8 @@ int mdx_pimd_close(mdx_pimd *pi);
 int mdx_pimd_run(mdx_pimd *pi, int32_t nsteps, int32_t nsttot, mdx_pimd_record *rec);
 /* nsteps more long steps without the preparation. */
 int mdx_pimd_steps(mdx_pimd *pi, int32_t nsteps, int32_t mstep0, mdx_pimd_record *rec);
+/* The stream the bead ensemble's steps run on (for timing with events). */
+void *mdx_pimd_stream(mdx_pimd *pi);
 /* THERMO(NSTOT, JNH), column-major, in and out. */
 int mdx_pimd_get_thermo(mdx_pimd *pi, double *thermo);
 int mdx_pimd_set_thermo(mdx_pimd *pi, const double *thermo);

@@ -310,15 +310,16 @@ int ensure_records(mdx_ctx *ctx, int n) {
   return MDX_OK;
 }
 
-// One DOUBLE long step replayed from its captured graph (captured on first
-// use; four variants: list rebuild or not x records or not).
-int graph_step(mdx_ctx *ctx, int mstep, bool rec) {
+// One DOUBLE or SULTAN long step replayed from its captured graph
+// (captured on first use; four variants each: list rebuild or not x
+// records or not).
+int graph_step(mdx_ctx *ctx, int mstep, bool rec, bool dbl) {
   const bool list = list_update_every_step(ctx) || mstep % ctx->p.ichnb == 0;
-  const int g = (list ? 1 : 0) + (rec ? 2 : 0);
+  const int g = (list ? 1 : 0) + (rec ? 2 : 0) + (dbl ? 0 : 4);
   if (!ctx->gexec[g]) {
     const int64_t l0 = ctx->launches;
     MDX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = double_step(ctx, mstep, rec ? -1 : -2);
+    int rc = dbl ? double_step(ctx, mstep, rec ? -1 : -2) : sultan_step(ctx, mstep, rec ? -1 : -2);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (rc) {
@@ -352,9 +353,10 @@ int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
     return MDX_ERR_STATE;
   }
   if (rec) RC(ensure_records(ctx, nsteps));
-  // CUDA-graph replay of whole long steps: DOUBLE at constant volume has a
-  // fixed launch sequence, with or without the mid-step list rebuild.
-  const bool graphs = dbl && !ctx->p.lnpt && !ctx->timing && ctx->use_graphs;
+  // CUDA-graph replay of whole long steps: DOUBLE and SULTAN at constant
+  // volume have a fixed launch sequence, with or without the list rebuild
+  // (SULTAN's first step, with its temperature rescale, runs eagerly).
+  const bool graphs = !ctx->p.lnpt && !ctx->timing && ctx->use_graphs;
   if (graphs && rec) {
     int c0[2] = {0, mstep0 + 1};
     MDX_CUDA(cudaMemcpyAsync(ctx->dv.shake_iter + 16, c0, sizeof c0, cudaMemcpyHostToDevice,
@@ -363,12 +365,13 @@ int run_steps(mdx_ctx *ctx, bool dbl, int32_t nsteps, int32_t mstep0,
   }
   for (int s = 1; s <= nsteps; ++s) {
     const int mstep = mstep0 + s;
-    if (graphs) {
-      RC(graph_step(ctx, mstep, rec != nullptr));
+    if (graphs && (dbl || mstep != 1)) {
+      RC(graph_step(ctx, mstep, rec != nullptr, dbl));
     } else if (dbl) {
       RC(double_step(ctx, mstep, rec ? s - 1 : -2));
     } else {
-      RC(sultan_step(ctx, mstep, rec ? s - 1 : -2));
+      // with graphs on, the records' slot counter on the device is in use
+      RC(sultan_step(ctx, mstep, rec ? (graphs ? -1 : s - 1) : -2));
     }
   }
   RC(check_err(ctx));
@@ -1227,7 +1230,7 @@ int mdx_double_enqueue(mdx_ctx *ctx, int32_t nsteps, int32_t mstep0, int32_t pro
     ctx->err = "neighbour lists not built (enqueue with the prologue first)";
     return MDX_ERR_STATE;
   }
-  for (int s = 1; s <= nsteps; ++s) RC(graph_step(ctx, mstep0 + s, false));
+  for (int s = 1; s <= nsteps; ++s) RC(graph_step(ctx, mstep0 + s, false, true));
   return MDX_OK;
 }
 

@@ -281,9 +281,9 @@ struct mdx_ctx {
   CellGrid grid{};
   double list_rl2 = 0;  // squared list radius used by the last build
   FixScale fix{};
-  // CUDA graphs of one long step: [rebuild?] + 2 * [records?]
-  cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
-  int64_t glaunches[4] = {0, 0, 0, 0};
+  // CUDA graphs of one long step: [rebuild?] + 2 * [records?] + 4 * [SULTAN?]
+  cudaGraphExec_t gexec[8] = {};
+  int64_t glaunches[8] = {};
   bool use_graphs = true;
   bool averaging = false;  // mdx_set_averaging: LAVER forces + statistics every long step
   void drop_graphs() {

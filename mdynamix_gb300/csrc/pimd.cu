@@ -465,6 +465,8 @@ int mdx_pimd_steps(mdx_pimd *pi, int32_t nsteps, int32_t mstep0, mdx_pimd_record
   return run(pi, nsteps, mstep0, false, rec);
 }
 
+void *mdx_pimd_stream(mdx_pimd *pi) { return pi ? (void *)pi->stream : nullptr; }
+
 int mdx_pimd_get_thermo(mdx_pimd *pi, double *thermo) {
   if (!pi || !thermo) return MDX_ERR_ARG;
   if (cudaStreamSynchronize(pi->stream) != cudaSuccess ||

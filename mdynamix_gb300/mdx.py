@@ -114,6 +114,8 @@ def load():
     L.mdx_pimd_run.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxPimdRecord)]
     L.mdx_pimd_steps.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxPimdRecord)]
     L.mdx_pimd_get_thermo.argtypes = [P, F64P]
+    L.mdx_pimd_stream.argtypes = [P]
+    L.mdx_pimd_stream.restype = P
     L.mdx_pimd_set_thermo.argtypes = [P, F64P]
     _lib = L
     return L
@@ -378,6 +380,10 @@ class PimdPath:
             raise MdxError(rc, "PIMD: " + " / ".join(
                 self.L.mdx_last_error(b.h).decode() for b in self.beads[:1]))
         return [recs[i] for i in range(nsteps)]
+
+    @property
+    def stream(self) -> int:
+        return self.L.mdx_pimd_stream(self.h)
 
     def run(self, nsteps: int, nsttot: int = 0):
         return self._run("mdx_pimd_run", nsteps, nsttot)

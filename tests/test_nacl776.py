@@ -215,3 +215,34 @@ def test_sample_run_averages_agree_with_reference(precision):
     for k, (v, e) in ours.items():
         rv, re_ = ref[k]
         assert abs(v - rv) <= 4.0 * math.hypot(e, re_) + 1e-12, (k, v, e, rv, re_)
+
+
+@pytest.mark.gpu
+def test_snapshot_dumper_writes_device_state(tmp_path):
+    """Restart file and XMOL frames written from device snapshots while the
+    step loop goes on: the restart file read back equals the state after the
+    last block, each frame the positions at its request."""
+    from mdynamix_gb300.mdx import ForcePath
+    s, st, th = load_sample()
+    g = ForcePath(s)
+    g.set_state(*st, thermo=th)
+    g.double(0)
+    tw = restart.TraceWriter(s, str(tmp_path / "NaCl"), itrek=2, ltrek=100)
+    d = restart.SnapshotDumper(g, trace=tw)
+    frames = []
+    for b in range(3):
+        g.double_steps(5, 5 * b, records=False)
+        d.request("trace", time_s=(b + 1) * 5 * 2e-15)
+        frames.append(g.get_state()[0])
+    path = str(tmp_path / "NaCl.dmp")
+    d.request("restart", path=path, nstep=15, nsttot=10015, tim=2.003e-11)
+    d.close()
+    (x, y, z, vx, vy, vz), th_end = g.get_state()
+    r = restart.read_dmp(path)
+    assert np.array_equal(r.sx, x) and np.array_equal(r.vz, vz)
+    assert r.nsttot == 10015 and r.sc == th_end.sc
+    lines = open(tw.files[0]).read().splitlines()
+    assert len(lines) == 3 * 778
+    for b in range(3):
+        first = lines[b * 778 + 2].split()
+        assert abs(float(first[1]) - frames[b][0][0]) < 6e-4
