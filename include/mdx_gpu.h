@@ -134,6 +134,12 @@ typedef struct {
   const int32_t *itors, *nmul;
   const double *ft, *rt, *ft1, *ft2, *ft3, *ft4, *ft5;
   const int32_t *iti, *jtj, *ktk, *ltl, *ituk;
+  /* per bond record (length nrbb): 1 if SHEJK holds it as a constraint.
+   * NULL gives the reference's rule, every record with ID != 2
+   * (mdstep.f:1135); a flag per record allows e.g. bonds to hydrogen only,
+   * which the reference cannot express (its ID = 2 also drops the pair
+   * from the exclusions, setup.f:787). */
+  const int32_t *lcon;
 } mdx_topo;
 
 /* Run parameters (/SIZES/, /ENERGY/, /NVTNPT/, main.f:380-450, 729-812). */

@@ -49,6 +49,7 @@ _TOPO_FIELDS = [
     ("itors", I32P), ("nmul", I32P), ("ft", F64P), ("rt", F64P), ("ft1", F64P), ("ft2", F64P),
     ("ft3", F64P), ("ft4", F64P), ("ft5", F64P),
     ("iti", I32P), ("jtj", I32P), ("ktk", I32P), ("ltl", I32P), ("ituk", I32P),
+    ("lcon", I32P),
 ]
 
 
@@ -230,6 +231,7 @@ def pack(s: System, precision: int = MDX_FP64, cap_short: int = 0, cap_long: int
         setattr(t, name, p(src, "f"))
     t.iti = p(s.iti, "i"); t.jtj = p(s.jtj, "i"); t.ktk = p(s.ktk, "i"); t.ltl = p(s.ltl, "i")
     t.ituk = p(s.ituk, "i")
+    t.lcon = p(s.b_lcon, "i")
     par = params_of(s)
     return Packed(dims, t, par, keep)
 

@@ -373,13 +373,14 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
 
 // SULTAN 1.3.1-1.3.2.2 (mdstep.f:89-113): OX = SX, V += TSTEP F,
 // SX += TSTEP V MASSDI.
+// save != 0: the new positions also go to fx/fy/fz (SHEJK's copy of the
+// unconstrained positions, mdstep.f:1128-1132; the forces are not needed
+// again before the next ALLFORCE).
 __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
-                           double tstep, const double *__restrict__ fx,
-                           const double *__restrict__ fy,
-                           const double *__restrict__ fz,
+                           double tstep, double *fx, double *fy, double *fz,
                            const double *__restrict__ massdi, double *vx,
                            double *vy, double *vz, dbl4 *pos, double *ox,
-                           double *oy, double *oz) {
+                           double *oy, double *oz, int save) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (!mv.lmove[ainfo[i].x]) return;
@@ -398,6 +399,11 @@ __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
   p.y = p.y + tstep * y * mi;
   p.z = p.z + tstep * z * mi;
   pos[i] = p;
+  if (save) {
+    fx[i] = p.x;
+    fy[i] = p.y;
+    fz[i] = p.z;
+  }
 }
 
 // ------------------------------------------------------------------ GETEMP
@@ -883,94 +889,120 @@ struct ShakeConst {
   double tol2, tstep;
 };
 
-__global__ void k_shejk(int nop, const int *__restrict__ mol_first,
-                        const int *__restrict__ mol_nat,
-                        const int *__restrict__ mol_type, MoveConst mv,
-                        ShakeConst sk, const int *__restrict__ bib,
-                        const int *__restrict__ bjb, const int *__restrict__ bid,
-                        const double *__restrict__ brb,
-                        const double *__restrict__ massdi, dbl4 *pos,
-                        double *vx, double *vy, double *vz,
-                        const double *__restrict__ ox,
-                        const double *__restrict__ oy,
-                        const double *__restrict__ oz, double *fx, double *fy,
-                        double *fz, double bx, double by, double bz,
-                        mdx_thermo *th, int *err, Dst6 vdst) {
+// SHEJK (mdstep.f:1105-1283) over independent constraint clusters.  The
+// reference sweeps all constraints of a molecule in record order until no
+// bond needs adjusting; constraints that share no atom (e.g. the CH2 and CH3
+// groups of a lipid under SHAKE on bonds to hydrogen) never see each
+// other's updates, so each cluster runs the same sweeps on its own and ends
+// in the same positions bit for bit; the molecule's iteration count is the
+// largest of its clusters'.  Thread per (molecule, cluster); the positions
+// before SHAKE are in fx/fy/fz (written by the leap-frog pass).
+__global__ void k_shake_cluster(int nitem, const int2 *__restrict__ items,
+                                const int2 *__restrict__ clusters,
+                                const int *__restrict__ recs,
+                                const int *__restrict__ mol_first,
+                                const int *__restrict__ mol_type, MoveConst mv,
+                                ShakeConst sk, const int *__restrict__ bib,
+                                const int *__restrict__ bjb,
+                                const double *__restrict__ brb,
+                                const double *__restrict__ massdi, dbl4 *pos,
+                                const double *__restrict__ ox,
+                                const double *__restrict__ oy,
+                                const double *__restrict__ oz, double bx, double by,
+                                double bz, mdx_thermo *th, int *__restrict__ mfail) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nitem) return;
+  const int2 item = items[it];
+  const int m = item.x, t = mol_type[m];
+  if (!(mv.lmove[t] && sk.ishejk[t] > 0)) return;
+  const int2 cl = clusters[item.y];  // (first record slot, records)
+  const int *rr = recs + cl.x;
+  const int f = mol_first[m];
+  // MOVING / MOVED flags as bit masks over the molecule's atoms (<= 128)
+  unsigned long long moving[2] = {0, 0}, moved[2] = {0, 0};
+  for (int q = 0; q < cl.y; ++q) {
+    const int b = rr[q];
+    const int li = bib[b] - 1, lj = bjb[b] - 1;
+    moved[li >> 6] |= 1ull << (li & 63);
+    moved[lj >> 6] |= 1ull << (lj & 63);
+  }
+  int ITER = 0;
+  bool DONE = false;
+  for (;;) {
+    if (ITER > sk.maxit || DONE) break;
+    DONE = true;
+    for (int q = 0; q < cl.y; ++q) {
+      const int b = rr[q];
+      const int li = bib[b] - 1, lj = bjb[b] - 1;
+      const bool mvi = (moved[li >> 6] >> (li & 63)) & 1ull;
+      const bool mvj = (moved[lj >> 6] >> (lj & 63)) & 1ull;
+      if (!(mvi || mvj)) continue;
+      const int I = f + li, J = f + lj;
+      const double rbb = brb[b];
+      const double BNDSQ = rbb * rbb;
+      dbl4 pi = pos[I], pj = pos[J];
+      double BXN = pi.x - pj.x, BYN = pi.y - pj.y, BZN = pi.z - pj.z;
+      pbc_rect(BXN, BYN, BZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      const double BSQ = BXN * BXN + BYN * BYN + BZN * BZN;
+      const double DIFFSQ = BNDSQ - BSQ;
+      if (fabs(DIFFSQ) > (BNDSQ * sk.tol2)) {
+        double DXN = ox[I] - ox[J], DYN = oy[I] - oy[J], DZN = oz[I] - oz[J];
+        pbc_rect(DXN, DYN, DZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+        const double VDOT = BXN * DXN + BYN * DYN + BZN * DZN;
+        const double RMA = massdi[I], RMB = massdi[J];
+        const double GAB = DIFFSQ / (2.0 * (RMA + RMB) * VDOT);
+        DXN = DXN * GAB;
+        DYN = DYN * GAB;
+        DZN = DZN * GAB;
+        pi.x = pi.x + RMA * DXN;
+        pi.y = pi.y + RMA * DYN;
+        pi.z = pi.z + RMA * DZN;
+        pj.x = pj.x - RMB * DXN;
+        pj.y = pj.y - RMB * DYN;
+        pj.z = pj.z - RMB * DZN;
+        pos[I] = pi;
+        pos[J] = pj;
+        moving[li >> 6] |= 1ull << (li & 63);
+        moving[lj >> 6] |= 1ull << (lj & 63);
+        DONE = false;
+      }
+    }
+    // MOVED := MOVING restricted to constrained atoms; MOVING := 0
+    moved[0] = moving[0];
+    moved[1] = moving[1];
+    moving[0] = moving[1] = 0;
+    ITER = ITER + 1;
+  }
+  atomicMax(&th->shake_iter_max, ITER);
+  if (ITER >= sk.maxit) mfail[m] = 1;
+}
+
+// SHEJK's end per molecule (mdstep.f:1240-1275): velocity correction and
+// constraint virial from the displacement SHAKE made, the count of
+// molecules past MAXIT.  Thread per molecule (the virial sums in molecule
+// order).
+__global__ void k_shake_finish(int nop, const int *__restrict__ mol_first,
+                               const int *__restrict__ mol_nat,
+                               const int *__restrict__ mol_type, MoveConst mv,
+                               ShakeConst sk, const double *__restrict__ massdi,
+                               const dbl4 *__restrict__ pos, double *vx, double *vy,
+                               double *vz, const double *__restrict__ ox,
+                               const double *__restrict__ oy,
+                               const double *__restrict__ oz, const double *__restrict__ fx,
+                               const double *__restrict__ fy,
+                               const double *__restrict__ fz, mdx_thermo *th, int *err,
+                               int *__restrict__ mfail, Dst6 vdst) {
   double vir[3] = {0, 0, 0};
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  int iter_out = 0;
   if (m < nop) {
     const int t = mol_type[m];
-    const int nrbs = sk.nrb[t];
-    if (mv.lmove[t] && sk.ishejk[t] > 0 && nrbs > 0) {
-      const int f = mol_first[m], na = mol_nat[m];
-      const int nb0 = sk.iadb[t] - 1;  // 0-based first bond record
-      for (int k = 0; k < na; ++k) {
-        const dbl4 p = pos[f + k];
-        fx[f + k] = p.x;
-        fy[f + k] = p.y;
-        fz[f + k] = p.z;
-      }
-      // MOVING / MOVED flags as bit masks over the molecule's atoms (<= 128)
-      unsigned long long moving[2] = {0, 0}, moved[2] = {0, 0};
-      for (int b = 0; b < nrbs; ++b) {
-        if (bid[nb0 + b] == 2) continue;
-        const int li = bib[nb0 + b] - 1, lj = bjb[nb0 + b] - 1;
-        moved[li >> 6] |= 1ull << (li & 63);
-        moved[lj >> 6] |= 1ull << (lj & 63);
-      }
-      int ITER = 0;
-      bool DONE = false;
-      for (;;) {
-        if (ITER > sk.maxit || DONE) break;
-        DONE = true;
-        for (int b = 0; b < nrbs; ++b) {
-          if (bid[nb0 + b] == 2) continue;
-          const int li = bib[nb0 + b] - 1, lj = bjb[nb0 + b] - 1;
-          const bool mvi = (moved[li >> 6] >> (li & 63)) & 1ull;
-          const bool mvj = (moved[lj >> 6] >> (lj & 63)) & 1ull;
-          if (!(mvi || mvj)) continue;
-          const int I = f + li, J = f + lj;
-          const double rbb = brb[nb0 + b];
-          const double BNDSQ = rbb * rbb;
-          dbl4 pi = pos[I], pj = pos[J];
-          double BXN = pi.x - pj.x, BYN = pi.y - pj.y, BZN = pi.z - pj.z;
-          pbc_rect(BXN, BYN, BZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
-          const double BSQ = BXN * BXN + BYN * BYN + BZN * BZN;
-          const double DIFFSQ = BNDSQ - BSQ;
-          if (fabs(DIFFSQ) > (BNDSQ * sk.tol2)) {
-            double DXN = ox[I] - ox[J], DYN = oy[I] - oy[J], DZN = oz[I] - oz[J];
-            pbc_rect(DXN, DYN, DZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
-            const double VDOT = BXN * DXN + BYN * DYN + BZN * DZN;
-            const double RMA = massdi[I], RMB = massdi[J];
-            const double GAB = DIFFSQ / (2.0 * (RMA + RMB) * VDOT);
-            DXN = DXN * GAB;
-            DYN = DYN * GAB;
-            DZN = DZN * GAB;
-            pi.x = pi.x + RMA * DXN;
-            pi.y = pi.y + RMA * DYN;
-            pi.z = pi.z + RMA * DZN;
-            pj.x = pj.x - RMB * DXN;
-            pj.y = pj.y - RMB * DYN;
-            pj.z = pj.z - RMB * DZN;
-            pos[I] = pi;
-            pos[J] = pj;
-            moving[li >> 6] |= 1ull << (li & 63);
-            moving[lj >> 6] |= 1ull << (lj & 63);
-            DONE = false;
-          }
-        }
-        // MOVED := MOVING restricted to constrained atoms; MOVING := 0
-        moved[0] = moving[0];
-        moved[1] = moving[1];
-        moving[0] = moving[1] = 0;
-        ITER = ITER + 1;
-      }
-      iter_out = ITER;
-      if (ITER >= sk.maxit) {
+    if (mv.lmove[t] && sk.ishejk[t] > 0 && sk.nrb[t] > 0) {
+      if (mfail[m]) {
+        mfail[m] = 0;
         atomicAdd(&th->shake_fail, 1);
         atomicOr(err, DERR_SHAKE);
       }
+      const int f = mol_first[m], na = mol_nat[m];
       const double TS = sk.tstep;
       for (int k = 0; k < na; ++k) {
         const int I = f + k;
@@ -988,7 +1020,6 @@ __global__ void k_shejk(int nop, const int *__restrict__ mol_first,
     }
   }
   block_add<3>(vir, vdst);
-  if (iter_out > 0) atomicMax(&th->shake_iter_max, iter_out);
 }
 
 __global__ void k_shake_prep(mdx_thermo *th) {
@@ -1496,7 +1527,7 @@ int launch_leapfrog_shake(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   k_leapfrog<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.ainfo, move_const(ctx), ctx->p.tstep, d.fx, d.fy, d.fz, d.massdi, d.vx,
-      d.vy, d.vz, d.pos, d.ox, d.oy, d.oz);
+      d.vy, d.vz, d.pos, d.ox, d.oy, d.oz, ctx->p.lshejk ? 1 : 0);
   MDX_LAUNCHED(ctx);
   k_shake_prep<<<1, 1, 0, ctx->stream>>>(d.th);
   MDX_LAUNCHED(ctx);
@@ -1510,10 +1541,16 @@ int launch_leapfrog_shake(mdx_ctx *ctx) {
     sk.maxit = ctx->p.maxit > 0 ? ctx->p.maxit : 2000;
     sk.tol2 = ctx->p.toler * ctx->p.toler;
     sk.tstep = ctx->p.tstep;
-    k_shejk<<<(d.nop + 63) / 64, 64, 0, ctx->stream>>>(
-        d.nop, d.mol_first, d.mol_nat, d.mol_type, move_const(ctx), sk, d.bib, d.bjb,
-        d.bid, d.brb, d.massdi, d.pos, d.vx, d.vy, d.vz, d.ox, d.oy, d.oz, d.fx, d.fy,
-        d.fz, ctx->boxl, ctx->boyl, ctx->bozl, d.th, d.err,
+    if (d.shk_nitem > 0) {
+      k_shake_cluster<<<(d.shk_nitem + 63) / 64, 64, 0, ctx->stream>>>(
+          d.shk_nitem, d.shk_item, d.shk_cl, d.shk_rec, d.mol_first, d.mol_type,
+          move_const(ctx), sk, d.bib, d.bjb, d.brb, d.massdi, d.pos, d.ox, d.oy, d.oz,
+          ctx->boxl, ctx->boyl, ctx->bozl, d.th, d.shk_mfail);
+      MDX_LAUNCHED(ctx);
+    }
+    k_shake_finish<<<(d.nop + 63) / 64, 64, 0, ctx->stream>>>(
+        d.nop, d.mol_first, d.mol_nat, d.mol_type, move_const(ctx), sk, d.massdi, d.pos,
+        d.vx, d.vy, d.vz, d.ox, d.oy, d.oz, d.fx, d.fy, d.fz, d.th, d.err, d.shk_mfail,
         dst6(ctx, (d.nop + 63) / 64, 3, &d.th->viran[0], &d.th->viran[1], &d.th->viran[2]));
     MDX_LAUNCHED(ctx);
   }

@@ -530,7 +530,8 @@ int mdx_close(mdx_ctx *ctx) {
                   d.bid, d.brb, d.ibi, d.ara, d.iai, d.titors, d.tft, d.iti, d.br,
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.kconst, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
-                  d.red_part, d.red_ctr, d.sk_part, d.snap, d.avsum};
+                  d.red_part, d.red_ctr, d.sk_part, d.snap, d.avsum, d.shk_item,
+                  d.shk_cl, d.shk_rec, d.shk_mfail};
   if (ctx->stream) {
     for (void *p : ptrs) ctx_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
@@ -658,6 +659,68 @@ static int split_bonded(mdx_ctx *ctx, const mdx_topo *t) {
   if (d.ntpl) {
     RC(dmalloc(ctx, &d.moltpl, use.size()));
     RC(upload(ctx, d.moltpl, use.data(), use.size()));
+  }
+  return MDX_OK;
+}
+
+// SHEJK work items.  A molecule type's constraints (records flagged in
+// lcon, or with ID != 2) fall into clusters connected through shared atoms;
+// updates in one cluster never touch another's atoms, so each cluster can
+// run the reference's sweeps on its own (see k_shake_cluster).  One item
+// per (molecule, cluster); clusters list their records in record order.
+static int shake_clusters(mdx_ctx *ctx, const mdx_topo *t) {
+  DevData &d = ctx->dv;
+  std::vector<int> rec;
+  std::vector<int2> cl, items;
+  for (int k = 0; k < ctx->d.ntypes; ++k) {
+    const int nb = t->nrb[k], ns = t->nsits[k], nb0 = t->iadb[k] - 1;
+    if (nb <= 0 || ns > 128) continue;
+    std::vector<int> root(ns);
+    for (int a = 0; a < ns; ++a) root[a] = a;
+    auto find = [&](int a) {
+      while (root[a] != a) a = root[a] = root[root[a]];
+      return a;
+    };
+    auto con = [&](int b) { return t->lcon ? t->lcon[nb0 + b] != 0 : t->id[nb0 + b] != 2; };
+    for (int b = 0; b < nb; ++b)
+      if (con(b)) {
+        const int x = find(t->ib[nb0 + b] - 1), y = find(t->jb[nb0 + b] - 1);
+        if (x != y) root[std::max(x, y)] = std::min(x, y);
+      }
+    std::vector<int> cid(ns, -1);
+    const int c0 = (int)cl.size();
+    for (int b = 0; b < nb; ++b) {
+      if (!con(b)) continue;
+      const int r = find(t->ib[nb0 + b] - 1);
+      if (cid[r] < 0) {
+        cid[r] = (int)cl.size();
+        cl.push_back(make_int2(0, 0));
+      }
+    }
+    // records of each cluster, in record order
+    for (int c = c0; c < (int)cl.size(); ++c) {
+      cl[c].x = (int)rec.size();
+      for (int b = 0; b < nb; ++b)
+        if (con(b) && cid[find(t->ib[nb0 + b] - 1)] == c) rec.push_back(nb0 + b);
+      cl[c].y = (int)rec.size() - cl[c].x;
+    }
+    for (int mm = 0; mm < t->nspec[k]; ++mm)
+      for (int c = c0; c < (int)cl.size(); ++c) items.push_back(make_int2(t->iaddr[k] + mm, c));
+  }
+  ctx_free(ctx, d.shk_item);
+  ctx_free(ctx, d.shk_cl);
+  ctx_free(ctx, d.shk_rec);
+  d.shk_item = d.shk_cl = nullptr;
+  d.shk_rec = nullptr;
+  d.shk_nitem = (int)items.size();
+  if (!d.shk_mfail) RC(dmalloc(ctx, &d.shk_mfail, (size_t)d.nop));
+  if (d.shk_nitem) {
+    RC(dmalloc(ctx, &d.shk_item, items.size()));
+    RC(dmalloc(ctx, &d.shk_cl, cl.size()));
+    RC(dmalloc(ctx, &d.shk_rec, rec.size()));
+    RC(upload(ctx, d.shk_item, items.data(), items.size()));
+    RC(upload(ctx, d.shk_cl, cl.data(), cl.size()));
+    RC(upload(ctx, d.shk_rec, rec.data(), rec.size()));
   }
   return MDX_OK;
 }
@@ -853,6 +916,7 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
     RC(upload(ctx, d.ituk, f.data(), d.nrrt));
   }
   RC(upload(ctx, d.nspec_d, t->nspec, nt));
+  RC(shake_clusters(ctx, t));
   if (ctx->mixed()) RC(upload_site_table(ctx));
   ctx->have_topo = true;
   return MDX_OK;

@@ -247,6 +247,12 @@ struct DevData {
   double2 *sk_part;    // per-slice S(k) partials (deterministic slice sum)
   double *snap;        // mdx_snapshot: positions unpacked for the copy out (3n)
   double *avsum;       // mdx_set_averaging: running sums of the bonded statistics
+  // SHEJK work: (molecule, cluster) items; per cluster (first slot, count)
+  // into shk_rec, the cluster's constraint records in record order; a
+  // failure flag per molecule
+  int2 *shk_item, *shk_cl;
+  int *shk_rec, *shk_mfail;
+  int shk_nitem;
   size_t sk_part_cap;
 };
 

@@ -339,6 +339,7 @@ class RunSpec:
     lmove: Optional[List[int]] = None
     icr: int = 0                                   # combination rule
     cut_forces: Optional[float] = None             # Cut_forces FTSCL
+    shake_hbonds: bool = False                     # constrain bonds to H only (not in the reference)
     rskin: float = 0.0                             # list skin (build mode)
     iee_type: Optional[int] = None                 # EE_type (1-based)
     nbeads: int = 1                                # PIMD NBEADS (bead masses MASS/NBEADS)
@@ -374,7 +375,19 @@ class System:
         self.nrb = np.array([len(t["bonds"]) for t in self.types], dtype=np.int32)
         self.nra = np.array([len(t["angles"]) for t in self.types], dtype=np.int32)
         self.nrt = np.array([len(t["tors"]) for t in self.types], dtype=np.int32)
-        self.nrcon = np.array([sum(1 for b in t["bonds"] if b["id"] != 2) for t in self.types],
+        # SHAKE constraints per bond record: the reference's ID != 2
+        # (mdstep.f:1135), or with shake_hbonds only those of them that
+        # bind a hydrogen (a site lighter than 1.5 amu)
+        def con(t, b):
+            if b["id"] == 2:
+                return 0
+            if not spec.shake_hbonds:
+                return 1
+            m = [t["sites"][b["i"] - 1]["mass"], t["sites"][b["j"] - 1]["mass"]]
+            return int(min(m) < 1.5)
+        self.b_lcon = np.array([con(t, b) for t in self.types for b in t["bonds"]],
+                               dtype=np.int32)
+        self.nrcon = np.array([sum(con(t, b) for b in t["bonds"]) for t in self.types],
                               dtype=np.int32)
         self.iadb = (np.concatenate([[0], np.cumsum(self.nrb)[:-1]]) + 1).astype(np.int32)
         self.iada = (np.concatenate([[0], np.cumsum(self.nra)[:-1]]) + 1).astype(np.int32)
@@ -1055,18 +1068,20 @@ def pimd_water(nwater: int = 256, nbeads: int = 32) -> RunSpec:
 
 
 def dmpc_bilayer(nside: int = 7, nwater: int = 3655, box=(62.0, 62.0, 76.0),
-                 rcut: float = 12.0, alpha: float = 3.12, fexp: float = 9.72) -> RunSpec:
+                 rcut: float = 12.0, alpha: float = 3.12, fexp: float = 9.72,
+                 shake_hbonds: bool = False) -> RunSpec:
     """DMPC bilayer (2 x nside^2 lipids, tails along z) in SPC water.  The
     all-atom, fully extended dmpc.mmol conformation needs 76 A of box height
     to leave room for 3655 waters at 1.0 g/cm3, and packs without overlaps
     (every intermolecular distance >= 1.5 A) at 7 x 7 lipids per leaflet in
     62 x 62 A; 8 x 8 would start with atoms 0.9 A apart.  Then
     anisotropic Nose-Hoover NPT at 303 K / 1 bar, SHAKE on every constrained
-    bond (the reference's per-type rule: ID != 2), dt 2 fs, Ewald A, B."""
+    bond (the reference's per-type rule: ID != 2; with shake_hbonds only
+    the bonds to hydrogen), dt 2 fs, Ewald A, B."""
     return RunSpec(molecules=[("dmpc", 2 * nside * nside), ("SPC", nwater)], box=tuple(box),
                    dt_fs=2.0, nfreq=1, rcut=rcut, rshort=5.0, alpha=alpha, fexp=fexp,
                    ichnb=10, shake=True, toler=1e-5, nvt=(303.0, 50.0), npt=(1.0, 1000.0),
-                   anisotropic=True, trtemp=303.0)
+                   anisotropic=True, trtemp=303.0, shake_hbonds=shake_hbonds)
 
 
 def bilayer_configuration(s: System, seed: int = 1, clearance: float = 2.3,

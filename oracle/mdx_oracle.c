@@ -78,7 +78,7 @@ struct ox_state {
   double *a6lj, *b12lj, *a6lj0, *b12lj0, *a6_14, *b12_14;
   int mdxt[NT + 2][NT + 2];
   int *nnbb, *inbb;
-  int *ib, *jb, *id;
+  int *ib, *jb, *id, *lcon; /* lcon: SHAKE constraint per bond record */
   double *rb, *fb, *db, *ro;
   int *ibi, *jbj, *ibuk;
   double *ra, *fa;
@@ -289,6 +289,8 @@ int ox_open(const mdx_dims *d, const mdx_topo *t, const mdx_params *p,
   st->ib = copy_i(t->ib, st->nrbb);
   st->jb = copy_i(t->jb, st->nrbb);
   st->id = copy_i(t->id, st->nrbb);
+  st->lcon = (int *)xcalloc((size_t)st->nrbb + 1, sizeof(int));
+  for (int m = 1; m <= st->nrbb; ++m) st->lcon[m] = t->lcon ? t->lcon[m - 1] : st->id[m] != 2;
   st->rb = copy_d(t->rb, st->nrbb);
   st->fb = copy_d(t->fb, st->nrbb);
   st->db = copy_d(t->db, st->nrbb);
@@ -369,7 +371,7 @@ void ox_close(ox_state *st) {
   void *ptrs[] = {st->itype, st->nnum, st->nsite, st->itm, st->massdi, st->q,
                   st->charge, st->mass, st->inbt, st->a6lj, st->b12lj,
                   st->a6lj0, st->b12lj0, st->a6_14, st->b12_14, st->nnbb,
-                  st->inbb, st->ib, st->jb, st->id, st->rb, st->fb, st->db,
+                  st->inbb, st->ib, st->jb, st->id, st->lcon, st->rb, st->fb, st->db,
                   st->ro, st->ibi, st->jbj, st->ibuk, st->ra, st->fa, st->iai,
                   st->jaj, st->kak, st->iauk, st->itors, st->nmul, st->ft,
                   st->rt, st->ft1, st->ft2, st->ft3, st->ft4, st->ft5, st->iti,
@@ -2199,7 +2201,7 @@ static void shejk(ox_state *st, int IMOL, unsigned char *moving,
     st->fz[I] = st->sz[I];
   }
   for (int M = NBBEG; M <= NBEND; ++M)
-    if (st->id[M] != 2) {
+    if (st->lcon[M]) {
       int LI = st->ib[M] + ISHF, LJ = st->jb[M] + ISHF;
       moving[LI] = 0; moved[LI] = 1;
       moving[LJ] = 0; moved[LJ] = 1;
@@ -2210,7 +2212,7 @@ static void shejk(ox_state *st, int IMOL, unsigned char *moving,
     if (DONE) break;
     DONE = 1;
     for (int M = NBBEG; M <= NBEND; ++M) {
-      if (st->id[M] == 2) continue;
+      if (!st->lcon[M]) continue;
       int I = st->ib[M] + ISHF, J = st->jb[M] + ISHF;
       if (!(moved[I] || moved[J])) continue;
       double BNDSQ = st->rb[M] * st->rb[M];
@@ -2243,12 +2245,12 @@ static void shejk(ox_state *st, int IMOL, unsigned char *moving,
       }
     }
     for (int M = NBBEG; M <= NBEND; ++M)
-      if (st->id[M] != 2) {
+      if (st->lcon[M]) {
         moved[st->ib[M] + ISHF] = 0;
         moved[st->jb[M] + ISHF] = 0;
       }
     for (int M = NBBEG; M <= NBEND; ++M)
-      if (st->id[M] != 2) {
+      if (st->lcon[M]) {
         int I = st->ib[M] + ISHF, J = st->jb[M] + ISHF;
         if (moving[I]) moved[I] = 1;
         if (moving[J]) moved[J] = 1;

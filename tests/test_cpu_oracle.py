@@ -341,3 +341,19 @@ def test_float_to_int64_rounding_is_exact():
                           8388608.5, 16777215.0]]).astype(np.float32)
     for y in ys:
         assert _f2ll_rn(y) == int(np.rint(np.float64(y))), y
+
+
+def test_shake_on_bonds_to_hydrogen_counts_constraints():
+    """SHAKE on bonds to hydrogen: fewer constraints per lipid than the
+    reference's ID != 2 rule, and the degrees of freedom grow by the
+    difference (main.f:297-350 counts NRCON per type)."""
+    from mdynamix_gb300 import system as S
+    kw = dict(nside=1, nwater=100, box=(20.0, 20.0, 60.0), rcut=9.0, alpha=2.8, fexp=9.0)
+    a = S.System(S.dmpc_bilayer(**kw))
+    b = S.System(S.dmpc_bilayer(shake_hbonds=True, **kw))
+    assert b.nrcon[0] < a.nrcon[0] and b.nrcon[1] == a.nrcon[1] == 3
+    assert b.fnst - a.fnst == (a.nrcon[0] - b.nrcon[0]) * a.nspec[0]
+    lip = a.types[0]
+    heavy = [i for i, st in enumerate(lip["sites"]) if st["mass"] > 1.5]
+    cons = [bd for bd, f in zip(lip["bonds"], b.b_lcon[:a.nrb[0]]) if f]
+    assert all(bd["i"] - 1 not in heavy or bd["j"] - 1 not in heavy for bd in cons)

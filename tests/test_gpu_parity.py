@@ -335,3 +335,37 @@ def test_graph_replay_matches_eager(monkeypatch):
     assert np.array_equal(runs[0][0], runs[1][0])
     assert runs[0][1] == runs[1][1]
     assert runs[0][2] == list(range(1, 13))
+
+
+def _bilayer_patch_hbonds():
+    from mdynamix_gb300 import system as S
+    spec = S.dmpc_bilayer(nside=1, nwater=500, box=(20.0, 20.0, 60.0), rcut=9.0,
+                          alpha=2.8, fexp=9.0, shake_hbonds=True)
+    s = S.System(spec)
+    return s, S.bilayer_configuration(s, seed=2)
+
+
+@pytest.mark.parametrize("npt", [False, True])
+def test_sultan_shake_hbonds_bilayer_fp64(npt):
+    """SHAKE on the bonds to hydrogen only (a per-record constraint flag the
+    reference cannot express; its ID != 2 rule constrains every bond of a
+    type): the lipid's constraints fall into small independent clusters,
+    each iterated on its own on the GPU; positions, SHAKE iteration counts
+    and the NPT box follow the oracle's molecule-wide sweeps."""
+    s, st = _bilayer_patch_hbonds()
+    if not npt:
+        import dataclasses
+        from mdynamix_gb300 import system as S
+        s = S.System(dataclasses.replace(s.spec, npt=None, anisotropic=False))
+    g = ForcePath(s)
+    o = oracle.Oracle(s)
+    g.set_state(*st)
+    o.set_state(*st)
+    rg, ro = g.sultan(3), o.sultan(3)
+    (gx, gy, gz, *_), tg = g.get_state()
+    (ox, oy, oz, *_), to = o.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
+    assert [r.shake_iter for r in rg] == [r.shake_iter for r in ro]
+    for a, b in zip(rg, ro):
+        for n in ("temp", "pels1", "boxl", "tryck"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-8 * max(abs(getattr(b, n)), 1e-12), n
