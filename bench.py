@@ -382,7 +382,7 @@ def bilayer_leg(args):
     from mdynamix_gb300 import system as S
     from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
     from mdynamix_gb300.mdx import ForcePath
-    s = S.System(S.dmpc_bilayer())
+    s = S.System(S.dmpc_bilayer(shake_hbonds=True))
     st = S.bilayer_configuration(s, seed=1)
     out = {}
     sc = {}
@@ -417,7 +417,8 @@ def bilayer_leg(args):
     out["mixed_vs_fp64_rel_err"] = err
     out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
     out["sample"] = (f"{s.nspec[0]} DMPC + {s.nspec[1]} SPC ({s.nstot} atoms), box "
-                     f"{s.boxl:.0f}x{s.boyl:.0f}x{s.bozl:.0f} A, Rc 12, Ewald 3.12/9.72, SHAKE, "
+                     f"{s.boxl:.0f}x{s.boyl:.0f}x{s.bozl:.0f} A, Rc 12, Ewald 3.12/9.72, SHAKE on "
+                     f"bonds to H, "
                      f"anisotropic NPT 303 K / 1 bar, dt 2 fs; {args.bilayer_warmup} + "
                      f"{args.bilayer_steps} timed SULTAN steps (CUDA events on the stream)")
     return out
