@@ -241,11 +241,13 @@ def params_of(s: System) -> MdxParams:
     par = MdxParams()
     par.boxl, par.boyl, par.bozl = s.boxl, s.boyl, s.bozl
     par.icell = 0
-    par.lmnbl = 0
+    par.lmnbl = int(s.lmnbl)
+    par.rff = s.rff
+    par.rff2 = s.rff2
     par.coulf = s.coulf
     par.alphad = s.alphad
     par.fexp = s.fexp
-    par.rcut = sp.rcut
+    par.rcut = s.rcutt
     par.rshort = sp.rshort
     par.rskin = sp.rskin
     par.tstep = s.tstep

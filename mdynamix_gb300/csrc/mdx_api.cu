@@ -941,6 +941,10 @@ int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
     ctx->err = "Verlet skin: not with the reaction-field molecular cutoff";
     return MDX_ERR_UNSUPPORTED;
   }
+  if (p->lmnbl && 2.0 * p->rcut > std::min(p->boxl, std::min(p->boyl, p->bozl)) + 1e-9) {
+    ctx->err = "reaction field: RCUT must be within half the box (main.f:745-749)";
+    return MDX_ERR_ARG;
+  }
   if (p->rskin > 0.0 &&
       p->rcut + p->rskin > 0.5 * std::min(p->boxl, std::min(p->boyl, p->bozl))) {
     ctx->err = "Verlet skin: RCUT + skin must stay within half the box";
@@ -998,6 +1002,43 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
   RC(upload(ctx, d.vx, vx, n));
   RC(upload(ctx, d.vy, vy, n));
   RC(upload(ctx, d.vz, vz, n));
+  {
+    // reach of small molecules (at most 5 sites) from their centres of mass,
+    // for the search radius of the reaction field's molecular cutoff list
+    double reach = 0.0;
+    const double hb[3] = {0.5 * ctx->boxl, 0.5 * ctx->boyl, 0.5 * ctx->bozl};
+    const double bl[3] = {ctx->boxl, ctx->boyl, ctx->bozl};
+    for (size_t i = 0; i < n;) {
+      const int m = ctx->h_nnum[i];
+      size_t e = i;
+      while (e < n && ctx->h_nnum[e] == m) ++e;
+      if (e - i <= 5) {
+        double c[3] = {0, 0, 0}, mt = 0.0;
+        const double *xs[3] = {sx, sy, sz};
+        for (size_t a = i; a < e; ++a) {
+          const double w = ctx->h_mass[ctx->h_nsite[a] - 1];
+          mt += w;
+          for (int k = 0; k < 3; ++k) {
+            double dxk = xs[k][a] - xs[k][i];
+            if (std::fabs(dxk) > hb[k]) dxk -= std::copysign(bl[k], dxk);
+            c[k] += w * dxk;
+          }
+        }
+        for (size_t a = i; a < e; ++a) {
+          double r2 = 0.0;
+          for (int k = 0; k < 3; ++k) {
+            double dxk = xs[k][a] - xs[k][i];
+            if (std::fabs(dxk) > hb[k]) dxk -= std::copysign(bl[k], dxk);
+            dxk -= c[k] / mt;
+            r2 += dxk * dxk;
+          }
+          reach = std::max(reach, std::sqrt(r2));
+        }
+      }
+      i = e;
+    }
+    ctx->mol_reach = reach + 1.0;
+  }
   mdx_thermo h{};
   if (th) h = *th;
   if (h.boxl > 0) {
@@ -1151,10 +1192,6 @@ int mdx_inifur(mdx_ctx *ctx, int32_t *nkv) {
 int mdx_chcnb(mdx_ctx *ctx, int32_t *mbsh, int32_t *mbln) {
   if (!ctx) return MDX_ERR_ARG;
   RC(require(ctx, true, true, true));
-  if (ctx->p.lmnbl) {
-    ctx->err = "reaction-field molecular cutoff list is not built";
-    return MDX_ERR_UNSUPPORTED;
-  }
   RC(launch_build_lists(ctx));
   RC(check_err(ctx));
   int c[2];

@@ -286,6 +286,9 @@ struct mdx_ctx {
   double spei = 0, speei[MDX_NT]{};
   CellGrid grid{};
   double list_rl2 = 0;  // squared list radius used by the last build
+  // reaction field: largest distance of an atom of a small molecule from the
+  // molecule's centre of mass (+ 1 A for flexing), set at the state upload
+  double mol_reach = 0;
   FixScale fix{};
   // CUDA graphs of one long step: [rebuild?] + 2 * [records?] + 4 * [SULTAN?]
   cudaGraphExec_t gexec[8] = {};

@@ -147,15 +147,43 @@ __device__ __forceinline__ bool owns(int i, int j) {
   return (((i - j) & 1) == 0) ? (j < i) : (j > i);
 }
 
+// Reaction field (LMNBL): small molecules (at most MMOL = 5 sites) enter
+// the lists whole, by the distance of their centres of mass
+// (forces.f:1882-1936).
+struct MolCut {
+  int lmnbl;
+  int nsits[MDX_NT];
+  const double *X, *Y, *Z;  // centres of mass of the last GETCOM
+  const int4 *ainfo;
+};
+
 // Exact classification (forces.f:1938-1981): 0 none, 1 short, 2 long,
 // 3 short 1-4, -1 excluded bonded pair.
 __device__ __forceinline__ int classify_exact(
     int i, int j, bool same_mol, const dbl4 &pi, const dbl4 &pj,
     const BoxD &b, double short2, double rl2, const int *__restrict__ nnbb,
-    const int *__restrict__ inbb, int nbdmax) {
+    const int *__restrict__ inbb, int nbdmax, const MolCut &mc) {
   double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
   pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
   double rr2 = dx * dx + dy * dy + dz * dz;
+  double rrm = rr2;
+  if (mc.lmnbl) {
+    constexpr int MMOL = 5;
+    const int4 ai = mc.ainfo[i], aj = mc.ainfo[j];
+    const int nmi = mc.nsits[ai.x], nmj = mc.nsits[aj.x];
+    if (!(nmi > MMOL && nmj > MMOL)) {
+      double ex, ey, ez;
+      if (nmi > MMOL) {
+        ex = pi.x - mc.X[aj.y]; ey = pi.y - mc.Y[aj.y]; ez = pi.z - mc.Z[aj.y];
+      } else if (nmj > MMOL) {
+        ex = mc.X[ai.y] - pj.x; ey = mc.Y[ai.y] - pj.y; ez = mc.Z[ai.y] - pj.z;
+      } else {
+        ex = mc.X[ai.y] - mc.X[aj.y]; ey = mc.Y[ai.y] - mc.Y[aj.y]; ez = mc.Z[ai.y] - mc.Z[aj.y];
+      }
+      pbc_rect(ex, ey, ez, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+      rrm = ex * ex + ey * ey + ez * ez;
+    }
+  }
   if (same_mol && rr2 <= 64.0) {
     int nb = nnbb[i];
     const int jf = j + 1;
@@ -165,8 +193,8 @@ __device__ __forceinline__ int classify_exact(
       if (v == -jf) return 3;
     }
   }
-  if (rr2 <= short2) return 1;
-  if (rr2 <= rl2) return 2;
+  if (rrm <= short2) return 1;
+  if (rrm <= rl2) return 2;
   return 0;
 }
 
@@ -181,7 +209,7 @@ __global__ void __launch_bounds__(BLK) k_build(
     int cap_l, int *__restrict__ ns_cnt, int *__restrict__ nl_cnt,
     int *__restrict__ ns_idx, int *__restrict__ nl_idx, int *__restrict__ err,
     int *__restrict__ need, int full, const int4 *__restrict__ posi, float sxf, float syf,
-    float szf, dbl4 *__restrict__ pos_ref, const int *__restrict__ gate) {
+    float szf, dbl4 *__restrict__ pos_ref, const int *__restrict__ gate, MolCut mc) {
   // posi (mixed path): the prefilter takes the wrapped differences of the
   // fixed-point positions and the molecule from their packed word, one
   // 16-byte gather per candidate
@@ -232,9 +260,9 @@ __global__ void __launch_bounds__(BLK) k_build(
               const bool same =
                   posi ? ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS)
                        : qj.w == imol;
-              if (same) {
-                kind = classify_exact(i, j, true, pi, pos[j], b, short2, rl2,
-                                      nnbb, inbb, nbdmax);
+              if (same || mc.lmnbl) {  // the molecular cutoff: exact test only
+                kind = classify_exact(i, j, same, pi, pos[j], b, short2, rl2,
+                                      nnbb, inbb, nbdmax, mc);
               } else {
                 float dx, dy, dz;
                 if (posi) {
@@ -254,7 +282,7 @@ __global__ void __launch_bounds__(BLK) k_build(
                   kind = d2 < s2f_lo ? 1 : 2;
                 } else {
                   kind = classify_exact(i, j, false, pi, pos[j], b, short2, rl2,
-                                        nnbb, inbb, nbdmax);
+                                        nnbb, inbb, nbdmax, mc);
                 }
               }
             }
@@ -386,6 +414,17 @@ int launch_cell_refresh(mdx_ctx *ctx) {
   return MDX_OK;
 }
 
+static MolCut mol_cut(const mdx_ctx *ctx) {
+  MolCut m{};
+  m.lmnbl = ctx->p.lmnbl;
+  for (int t = 0; t < MDX_NT; ++t) m.nsits[t] = ctx->nsits[t];
+  m.X = ctx->dv.X;
+  m.Y = ctx->dv.Y;
+  m.Z = ctx->dv.Z;
+  m.ainfo = ctx->dv.ainfo;
+  return m;
+}
+
 // CHCNB.  gate != nullptr (skin mode, inside a step): every kernel of the
 // build runs only if the displacement check of this step opened the gate, so
 // a captured step graph holds the build whether or not it happens.
@@ -395,15 +434,18 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
   // CHCNB puts every pair within SHORT in the short list even when SHORT
   // exceeds the cutoff (forces.f:1964-1976), so the search radius covers both
   const double rl = std::max(ctx->p.rcut + ctx->p.rskin, ctx->p.rshort);
+  // the molecular cutoff lists atoms up to twice a small molecule's reach
+  // from its centre of mass beyond the cutoff
+  const double rsearch = ctx->p.lmnbl ? rl + 2.0 * ctx->mol_reach : rl;
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
          0.5 * ctx->bozl};
   CellGrid g;
   // cells at least rl / CELL_REACH wide, stencil +-CELL_REACH cells (a
   // (2 R + 1)^3 stencil of thinner cells tests fewer far candidates than
   // 27 cells of width rl); below 2 R + 1 cells a dimension is scanned whole
-  g.nx = std::max(1, (int)std::floor(CELL_REACH * ctx->boxl / rl));
-  g.ny = std::max(1, (int)std::floor(CELL_REACH * ctx->boyl / rl));
-  g.nz = std::max(1, (int)std::floor(CELL_REACH * ctx->bozl / rl));
+  g.nx = std::max(1, (int)std::floor(CELL_REACH * ctx->boxl / rsearch));
+  g.ny = std::max(1, (int)std::floor(CELL_REACH * ctx->boyl / rsearch));
+  g.nz = std::max(1, (int)std::floor(CELL_REACH * ctx->bozl / rsearch));
   g.cx = ctx->boxl / g.nx;
   g.cy = ctx->boyl / g.ny;
   g.cz = ctx->bozl / g.nz;
@@ -464,7 +506,7 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
       d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
       ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,
       (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),
-      (float)(ctx->bozl / 4294967296.0), pos_ref, gate);
+      (float)(ctx->bozl / 4294967296.0), pos_ref, gate, mol_cut(ctx));
   MDX_LAUNCHED(ctx);
   k_zero_gated<<<1, 32, 0, ctx->stream>>>(&d.sc->mbsh, 2, gate);
   MDX_LAUNCHED(ctx);

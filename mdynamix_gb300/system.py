@@ -449,6 +449,8 @@ class System:
             self.boxl, self.boyl, self.bozl = (float(x) for x in sp.box)
         self.vol = self.boxl * self.boyl * self.bozl
         self.rcutt = sp.rcut
+        if sp.alpha <= 0.0:  # reaction field: a spherical cutoff within L/2 (main.f:745-749)
+            self.rcutt = min(self.rcutt, 0.5 * min(self.boxl, self.boyl, self.bozl))
         self.rssq = self.rcutt ** 2
         dt = sp.dt_fs * 1.0e-15
         self.unitl = 1.0e-10
@@ -789,6 +791,21 @@ class System:
         cl = min(self.boxl, self.boyl, self.bozl)
         self.alphad = ewald_alpha(sp.alpha, self.rcutt, cl) if sp.alpha > 0 else 0.0
         self.fexp = sp.fexp
+        # Electrostatics with ALPHA <= 0: reaction field of dielectric
+        # constant DIEL = -ALPHA, FEXP the Debye length (0: no salt), with the
+        # molecular cutoff list (LMNBL); DIEL <= 1 is a plain cutoff
+        # (main.f:740-793)
+        self.lmnbl = sp.alpha <= 0.0
+        self.rff = self.rff2 = 0.0
+        if self.lmnbl:
+            diel = -sp.alpha
+            rdeb = sp.fexp
+            rck = self.rcutt / rdeb if rdeb > 1e-3 else 0.0
+            self.rff2 = -((2.0 * (diel - 1.0) * (rck + 1.0) + diel * rck ** 2)
+                          / (((2.0 * diel + 1.0) * (rck + 1.0) + diel * rck ** 2) * self.rcutt ** 3))
+            self.rff = (1.0 / (diel * (1.0 + rck)) - 1.0) / self.rcutt
+            if diel <= 1.0000001:
+                self.rff = self.rff2 = 0.0
         self.lnvt = sp.nvt is not None
         self.lnpt = sp.npt is not None
         self.dqt = (self.unitt * 1e15 / sp.nvt[1]) ** 2 if self.lnvt else 0.0

@@ -5,10 +5,17 @@
  * TEST INFRASTRUCTURE ONLY: tests, the smoke check and the benchmark's
  * CPU-baseline leg call it; the product never does.
  *
- * Parity unpinned against the reference binary (Fortran; no compiler on
- * either machine).  Pinned by invariants in the tests: momentum conservation
- * of pair and bonded forces, finite-difference forces, alpha independence of
- * the Ewald total, NVE energy conservation.
+ * Pinned to the reference's own example run (sample/4nacl.in, its restart
+ * file sample/NaCl.dmp and its output sample/4nacl.out, committed as
+ * fixtures under tests/golden/): the setup numbers the output prints (box
+ * from the density, INIFUR's k-vector count, degrees of freedom, LJ tail
+ * corrections per molecule-type pair) agree to the printed digits, and a
+ * continuation of that run from its restart file reproduces its averages
+ * within stated bars.  The reference binary itself cannot run here
+ * (Fortran; no compiler on either machine), so no bit-for-bit comparison
+ * with it exists.  Invariants in the tests pin the rest: momentum
+ * conservation of pair and bonded forces, finite-difference forces, alpha
+ * independence of the Ewald total, NVE energy conservation.
  *
  * Each routine follows the Fortran statement by statement, in double
  * precision, with the same operation order.  Arrays are indexed 1..N as in
@@ -509,7 +516,24 @@ static inline int chcnb_pair(const ox_state *st, int I, int J, int imol) {
   double DZ = st->sz[I] - st->sz[J];
   pbc(st, &DX, &DY, &DZ);
   double RR2 = DX * DX + DY * DY + DZ * DZ;
-  double RRM = RR2; /* Ewald: atomic cutoff (LMNBL handled by the caller) */
+  double RRM = RR2; /* Ewald: atomic cutoff */
+  if (st->p.lmnbl) {
+    /* molecular cutoff: small molecules (at most MMOL = 5 sites) are in or
+     * out of the list as a whole, by their centre of mass (forces.f:1882-1936) */
+    const int MMOL = 5;
+    int NMI = st->nsits[st->itype[I]], NMJ = st->nsits[st->itype[J]];
+    if (!(NMI > MMOL && NMJ > MMOL)) {
+      if (NMI > MMOL && NMJ <= MMOL) {
+        DX = st->sx[I] - st->X[jmol]; DY = st->sy[I] - st->Y[jmol]; DZ = st->sz[I] - st->Z[jmol];
+      } else if (NMJ > MMOL) {
+        DX = st->X[imol] - st->sx[J]; DY = st->Y[imol] - st->sy[J]; DZ = st->Z[imol] - st->sz[J];
+      } else {
+        DX = st->X[imol] - st->X[jmol]; DY = st->Y[imol] - st->Y[jmol]; DZ = st->Z[imol] - st->Z[jmol];
+      }
+      pbc(st, &DX, &DY, &DZ);
+      RRM = DX * DX + DY * DY + DZ * DZ;
+    }
+  }
   if (imol == jmol) {
     if (RR2 <= 64.0) {
       int nb = st->nnbb[I];
@@ -545,10 +569,6 @@ static int list_due(ox_state *st, int MSTEP) {
 }
 
 int ox_chcnb(ox_state *st, int32_t *mbsh, int32_t *mbln) {
-  if (st->p.lmnbl) {
-    snprintf(st->msg, sizeof st->msg, "reaction-field list not restated");
-    return MDX_ERR_UNSUPPORTED;
-  }
   const int n = st->nstot;
   long capS = (long)st->caps * n, capL = (long)st->capl * n;
   long MBSH = 0, MBLN = 0;

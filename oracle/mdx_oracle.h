@@ -4,11 +4,13 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this;
  * only tests, the smoke check and the CPU-baseline leg of the benchmark do.
  *
- * Parity status: unpinned against the reference binary.  The reference is
- * Fortran and no Fortran compiler exists on either machine, so the
- * restatement cannot be compared with the original program's output.  It is
- * pinned instead by physical invariants (Newton's third law, finite-difference
- * forces, Ewald alpha independence, NVE energy conservation) in tests/.
+ * Parity status: pinned to the reference's own example run (its input,
+ * restart file and printed output, as fixtures under tests/golden/): setup
+ * numbers to the printed digits, run averages within stated bars.  The
+ * reference is Fortran and no Fortran compiler exists on either machine, so
+ * no bit-for-bit comparison with the original program exists; physical
+ * invariants (Newton's third law, finite-difference forces, Ewald alpha
+ * independence, NVE energy conservation) in tests/ pin the rest.
  *
  * The functions take the same structures as the C ABI in include/mdx_gpu.h
  * and mirror the reference routines one to one (ox_chcnb = CHCNB, ...).

@@ -117,8 +117,15 @@ def test_oracle_lists_against_numpy(spec):
     assert got_short == short and got_long == long_ and got_14 == s14
 
 
+def _rf(spec, diel=78.0, debye=0.0):
+    import dataclasses
+    return dataclasses.replace(spec, alpha=-diel, fexp=debye)
+
+
 @pytest.mark.parametrize("spec", [systems.spce_ions(n=64, ions=1), systems.organics(nw=40),
-                                  systems.spcfw(n=64, rcut=6.0)])
+                                  systems.spcfw(n=64, rcut=6.0),
+                                  _rf(systems.spce_ions(n=64, ions=1)),
+                                  _rf(systems.organics(nw=40), diel=60.0, debye=8.0)])
 def test_oracle_newton_and_finite_difference(spec):
     s = S.System(spec)
     st = S.make_configuration(s, seed=3, jitter=0.05)

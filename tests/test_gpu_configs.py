@@ -172,3 +172,55 @@ def test_torsion_forms_mixed_error():
         f[prec] = g.forces(1)
     rms = np.sqrt(((f[MDX_MIXED] - f[MDX_FP64]) ** 2).sum() / (f[MDX_FP64] ** 2).sum())
     assert rms < 1e-5, rms
+
+
+# ------------------------------------------------------ reaction field --
+def rf_system(diel=78.0, debye=0.0, rigid=True):
+    """Electrostatics ALPHA <= 0 (main.f:740-793): reaction field of
+    dielectric constant -ALPHA (FEXP the Debye length), molecular cutoff
+    lists; DIEL = 1 is a plain cutoff."""
+    base = systems.spce_ions(n=216, ions=2) if rigid else systems.organics(nw=150)
+    spec = dataclasses.replace(base, alpha=-diel, fexp=debye, rcut=9.0)
+    s = S.System(spec)
+    assert s.lmnbl and s.alphad == 0.0
+    return s, S.make_configuration(s, seed=3, jitter=0.05)
+
+
+@pytest.mark.parametrize("diel,debye,rigid", [(78.0, 0.0, True), (1.0, 0.0, True),
+                                              (60.0, 8.0, False)])
+def test_reaction_field_lists_and_forces(diel, debye, rigid):
+    """The molecular cutoff list (small molecules whole, by centre of mass,
+    forces.f:1882-1936) bit for bit, and the reaction-field forces and
+    energies at 1e-10, against the oracle."""
+    s, st = rf_system(diel, debye, rigid)
+    g, o = _pair(s, st)
+    assert g.chcnb() == o.chcnb()
+    (gs1, gs2), (gl1, gl2) = g.lists()
+    (os1, os2), (ol1, ol2) = o.lists()
+    assert np.array_equal(gs1, os1) and np.array_equal(gs2, os2)
+    assert np.array_equal(gl1, ol1) and np.array_equal(gl2, ol2)
+    g.getcom(); o.getcom()
+    a, b = g.allforce(), o.allforce()
+    assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
+    for n in ("pe1", "pels1", "pe2", "pels2", "vir1", "vir2", "wirs", "wirss"):
+        assert abs(getattr(a, n) - getattr(b, n)) <= FP64_TOL * max(abs(getattr(b, n)), 1e-12), n
+
+
+def test_reaction_field_dynamics_and_mixed():
+    s, st = rf_system()
+    g, o = _pair(s, st)
+    rg, ro = g.sultan(3), o.sultan(3)
+    (gx, gy, gz, *_), _ = g.get_state()
+    (ox, oy, oz, *_), _ = o.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
+    from mdynamix_gb300.mdx import ForcePath
+    f = {}
+    for prec in (MDX_FP64, MDX_MIXED):
+        x = ForcePath(s, precision=prec)
+        x.set_state(*st)
+        x.chcnb()
+        x.getcom()
+        x.allforce()
+        f[prec] = x.forces(3)
+    rms = np.sqrt(((f[MDX_MIXED] - f[MDX_FP64]) ** 2).sum() / (f[MDX_FP64] ** 2).sum())
+    assert rms < 1e-5, rms
