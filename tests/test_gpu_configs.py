@@ -19,6 +19,7 @@ import pytest
 import oracle
 from mdynamix_gb300 import system as S
 from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
+from tests import systems
 
 pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-10
