@@ -386,6 +386,30 @@ int mdx_get_bonded_averages(mdx_ctx *ctx, double *br, double *be, double *ar, do
 int mdx_set_averaging(mdx_ctx *ctx, int on);
 int mdx_get_bonded_sums(mdx_ctx *ctx, double *sums, int32_t clear);
 
+/* PULLBACK (forces.f:1756-1799): what SLFORCES and ALLFORCE add to the slow
+ * forces G after the pair and Ewald terms and before SCLFRC -- a constant
+ * drag on the atoms of chosen types (LDRAG: GZ += MASSD FDRAG), harmonic
+ * wells that hold chosen atoms near reference positions (LRR: G -= RLR
+ * (S - S_ref), no minimum image, as the reference), and an external field
+ * along z (IEXT = 1: GZ += Q EXAMPL cos(EXFREQ FULTIM / (2 PI)), FULTIM =
+ * TIM + NSTEP DT).  NSTEP counts long steps on the device: nstep at the
+ * call, one more at the start of every DOUBLE / SULTAN long step.  pb =
+ * NULL switches it off.  Arrays are copied in. */
+typedef struct {
+  int32_t ldrag;                 /* LDRAG                                   */
+  int32_t ldragt[MDX_NTPS];      /* LDRAGT per molecule type                */
+  double fdrag[MDX_NTPS];        /* FDRAG per type (internal units)          */
+  int32_t npull;                 /* NPULL atoms in wells (LRR when > 0)      */
+  const int32_t *inpl;           /* INPL: their atom numbers, 1-based        */
+  const double *xpl, *ypl, *zpl; /* XPL, YPL, ZPL: the wells' centres (A)    */
+  double rlr;                    /* RLR spring constant (internal units)     */
+  int32_t iext;                  /* IEXT: 1 = external field along z         */
+  double exampl, exfreq;         /* EXAMPL, EXFREQ                           */
+  double tim, dt;                /* TIM and DT (seconds)                     */
+  int32_t nstep;                 /* NSTEP of the next force evaluation       */
+} mdx_pullback;
+int mdx_set_pullback(mdx_ctx *ctx, const mdx_pullback *pb);
+
 /* expanded-ensemble scaling (RECINT) */
 int mdx_set_lambda(mdx_ctx *ctx, double ec, double pw1, double pw2,
                    double bee);

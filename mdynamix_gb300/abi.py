@@ -137,6 +137,45 @@ class MdxPathInfo(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MdxPullback(C.Structure):
+    """mdx_pullback: PULLBACK's drag, wells and external field."""
+    _fields_ = [("ldrag", C.c_int32), ("ldragt", C.c_int32 * NTPS), ("fdrag", C.c_double * NTPS),
+                ("npull", C.c_int32), ("inpl", I32P), ("xpl", F64P), ("ypl", F64P),
+                ("zpl", F64P), ("rlr", C.c_double), ("iext", C.c_int32),
+                ("exampl", C.c_double), ("exfreq", C.c_double), ("tim", C.c_double),
+                ("dt", C.c_double), ("nstep", C.c_int32)]
+
+
+def pullback(s: System, drag=None, wells=None, rlr=0.0, field=None, tim=0.0, nstep=0):
+    """An MdxPullback (and the arrays it points to) for a System: drag =
+    {type (1-based): FDRAG}, wells = (atoms 1-based, x, y, z), field =
+    (EXAMPL, EXFREQ) or None."""
+    pb = MdxPullback()
+    keep = []
+    if drag:
+        pb.ldrag = 1
+        for t, f in drag.items():
+            pb.ldragt[t - 1] = 1
+            pb.fdrag[t - 1] = f
+    if wells is not None:
+        atoms, x, y, z = (np.ascontiguousarray(a) for a in wells)
+        atoms = atoms.astype(np.int32)
+        x, y, z = (a.astype(np.float64) for a in (x, y, z))
+        keep += [atoms, x, y, z]
+        pb.npull = len(atoms)
+        pb.inpl = atoms.ctypes.data_as(I32P)
+        pb.xpl, pb.ypl, pb.zpl = (a.ctypes.data_as(F64P) for a in (x, y, z))
+        pb.rlr = rlr
+    if field is not None:
+        pb.iext = 1
+        pb.exampl, pb.exfreq = field
+    pb.tim = tim
+    pb.dt = s.unitt
+    pb.nstep = nstep
+    pb._keep = keep
+    return pb
+
+
 class MdxKin(C.Structure):
     """mdx_kin: GETKIN's kinetic energies and temperatures."""
     _fields_ = [(n, C.c_double) for n in ("ektr", "ekrot", "ekint", "tke", "ttr", "trot",

@@ -9,6 +9,8 @@
 // whole step is a fixed sequence of launches with no host round trip.
 #include <cmath>
 
+#include <algorithm>
+
 #include "mdx_internal.cuh"
 
 namespace {
@@ -1440,6 +1442,75 @@ int launch_sclfrc(mdx_ctx *ctx, int nnn) {
   double *y = nnn == 1 ? d.hy : nnn == 2 ? d.gy : d.fy;
   double *z = nnn == 1 ? d.hz : nnn == 2 ? d.gz : d.fz;
   k_sclfrc<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, fct, d.massdi, x, y, z, d.sc);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+// PULLBACK (forces.f:1756-1799) on G: drag on chosen types, harmonic wells
+// on chosen atoms, external field along z at FULTIM = TIM + NSTEP DT.
+struct PullConst {
+  int ldrag, npull, iext;
+  int ldragt[MDX_NT];
+  double fdrag[MDX_NT];
+  double rlr, exampl, exfreq, tim, dt;
+};
+
+// Thread per atom, the reference's order on each atom: drag, well, field.
+// well[i]: the atom's well (-1: none; the last one if listed twice).
+__global__ void k_pullback(int n, const int4 *__restrict__ ainfo,
+                           const double *__restrict__ massdi, const dbl4 *__restrict__ pos,
+                           PullConst pc, const int *__restrict__ well,
+                           const double *__restrict__ ref, const int *__restrict__ nstep,
+                           double *gx, double *gy, double *gz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t = ainfo[i].x;
+  const dbl4 p = pos[i];
+  if (pc.ldrag && pc.ldragt[t]) gz[i] = gz[i] + (1.0 / massdi[i]) * pc.fdrag[t];
+  if (pc.npull > 0) {
+    const int w = well[i];
+    if (w >= 0) {
+      gx[i] = gx[i] - pc.rlr * (p.x - ref[w]);
+      gy[i] = gy[i] - pc.rlr * (p.y - ref[pc.npull + w]);
+      gz[i] = gz[i] - pc.rlr * (p.z - ref[2 * pc.npull + w]);
+    }
+  }
+  if (pc.iext == 1) {
+    const double FULTIM = pc.tim + (*nstep) * pc.dt;
+    const double EFIELD = pc.exampl * cos(pc.exfreq * FULTIM * 0.5 / MDX_PI);
+    gz[i] = gz[i] + p.w * EFIELD;
+  }
+}
+
+__global__ void k_step_tick(int *nstep) { *nstep = *nstep + 1; }
+
+int launch_pullback(mdx_ctx *ctx) {
+  if (!ctx->pullback) return MDX_OK;
+  MDX_TIMER(ctx, MDX_T_OTHER);
+  DevData &d = ctx->dv;
+  PullConst pc{};
+  pc.ldrag = ctx->pb.ldrag;
+  pc.npull = ctx->pb.npull;
+  pc.iext = ctx->pb.iext;
+  for (int t = 0; t < MDX_NT; ++t) {
+    pc.ldragt[t] = ctx->pb.ldragt[t];
+    pc.fdrag[t] = ctx->pb.fdrag[t];
+  }
+  pc.rlr = ctx->pb.rlr;
+  pc.exampl = ctx->pb.exampl;
+  pc.exfreq = ctx->pb.exfreq;
+  pc.tim = ctx->pb.tim;
+  pc.dt = ctx->pb.dt;
+  k_pullback<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, d.ainfo, d.massdi, d.pos, pc,
+                                                        d.pull_atom, d.pull_ref, d.pull_step,
+                                                        d.gx, d.gy, d.gz);
+  MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+int launch_step_tick(mdx_ctx *ctx) {
+  if (!ctx->pullback) return MDX_OK;
+  k_step_tick<<<1, 1, 0, ctx->stream>>>(ctx->dv.pull_step);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

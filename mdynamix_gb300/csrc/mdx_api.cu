@@ -223,6 +223,7 @@ int do_slforces(mdx_ctx *ctx, bool split, bool mirrored = false) {
   RC(launch_zero_slow(ctx));
   RC(do_slow_parts(ctx, split, mirrored));
   RC(launch_wir(ctx, 2));
+  RC(launch_pullback(ctx));
   RC(launch_sclfrc(ctx, 2));
   return MDX_OK;
 }
@@ -238,6 +239,9 @@ int do_allforce(mdx_ctx *ctx, bool split, bool laver = false) {
   RC(do_slow_parts(ctx, split));
   RC(launch_wir(ctx, 2));
   RC(launch_sum_forces(ctx));
+  // PULLBACK adds to G after CM_ADDLA has formed F (forces.f:88-95): SULTAN,
+  // which moves with F, does not see it -- the reference's order, kept
+  RC(launch_pullback(ctx));
   RC(launch_sclfrc(ctx, 3));
   return MDX_OK;
 }
@@ -258,6 +262,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
   const int NFREQ = p.nfreq, NFREQ2 = NFREQ / 2 + 1;
   const double HTSTEP = 0.5 * p.tstep, TSTEB = p.tsteb, HTSTEB = 0.5 * p.tsteb;
   bool pend = false;
+  RC(launch_step_tick(ctx));  // NSTEP = NSTEP + 1 (mdstep.f:325)
   RC(launch_scaling(ctx, 1, &pend));
   if (p.lnpt) RC(sync_box_from_device(ctx));
   RC(launch_kick(ctx, 2, HTSTEP, pend));
@@ -289,6 +294,7 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
 // one step of SULTAN (mdstep.f:83-162)
 int sultan_step(mdx_ctx *ctx, int mstep, int slot) {
   const mdx_params &p = ctx->p;
+  RC(launch_step_tick(ctx));  // NSTEP = NSTEP + 1 (mdstep.f:75)
   RC(launch_leapfrog_shake(ctx));
   if (mstep == 1) RC(launch_mstep1_rescale(ctx));
   RC(launch_vira(ctx, 1));
@@ -531,7 +537,7 @@ int mdx_close(mdx_ctx *ctx) {
                   d.ar, d.tr, d.cols, d.kchunks, d.kgroups, d.kconst, d.rf_part, d.tc_slot, d.tc_w, d.tc_meta, d.tcs_part, d.tcs_cp0, d.tc_zimg, d.tcs_zimg, d.tcs_red, d.sitems, d.tabx, d.tabxf, d.sk, d.sc, d.th,
                   d.rec, d.err, d.shake_iter, d.red, d.scal_scratch, d.nspec_d,
                   d.red_part, d.red_ctr, d.sk_part, d.snap, d.avsum, d.shk_item,
-                  d.shk_cl, d.shk_rec, d.shk_mfail};
+                  d.shk_cl, d.shk_rec, d.shk_mfail, d.pull_atom, d.pull_ref, d.pull_step};
   if (ctx->stream) {
     for (void *p : ptrs) ctx_free(ctx, p);
     cudaStreamSynchronize(ctx->stream);
@@ -1138,6 +1144,52 @@ int mdx_get_bonded_averages(mdx_ctx *ctx, double *br, double *be, double *ar, do
     if (dst[k] && len[k] > 0)
       MDX_CUDA(ctx_copy(ctx->stream, dst[k], src[k], sizeof(double) * len[k],
                         cudaMemcpyDeviceToHost));
+  return MDX_OK;
+}
+
+int mdx_set_pullback(mdx_ctx *ctx, const mdx_pullback *pb) {
+  if (!ctx) return MDX_ERR_ARG;
+  RC(require(ctx, true, false, false));
+  DevData &d = ctx->dv;
+  ctx->drop_graphs();  // the step's launches change
+  if (!pb) {
+    ctx->pullback = false;
+    return MDX_OK;
+  }
+  if (pb->npull < 0 || (pb->npull > 0 && (!pb->inpl || !pb->xpl || !pb->ypl || !pb->zpl))) {
+    ctx->err = "mdx_set_pullback: NPULL wells need INPL, XPL, YPL, ZPL";
+    return MDX_ERR_ARG;
+  }
+  std::vector<int> well(d.n, -1);
+  for (int k = 0; k < pb->npull; ++k) {
+    if (pb->inpl[k] < 1 || pb->inpl[k] > d.n) {
+      ctx->err = "mdx_set_pullback: INPL out of range";
+      return MDX_ERR_ARG;
+    }
+    well[pb->inpl[k] - 1] = k;
+  }
+  ctx_free(ctx, d.pull_atom);
+  ctx_free(ctx, d.pull_ref);
+  d.pull_atom = nullptr;
+  d.pull_ref = nullptr;
+  RC(dmalloc(ctx, &d.pull_atom, (size_t)d.n));
+  RC(upload(ctx, d.pull_atom, well.data(), (size_t)d.n));
+  if (pb->npull > 0) {
+    std::vector<double> ref(3 * (size_t)pb->npull);
+    for (int k = 0; k < pb->npull; ++k) {
+      ref[k] = pb->xpl[k];
+      ref[pb->npull + k] = pb->ypl[k];
+      ref[2 * (size_t)pb->npull + k] = pb->zpl[k];
+    }
+    RC(dmalloc(ctx, &d.pull_ref, ref.size()));
+    RC(upload(ctx, d.pull_ref, ref.data(), ref.size()));
+  }
+  if (!d.pull_step) RC(dmalloc(ctx, &d.pull_step, 1));
+  RC(upload(ctx, d.pull_step, &pb->nstep, 1));
+  ctx->pb = *pb;
+  ctx->pb.inpl = nullptr;
+  ctx->pb.xpl = ctx->pb.ypl = ctx->pb.zpl = nullptr;
+  ctx->pullback = pb->ldrag || pb->npull > 0 || pb->iext == 1;
   return MDX_OK;
 }
 

@@ -253,6 +253,10 @@ struct DevData {
   int2 *shk_item, *shk_cl;
   int *shk_rec, *shk_mfail;
   int shk_nitem;
+  // PULLBACK: restrained atoms and their wells; the device's NSTEP
+  int *pull_atom;
+  double *pull_ref;   // 3 x npull: x, y, z
+  int *pull_step;
   size_t sk_part_cap;
 };
 
@@ -295,6 +299,8 @@ struct mdx_ctx {
   int64_t glaunches[8] = {};
   bool use_graphs = true;
   bool averaging = false;  // mdx_set_averaging: LAVER forces + statistics every long step
+  bool pullback = false;   // mdx_set_pullback: drag, wells or field on
+  mdx_pullback pb{};       // its constants (array pointers not kept)
   void drop_graphs() {
     for (auto &g : gexec)
       if (g) {
@@ -613,6 +619,8 @@ int launch_zero_slow(mdx_ctx *ctx);
 int launch_fix_to_double(mdx_ctx *ctx, int which);  // mixed: int64 -> G/H
 int launch_sclfrc(mdx_ctx *ctx, int nnn);
 int launch_sum_forces(mdx_ctx *ctx);                // F = G + H
+int launch_pullback(mdx_ctx *ctx);                  // PULLBACK into G
+int launch_step_tick(mdx_ctx *ctx);                 // NSTEP += 1 on the device
 int launch_getcom(mdx_ctx *ctx, bool mirror = false);  // mirror: refresh posf/posi too
 int launch_getkin(mdx_ctx *ctx, const double *summd, double *out);  // EKTR, EKROT, TKE
 int launch_chkmom(mdx_ctx *ctx, double sumasd, double *pt);        // removed momentum

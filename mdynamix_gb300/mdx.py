@@ -76,6 +76,8 @@ def load():
     L.mdx_snapshot_wait.argtypes = [P, C.c_int32]
     L.mdx_get_bonded_averages.argtypes = [P, F64P, F64P, F64P, F64P, F64P, F64P]
     L.mdx_set_averaging.argtypes = [P, C.c_int]
+    from mdynamix_gb300.abi import MdxPullback
+    L.mdx_set_pullback.argtypes = [P, C.POINTER(MdxPullback)]
     L.mdx_get_bonded_sums.argtypes = [P, F64P, C.c_int32]
     L.mdx_inifur.argtypes = [P, I32P]
     L.mdx_chcnb.argtypes = [P, I32P, I32P]
@@ -286,6 +288,11 @@ class ForcePath:
                                                              ("br", "be", "ar", "ae", "tr", "te")]))
         n = {"br": s.nrbb, "be": s.nrbb, "ar": s.nraa, "ae": s.nraa, "tr": s.nrtt, "te": s.nrtt}
         return {k: v[:n[k]] for k, v in out.items()}
+
+    def set_pullback(self, pb=None):
+        """PULLBACK's drag, wells and external field (abi.pullback builds
+        pb); None switches them off."""
+        self._check(self.L.mdx_set_pullback(self.h, C.byref(pb) if pb is not None else None))
 
     def set_averaging(self, on: bool = True):
         """Keep GETAVR's bonded statistics on the device, one sample per long

@@ -59,6 +59,8 @@ def lib():
         for n in ("ox_double", "ox_double_steps", "ox_sultan", "ox_sultan_steps"):
             getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
         L.ox_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
+        from mdynamix_gb300.abi import MdxPullback
+        L.ox_set_pullback.argtypes = [P, C.POINTER(MdxPullback)]
         L.ox_ee_delta.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, F64P]
         from mdynamix_gb300.abi import MdxPimdParams, MdxPimdRecord
@@ -217,6 +219,9 @@ class Oracle:
 
     def sultan_steps(self, nsteps, mstep0):
         return self._run("ox_sultan_steps", nsteps, mstep0)
+
+    def set_pullback(self, pb=None):
+        self._check(self.L.ox_set_pullback(self.h, C.byref(pb) if pb is not None else None))
 
     def ee_delta(self, ec_old, ec_new, pw1=1.0, pw2=1.0 / 3.0, bee=3.0):
         out = np.zeros(4)

@@ -102,6 +102,10 @@ struct ox_state {
    * the positions of the last list build; list builds counted */
   double rlist2, *rsx, *rsy, *rsz;
   int nbuild;
+  /* PULLBACK (forces.f:1756-1799): drag, wells, external field; NSTEP */
+  int pull_on, pull_nstep, *pull_atom;
+  double *pull_ref;
+  mdx_pullback pb;
   double *X, *Y, *Z, *PX, *PY, *PZ;
   int mbsh, mbln;
   int *nbs1, *nbs2, *nbl1, *nbl2;
@@ -385,7 +389,8 @@ void ox_close(ox_state *st) {
                   st->jtj, st->ktk, st->ltl, st->ituk, st->sx, st->sy, st->sz,
                   st->vx, st->vy, st->vz, st->fx, st->fy, st->fz, st->gx,
                   st->gy, st->gz, st->hx, st->hy, st->hz, st->ox, st->oy,
-                  st->oz, st->wx, st->wy, st->wz, st->rsx, st->rsy, st->rsz, st->X, st->Y, st->Z, st->PX,
+                  st->oz, st->wx, st->wy, st->wz, st->rsx, st->rsy, st->rsz, st->pull_atom,
+                  st->pull_ref, st->X, st->Y, st->Z, st->PX,
                   st->PY, st->PZ, st->nbs1, st->nbs2, st->nbl1, st->nbl2,
                   st->rkx, st->rky, st->rkz, st->br, st->be, st->ar, st->ae,
                   st->tr, st->te};
@@ -1845,6 +1850,59 @@ static void cm_addl_wirs(ox_state *st) {
   }
 }
 
+int ox_set_pullback(ox_state *st, const mdx_pullback *pb) {
+  free(st->pull_atom);
+  free(st->pull_ref);
+  st->pull_atom = NULL;
+  st->pull_ref = NULL;
+  st->pull_on = 0;
+  if (!pb) return MDX_OK;
+  st->pb = *pb;
+  st->pull_nstep = pb->nstep;
+  if (pb->npull > 0) {
+    st->pull_atom = (int *)xcalloc((size_t)pb->npull + 1, sizeof(int));
+    st->pull_ref = (double *)xcalloc(3 * (size_t)pb->npull + 3, sizeof(double));
+    for (int k = 0; k < pb->npull; ++k) {
+      st->pull_atom[k + 1] = pb->inpl[k];
+      st->pull_ref[3 * k + 0] = pb->xpl[k];
+      st->pull_ref[3 * k + 1] = pb->ypl[k];
+      st->pull_ref[3 * k + 2] = pb->zpl[k];
+    }
+  }
+  st->pull_on = pb->ldrag || pb->npull > 0 || pb->iext == 1;
+  return MDX_OK;
+}
+
+/* PULLBACK, forces.f:1756-1799 */
+static void pullback(ox_state *st) {
+  if (!st->pull_on) return;
+  const mdx_pullback *pb = &st->pb;
+  if (pb->ldrag)
+    for (int I = 1; I <= st->nstot; ++I) {
+      int ITYP = st->itype[I];
+      if (pb->ldragt[ITYP - 1]) {
+        int IS = st->nsite[I];
+        (void)IS;
+        st->gz[I] = st->gz[I] + (1.0 / st->massdi[I]) * pb->fdrag[ITYP - 1];
+      }
+    }
+  if (pb->npull > 0)
+    for (int IL = 1; IL <= pb->npull; ++IL) {
+      int I = st->pull_atom[IL];
+      double DX = st->sx[I] - st->pull_ref[3 * (IL - 1) + 0];
+      double DY = st->sy[I] - st->pull_ref[3 * (IL - 1) + 1];
+      double DZ = st->sz[I] - st->pull_ref[3 * (IL - 1) + 2];
+      st->gx[I] = st->gx[I] - pb->rlr * DX;
+      st->gy[I] = st->gy[I] - pb->rlr * DY;
+      st->gz[I] = st->gz[I] - pb->rlr * DZ;
+    }
+  if (pb->iext == 1) {
+    double FULTIM = pb->tim + st->pull_nstep * pb->dt;
+    double EFIELD = pb->exampl * cos(pb->exfreq * FULTIM * 0.5 / PI);
+    for (int I = 1; I <= st->nstot; ++I) st->gz[I] = st->gz[I] + st->q[I] * EFIELD;
+  }
+}
+
 int ox_slforces(ox_state *st, mdx_scalars *out) {
   int rc;
   zerofs(st, 2);
@@ -1853,6 +1911,7 @@ int ox_slforces(ox_state *st, mdx_scalars *out) {
   eterms(st);
   forces_long(st);
   cm_addl_wirs(st); /* CM_ADDLF, scalar.f:77-82 */
+  pullback(st);
   sclfrc(st, 2);
   st->s.mbsh = st->mbsh;
   st->s.mbln = st->mbln;
@@ -1882,6 +1941,7 @@ int ox_allforce(ox_state *st, mdx_scalars *out) {
                  st->gy[N] * (st->sy[N] - st->Y[M]) -
                  st->gz[N] * (st->sz[N] - st->Z[M]);
   }
+  pullback(st); /* into G after F = G + H, as ALLFORCE orders it */
   sclfrc(st, 3);
   st->s.mbsh = st->mbsh;
   st->s.mbln = st->mbln;
@@ -2334,6 +2394,7 @@ int ox_double_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
   const double TSTEB = st->p.tsteb, HTSTEB = 0.5 * st->p.tsteb;
   for (int NSTEP = 1; NSTEP <= nsteps; ++NSTEP) {
     int MSTEP = mstep0 + NSTEP;
+    st->pull_nstep++;
     if ((rc = scaling(st, 1))) return rc;
     kick(st, st->gx, st->gy, st->gz, HTSTEP);
     int LMEM = 0;
@@ -2387,6 +2448,7 @@ int ox_sultan_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
   unsigned char *moved = (unsigned char *)xcalloc((size_t)st->nstot + 1, 1);
   for (int NSTEP = 1; NSTEP <= nsteps; ++NSTEP) {
     int MSTEP = mstep0 + NSTEP;
+    st->pull_nstep++;
     for (int I = 1; I <= st->nstot; ++I)
       if (st->lmove[st->itype[I]]) {
         st->ox[I] = st->sx[I];

@@ -60,6 +60,7 @@ int ox_sultan(ox_state *st, int32_t nsteps, int32_t nsttot,
 int ox_sultan_steps(ox_state *st, int32_t nsteps, int32_t mstep0,
                     mdx_step_record *rec);
 int ox_set_lambda(ox_state *st, double ec, double pw1, double pw2, double bee);
+int ox_set_pullback(ox_state *st, const mdx_pullback *pb);
 int ox_ee_delta(ox_state *st, double ec_old, double ec_new, double pw1, double pw2,
                 double bee, double *out);
 /* PIMD over nbeads bead states (pimd.f:18-444); thermo: THERMO(NSTOT, JNH)

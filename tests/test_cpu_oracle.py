@@ -364,3 +364,28 @@ def test_shake_on_bonds_to_hydrogen_counts_constraints():
     heavy = [i for i, st in enumerate(lip["sites"]) if st["mass"] > 1.5]
     cons = [bd for bd, f in zip(lip["bonds"], b.b_lcon[:a.nrb[0]]) if f]
     assert all(bd["i"] - 1 not in heavy or bd["j"] - 1 not in heavy for bd in cons)
+
+
+def test_oracle_pullback_field_and_wells():
+    """The oracle's PULLBACK: the field adds Q E along z with E at
+    TIM + NSTEP DT, a well pulls its atom back to the well's centre."""
+    from mdynamix_gb300.abi import pullback
+    s, st = systems.build(systems.spcfw(n=64, ions=1, rcut=6.0))
+    o = oracle.Oracle(s)
+    o.set_state(*st)
+    o.chcnb()
+    o.getcom()
+    o.slforces()
+    g0 = o.forces(2)
+    E0, w, t0 = 2.0e-3, 3.0e13, 5.0e-13
+    atom = 7
+    ref = (st[0][atom - 1] + 0.2, st[1][atom - 1], st[2][atom - 1] - 0.1)
+    o.set_pullback(pullback(s, field=(E0, w), tim=t0, nstep=4,
+                            wells=(np.array([atom]), *[np.array([r]) for r in ref]), rlr=1e-2))
+    o.slforces()
+    d = o.forces(2) - g0
+    E = E0 * np.cos(w * (t0 + 4 * s.unitt) * 0.5 / S.PI)
+    qz = s.q * E
+    qz[atom - 1] += -1e-2 * (st[2][atom - 1] - ref[2])
+    assert np.allclose(d[:, 2], qz, rtol=1e-9, atol=1e-12 * np.abs(g0).max())
+    assert abs(d[atom - 1, 0] - (-1e-2 * (st[0][atom - 1] - ref[0]))) < 1e-12

@@ -225,3 +225,39 @@ def test_reaction_field_dynamics_and_mixed():
         f[prec] = x.forces(3)
     rms = np.sqrt(((f[MDX_MIXED] - f[MDX_FP64]) ** 2).sum() / (f[MDX_FP64] ** 2).sum())
     assert rms < 1e-5, rms
+
+
+# ---------------------------------------------------------- PULLBACK --
+def pullback_case():
+    from mdynamix_gb300.abi import pullback
+    s, st = systems.build(systems.spcfw(n=216, ions=2))
+    rng = np.random.default_rng(8)
+    atoms = rng.choice(s.nstot, 6, replace=False) + 1
+    ref = [st[k][atoms - 1] + rng.normal(scale=0.3, size=6) for k in range(3)]
+    pb = pullback(s, drag={2: 2.0e-4, 3: -1.5e-4}, wells=(atoms, *ref), rlr=5.0e-3,
+                  field=(3.0e-3, 4.0e13), tim=1.0e-12)
+    return s, st, pb
+
+
+def test_pullback_matches_oracle():
+    """PULLBACK (forces.f:1756-1799): drag on the ion types, wells on six
+    atoms, an oscillating field along z -- on G after the slow forces, and
+    along DOUBLE steps whose field follows the step count."""
+    s, st, pb = pullback_case()
+    g, o = _pair(s, st)
+    g.set_pullback(pb)
+    o.set_pullback(pb)
+    g.chcnb(); o.chcnb()
+    g.getcom(); o.getcom()
+    g.slforces(); o.slforces()
+    assert relmax(g.forces(2), o.forces(2)) < FP64_TOL
+    g.allforce(); o.allforce()
+    assert relmax(g.forces(2), o.forces(2)) < FP64_TOL
+    assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
+    g2, o2 = _pair(s, st)
+    g2.set_pullback(pb)
+    o2.set_pullback(pb)
+    g2.double(3), o2.double(3)
+    (gx, gy, gz, *_), _ = g2.get_state()
+    (ox, oy, oz, *_), _ = o2.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gz - oz).max()) < 1e-9
