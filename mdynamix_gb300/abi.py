@@ -147,16 +147,24 @@ class MdxPullback(C.Structure):
 
 
 def pullback(s: System, drag=None, wells=None, rlr=0.0, field=None, tim=0.0, nstep=0):
-    """An MdxPullback (and the arrays it points to) for a System: drag =
-    {type (1-based): FDRAG}, wells = (atoms 1-based, x, y, z), field =
-    (EXAMPL, EXFREQ) or None."""
+    """An MdxPullback (and the arrays it points to) for a System, from the
+    values in the reference's input units, converted as setup.f does:
+
+    drag  = {type (1-based): FDRAG in 10^12 m/s^2}  (x 1e12 UNITT^2/UNITL,
+            setup.f:250)
+    wells = (atoms 1-based, x, y, z in A), rlr = the allowed deviation in A
+            (RLR = 1/(BETA RLR^2), setup.f:113)
+    field = (EXAMPL in V/cm, EXFREQ in Hz)  (EXAMPL x UNITL 1e2 ELECHG/UNITE,
+            setup.f:263)
+    tim   = TIM in s, nstep = NSTEP (the field's time is TIM + NSTEP DT)."""
+    from .system import BOLTZ, ELECHG
     pb = MdxPullback()
     keep = []
     if drag:
         pb.ldrag = 1
         for t, f in drag.items():
             pb.ldragt[t - 1] = 1
-            pb.fdrag[t - 1] = f
+            pb.fdrag[t - 1] = f * (1.0e12 * s.unitt ** 2 / s.unitl)
     if wells is not None:
         atoms, x, y, z = (np.ascontiguousarray(a) for a in wells)
         atoms = atoms.astype(np.int32)
@@ -165,10 +173,12 @@ def pullback(s: System, drag=None, wells=None, rlr=0.0, field=None, tim=0.0, nst
         pb.npull = len(atoms)
         pb.inpl = atoms.ctypes.data_as(I32P)
         pb.xpl, pb.ypl, pb.zpl = (a.ctypes.data_as(F64P) for a in (x, y, z))
-        pb.rlr = rlr
+        beta = s.unite / (BOLTZ * s.trtemp)
+        pb.rlr = 1.0 / (beta * rlr ** 2)
     if field is not None:
         pb.iext = 1
-        pb.exampl, pb.exfreq = field
+        pb.exampl = field[0] * s.unitl * 1.0e2 * ELECHG / s.unite
+        pb.exfreq = field[1]
     pb.tim = tim
     pb.dt = s.unitt
     pb.nstep = nstep

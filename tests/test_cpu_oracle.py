@@ -377,15 +377,21 @@ def test_oracle_pullback_field_and_wells():
     o.getcom()
     o.slforces()
     g0 = o.forces(2)
-    E0, w, t0 = 2.0e-3, 3.0e13, 5.0e-13
+    E0, w, t0 = 5.0e6, 3.0e13, 5.0e-13     # V/cm, Hz, s
     atom = 7
     ref = (st[0][atom - 1] + 0.2, st[1][atom - 1], st[2][atom - 1] - 0.1)
-    o.set_pullback(pullback(s, field=(E0, w), tim=t0, nstep=4,
-                            wells=(np.array([atom]), *[np.array([r]) for r in ref]), rlr=1e-2))
+    pb = pullback(s, field=(E0, w), tim=t0, nstep=4,
+                  wells=(np.array([atom]), *[np.array([r]) for r in ref]), rlr=0.5)
+    # setup.f:113 and setup.f:263 conversions
+    k = 1.0 / (s.unite / (S.BOLTZ * s.trtemp) * 0.25)
+    assert abs(pb.rlr - k) <= 1e-15 * k
+    assert abs(pb.exampl - E0 * 1e-8 * S.ELECHG / s.unite) <= 1e-15 * pb.exampl
+    o.set_pullback(pb)
     o.slforces()
     d = o.forces(2) - g0
-    E = E0 * np.cos(w * (t0 + 4 * s.unitt) * 0.5 / S.PI)
+    E = pb.exampl * np.cos(w * (t0 + 4 * s.unitt) * 0.5 / S.PI)
     qz = s.q * E
-    qz[atom - 1] += -1e-2 * (st[2][atom - 1] - ref[2])
+    qz[atom - 1] += -k * (st[2][atom - 1] - ref[2])
+    assert np.abs(qz).max() > 0.05 * np.abs(g0).max()
     assert np.allclose(d[:, 2], qz, rtol=1e-9, atol=1e-12 * np.abs(g0).max())
-    assert abs(d[atom - 1, 0] - (-1e-2 * (st[0][atom - 1] - ref[0]))) < 1e-12
+    assert abs(d[atom - 1, 0] - (-k * (st[0][atom - 1] - ref[0]))) < 1e-12 * np.abs(g0).max()

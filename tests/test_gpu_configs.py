@@ -234,8 +234,9 @@ def pullback_case():
     rng = np.random.default_rng(8)
     atoms = rng.choice(s.nstot, 6, replace=False) + 1
     ref = [st[k][atoms - 1] + rng.normal(scale=0.3, size=6) for k in range(3)]
-    pb = pullback(s, drag={2: 2.0e-4, 3: -1.5e-4}, wells=(atoms, *ref), rlr=5.0e-3,
-                  field=(3.0e-3, 4.0e13), tim=1.0e-12)
+    # 10^15 m/s^2 drags, 0.5 A wells, a 5 MV/cm field at 40 THz
+    pb = pullback(s, drag={2: 1.0e3, 3: -8.0e2}, wells=(atoms, *ref), rlr=0.5,
+                  field=(5.0e6, 4.0e13), tim=1.0e-12)
     return s, st, pb
 
 
