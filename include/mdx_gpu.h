@@ -506,6 +506,13 @@ int mdx_get_timers(mdx_ctx *ctx, double *ms, int64_t *count);
  * reference. */
 int mdx_probe_fma_peak(int fp64, double *tflops);
 
+/* The FP64 pair sweeps' own exp(-y) and 1/d (pair_math.cuh) beside the CUDA
+ * library's exp(-y) and 1.0/d, evaluated on the device for n host values
+ * (y >= 0, d >= 1); a check of those routines, not a routine of the
+ * reference.  Outputs: own_exp, lib_exp, own_rcp, lib_rcp (n each). */
+int mdx_probe_pair_math(int n, const double *y, const double *d, double *own_exp,
+                        double *lib_exp, double *own_rcp, double *lib_rcp);
+
 #ifdef __cplusplus
 }
 #endif

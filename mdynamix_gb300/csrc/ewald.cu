@@ -193,15 +193,16 @@ __global__ void __launch_bounds__(128) k_sfac(
         const double2 Y = conj_if(sy[j * ky + ny], nyneg);
         const double tr = fma(X.x, Y.x, -X.y * Y.y), ti = fma(X.x, Y.y, X.y * Y.x);
         const double2 *zr = sz + j * kz + cc.nz0;
+        // chunks are sorted by length, so a warp's lanes mostly leave
+        // together and a short chunk issues only its own FMAs
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
-          if (t < cc.len) {
-            const double2 Z = zr[t];
-            A[t][0] = fma(tr, Z.x, A[t][0]);
-            A[t][1] = fma(ti, Z.y, A[t][1]);
-            A[t][2] = fma(tr, Z.y, A[t][2]);
-            A[t][3] = fma(ti, Z.x, A[t][3]);
-          }
+          if (t >= cc.len) break;
+          const double2 Z = zr[t];
+          A[t][0] = fma(tr, Z.x, A[t][0]);
+          A[t][1] = fma(ti, Z.y, A[t][1]);
+          A[t][2] = fma(tr, Z.y, A[t][2]);
+          A[t][3] = fma(ti, Z.x, A[t][3]);
         }
       }
     }
@@ -896,6 +897,9 @@ int host_inifur(mdx_ctx *ctx) {
       koff += cnt;
       poff += m + 1;
     }
+  // longest chunks first (stable): the lanes of a warp share a length
+  std::stable_sort(chunks.begin(), chunks.end(),
+                   [](const Chunk &a, const Chunk &b) { return a.len > b.len; });
   // column groups of the mixed passes: columns sorted by m (then by column
   // index), four at a time, the last group of an m padded
   std::vector<int> order(cols.size());

@@ -415,13 +415,37 @@ __global__ void k_leapfrog(int n, const int4 *__restrict__ ainfo, MoveConst mv,
 // types of ekacc are left alone).  R = float (mixed path): the per-atom
 // terms and the warp sums in FP32 (a few atoms a thread, 32 threads a warp),
 // the block and grid sums in FP64.
-template <int NT, typename R>
+// KICK: a half kick folded into the pass, before the kinetic energy is taken
+// (pre) and/or after it (post): V += h1 A (+ h2 B) for the movable atoms,
+// the operations of k_kick in the same order, so the pass gives the values
+// of kick, GETEMP, kick launched one after the other.
+// vs (pre only): SCALING's per-type velocity factor applied first, as
+// k_scale_atoms (mode 0) and k_kick do.
+struct KickArgs {
+  double h1, h2;
+  const double *ax, *ay, *az;  // null: no kick
+  const double *bx, *by, *bz;  // null: one force only
+  const double *vs;            // null: no velocity factor
+};
+
+__device__ __forceinline__ void kick_atom(const KickArgs &k, int i, double &x, double &y,
+                                          double &z) {
+  if (!k.ax) return;
+  x = x + k.h1 * k.ax[i];
+  y = y + k.h1 * k.ay[i];
+  z = z + k.h1 * k.az[i];
+  if (k.bx) {
+    x = x + k.h2 * k.bx[i];
+    y = y + k.h2 * k.by[i];
+    z = z + k.h2 * k.bz[i];
+  }
+}
+
+template <int NT, typename R, bool KICK>
 __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
                          int ntypes, const double *__restrict__ massdi,
-                         const double *__restrict__ vx,
-                         const double *__restrict__ vy,
-                         const double *__restrict__ vz, double *ekacc,
-                         double *part, unsigned *ctr) {
+                         double *vx, double *vy, double *vz, double *ekacc,
+                         double *part, unsigned *ctr, KickArgs pre, KickArgs post) {
   R e[NT + 4];
 #pragma unroll
   for (int k = 0; k < NT + 4; ++k) e[k] = R(0);
@@ -429,7 +453,15 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
        i += gridDim.x * blockDim.x) {
     const int t = ainfo[i].x;
     if (!mv.lmove[t]) continue;
-    const R m = (R)massdi[i], ux = (R)vx[i], uy = (R)vy[i], uz = (R)vz[i];
+    double px = vx[i], py = vy[i], pz = vz[i];
+    if (KICK && pre.vs) {
+      const double f = pre.vs[t];
+      px = px * f;
+      py = py * f;
+      pz = pz * f;
+    }
+    if (KICK) kick_atom(pre, i, px, py, pz);
+    const R m = (R)massdi[i], ux = (R)px, uy = (R)py, uz = (R)pz;
     const R VVX = m * (ux * ux);
     const R VVY = m * (uy * uy);
     const R VVZ = m * (uz * uz);
@@ -441,6 +473,12 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
 #pragma unroll
     for (int k = 0; k < NT; ++k)
       if (k == t) e[k] += R(0.5) * VSC;
+    if (KICK) {
+      kick_atom(post, i, px, py, pz);
+      vx[i] = px;
+      vy[i] = py;
+      vz[i] = pz;
+    }
   }
   // value k < NT -> ekacc[k] (type k), NT + j -> ekacc[MDX_NT + j]
   double *dst[NT + 4];
@@ -1267,28 +1305,58 @@ struct StageQ {
   }
 };
 
-// The kinetic-energy reduction of GETEMP; its fold is the ST_GETEMP stage.
-static int getemp_kernel(mdx_ctx *ctx) {
+static KickArgs kick_args(mdx_ctx *ctx, const KickSpec &k) {
+  DevData &d = ctx->dv;
+  KickArgs a{};
+  auto set = [&](int w, const double *&x, const double *&y, const double *&z) {
+    x = w == 1 ? d.hx : w == 2 ? d.gx : w == 3 ? d.fx : nullptr;
+    y = w == 1 ? d.hy : w == 2 ? d.gy : w == 3 ? d.fy : nullptr;
+    z = w == 1 ? d.hz : w == 2 ? d.gz : w == 3 ? d.fz : nullptr;
+  };
+  set(k.w1, a.ax, a.ay, a.az);
+  set(k.w2, a.bx, a.by, a.bz);
+  a.h1 = k.h1;
+  a.h2 = k.h2;
+  a.vs = k.vscale ? scratch(ctx)->vscale : nullptr;
+  return a;
+}
+
+// The kinetic-energy reduction of GETEMP, with kicks folded in (pre, post;
+// w1 = 0: none); its fold is the ST_GETEMP stage.
+static int getemp_kernel(mdx_ctx *ctx, const KickSpec &pre = {}, const KickSpec &post = {}) {
   DevData &d = ctx->dv;
   const int nt = ctx->d.ntypes;
+  const KickArgs a = kick_args(ctx, pre), b = kick_args(ctx, post);
+  const bool kick = a.ax || b.ax || a.vs;
+#define GETEMP_K(NT, R, K)                                                             \
+  k_getemp<NT, R, K><<<ctx->nsm, 256, 0, ctx->stream>>>(                               \
+      d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,                   \
+      scratch(ctx)->ekacc, d.red_part, d.red_ctr, a, b)
 #define GETEMP(NT)                                                                    \
   do {                                                                                \
-    if (ctx->mixed())                                                                 \
-      k_getemp<NT, float><<<ctx->nsm, 256, 0, ctx->stream>>>(                         \
-          d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,              \
-          scratch(ctx)->ekacc, d.red_part, d.red_ctr);                                \
-    else                                                                              \
-      k_getemp<NT, double><<<ctx->nsm, 256, 0, ctx->stream>>>(                        \
-          d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,              \
-          scratch(ctx)->ekacc, d.red_part, d.red_ctr);                                \
+    if (ctx->mixed()) {                                                               \
+      if (kick) GETEMP_K(NT, float, true);                                            \
+      else GETEMP_K(NT, float, false);                                                \
+    } else {                                                                          \
+      if (kick) GETEMP_K(NT, double, true);                                           \
+      else GETEMP_K(NT, double, false);                                               \
+    }                                                                                 \
   } while (0)
   if (nt <= 1) GETEMP(1);
   else if (nt <= 2) GETEMP(2);
   else if (nt <= 4) GETEMP(4);
   else GETEMP(MDX_NT);
 #undef GETEMP
+#undef GETEMP_K
   MDX_LAUNCHED(ctx);
   return MDX_OK;
+}
+
+// kick(s), GETEMP, kick(s) in one pass over the atoms, then the ST_GETEMP fold
+int launch_getemp_kick(mdx_ctx *ctx, const KickSpec &pre, const KickSpec &post) {
+  MDX_TIMER(ctx, MDX_T_MOVE);
+  const int rc = getemp_kernel(ctx, pre, post);
+  return rc ? rc : stage(ctx, ST_GETEMP);
 }
 
 int launch_getemp(mdx_ctx *ctx) {
@@ -1314,17 +1382,19 @@ static int scale_atoms(mdx_ctx *ctx, int mode) {
 // in the scratch for the following slow half-kick, which applies it first
 // (same operation order as the reference: V*SCV, then V + HTSTEP*G);
 // *pending_vscale tells the caller.
-int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
+int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale, const KickSpec *kick_first) {
   MDX_TIMER(ctx, MDX_T_MOVE);
   const mdx_params &p = ctx->p;
   StageQ q{ctx};
+  KickSpec scv;  // V *= SCV (per type) folded into the GETEMP pass that follows it
+  scv.vscale = true;
   if (pending_vscale) *pending_vscale = false;
   if (ial == 3 && p.lnvt) {
     q.push(ST_3V);
     RC(q.flush());
     RC(scale_atoms(ctx, 0));
   }
-  RC(getemp_kernel(ctx));
+  RC(getemp_kernel(ctx, kick_first ? *kick_first : KickSpec{}));
   q.push(ST_GETEMP);
   q.push(ST_PRESS);
   if (ial == 1) {
@@ -1350,8 +1420,8 @@ int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
     if (p.lnvt) {
       q.push(ST_2V);
       RC(q.flush());
-      RC(scale_atoms(ctx, 0));
       if (p.lnpt) {
+        RC(scale_atoms(ctx, 0));
         q.push(ST_2NPTV);
         RC(q.flush());
         RC(scale_atoms(ctx, 3));
@@ -1359,7 +1429,7 @@ int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
         q.push(ST_GETEMP);
         q.push(ST_2SCL);
       } else {
-        RC(getemp_kernel(ctx));
+        RC(getemp_kernel(ctx, scv));
         q.push(ST_GETEMP);
       }
       q.push(ST_2SC);
@@ -1382,8 +1452,7 @@ int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale) {
   if (p.lsclt && (ial == 2 || ial == 3)) {
     q.push(ST_SCLT);
     RC(q.flush());
-    RC(scale_atoms(ctx, 0));
-    RC(getemp_kernel(ctx));
+    RC(getemp_kernel(ctx, scv));
     q.push(ST_GETEMP);
   }
   return q.flush();

@@ -13,7 +13,8 @@
 
 // integrate.cu
 int launch_getemp(mdx_ctx *ctx);
-int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale);
+int launch_scaling(mdx_ctx *ctx, int ial, bool *pending_vscale,
+                   const KickSpec *kick_first = nullptr);
 int launch_mstep1_rescale(mdx_ctx *ctx);
 int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
 int launch_leapfrog_shake(mdx_ctx *ctx);
@@ -284,8 +285,9 @@ int double_step(mdx_ctx *ctx, int mstep, int slot) {
       RC(do_fforces(ctx, 0, false, false, true, !keep_fix));
     }
   }
-  RC(launch_kick2(ctx, 1, HTSTEB, 2, HTSTEP));  // the two closing half kicks, one pass
-  RC(launch_scaling(ctx, 2, nullptr));
+  // the two closing half kicks (mdstep.f:405-430) in SCALING(2)'s first GETEMP pass
+  const KickSpec closing{1, HTSTEB, 2, HTSTEP};
+  RC(launch_scaling(ctx, 2, nullptr, &closing));
   if (p.lnpt) RC(sync_box_from_device(ctx));
   if (slot != -2) RC(launch_record(ctx, slot, mstep));  // -1: device counters
   return MDX_OK;
@@ -1595,5 +1597,9 @@ int api_require(mdx_ctx *ctx, bool topo, bool par, bool state) {
 }
 int api_check_err(mdx_ctx *ctx) { return check_err(ctx); }
 int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out) { return copy_scalars(ctx, out); }
-int api_do_slforces(mdx_ctx *ctx, bool split) { return do_slforces(ctx, split); }
-int api_do_fforces(mdx_ctx *ctx, int laver, bool split) { return do_fforces(ctx, laver, split); }
+int api_do_slforces(mdx_ctx *ctx, bool split, bool mirrored) {
+  return do_slforces(ctx, split, mirrored);
+}
+int api_do_fforces(mdx_ctx *ctx, int laver, bool split, bool mirrored) {
+  return do_fforces(ctx, laver, split, true, mirrored);
+}

@@ -608,8 +608,8 @@ cudaError_t raise_smem_limit(K kernel, size_t bytes) {
 int api_require(mdx_ctx *ctx, bool topo, bool par, bool state);
 int api_check_err(mdx_ctx *ctx);
 int api_copy_scalars(mdx_ctx *ctx, mdx_scalars *out);
-int api_do_slforces(mdx_ctx *ctx, bool split);
-int api_do_fforces(mdx_ctx *ctx, int laver, bool split);
+int api_do_slforces(mdx_ctx *ctx, bool split, bool mirrored = false);
+int api_do_fforces(mdx_ctx *ctx, int laver, bool split, bool mirrored = false);
 // bonded.cu: running sums of the per-record bonded statistics
 int launch_acc_bonded(mdx_ctx *ctx);
 int bonded_sums_len(const mdx_ctx *ctx);
@@ -632,6 +632,15 @@ int launch_record(mdx_ctx *ctx, int slot, int mstep);
 int launch_getemp(mdx_ctx *ctx);
 int launch_kick(mdx_ctx *ctx, int which, double h, bool apply_vscale);
 int launch_kick2(mdx_ctx *ctx, int which1, double h1, int which2, double h2);
+// a kick on forces w1 (1 H, 2 G, 3 F; 0 none) with h1, then w2 with h2
+struct KickSpec {
+  int w1 = 0;
+  double h1 = 0.0;
+  int w2 = 0;
+  double h2 = 0.0;
+  bool vscale = false;  // SCALING's per-type velocity factor first (GETEMP passes only)
+};
+int launch_getemp_kick(mdx_ctx *ctx, const KickSpec &pre, const KickSpec &post);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);

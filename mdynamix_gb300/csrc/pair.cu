@@ -18,6 +18,7 @@
 #include <cmath>
 
 #include "mdx_internal.cuh"
+#include "pair_math.cuh"
 
 namespace {
 
@@ -65,9 +66,13 @@ __global__ void __launch_bounds__(256) k_pair64(
   }
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const double hbx = 0.5 * bx, hby = 0.5 * by, hbz = 0.5 * bz;
+  // ABS(D) > HBOX tests as integer compares of the magnitudes' bit patterns
+  // (the same order as the FP64 compare for finite values; no FP64 issue)
+  const long long hbxb = __double_as_longlong(0.5 * bx), hbyb = __double_as_longlong(0.5 * by);
   // LOCALF tests DZ against HBOXL (forces.f:871); FORCES against HBOZL
-  const double hbzt = SHORT ? hbx : hbz;
+  const long long hbzb = __double_as_longlong(SHORT ? 0.5 * bx : 0.5 * bz);
+  const long long rc2b = __double_as_longlong(pc.rc2);
+  const bool rae_on = pc.lmdee && pc.raex != 0.0;
   double acc[6] = {0, 0, 0, 0, 0, 0};
   if (i < n) {
     const dbl4 pi = pos[i];
@@ -86,7 +91,8 @@ __global__ void __launch_bounds__(256) k_pair64(
       const int tj = aj.x, nj = aj.z;
       const bool same = aj.y == mi;
       const int mtr = tc.mdx[ti][tj];
-      double QIJ, A6, B12, RAE = 0.0;
+      double QIJ, A6, B12;
+      bool rae = false;  // RAEX shifts this pair's distance (MDEE)
       const int tix = ni * pc.nnbt + nj;
       if (same) {
         if (is14) {
@@ -102,18 +108,24 @@ __global__ void __launch_bounds__(256) k_pair64(
         QIJ = pi.w * pj.w * pc.coulf;
         A6 = __ldg(&tb.a6lj[tix]);
         B12 = __ldg(&tb.b12lj[tix]);
-        if (pc.lmdee) RAE = (tc.iee[ti] * tc.iee[tj] == 0) ? pc.raex : 0.0;
+        rae = rae_on && tc.iee[ti] * tc.iee[tj] == 0;
       }
       double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
-      pbc_rect(DX, DY, DZ, bx, by, bz, hbx, hby, hbzt);
+      constexpr long long MAG = 0x7fffffffffffffffLL;
+      if ((__double_as_longlong(DX) & MAG) > hbxb) DX = DX - fsign(bx, DX);
+      if ((__double_as_longlong(DZ) & MAG) > hbzb) DZ = DZ - fsign(bz, DZ);
+      if ((__double_as_longlong(DY) & MAG) > hbyb) DY = DY - fsign(by, DY);
       const double RR = DX * DX + DY * DY + DZ * DZ;
-      if (!SHORT && RR > pc.rc2) continue;  // skin mode: listed beyond RCUT
+      if (!SHORT && __double_as_longlong(RR) > rc2b) continue;  // skin mode: listed beyond RCUT
       // one reciprocal square root instead of a square root and a division
       // (within an ulp of DSQRT and 1/R1)
       const double R1I = rsqrt(RR);
       const double R1 = RR * R1I;
-      const double R1E = R1 + RAE;
-      const double R1EI = RAE == 0.0 ? R1I : 1. / R1E;
+      double R1E = R1, R1EI = R1I;
+      if (rae) {
+        R1E = R1 + pc.raex;
+        R1EI = 1. / R1E;
+      }
       double EE1, EES, FORCE;
       if (is14 || (same && tc.iee[ti] == 0)) {
         if (SHORT) {
@@ -136,8 +148,8 @@ __global__ void __launch_bounds__(256) k_pair64(
         }
       } else {
         const double ALPHAR = pc.alphad * R1;
-        const double TTT = 1.0 / (1.0 + MDX_B1 * ALPHAR);
-        const double EXP2A = exp(-(ALPHAR * ALPHAR));
+        const double TTT = rcp_nr(1.0 + MDX_B1 * ALPHAR);
+        const double EXP2A = exp_neg(ALPHAR * ALPHAR);
         const double ERFCT = ewald_erfc_poly(TTT, EXP2A);
         EE1 = QIJ * R1EI;
         EES = EE1 * ERFCT;
@@ -148,7 +160,7 @@ __global__ void __launch_bounds__(256) k_pair64(
         else atomicAdd(&s_split[mtr], EE1);
       }
       if (ENER) acc[P_EES] += EES;
-      if (B12 != 0.0) {
+      if ((__double_as_longlong(B12) << 1) != 0) {  // B12 != 0
         const double R2I = R1EI * R1EI;
         const double R6I = R2I * R2I * R2I;
         double ESR = (A6 + B12 * R6I) * R6I;
@@ -173,12 +185,12 @@ __global__ void __launch_bounds__(256) k_pair64(
         }
         if (ENER) acc[P_ESR] += ESR;
       }
-      if (SHORT || !same || tc.lmove[ti]) {
-        if (ENER) acc[3] += FORCE * (DX * DX);
-        if (ENER) acc[4] += FORCE * (DY * DY);
-        if (ENER) acc[5] += FORCE * (DZ * DZ);
-      }
       const double gxv = FORCE * DX, gyv = FORCE * DY, gzv = FORCE * DZ;
+      if (SHORT || !same || tc.lmove[ti]) {  // FORCE DX^2 as (FORCE DX) DX
+        if (ENER) acc[3] += gxv * DX;
+        if (ENER) acc[4] += gyv * DY;
+        if (ENER) acc[5] += gzv * DZ;
+      }
       fix += gxv;
       fiy += gyv;
       fiz += gzv;

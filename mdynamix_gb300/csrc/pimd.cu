@@ -287,28 +287,30 @@ int long_step(mdx_pimd *pi, int mstep) {
   const mdx_params &p = c0->p;
   const int NFREQ = p.nfreq, NFREQ2 = NFREQ / 2 + 1;
   const double HTSTEP = 0.5 * p.tstep, TSTEB = p.tsteb, HTSTEB = 0.5 * p.tsteb;
+  // Kicks and GETEMP share passes over the atoms (launch_getemp_kick), and
+  // the drift carries GETCOM and the coordinate mirrors
+  // (launch_kick_drift_com): the same operations in the same order as the
+  // separate kernels, in fewer launches per bead.
   RC(fork(pi));
-  EACH_BEAD(RC(launch_getemp(ctx)); RC(launch_kick(ctx, 2, HTSTEP, false));
-            RC(launch_kick(ctx, 1, HTSTEB, false)));
+  EACH_BEAD(RC(launch_getemp_kick(ctx, {}, {2, HTSTEP, 1, HTSTEB})));
   RC(join(pi));
   RC(nose(pi));
   for (int s = 1; s <= NFREQ; ++s) {
     RC(fork(pi));
-    EACH_BEAD(RC(launch_kick_drift(ctx, 0.0, TSTEB, 0)); RC(launch_getcom(ctx));
+    EACH_BEAD(RC(launch_kick_drift_com(ctx, 0.0, TSTEB, 0, false));
               if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
               if (s == NFREQ) {
-                RC(api_do_slforces(ctx, false));
-                RC(api_do_fforces(ctx, 1, false));
+                RC(api_do_slforces(ctx, false, true));
+                RC(api_do_fforces(ctx, 1, false, true));
               } else {
-                RC(api_do_fforces(ctx, 0, false));
+                RC(api_do_fforces(ctx, 0, false, true));
               });
     RC(join(pi));
     RC(springs(pi, s == NFREQ));
     RC(fork(pi));
-    EACH_BEAD(RC(launch_kick(ctx, 1, HTSTEB, false)); RC(launch_getemp(ctx));
-              if (s < NFREQ) RC(launch_kick(ctx, 1, HTSTEB, false));
+    EACH_BEAD(if (s < NFREQ) RC(launch_getemp_kick(ctx, {1, HTSTEB}, {1, HTSTEB}));
               else {
-                RC(launch_kick(ctx, 2, HTSTEP, false));
+                RC(launch_getemp_kick(ctx, {1, HTSTEB}, {2, HTSTEP}));
                 RC(launch_getemp(ctx));
               });
     RC(join(pi));

@@ -5,6 +5,7 @@
 // launches of roughly 10-20 ms); the best configuration is reported.  Results
 // are written out so nothing is optimised away.
 #include "mdx_internal.cuh"
+#include "pair_math.cuh"
 
 namespace {
 
@@ -67,7 +68,38 @@ double run(int iters) {
   return best;
 }
 
+__global__ void k_pair_math(int n, const double *y, const double *d, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = exp_neg(y[i]);
+  out[n + i] = exp(-y[i]);
+  out[2 * n + i] = rcp_nr(d[i]);
+  out[3 * n + i] = 1.0 / d[i];
+}
+
 }  // namespace
+
+extern "C" int mdx_probe_pair_math(int n, const double *y, const double *d, double *own_exp,
+                                   double *lib_exp, double *own_rcp, double *lib_rcp) {
+  if (n <= 0 || !y || !d || !own_exp || !lib_exp || !own_rcp || !lib_rcp) return MDX_ERR_ARG;
+  double *buf = nullptr;
+  const size_t nb = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&buf, 6 * nb) != cudaSuccess) return MDX_ERR_NOMEM;
+  int rc = MDX_OK;
+  double *dy = buf, *dd = buf + n, *out = buf + 2 * (size_t)n;
+  if (cudaMemcpy(dy, y, nb, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dd, d, nb, cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = MDX_ERR_CUDA;
+  } else {
+    k_pair_math<<<(n + 255) / 256, 256>>>(n, dy, dd, out);
+    double *dst[4] = {own_exp, lib_exp, own_rcp, lib_rcp};
+    for (int k = 0; k < 4 && rc == MDX_OK; ++k)
+      if (cudaMemcpy(dst[k], out + (size_t)k * n, nb, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = MDX_ERR_CUDA;
+  }
+  cudaFree(buf);
+  return rc;
+}
 
 extern "C" int mdx_probe_fma_peak(int fp64, double *tflops) {
   if (!tflops) return MDX_ERR_ARG;

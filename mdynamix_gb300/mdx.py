@@ -45,6 +45,21 @@ def probe_fma_peak(fp64: bool) -> float:
     return v.value
 
 
+def probe_pair_math(y, d):
+    """The FP64 pair sweeps' exp(-y) and 1/d beside the CUDA library's, on
+    the current GPU: (own_exp, lib_exp, own_rcp, lib_rcp)."""
+    L = load()
+    y = np.ascontiguousarray(y, np.float64)
+    d = np.ascontiguousarray(d, np.float64)
+    n = len(y)
+    assert len(d) == n
+    out = [np.zeros(n) for _ in range(4)]
+    rc = L.mdx_probe_pair_math(n, _fp(y), _fp(d), *[_fp(a) for a in out])
+    if rc != 0:
+        raise MdxError(rc, "probe failed")
+    return tuple(out)
+
+
 class MdxError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
@@ -110,6 +125,7 @@ def load():
     L.mdx_set_timers.argtypes = [P, C.c_int]
     L.mdx_get_timers.argtypes = [P, F64P, C.POINTER(C.c_int64)]
     L.mdx_probe_fma_peak.argtypes = [C.c_int, F64P]
+    L.mdx_probe_pair_math.argtypes = [C.c_int, F64P, F64P, F64P, F64P, F64P, F64P]
     from .abi import MdxPimdParams, MdxPimdRecord
     L.mdx_pimd_open.argtypes = [C.POINTER(P), C.POINTER(MdxPimdParams), C.POINTER(P)]
     L.mdx_pimd_close.argtypes = [P]

@@ -262,3 +262,25 @@ def test_pullback_matches_oracle():
     (gx, gy, gz, *_), _ = g2.get_state()
     (ox, oy, oz, *_), _ = o2.get_state()
     assert max(np.abs(gx - ox).max(), np.abs(gz - oz).max()) < 1e-9
+
+
+# --------------------------------------------------- FP64 sweep math --
+def test_pair_math_against_library():
+    """The FP64 pair sweeps' exp(-y) (Tang's table method) and 1/d (FP32
+    seed + two Newton steps) against the CUDA library's exp and division on
+    the device: within 4 units in the last place over the sweeps' ranges
+    (y = (alpha r)^2 up to 40 and beyond to the 700 clamp, d = 1 + p alpha r
+    in [1, 4])."""
+    from mdynamix_gb300.mdx import probe_pair_math
+    rng = np.random.default_rng(3)
+    y = np.concatenate([np.linspace(0.0, 40.0, 200001), rng.uniform(0, 700, 20000),
+                        [0.0, 5e-324, 1e-300, 1e-17, 1e-9, 700.0, 699.999]])
+    d = np.concatenate([np.linspace(1.0, 4.0, 200001), rng.uniform(1, 1e6, 20000),
+                        [1.0, 1.0 + 2.0 ** -52, 2.0, 2.0 - 2.0 ** -52, 3.0, 1e6, 7.0]])
+    own_e, lib_e, own_r, lib_r = probe_pair_math(y, d)
+    ulp = 2.0 ** -52
+    assert np.all(np.abs(own_e - lib_e) <= 4 * ulp * lib_e)
+    assert np.all(np.abs(own_r - lib_r) <= 4 * ulp * lib_r)
+    # and against numpy's exp / division (the host's libm)
+    assert np.all(np.abs(own_e - np.exp(-y)) <= 4 * ulp * np.exp(-y))
+    assert np.all(np.abs(own_r - 1.0 / d) <= 4 * ulp / d)
