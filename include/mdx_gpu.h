@@ -339,6 +339,24 @@ typedef struct {
   int32_t sfac_ordered, list_mode, graphs, nkv;
 } mdx_path_info;
 int mdx_get_path_info(const mdx_ctx *ctx, mdx_path_info *out);
+
+/* Work split of the mixed pair sweeps: threads per owner atom of the short
+ * rows (tpo_short: 2, 4 or 8) and of the long rows (tpo_long: 8, 16 or 32).
+ * No counterpart in the reference (a launch-shape choice of this library).
+ * By default a context takes the choice of the tuning table built into the
+ * library (written by mdynamix_gb300/autotune.py from timings of each split
+ * on a GB300, keyed by system size and mean row length), fixed at its first
+ * pair sweep from the sizes alone, so equal systems always run the same
+ * split.  The split changes the FP32 lane partials before the fixed-point
+ * sums, so forces differ between splits at the mixed path's rounding level,
+ * not beyond.  mdx_set_tuning overrides it (NULL: back to the table) and
+ * drops the captured step graphs; set it before a PIMD ensemble is opened
+ * on the context.  source: 1 table, 2 mdx_set_tuning. */
+typedef struct {
+  int32_t tpo_short, tpo_long, source, reserved;
+} mdx_tuning;
+int mdx_set_tuning(mdx_ctx *ctx, const mdx_tuning *t);
+int mdx_get_tuning(mdx_ctx *ctx, mdx_tuning *out);
 /* Diagnostic: the CUDA runtime error recorded for the calling thread and not
  * yet consumed (0 = none), without clearing it. */
 int mdx_pending_cuda_error(void);

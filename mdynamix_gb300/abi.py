@@ -137,6 +137,14 @@ class MdxPathInfo(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class MdxTuning(C.Structure):
+    """mdx_tuning: threads per owner atom of the mixed pair sweeps."""
+    _fields_ = [(n, C.c_int32) for n in ("tpo_short", "tpo_long", "source", "reserved")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_[:3]}
+
+
 class MdxPullback(C.Structure):
     """mdx_pullback: PULLBACK's drag, wells and external field."""
     _fields_ = [("ldrag", C.c_int32), ("ldragt", C.c_int32 * NTPS), ("fdrag", C.c_double * NTPS),

@@ -11,6 +11,8 @@
 
 #include <algorithm>
 
+#include <cstring>
+
 #include "mdx_internal.cuh"
 
 namespace {
@@ -212,7 +214,7 @@ constexpr int KD_MAXA = 4;  // atoms per molecule of the register path below
 // 463-563) and the fixed-point mirror, all in the order the separate
 // kernels use.  hfix (mixed path): the previous short step's fast forces are read
 // as fixed point, so that step needs no fold to FP64.
-__global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
+__device__ __forceinline__ void kick_drift_com_body(int m, int nop, const int *__restrict__ mol_first,
                                  const int *__restrict__ mol_nat,
                                  const int *__restrict__ mol_type,
                                  const int4 *__restrict__ ainfo, MoveConst mv,
@@ -231,7 +233,6 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
   // ibs: 2^32 / box per axis (host-computed: no FP64 division per thread);
   // posi set (mixed path): centre of mass by the reciprocal mass, the
   // fixed-point mirror refreshed, and (posc set) its cell-order copy
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
   if (posi && na <= KD_MAXA) {
@@ -373,6 +374,28 @@ __global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
   }
 }
 
+__global__ void k_kick_drift_com(int nop, const int *__restrict__ mol_first,
+                                 const int *__restrict__ mol_nat,
+                                 const int *__restrict__ mol_type,
+                                 const int4 *__restrict__ ainfo, MoveConst mv,
+                                 MolConst mc, double htsteb, double tsteb, int prev,
+                                 const double *__restrict__ hx, const double *__restrict__ hy,
+                                 const double *__restrict__ hz,
+                                 const unsigned long long *__restrict__ hfix, int n,
+                                 double inv, const double *__restrict__ massdi,
+                                 const double *__restrict__ amass, double *__restrict__ vx,
+                                 double *__restrict__ vy, double *__restrict__ vz,
+                                 dbl4 *__restrict__ pos, double *__restrict__ X,
+                                 double *__restrict__ Y, double *__restrict__ Z,
+                                 double bx, double by, double bz, double3 ibs,
+                                 int4 *__restrict__ posi, const int *__restrict__ pinfo,
+                                 int4 *__restrict__ posc, const int *__restrict__ slot_of) {
+  kick_drift_com_body(blockIdx.x * blockDim.x + threadIdx.x, nop, mol_first, mol_nat, mol_type,
+                      ainfo, mv, mc, htsteb, tsteb, prev, hx, hy, hz, hfix, n, inv, massdi,
+                      amass, vx, vy, vz, pos, X, Y, Z, bx, by, bz, ibs, posi, pinfo, posc,
+                      slot_of);
+}
+
 // SULTAN 1.3.1-1.3.2.2 (mdstep.f:89-113): OX = SX, V += TSTEP F,
 // SX += TSTEP V MASSDI.
 // save != 0: the new positions also go to fx/fy/fz (SHEJK's copy of the
@@ -441,11 +464,13 @@ __device__ __forceinline__ void kick_atom(const KickArgs &k, int i, double &x, d
   }
 }
 
-template <int NT, typename R, bool KICK>
-__global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
-                         int ntypes, const double *__restrict__ massdi,
-                         double *vx, double *vy, double *vz, double *ekacc,
-                         double *part, unsigned *ctr, KickArgs pre, KickArgs post) {
+template <int NT, typename R, bool KICK, bool ROW>
+__device__ __forceinline__ void getemp_body(int n, const int4 *__restrict__ ainfo,
+                                            const MoveConst &mv, int ntypes,
+                                            const double *__restrict__ massdi, double *vx,
+                                            double *vy, double *vz, double *ekacc, double *part,
+                                            unsigned *ctr, const KickArgs &pre,
+                                            const KickArgs &post) {
   R e[NT + 4];
 #pragma unroll
   for (int k = 0; k < NT + 4; ++k) e[k] = R(0);
@@ -489,12 +514,21 @@ __global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
   if (sizeof(R) == sizeof(double)) {
 #pragma unroll
     for (int k = 0; k < NT + 4; ++k) ed[k] = (double)e[k];
-    block_add_core<NT + 4>(ed, dst, part, ctr);
+    block_add_core<NT + 4, false, ROW>(ed, dst, part, ctr);
   } else {
 #pragma unroll
     for (int k = 0; k < NT + 4; ++k) ed[k] = (double)warp_sumf((float)e[k]);
-    block_add_core<NT + 4, true>(ed, dst, part, ctr);
+    block_add_core<NT + 4, true, ROW>(ed, dst, part, ctr);
   }
+}
+
+template <int NT, typename R, bool KICK>
+__global__ void k_getemp(int n, const int4 *__restrict__ ainfo, MoveConst mv,
+                         int ntypes, const double *__restrict__ massdi,
+                         double *vx, double *vy, double *vz, double *ekacc,
+                         double *part, unsigned *ctr, KickArgs pre, KickArgs post) {
+  getemp_body<NT, R, KICK, false>(n, ainfo, mv, ntypes, massdi, vx, vy, vz, ekacc, part, ctr,
+                                  pre, post);
 }
 
 // Device scratch of SCALING between stages.
@@ -827,8 +861,9 @@ __device__ __forceinline__ void copy_words(void *dst, const void *src, int bytes
 // each of its loads would be a round trip.  The block brings the scratch,
 // the thermostat state and the scalars into shared memory at once, thread 0
 // runs the stages there, and the block writes the first two back.
-__global__ void k_scal_list(StageList L, ScalConst c, ScalScratch *ss, mdx_thermo *th,
-                            const mdx_scalars *s, int *err) {
+__device__ __forceinline__ void scal_list_body(const StageList &L, const ScalConst &c,
+                                               ScalScratch *ss, mdx_thermo *th,
+                                               const mdx_scalars *s, int *err) {
   __shared__ ScalScratch ss_s;
   __shared__ mdx_thermo th_s;
   __shared__ mdx_scalars s_s;
@@ -844,6 +879,69 @@ __global__ void k_scal_list(StageList L, ScalConst c, ScalScratch *ss, mdx_therm
   __syncthreads();
   copy_words(ss, &ss_s, sizeof(ScalScratch));
   copy_words(th, &th_s, sizeof(mdx_thermo));
+}
+
+__global__ void k_scal_list(StageList L, ScalConst c, ScalScratch *ss, mdx_thermo *th,
+                            const mdx_scalars *s, int *err) {
+  scal_list_body(L, c, ss, th, s, err);
+}
+
+// ------------------------------------------------ bead ensembles (PIMD) ---
+// The integrator passes of every bead of a PIMD ensemble in one launch each:
+// grid row blockIdx.y (the stage blocks: blockIdx.x) is the bead, its arrays
+// come from a device table.  A bead's blocks, per-atom operations and sums
+// are those of the single-context launches, so the values are the same.
+struct BeadMove {
+  dbl4 *pos;
+  double *vx, *vy, *vz;
+  const double *f[3][3];  // forces H, G, F; x, y, z
+  double *X, *Y, *Z;
+  int4 *posi, *posc;
+  const int *slot_of;
+  double *part;
+  unsigned *ctr;
+  ScalScratch *ss;
+  mdx_thermo *th;
+  const mdx_scalars *sc;
+  int *err;
+};
+
+struct KickW {  // KickSpec by force index, resolved per bead on the device
+  int w1, w2, vs;
+  double h1, h2;
+};
+
+__device__ __forceinline__ KickArgs bead_kick(const BeadMove &b, const KickW &k) {
+  KickArgs a{};
+  a.h1 = k.h1;
+  a.h2 = k.h2;
+  if (k.w1) {
+    a.ax = b.f[k.w1 - 1][0];
+    a.ay = b.f[k.w1 - 1][1];
+    a.az = b.f[k.w1 - 1][2];
+  }
+  if (k.w2) {
+    a.bx = b.f[k.w2 - 1][0];
+    a.by = b.f[k.w2 - 1][1];
+    a.bz = b.f[k.w2 - 1][2];
+  }
+  a.vs = k.vs ? b.ss->vscale : nullptr;
+  return a;
+}
+
+template <int NT, typename R, bool KICK>
+__global__ void k_getemp_beads(int n, const int4 *__restrict__ ainfo, MoveConst mv, int ntypes,
+                               const double *__restrict__ massdi,
+                               const BeadMove *__restrict__ beads, KickW pre, KickW post) {
+  const BeadMove &b = beads[blockIdx.y];
+  const KickArgs a = bead_kick(b, pre), c = bead_kick(b, post);
+  getemp_body<NT, R, KICK, true>(n, ainfo, mv, ntypes, massdi, b.vx, b.vy, b.vz, b.ss->ekacc,
+                                 b.part, b.ctr, a, c);
+}
+
+__global__ void k_scal_list_beads(StageList L, ScalConst c, const BeadMove *__restrict__ beads) {
+  const BeadMove &b = beads[blockIdx.x];
+  scal_list_body(L, c, b.ss, b.th, b.sc, b.err);
 }
 
 // Velocity (and position) scaling of the SCALING stages.
@@ -1305,6 +1403,23 @@ struct StageQ {
   }
 };
 
+// DOUBLE-style drift of every bead (no kick before it: htsteb applies to H)
+__global__ void k_kick_drift_com_beads(int nop, const int *__restrict__ mol_first,
+                                       const int *__restrict__ mol_nat,
+                                       const int *__restrict__ mol_type,
+                                       const int4 *__restrict__ ainfo, MoveConst mv, MolConst mc,
+                                       double htsteb, double tsteb, int n,
+                                       const double *__restrict__ massdi,
+                                       const double *__restrict__ amass, double bx, double by,
+                                       double bz, double3 ibs, const int *__restrict__ pinfo,
+                                       const BeadMove *__restrict__ beads) {
+  const BeadMove &b = beads[blockIdx.y];
+  kick_drift_com_body(blockIdx.x * blockDim.x + threadIdx.x, nop, mol_first, mol_nat, mol_type,
+                      ainfo, mv, mc, htsteb, tsteb, 0, b.f[0][0], b.f[0][1], b.f[0][2], nullptr,
+                      n, 0.0, massdi, amass, b.vx, b.vy, b.vz, b.pos, b.X, b.Y, b.Z, bx, by, bz,
+                      ibs, b.posi, pinfo, b.posc, b.slot_of);
+}
+
 static KickArgs kick_args(mdx_ctx *ctx, const KickSpec &k) {
   DevData &d = ctx->dv;
   KickArgs a{};
@@ -1659,6 +1774,102 @@ int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, b
       ctx->mixed() ? d.posi : nullptr, d.pinfo,
       ctx->mixed() && ctx->have_lists ? d.cell_pos : nullptr, d.slot_of);
   MDX_LAUNCHED(ctx);
+  return MDX_OK;
+}
+
+// ------------------------------------------ bead ensembles: host side ---
+size_t bead_move_bytes() { return sizeof(BeadMove); }
+
+// One bead's entry of the device table (pointers only; written once the
+// bead's lists exist, they stay valid for the context's life).
+void bead_move_fill(mdx_ctx *ctx, void *out) {
+  DevData &d = ctx->dv;
+  BeadMove b{};
+  b.pos = d.pos;
+  b.vx = d.vx;
+  b.vy = d.vy;
+  b.vz = d.vz;
+  const double *f[3][3] = {{d.hx, d.hy, d.hz}, {d.gx, d.gy, d.gz}, {d.fx, d.fy, d.fz}};
+  for (int w = 0; w < 3; ++w)
+    for (int a = 0; a < 3; ++a) b.f[w][a] = f[w][a];
+  b.X = d.X;
+  b.Y = d.Y;
+  b.Z = d.Z;
+  b.posi = ctx->mixed() ? d.posi : nullptr;
+  b.posc = ctx->mixed() && ctx->have_lists ? d.cell_pos : nullptr;
+  b.slot_of = d.slot_of;
+  b.part = d.red_part;
+  b.ctr = d.red_ctr;
+  b.ss = reinterpret_cast<ScalScratch *>(d.scal_scratch);
+  b.th = d.th;
+  b.sc = d.sc;
+  b.err = d.err;
+  std::memcpy(out, &b, sizeof b);
+}
+
+static KickW kick_w(const KickSpec &k) {
+  KickW w{};
+  w.w1 = k.w1;
+  w.w2 = k.w2;
+  w.vs = k.vscale ? 1 : 0;
+  w.h1 = k.h1;
+  w.h2 = k.h2;
+  return w;
+}
+
+// kick(s), GETEMP, kick(s) and the ST_GETEMP fold of all P beads (c0: any
+// bead; the beads share sizes, topology and parameters), on stream st.
+int launch_getemp_beads(mdx_ctx *c0, int P, const void *table, cudaStream_t st,
+                        const KickSpec &pre, const KickSpec &post) {
+  MDX_TIMER(c0, MDX_T_MOVE);
+  DevData &d = c0->dv;
+  const int nt = c0->d.ntypes;
+  const KickW a = kick_w(pre), b = kick_w(post);
+  const bool kick = a.w1 || b.w1 || a.vs;
+  const BeadMove *tab = static_cast<const BeadMove *>(table);
+  const dim3 grid(c0->nsm, P);
+#define GB_K(NT, R, K)                                                                   \
+  k_getemp_beads<NT, R, K><<<grid, 256, 0, st>>>(d.n, d.ainfo, move_const(c0), nt, d.massdi, \
+                                                 tab, a, b)
+#define GB(NT)                                   \
+  do {                                           \
+    if (c0->mixed()) {                           \
+      if (kick) GB_K(NT, float, true);           \
+      else GB_K(NT, float, false);               \
+    } else {                                     \
+      if (kick) GB_K(NT, double, true);          \
+      else GB_K(NT, double, false);              \
+    }                                            \
+  } while (0)
+  if (nt <= 1) GB(1);
+  else if (nt <= 2) GB(2);
+  else if (nt <= 4) GB(4);
+  else GB(MDX_NT);
+#undef GB
+#undef GB_K
+  MDX_LAUNCHED(c0);
+  StageList L{};
+  L.n = 1;
+  L.st[0] = ST_GETEMP;
+  k_scal_list_beads<<<P, 128, 0, st>>>(L, scal_const(c0), tab);
+  MDX_LAUNCHED(c0);
+  return MDX_OK;
+}
+
+// drift (after a kick of htsteb on H), GETCOM and the coordinate mirrors of
+// all P beads, on stream st
+int launch_kick_drift_com_beads(mdx_ctx *c0, int P, const void *table, cudaStream_t st,
+                                double htsteb, double tsteb) {
+  MDX_TIMER(c0, MDX_T_MOVE);
+  DevData &d = c0->dv;
+  const dim3 grid((d.nop + 127) / 128, P);
+  k_kick_drift_com_beads<<<grid, 128, 0, st>>>(
+      d.nop, d.mol_first, d.mol_nat, d.mol_type, d.ainfo, move_const(c0), mol_const(c0), htsteb,
+      tsteb, d.n, d.massdi, d.amass, c0->boxl, c0->boyl, c0->bozl,
+      make_double3(4294967296.0 * (1.0 / c0->boxl), 4294967296.0 * (1.0 / c0->boyl),
+                   4294967296.0 * (1.0 / c0->bozl)),
+      d.pinfo, static_cast<const BeadMove *>(table));
+  MDX_LAUNCHED(c0);
   return MDX_OK;
 }
 

@@ -1429,6 +1429,31 @@ int mdx_get_path_info(const mdx_ctx *ctx, mdx_path_info *out) {
   return MDX_OK;
 }
 
+int mdx_set_tuning(mdx_ctx *ctx, const mdx_tuning *t) {
+  if (!ctx) return MDX_ERR_ARG;
+  if (t) {
+    const bool ok_s = t->tpo_short == 2 || t->tpo_short == 4 || t->tpo_short == 8;
+    const bool ok_l = t->tpo_long == 8 || t->tpo_long == 16 || t->tpo_long == 32;
+    if (!ok_s || !ok_l) {
+      ctx->err = "tuning: tpo_short must be 2, 4 or 8 and tpo_long 8, 16 or 32";
+      return MDX_ERR_ARG;
+    }
+    ctx->tune = mdx_tuning{t->tpo_short, t->tpo_long, 2, 0};
+  } else {
+    ctx->tune = mdx_tuning{};
+  }
+  ctx->drop_graphs();  // the step graphs hold the sweeps' launch shapes
+  return MDX_OK;
+}
+
+int mdx_get_tuning(mdx_ctx *ctx, mdx_tuning *out) {
+  if (!ctx || !out) return MDX_ERR_ARG;
+  RC(require(ctx, true, true, true));
+  resolve_tuning(ctx);
+  *out = ctx->tune;
+  return MDX_OK;
+}
+
 int mdx_pool_usage(size_t *used_bytes, size_t *reserved_bytes) {
   int dev = 0;
   cudaMemPool_t pool;

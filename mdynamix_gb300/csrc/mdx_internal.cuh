@@ -72,6 +72,11 @@ struct PairConst {
   float rc2f;
 };
 
+// Threads per owner atom of the mixed pair sweeps when nothing else is chosen.
+constexpr int TPO_SHORT_DEFAULT = 4;
+constexpr int TPO_LONG_DEFAULT = 32;
+void resolve_tuning(mdx_ctx *ctx);  // pair.cu: the tuning table's choice, once
+
 // Cell grid used by the list build.
 struct CellGrid {
   int nx, ny, nz, ncell;
@@ -299,6 +304,9 @@ struct mdx_ctx {
   int64_t glaunches[8] = {};
   bool use_graphs = true;
   bool averaging = false;  // mdx_set_averaging: LAVER forces + statistics every long step
+  // threads per owner atom of the mixed pair sweeps (0: not chosen yet;
+  // source 1: the tuning table, 2: mdx_set_tuning)
+  mdx_tuning tune{};
   bool pullback = false;   // mdx_set_pullback: drag, wells or field on
   mdx_pullback pb{};       // its constants (array pointers not kept)
   void drop_graphs() {
@@ -435,7 +443,9 @@ __device__ __forceinline__ float warp_sumf(float v) {
 // adds with atomicAdd (order-dependent in the last bit).
 // WARP_DONE: the caller has already summed each value over its warp (lane 0
 // holds the warp totals), e.g. in FP32 for a few terms a thread.
-template <int NV, bool WARP_DONE = false>
+// ROW: blocks of one grid row (blockIdx.y) reduce together, each row with its
+// own part / ctr (batched launches over several systems).
+template <int NV, bool WARP_DONE = false, bool ROW = false>
 __device__ __forceinline__ void block_add_core(double (&v)[NV], double *const *dst,
                                                double *part, unsigned *ctr) {
   __shared__ double sh[32][NV];
@@ -451,8 +461,8 @@ __device__ __forceinline__ void block_add_core(double (&v)[NV], double *const *d
     for (int k = 0; k < NV; ++k) sh[wid][k] = v[k];
   }
   __syncthreads();
-  const unsigned nblk = gridDim.x * gridDim.y;
-  const unsigned blin = blockIdx.y * gridDim.x + blockIdx.x;
+  const unsigned nblk = ROW ? gridDim.x : gridDim.x * gridDim.y;
+  const unsigned blin = ROW ? blockIdx.x : blockIdx.y * gridDim.x + blockIdx.x;
   // the block's total of value k is formed by warp k % nw (the same sums in
   // the same order as one warp doing all of them, NV times shorter)
   for (int k = wid; k < NV; k += nw) {
@@ -641,6 +651,14 @@ struct KickSpec {
   bool vscale = false;  // SCALING's per-type velocity factor first (GETEMP passes only)
 };
 int launch_getemp_kick(mdx_ctx *ctx, const KickSpec &pre, const KickSpec &post);
+// PIMD bead ensembles: one device table entry per bead, then the integrator
+// passes of all beads in one launch each (integrate.cu)
+size_t bead_move_bytes();
+void bead_move_fill(mdx_ctx *ctx, void *out);
+int launch_getemp_beads(mdx_ctx *c0, int P, const void *table, cudaStream_t st,
+                        const KickSpec &pre = {}, const KickSpec &post = {});
+int launch_kick_drift_com_beads(mdx_ctx *c0, int P, const void *table, cudaStream_t st,
+                                double htsteb, double tsteb);
 int launch_vira(mdx_ctx *ctx, int from_viran);
 // nblist.cu
 int launch_mirror_f32(mdx_ctx *ctx);

@@ -19,6 +19,7 @@
 
 #include "mdx_internal.cuh"
 #include "pair_math.cuh"
+#include "tune_table.cuh"
 
 namespace {
 
@@ -254,14 +255,13 @@ __global__ void k_wir_fix(int n, const dbl4 *__restrict__ pos,
 
 // ---------------------------------------------------------------- mixed ---
 constexpr int PAIR32_BLOCKS = 6;  // resident blocks per SM the register cap aims at
-constexpr int SPO = 4;  // threads per owner atom of the short sweep (adjacent lanes; 4: 5 % faster than 2)
 
 __device__ __forceinline__ float idiff(int a, int b, float s) { return fixdiff(a, b, s); }
 
 // Register cap for occupancy: the sweeps wait on gathered neighbour records,
 // and more resident warps hide more of that (6 blocks of 256: 40 registers;
 // measured 12 % faster than the uncapped 44-64 registers).
-template <bool SHORT, bool SPLIT, bool ENER>
+template <bool SHORT, bool SPLIT, bool ENER, int TPO>
 __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     int n, const int4 *__restrict__ posi, const int4 *__restrict__ posn,
     const float4 *__restrict__ stab,
@@ -276,14 +276,14 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
     __syncthreads();
   }
-  // short rows (about 50 entries): SPO threads per owner atom over its tiled
-  // row (list_slot; entry k of 32 atoms in one 128-byte line), even and odd
-  // entries; long rows (several hundred entries): warp per owner atom, lanes
-  // stride the row
+  // TPO adjacent lanes per owner atom stride its row: short rows (about 50
+  // entries, tiled: list_slot puts entry k of 32 atoms in one 128-byte line)
+  // take a few lanes, long rows (several hundred entries) up to a warp.  The
+  // split is a tuning choice (tune_table.cuh); the forces' integer sums do
+  // not depend on it, the FP32 lane partials before them do.
   const int lane = threadIdx.x & 31;
-  const int i = SHORT ? (blockIdx.x * blockDim.x + threadIdx.x) / SPO
-                      : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int k0 = SHORT ? lane % SPO : lane, kstep = SHORT ? SPO : 32;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / TPO;
+  const int k0 = lane % TPO, kstep = TPO;
   long long tot[P_NSLOT];
 #pragma unroll
   for (int k = 0; k < P_NSLOT; ++k) tot[k] = 0;
@@ -433,32 +433,18 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     qx = f2ll_rn(fxa * fsc.scalef);
     qy = f2ll_rn(fya * fsc.scalef);
     qz = f2ll_rn(fza * fsc.scalef);
-    if (!SHORT) {  // the whole warp shares the owner: uniform branch
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        qx += __shfl_xor_sync(0xffffffffu, qx, o);
-        qy += __shfl_xor_sync(0xffffffffu, qy, o);
-        qz += __shfl_xor_sync(0xffffffffu, qz, o);
-      }
-      if (lane == 0) {
-        ffix[i] = (unsigned long long)qx;
-        ffix[n + i] = (unsigned long long)qy;
-        ffix[2 * n + i] = (unsigned long long)qz;
-      }
-    }
   }
-  if (SHORT) {  // the owner's threads are adjacent lanes; every lane takes part
+  // the owner's lanes are adjacent; every lane of the warp takes part
 #pragma unroll
-    for (int o = 1; o < SPO; o <<= 1) {
-      qx += __shfl_xor_sync(0xffffffffu, qx, o);
-      qy += __shfl_xor_sync(0xffffffffu, qy, o);
-      qz += __shfl_xor_sync(0xffffffffu, qz, o);
-    }
-    if (i < n && lane % SPO == 0) {
-      ffix[i] = (unsigned long long)qx;
-      ffix[n + i] = (unsigned long long)qy;
-      ffix[2 * n + i] = (unsigned long long)qz;
-    }
+  for (int o = 1; o < TPO; o <<= 1) {
+    qx += __shfl_xor_sync(0xffffffffu, qx, o);
+    qy += __shfl_xor_sync(0xffffffffu, qy, o);
+    qz += __shfl_xor_sync(0xffffffffu, qz, o);
+  }
+  if (i < n && lane % TPO == 0) {
+    ffix[i] = (unsigned long long)qx;
+    ffix[n + i] = (unsigned long long)qy;
+    ffix[2 * n + i] = (unsigned long long)qz;
   }
   if (ENER) {
 #pragma unroll
@@ -564,6 +550,7 @@ __global__ void k_pack_lj(int nn, const float *__restrict__ f, float2 *__restric
 // reads them, forces.f:36-49).
 int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   DevData &d = ctx->dv;
+  if (ctx->mixed() && !ctx->tune.tpo_short) resolve_tuning(ctx);
   const int T = 256, WPB = T / 32;
   const int grid = (d.n + WPB - 1) / WPB;
   const int *cnt = shrt ? d.ns_cnt : d.nl_cnt;
@@ -595,21 +582,39 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
-    const int grid32 = shrt ? (SPO * d.n + T - 1) / T : grid;  // short: SPO threads per atom
-#define LP32(S, P)                                                                \
-  if (ener) k_pair32<S, P, true><<<grid32, T, 0, ctx->stream>>>(                  \
-      d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
-      ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
-      d.Y, d.Z, escale, slots, split_buf);                                        \
-  else k_pair32<S, P, false><<<grid32, T, 0, ctx->stream>>>(                      \
+    // threads per owner atom: the context's tuning (the energy-split sweeps
+    // of RECINT keep the defaults)
+    const int tpo = split ? (shrt ? TPO_SHORT_DEFAULT : TPO_LONG_DEFAULT)
+                          : (shrt ? ctx->tune.tpo_short : ctx->tune.tpo_long);
+    const int grid32 = (int)(((long long)tpo * d.n + T - 1) / T);
+#define LP32(S, P, E, K)                                                          \
+  k_pair32<S, P, E, K><<<grid32, T, 0, ctx->stream>>>(                            \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
       d.Y, d.Z, escale, slots, split_buf)
-    if (shrt) {
-      if (split) { LP32(true, true); } else { LP32(true, false); }
+#define LP32E(S, K)                      \
+  do {                                   \
+    if (ener) LP32(S, false, true, K);   \
+    else LP32(S, false, false, K);       \
+  } while (0)
+    if (split) {
+      if (shrt) {
+        if (ener) LP32(true, true, true, TPO_SHORT_DEFAULT);
+        else LP32(true, true, false, TPO_SHORT_DEFAULT);
+      } else {
+        if (ener) LP32(false, true, true, TPO_LONG_DEFAULT);
+        else LP32(false, true, false, TPO_LONG_DEFAULT);
+      }
+    } else if (shrt) {
+      if (tpo == 2) LP32E(true, 2);
+      else if (tpo == 8) LP32E(true, 8);
+      else LP32E(true, 4);
     } else {
-      if (split) { LP32(false, true); } else { LP32(false, false); }
+      if (tpo == 8) LP32E(false, 8);
+      else if (tpo == 16) LP32E(false, 16);
+      else LP32E(false, 32);
     }
+#undef LP32E
 #undef LP32
     MDX_LAUNCHED(ctx);
     if (ener) {
@@ -625,7 +630,27 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   return MDX_OK;
 }
 
+template <int N>
+int tune_pick(const TuneCell (&cells)[N], int n, double row, int dflt) {
+  for (const TuneCell &c : cells)
+    if (n <= c.max_atoms && row <= c.max_row) return c.tpo;
+  return dflt;
+}
+
 }  // namespace
+
+// The tuning table's split for this system, from its sizes alone: atoms and
+// the mean full-row lengths rho (4/3) pi r^3 of the short and long lists.
+void resolve_tuning(mdx_ctx *ctx) {
+  if (ctx->tune.tpo_short) return;
+  const double vol = ctx->boxl * ctx->boyl * ctx->bozl;
+  const double rho = vol > 0 ? ctx->dv.n / vol : 0.0, c = 4.0 / 3.0 * 3.141592653589793;
+  const double rs = ctx->p.rshort, rl = ctx->p.rcut + ctx->p.rskin;
+  const double row_s = rho * c * rs * rs * rs, row_l = rho * c * (rl * rl * rl - rs * rs * rs);
+  ctx->tune.tpo_short = tune_pick(TUNE_SHORT, ctx->dv.n, row_s, TPO_SHORT_DEFAULT);
+  ctx->tune.tpo_long = tune_pick(TUNE_LONG, ctx->dv.n, row_l, TPO_LONG_DEFAULT);
+  ctx->tune.source = 1;
+}
 
 // The interleaved FP32 (A6, B12) tables of the mixed sweeps, from the FP32
 // tables (after the topology upload and every RECINT).

@@ -3,10 +3,12 @@
 //
 // The reference runs one bead per MPI rank; every short step the ranks
 // exchange coordinates (ring springs) and kinetic energies (bead
-// thermostats).  Here the NBEADS contexts stay on one GPU.  A long step is
-// a fork/join graph: each bead's own work (kicks, drift, GETCOM, lists,
-// forces) runs on the bead's stream, concurrently with the other beads; the
-// two cross-bead operations run on the PIMD stream between joins:
+// thermostats).  Here the NBEADS contexts stay on one GPU.  The integrator
+// passes of all beads run as one launch each on the ensemble's stream
+// (grid row = bead, the bead's arrays from a device table:
+// launch_getemp_beads, launch_kick_drift_com_beads); each bead's lists and
+// forces run on the bead's own stream, concurrently with the other beads
+// (fork/join); the two cross-bead operations run on the ensemble's stream:
 //   k_pi_nose     BEADNOSE: per atom, kinetic energy summed over beads
 //                 drives a Nose-Hoover chain shared by the atom's beads;
 //   k_pi_springs  forces / NBEADS, then PIFORCES: springs to bead b-1 and
@@ -14,11 +16,11 @@
 //                 (the reference sends them as REAL*4, pimd.f:450-486).
 // Per long step (NFREQ short steps, no NVT/NPT scaling: PI_SCALING only
 // evaluates GETEMP then):
-//   fork [GETEMP, V += HTSTEP G, V += HTSTEB H] join, nose
+//   [GETEMP, V += HTSTEP G, V += HTSTEB H], nose
 //   for each short step:
-//     fork [drift, GETCOM, CHCNB?, SLFORCES+FFORCES | FFORCES] join, springs
-//     fork [V += HTSTEB H, GETEMP, (next: V += HTSTEB H) |
-//           (last: V += HTSTEP G, GETEMP)] join, (nose | record)
+//     [drift, GETCOM], fork [CHCNB?, SLFORCES+FFORCES | FFORCES] join, springs
+//     [V += HTSTEB H, GETEMP, (next: V += HTSTEB H) | (last: V += HTSTEP G)],
+//     (nose | GETEMP, record)
 // Long steps are captured once (with and without the list rebuild) and
 // replayed.  Spring energies and virials are summed per bead in block order
 // (deterministic).
@@ -202,6 +204,8 @@ struct mdx_pimd {
   int *rec_ctr = nullptr;
   int rec_cap = 0;
   cudaGraphExec_t g[2] = {nullptr, nullptr};
+  void *mv_tab = nullptr;            // [P] bead table of the batched integrator passes
+  std::vector<unsigned char> mv_host;  // its host image
   std::string err;
   int nblk() const { return (n + PI_THREADS - 1) / PI_THREADS; }
 };
@@ -281,24 +285,33 @@ int prologue(mdx_pimd *pi) {
   return MDX_OK;
 }
 
-// One long step (pimd.f:84-194).
+// The bead table of the batched integrator passes (pointers only: written
+// before a run, once every bead has its lists).
+int fill_bead_table(mdx_pimd *pi) {
+  const size_t b = bead_move_bytes();
+  pi->mv_host.resize(b * pi->P);
+  for (int k = 0; k < pi->P; ++k) bead_move_fill(pi->beads[k], pi->mv_host.data() + b * k);
+  PI_CUDA(ctx_copy(pi->stream, pi->mv_tab, pi->mv_host.data(), b * pi->P, cudaMemcpyHostToDevice));
+  return MDX_OK;
+}
+
+// One long step (pimd.f:84-194).  The integrator passes of all beads run as
+// one launch each on the ensemble's stream (kicks and GETEMP share a pass
+// over the atoms; the drift carries GETCOM and the coordinate mirrors): the
+// same operations in the same order as per-bead kernels.  The forces run
+// per bead, forked across the bead streams.
 int long_step(mdx_pimd *pi, int mstep) {
   mdx_ctx *c0 = pi->beads[0];
   const mdx_params &p = c0->p;
-  const int NFREQ = p.nfreq, NFREQ2 = NFREQ / 2 + 1;
+  const int NFREQ = p.nfreq, NFREQ2 = NFREQ / 2 + 1, P = pi->P;
   const double HTSTEP = 0.5 * p.tstep, TSTEB = p.tsteb, HTSTEB = 0.5 * p.tsteb;
-  // Kicks and GETEMP share passes over the atoms (launch_getemp_kick), and
-  // the drift carries GETCOM and the coordinate mirrors
-  // (launch_kick_drift_com): the same operations in the same order as the
-  // separate kernels, in fewer launches per bead.
-  RC(fork(pi));
-  EACH_BEAD(RC(launch_getemp_kick(ctx, {}, {2, HTSTEP, 1, HTSTEB})));
-  RC(join(pi));
+  cudaStream_t st = pi->stream;
+  RC(launch_getemp_beads(c0, P, pi->mv_tab, st, {}, {2, HTSTEP, 1, HTSTEB}));
   RC(nose(pi));
   for (int s = 1; s <= NFREQ; ++s) {
+    RC(launch_kick_drift_com_beads(c0, P, pi->mv_tab, st, 0.0, TSTEB));
     RC(fork(pi));
-    EACH_BEAD(RC(launch_kick_drift_com(ctx, 0.0, TSTEB, 0, false));
-              if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
+    EACH_BEAD(if (s == NFREQ2) RC(launch_list_update(ctx, mstep));
               if (s == NFREQ) {
                 RC(api_do_slforces(ctx, false, true));
                 RC(api_do_fforces(ctx, 1, false, true));
@@ -307,14 +320,13 @@ int long_step(mdx_pimd *pi, int mstep) {
               });
     RC(join(pi));
     RC(springs(pi, s == NFREQ));
-    RC(fork(pi));
-    EACH_BEAD(if (s < NFREQ) RC(launch_getemp_kick(ctx, {1, HTSTEB}, {1, HTSTEB}));
-              else {
-                RC(launch_getemp_kick(ctx, {1, HTSTEB}, {2, HTSTEP}));
-                RC(launch_getemp(ctx));
-              });
-    RC(join(pi));
-    if (s < NFREQ) RC(nose(pi));
+    if (s < NFREQ) {
+      RC(launch_getemp_beads(c0, P, pi->mv_tab, st, {1, HTSTEB}, {1, HTSTEB}));
+      RC(nose(pi));
+    } else {
+      RC(launch_getemp_beads(c0, P, pi->mv_tab, st, {1, HTSTEB}, {2, HTSTEP}));
+      RC(launch_getemp_beads(c0, P, pi->mv_tab, st));
+    }
   }
   k_pi_record<<<1, 1, 0, pi->stream>>>(pi->P, pi->db, pi->bead, pi->qeks, NFREQ, pi->rec,
                                         pi->rec_ctr);
@@ -366,6 +378,7 @@ int run(mdx_pimd *pi, int32_t nsteps, int32_t mstep0, bool with_prologue,
       }
   }
   if (with_prologue) RC(prologue(pi));
+  RC(fill_bead_table(pi));
   k_pi_start<<<1, 1, 0, pi->stream>>>(pi->rec_ctr, mstep0);
   PI_CUDA(cudaGetLastError());
   const bool graphs = pi->beads[0]->use_graphs;
@@ -387,7 +400,8 @@ int mdx_pimd_open(mdx_ctx *const *beads, const mdx_pimd_params *par, mdx_pimd **
   for (int k = 0; k < par->nbeads; ++k) {
     mdx_ctx *c = beads[k];
     if (!c || !c->have_topo || !c->have_params || !c->have_state) return MDX_ERR_STATE;
-    if (c->dv.n != c0->dv.n || c->d.precision != c0->d.precision || c->device != c0->device)
+    if (c->dv.n != c0->dv.n || c->dv.nop != c0->dv.nop || c->d.ntypes != c0->d.ntypes ||
+        c->d.precision != c0->d.precision || c->device != c0->device)
       return MDX_ERR_ARG;
     if (c->p.lnvt || c->p.lnpt || c->p.icell != 0) {
       c0->err = "PIMD: bead thermostats only (no NVT/NPT scaling), rectangular cell";
@@ -426,7 +440,8 @@ int mdx_pimd_open(mdx_ctx *const *beads, const mdx_pimd_params *par, mdx_pimd **
                      sizeof(double) * (size_t)pi->P * pi->nblk() * PI_NV)) ||
       (rc = pi_alloc(pi, reinterpret_cast<void **>(&pi->bead), sizeof(double) * 2 * pi->P)) ||
       (rc = pi_alloc(pi, reinterpret_cast<void **>(&pi->qeks), sizeof(double))) ||
-      (rc = pi_alloc(pi, reinterpret_cast<void **>(&pi->rec_ctr), 2 * sizeof(int))))
+      (rc = pi_alloc(pi, reinterpret_cast<void **>(&pi->rec_ctr), 2 * sizeof(int))) ||
+      (rc = pi_alloc(pi, &pi->mv_tab, bead_move_bytes() * pi->P)))
     return fail(rc);
   if (cudaStreamSynchronize(pi->stream) != cudaSuccess ||
       ctx_copy(pi->stream, pi->db, hb.data(), sizeof(PiBead) * pi->P, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -442,7 +457,7 @@ int mdx_pimd_close(mdx_pimd *pi) {
     if (g) cudaGraphExecDestroy(g);
   if (pi->stream) {
     void *ptrs[] = {pi->db, pi->thermo, pi->smass, pi->part, pi->bead, pi->qeks, pi->rec,
-                    pi->rec_ctr};
+                    pi->rec_ctr, pi->mv_tab};
     for (void *p : ptrs)
       if (p) cudaFreeAsync(p, pi->stream);
     cudaStreamSynchronize(pi->stream);

@@ -109,8 +109,10 @@ def load():
     L.mdx_poll.argtypes = [P, I32P]
     L.mdx_device_memory.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     L.mdx_pool_usage.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
-    from mdynamix_gb300.abi import MdxPathInfo
+    from mdynamix_gb300.abi import MdxPathInfo, MdxTuning
     L.mdx_get_path_info.argtypes = [P, C.POINTER(MdxPathInfo)]
+    L.mdx_set_tuning.argtypes = [P, C.POINTER(MdxTuning)]
+    L.mdx_get_tuning.argtypes = [P, C.POINTER(MdxTuning)]
     for n in ("mdx_double", "mdx_double_steps", "mdx_sultan", "mdx_sultan_steps"):
         getattr(L, n).argtypes = [P, C.c_int32, C.c_int32, C.POINTER(MdxStepRecord)]
     L.mdx_set_lambda.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -291,6 +293,25 @@ class ForcePath:
         info = MdxPathInfo()
         self._check(self.L.mdx_get_path_info(self.h, C.byref(info)))
         return info.as_dict()
+
+    def tuning(self) -> dict:
+        """Threads per owner atom of the mixed pair sweeps and where the
+        choice came from (1 the tuning table, 2 set_tuning)."""
+        from mdynamix_gb300.abi import MdxTuning
+        t = MdxTuning()
+        self._check(self.L.mdx_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, tpo_short: int = None, tpo_long: int = None):
+        """Override the split (both None: back to the tuning table)."""
+        from mdynamix_gb300.abi import MdxTuning
+        if tpo_short is None and tpo_long is None:
+            self._check(self.L.mdx_set_tuning(self.h, None))
+            return
+        cur = self.tuning()
+        t = MdxTuning(tpo_short if tpo_short is not None else cur["tpo_short"],
+                      tpo_long if tpo_long is not None else cur["tpo_long"], 2, 0)
+        self._check(self.L.mdx_set_tuning(self.h, C.byref(t)))
 
     def bonded_averages(self) -> dict:
         """BR, BE, AR, AE, TR, TE of the last FFORCES with LAVER: per bond,

@@ -212,9 +212,10 @@ def test_abi_struct_sizes_match_c():
 #include <stdio.h>
 #include <stddef.h>
 #include "mdx_gpu.h"
-int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_topo),
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mdx_dims), sizeof(mdx_topo),
  sizeof(mdx_params), sizeof(mdx_scalars), sizeof(mdx_thermo), sizeof(mdx_step_record),
- sizeof(mdx_kin), sizeof(mdx_pimd_params), sizeof(mdx_pimd_record), sizeof(mdx_path_info));
+ sizeof(mdx_kin), sizeof(mdx_pimd_params), sizeof(mdx_pimd_record), sizeof(mdx_path_info),
+ sizeof(mdx_tuning));
  return 0;}
 '''
     tmp = os.path.join(ROOT, "_build")
@@ -228,7 +229,7 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(mdx_di
     want = [ctypes.sizeof(t) for t in (abi.MdxDims, abi.MdxTopo, abi.MdxParams,
                                        abi.MdxScalars, abi.MdxThermo, abi.MdxStepRecord,
                                        abi.MdxKin, abi.MdxPimdParams, abi.MdxPimdRecord,
-                                       abi.MdxPathInfo)]
+                                       abi.MdxPathInfo, abi.MdxTuning)]
     assert got == want
 
 

@@ -369,3 +369,52 @@ def test_sultan_shake_hbonds_bilayer_fp64(npt):
     for a, b in zip(rg, ro):
         for n in ("temp", "pels1", "boxl", "tryck"):
             assert abs(getattr(a, n) - getattr(b, n)) <= 1e-8 * max(abs(getattr(b, n)), 1e-12), n
+
+
+def test_mixed_sweep_splits():
+    """Every work split of the mixed pair sweeps (threads per owner atom):
+    forces within the mixed bar of FP64 and within 1e-6 of the default
+    split, the same split twice bit for bit (also through the step graphs,
+    which a change of split recaptures), and the table's choice restored by
+    set_tuning()."""
+    s, st = CASES["spcfw"]()
+    g64 = ForcePath(s, precision=MDX_FP64)
+    g64.set_state(*st)
+    g64.chcnb()
+    g64.getcom()
+    g64.allforce()
+    f64 = g64.forces(3)
+    nrm = np.sqrt((f64 ** 2).sum())
+    g = ForcePath(s, precision=MDX_MIXED)
+    g.set_state(*st)
+    g.chcnb()
+    g.getcom()
+    g.allforce()
+    t0 = g.tuning()
+    assert t0["source"] == 1 and t0["tpo_short"] in (2, 4, 8) and t0["tpo_long"] in (8, 16, 32)
+    f0 = g.forces(3)
+    for ts, tl in ((2, 8), (8, 16), (4, 32), (8, 32)):
+        g.set_tuning(ts, tl)
+        assert g.tuning() == {"tpo_short": ts, "tpo_long": tl, "source": 2}
+        g.allforce()
+        f = g.forces(3)
+        assert np.sqrt(((f - f64) ** 2).sum()) / nrm < MIXED_TOL, (ts, tl)
+        assert np.sqrt(((f - f0) ** 2).sum()) / nrm < 1e-6, (ts, tl)
+        g.allforce()
+        assert np.array_equal(g.forces(3), f), (ts, tl)
+    with pytest.raises(MdxError):
+        g.set_tuning(3, 32)
+    g.set_tuning()
+    assert g.tuning() == t0
+    outs = []
+    for split in ((2, 16), (2, 16), None):
+        h = ForcePath(s, precision=MDX_MIXED)
+        h.set_state(*st)
+        if split:
+            h.set_tuning(*split)
+        h.double(3, records=False)
+        (x, y, z, *_), _ = h.get_state()
+        outs.append(np.stack([x, y, z]))
+        h.close()
+    assert np.array_equal(outs[0], outs[1])
+    assert np.abs(outs[0] - outs[2]).max() < 1e-6
