@@ -334,6 +334,22 @@ __global__ void __launch_bounds__(128) k_molbonded(
     g -= tpl[t].nmol;
     ++t;
   }
+  // a warp whose molecules all share one template adds to the same records
+  // in the same order: its statistics go out as one warp sum per record
+  // (shared-memory FP64 atomics from every lane serialise on those records)
+  // (every lane takes part in both warp operations: no short-circuit
+  // around them)
+  const int t0 = __shfl_sync(0xffffffffu, t, 0);
+  const bool same_tpl = t < ntpl && t == t0;
+  const bool wsum = __all_sync(0xffffffffu, same_tpl) && laver;
+  auto add = [&](double *sh, double *gl, int M, int nr, double v) {
+    if (wsum) {
+      v = warp_sum(v);
+      if ((threadIdx.x & 31) == 0) avg_add(sh, gl, M, nr, v);
+    } else {
+      avg_add(sh, gl, M, nr, v);
+    }
+  };
   if (t < ntpl) {
     const MolTpl &T = tpl[t];
     const int base = T.first + g * T.nsit;
@@ -345,8 +361,8 @@ __global__ void __launch_bounds__(128) k_molbonded(
       bond_term<R, true, R>(pos, base + T.bi[b], base + T.bj[b], M, bid, rb, fb, db, ro, lmove,
                          bx, by, bz, o, acc, &BD, &EB);
       if (laver) {
-        avg_add(sav[0], br, M, nrbb, (double)BD * fnspi);
-        avg_add(sav[1], be, M, nrbb, (double)EB * fnspi);
+        add(sav[0], br, M, nrbb, (double)BD * fnspi);
+        add(sav[1], be, M, nrbb, (double)EB * fnspi);
       }
     }
     for (int a = 0; a < T.na; ++a) {
@@ -355,8 +371,8 @@ __global__ void __launch_bounds__(128) k_molbonded(
       angle_term<R, true, R>(pos, base + T.ai[a], base + T.aj[a], base + T.ak[a], M, ra, fa,
                           lmove, bx, by, bz, o, acc, &ALF, &EA);
       if (laver) {
-        avg_add(sav[2], ar, M, nraa, (double)ALF * fnspi);
-        avg_add(sav[3], ae, M, nraa, (double)EA * fnspi);
+        add(sav[2], ar, M, nraa, (double)ALF * fnspi);
+        add(sav[3], ae, M, nraa, (double)EA * fnspi);
       }
     }
   }

@@ -1444,7 +1444,7 @@ static int getemp_kernel(mdx_ctx *ctx, const KickSpec &pre = {}, const KickSpec 
   const KickArgs a = kick_args(ctx, pre), b = kick_args(ctx, post);
   const bool kick = a.ax || b.ax || a.vs;
 #define GETEMP_K(NT, R, K)                                                             \
-  k_getemp<NT, R, K><<<ctx->nsm, 256, 0, ctx->stream>>>(                               \
+  k_getemp<NT, R, K><<<red_blocks(ctx), 256, 0, ctx->stream>>>(                               \
       d.n, d.ainfo, move_const(ctx), nt, d.massdi, d.vx, d.vy, d.vz,                   \
       scratch(ctx)->ekacc, d.red_part, d.red_ctr, a, b)
 #define GETEMP(NT)                                                                    \
@@ -1827,7 +1827,7 @@ int launch_getemp_beads(mdx_ctx *c0, int P, const void *table, cudaStream_t st,
   const KickW a = kick_w(pre), b = kick_w(post);
   const bool kick = a.w1 || b.w1 || a.vs;
   const BeadMove *tab = static_cast<const BeadMove *>(table);
-  const dim3 grid(c0->nsm, P);
+  const dim3 grid(red_blocks(c0), P);
 #define GB_K(NT, R, K)                                                                   \
   k_getemp_beads<NT, R, K><<<grid, 256, 0, st>>>(d.n, d.ainfo, move_const(c0), nt, d.massdi, \
                                                  tab, a, b)
@@ -1954,8 +1954,9 @@ int launch_chkmom(mdx_ctx *ctx, double sumasd, double *pt) {
   DevData &d = ctx->dv;
   double *acc = d.red + 484;
   MDX_CUDA(cudaMemsetAsync(acc, 0, 3 * sizeof(double), ctx->stream));
-  k_mom_sum<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.vx, d.vy, d.vz,
-                                               dst6(ctx, ctx->nsm, 3, acc, acc + 1, acc + 2));
+  const int nb = red_blocks(ctx);
+  k_mom_sum<<<nb, 256, 0, ctx->stream>>>(d.n, d.vx, d.vy, d.vz,
+                                         dst6(ctx, nb, 3, acc, acc + 1, acc + 2));
   MDX_LAUNCHED(ctx);
   k_mom_remove<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, sumasd, acc, d.massdi, d.vx,
                                                            d.vy, d.vz);

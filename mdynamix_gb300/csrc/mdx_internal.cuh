@@ -76,6 +76,12 @@ struct PairConst {
 constexpr int TPO_SHORT_DEFAULT = 4;
 constexpr int TPO_LONG_DEFAULT = 32;
 void resolve_tuning(mdx_ctx *ctx);  // pair.cu: the tuning table's choice, once
+// Blocks of the grid-stride per-atom reductions (GETEMP, WIRS, momenta):
+// one per SM, or one per 256 atoms when that is fewer (a small system's
+// reduction then is not spread over mostly idle blocks).  A function of the
+// atom count alone, so the sums' order is fixed for a system.
+struct mdx_ctx;
+int red_blocks(const mdx_ctx *ctx);
 
 // Cell grid used by the list build.
 struct CellGrid {

@@ -15,6 +15,7 @@
 // lane partial forces are rounded to 64-bit fixed point and summed as
 // integers, so the result does not depend on the order of the sums.  Energy
 // and virial lane partials go the same way into 64-bit integer slots.
+#include <algorithm>
 #include <cmath>
 
 #include "mdx_internal.cuh"
@@ -479,34 +480,28 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
 __global__ void k_fold_slots(unsigned long long *__restrict__ slots, double einv,
                              mdx_scalars *__restrict__ sc, int which, int ntypes,
                              int split) {
-  double v[P_NSLOT];
-  for (int k = 0; k < P_NSLOT; ++k) {
-    v[k] = (double)(long long)slots[k] * einv;
-    slots[k] = 0ull;
+  // thread k folds slot k into its own scalar (the slots' sums are
+  // independent): one conversion deep instead of P_NSLOT in a row
+  const int k = threadIdx.x;
+  if (k >= P_NSLOT) return;
+  double v = (double)(long long)slots[k] * einv;
+  slots[k] = 0ull;
+  if (k < P_WIR) v *= 0.5;
+  double *dst = nullptr;
+  switch (k) {
+    case P_EES: dst = which == 1 ? &sc->pels2 : &sc->pels1; break;
+    case P_ESR: dst = which == 1 ? &sc->pe2 : &sc->pe1; break;
+    case P_VIR: dst = which == 1 ? &sc->vir2 : &sc->vir1; break;
+    case P_VX: dst = which == 1 ? &sc->virfx : &sc->virx; break;
+    case P_VY: dst = which == 1 ? &sc->virfy : &sc->viry; break;
+    case P_VZ: dst = which == 1 ? &sc->virfz : &sc->virz; break;
+    case P_WIR: dst = which == 1 ? &sc->wirss : nullptr; break;
+    case P_EE_DIFF: dst = ntypes == 1 && !split ? &sc->pote1[0] : nullptr; break;
+    case P_ESR_DIFF: dst = ntypes == 1 && !split ? &sc->potl1[0] : nullptr; break;
+    case P_EE_SAME: dst = ntypes == 1 && !split ? &sc->pes141[0] : nullptr; break;
+    case P_ESR_SAME: dst = ntypes == 1 && !split ? &sc->psr141[0] : nullptr; break;
   }
-  for (int k = 0; k < P_WIR; ++k) v[k] *= 0.5;
-  if (which == 1) {
-    sc->pels2 += v[P_EES];
-    sc->pe2 += v[P_ESR];
-    sc->vir2 += v[P_VIR];
-    sc->virfx += v[P_VX];
-    sc->virfy += v[P_VY];
-    sc->virfz += v[P_VZ];
-    sc->wirss += v[P_WIR];
-  } else {
-    sc->pels1 += v[P_EES];
-    sc->pe1 += v[P_ESR];
-    sc->vir1 += v[P_VIR];
-    sc->virx += v[P_VX];
-    sc->viry += v[P_VY];
-    sc->virz += v[P_VZ];
-  }
-  if (ntypes == 1 && !split) {
-    sc->pote1[0] += v[P_EE_DIFF];
-    sc->potl1[0] += v[P_ESR_DIFF];
-    sc->pes141[0] += v[P_EE_SAME];
-    sc->psr141[0] += v[P_ESR_SAME];
-  }
+  if (dst) *dst += v;
 }
 
 // Copy the split accumulators (POTE1, POTL1, PES141, PSR141) out.
@@ -618,7 +613,7 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
 #undef LP32
     MDX_LAUNCHED(ctx);
     if (ener) {
-      k_fold_slots<<<1, 1, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
+      k_fold_slots<<<1, 32, 0, ctx->stream>>>(slots, 1.0 / escale, d.sc, shrt ? 1 : 2,
                                               ctx->d.ntypes, split ? 1 : 0);
       MDX_LAUNCHED(ctx);
     }
@@ -638,6 +633,10 @@ int tune_pick(const TuneCell (&cells)[N], int n, double row, int dflt) {
 }
 
 }  // namespace
+
+int red_blocks(const mdx_ctx *ctx) {
+  return std::max(1, std::min(ctx->nsm, (ctx->dv.n + 255) / 256));
+}
 
 // The tuning table's split for this system, from its sizes alone: atoms and
 // the mean full-row lengths rho (4/3) pi r^3 of the short and long lists.
@@ -674,15 +673,17 @@ int launch_wir(mdx_ctx *ctx, int which) {
   DevData &d = ctx->dv;
   double *dst = which == 1 ? &d.sc->wirss : &d.sc->wirs;
   if (which == 1 && ctx->mixed()) {
-    k_wir_fix<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, d.hfix,
-                                                 ctx->fix.inv, dst6(ctx, ctx->nsm, 1, dst));
+    const int nb = red_blocks(ctx);
+    k_wir_fix<<<nb, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, d.hfix,
+                                           ctx->fix.inv, dst6(ctx, nb, 1, dst));
     MDX_LAUNCHED(ctx);
     return MDX_OK;
   }
   const double *fx = which == 1 ? d.hx : d.gx, *fy = which == 1 ? d.hy : d.gy,
                *fz = which == 1 ? d.hz : d.gz;
-  k_wir<<<ctx->nsm, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz,
-                                           dst6(ctx, ctx->nsm, 1, dst));
+  const int nbw = red_blocks(ctx);
+  k_wir<<<nbw, 256, 0, ctx->stream>>>(d.n, d.pos, d.ainfo, d.X, d.Y, d.Z, fx, fy, fz,
+                                      dst6(ctx, nbw, 1, dst));
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }
