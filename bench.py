@@ -189,6 +189,15 @@ def run_gpu(args, rank, world, local):
         if dist:
             dist.barrier()
 
+    if args.only == "pimd":
+        from mdynamix_gb300 import system as S
+        from mdynamix_gb300.mdx import PimdPath
+        sp = S.System(S.pimd_water(nwater=256, nbeads=32))
+        pp = PimdPath(sp, S.pimd_beads(sp, seed=5), precision=MDX_MIXED)
+        pp.run(args.warmup)
+        pp.steps(args.steps, args.warmup)
+        pp.close()
+        return None
     s, st = make_system()
     n = s.nstot
     out = {}
@@ -646,9 +655,10 @@ def main():
     ap.add_argument("--serve-steps", type=int, default=20, help="long steps per coupling state")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
     ap.add_argument("--serve-slots", type=int, default=64)
-    ap.add_argument("--pimd-steps", type=int, default=20, help="PIMD leg timed steps (0 = off)")
+    ap.add_argument("--pimd-steps", type=int, default=2000,
+                    help="PIMD leg timed steps (config 5: 2000; 0 = off)")
     ap.add_argument("--pimd-warmup", type=int, default=3)
-    ap.add_argument("--bilayer-steps", type=int, default=10, help="bilayer leg timed steps (0 = off)")
+    ap.add_argument("--bilayer-steps", type=int, default=100, help="bilayer leg timed steps (0 = off)")
     ap.add_argument("--bilayer-warmup", type=int, default=3)
     ap.add_argument("--nve-steps", type=int, default=500, help="NVE leg long steps (0 = off)")
     ap.add_argument("--nve-equil", type=int, default=100)
@@ -657,8 +667,9 @@ def main():
     ap.add_argument("--cfg1-steps", type=int, default=1000)
     ap.add_argument("--cfg1-equil", type=int, default=1000)
     ap.add_argument("--detail", default=None, help="also write the full results to this file")
-    ap.add_argument("--only", choices=["fp64", "mixed"], default=None,
-                    help="profiling runs: one precision, no e2e/error legs, no JSON line")
+    ap.add_argument("--only", choices=["fp64", "mixed", "pimd"], default=None,
+                    help="profiling runs: one precision (or the mixed PIMD ensemble of "
+                         "the pimd leg), warm-up + steps only, no JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = env_rank()
