@@ -158,7 +158,10 @@ struct MolCut {
 };
 
 // Exact classification (forces.f:1938-1981): 0 none, 1 short, 2 long,
-// 3 short 1-4, -1 excluded bonded pair.
+// 3 short 1-4, -1 excluded bonded pair.  LMNBL: the molecular cutoff (a
+// template parameter, so the atomic-cutoff build carries none of its code
+// or its runtime-indexed per-type table).
+template <bool LMNBL>
 __device__ __forceinline__ int classify_exact(
     int i, int j, bool same_mol, const dbl4 &pi, const dbl4 &pj,
     const BoxD &b, double short2, double rl2, const int *__restrict__ nnbb,
@@ -167,7 +170,7 @@ __device__ __forceinline__ int classify_exact(
   pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
   double rr2 = dx * dx + dy * dy + dz * dz;
   double rrm = rr2;
-  if (mc.lmnbl) {
+  if (LMNBL) {
     constexpr int MMOL = 5;
     const int4 ai = mc.ainfo[i], aj = mc.ainfo[j];
     const int nmi = mc.nsits[ai.x], nmj = mc.nsits[aj.x];
@@ -198,7 +201,7 @@ __device__ __forceinline__ int classify_exact(
   return 0;
 }
 
-template <int BLK>
+template <int BLK, bool LMNBL>
 __global__ void __launch_bounds__(BLK) k_build(
     int n, const dbl4 *__restrict__ pos, const float4 *__restrict__ posf,
     const int4 *__restrict__ ainfo, const int *__restrict__ nnbb,
@@ -260,8 +263,8 @@ __global__ void __launch_bounds__(BLK) k_build(
               const bool same =
                   posi ? ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS)
                        : qj.w == imol;
-              if (same || mc.lmnbl) {  // the molecular cutoff: exact test only
-                kind = classify_exact(i, j, same, pi, pos[j], b, short2, rl2,
+              if (same || LMNBL) {  // the molecular cutoff: exact test only
+                kind = classify_exact<LMNBL>(i, j, same, pi, pos[j], b, short2, rl2,
                                       nnbb, inbb, nbdmax, mc);
               } else {
                 float dx, dy, dz;
@@ -281,7 +284,7 @@ __global__ void __launch_bounds__(BLK) k_build(
                 } else if (d2 < rl2f_lo && (d2 < s2f_lo || d2 > s2f_hi)) {
                   kind = d2 < s2f_lo ? 1 : 2;
                 } else {
-                  kind = classify_exact(i, j, false, pi, pos[j], b, short2, rl2,
+                  kind = classify_exact<LMNBL>(i, j, false, pi, pos[j], b, short2, rl2,
                                         nnbb, inbb, nbdmax, mc);
                 }
               }
@@ -436,7 +439,11 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
   const double rl = std::max(ctx->p.rcut + ctx->p.rskin, ctx->p.rshort);
   // the molecular cutoff lists atoms up to twice a small molecule's reach
   // from its centre of mass beyond the cutoff
-  const double rsearch = ctx->p.lmnbl ? rl + 2.0 * ctx->mol_reach : rl;
+  const double rsearch =
+      !ctx->p.lmnbl ? rl
+      : ctx->mol_reach >= 0.0
+          ? rl + 2.0 * ctx->mol_reach
+          : rl + std::min(ctx->boxl, std::min(ctx->boyl, ctx->bozl));  // reach unknown
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
          0.5 * ctx->bozl};
   CellGrid g;
@@ -500,13 +507,17 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
   k_zero_gated<<<1, 32, 0, ctx->stream>>>(need, 2, gate);
   MDX_LAUNCHED(ctx);
   const int BLK = 256;
-  k_build<BLK><<<(d.n + BLK / 32 - 1) / (BLK / 32), BLK, 0, ctx->stream>>>(
-      d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,
-      d.cell_start, d.cell_list, d.cell_pos, ctx->p.rshort * ctx->p.rshort, rl * rl,
-      d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,
-      ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,
-      (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),
-      (float)(ctx->bozl / 4294967296.0), pos_ref, gate, mol_cut(ctx));
+#define KB(L)                                                                              \
+  k_build<BLK, L><<<(d.n + BLK / 32 - 1) / (BLK / 32), BLK, 0, ctx->stream>>>(              \
+      d.n, d.pos, d.posf, d.ainfo, d.nnbb, d.inbb, d.nbdmax, b, g, d.atom_cell,            \
+      d.cell_start, d.cell_list, d.cell_pos, ctx->p.rshort * ctx->p.rshort, rl * rl,       \
+      d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,               \
+      ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,                               \
+      (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),               \
+      (float)(ctx->bozl / 4294967296.0), pos_ref, gate, mol_cut(ctx))
+  if (ctx->p.lmnbl) KB(true);
+  else KB(false);
+#undef KB
   MDX_LAUNCHED(ctx);
   k_zero_gated<<<1, 32, 0, ctx->stream>>>(&d.sc->mbsh, 2, gate);
   MDX_LAUNCHED(ctx);
