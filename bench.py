@@ -281,14 +281,20 @@ def run_gpu(args, rank, world, local):
         a[:] = b
     ke = max(2, min(args.steps, 10))
     mstep = 2 * args.steps + args.warmup
+
+    def e2e_step(k):
+        # upload positions and momenta, one long step with its record, and
+        # download them again, host buffers page-locked
+        nonlocal th
+        g.set_state(*pinned, thermo=th)
+        g.double_steps(1, mstep + k, records=True)
+        _, th = g.get_state(out=pinned)
+
+    e2e_step(0)  # warm-up: the step graph with records is captured here
     barrier()
     t0 = time.perf_counter()
     for k in range(ke):
-        g.set_state(*pinned, thermo=th)
-        rec = g.double_steps(1, mstep + k, records=True)
-        (xx, yy, zz, uu, vv, ww), th = g.get_state()
-        for a, b in zip(pinned, (xx, yy, zz, uu, vv, ww)):
-            a[:] = b
+        e2e_step(1 + k)
     e2e_s = (time.perf_counter() - t0) / ke
     peak64 = probe_fma_peak(True)
     peak32 = probe_fma_peak(False)

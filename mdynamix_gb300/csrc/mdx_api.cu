@@ -93,7 +93,7 @@ __global__ void k_set_pos(int n, const double *sx, const double *sy,
   p.x = sx[i];
   p.y = sy[i];
   p.z = sz[i];
-  p.w = q[i];
+  p.w = q ? q[i] : pos[i].w;  // q null: the charges already on the device stay
   pos[i] = p;
 }
 
@@ -788,6 +788,7 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
   RC(upload(ctx, d.qsite, qsite.data(), n));
   RC(upload(ctx, d.qsitef, qsitef.data(), n));
   ctx->h_q.assign(t->q, t->q + n);
+  ctx->q_dirty = true;
   if (ctx->mixed()) {
     if (ns >= (1 << MDX_SITE_BITS) || d.nop >= (1 << (32 - MDX_SITE_BITS))) {
       ctx->err = "mixed path: at most 8191 sites and 524287 molecules";
@@ -998,21 +999,27 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
   rc = rc ? rc : upload(ctx, tmp, sx, n);
   rc = rc ? rc : upload(ctx, tmp + n, sy, n);
   rc = rc ? rc : upload(ctx, tmp + 2 * n, sz, n);
-  rc = rc ? rc : upload(ctx, tmp + 3 * n, ctx->h_q.data(), n);
+  // the charges (kept in step with RECINT on the device) go up only once
+  const bool charges = !ctx->have_state || ctx->q_dirty;
+  if (charges) rc = rc ? rc : upload(ctx, tmp + 3 * n, ctx->h_q.data(), n);
   if (!rc) {
     k_set_pos<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(d.n, tmp, tmp + n, tmp + 2 * n,
-                                                         tmp + 3 * n, d.pos);
+                                                         charges ? tmp + 3 * n : nullptr,
+                                                         d.pos);
     ctx->launches++;
   }
   ctx_free(ctx, tmp);
   cudaStreamSynchronize(ctx->stream);
   if (rc) return rc;
+  ctx->q_dirty = false;
   RC(upload(ctx, d.vx, vx, n));
   RC(upload(ctx, d.vy, vy, n));
   RC(upload(ctx, d.vz, vz, n));
-  {
+  if (ctx->p.lmnbl) {
     // reach of small molecules (at most 5 sites) from their centres of mass,
     // for the search radius of the reaction field's molecular cutoff list
+    // (unknown, -1, when the state came without that list: the build then
+    // searches the whole box)
     double reach = 0.0;
     const double hb[3] = {0.5 * ctx->boxl, 0.5 * ctx->boyl, 0.5 * ctx->bozl};
     const double bl[3] = {ctx->boxl, ctx->boyl, ctx->bozl};
@@ -1046,6 +1053,8 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
       i = e;
     }
     ctx->mol_reach = reach + 1.0;
+  } else {
+    ctx->mol_reach = -1.0;
   }
   mdx_thermo h{};
   if (th) h = *th;

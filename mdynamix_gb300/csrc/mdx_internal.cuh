@@ -304,6 +304,7 @@ struct mdx_ctx {
   // reaction field: largest distance of an atom of a small molecule from the
   // molecule's centre of mass (+ 1 A for flexing), set at the state upload
   double mol_reach = 0;
+  bool q_dirty = true;  // the device charges (pos.w) lag the host's (topology upload)
   FixScale fix{};
   // CUDA graphs of one long step: [rebuild?] + 2 * [records?] + 4 * [SULTAN?]
   cudaGraphExec_t gexec[8] = {};

@@ -218,8 +218,14 @@ class ForcePath:
         th = thermo if thermo is not None else thermo_init(self.system)
         self._check(self.L.mdx_upload_state(self.h, *[_fp(a) for a in arrs], C.byref(th)))
 
-    def get_state(self):
-        out = [np.zeros(self.n) for _ in range(6)]
+    def get_state(self, out=None):
+        """(sx, sy, sz, vx, vy, vz), thermo; ``out``: six contiguous float64
+        arrays to download into (e.g. page-locked host buffers)."""
+        if out is None:
+            out = [np.zeros(self.n) for _ in range(6)]
+        else:
+            assert len(out) == 6 and all(a.dtype == np.float64 and a.flags.c_contiguous
+                                         and a.size == self.n for a in out)
         th = MdxThermo()
         self._check(self.L.mdx_download_state(self.h, *[_fp(a) for a in out], C.byref(th)))
         return out, th

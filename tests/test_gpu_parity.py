@@ -318,6 +318,11 @@ def test_set_lambda_matches_oracle():
     g.chcnb(); o.chcnb()
     g.allforce(); o.allforce()
     assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
+    # a later state upload keeps the scaled charges (they go up only once)
+    g.set_state(*st); o.set_state(*st)
+    g.chcnb(); o.chcnb()
+    g.allforce(); o.allforce()
+    assert relmax(g.forces(3), o.forces(3)) < FP64_TOL
 
 
 def test_graph_replay_matches_eager(monkeypatch):
