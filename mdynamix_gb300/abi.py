@@ -297,7 +297,7 @@ def params_of(s: System) -> MdxParams:
     sp = s.spec
     par = MdxParams()
     par.boxl, par.boyl, par.bozl = s.boxl, s.boyl, s.bozl
-    par.icell = 0
+    par.icell = int(sp.icell)
     par.lmnbl = int(s.lmnbl)
     par.rff = s.rff
     par.rff2 = s.rff2

@@ -27,6 +27,7 @@ struct BondOut {
   const int4 *posi;   // mixed: fixed-point positions (bond vectors by integer wrap)
   float sx, sy, sz;   // box / 2^32
   float limx, limy, limz;  // 0.99 x half box: below it no minimum-image shift
+  CellPbc cell;            // cell shape (FP64 path: hexagonal / octahedral PBC)
 };
 
 // Fixed-point force term: R = float rounds v * 2^k with FP32 operations only
@@ -53,12 +54,13 @@ __device__ __forceinline__ void add_force(const BondOut &o, int i, R fx, R fy, R
 
 __device__ __forceinline__ void vec(const dbl4 *pos, int a, int b, double bx,
                                     double by, double bz, double &x, double &y,
-                                    double &z) {
+                                    double &z, const CellPbc &c) {
   const dbl4 pa = pos[a], pb = pos[b];
   x = pa.x - pb.x;
   y = pa.y - pb.y;
   z = pa.z - pb.z;
-  pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  if (c.icell == 0) pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  else pbc_cell(x, y, z, c);  // PBC (forces.f:149, 248, 359)
 }
 
 // Bond vector a - b in R: FP64 minimum image of the FP64 positions, or on
@@ -90,7 +92,7 @@ __device__ __forceinline__ void vec_r(const dbl4 *pos, const BondOut &o, int a, 
     }
   } else {
     double xd, yd, zd;
-    vec(pos, a, b, bx, by, bz, xd, yd, zd);
+    vec(pos, a, b, bx, by, bz, xd, yd, zd, o.cell);
     x = (R)xd;
     y = (R)yd;
     z = (R)zd;
@@ -423,9 +425,9 @@ __global__ void k_gettrs(int nrrt, const int *__restrict__ iti,
     const int I = iti[N], J = jtj[N], K = ktk[N], L = ltl[N], M = ituk[N];
     const int ityp = ainfo[I].x;
     double a0, a1, a2, b0, b1, b2, c0, c1, c2;
-    vec(pos, J, I, bxl, byl, bzl, a0, a1, a2);
-    vec(pos, K, J, bxl, byl, bzl, b0, b1, b2);
-    vec(pos, L, K, bxl, byl, bzl, c0, c1, c2);
+    vec(pos, J, I, bxl, byl, bzl, a0, a1, a2, o.cell);
+    vec(pos, K, J, bxl, byl, bzl, b0, b1, b2, o.cell);
+    vec(pos, L, K, bxl, byl, bzl, c0, c1, c2, o.cell);
     const R ax = (R)a0, ay = (R)a1, az = (R)a2;
     const R bx = (R)b0, by = (R)b1, bz = (R)b2;
     const R cx = (R)c0, cy = (R)c1, cz = (R)c2;
@@ -562,9 +564,15 @@ __global__ void k_strbnd(WaterPar w, const dbl4 *__restrict__ pos, double bxl,
     double b0 = pk.x - pi.x, b1 = pk.y - pi.y, b2 = pk.z - pi.z;
     double c0 = pk.x - pj.x, c1 = pk.y - pj.y, c2 = pk.z - pj.z;
     if (w.ipt == 2) {  // only the Morse variant applies PBC (forces.f:626-640)
-      pbc_rect(a0, a1, a2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
-      pbc_rect(b0, b1, b2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
-      pbc_rect(c0, c1, c2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
+      if (o.cell.icell == 0) {
+        pbc_rect(a0, a1, a2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
+        pbc_rect(b0, b1, b2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
+        pbc_rect(c0, c1, c2, bxl, byl, bzl, 0.5 * bxl, 0.5 * byl, 0.5 * bzl);
+      } else {
+        pbc_cell(a0, a1, a2, o.cell);
+        pbc_cell(b0, b1, b2, o.cell);
+        pbc_cell(c0, c1, c2, o.cell);
+      }
     }
     const R AX = (R)a0, AY = (R)a1, AZ = (R)a2, BX = (R)b0, BY = (R)b1, BZ = (R)b2,
             CX = (R)c0, CY = (R)c1, CZ = (R)c2;
@@ -649,7 +657,8 @@ int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
   BondOut o{d.hx, d.hy, d.hz, mx ? d.hfix : nullptr, d.n, ctx->fix.scale, ctx->fix.scalef,
             nullptr, (float)(ctx->boxl / 4294967296.0),
             (float)(ctx->boyl / 4294967296.0), (float)(ctx->bozl / 4294967296.0),
-            (float)(0.495 * ctx->boxl), (float)(0.495 * ctx->boyl), (float)(0.495 * ctx->bozl)};
+            (float)(0.495 * ctx->boxl), (float)(0.495 * ctx->boyl), (float)(0.495 * ctx->bozl),
+            cell_pbc(ctx)};
   const int T = 128;
   const double bx = ctx->boxl, by = ctx->boyl, bz = ctx->bozl;
   const int *nspec = d.nspec_d;

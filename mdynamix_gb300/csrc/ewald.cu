@@ -78,12 +78,15 @@ __device__ __forceinline__ void cp_async_wait0() {
 }
 
 // Phase tables: thread per (axis, atom), FP64 recurrence from one sincos.
+// hexy (hexagonal cell, FP64 path): the x phase is 2 pi (x / BOXL + y / (2
+// BOYL)), which makes k . r = IKX theta_x + IKY theta_y + IKZ theta_z with
+// RYV = 2 pi IKY + pi IKX (forces.f:1399-1403); 0 otherwise.
 __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ibx,
                          double iby, double ibz, int kx, int ky, int kz,
                          double2 *__restrict__ tx, double2 *__restrict__ ty,
                          double2 *__restrict__ tz, float2 *__restrict__ txf,
                          float2 *__restrict__ tyf, float2 *__restrict__ tzf,
-                         const int4 *__restrict__ posi) {
+                         const int4 *__restrict__ posi, double hexy) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 3 * n) return;
   const int a = t / n, i = t - a * n;
@@ -110,7 +113,8 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
     return;
   }
   const dbl4 p = pos[i];
-  const double x = a == 0 ? p.x * ibx : a == 1 ? p.y * iby : p.z * ibz;
+  double x = a == 0 ? p.x * ibx : a == 1 ? p.y * iby : p.z * ibz;
+  if (a == 0 && hexy != 0.0) x = fma(p.y, hexy, x);
   double s, c;
   sincos(2.0 * PI_REF * x, &s, &c);
   const double2 e = make_double2(c, s);
@@ -130,7 +134,8 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
 // atomic.
 __device__ __forceinline__ void sfac_out(const KCol &col, int p, double A1, double A2,
                                          double A3, double A4, double2 *part, double2 *sk) {
-  const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
+  const int z = kcol_z(col, p);
+  const int kp = kcol_k(col, z), km = z > 0 ? kcol_k(col, -z) : -1;
   const double2 vp = make_double2(A1 - A2, A3 + A4), vm = make_double2(A1 + A2, A4 - A3);
   if (part) {
     if (kp >= 0) part[kp] = vp;
@@ -161,7 +166,7 @@ __global__ void __launch_bounds__(128) k_sfac(
   const int ch = blockIdx.x * blockDim.x + threadIdx.x;
   const int a0 = blockIdx.y * SLICE, a1 = min(n, a0 + SLICE);
   Chunk cc{0, 0, 0, 0};
-  KCol col{0, 0, 0, 0, 0, 0, 0, 0};
+  KCol col{0, 0, 0, 0, 0, 0, 0, 0, 0, 1};
   if (ch < nchunk) {
     cc = chunks[ch];
     col = cols[cc.col];
@@ -192,13 +197,14 @@ __global__ void __launch_bounds__(128) k_sfac(
         const double2 X = sx[j * kx + col.nx];
         const double2 Y = conj_if(sy[j * ky + ny], nyneg);
         const double tr = fma(X.x, Y.x, -X.y * Y.y), ti = fma(X.x, Y.y, X.y * Y.x);
-        const double2 *zr = sz + j * kz + cc.nz0;
+        const double2 *zr = sz + j * kz + kcol_z(col, cc.nz0);
+        const int zs = col.zstep;
         // chunks are sorted by length, so a warp's lanes mostly leave
         // together and a short chunk issues only its own FMAs
 #pragma unroll
         for (int t = 0; t < CH; ++t) {
           if (t >= cc.len) break;
-          const double2 Z = zr[t];
+          const double2 Z = zr[zs * t];
           A[t][0] = fma(tr, Z.x, A[t][0]);
           A[t][1] = fma(ti, Z.y, A[t][1]);
           A[t][2] = fma(tr, Z.y, A[t][2]);
@@ -250,7 +256,7 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
 #pragma unroll
     for (int c = 0; c < KGRP; ++c) {
       const int ci = active ? G.col[c] : -1;
-      const KCol col = ci >= 0 ? cols[ci] : KCol{0, 0, 0, 0, 0, 0, 0, 0};
+      const KCol col = ci >= 0 ? cols[ci] : KCol{0, 0, 0, 0, 0, 0, 0, 0, 0, 1};
       xo[c] = ci >= 0 ? col.nx : zpad;  // padding column: X = 0
       yo[c] = kx + (col.ny < 0 ? -col.ny : col.ny);
       ysg[c] = col.ny < 0 ? 0x80000000u : 0u;
@@ -365,23 +371,27 @@ __global__ void __launch_bounds__(SUM_K * SUM_G) k_sfac_sum(int nkv, int nslice,
 // Per-k constants of FURIR that depend on the box and alpha only (forces.f:
 // 1316-1331): AKC, (RXV^2, RYV^2, RZV^2) AKV and RZV, five doubles per k,
 // and the column's (RXV, RYV); rebuilt when the box or alpha changes.
+// hexk: pi for the hexagonal cell (RYV = 2 pi IKY + pi IKX, forces.f:1402),
+// 0 otherwise.
 __global__ void k_kconst(int ncol, const KCol *__restrict__ cols, double bx, double by,
                          double bz, double alp2, double cfur, double *__restrict__ kc,
-                         double2 *__restrict__ colrv, float2 *__restrict__ colrvf) {
+                         double2 *__restrict__ colrv, float2 *__restrict__ colrvf,
+                         double hexk) {
   const double twopi = 2.0 * PI_REF;
   for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
     const KCol col = cols[c];
-    const int len = col.nzhi - col.nzlo + 1;
+    const int len = (col.nzhi - col.nzlo) / col.zstep + 1;
+    const double ryv = hexk != 0.0 ? twopi * col.ny + hexk * col.nx : twopi * col.ny;
     if (threadIdx.x == 0) {
-      const double rx = (twopi * col.nx) / bx, ry = (twopi * col.ny) / by;
+      const double rx = (twopi * col.nx) / bx, ry = ryv / by;
       colrv[c] = make_double2(rx, ry);
       colrvf[c] = make_float2((float)rx, (float)ry);
     }
     for (int t = threadIdx.x; t < len; t += blockDim.x) {
       const int k = col.koff + t;
-      const int nz = col.nzlo + t;
+      const int nz = col.nzlo + col.zstep * t;
       const double RXV = (twopi * col.nx) / bx;
-      const double RYV = (twopi * col.ny) / by;
+      const double RYV = ryv / by;
       const double RZV = (twopi * nz) / bz;
       const double RK2 = RXV * RXV + RYV * RYV + RZV * RZV;
       const double AKC = cfur * exp(-0.25 * RK2 / alp2) / RK2;
@@ -432,7 +442,8 @@ __global__ void k_wpairs(int ncol, const KCol *__restrict__ cols, const dbl4 *__
   for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
     const KCol col = cols[c];
     for (int p = threadIdx.x; p <= col.m; p += blockDim.x) {
-      const int kp = kcol_k(col, p), km = p > 0 ? kcol_k(col, -p) : -1;
+      const int z = kcol_z(col, p);
+      const int kp = kcol_k(col, z), km = z > 0 ? kcol_k(col, -z) : -1;
       dbl4 a, b;
       a.x = a.y = a.z = a.w = 0.0;
       b = a;
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(RF_ATOMS *RF_PARTS) k_rforce64(
       const dbl4 *w = wp + 2 * (size_t)col.poff;
 #pragma unroll 4
       for (int p = 0; p <= col.m; ++p) {
-        const double2 z = Z[(size_t)p * n];
+        const double2 z = Z[(size_t)kcol_z(col, p) * n];
         const dbl4 u = w[2 * p], v = w[2 * p + 1];
         ux = fma(u.x, z.x, ux);
         ux = fma(-u.w, z.y, ux);
@@ -708,11 +719,12 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
 template <typename R>
 __device__ __forceinline__ void eterms_pair(
     int isp, int jsp, int ityp, const dbl4 &pi, const dbl4 &pj, double coulf,
-    double alphad, double bx, double by, double bz, const TypeConst &tc,
+    double alphad, double bx, double by, double bz, const CellPbc &cell, const TypeConst &tc,
     R *acc, double *gx, double *gy, double *gz,
     unsigned long long *gfix, int n, float fscalef) {
   double DXd = pi.x - pj.x, DYd = pi.y - pj.y, DZd = pi.z - pj.z;
-  pbc_rect(DXd, DYd, DZd, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  if (cell.icell == 0) pbc_rect(DXd, DYd, DZd, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  else pbc_cell(DXd, DYd, DZd, cell);  // forces.f:1516-1551
   const R QIJ = (R)(coulf * pi.w * pj.w);
   const R DX = (R)DXd, DY = (R)DYd, DZ = (R)DZd;
   const R R2 = DX * DX + DY * DY + DZ * DZ;
@@ -759,7 +771,7 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
                          const int *__restrict__ inbb, int nbdmax,
                          const int *__restrict__ mol_first, TypeConst tc,
                          double coulf, double alphad, double bx, double by,
-                         double bz, double *gx, double *gy, double *gz,
+                         double bz, CellPbc cell, double *gx, double *gy, double *gz,
                          unsigned long long *gfix, float fscalef, Dst6 dst,
                          double *spee) {
   __shared__ double spee_sh[MDX_NT];
@@ -779,15 +791,15 @@ __global__ void k_eterms(int n, const dbl4 *__restrict__ pos,
         int jf = inbb[isp * nbdmax + k];
         int jsp = (jf < 0 ? -jf : jf) - 1;
         if (isp > jsp)
-          eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc, acc, gx,
-                         gy, gz, gfix, n, fscalef);
+          eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, cell, tc,
+                         acc, gx, gy, gz, gfix, n, fscalef);
       }
     } else {
       // EE molecule: every intramolecular pair JSM < ISM (forces.f:1585-1594)
       const int f = mol_first[ai.y];
       for (int jsp = f; jsp < isp; ++jsp)
-        eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, tc, acc, gx,
-                       gy, gz, gfix, n, fscalef);
+        eterms_pair<R>(isp, jsp, ityp, pi, pos[jsp], coulf, alphad, bx, by, bz, cell, tc,
+                       acc, gx, gy, gz, gfix, n, fscalef);
     }
     // SPEE of the atom's type: the thread's own sum (one shared atomic per
     // thread, not per pair)
@@ -838,8 +850,9 @@ cudaError_t raise_smem_limit_fn(const void *kernel, size_t bytes) {
 // INIFUR: the reference's k-set (forces.f:1366-1424) regrouped in columns,
 // and the self-energy SPEEI/SPEI (forces.f:1426-1447).
 int host_inifur(mdx_ctx *ctx) {
-  if (ctx->p.icell != 0) {
-    ctx->err = "Ewald sum for non-rectangular cells is not built";
+  const int icell = ctx->p.icell;
+  if (icell != 0 && ctx->mixed()) {
+    ctx->err = "non-rectangular cells run on the FP64 path only";
     return MDX_ERR_UNSUPPORTED;
   }
   DevData &d = ctx->dv;
@@ -852,19 +865,24 @@ int host_inifur(mdx_ctx *ctx) {
   const int KMAX = (int)(CUTK * ctx->boxl / TWOPI + 1);
   const int KMAY = (int)(CUTK * ctx->boyl / TWOPI + 1);
   const int KMAZ = (int)(CUTK * ctx->bozl / TWOPI + 1);
-  const int NY = 2 * KMAY + 1, NZ = 2 * KMAZ + 1;
+  // the z index of a k-vector: IKZ, or -IKX + IKY + 2 IKZ in the truncated
+  // octahedron (forces.f:1392-1406)
+  const int MZ = icell == 1 ? KMAX + KMAY + 2 * KMAZ : KMAZ;
+  const int NY = 2 * KMAY + 1, NZ = 2 * MZ + 1;
   std::vector<unsigned char> in((size_t)(KMAX + 1) * NY * NZ, 0);
   int nkv = 0;
   for (int IKZ = -KMAZ; IKZ <= KMAZ; ++IKZ)
     for (int IKX = 0; IKX <= KMAX; ++IKX) {
       int KY1 = IKX == 0 ? (IKZ > 0 ? 0 : 1) : -KMAY;
       for (int IKY = KY1; IKY <= KMAY; ++IKY) {
-        double RXV = TWOPI * IKX, RYV = TWOPI * IKY, RZV = TWOPI * IKZ;
+        const int iz = icell == 1 ? -IKX + IKY + 2 * IKZ : IKZ;
+        double RXV = TWOPI * IKX, RYV = TWOPI * IKY, RZV = TWOPI * iz;
+        if (icell == 2) RYV = TWOPI * IKY + PI_REF * IKX;
         double rx = RXV / ctx->boxl, ry = RYV / ctx->boyl, rz = RZV / ctx->bozl;
         double RK2 = rx * rx + ry * ry + rz * rz;
         if (RK2 <= CUTK2) {
           ++nkv;
-          in[((size_t)IKX * NY + (IKY + KMAY)) * NZ + (IKZ + KMAZ)] = 1;
+          in[((size_t)IKX * NY + (IKY + KMAY)) * NZ + (iz + MZ)] = 1;
         }
       }
     }
@@ -874,24 +892,31 @@ int host_inifur(mdx_ctx *ctx) {
   }
   std::vector<KCol> cols;
   std::vector<Chunk> chunks;
-  int koff = 0, poff = 0;
+  int koff = 0, poff = 0, mzmax = 0;
+  const int zstep = icell == 1 ? 2 : 1;
   for (int ix = 0; ix <= KMAX; ++ix)
     for (int iy = -KMAY; iy <= KMAY; ++iy) {
       int lo = 1 << 30, hi = -(1 << 30), cnt = 0;
-      for (int iz = -KMAZ; iz <= KMAZ; ++iz)
-        if (in[((size_t)ix * NY + (iy + KMAY)) * NZ + (iz + KMAZ)]) {
+      for (int iz = -MZ; iz <= MZ; ++iz)
+        if (in[((size_t)ix * NY + (iy + KMAY)) * NZ + (iz + MZ)]) {
           lo = std::min(lo, iz);
           hi = std::max(hi, iz);
           ++cnt;
         }
       if (!cnt) continue;
-      if (cnt != hi - lo + 1) {
+      bool steps = cnt == (hi - lo) / zstep + 1 && (hi - lo) % zstep == 0;
+      for (int iz = lo; steps && iz <= hi; iz += zstep)
+        steps = in[((size_t)ix * NY + (iy + KMAY)) * NZ + (iz + MZ)] != 0;
+      if (!steps) {
         ctx->err = "k-set column is not contiguous";
         return MDX_ERR_UNSUPPORTED;
       }
       const int c = (int)cols.size();
-      const int m = std::max(std::abs(lo), std::abs(hi));
-      cols.push_back(KCol{ix, iy, lo, hi, koff, 0, m, poff});
+      const int zmax = std::max(std::abs(lo), std::abs(hi));
+      const int zoff = zmax % zstep;
+      const int m = (zmax - zoff) / zstep;
+      mzmax = std::max(mzmax, zmax);
+      cols.push_back(KCol{ix, iy, lo, hi, koff, 0, m, poff, zoff, zstep});
       for (int p0 = 0; p0 <= m; p0 += CH)
         chunks.push_back(Chunk{c, p0, std::min(CH, m - p0 + 1), 0});
       koff += cnt;
@@ -924,7 +949,7 @@ int host_inifur(mdx_ctx *ctx) {
     for (int t0 = 0; t0 < groups[g].len; t0 += SCH) items.push_back(SItem{(int)g, t0});
   std::stable_sort(items.begin(), items.end(),
                    [](const SItem &a, const SItem &b) { return a.t0 < b.t0; });
-  const int kx = KMAX + 1, ky = KMAY + 1, kz = KMAZ + 1;
+  const int kx = KMAX + 1, ky = KMAY + 1, kz = (icell == 1 ? mzmax : KMAZ) + 1;
   d.ldn = ((d.n + 127) / 128) * 128;  // row stride of the FP32 tables
   const bool realloc_tables = kx != d.kx || ky != d.ky || kz != d.kz;
   d.kx = kx;
@@ -1151,7 +1176,8 @@ int furir_sfac(mdx_ctx *ctx, bool *skip) {
     MDX_TIMER(ctx, MDX_T_EW_TABLES);
     k_tables<<<(3 * d.n + 255) / 256, 256, 0, ctx->stream>>>(
         d.n, d.ldn, d.pos, ibx, iby, ibz, d.kx, d.ky, d.kz, d.tabx, d.taby, d.tabz,
-        d.tabxf, d.tabyf, d.tabzf, mx ? d.posi : nullptr);
+        d.tabxf, d.tabyf, d.tabzf, mx ? d.posi : nullptr,
+        ctx->p.icell == 2 ? 0.5 * iby : 0.0);
     MDX_LAUNCHED(ctx);
     if (mx && (rc = tc_zimages_launch(ctx))) return rc;
   }
@@ -1190,14 +1216,15 @@ int furir_sfac(mdx_ctx *ctx, bool *skip) {
 // for the current box, rebuilt only when the box or alpha changed.
 int ensure_kconst(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
-  const double vol = ctx->boxl * ctx->boyl * ctx->bozl;
+  double vol = ctx->boxl * ctx->boyl * ctx->bozl;
+  if (ctx->p.icell == 1) vol = 0.5 * vol;  // the octahedron is half its cube (service.f:602)
   const double alp2 = ctx->p.alphad * ctx->p.alphad;
   const double cfur = 4.0 * PI_REF * ctx->p.coulf / vol;
   if (ctx->kc_box[0] != ctx->boxl || ctx->kc_box[1] != ctx->boyl ||
       ctx->kc_box[2] != ctx->bozl || ctx->kc_box[3] != alp2 || ctx->kc_box[4] != cfur) {
     k_kconst<<<std::min(d.ncol, 1024), 64, 0, ctx->stream>>>(
         d.ncol, d.cols, ctx->boxl, ctx->boyl, ctx->bozl, alp2, cfur, d.kconst, d.colrv,
-        d.colrvf);
+        d.colrvf, ctx->p.icell == 2 ? PI_REF : 0.0);
     MDX_LAUNCHED(ctx);
     ctx->kc_box[0] = ctx->boxl;
     ctx->kc_box[1] = ctx->boyl;
@@ -1263,13 +1290,13 @@ int launch_eterms(mdx_ctx *ctx) {
   if (ctx->mixed())
     k_eterms<float><<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
         d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc, ctx->p.coulf,
-        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy, d.gz, d.gfix,
-        ctx->fix.scalef, dst, sc->spee);
+        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, cell_pbc(ctx), d.gx, d.gy, d.gz,
+        d.gfix, ctx->fix.scalef, dst, sc->spee);
   else
     k_eterms<double><<<(d.n + 127) / 128, 128, 0, ctx->stream>>>(
         d.n, d.pos, d.ainfo, d.nnbb, d.inbb, d.nbdmax, d.mol_first, ctx->tc, ctx->p.coulf,
-        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, d.gx, d.gy, d.gz, nullptr, 0.f, dst,
-        sc->spee);
+        ctx->p.alphad, ctx->boxl, ctx->boyl, ctx->bozl, cell_pbc(ctx), d.gx, d.gy, d.gz,
+        nullptr, 0.f, dst, sc->spee);
   MDX_LAUNCHED(ctx);
   return MDX_OK;
 }

@@ -83,7 +83,15 @@ __global__ void k_sum_forces(int n, const double *gx, const double *gy,
 struct MolConst {
   double summas[MDX_NT];
   double rsummas[MDX_NT];  // 1 / summas (mixed path's centre of mass)
+  CellPbc cell;            // cell shape of the centres' PBC (service.f:530-537)
 };
+
+// PBC of a centre of mass: the rectangular fold, or the cell's
+__device__ __forceinline__ void pbc_com(double &x, double &y, double &z, double bx, double by,
+                                        double bz, const MolConst &mc) {
+  if (mc.cell.icell == 0) pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  else pbc_cell(x, y, z, mc.cell);
+}
 
 // GETCOM (service.f:463-563); with posi set it also refreshes the
 // fixed-point mirror of the wrapped positions (what k_mirror writes for the
@@ -112,7 +120,7 @@ __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
   y = y / summ;
   z = z / summ;
   double xw = x, yw = y, zw = z;
-  pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  pbc_com(xw, yw, zw, bx, by, bz, mc);
   X[m] = xw;
   Y[m] = yw;
   Z[m] = zw;
@@ -281,7 +289,7 @@ __device__ __forceinline__ void kick_drift_com_body(int m, int nop, const int *_
     y = y * rs;
     z = z * rs;
     double xw = x, yw = y, zw = z;
-    pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+    pbc_com(xw, yw, zw, bx, by, bz, mc);
     X[m] = xw;
     Y[m] = yw;
     Z[m] = zw;
@@ -355,7 +363,7 @@ __device__ __forceinline__ void kick_drift_com_body(int m, int nop, const int *_
     z = z / summ;
   }
   double xw = x, yw = y, zw = z;
-  pbc_rect(xw, yw, zw, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  pbc_com(xw, yw, zw, bx, by, bz, mc);
   X[m] = xw;
   Y[m] = yw;
   Z[m] = zw;
@@ -1025,6 +1033,7 @@ struct ShakeConst {
   int iadb[MDX_NT], nrb[MDX_NT], ishejk[MDX_NT];
   int maxit;
   double tol2, tstep;
+  CellPbc cell;
 };
 
 // SHEJK (mdstep.f:1105-1283) over independent constraint clusters.  The
@@ -1080,12 +1089,14 @@ __global__ void k_shake_cluster(int nitem, const int2 *__restrict__ items,
       const double BNDSQ = rbb * rbb;
       dbl4 pi = pos[I], pj = pos[J];
       double BXN = pi.x - pj.x, BYN = pi.y - pj.y, BZN = pi.z - pj.z;
-      pbc_rect(BXN, BYN, BZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      if (sk.cell.icell == 0) pbc_rect(BXN, BYN, BZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      else pbc_cell(BXN, BYN, BZN, sk.cell);  // mdstep.f:1175
       const double BSQ = BXN * BXN + BYN * BYN + BZN * BZN;
       const double DIFFSQ = BNDSQ - BSQ;
       if (fabs(DIFFSQ) > (BNDSQ * sk.tol2)) {
         double DXN = ox[I] - ox[J], DYN = oy[I] - oy[J], DZN = oz[I] - oz[J];
-        pbc_rect(DXN, DYN, DZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+        if (sk.cell.icell == 0) pbc_rect(DXN, DYN, DZN, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+        else pbc_cell(DXN, DYN, DZN, sk.cell);  // mdstep.f:1186
         const double VDOT = BXN * DXN + BYN * DYN + BZN * DZN;
         const double RMA = massdi[I], RMB = massdi[J];
         const double GAB = DIFFSQ / (2.0 * (RMA + RMB) * VDOT);
@@ -1344,6 +1355,7 @@ MolConst mol_const(mdx_ctx *ctx) {
     m.summas[t] = ctx->summas[t];
     m.rsummas[t] = ctx->summas[t] != 0.0 ? 1.0 / ctx->summas[t] : 0.0;
   }
+  m.cell = cell_pbc(ctx);
   return m;
 }
 
@@ -1892,6 +1904,7 @@ int launch_leapfrog_shake(mdx_ctx *ctx) {
     sk.maxit = ctx->p.maxit > 0 ? ctx->p.maxit : 2000;
     sk.tol2 = ctx->p.toler * ctx->p.toler;
     sk.tstep = ctx->p.tstep;
+    sk.cell = cell_pbc(ctx);
     if (d.shk_nitem > 0) {
       k_shake_cluster<<<(d.shk_nitem + 63) / 64, 64, 0, ctx->stream>>>(
           d.shk_nitem, d.shk_item, d.shk_cl, d.shk_rec, d.mol_first, d.mol_type,

@@ -186,6 +186,10 @@ extern "C" int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double p
     ctx->err = "mdx_ee_delta: neighbour lists not built";
     return MDX_ERR_STATE;
   }
+  if (ctx->p.icell != 0) {
+    ctx->err = "mdx_ee_delta: rectangular cells only";
+    return MDX_ERR_UNSUPPORTED;
+  }
   if (ctx->p.lmnbl) {
     ctx->err = "mdx_ee_delta: reaction field not built";
     return MDX_ERR_UNSUPPORTED;

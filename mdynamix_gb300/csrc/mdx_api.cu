@@ -64,7 +64,7 @@ __global__ void k_com_only(int nop, const int *mol_first, const int *mol_nat,
                            const int *mol_type, const double *amass,
                            const dbl4 *pos, double *X, double *Y, double *Z,
                            const double *summas, double bx, double by,
-                           double bz) {
+                           double bz, CellPbc cell) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nop) return;
   const int f = mol_first[m], na = mol_nat[m];
@@ -79,7 +79,8 @@ __global__ void k_com_only(int nop, const int *mol_first, const int *mol_nat,
   x = x / s;
   y = y / s;
   z = z / s;
-  pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  if (cell.icell == 0) pbc_rect(x, y, z, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  else pbc_cell(x, y, z, cell);
   X[m] = x;
   Y[m] = y;
   Z[m] = z;
@@ -933,8 +934,12 @@ int mdx_upload_topology(mdx_ctx *ctx, const mdx_topo *t) {
 
 int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
   if (!ctx || !p) return MDX_ERR_ARG;
-  if (p->icell != 0) {
-    ctx->err = "only rectangular cells (ICELL=0) are built";
+  if (p->icell < 0 || p->icell > 2) {
+    ctx->err = "ICELL must be 0 (rectangular), 1 (truncated octahedron) or 2 (hexagonal)";
+    return MDX_ERR_ARG;
+  }
+  if (p->icell != 0 && (ctx->mixed() || p->lnpt || p->rskin > 0.0)) {
+    ctx->err = "non-rectangular cells: FP64 path, constant volume, reference list mode only";
     return MDX_ERR_UNSUPPORTED;
   }
   if (p->boxl <= 0 || p->boyl <= 0 || p->bozl <= 0 || p->rcut <= 0 || p->nfreq < 1 ||
@@ -1068,6 +1073,7 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
     h.bozl = ctx->bozl;
   }
   h.vol = h.boxl * h.boyl * h.bozl;
+  if (ctx->p.icell == 1) h.vol = 0.5 * h.vol;  // RECLEN (service.f:602)
   RC(upload(ctx, d.th, &h, 1));
   // molecular centres (the driver's last GETCOM left them consistent)
   std::vector<double> sm(MDX_NT, 1.0);
@@ -1076,7 +1082,7 @@ int mdx_upload_state(mdx_ctx *ctx, const double *sx, const double *sy,
   RC(upload(ctx, dsm, sm.data(), MDX_NT));
   k_com_only<<<(d.nop + 127) / 128, 128, 0, ctx->stream>>>(
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.amass, d.pos, d.X, d.Y, d.Z, dsm,
-      ctx->boxl, ctx->boyl, ctx->bozl);
+      ctx->boxl, ctx->boyl, ctx->bozl, cell_pbc(ctx));
   ctx->launches++;
   RC(launch_mirror_f32(ctx));
   MDX_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -82,6 +82,8 @@ void resolve_tuning(mdx_ctx *ctx);  // pair.cu: the tuning table's choice, once
 // atom count alone, so the sums' order is fixed for a system.
 struct mdx_ctx;
 int red_blocks(const mdx_ctx *ctx);
+struct CellPbc;
+CellPbc cell_pbc(const mdx_ctx *ctx);  // the context's cell and box (pair.cu)
 
 // Cell grid used by the list build.
 struct CellGrid {
@@ -89,19 +91,31 @@ struct CellGrid {
   double cx, cy, cz;  // cell edge lengths
 };
 
-// Ewald k-space layout: k-vectors grouped in columns of fixed (nx, ny) with a
-// contiguous nz range; tables of per-atom phase factors e^{i n theta}.
+// Ewald k-space layout: k-vectors grouped in columns of fixed (nx, ny) with
+// an nz range in steps of zstep; tables of per-atom phase factors
+// e^{i n theta}.  Record p of a column pairs nz = +z(p) and -z(p), z(p) =
+// zoff + zstep p: rectangular and hexagonal cells zoff 0, zstep 1; the
+// truncated octahedron's k-set (forces.f:1392-1397: RZV = 2 pi (-IKX + IKY +
+// 2 IKZ)) has in each column the nz of one parity, zoff = that parity,
+// zstep 2.
 struct KCol {
-  int nx, ny, nzlo, nzhi;  // integer k components (rectangular cell)
+  int nx, ny, nzlo, nzhi;  // integer k components
   int koff;                // first k of the column in the column-ordered list
   int wpos;                // mixed: slot of (group, p = 0) in the paired W array
-  int m;                   // max |nz|: the column pairs nz = +p and -p, p = 0..m
+  int m;                   // last record: the column pairs nz = +z(p) and -z(p), p = 0..m
   int poff;                // FP64: first paired-W record of the column
+  int zoff, zstep;         // z(p) = zoff + zstep p
 };
 
-// k index of (column, nz), -1 outside the column's range.
+// k index of (column, nz), -1 outside the column's set.
 __host__ __device__ __forceinline__ int kcol_k(const KCol &c, int nz) {
-  return nz < c.nzlo || nz > c.nzhi ? -1 : c.koff + (nz - c.nzlo);
+  if (nz < c.nzlo || nz > c.nzhi) return -1;
+  const int d = nz - c.nzlo;
+  if (c.zstep == 1) return c.koff + d;
+  return d % c.zstep ? -1 : c.koff + d / c.zstep;
+}
+__host__ __device__ __forceinline__ int kcol_z(const KCol &c, int p) {
+  return c.zoff + c.zstep * p;
 }
 
 // Bonds and angles of one small molecule type, atoms as offsets within the
@@ -421,6 +435,60 @@ __device__ __forceinline__ void pbc_rect(double &dx, double &dy, double &dz,
   if (fabs(dz) > hbz) dz = dz - fsign(bz, dz);
   if (fabs(dy) > hby) dy = dy - fsign(by, dy);
 }
+// Minimum image of the three cell shapes of PBC (service.f:953-990, and
+// its inlined copies in LOCALF, FORCES, ETERMS and CHCNB): ICELL 0
+// rectangular; 2 hexagonal (the x-y lattice (BOXL, 0), (HBOXL, BOYL), BOYL =
+// BOXL cos30, minimum image up to 1.5 BOXL from the centre); 1 truncated
+// octahedron (the cube's image, then the fold |x| + |y| + |z| < 0.75 BOXL).
+// cos30 and 4/3 are the reference's REAL*4 literals (common_inc.f:33,
+// service.f:985).  hbz: HBOZL, or HBOXL in LOCALF (forces.f:873).
+struct CellPbc {
+  int icell;
+  double bx, by, bz, hbx, hby, hbz, boxy3;
+};
+
+__device__ __forceinline__ void pbc_cell(double &xx, double &yy, double &zz, const CellPbc &c,
+                                         double hbz) {
+  if (fabs(xx) > c.hbx) xx = xx - fsign(c.bx, xx);
+  if (fabs(zz) > hbz) zz = zz - fsign(c.bz, zz);
+  if (c.icell == 2) {
+    const double cos30 = (double)0.8660254037844386f;
+    const double boxyc = 0.5 / cos30;
+    double xy = boxyc * xx;
+    if (yy > c.boxy3 - xy && (xx > 0. || yy > 2. * c.boxy3 - xy)) {
+      yy = yy - c.by;
+      xx = xx - c.hbx;
+      xy = boxyc * xx;
+    }
+    if (yy < -c.boxy3 - xy && (xx < 0. || yy < -2. * c.boxy3 - xy)) {
+      yy = yy + c.by;
+      xx = xx + c.hbx;
+      xy = boxyc * xx;
+    }
+    if (yy > c.boxy3 + xy) {
+      yy = yy - c.by;
+      xx = xx + c.hbx;
+      xy = boxyc * xx;
+    }
+    if (yy < -c.boxy3 + xy) {
+      yy = yy + c.by;
+      xx = xx - c.hbx;
+    }
+  } else {
+    if (fabs(yy) > c.hby) yy = yy - fsign(c.by, yy);
+  }
+  if (c.icell == 1) {
+    const double corss =
+        c.hbx * (double)(int)((double)(4.0f / 3.0f) * (fabs(xx) + fabs(yy) + fabs(zz)) / c.bx);
+    xx = xx - fsign(corss, xx);
+    yy = yy - fsign(corss, yy);
+    zz = zz - fsign(corss, zz);
+  }
+}
+__device__ __forceinline__ void pbc_cell(double &xx, double &yy, double &zz, const CellPbc &c) {
+  pbc_cell(xx, yy, zz, c, c.hbz);
+}
+
 __device__ __forceinline__ void pbc_rectf(float &dx, float &dy, float &dz,
                                           float bx, float by, float bz,
                                           float hbx, float hby, float hbz) {

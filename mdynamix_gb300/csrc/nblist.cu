@@ -28,7 +28,19 @@ namespace {
 
 struct BoxD {
   double bx, by, bz, hbx, hby, hbz;
+  int icell;     // ICELL: 0 rectangular, 1 truncated octahedron, 2 hexagonal
+  double boxy3;  // BOXY3 of the hexagonal cell
 };
+
+// CHCNB's minimum image for the box's cell shape (forces.f:1840-1875)
+__device__ __forceinline__ void pbc_box(double &dx, double &dy, double &dz, const BoxD &b) {
+  if (b.icell == 0) {
+    pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+  } else {
+    const CellPbc c{b.icell, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz, b.boxy3};
+    pbc_cell(dx, dy, dz, c);
+  }
+}
 
 // Skin mode: the list kernels of a step run only when the displacement check
 // of that step asked for a rebuild (gate == nullptr: always).
@@ -167,7 +179,7 @@ __device__ __forceinline__ int classify_exact(
     const BoxD &b, double short2, double rl2, const int *__restrict__ nnbb,
     const int *__restrict__ inbb, int nbdmax, const MolCut &mc) {
   double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-  pbc_rect(dx, dy, dz, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+  pbc_box(dx, dy, dz, b);
   double rr2 = dx * dx + dy * dy + dz * dz;
   double rrm = rr2;
   if (LMNBL) {
@@ -183,7 +195,7 @@ __device__ __forceinline__ int classify_exact(
       } else {
         ex = mc.X[ai.y] - mc.X[aj.y]; ey = mc.Y[ai.y] - mc.Y[aj.y]; ez = mc.Z[ai.y] - mc.Z[aj.y];
       }
-      pbc_rect(ex, ey, ez, b.bx, b.by, b.bz, b.hbx, b.hby, b.hbz);
+      pbc_box(ex, ey, ez, b);
       rrm = ex * ex + ey * ey + ez * ez;
     }
   }
@@ -263,7 +275,8 @@ __global__ void __launch_bounds__(BLK) k_build(
               const bool same =
                   posi ? ((unsigned)qj.w >> MDX_SITE_BITS) == ((unsigned)qi.w >> MDX_SITE_BITS)
                        : qj.w == imol;
-              if (same || LMNBL) {  // the molecular cutoff: exact test only
+              // the molecular cutoff and the non-rectangular cells: exact test only
+              if (same || LMNBL || b.icell) {
                 kind = classify_exact<LMNBL>(i, j, same, pi, pos[j], b, short2, rl2,
                                       nnbb, inbb, nbdmax, mc);
               } else {
@@ -445,14 +458,17 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
           ? rl + 2.0 * ctx->mol_reach
           : rl + std::min(ctx->boxl, std::min(ctx->boyl, ctx->bozl));  // reach unknown
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
-         0.5 * ctx->bozl};
+         0.5 * ctx->bozl, ctx->p.icell, 0.66666666666666666667 * ctx->boyl};
   CellGrid g;
   // cells at least rl / CELL_REACH wide, stencil +-CELL_REACH cells (a
   // (2 R + 1)^3 stencil of thinner cells tests fewer far candidates than
-  // 27 cells of width rl); below 2 R + 1 cells a dimension is scanned whole
-  g.nx = std::max(1, (int)std::floor(CELL_REACH * ctx->boxl / rsearch));
-  g.ny = std::max(1, (int)std::floor(CELL_REACH * ctx->boyl / rsearch));
-  g.nz = std::max(1, (int)std::floor(CELL_REACH * ctx->bozl / rsearch));
+  // 27 cells of width rl); below 2 R + 1 cells a dimension is scanned whole.
+  // A non-rectangular cell's nearest image need not lie in the rectangular
+  // stencil: one cell, every pair tested (as the reference's CHCNB does).
+  const bool whole = ctx->p.icell != 0;
+  g.nx = whole ? 1 : std::max(1, (int)std::floor(CELL_REACH * ctx->boxl / rsearch));
+  g.ny = whole ? 1 : std::max(1, (int)std::floor(CELL_REACH * ctx->boyl / rsearch));
+  g.nz = whole ? 1 : std::max(1, (int)std::floor(CELL_REACH * ctx->bozl / rsearch));
   g.cx = ctx->boxl / g.nx;
   g.cy = ctx->boyl / g.ny;
   g.cz = ctx->bozl / g.nz;
@@ -548,7 +564,7 @@ int launch_list_update(mdx_ctx *ctx, int mstep) {
   }
   int *gate = d.shake_iter + 6;
   BoxD b{ctx->boxl, ctx->boyl, ctx->bozl, 0.5 * ctx->boxl, 0.5 * ctx->boyl,
-         0.5 * ctx->bozl};
+         0.5 * ctx->bozl, 0, 0.0};  // skin mode: rectangular cells only
   {
     MDX_TIMER(ctx, MDX_T_LIST);
     k_gate_zero<<<1, 1, 0, ctx->stream>>>(gate);

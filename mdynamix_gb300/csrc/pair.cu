@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) k_pair64(
     int n, const dbl4 *__restrict__ pos, const int4 *__restrict__ ainfo,
     const double *__restrict__ qsite, const int *__restrict__ cnt,
     const int *__restrict__ idx, int cap, PairTables tb, TypeConst tc,
-    PairConst pc, double bx, double by, double bz, double *__restrict__ fx,
+    PairConst pc, double bx, double by, double bz, CellPbc cp, double *__restrict__ fx,
     double *__restrict__ fy, double *__restrict__ fz,
     Dst6 dst, double *__restrict__ split) {
   __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
@@ -114,9 +114,13 @@ __global__ void __launch_bounds__(256) k_pair64(
       }
       double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
       constexpr long long MAG = 0x7fffffffffffffffLL;
-      if ((__double_as_longlong(DX) & MAG) > hbxb) DX = DX - fsign(bx, DX);
-      if ((__double_as_longlong(DZ) & MAG) > hbzb) DZ = DZ - fsign(bz, DZ);
-      if ((__double_as_longlong(DY) & MAG) > hbyb) DY = DY - fsign(by, DY);
+      if (cp.icell == 0) {
+        if ((__double_as_longlong(DX) & MAG) > hbxb) DX = DX - fsign(bx, DX);
+        if ((__double_as_longlong(DZ) & MAG) > hbzb) DZ = DZ - fsign(bz, DZ);
+        if ((__double_as_longlong(DY) & MAG) > hbyb) DY = DY - fsign(by, DY);
+      } else {  // hexagonal / truncated octahedron (forces.f:872-906, 1077-1111)
+        pbc_cell(DX, DY, DZ, cp, SHORT ? cp.hbx : cp.hbz);
+      }
       const double RR = DX * DX + DY * DY + DZ * DZ;
       if (!SHORT && __double_as_longlong(RR) > rc2b) continue;  // skin mode: listed beyond RCUT
       // one reciprocal square root instead of a square root and a division
@@ -560,10 +564,10 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
 #define LP64(S, P)                                                                \
   if (ener) k_pair64<S, P, true><<<grid, T, 0, ctx->stream>>>(                    \
       d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
-      ctx->boxl, ctx->boyl, ctx->bozl, fx, fy, fz, ddst, split_buf);              \
+      ctx->boxl, ctx->boyl, ctx->bozl, cell_pbc(ctx), fx, fy, fz, ddst, split_buf); \
   else k_pair64<S, P, false><<<grid, T, 0, ctx->stream>>>(                        \
       d.n, d.pos, d.ainfo, d.qsite, cnt, idx, cap, tables(d), ctx->tc, ctx->pc,   \
-      ctx->boxl, ctx->boyl, ctx->bozl, fx, fy, fz, ddst, split_buf)
+      ctx->boxl, ctx->boyl, ctx->bozl, cell_pbc(ctx), fx, fy, fz, ddst, split_buf)
     if (shrt) {
       if (split) { LP64(true, true); } else { LP64(true, false); }
     } else {
@@ -633,6 +637,19 @@ int tune_pick(const TuneCell (&cells)[N], int n, double row, int dflt) {
 }
 
 }  // namespace
+
+CellPbc cell_pbc(const mdx_ctx *ctx) {
+  CellPbc c{};
+  c.icell = ctx->p.icell;
+  c.bx = ctx->boxl;
+  c.by = ctx->boyl;
+  c.bz = ctx->bozl;
+  c.hbx = 0.5 * ctx->boxl;
+  c.hby = 0.5 * ctx->boyl;
+  c.hbz = 0.5 * ctx->bozl;
+  c.boxy3 = 0.66666666666666666667 * ctx->boyl;  // RECLEN (service.f:579)
+  return c;
+}
 
 int red_blocks(const mdx_ctx *ctx) {
   return std::max(1, std::min(ctx->nsm, (ctx->dv.n + 255) / 256));

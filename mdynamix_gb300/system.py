@@ -46,6 +46,7 @@ COS30 = float(np.float32(0.8660254037844386))  # REAL*4 literal, common_inc.f:33
 NTPS = 10
 NTPP = NTPS * (NTPS + 1) // 2 + 1
 F32_1EM5 = float(np.float32(1.0e-5))           # UNITP literal, setup.f:103
+COS30 = float(np.float32(0.8660254037844386))  # cos30, a REAL*4 literal (common_inc.f:33)
 BDTOL_DEFAULT = float(np.float32(0.0001))       # main.f:124
 
 DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
@@ -344,6 +345,7 @@ class RunSpec:
     iee_type: Optional[int] = None                 # EE_type (1-based)
     nbeads: int = 1                                # PIMD NBEADS (bead masses MASS/NBEADS)
     pi_thermo: Optional[Tuple[float, int]] = None  # PI_thermo BTAU (fs), JNH (TRTEMP: trtemp)
+    icell: int = 0                                 # PBC: 0 rectangular, 1 truncated octahedron, 2 hexagonal
 
 
 class System:
@@ -440,14 +442,26 @@ class System:
         fnop = float(self.nop)
         self.fnop = fnop
         avofnr = AVSNO / fnop
-        if sp.box is None:
+        if sp.box is None:  # setup.f:38-60
             volm = avofnr * (totmas / (sp.density * 1000.0))
             vol = volm * fnop * 1.0e30 / AVSNO
+            if sp.icell == 1:
+                vol = 2.0 * vol
+            elif sp.icell == 2:
+                vol = vol / COS30
             cl = vol ** (1.0 / 3.0)
             self.boxl = self.boyl = self.bozl = cl
+            if sp.icell == 2:
+                self.boyl = self.boxl * COS30
         else:
             self.boxl, self.boyl, self.bozl = (float(x) for x in sp.box)
+            if sp.icell == 2:  # RECLEN (service.f:576-579)
+                self.boyl = self.boxl * COS30
+            elif sp.icell == 1:
+                self.boyl = self.bozl = self.boxl
         self.vol = self.boxl * self.boyl * self.bozl
+        if sp.icell == 1:  # the truncated octahedron is half its cube (service.f:602)
+            self.vol = 0.5 * self.vol
         self.rcutt = sp.rcut
         if sp.alpha <= 0.0:  # reaction field: a spherical cutoff within L/2 (main.f:745-749)
             self.rcutt = min(self.rcutt, 0.5 * min(self.boxl, self.boyl, self.bozl))
@@ -825,7 +839,8 @@ class System:
 
     # --------------------------------------------------------- helpers ---
     def kvector_count(self) -> int:
-        return kvector_count(self.alphad, self.fexp, self.boxl, self.boyl, self.bozl)
+        return kvector_count(self.alphad, self.fexp, self.boxl, self.boyl, self.bozl,
+                             self.spec.icell)
 
     def kcolumn_counts(self) -> Tuple[int, int, int]:
         return kcolumn_counts(self.alphad, self.fexp, self.boxl, self.boyl, self.bozl)
@@ -919,6 +934,52 @@ def _lattice_with_room(rng, nside: int, nop: int, big: List[int]) -> np.ndarray:
     return cell_of
 
 
+def _cell_lattice(s: System, rng):
+    """Molecular centres for the non-rectangular cells: a point set that the
+    cell's lattice maps onto itself, one point of each lattice class (each
+    brought into the cell by the cell's minimum image), in random order,
+    shifted off the cell's faces.  Truncated octahedron (ICELL 1): a
+    body-centred grid of the cube, n^3 classes, nearest points sqrt(3)/2 of
+    the grid spacing apart (n even: the half-diagonal (L/2)(1, 1, 1) is a
+    grid vector).  Hexagonal (ICELL 2): the grid of the L x L cos30 x Lz
+    rectangle with an even count along x (the lattice vector
+    (L/2, L cos30, 0) is then a grid vector)."""
+    nop = s.nop
+    box = np.array([s.boxl, s.boyl, s.bozl])
+    if s.spec.icell == 1:
+        L = s.boxl
+        n = 2
+        while n ** 3 < nop:
+            n += 2
+        a = L / n
+        g = np.arange(n) * a - 0.5 * L
+        cube = np.array([(x, y, z) for x in g for y in g for z in g])
+        pts = np.concatenate([cube, cube + 0.5 * a]) + np.array([0.11, 0.23, 0.37]) * a
+        pts = pts - L * np.round(pts / L)  # cube wrap, then the octahedral fold
+        corss = 0.5 * L * np.floor((4.0 / 3.0) * np.abs(pts).sum(axis=1) / L)
+        pts = pts - np.sign(pts) * corss[:, None]
+        key = np.round(pts / (1e-6 * L)).astype(np.int64)
+        _, first = np.unique(key, axis=0, return_index=True)
+        pts = pts[np.sort(first)]
+        a = np.full(3, a)
+    else:
+        # the counts with the largest smallest spacing that hold nop points
+        best = None
+        for nx in range(2, 2 * int(s.boxl) + 3, 2):
+            for ny in range(1, int(s.boyl) + 2):
+                nz = max(1, -(-nop // (nx * ny)))
+                gap = min(s.boxl / nx, s.boyl / ny, s.bozl / nz)
+                if best is None or gap > best[0]:
+                    best = (gap, nx, ny, nz)
+        _, nx, ny, nz = best
+        a = box / np.array([nx, ny, nz])
+        pts = np.array([((i + 0.5) * a[0], (j + 0.5) * a[1], (k + 0.5) * a[2])
+                        for i in range(nx) for j in range(ny) for k in range(nz)]) - 0.5 * box
+    if len(pts) < nop:
+        raise ValueError("cell lattice too small")
+    return pts[rng.permutation(len(pts))[:nop]], a
+
+
 def make_configuration(s: System, seed: int = 1, jitter: float = 0.3,
                        order: Optional[np.ndarray] = None):
     """Seeded start: molecular centres on a jittered simple-cubic lattice
@@ -927,19 +988,22 @@ def make_configuration(s: System, seed: int = 1, jitter: float = 0.3,
     reference's formula (main.f:689-714).  Returns sx, sy, sz, vx, vy, vz."""
     rng = np.random.default_rng(seed)
     nop = s.nop
-    nside = int(math.ceil(nop ** (1.0 / 3.0) - 1e-9))
-    cells = np.array([(i, j, k) for i in range(nside) for j in range(nside) for k in range(nside)],
-                     dtype=np.float64)
-    mtype = np.repeat(np.arange(s.ntypes), s.nspec[:s.ntypes])
-    big = [int(m) for m in np.nonzero(s.nsits[mtype] > 3)[0]]
-    if big and len(cells) > nop:
-        cells = cells[_lattice_with_room(rng, nside, nop, big)]
-    else:
-        perm = rng.permutation(len(cells))[:nop]
-        cells = cells[perm]
     box = np.array([s.boxl, s.boyl, s.bozl])
-    a = box / nside
-    com = (cells + 0.5) * a - 0.5 * box
+    if s.spec.icell != 0:
+        com, a = _cell_lattice(s, rng)
+    else:
+        nside = int(math.ceil(nop ** (1.0 / 3.0) - 1e-9))
+        cells = np.array([(i, j, k) for i in range(nside) for j in range(nside)
+                          for k in range(nside)], dtype=np.float64)
+        mtype = np.repeat(np.arange(s.ntypes), s.nspec[:s.ntypes])
+        big = [int(m) for m in np.nonzero(s.nsits[mtype] > 3)[0]]
+        if big and len(cells) > nop:
+            cells = cells[_lattice_with_room(rng, nside, nop, big)]
+        else:
+            perm = rng.permutation(len(cells))[:nop]
+            cells = cells[perm]
+        a = box / nside
+        com = (cells + 0.5) * a - 0.5 * box
     com += rng.uniform(-jitter, jitter, size=com.shape) * a
     sx = np.zeros(s.nstot); sy = np.zeros(s.nstot); sz = np.zeros(s.nstot)
     n = 0

@@ -396,3 +396,29 @@ def test_oracle_pullback_field_and_wells():
     assert np.abs(qz).max() > 0.05 * np.abs(g0).max()
     assert np.allclose(d[:, 2], qz, rtol=1e-9, atol=1e-12 * np.abs(g0).max())
     assert abs(d[atom - 1, 0] - (-k * (st[0][atom - 1] - ref[0]))) < 1e-12 * np.abs(g0).max()
+
+
+@pytest.mark.parametrize("icell", [1, 2])
+def test_cell_shapes_oracle_ewald_consistent(icell):
+    """The oracle's truncated octahedron (ICELL 1) and hexagonal cell
+    (ICELL 2): INIFUR's k-set count equals the host's count of the same rule
+    (forces.f:1392-1406), and the Ewald total (reciprocal + real-space + self
+    terms) barely moves between two splittings (alpha 3.0 / Rc and 3.6 / Rc
+    with B = A^2), as a correct lattice sum must (the rectangular cell moves
+    as much)."""
+    import dataclasses
+    base = dataclasses.replace(systems.spcfw(n=256, ions=2, rcut=8.0), icell=icell)
+    s, st = systems.build(base)
+    out = []
+    for A in (3.0, 3.6):
+        s2 = S.System(dataclasses.replace(base, alpha=A, fexp=A * A))
+        o = oracle.Oracle(s2)
+        o.set_state(*st)
+        assert o.inifur() == s2.kvector_count()
+        o.chcnb()
+        o.getcom()
+        r = o.allforce()
+        out.append((r.pels1 + r.pels2 + r.spe, r.pels1, o.forces(3)))
+    assert abs(out[0][0] - out[1][0]) < 2e-3 * abs(out[0][1])
+    f0, f1 = out[0][2], out[1][2]
+    assert np.abs(f0 - f1).max() < 1e-4 * np.abs(f0).max()

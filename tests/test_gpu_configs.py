@@ -284,3 +284,66 @@ def test_pair_math_against_library():
     # and against numpy's exp / division (the host's libm)
     assert np.all(np.abs(own_e - np.exp(-y)) <= 4 * ulp * np.exp(-y))
     assert np.all(np.abs(own_r - 1.0 / d) <= 4 * ulp / d)
+
+
+# ------------------------------------------- non-rectangular cells ---
+def cell_system(icell, rigid=False):
+    """Water + ions in a truncated octahedron (ICELL 1) or a hexagonal cell
+    (ICELL 2): flexible SPC-FW with DOUBLE, or rigid SPC/E with SULTAN +
+    SHEJK."""
+    base = systems.spce_ions(n=200, ions=2, toler=1e-6) if rigid else systems.spcfw(
+        n=256, ions=2, rcut=8.0)
+    return systems.build(dataclasses.replace(base, icell=icell))
+
+
+@pytest.mark.parametrize("icell", [1, 2])
+def test_cell_shapes_match_oracle(icell):
+    """PBC of the truncated octahedron and the hexagonal cell (service.f:
+    953-990, inlined in LOCALF, FORCES, ETERMS, CHCNB) and INIFUR's k-sets
+    for them (forces.f:1392-1406): lists bit for bit, SLFORCES / FFORCES /
+    ALLFORCE forces and scalars at 1e-10, and three DOUBLE steps."""
+    s, st = cell_system(icell)
+    g, o = _pair(s, st)
+    assert g.inifur() == o.inifur() == s.kvector_count()
+    assert g.chcnb() == o.chcnb()
+    (gs1, gs2), (gl1, gl2) = g.lists()
+    (os1, os2), (ol1, ol2) = o.lists()
+    assert np.array_equal(gs1, os1) and np.array_equal(gs2, os2)
+    assert np.array_equal(gl1, ol1) and np.array_equal(gl2, ol2)
+    g.getcom(); o.getcom()
+    for routine in ("slforces", "fforces", "allforce"):
+        a, b = getattr(g, routine)(), getattr(o, routine)()
+        which = {"slforces": 2, "fforces": 1, "allforce": 3}[routine]
+        assert relmax(g.forces(which), o.forces(which)) < FP64_TOL, routine
+        names = {"slforces": ("pels1", "pe1", "spe", "vir1", "virx", "viry", "virz", "wirs"),
+                 "fforces": ("pels2", "pe2", "vir2", "pint", "wirss"),
+                 "allforce": ("pe1", "pels1", "pe2", "pels2", "spe", "vir1", "vir2", "wirs")}
+        for n in names[routine]:
+            assert abs(getattr(a, n) - getattr(b, n)) <= FP64_TOL * max(abs(getattr(b, n)),
+                                                                        1e-12), (routine, n)
+    g2, o2 = _pair(s, st)
+    g2.double(3), o2.double(3)
+    (gx, gy, gz, *_), _ = g2.get_state()
+    (ox, oy, oz, *_), _ = o2.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
+
+
+@pytest.mark.parametrize("icell", [1, 2])
+def test_cell_shapes_sultan_shake(icell):
+    """Rigid water under SULTAN + SHEJK in the two cells: the constraint
+    vectors take the cell's minimum image (mdstep.f:1175, 1186); three steps
+    against the oracle."""
+    s, st = cell_system(icell, rigid=True)
+    g, o = _pair(s, st)
+    g.sultan(3), o.sultan(3)
+    (gx, gy, gz, *_), _ = g.get_state()
+    (ox, oy, oz, *_), _ = o.get_state()
+    assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
+
+
+def test_cell_shapes_refused_where_not_built():
+    """The mixed path refuses non-rectangular cells (FP64 only)."""
+    from mdynamix_gb300.mdx import ForcePath, MdxError
+    s, st = cell_system(1)
+    with pytest.raises(MdxError):
+        ForcePath(s, precision=MDX_MIXED)
