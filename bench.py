@@ -174,6 +174,23 @@ def roofline_of(timers, mbsh, mbln, nfreq, kset, n, peak64, peak32, prec, nsteps
             "peak_source": "measured in-run FMA probe (mdx_probe_fma_peak, of measured)"}
 
 
+def max_over_ranks(value: float, dist, device) -> float:
+    """The largest of the ranks' values (each replica's timed region: the job
+    takes as long as its slowest rank); the value itself on one rank."""
+    if not dist:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, atoms: int, steps: int, ms: float) -> float:
+    """Whole-job atom-steps/s of ``world`` replicas of ``atoms`` atoms, each
+    running ``steps`` long steps, the slowest taking ``ms``."""
+    return world * atoms * steps / (ms * 1e-3)
+
+
 def run_gpu(args, rank, world, local):
     import torch
     from mdynamix_gb300.abi import MDX_FP64, MDX_MIXED
@@ -224,12 +241,8 @@ def run_gpu(args, rank, world, local):
             e1.record(stream)
             torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
+        ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
         launches = g.launches - l0
-        t = torch.tensor([ms], device="cuda")
-        if dist:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         # instrumented pass: per-group device time (CUDA events on the same stream)
         g.set_timers(True)
         g.timers()
@@ -695,8 +708,8 @@ def main():
         return
     n = r["n"]
     o64, o32 = r["out"]["fp64"], r["out"]["mixed"]
-    v64 = world * n * args.steps / (o64["ms"] * 1e-3)
-    v32 = world * n * args.steps / (o32["ms"] * 1e-3)
+    v64 = replica_rate(world, n, args.steps, o64["ms"])
+    v32 = replica_rate(world, n, args.steps, o32["ms"])
     nfreq = r["nfreq"]
     roof = roofline_of(o64["timers"], r["mbsh"], r["mbln"], nfreq, r["kset"], n,
                        r["peak64"], r["peak32"], "fp64", args.steps)
