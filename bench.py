@@ -272,7 +272,8 @@ def run_gpu(args, rank, world, local):
             e1.record(stream)
             torch.cuda.synchronize()
             _, th1 = g.get_state()
-            skin[prec] = dict(ms=e0.elapsed_time(e1), builds=th1.list_builds - th0.list_builds)
+            skin[prec] = dict(ms=max_over_ranks(e0.elapsed_time(e1), dist, "cuda"),
+                              builds=th1.list_builds - th0.list_builds)
             g.close()
     # list sizes and force error at the shared start state
     g64 = ForcePath(s, precision=MDX_FP64)
@@ -308,7 +309,7 @@ def run_gpu(args, rank, world, local):
     t0 = time.perf_counter()
     for k in range(ke):
         e2e_step(1 + k)
-    e2e_s = (time.perf_counter() - t0) / ke
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dist, "cuda")
     peak64 = probe_fma_peak(True)
     peak32 = probe_fma_peak(False)
     from mdynamix_gb300.abi import MdxStepRecord
@@ -745,8 +746,8 @@ def main():
     if r["skin"]:
         k64, k32 = r["skin"]["fp64"], r["skin"]["mixed"]
         skin = {"rskin_A": 1.5,
-                "fp64": world * n * args.steps / (k64["ms"] * 1e-3),
-                "mixed": world * n * args.steps / (k32["ms"] * 1e-3),
+                "fp64": replica_rate(world, n, args.steps, k64["ms"]),
+                "mixed": replica_rate(world, n, args.steps, k32["ms"]),
                 "list_builds": [k64["builds"], k32["builds"]]}
     line = {
         "metric": METRIC, "value": v64, "unit": UNIT, "n_gpus": world, "steps": args.steps,
