@@ -146,9 +146,9 @@ typedef struct {
 typedef struct {
   double boxl, boyl, bozl;   /* box lengths (Angstrom)                   */
   int32_t icell;             /* ICELL 0 rect, 1 truncated oct, 2 hex
-                                (FP64 path at constant volume; BOYL =
-                                BOXL cos30 for hex, BOYL = BOZL = BOXL for
-                                oct, as RECLEN leaves them)              */
+                                (FP64 path; BOYL = BOXL cos30 for hex,
+                                BOYL = BOZL = BOXL for oct, as RECLEN
+                                leaves them)                             */
   int32_t lmnbl;             /* reaction field instead of Ewald          */
   double coulf;              /* COULF                                    */
   double alphad;             /* ALPHAD Ewald alpha (1/Angstrom)          */

@@ -551,7 +551,7 @@ struct ScalScratch {
 };
 
 struct ScalConst {
-  int ntypes, lnvt, lnpt, lsep, lsctd, lp_xy, lshejk, lsclt;
+  int ntypes, lnvt, lnpt, lsep, lsctd, lp_xy, lshejk, lsclt, icell;
   double tstep, htstep, trtemp, tdelt, trpres, trpresx, trpresy, trpresz, dqt,
       dqp, rtp, fnst, fnop, unitp, vird, tridm_coef, tridee_coef, convet, chktf;
   double tfact[MDX_NT];
@@ -608,11 +608,23 @@ enum {
   ST_MSTEP1,       // SULTAN first step correction factor (mdstep.f:131-139)
 };
 
-__device__ void reclen_dev(mdx_thermo *th, double sx, double sy, double sz) {
+// RECLEN (service.f:572-605): the hexagonal cell keeps BOYL = BOXL cos30,
+// the truncated octahedron a cube of the mean factor and half its volume.
+__device__ void reclen_dev(mdx_thermo *th, double sx, double sy, double sz, int icell) {
   th->boxl = sx * th->boxl;
-  th->boyl = sy * th->boyl;
-  th->bozl = sz * th->bozl;
+  if (icell == 2) {
+    th->boyl = th->boxl * (double)0.8660254037844386f;
+    th->bozl = sz * th->bozl;
+  } else if (icell == 1) {
+    th->boxl = (sx + sy + sz) * th->boxl / (3. * sx);
+    th->boyl = th->boxl;
+    th->bozl = th->boxl;
+  } else {
+    th->boyl = sy * th->boyl;
+    th->bozl = sz * th->bozl;
+  }
   th->vol = th->boxl * th->boyl * th->bozl;
+  if (icell == 1) th->vol = 0.5 * th->vol;
 }
 
 __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_thermo *th,
@@ -715,7 +727,7 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
       break;
     }
     case ST_1RECLEN:
-      reclen_dev(th, ss->drcx, ss->drcy, ss->drcz);
+      reclen_dev(th, ss->drcx, ss->drcy, ss->drcz, c.icell);
       break;
     case ST_1NVT:
     case ST_2V:
@@ -818,7 +830,7 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
       break;
     }
     case ST_3B: {
-      reclen_dev(th, ss->drcx + 1., ss->drcy + 1., ss->drcz + 1.);
+      reclen_dev(th, ss->drcx + 1., ss->drcy + 1., ss->drcz + 1., c.icell);
       th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
       if (c.lsctd) {
         double SCA = 0.;
@@ -1376,7 +1388,7 @@ static ScalConst scal_const(mdx_ctx *ctx) {
   ScalConst c{};
   c.ntypes = ctx->d.ntypes;
   c.lnvt = p.lnvt; c.lnpt = p.lnpt; c.lsep = p.lsep; c.lsctd = p.lsctd;
-  c.lp_xy = p.lp_xy; c.lshejk = p.lshejk; c.lsclt = p.lsclt;
+  c.lp_xy = p.lp_xy; c.lshejk = p.lshejk; c.lsclt = p.lsclt; c.icell = p.icell;
   c.tstep = p.tstep; c.htstep = 0.5 * p.tstep; c.trtemp = p.trtemp; c.tdelt = p.tdelt;
   c.trpres = p.trpres; c.trpresx = p.trpresx; c.trpresy = p.trpresy; c.trpresz = p.trpresz;
   c.dqt = p.dqt; c.dqp = p.dqp; c.rtp = p.rtp; c.fnst = p.fnst; c.fnop = p.fnop;

@@ -423,3 +423,26 @@ def test_mixed_sweep_splits():
         h.close()
     assert np.array_equal(outs[0], outs[1])
     assert np.abs(outs[0] - outs[2]).max() < 1e-6
+
+
+@pytest.mark.parametrize("icell", [1, 2])
+def test_npt_cell_shapes_fp64(icell):
+    """NPT in the truncated octahedron and the hexagonal cell: RECLEN keeps
+    the cell's shape (service.f:576-585) and the octahedron's half-cube
+    volume; SULTAN + SHEJK and DOUBLE against the oracle."""
+    import dataclasses
+    spec = dataclasses.replace(systems.spce_ions(n=200, toler=1e-6), icell=icell,
+                               nvt=(300.0, 30.0), npt=(1.0, 500.0))
+    g, o = _npt_pair(spec)
+    rg, ro = g.sultan(5), o.sultan(5)
+    _check_npt(g, o, rg, ro)
+    if icell == 2:
+        assert abs(rg[-1].boyl - rg[-1].boxl * 0.8660254037844386) < 1e-6 * rg[-1].boxl
+    else:
+        assert rg[-1].boxl == rg[-1].boyl == rg[-1].bozl
+        assert abs(rg[-1].vol - 0.5 * rg[-1].boxl ** 3) < 1e-9 * rg[-1].vol
+    spec2 = dataclasses.replace(systems.spcfw(n=256, ions=2, rcut=8.0), icell=icell,
+                                npt=(1.0, 500.0))
+    g2, o2 = _npt_pair(spec2)
+    rg2, ro2 = g2.double(3), o2.double(3)
+    _check_npt(g2, o2, rg2, ro2)
