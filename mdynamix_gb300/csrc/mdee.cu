@@ -39,16 +39,19 @@ __global__ void k_ee_recip(int ncol, const KCol *__restrict__ cols,
                            const double *__restrict__ kconst, const double2 *__restrict__ sk,
                            int nee, const int *__restrict__ ee_atom,
                            const double *__restrict__ dq, const dbl4 *__restrict__ pos,
-                           double bx, double by, double bz, Dst6 dst) {
+                           double bx, double by, double bz, double hexk, Dst6 dst) {
+  // hexk: pi for the hexagonal cell's RYV = 2 pi IKY + pi IKX, else 0; the
+  // octahedral columns step nz by 2 (KCol.zstep)
   const double twopi = 2.0 * PI_REF;
   double acc[2] = {0.0, 0.0};  // EFN, EFO
   for (int c = blockIdx.x; c < ncol; c += gridDim.x) {
     const KCol col = cols[c];
-    const int len = col.nzhi - col.nzlo + 1;
-    const double RXV = (twopi * col.nx) / bx, RYV = (twopi * col.ny) / by;
+    const int len = (col.nzhi - col.nzlo) / col.zstep + 1;
+    const double ryv = hexk != 0.0 ? twopi * col.ny + hexk * col.nx : twopi * col.ny;
+    const double RXV = (twopi * col.nx) / bx, RYV = ryv / by;
     for (int t = threadIdx.x; t < len; t += blockDim.x) {
       const int k = col.koff + t;
-      const double RZV = (twopi * (col.nzlo + t)) / bz;
+      const double RZV = (twopi * (col.nzlo + col.zstep * t)) / bz;
       double dr = 0.0, di = 0.0;
       for (int e = 0; e < nee; ++e) {
         const dbl4 p = pos[ee_atom[e]];
@@ -81,7 +84,7 @@ __global__ void k_ee_intra(int nee, const int *__restrict__ ee_atom, const dbl4 
                            const int *__restrict__ mol_first, const int *__restrict__ mol_nat,
                            const int4 *__restrict__ ainfo, const double *__restrict__ qsite,
                            double coulf, double aleen2, double alphad, double bx, double by,
-                           double bz, Dst6 dst) {
+                           double bz, CellPbc cell, Dst6 dst) {
   double acc[2] = {0.0, 0.0};  // EFN, EFO
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nee; e += gridDim.x * blockDim.x) {
     const int i = ee_atom[e];
@@ -92,7 +95,8 @@ __global__ void k_ee_intra(int nee, const int *__restrict__ ee_atom, const dbl4 
       const double QIJO = coulf * pi.w * pj.w;
       const double QIJN = coulf * aleen2 * qsite[i] * qsite[j];
       double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
-      pbc_rect(DX, DY, DZ, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      if (cell.icell == 0) pbc_rect(DX, DY, DZ, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+      else pbc_cell(DX, DY, DZ, cell);  // mdee.f:351
       const double R2 = DX * DX + DY * DY + DZ * DZ;
       const double R2I = 1.0 / R2;
       const double R1 = sqrt(R2);
@@ -108,6 +112,7 @@ __global__ void k_ee_intra(int nee, const int *__restrict__ ee_atom, const dbl4 
 struct EEPair {
   double coulf, alphad, ealn1, rsho, rshn;
   int nnbt;
+  CellPbc cell;  // PBC of the pair (mdee.f:432, 502)
 };
 
 // DIFEN's pair term for one listed pair (mdee.f:404-455 / 466-519); adds to
@@ -135,7 +140,8 @@ __device__ __forceinline__ void ee_pair(int i, int j, const dbl4 *__restrict__ p
   const double A6N = ESCI * a6lj0[ix], B12N = ESCI * b12lj0[ix];
   const double QIJN = ESCL * qsite[i] * qsite[j] * c.coulf;
   double DX = pi.x - pj.x, DY = pi.y - pj.y, DZ = pi.z - pj.z;
-  pbc_rect(DX, DY, DZ, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  if (c.cell.icell == 0) pbc_rect(DX, DY, DZ, bx, by, bz, 0.5 * bx, 0.5 * by, 0.5 * bz);
+  else pbc_cell(DX, DY, DZ, c.cell);
   const double RR = DX * DX + DY * DY + DZ * DZ;
   const double R1 = sqrt(RR);
   const double R1OI = 1. / (R1 + c.rsho), R1NI = 1. / (R1 + c.rshn);
@@ -186,10 +192,6 @@ extern "C" int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double p
     ctx->err = "mdx_ee_delta: neighbour lists not built";
     return MDX_ERR_STATE;
   }
-  if (ctx->p.icell != 0) {
-    ctx->err = "mdx_ee_delta: rectangular cells only";
-    return MDX_ERR_UNSUPPORTED;
-  }
   if (ctx->p.lmnbl) {
     ctx->err = "mdx_ee_delta: reaction field not built";
     return MDX_ERR_UNSUPPORTED;
@@ -227,7 +229,9 @@ extern "C" int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double p
     if (!rc && !skip) {
       const int nb = std::min(d.ncol, 2 * ctx->nsm);
       k_ee_recip<<<nb, 64, 0, ctx->stream>>>(d.ncol, d.cols, d.kconst, d.sk, nee, dee, ddq,
-                                             d.pos, bx, by, bz, dst6(ctx, nb, 2, acc, acc + 1));
+                                             d.pos, bx, by, bz,
+                                             ctx->p.icell == 2 ? PI_REF : 0.0,
+                                             dst6(ctx, nb, 2, acc, acc + 1));
       ctx->launches++;
       if (cudaGetLastError() != cudaSuccess) rc = MDX_ERR_CUDA;
     }
@@ -236,7 +240,7 @@ extern "C" int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double p
       const int nb = (nee + 127) / 128;
       k_ee_intra<<<nb, 128, 0, ctx->stream>>>(nee, dee, d.pos, d.mol_first, d.mol_nat, d.ainfo,
                                               d.qsite, ctx->p.coulf, aleen * aleen,
-                                              ctx->p.alphad, bx, by, bz,
+                                              ctx->p.alphad, bx, by, bz, cell_pbc(ctx),
                                               dst6(ctx, nb, 2, acc, acc + 1));
       ctx->launches++;
       if (cudaGetLastError() != cudaSuccess) rc = MDX_ERR_CUDA;
@@ -245,7 +249,7 @@ extern "C" int mdx_ee_delta(mdx_ctx *ctx, double ec_old, double ec_new, double p
   // DIFEN over the long and the short rows
   if (!rc) {
     const EEPair c{ctx->p.coulf, ctx->p.alphad, aleen, bee * (1. - std::pow(ec_old, pw2)),
-                   bee * (1. - std::pow(ec_new, pw2)), ctx->d.nnbt};
+                   bee * (1. - std::pow(ec_new, pw2)), ctx->d.nnbt, cell_pbc(ctx)};
     const bool full = ctx->mixed();
     const int nown = full ? nee : d.n;
     if (nown > 0) {

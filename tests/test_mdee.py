@@ -125,3 +125,32 @@ def test_walk_jobs_same_alone_and_in_the_mix():
     assert len(a.states) == 7
     for x, y in zip(a.states[-1]["state"], b.states[-1]["state"]):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("icell", [1, 2])
+def test_ee_delta_cell_shapes(icell):
+    """DIFFUR / DIFEN in the truncated octahedron and the hexagonal cell:
+    the cell's k-set (octahedral columns of one nz parity, the hexagonal
+    RYV) and minimum image (mdee.f:351, 432, 502), FP64 against the
+    oracle."""
+    import dataclasses
+    from mdynamix_gb300.mdx import ForcePath
+    spec = dataclasses.replace(S.solvation_job("CH3OH", 300), icell=icell)
+    s = S.System(spec)
+    st = S.make_configuration(s, seed=4, jitter=0.05)
+    a, b = 0.75, 0.5
+    o = _oracle(s, st, a)
+    g = ForcePath(s, precision=MDX_FP64)
+    p = g.packed.params
+    p.lmdee = 1
+    g.set_params(p)
+    g.set_state(*st)
+    g.set_lambda(a, PW1, PW2, BEE)
+    g.chcnb()
+    g.allforce()
+    rg = g.ee_delta(a, b, PW1, PW2, BEE)
+    ro = o.ee_delta(a, b, PW1, PW2, BEE)
+    for x, y in zip(rg, ro):
+        assert abs(x - y) <= 1e-10 * abs(y), (rg, ro)
+    g.close()
