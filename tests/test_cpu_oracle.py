@@ -422,3 +422,30 @@ def test_cell_shapes_oracle_ewald_consistent(icell):
     assert abs(out[0][0] - out[1][0]) < 2e-3 * abs(out[0][1])
     f0, f1 = out[0][2], out[1][2]
     assert np.abs(f0 - f1).max() < 1e-4 * np.abs(f0).max()
+
+
+def test_autotune_table_from_timings():
+    """The tuning table's construction: size classes between the measured
+    systems, the fastest split of each class's largest measured system, and
+    the lookup that a context makes with its sizes."""
+    from mdynamix_gb300 import autotune
+    res = [
+        dict(n=768, row_short=52.0, row_long=254.0, short={2: 3.0, 4: 2.0, 8: 1.0},
+             long={8: 3.0, 16: 2.0, 32: 1.0}),
+        dict(n=24000, row_short=52.0, row_long=254.0, short={2: 3.0, 4: 1.0, 8: 2.0},
+             long={8: 2.0, 16: 1.0, 32: 3.0}),
+        dict(n=24000, row_short=52.0, row_long=673.0, short={2: 3.0, 4: 1.0, 8: 2.0},
+             long={8: 3.0, 16: 2.0, 32: 1.0}),
+    ]
+    sc = autotune.table(res, "row_short", "short")
+    lc = autotune.table(res, "row_long", "long")
+
+    def pick(cells, n, row):
+        for mx, mr, t in cells:
+            if n <= mx and row <= mr:
+                return t
+
+    assert pick(sc, 768, 52.0) == 8 and pick(sc, 24000, 52.0) == 4
+    assert pick(lc, 768, 254.0) == 32
+    assert pick(lc, 24000, 254.0) == 16 and pick(lc, 24000, 673.0) == 32
+    assert pick(lc, 10 ** 9, 1e9) is not None  # the last class is open
