@@ -344,7 +344,7 @@ typedef struct {
 int mdx_get_path_info(const mdx_ctx *ctx, mdx_path_info *out);
 
 /* Work split of the mixed pair sweeps: threads per owner atom of the short
- * rows (tpo_short: 2, 4 or 8) and of the long rows (tpo_long: 8, 16 or 32).
+ * rows (tpo_short: 2, 4 or 8) and of the long rows (tpo_long: 4, 8, 16 or 32).
  * No counterpart in the reference (a launch-shape choice of this library).
  * By default a context takes the choice of the tuning table built into the
  * library (written by mdynamix_gb300/autotune.py from timings of each split

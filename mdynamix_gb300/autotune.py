@@ -3,7 +3,7 @@
 For a set of water systems spanning the sizes this library serves (PIMD
 beads of 768 atoms, solvation jobs of 1-6 k atoms, the 98,304-atom box) and
 the cutoffs they use, each split of the short sweep (2, 4, 8 threads per
-owner) and of the long sweep (8, 16, 32) is timed on the GPU with the
+owner) and of the long sweep (4, 8, 16, 32) is timed on the GPU with the
 library's device timers over DOUBLE long steps, and the fastest is kept.
 The result is written as ``csrc/tune_table.cuh`` (compiled into the
 library, so a context's choice depends on its sizes alone and equal systems
@@ -27,7 +27,7 @@ from .abi import MDX_MIXED
 from .mdx import ForcePath
 
 SHORT_SPLITS = (2, 4, 8)
-LONG_SPLITS = (8, 16, 32)
+LONG_SPLITS = (4, 8, 16, 32)
 # (waters, cutoff A): beads and small jobs at 9 A, the named water box at 12 A
 SYSTEMS = ((256, 9.0), (700, 9.0), (2000, 9.0), (2000, 12.0), (8000, 9.0), (8000, 12.0),
            (32768, 12.0))
@@ -136,7 +136,7 @@ def write_record(path: str, results, short_cells, long_cells, device: str, cmd: 
              "short sweep (10 per long step) by threads per owner atom (long split 32), and of the",
              "long sweep by threads per owner (short split 4).  SPC-FW water at 1 g/cm3, Rshort 5 A.",
              "", f"Command: `{cmd}`", "",
-             "| atoms | Rcut | mean row short / long | short 2 / 4 / 8 | long 8 / 16 / 32 | chosen |",
+             "| atoms | Rcut | mean row short / long | short 2 / 4 / 8 | long 4 / 8 / 16 / 32 | chosen |",
              "|---|---|---|---|---|---|"]
     for r in results:
         sh = " / ".join(f"{r['short'][k]:.4f}" for k in SHORT_SPLITS)

@@ -1448,9 +1448,10 @@ int mdx_set_tuning(mdx_ctx *ctx, const mdx_tuning *t) {
   if (!ctx) return MDX_ERR_ARG;
   if (t) {
     const bool ok_s = t->tpo_short == 2 || t->tpo_short == 4 || t->tpo_short == 8;
-    const bool ok_l = t->tpo_long == 8 || t->tpo_long == 16 || t->tpo_long == 32;
+    const bool ok_l =
+        t->tpo_long == 4 || t->tpo_long == 8 || t->tpo_long == 16 || t->tpo_long == 32;
     if (!ok_s || !ok_l) {
-      ctx->err = "tuning: tpo_short must be 2, 4 or 8 and tpo_long 8, 16 or 32";
+      ctx->err = "tuning: tpo_short must be 2, 4 or 8 and tpo_long 4, 8, 16 or 32";
       return MDX_ERR_ARG;
     }
     ctx->tune = mdx_tuning{t->tpo_short, t->tpo_long, 2, 0};

@@ -260,6 +260,7 @@ __global__ void k_wir_fix(int n, const dbl4 *__restrict__ pos,
 
 // ---------------------------------------------------------------- mixed ---
 constexpr int PAIR32_BLOCKS = 6;  // resident blocks per SM the register cap aims at
+constexpr int PAIR32X2_BLOCKS = 4;  // resident blocks per SM of the paired sweeps (64 registers)
 
 __device__ __forceinline__ float idiff(int a, int b, float s) { return fixdiff(a, b, s); }
 
@@ -275,7 +276,8 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     FixScale fsc, unsigned long long *__restrict__ ffix,
     const double *__restrict__ X, const double *__restrict__ Y,
     const double *__restrict__ Z, double escale,
-    unsigned long long *__restrict__ slots, double *__restrict__ split) {
+    unsigned long long *__restrict__ slots, double *__restrict__ split,
+    const int *__restrict__ owner_of) {
   __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
   if (SPLIT) {
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
@@ -286,8 +288,13 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
   // take a few lanes, long rows (several hundred entries) up to a warp.  The
   // split is a tuning choice (tune_table.cuh); the forces' integer sums do
   // not depend on it, the FP32 lane partials before them do.
+  // owner_of (long rows, stored whole per atom): owners are taken in the
+  // cell order of the last build (slot -> atom), so that the owners of a
+  // block are neighbours in space and share their neighbours' records in
+  // L1; null (short rows, tiled by 32 atoms): atom order.
   const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / TPO;
+  const int sl = (blockIdx.x * blockDim.x + threadIdx.x) / TPO;
+  const int i = owner_of && sl < n ? owner_of[sl] : sl;
   const int k0 = lane % TPO, kstep = TPO;
   long long tot[P_NSLOT];
 #pragma unroll
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     // one 16-byte record per atom: fixed-point x, y, z and (molecule, site);
     // charges and types come from the per-site table (L1-resident)
     constexpr unsigned SITE_MASK = (1u << MDX_SITE_BITS) - 1u;
-    const int4 pi = posi[i];
+    const int4 pi = owner_of ? posn[sl] : posi[i];
     const float4 sti = __ldg(&stab[(unsigned)pi.w & SITE_MASK]);
     const unsigned mi = (unsigned)pi.w >> MDX_SITE_BITS;
     const int ti = __float_as_int(sti.w), ni = __float_as_int(sti.z);
@@ -479,6 +486,357 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
   }
 }
 
+// ------------------------------------------------------- mixed, paired ---
+// The common case of the mixed sweeps (Ewald, no energy split by type pair,
+// no MDEE shift): each lane evaluates two row entries per iteration with the
+// paired FP32 instructions of this GPU (__ffma2_rn / __fmul2_rn /
+// __fadd2_rn: two FP32 operations per issued instruction).  The sweeps are
+// issue-bound, and pairing halves their FP32 instructions.  Entries of the
+// owner's own molecule (intramolecular non-bonded and 1-4 pairs; water has
+// none) are evaluated one at a time by pair_same.
+
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
+
+// Per-thread asynchronous copies into shared memory (the thread reads back
+// only its own slots, so no barrier is involved).
+__device__ __forceinline__ void cpa4(int *smem, const int *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpa16(int4 *smem, const int4 *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Sums of one lane: element .x and .y of each are independent partials.
+struct Acc2 {
+  float2 fx, fy, fz;              // force on the owner
+  float2 ees, ee, esr, vir;       // PELS, unscreened Coulomb, PE, VIR (all pairs)
+  float2 vx, vy, vz;              // diagonal virial
+  float ee_same, esr_same;        // the owner's own molecule's share of ee, esr
+};
+
+// One entry of the owner's own molecule (forces.f:868-998 / 1071-1198 with
+// SAME set): scaled 1-4 or plain Coulomb for an ion-free site (IEE = 0), the
+// Ewald real-space term otherwise; LJ only where B12 is nonzero.
+template <bool SHORT, bool ENER>
+__device__ __forceinline__ void pair_same(float DX, float DY, float DZ, bool is14, float QIJ,
+                                          float A6, float B12, int eei, int lmovei,
+                                          float alphad, float rc2f, Acc2 &s) {
+  const float RR = DX * DX + DY * DY + DZ * DZ;
+  if (!(SHORT || RR <= rc2f)) return;
+  const float R1I = rsqrtf(RR);
+  const float R1 = RR * R1I;
+  float EE1, EES, FORCE;
+  if (is14 || eei == 0) {
+    EE1 = QIJ * R1I;
+    FORCE = lmovei ? EE1 * (R1I * R1I) : 0.f;
+    EES = EE1;
+  } else {
+    const float ALPHAR = alphad * R1;
+    const float TTT = __fdividef(1.f, 1.f + (float)MDX_B1 * ALPHAR);
+    const float EXP2A = __expf(-(ALPHAR * ALPHAR));
+    const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
+    EE1 = QIJ * R1I;
+    EES = EE1 * ERFCT;
+    FORCE = EE1 * ((float)MDX_TOTPI * alphad * EXP2A + ERFCT * R1I) * R1I;
+  }
+  if (ENER) {
+    s.ee.x += EE1;
+    s.ee_same += EE1;
+    s.ees.x += EES;
+  }
+  if (B12 != 0.f) {
+    const float R2I = R1I * R1I;
+    const float R6I = R2I * R2I * R2I;
+    float ESR = (A6 + B12 * R6I) * R6I;
+    const float FSR = (6.f * A6 + 12.f * B12 * R6I) * R6I * R1I;
+    FORCE = FORCE + FSR * R1I;
+    if (SHORT && !lmovei) {
+      ESR = 0.f;
+      FORCE = 0.f;
+    }
+    if (ENER) {
+      if (lmovei) s.vir.x += FSR * R1;
+      s.esr.x += ESR;
+      s.esr_same += ESR;
+    }
+  }
+  if (ENER && (SHORT || lmovei)) {
+    s.vx.x += FORCE * (DX * DX);
+    s.vy.x += FORCE * (DY * DY);
+    s.vz.x += FORCE * (DZ * DZ);
+  }
+  s.fx.x += FORCE * DX;
+  s.fy.x += FORCE * DY;
+  s.fz.x += FORCE * DZ;
+}
+
+// Block sum of a sweep's integer energy/virial slots: warp sums of the lane
+// partials, fixed point, one atomic per slot per block.
+__device__ __forceinline__ void slots_out(const float (&a)[P_NSLOT], float escalef,
+                                          unsigned long long *__restrict__ slots) {
+  const int lane = threadIdx.x & 31;
+  long long tot[P_WIR];
+#pragma unroll
+  for (int k = 0; k < P_WIR; ++k) {
+    const float t = warp_sumf(a[k]);
+    tot[k] = lane == 0 ? f2ll_rn(t * escalef) : 0;
+  }
+  __shared__ long long sh[8][P_WIR];
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < P_WIR; ++k) sh[wid][k] = tot[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < P_WIR) {
+    long long s = 0;
+    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+    if (s != 0) atomicAdd(&slots[threadIdx.x], (unsigned long long)s);
+  }
+}
+
+template <bool SHORT, bool ENER, int TPO>
+__global__ void __launch_bounds__(256, PAIR32X2_BLOCKS) k_pair32x2(
+    int n, const int4 *__restrict__ posi, const int4 *__restrict__ posn,
+    const float4 *__restrict__ stab, const int *__restrict__ cnt, const int *__restrict__ idx,
+    int cap, PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
+    FixScale fsc, unsigned long long *__restrict__ ffix,
+    unsigned long long *__restrict__ slots, const int *__restrict__ owner_of) {
+  // TPO adjacent lanes per owner atom; lane k0 of an owner takes entries
+  // k0 + 2 TPO m and k0 + TPO + 2 TPO m as one pair.  Owner order as in
+  // k_pair32.
+  const int lane = threadIdx.x & 31;
+  const int sl = (blockIdx.x * blockDim.x + threadIdx.x) / TPO;
+  const int i = owner_of && sl < n ? owner_of[sl] : sl;
+  const int k0 = lane % TPO;
+  Acc2 s;
+  s.fx = s.fy = s.fz = splat(0.f);
+  s.ees = s.ee = s.esr = s.vir = splat(0.f);
+  s.vx = s.vy = s.vz = splat(0.f);
+  s.ee_same = s.esr_same = 0.f;
+  long long qx = 0, qy = 0, qz = 0;
+  if (i < n) {
+    constexpr unsigned SITE_MASK = (1u << MDX_SITE_BITS) - 1u;
+    const int4 pi = owner_of ? posn[sl] : posi[i];
+    const float4 sti = __ldg(&stab[(unsigned)pi.w & SITE_MASK]);
+    const unsigned mi = (unsigned)pi.w >> MDX_SITE_BITS;
+    const int ti = __float_as_int(sti.w), ni = __float_as_int(sti.z);
+    const float coulf = (float)pc.coulf, alphad = (float)pc.alphad;
+    const int eei = tc.iee[ti], lmovei = tc.lmove[ti];
+    const float c14e = tc.c14elf[ti], c14l = tc.c14ljf[ti];
+    const float qsc = sti.y * coulf, qic = sti.x * coulf;
+    const float2 *abrow = tb.abf + ni * pc.nnbt;
+    const int c = cnt[i];
+    const int *row = idx + list_slot(i, 0, cap, SHORT);
+    const size_t rs = SHORT ? 32 : 1;
+    const float2 sx2 = splat(sx), sy2 = splat(sy), sz2 = splat(sz);
+    const float2 al2 = splat(alphad), qic2 = splat(qic);
+    const float2 tpa2 = splat((float)MDX_TOTPI * alphad);
+    // one iteration: row entries va, vb (vb a copy of va when hb is false)
+    // with their neighbour records pa, pb
+    auto pair2 = [&](const int va, const int vb, const int4 pa, const int4 pb, const bool hb) {
+      const float4 sa = __ldg(&stab[(unsigned)pa.w & SITE_MASK]);
+      const float4 sb = __ldg(&stab[(unsigned)pb.w & SITE_MASK]);
+      const bool same_a = ((unsigned)pa.w >> MDX_SITE_BITS) == mi;
+      const bool same_b = hb && ((unsigned)pb.w >> MDX_SITE_BITS) == mi;
+      const float dxa = fixdiff(pi.x, pa.x, sx), dya = fixdiff(pi.y, pa.y, sy),
+                  dza = fixdiff(pi.z, pa.z, sz);
+      const float dxb = fixdiff(pi.x, pb.x, sx), dyb = fixdiff(pi.y, pb.y, sy),
+                  dzb = fixdiff(pi.z, pb.z, sz);
+      if (same_a || same_b) {
+        // the owner's own molecule: one entry at a time, other entry too
+        const int nja = __float_as_int(sa.z), njb = __float_as_int(sb.z);
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          if (e == 1 && !hb) break;
+          const int v = e ? vb : va;
+          const bool same = e ? same_b : same_a;
+          const float4 st = e ? sb : sa;
+          const bool is14 = SHORT && v < 0;
+          const float2 ab = __ldg(&abrow[(same ? (is14 ? 2 : 1) : 0) * tb.nn + (e ? njb : nja)]);
+          const float QIJ = same ? (is14 ? qsc * st.y * c14e : qsc * st.y) : qic * st.x;
+          const float A6 = is14 ? ab.x * c14l : ab.x, B12 = is14 ? ab.y * c14l : ab.y;
+          const float DX = e ? dxb : dxa, DY = e ? dyb : dya, DZ = e ? dzb : dza;
+          if (same) {
+            pair_same<SHORT, ENER>(DX, DY, DZ, is14, QIJ, A6, B12, eei, lmovei, alphad,
+                                   pc.rc2f, s);
+          } else {
+            // an inter-molecular entry beside one of the own molecule: the
+            // paired arithmetic below with the other half empty
+            const float RR = DX * DX + DY * DY + DZ * DZ;
+            if (SHORT || RR <= pc.rc2f) {
+              const float R1I = rsqrtf(RR);
+              const float R1 = RR * R1I;
+              const float ALPHAR = alphad * R1;
+              const float TTT = __fdividef(1.f, 1.f + (float)MDX_B1 * ALPHAR);
+              const float EXP2A = __expf(-(ALPHAR * ALPHAR));
+              const float ERFCT = ewald_erfc_polyf(TTT, EXP2A);
+              const float EE1 = QIJ * R1I;
+              float FORCE = EE1 * ((float)MDX_TOTPI * alphad * EXP2A + ERFCT * R1I) * R1I;
+              const float R2I = R1I * R1I;
+              const float R6I = R2I * R2I * R2I;
+              const float ESR = (A6 + B12 * R6I) * R6I;
+              const float FSR = (6.f * A6 + 12.f * B12 * R6I) * R6I * R1I;
+              FORCE = FORCE + FSR * R1I;
+              if (ENER) {
+                s.ees.x += EE1 * ERFCT;
+                s.ee.x += EE1;
+                s.esr.x += ESR;
+                s.vir.x += FSR * R1;
+                s.vx.x += FORCE * (DX * DX);
+                s.vy.x += FORCE * (DY * DY);
+                s.vz.x += FORCE * (DZ * DZ);
+              }
+              s.fx.x += FORCE * DX;
+              s.fy.x += FORCE * DY;
+              s.fz.x += FORCE * DZ;
+            }
+          }
+        }
+        return;
+      }
+      // two inter-molecular entries (or one and an empty half)
+      const float2 aba = __ldg(&abrow[__float_as_int(sa.z)]);
+      const float2 abb = __ldg(&abrow[__float_as_int(sb.z)]);
+      const float2 DX = mul2(make_float2((float)(int)((unsigned)pi.x - (unsigned)pa.x),
+                                         (float)(int)((unsigned)pi.x - (unsigned)pb.x)), sx2);
+      const float2 DY = mul2(make_float2((float)(int)((unsigned)pi.y - (unsigned)pa.y),
+                                         (float)(int)((unsigned)pi.y - (unsigned)pb.y)), sy2);
+      const float2 DZ = mul2(make_float2((float)(int)((unsigned)pi.z - (unsigned)pa.z),
+                                         (float)(int)((unsigned)pi.z - (unsigned)pb.z)), sz2);
+      float2 RR = fma2(DZ, DZ, fma2(DY, DY, mul2(DX, DX)));
+      // an empty half or a pair beyond RCUT (skin mode) contributes nothing
+      const bool oka = SHORT || RR.x <= pc.rc2f;
+      const bool okb = hb && (SHORT || RR.y <= pc.rc2f);
+      float2 QIJ = mul2(make_float2(sa.x, sb.x), qic2);
+      float2 A6 = make_float2(aba.x, abb.x), B12 = make_float2(aba.y, abb.y);
+      if (!oka) { QIJ.x = 0.f; A6.x = 0.f; B12.x = 0.f; RR.x = 1.f; }
+      if (!okb) { QIJ.y = 0.f; A6.y = 0.f; B12.y = 0.f; RR.y = 1.f; }
+      const float2 R1I = make_float2(rsqrtf(RR.x), rsqrtf(RR.y));
+      const float2 R1 = mul2(RR, R1I);
+      const float2 ALPHAR = mul2(al2, R1);
+      const float2 den = fma2(splat((float)MDX_B1), ALPHAR, splat(1.f));
+      const float2 TTT = make_float2(__fdividef(1.f, den.x), __fdividef(1.f, den.y));
+      const float2 A2 = mul2(ALPHAR, ALPHAR);
+      const float2 EXP2A = make_float2(__expf(-A2.x), __expf(-A2.y));
+      float2 P = fma2(splat((float)MDX_A5), TTT, splat((float)MDX_A4));
+      P = fma2(P, TTT, splat((float)MDX_A3));
+      P = fma2(P, TTT, splat((float)MDX_A2));
+      P = fma2(P, TTT, splat((float)MDX_A1));
+      const float2 ERFCT = mul2(mul2(P, TTT), EXP2A);
+      const float2 EE1 = mul2(QIJ, R1I);
+      float2 FORCE = mul2(mul2(EE1, fma2(tpa2, EXP2A, mul2(ERFCT, R1I))), R1I);
+      // LJ (A6 is zero in the tables wherever B12 is, so no test is needed)
+      const float2 R2I = mul2(R1I, R1I);
+      const float2 R6I = mul2(mul2(R2I, R2I), R2I);
+      const float2 FSR = mul2(mul2(fma2(mul2(splat(12.f), B12), R6I, mul2(splat(6.f), A6)), R6I), R1I);
+      FORCE = fma2(FSR, R1I, FORCE);
+      if (ENER) {
+        const float2 ESR = mul2(fma2(B12, R6I, A6), R6I);
+        s.ees = fma2(EE1, ERFCT, s.ees);
+        s.ee = add2(s.ee, EE1);
+        s.esr = add2(s.esr, ESR);
+        s.vir = fma2(FSR, R1, s.vir);
+        s.vx = fma2(mul2(FORCE, DX), DX, s.vx);
+        s.vy = fma2(mul2(FORCE, DY), DY, s.vy);
+        s.vz = fma2(mul2(FORCE, DZ), DZ, s.vz);
+      }
+      s.fx = fma2(FORCE, DX, s.fx);
+      s.fy = fma2(FORCE, DY, s.fy);
+      s.fz = fma2(FORCE, DZ, s.fz);
+    };
+    if constexpr (SHORT) {
+      // short rows (a few dozen entries) are too short for a pipeline
+      for (int k = k0; k < c; k += 2 * TPO) {
+        const bool hb = k + TPO < c;
+        const int va = row[(size_t)k * rs];
+        const int vb = hb ? row[(size_t)(k + TPO) * rs] : va;
+        pair2(va, vb, posn[va & 0x7fffffff], posn[vb & 0x7fffffff], hb);
+      }
+    } else {
+      // Software pipeline through shared memory: the row entries of
+      // iteration m + 3 and the neighbour records of iteration m + 1 are in
+      // flight (cp.async groups, in commit order) while iteration m
+      // computes, so the index -> record load chain does not stall every
+      // iteration and holds no registers.  Each thread reads back only its
+      // own slots.  Entry slots: ring of 4 iterations; records: ring of 2.
+      __shared__ int s_v[4][2][256];
+      __shared__ int4 s_p[2][2][256];
+      const int t = threadIdx.x;
+      auto issue_idx = [&](int m) {
+        const int e = k0 + 2 * TPO * m;
+        if (e < c) cpa4(&s_v[m & 3][0][t], row + (size_t)e * rs);
+        if (e + TPO < c) cpa4(&s_v[m & 3][1][t], row + (size_t)(e + TPO) * rs);
+        cpa_commit();
+      };
+      auto issue_rec = [&](int m) {
+        const int e = k0 + 2 * TPO * m;
+        if (e < c) cpa16(&s_p[m & 1][0][t], posn + (s_v[m & 3][0][t] & 0x7fffffff));
+        if (e + TPO < c) cpa16(&s_p[m & 1][1][t], posn + (s_v[m & 3][1][t] & 0x7fffffff));
+        cpa_commit();
+      };
+      const int nit = c > k0 ? (c - k0 + 2 * TPO - 1) / (2 * TPO) : 0;
+      issue_idx(0);
+      issue_idx(1);
+      issue_idx(2);
+      cpa_wait<2>();  // entries of iteration 0
+      issue_rec(0);
+      cpa_wait<1>();  // entries of iterations 1 and 2
+      for (int m = 0; m < nit; ++m) {
+        const bool hb = k0 + 2 * TPO * m + TPO < c;
+        issue_rec(m + 1);
+        issue_idx(m + 3);
+        cpa_wait<2>();  // records of iteration m, entries of iteration m + 2
+        const int va = s_v[m & 3][0][t];
+        const int vb = hb ? s_v[m & 3][1][t] : va;
+        const int4 pa = s_p[m & 1][0][t];
+        const int4 pb = hb ? s_p[m & 1][1][t] : pa;
+        pair2(va, vb, pa, pb, hb);
+      }
+      cpa_wait<0>();  // nothing of this thread left in flight
+    }
+    qx = f2ll_rn((s.fx.x + s.fx.y) * fsc.scalef);
+    qy = f2ll_rn((s.fy.x + s.fy.y) * fsc.scalef);
+    qz = f2ll_rn((s.fz.x + s.fz.y) * fsc.scalef);
+  }
+#pragma unroll
+  for (int o = 1; o < TPO; o <<= 1) {
+    qx += __shfl_xor_sync(0xffffffffu, qx, o);
+    qy += __shfl_xor_sync(0xffffffffu, qy, o);
+    qz += __shfl_xor_sync(0xffffffffu, qz, o);
+  }
+  if (i < n && lane % TPO == 0) {
+    ffix[i] = (unsigned long long)qx;
+    ffix[n + i] = (unsigned long long)qy;
+    ffix[2 * n + i] = (unsigned long long)qz;
+  }
+  if (!ENER) return;
+  float a[P_NSLOT];
+  const float ee = s.ee.x + s.ee.y, esr = s.esr.x + s.esr.y;
+  a[P_EES] = s.ees.x + s.ees.y;
+  a[P_ESR] = esr;
+  a[P_VIR] = s.vir.x + s.vir.y;
+  a[P_VX] = s.vx.x + s.vx.y;
+  a[P_VY] = s.vy.x + s.vy.y;
+  a[P_VZ] = s.vz.x + s.vz.y;
+  a[P_EE_SAME] = s.ee_same;
+  a[P_EE_DIFF] = ee - s.ee_same;
+  a[P_ESR_SAME] = s.esr_same;
+  a[P_ESR_DIFF] = esr - s.esr_same;
+  a[P_WIR] = 0.f;
+  slots_out(a, fsc.escalef, slots);
+}
+
 // Fold the integer slots of a mixed sweep into mdx_scalars (full rows count
 // each pair twice, hence the 1/2 on pair sums).
 __global__ void k_fold_slots(unsigned long long *__restrict__ slots, double einv,
@@ -539,9 +897,12 @@ __global__ void k_pack_lj(int nn, const float *__restrict__ f, float2 *__restric
   // f: a6f, b12f, a60f, b120f, a614f, b1214f back to back (nn each)
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nn) return;
-  abf[k] = make_float2(f[k], f[nn + k]);
-  abf[nn + k] = make_float2(f[2 * nn + k], f[3 * nn + k]);
-  abf[2 * nn + k] = make_float2(f[4 * nn + k], f[5 * nn + k]);
+  // A6 is kept only where B12 is nonzero: the sweeps add the LJ term only
+  // for B12 != 0 (forces.f:955, 1166), and the paired sweeps then need no test
+  auto ab = [](float a6, float b12) { return make_float2(b12 != 0.f ? a6 : 0.f, b12); };
+  abf[k] = ab(f[k], f[nn + k]);
+  abf[nn + k] = ab(f[2 * nn + k], f[3 * nn + k]);
+  abf[2 * nn + k] = ab(f[4 * nn + k], f[5 * nn + k]);
 }
 
 // ener = false: forces only (an intermediate short step of DOUBLE, whose fast
@@ -590,11 +951,20 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   k_pair32<S, P, E, K><<<grid32, T, 0, ctx->stream>>>(                            \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
-      d.Y, d.Z, escale, slots, split_buf)
-#define LP32E(S, K)                      \
-  do {                                   \
-    if (ener) LP32(S, false, true, K);   \
-    else LP32(S, false, false, K);       \
+      d.Y, d.Z, escale, slots, split_buf, S ? nullptr : d.cell_list)
+#define LP32X2(S, E, K)                                                           \
+  k_pair32x2<S, E, K><<<grid32, T, 0, ctx->stream>>>(                             \
+      d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d), ctx->tc, ctx->pc, \
+      (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, slots, S ? nullptr : d.cell_list)
+    // the paired sweeps cover Ewald without MDEE's shifted Coulomb
+    const bool paired = !ctx->pc.lmnbl && !ctx->pc.lmdee;
+#define LP32E(S, K)                            \
+  do {                                         \
+    if (paired) {                              \
+      if (ener) LP32X2(S, true, K);            \
+      else LP32X2(S, false, K);                \
+    } else if (ener) LP32(S, false, true, K);  \
+    else LP32(S, false, false, K);             \
   } while (0)
     if (split) {
       if (shrt) {
@@ -609,11 +979,13 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
       else if (tpo == 8) LP32E(true, 8);
       else LP32E(true, 4);
     } else {
-      if (tpo == 8) LP32E(false, 8);
+      if (tpo == 4) LP32E(false, 4);
+      else if (tpo == 8) LP32E(false, 8);
       else if (tpo == 16) LP32E(false, 16);
       else LP32E(false, 32);
     }
 #undef LP32E
+#undef LP32X2
 #undef LP32
     MDX_LAUNCHED(ctx);
     if (ener) {

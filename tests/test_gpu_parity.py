@@ -396,7 +396,7 @@ def test_mixed_sweep_splits():
     g.getcom()
     g.allforce()
     t0 = g.tuning()
-    assert t0["source"] == 1 and t0["tpo_short"] in (2, 4, 8) and t0["tpo_long"] in (8, 16, 32)
+    assert t0["source"] == 1 and t0["tpo_short"] in (2, 4, 8) and t0["tpo_long"] in (4, 8, 16, 32)
     f0 = g.forces(3)
     for ts, tl in ((2, 8), (8, 16), (4, 32), (8, 32)):
         g.set_tuning(ts, tl)
