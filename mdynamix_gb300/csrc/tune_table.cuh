@@ -10,5 +10,5 @@ struct TuneCell {
   int tpo;
 };
 
-constexpr TuneCell TUNE_SHORT[] = {{1269, 1e30, 8}, {3549, 1e30, 8}, {12000, 1e30, 8}, {48572, 1e30, 8}, {2147483647, 1e30, 4}};
-constexpr TuneCell TUNE_LONG[] = {{1269, 1e30, 32}, {3549, 1e30, 32}, {12000, 413.4, 32}, {12000, 1e30, 32}, {48572, 413.4, 16}, {48572, 1e30, 32}, {2147483647, 1e30, 16}};
+constexpr TuneCell TUNE_SHORT[] = {{1269, 1e30, 8}, {3549, 1e30, 8}, {12000, 1e30, 8}, {48572, 1e30, 4}, {2147483647, 1e30, 4}};
+constexpr TuneCell TUNE_LONG[] = {{1269, 1e30, 32}, {3549, 1e30, 32}, {12000, 413.4, 16}, {12000, 1e30, 32}, {48572, 413.4, 8}, {48572, 1e30, 16}, {2147483647, 1e30, 8}};
