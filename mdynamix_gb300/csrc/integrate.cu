@@ -550,10 +550,17 @@ struct ScalScratch {
   int iskk;
 };
 
+// The stages run on one thread, and an FP64 division there is a long
+// dependent sequence on this GPU's FP64 pipe: the quotients of constants are
+// formed on the host (rtrtemp = 1 / TRTEMP, tlow = TRTEMP / CHKTF, dqt_f =
+// c.dqt_f, c3_fnst = 3 / FNST, c3_fnop = 3 / FNOP) and the pressure stage
+// takes one reciprocal of VOL; the values equal the reference's divisions to
+// rounding.
 struct ScalConst {
   int ntypes, lnvt, lnpt, lsep, lsctd, lp_xy, lshejk, lsclt, icell;
   double tstep, htstep, trtemp, tdelt, trpres, trpresx, trpresy, trpresz, dqt,
       dqp, rtp, fnst, fnop, unitp, vird, tridm_coef, tridee_coef, convet, chktf;
+  double rtrtemp, tlow, dqt_f, c3_fnst, c3_fnop, rfnst;
   double tfact[MDX_NT];
   int lmove[MDX_NT];
 };
@@ -577,7 +584,7 @@ __device__ void getemp_fold(const ScalConst &c, ScalScratch *ss, mdx_thermo *th,
   for (int t = 0; t < nt; ++t) th->tempr[t] = th->ekin[t] * c.tfact[t];
   th->temp = th->tke * c.convet;
   for (int k = 0; k < MDX_NT + 4; ++k) ss->ekacc[k] = 0.0;
-  if (c.chktf > 0.0 && (th->temp > c.chktf * c.trtemp || th->temp <= c.trtemp / c.chktf))
+  if (c.chktf > 0.0 && (th->temp > c.chktf * c.trtemp || th->temp <= c.tlow))
     atomicOr(err, DERR_TEMP);
   if (!(th->temp == th->temp)) atomicOr(err, DERR_NAN);
 }
@@ -641,19 +648,21 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
                             c.vird + th->vira[0] + th->vira[1] + th->vira[2];
       const double WIRSUM =
           s->vir1 + s->vir2 + s->pels1 + s->pels2 + s->spe + c.vird + s->wirs + s->wirss;
-      const double TRIDEE = c.tridee_coef / VOL;
-      const double TRID = 2. * th->tke * c.unitp / (3. * VOL) - TRIDEE;
-      const double TRIDM = c.tridm_coef * th->temp / VOL - TRIDEE;
-      const double TRIDX = th->virkx * c.unitp / VOL - TRIDEE / 3.;
-      const double TRIDY = th->virky * c.unitp / VOL - TRIDEE / 3.;
-      const double TRIDZ = th->virkz * c.unitp / VOL - TRIDEE / 3.;
-      th->tryck = VIRSUM * c.unitp / (3. * VOL) + TRID;
-      th->tryckm = WIRSUM * c.unitp / (3. * VOL) + TRIDM;
-      th->tryckx = (s->virx + s->virfx + c.vird / 3. + th->vira[0]) * c.unitp / VOL + TRIDX;
-      th->trycky = (s->viry + s->virfy + c.vird / 3. + th->vira[1]) * c.unitp / VOL + TRIDY;
-      th->tryckz = (s->virz + s->virfz + c.vird / 3. + th->vira[2]) * c.unitp / VOL + TRIDZ;
-      ss->dke = th->temp / c.trtemp - 1.0;
-      for (int t = 0; t < c.ntypes; ++t) ss->dte[t] = th->tempr[t] / c.trtemp - 1.0;
+      const double RV = 1.0 / VOL, UPV = c.unitp * RV, UPV3 = UPV * (1.0 / 3.0);
+      const double TRIDEE = c.tridee_coef * RV;
+      const double TRIDEE3 = TRIDEE * (1.0 / 3.0), VIRD3 = c.vird * (1.0 / 3.0);
+      const double TRID = 2. * th->tke * UPV3 - TRIDEE;
+      const double TRIDM = c.tridm_coef * th->temp * RV - TRIDEE;
+      const double TRIDX = th->virkx * UPV - TRIDEE3;
+      const double TRIDY = th->virky * UPV - TRIDEE3;
+      const double TRIDZ = th->virkz * UPV - TRIDEE3;
+      th->tryck = VIRSUM * UPV3 + TRID;
+      th->tryckm = WIRSUM * UPV3 + TRIDM;
+      th->tryckx = (s->virx + s->virfx + VIRD3 + th->vira[0]) * UPV + TRIDX;
+      th->trycky = (s->viry + s->virfy + VIRD3 + th->vira[1]) * UPV + TRIDY;
+      th->tryckz = (s->virz + s->virfz + VIRD3 + th->vira[2]) * UPV + TRIDZ;
+      ss->dke = th->temp * c.rtrtemp - 1.0;
+      for (int t = 0; t < c.ntypes; ++t) ss->dte[t] = th->tempr[t] * c.rtrtemp - 1.0;
       if (s->lscfl) {
         for (int k = 1; k <= 4; ++k) ss->dpe[k] = 0.;
       } else {
@@ -683,39 +692,39 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
         if (c.lsctd) {
           double SCA = 0.;
           for (int t = 0; t < c.ntypes; ++t) {
-            th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+            th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - c.dqt_f) * HTSTEP;
             SCA = SCA + th->scm[t] * th->ekin[t];
           }
           th->sc = SCA / th->tke;
         } else {
-          th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+          th->sc = th->sc + (th->scl * th->scl * RTP - c.dqt_f) * HTSTEP;
         }
         const double *DPE = ss->dpe;
         if (c.lsep) {
-          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
-          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke * c.rfnst - th->sclx * th->sc) * HTSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke * c.rfnst - th->scly * th->sc) * HTSTEP;
           if (c.lp_xy) {
             th->sclx = 0.5 * (th->sclx + th->scly);
             th->scly = th->sclx;
           }
-          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke * c.rfnst - th->sclz * th->sc) * HTSTEP;
           th->scl = th->sclx + th->scly + th->sclz;
         } else {
-          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke * c.rfnst - th->scl * th->sc) * HTSTEP;
           th->sclx = th->scl;
           th->scly = th->scl;
           th->sclz = th->scl;
           npt_guard(ss, th, th->scl * HTSTEP, err);
         }
-        double SCVX = 1. - ((1. - 3. / FNST) * th->sclx + th->sc) * HTSTEP;
-        double SCVY = 1. - ((1. - 3. / FNST) * th->scly + th->sc) * HTSTEP;
-        double SCVZ = 1. - ((1. - 3. / FNST) * th->sclz + th->sc) * HTSTEP;
+        double SCVX = 1. - ((1. - c.c3_fnst) * th->sclx + th->sc) * HTSTEP;
+        double SCVY = 1. - ((1. - c.c3_fnst) * th->scly + th->sc) * HTSTEP;
+        double SCVZ = 1. - ((1. - c.c3_fnst) * th->sclz + th->sc) * HTSTEP;
         if (c.lp_xy) {
           SCVX = 0.5 * (SCVX + SCVY);
           SCVY = SCVX;
         }
         double DRCX = TSTEP * th->sclx, DRCY = TSTEP * th->scly, DRCZ = TSTEP * th->sclz;
-        const double DRC = (DRCX + DRCY + DRCZ) / 3.;
+        const double DRC = (DRCX + DRCY + DRCZ) * (1.0 / 3.0);
         ss->drcv = DRC * HTSTEP;
         ss->drcx = 1. + DRCX + 0.5 * (DRCX * DRCX);
         ss->drcy = 1. + DRCY + 0.5 * (DRCY * DRCY);
@@ -739,12 +748,12 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
         ss->vscale[t] = c.lsctd ? 1. - th->scm[t] * TSTEP : 1. - th->sc * TSTEP;
       break;
     case ST_EABS:
-      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - c.c3_fnst)) * th->tke * TSTEP;
       break;
     case ST_2NPTV: {
-      double SCVX = 1. - (1. - 3. / c.fnop) * th->sclx * HTSTEP;
-      double SCVY = 1. - (1. - 3. / c.fnop) * th->scly * HTSTEP;
-      double SCVZ = 1. - (1. - 3. / c.fnop) * th->sclz * HTSTEP;
+      double SCVX = 1. - (1. - c.c3_fnop) * th->sclx * HTSTEP;
+      double SCVY = 1. - (1. - c.c3_fnop) * th->scly * HTSTEP;
+      double SCVZ = 1. - (1. - c.c3_fnop) * th->sclz * HTSTEP;
       if (c.lp_xy) {
         SCVX = 0.5 * (SCVX + SCVY);
         SCVY = SCVX;
@@ -757,41 +766,41 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
     case ST_2SCL: {
       const double *DPE = ss->dpe;
       if (c.lsep) {
-        th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * HTSTEP;
-        th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * HTSTEP;
+        th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke * c.rfnst - th->sclx * th->sc) * HTSTEP;
+        th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke * c.rfnst - th->scly * th->sc) * HTSTEP;
         if (c.lp_xy) {
           th->sclx = 0.5 * (th->sclx + th->scly);
           th->scly = th->sclx;
         }
-        th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * HTSTEP;
+        th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke * c.rfnst - th->sclz * th->sc) * HTSTEP;
         th->scl = th->sclx + th->scly + th->sclz;
       } else {
-        th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * HTSTEP;
+        th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke * c.rfnst - th->scl * th->sc) * HTSTEP;
         th->sclx = th->scl;
         th->scly = th->scl;
         th->sclz = th->scl;
         npt_guard(ss, th, th->scl * HTSTEP, err);
       }
-      th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+      th->sc = th->sc + (th->scl * th->scl * RTP - c.dqt_f) * HTSTEP;
       if (c.lsctd)
         for (int t = 0; t < c.ntypes; ++t)
-          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * HTSTEP;
+          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - c.dqt_f) * HTSTEP;
       break;
     }
     case ST_2SC: {
       if (c.lsctd) {
         double SCA = 0.;
         for (int t = 0; t < c.ntypes; ++t) {
-          const double DTE = th->tempr[t] / c.trtemp - 1.0;
+          const double DTE = th->tempr[t] * c.rtrtemp - 1.0;
           th->scm[t] = th->scm[t] + DTE * DQT * HTSTEP;
           SCA = SCA + th->scm[t] * th->ekin[t];
         }
         th->sc = SCA / th->tke;
       } else {
-        const double DKE = th->temp / c.trtemp - 1.0;
+        const double DKE = th->temp * c.rtrtemp - 1.0;
         th->sc = th->sc + DKE * DQT * HTSTEP;
       }
-      th->eabs = th->eabs - (th->sc + th->scl * (1. - 3. / FNST)) * th->tke * TSTEP;
+      th->eabs = th->eabs - (th->sc + th->scl * (1. - c.c3_fnst)) * th->tke * TSTEP;
       break;
     }
     case ST_3A: {
@@ -807,22 +816,22 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
       if (c.lnpt) {
         const double *DPE = ss->dpe;
         if (c.lsep) {
-          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke / FNST - th->sclx * th->sc) * TSTEP;
-          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke / FNST - th->scly * th->sc) * TSTEP;
+          th->sclx = th->sclx + DQP * (VOL * DPE[2] + 2. * th->tke * c.rfnst - th->sclx * th->sc) * TSTEP;
+          th->scly = th->scly + DQP * (VOL * DPE[3] + 2. * th->tke * c.rfnst - th->scly * th->sc) * TSTEP;
           if (c.lp_xy) {
             th->sclx = 0.5 * (th->sclx + th->scly);
             th->scly = th->sclx;
           }
-          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke / FNST - th->sclz * th->sc) * TSTEP;
+          th->sclz = th->sclz + DQP * (VOL * DPE[4] + 2. * th->tke * c.rfnst - th->sclz * th->sc) * TSTEP;
           th->scl = th->sclx + th->scly + th->sclz;
         } else {
-          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke / FNST - th->scl * th->sc) * TSTEP;
+          th->scl = th->scl + DQP * (3. * VOL * DPE[1] + 6. * th->tke * c.rfnst - th->scl * th->sc) * TSTEP;
           th->sclx = th->scl;
           th->scly = th->scl;
           th->sclz = th->scl;
           npt_guard(ss, th, th->scl * TSTEP, err);
         }
-        ss->dxc = ((1. - 3. / FNST) * th->scl) * TSTEP;  // SCV of 3.6.2.2
+        ss->dxc = ((1. - c.c3_fnst) * th->scl) * TSTEP;  // SCV of 3.6.2.2
         ss->drcx = TSTEP * th->sclx;
         ss->drcy = TSTEP * th->scly;
         ss->drcz = TSTEP * th->sclz;
@@ -831,11 +840,11 @@ __device__ void scal_stage(int stage, const ScalConst &c, ScalScratch *ss, mdx_t
     }
     case ST_3B: {
       reclen_dev(th, ss->drcx + 1., ss->drcy + 1., ss->drcz + 1., c.icell);
-      th->sc = th->sc + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+      th->sc = th->sc + (th->scl * th->scl * RTP - c.dqt_f) * TSTEP;
       if (c.lsctd) {
         double SCA = 0.;
         for (int t = 0; t < c.ntypes; ++t) {
-          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - DQT / FNST) * TSTEP;
+          th->scm[t] = th->scm[t] + (th->scl * th->scl * RTP - c.dqt_f) * TSTEP;
           SCA = SCA + th->scm[t] * th->ekin[t];
         }
         th->sc = SCA / th->tke;
@@ -1394,6 +1403,12 @@ static ScalConst scal_const(mdx_ctx *ctx) {
   c.dqt = p.dqt; c.dqp = p.dqp; c.rtp = p.rtp; c.fnst = p.fnst; c.fnop = p.fnop;
   c.unitp = p.unitp; c.vird = p.vird; c.tridm_coef = p.tridm_coef;
   c.tridee_coef = p.tridee_coef; c.convet = p.convet; c.chktf = p.chktf;
+  c.rtrtemp = 1.0 / p.trtemp;
+  c.tlow = p.chktf > 0.0 ? p.trtemp / p.chktf : 0.0;
+  c.dqt_f = p.dqt / p.fnst;
+  c.c3_fnst = 3. / p.fnst;
+  c.c3_fnop = 3. / p.fnop;
+  c.rfnst = 1.0 / p.fnst;
   for (int t = 0; t < MDX_NT; ++t) {
     c.tfact[t] = p.tfact[t];
     c.lmove[t] = ctx->tc.lmove[t];
