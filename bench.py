@@ -61,13 +61,13 @@ OPS_EW_FROZEN_KATOM = 21
 # group's kernels in one long step, MB).
 # fp64 ewald: k_tables 43.4 + k_sfac 126.0 + k_sfac_sum 51.3 + k_kterms 1.0
 #             + k_wpairs 0.6 + k_rforce64 102.9
-# mixed ewald: k_tables 4.7 + k_zimages 18.1 + k_sfac32 53.4 + k_sfac_sum 32.4
+# mixed ewald: k_tables 4.7 + k_zimages 18.0 + k_sfac32 53.7 + k_sfac_sum 32.4
 #              + k_kterms 1.0 + k_wtiles 0.6 + k_rforce_tc 75.4
 # fp64 pair: 9 x 30.7 (short, forces) + 30.7 (short, energies) + 153.1 (long)
-# mixed pair: 9 x 25.9 + 25.9 + 280.4
+# mixed pair: 9 x 25.9 (short, forces) + 25.9 (short, energies) + 283.2 (long)
 TRAFFIC_MB = {
-    ("fp64", "ewald"): 325.2, ("mixed", "ewald"): 185.5,
-    ("fp64", "pair"): 459.9, ("mixed", "pair"): 539.4,
+    ("fp64", "ewald"): 325.2, ("mixed", "ewald"): 185.8,
+    ("fp64", "pair"): 459.9, ("mixed", "pair"): 542.1,
 }
 
 
