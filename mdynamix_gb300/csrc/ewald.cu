@@ -263,11 +263,16 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
     }
     zo = kx + ky + si.t0;
   }
-  float A[KGRP][SCH][4];
+  // the four sums of (column c, p) as two pairs, P = (A1, A3) and
+  // Q = (A4, A2) of the paired-record scheme, each advanced by one paired
+  // FP32 FMA (FFMA2) per atom: P += (tr, tr) (Z.re, Z.im), Q += (ti, ti)
+  // (Z.re, Z.im).  Each half is the same rounded FMA in the same order as a
+  // scalar fmaf, so the sums are those of four scalar accumulators.
+  float2 P[KGRP][SCH], Q[KGRP][SCH];
 #pragma unroll
   for (int c = 0; c < KGRP; ++c)
 #pragma unroll
-    for (int s = 0; s < SCH; ++s) A[c][s][0] = A[c][s][1] = A[c][s][2] = A[c][s][3] = 0.f;
+    for (int s = 0; s < SCH; ++s) P[c][s] = Q[c][s] = make_float2(0.f, 0.f);
   const int bufsz = TILE * rowlen;
   for (int k = threadIdx.x; k < 2 * TILE * SCH; k += blockDim.x)
     srow[(k / SCH) * rowlen + zpad + k % SCH] = make_float2(0.f, 0.f);
@@ -308,10 +313,8 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
           const float2 Z = zr[s];
 #pragma unroll
           for (int c = 0; c < KGRP; ++c) {
-            A[c][s][0] = fmaf(tr[c], Z.x, A[c][s][0]);
-            A[c][s][1] = fmaf(ti[c], Z.y, A[c][s][1]);
-            A[c][s][2] = fmaf(tr[c], Z.y, A[c][s][2]);
-            A[c][s][3] = fmaf(ti[c], Z.x, A[c][s][3]);
+            P[c][s] = __ffma2_rn(make_float2(tr[c], tr[c]), Z, P[c][s]);
+            Q[c][s] = __ffma2_rn(make_float2(ti[c], ti[c]), Z, Q[c][s]);
           }
         }
       }
@@ -331,8 +334,8 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
 #pragma unroll
     for (int s = 0; s < SCH; ++s)
       if (si.t0 + s <= G.m)
-        sfac_out(col, si.t0 + s, (double)A[c][s][0], (double)A[c][s][1], (double)A[c][s][2],
-                 (double)A[c][s][3], pp, sk);
+        sfac_out(col, si.t0 + s, (double)P[c][s].x, (double)Q[c][s].y, (double)P[c][s].y,
+                 (double)Q[c][s].x, pp, sk);
   }
 }
 
