@@ -247,11 +247,14 @@ __global__ void __launch_bounds__(BLK) k_build(
   const int ox0 = g.nx >= W ? -R : 0, ox1 = g.nx >= W ? R : g.nx - 1;
   const int oy0 = g.ny >= W ? -R : 0, oy1 = g.ny >= W ? R : g.ny - 1;
   const int oz0 = g.nz >= W ? -R : 0, oz1 = g.nz >= W ? R : g.nz - 1;
-  auto wrapx = [&](int ox) { return g.nx >= W ? (cx0 + ox + g.nx) % g.nx : ox; };
+  // offsets stay within one period (|o| <= R < W <= n): a conditional wrap,
+  // no integer division
+  auto wrap = [](int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); };
+  auto wrapx = [&](int ox) { return g.nx >= W ? wrap(cx0 + ox, g.nx) : ox; };
   for (int oz = oz0; oz <= oz1; ++oz)
     for (int oy = oy0; oy <= oy1; ++oy) {
-      const int cy = g.ny >= W ? (cy0 + oy + g.ny) % g.ny : oy;
-      const int cz = g.nz >= W ? (cz0 + oz + g.nz) % g.nz : oz;
+      const int cy = g.ny >= W ? wrap(cy0 + oy, g.ny) : oy;
+      const int cz = g.nz >= W ? wrap(cz0 + oz, g.nz) : oz;
       const int crow = (cz * g.ny + cy) * g.nx;
       // the row's stencil cells in stencil order, consecutive cells merged
       // into one run of the cell-sorted arrays (the order of candidates is
