@@ -656,7 +656,7 @@ int launch_bonded(mdx_ctx *ctx, int laver, bool ener) {
   // length errors into large force errors) for 0.06 ms a long step
   BondOut o{d.hx, d.hy, d.hz, mx ? d.hfix : nullptr, d.n, ctx->fix.scale, ctx->fix.scalef,
             nullptr, (float)(ctx->boxl / 4294967296.0),
-            (float)(ctx->boyl / 4294967296.0), (float)(ctx->bozl / 4294967296.0),
+            (float)(fix_period_y(ctx) / 4294967296.0), (float)(ctx->bozl / 4294967296.0),
             (float)(0.495 * ctx->boxl), (float)(0.495 * ctx->boyl), (float)(0.495 * ctx->bozl),
             cell_pbc(ctx)};
   const int T = 128;

@@ -97,8 +97,14 @@ __global__ void k_tables(int n, int ldn, const dbl4 *__restrict__ pos, double ib
     // turn in units of 2^-31.  Its top 24 bits are exact in FP32 and go to
     // sincospif; the low 8 bits (under 3.7e-7 rad) rotate the result to
     // first order.  No recurrence, no FP64 work.
+    // hexagonal cell (hexy != 0): the y word is y / (2 BOYL), and the X
+    // table's phase is x / BOXL + y / (2 BOYL) (RYV = 2 pi IKY + pi IKX,
+    // forces.f:1402): the sum of the words; the Y table's, twice the y word
     const int4 pq = posi[i];
-    const unsigned u = (unsigned)(a == 0 ? pq.x : a == 1 ? pq.y : pq.z);
+    const bool hex = hexy != 0.0;
+    const unsigned u = a == 0   ? (hex ? (unsigned)pq.x + (unsigned)pq.y : (unsigned)pq.x)
+                       : a == 1 ? (hex ? 2u * (unsigned)pq.y : (unsigned)pq.y)
+                                : (unsigned)pq.z;
     const float qf = a == 0 ? (float)pos[i].w : 1.0f;
     const int len = a == 0 ? kx : a == 1 ? ky : kz;
     float2 *dst = (a == 0 ? txf : a == 1 ? tyf : tzf) + i;
@@ -854,8 +860,8 @@ cudaError_t raise_smem_limit_fn(const void *kernel, size_t bytes) {
 // and the self-energy SPEEI/SPEI (forces.f:1426-1447).
 int host_inifur(mdx_ctx *ctx) {
   const int icell = ctx->p.icell;
-  if (icell != 0 && ctx->mixed()) {
-    ctx->err = "non-rectangular cells run on the FP64 path only";
+  if (icell == 1 && ctx->mixed()) {
+    ctx->err = "the truncated octahedron runs on the FP64 path only";
     return MDX_ERR_UNSUPPORTED;
   }
   DevData &d = ctx->dv;

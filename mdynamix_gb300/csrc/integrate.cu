@@ -125,7 +125,9 @@ __global__ void k_getcom(int nop, const int *__restrict__ mol_first,
   Y[m] = yw;
   Z[m] = zw;
   // the reference rebuilds every coordinate as (S - X) + Xw (service.f:549-552)
-  const double two32 = 4294967296.0, ibx = 1.0 / bx, iby = 1.0 / by, ibz = 1.0 / bz;
+  // the fixed-point y word has period 2 BOYL in the hexagonal cell
+  const double two32 = 4294967296.0, ibx = 1.0 / bx, ibz = 1.0 / bz;
+  const double iby = mc.cell.icell == 2 ? 0.5 / by : 1.0 / by;
   for (int k = 0; k < na; ++k) {
     dbl4 p = pos[f + k];
     p.x = (p.x - x) + xw;
@@ -1808,7 +1810,7 @@ int launch_kick_drift_com(mdx_ctx *ctx, double htsteb, double tsteb, int prev, b
       htsteb, tsteb, prev, d.hx, d.hy, d.hz, from_fix ? d.hfix : nullptr, d.n, ctx->fix.inv,
       d.massdi, d.amass, d.vx, d.vy, d.vz, d.pos, d.X, d.Y, d.Z, ctx->boxl, ctx->boyl,
       ctx->bozl,
-      make_double3(4294967296.0 * (1.0 / ctx->boxl), 4294967296.0 * (1.0 / ctx->boyl),
+      make_double3(4294967296.0 * (1.0 / ctx->boxl), 4294967296.0 * (1.0 / fix_period_y(ctx)),
                    4294967296.0 * (1.0 / ctx->bozl)),
       ctx->mixed() ? d.posi : nullptr, d.pinfo,
       ctx->mixed() && ctx->have_lists ? d.cell_pos : nullptr, d.slot_of);
@@ -1905,7 +1907,7 @@ int launch_kick_drift_com_beads(mdx_ctx *c0, int P, const void *table, cudaStrea
   k_kick_drift_com_beads<<<grid, 128, 0, st>>>(
       d.nop, d.mol_first, d.mol_nat, d.mol_type, d.ainfo, move_const(c0), mol_const(c0), htsteb,
       tsteb, d.n, d.massdi, d.amass, c0->boxl, c0->boyl, c0->bozl,
-      make_double3(4294967296.0 * (1.0 / c0->boxl), 4294967296.0 * (1.0 / c0->boyl),
+      make_double3(4294967296.0 * (1.0 / c0->boxl), 4294967296.0 * (1.0 / fix_period_y(c0)),
                    4294967296.0 * (1.0 / c0->bozl)),
       d.pinfo, static_cast<const BeadMove *>(table));
   MDX_LAUNCHED(c0);

@@ -362,6 +362,15 @@ struct mdx_ctx {
   }
 };
 
+// Period of the mixed path's fixed-point y coordinate (y / period * 2^32,
+// kept modulo 2^32): BOYL, or 2 BOYL in the hexagonal cell, whose lattice
+// holds (BOXL / 2, BOYL) and (0, 2 BOYL) but not (0, BOYL), so that the
+// integer difference of two positions is always a lattice image of their
+// separation.
+inline double fix_period_y(const mdx_ctx *ctx) {
+  return ctx->p.icell == 2 ? 2.0 * ctx->boyl : ctx->boyl;
+}
+
 // Reduction destinations for a launch of nblocks blocks reducing nv values:
 // deterministic (partials + ordered sum) whenever the partials buffer is
 // large enough.
@@ -495,6 +504,37 @@ __device__ __forceinline__ void pbc_rectf(float &dx, float &dy, float &dz,
   if (fabsf(dx) > hbx) dx = dx - fsignf(bx, dx);
   if (fabsf(dz) > hbz) dz = dz - fsignf(bz, dz);
   if (fabsf(dy) > hby) dy = dy - fsignf(by, dy);
+}
+
+// The hexagonal cell's fold of PBC (service.f:956-979) in FP32, for the
+// mixed path's pair vectors: x already within +-BOXL/2 and y within +-BOYL
+// (the fixed-point differences), the four tests of the reference in its
+// order.  on = 0: rectangular cell, nothing to do.
+struct HexF {
+  int on;
+  float hbx, by, boxy3, boxyc;
+};
+__device__ __forceinline__ void pbc_hexf(float &xx, float &yy, const HexF &h) {
+  float xy = h.boxyc * xx;
+  if (yy > h.boxy3 - xy && (xx > 0.f || yy > 2.f * h.boxy3 - xy)) {
+    yy = yy - h.by;
+    xx = xx - h.hbx;
+    xy = h.boxyc * xx;
+  }
+  if (yy < -h.boxy3 - xy && (xx < 0.f || yy < -2.f * h.boxy3 - xy)) {
+    yy = yy + h.by;
+    xx = xx + h.hbx;
+    xy = h.boxyc * xx;
+  }
+  if (yy > h.boxy3 + xy) {
+    yy = yy - h.by;
+    xx = xx + h.hbx;
+    xy = h.boxyc * xx;
+  }
+  if (yy < -h.boxy3 + xy) {
+    yy = yy + h.by;
+    xx = xx - h.hbx;
+  }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

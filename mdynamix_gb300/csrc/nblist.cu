@@ -419,7 +419,7 @@ int launch_mirror_f32(mdx_ctx *ctx) {
   DevData &d = ctx->dv;
   k_mirror<<<(d.n + 255) / 256, 256, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
-      1.0 / ctx->boyl, 1.0 / ctx->bozl);
+      1.0 / fix_period_y(ctx), 1.0 / ctx->bozl);
   MDX_LAUNCHED(ctx);
   return launch_cell_refresh(ctx);
 }
@@ -503,7 +503,7 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
   MDX_LAUNCHED(ctx);
   k_mirror<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(
       d.n, d.pos, d.posf, ctx->mixed() ? d.posi : nullptr, d.pinfo, 1.0 / ctx->boxl,
-      1.0 / ctx->boyl, 1.0 / ctx->bozl, gate);
+      1.0 / fix_period_y(ctx), 1.0 / ctx->bozl, gate);
   MDX_LAUNCHED(ctx);
   k_cell_count<<<(d.n + T - 1) / T, T, 0, ctx->stream>>>(d.n, d.pos, b, g,
                                                           d.cell_cnt,
@@ -532,7 +532,7 @@ static int build_lists(mdx_ctx *ctx, const int *gate) {
       d.cell_start, d.cell_list, d.cell_pos, ctx->p.rshort * ctx->p.rshort, rl * rl,       \
       d.cap_s, d.cap_l, d.ns_cnt, d.nl_cnt, d.ns_idx, d.nl_idx, d.err, need,               \
       ctx->mixed() ? 1 : 0, ctx->mixed() ? d.posi : nullptr,                               \
-      (float)(ctx->boxl / 4294967296.0), (float)(ctx->boyl / 4294967296.0),               \
+      (float)(ctx->boxl / 4294967296.0), (float)(fix_period_y(ctx) / 4294967296.0),               \
       (float)(ctx->bozl / 4294967296.0), pos_ref, gate, mol_cut(ctx))
   if (ctx->p.lmnbl) KB(true);
   else KB(false);

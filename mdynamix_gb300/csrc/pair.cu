@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     const double *__restrict__ X, const double *__restrict__ Y,
     const double *__restrict__ Z, double escale,
     unsigned long long *__restrict__ slots, double *__restrict__ split,
-    const int *__restrict__ owner_of) {
+    const int *__restrict__ owner_of, HexF hex) {
   __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
   if (SPLIT) {
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
@@ -360,9 +360,10 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
         B12 = ab.y;
         if (pc.lmdee) RAE = (eei * tc.iee[tj] == 0) ? raex : 0.f;
       }
-      const float DX = idiff(pi.x, pj.x, sx);
-      const float DY = idiff(pi.y, pj.y, sy);
+      float DX = idiff(pi.x, pj.x, sx);
+      float DY = idiff(pi.y, pj.y, sy);
       const float DZ = idiff(pi.z, pj.z, sz);
+      if (hex.on) pbc_hexf(DX, DY, hex);
       const float RR = DX * DX + DY * DY + DZ * DZ;
       if (SHORT || RR <= pc.rc2f) {  // skin mode: long-row pairs beyond RCUT skipped
         const float R1I = rsqrtf(RR);
@@ -618,7 +619,7 @@ k_pair32x2(
     const float4 *__restrict__ stab, const int *__restrict__ cnt, const int *__restrict__ idx,
     int cap, PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
     FixScale fsc, unsigned long long *__restrict__ ffix,
-    unsigned long long *__restrict__ slots, const int *__restrict__ owner_of) {
+    unsigned long long *__restrict__ slots, const int *__restrict__ owner_of, HexF hex) {
   // TPO adjacent lanes per owner atom; lane k0 of an owner takes entries
   // k0 + 2 TPO m and k0 + TPO + 2 TPO m as one pair.  Owner order as in
   // k_pair32.
@@ -656,11 +657,15 @@ k_pair32x2(
       const float4 sb = __ldg(&stab[(unsigned)pb.w & SITE_MASK]);
       const bool same_a = ((unsigned)pa.w >> MDX_SITE_BITS) == mi;
       const bool same_b = hb && ((unsigned)pb.w >> MDX_SITE_BITS) == mi;
-      const float dxa = fixdiff(pi.x, pa.x, sx), dya = fixdiff(pi.y, pa.y, sy),
-                  dza = fixdiff(pi.z, pa.z, sz);
-      const float dxb = fixdiff(pi.x, pb.x, sx), dyb = fixdiff(pi.y, pb.y, sy),
-                  dzb = fixdiff(pi.z, pb.z, sz);
       if (same_a || same_b) {
+        float dxa = fixdiff(pi.x, pa.x, sx), dya = fixdiff(pi.y, pa.y, sy);
+        const float dza = fixdiff(pi.z, pa.z, sz);
+        float dxb = fixdiff(pi.x, pb.x, sx), dyb = fixdiff(pi.y, pb.y, sy);
+        const float dzb = fixdiff(pi.z, pb.z, sz);
+        if (hex.on) {
+          pbc_hexf(dxa, dya, hex);
+          pbc_hexf(dxb, dyb, hex);
+        }
         // the owner's own molecule: one entry at a time, other entry too
         const int nja = __float_as_int(sa.z), njb = __float_as_int(sb.z);
 #pragma unroll
@@ -715,12 +720,16 @@ k_pair32x2(
       // two inter-molecular entries (or one and an empty half)
       const float2 aba = __ldg(&abrow[__float_as_int(sa.z)]);
       const float2 abb = __ldg(&abrow[__float_as_int(sb.z)]);
-      const float2 DX = mul2(make_float2((float)(int)((unsigned)pi.x - (unsigned)pa.x),
-                                         (float)(int)((unsigned)pi.x - (unsigned)pb.x)), sx2);
-      const float2 DY = mul2(make_float2((float)(int)((unsigned)pi.y - (unsigned)pa.y),
-                                         (float)(int)((unsigned)pi.y - (unsigned)pb.y)), sy2);
+      float2 DX = mul2(make_float2((float)(int)((unsigned)pi.x - (unsigned)pa.x),
+                                   (float)(int)((unsigned)pi.x - (unsigned)pb.x)), sx2);
+      float2 DY = mul2(make_float2((float)(int)((unsigned)pi.y - (unsigned)pa.y),
+                                   (float)(int)((unsigned)pi.y - (unsigned)pb.y)), sy2);
       const float2 DZ = mul2(make_float2((float)(int)((unsigned)pi.z - (unsigned)pa.z),
                                          (float)(int)((unsigned)pi.z - (unsigned)pb.z)), sz2);
+      if (hex.on) {
+        pbc_hexf(DX.x, DY.x, hex);
+        pbc_hexf(DX.y, DY.y, hex);
+      }
       float2 RR = fma2(DZ, DZ, fma2(DY, DY, mul2(DX, DX)));
       // an empty half or a pair beyond RCUT (skin mode) contributes nothing
       const bool oka = SHORT || RR.x <= pc.rc2f;
@@ -946,9 +955,17 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   } else {
     unsigned long long *ffix = shrt ? d.hfix : d.gfix;
     unsigned long long *slots = reinterpret_cast<unsigned long long *>(d.red);
-    const double sxs = ctx->boxl / 4294967296.0, sys = ctx->boyl / 4294967296.0,
+    const double sxs = ctx->boxl / 4294967296.0, sys = fix_period_y(ctx) / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
+    // the hexagonal cell's fold after the fixed-point differences (its y
+    // period is 2 BOYL there); BOXY3 and 0.5 / cos30 as cell_pbc forms them
+    HexF hex{};
+    if (ctx->p.icell == 2) {
+      const CellPbc c = cell_pbc(ctx);
+      hex = HexF{1, (float)c.hbx, (float)c.by, (float)c.boxy3,
+                 (float)(0.5 / (double)0.8660254037844386f)};
+    }
     // threads per owner atom: the context's tuning (the energy-split sweeps
     // of RECINT keep the defaults)
     const int tpo = split ? (shrt ? TPO_SHORT_DEFAULT : TPO_LONG_DEFAULT)
@@ -958,11 +975,11 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   k_pair32<S, P, E, K><<<grid32, T, 0, ctx->stream>>>(                            \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
-      d.Y, d.Z, escale, slots, split_buf, S ? nullptr : d.cell_list)
+      d.Y, d.Z, escale, slots, split_buf, S ? nullptr : d.cell_list, hex)
 #define LP32X2(S, E, K)                                                           \
   k_pair32x2<S, E, K><<<grid32, T, 0, ctx->stream>>>(                             \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d), ctx->tc, ctx->pc, \
-      (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, slots, S ? nullptr : d.cell_list)
+      (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, slots, S ? nullptr : d.cell_list, hex)
     // the paired sweeps cover Ewald without MDEE's shifted Coulomb
     const bool paired = !ctx->pc.lmnbl && !ctx->pc.lmdee;
 #define LP32E(S, K)                            \

@@ -341,8 +341,46 @@ def test_cell_shapes_sultan_shake(icell):
     assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
 
 
+def test_cell_hexagonal_mixed():
+    """The mixed path in the hexagonal cell: fixed-point y words of period
+    2 BOYL, the cell's fold in FP32 after the integer differences, the X
+    phase of the Ewald tables as the sum of the x and y words.  Against the
+    FP64 path: force RMS error under 1e-5 in SLFORCES / FFORCES / ALLFORCE,
+    energies and virials to 1e-4, eleven DOUBLE steps tracking it to 1e-5 A."""
+    from mdynamix_gb300.mdx import ForcePath
+    s, st = cell_system(2)
+    g64 = ForcePath(s, precision=MDX_FP64)
+    g32 = ForcePath(s, precision=MDX_MIXED)
+    for g in (g64, g32):
+        g.set_state(*st)
+        assert g.inifur() == s.kvector_count()
+        g.chcnb()
+        g.getcom()
+    for routine in ("slforces", "fforces", "allforce"):
+        a, b = getattr(g64, routine)(), getattr(g32, routine)()
+        which = {"slforces": 2, "fforces": 1, "allforce": 3}[routine]
+        f64, f32 = g64.forces(which), g32.forces(which)
+        rms = np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum())
+        assert rms < 1e-5, (routine, rms)
+        for n in ("pe1", "pels1", "pe2", "pels2", "vir1", "vir2"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * max(abs(getattr(a, n)), 1e-9), \
+                (routine, n)
+    h64 = ForcePath(s, precision=MDX_FP64)
+    h32 = ForcePath(s, precision=MDX_MIXED)
+    for h in (h64, h32):
+        h.set_state(*st)
+    r64, r32 = h64.double(11), h32.double(11)
+    (ax, ay, az, *_), _ = h64.get_state()
+    (bx, by, bz, *_), _ = h32.get_state()
+    dpos = max(np.abs(ax - bx).max(), np.abs(ay - by).max(), np.abs(az - bz).max())
+    assert dpos < 1e-5, dpos
+    for a, b in zip(r64, r32):
+        for n in ("pe1", "pels1", "temp"):
+            assert abs(getattr(a, n) - getattr(b, n)) <= 1e-4 * max(abs(getattr(a, n)), 1e-9), n
+
+
 def test_cell_shapes_refused_where_not_built():
-    """The mixed path refuses non-rectangular cells (FP64 only)."""
+    """The mixed path refuses the truncated octahedron (FP64 only)."""
     from mdynamix_gb300.mdx import ForcePath, MdxError
     s, st = cell_system(1)
     with pytest.raises(MdxError):
