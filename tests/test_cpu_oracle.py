@@ -449,3 +449,69 @@ def test_autotune_table_from_timings():
     assert pick(lc, 768, 254.0) == 32
     assert pick(lc, 24000, 254.0) == 16 and pick(lc, 24000, 673.0) == 32
     assert pick(lc, 10 ** 9, 1e9) is not None  # the last class is open
+
+
+def _pbc_hex64(x, y, boxl, boyl):
+    """The reference's PBC for the hexagonal cell (service.f:953-990, LHEX),
+    elementwise in FP64: x folded to +-BOXL/2, then its four tests."""
+    cos30 = float(np.float32(0.8660254037844386))
+    boxyc = float(np.float32(0.5) / np.float32(cos30))  # REAL parameter (common_inc.f:33)
+    boxy3 = 0.66666666666666666667 * boyl               # RECLEN (service.f:579)
+    hbx = 0.5 * boxl
+    x = np.where(np.abs(x) > hbx, x - np.copysign(boxl, x), x)
+    xy = boxyc * x
+    m = (y > boxy3 - xy) & ((x > 0) | (y > 2 * boxy3 - xy))
+    y = np.where(m, y - boyl, y); x = np.where(m, x - hbx, x); xy = boxyc * x
+    m = (y < -boxy3 - xy) & ((x < 0) | (y < -2 * boxy3 - xy))
+    y = np.where(m, y + boyl, y); x = np.where(m, x + hbx, x); xy = boxyc * x
+    m = y > boxy3 + xy
+    y = np.where(m, y - boyl, y); x = np.where(m, x + hbx, x); xy = boxyc * x
+    m = y < -boxy3 + xy
+    y = np.where(m, y + boyl, y); x = np.where(m, x - hbx, x)
+    return x, y
+
+
+def test_hexagonal_fixed_point_images():
+    """The mixed path's hexagonal cell, restated in numpy: 32-bit words
+    x / BOXL and y / (2 BOYL) (2 BOYL is a lattice period, BOYL alone is
+    not), their wrapped integer differences in FP32 folded by the same four
+    tests in FP32 (pbc_hexf) give the FP64 minimum image of every pair
+    within 0.4 BOXL to FP32 rounding; the sum of the two words is the Ewald
+    X phase x / BOXL + y / (2 BOYL) (forces.f:1402) modulo one turn."""
+    rng = np.random.default_rng(7)
+    boxl = 41.3
+    boyl = boxl * float(np.float32(0.8660254037844386))
+    # positions inside the cell: raw points folded by the cell's PBC
+    x, y = _pbc_hex64(rng.uniform(-boxl, boxl, 3000), rng.uniform(-boyl, boyl, 3000), boxl, boyl)
+    two32 = 4294967296.0
+    xw = (np.rint(x / boxl * two32).astype(np.int64) & 0xffffffff).astype(np.uint32)
+    yw = (np.rint(y / (2 * boyl) * two32).astype(np.int64) & 0xffffffff).astype(np.uint32)
+    i, j = rng.integers(0, len(x), (2, 20000))
+    mx, my = _pbc_hex64(x[i] - x[j], y[i] - y[j], boxl, boyl)
+    near = np.hypot(mx, my) < 0.4 * boxl
+    dxw = (xw[i] - xw[j]).view(np.int32).astype(np.float32) * np.float32(boxl / two32)
+    dyw = (yw[i] - yw[j]).view(np.int32).astype(np.float32) * np.float32(2 * boyl / two32)
+    f32 = np.float32
+    hbx, by = f32(0.5 * boxl), f32(boyl)
+    boxy3 = f32(0.66666666666666666667 * boyl)
+    boxyc = f32(0.5) / f32(0.8660254037844386)
+    X, Y = dxw.copy(), dyw.copy()
+    for k in range(len(X)):  # the FP32 fold, one vector at a time as the kernel does
+        xx, yy = X[k], Y[k]
+        xy = boxyc * xx
+        if yy > boxy3 - xy and (xx > 0 or yy > f32(2) * boxy3 - xy):
+            yy = yy - by; xx = xx - hbx; xy = boxyc * xx
+        if yy < -boxy3 - xy and (xx < 0 or yy < -f32(2) * boxy3 - xy):
+            yy = yy + by; xx = xx + hbx; xy = boxyc * xx
+        if yy > boxy3 + xy:
+            yy = yy - by; xx = xx + hbx; xy = boxyc * xx
+        if yy < -boxy3 + xy:
+            yy = yy + by; xx = xx - hbx
+        X[k], Y[k] = xx, yy
+    assert near.sum() > 1000
+    assert np.abs(X[near] - mx[near]).max() < 1e-5 and np.abs(Y[near] - my[near]).max() < 1e-5
+    # X phase: the sum of the words against the FP64 fraction
+    ph = ((xw.astype(np.uint64) + yw) & 0xffffffff).astype(np.float64) / two32
+    ref = np.mod(x / boxl + y / (2 * boyl), 1.0)
+    d = np.abs(ph - ref)
+    assert np.minimum(d, 1.0 - d).max() < 2.0 ** -30
