@@ -145,11 +145,10 @@ typedef struct {
 /* Run parameters (/SIZES/, /ENERGY/, /NVTNPT/, main.f:380-450, 729-812). */
 typedef struct {
   double boxl, boyl, bozl;   /* box lengths (Angstrom)                   */
-  int32_t icell;             /* ICELL 0 rect, 1 truncated oct (FP64
-                                path), 2 hex (both paths); BOYL = BOXL
-                                cos30 for hex, BOYL = BOZL = BOXL for
-                                oct, as RECLEN leaves them; not with a
-                                Verlet skin                              */
+  int32_t icell;             /* ICELL 0 rect, 1 truncated oct, 2 hex
+                                (both paths); BOYL = BOXL cos30 for hex,
+                                BOYL = BOZL = BOXL for oct, as RECLEN
+                                leaves them; not with a Verlet skin      */
   int32_t lmnbl;             /* reaction field instead of Ewald          */
   double coulf;              /* COULF                                    */
   double alphad;             /* ALPHAD Ewald alpha (1/Angstrom)          */

@@ -242,14 +242,20 @@ struct SItem {
 };
 
 // 4 blocks a SM (128 registers, a few spilled): measured 4 % faster than 3
+template <int ZS>
 __global__ void __launch_bounds__(128, 4) k_sfac32(
     int n, int nitem, const SItem *__restrict__ items, const KGroup *__restrict__ groups,
     const KCol *__restrict__ cols, const float2 *__restrict__ tab, int ldn, int kx, int ky,
     int kz, int slice, double2 *__restrict__ sk, double2 *__restrict__ part, int nkv) {
-  // tab: the X, Y and Z tables back to back, row r at tab + r * ldn
-  extern __shared__ float2 srow[];  // [2][TILE][kx + ky + kz + SCH], double buffer
+  // tab: the X, Y and Z tables back to back, row r at tab + r * ldn;
+  // ZS: the z step of the records, 2 for the octahedron's k-set (a window
+  // reads every other z); a template parameter, so that the rectangular
+  // and hexagonal windows keep constant offsets
+  constexpr int zstep = ZS;
+  extern __shared__ float2 srow[];  // [2][TILE][kx + ky + kz + SCH zstep], double buffer
   const int zpad = kx + ky + kz;    // first zero entry of a row
-  const int rowlen = zpad + SCH;
+  const int nzp = SCH * zstep;      // zeros after the z rows
+  const int rowlen = zpad + nzp;
   const int it = blockIdx.x * blockDim.x + threadIdx.x;
   const int a0 = blockIdx.y * slice, a1 = min(n, a0 + slice);
   const bool active = it < nitem;
@@ -267,7 +273,7 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
       yo[c] = kx + (col.ny < 0 ? -col.ny : col.ny);
       ysg[c] = col.ny < 0 ? 0x80000000u : 0u;
     }
-    zo = kx + ky + si.t0;
+    zo = kx + ky + G.zoff + zstep * si.t0;
   }
   // the four sums of (column c, p) as two pairs, P = (A1, A3) and
   // Q = (A4, A2) of the paired-record scheme, each advanced by one paired
@@ -280,8 +286,8 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
 #pragma unroll
     for (int s = 0; s < SCH; ++s) P[c][s] = Q[c][s] = make_float2(0.f, 0.f);
   const int bufsz = TILE * rowlen;
-  for (int k = threadIdx.x; k < 2 * TILE * SCH; k += blockDim.x)
-    srow[(k / SCH) * rowlen + zpad + k % SCH] = make_float2(0.f, 0.f);
+  for (int k = threadIdx.x; k < 2 * TILE * nzp; k += blockDim.x)
+    srow[(k / nzp) * rowlen + zpad + k % nzp] = make_float2(0.f, 0.f);
   // stage a tile of atoms asynchronously (cp.async, one group per tile)
   auto stage = [&](int buf, int base) {
     const int m = min(TILE, a1 - base);
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(128, 4) k_sfac32(
         const float2 *zr = row + zo;
 #pragma unroll
         for (int s = 0; s < SCH; ++s) {
-          const float2 Z = zr[s];
+          const float2 Z = zr[zstep * s];
 #pragma unroll
           for (int c = 0; c < KGRP; ++c) {
             P[c][s] = __ffma2_rn(make_float2(tr[c], tr[c]), Z, P[c][s]);
@@ -577,12 +583,14 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
+template <int ZS>
 __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
     int n, const int *__restrict__ parts, const KGroup *__restrict__ groups,
     const KCol *__restrict__ cols,
     const float4 *__restrict__ wg, const float2 *__restrict__ tab, int ldn, int kx, int ky,
     int kz, const float2 *__restrict__ colrv, FixScale fsc,
     unsigned long long *__restrict__ gfix) {
+  constexpr int zstep = ZS;  // z step of the records (2: truncated octahedron)
   // tab: the X, Y and Z tables back to back, row r at tab + r * ldn
   extern __shared__ float2 srf[];  // [kz][RF_BATOMS]
   __shared__ long long red[3][RF_PARTS][RF_BATOMS];
@@ -640,7 +648,7 @@ __global__ void __launch_bounds__(32 * RF_PARTS, 6) k_rforce32(
         const float4 *w = wr + (((qb / RF_WB) & 1) * RF_WB + qb % RF_WB) * RF_REC;
         float2 zz[RF_APT];
 #pragma unroll
-        for (int q = 0; q < RF_APT; ++q) zz[q] = Z[p * RF_BATOMS + 32 * q];
+        for (int q = 0; q < RF_APT; ++q) zz[q] = Z[(G.zoff + zstep * p) * RF_BATOMS + 32 * q];
 #pragma unroll
         for (int c = 0; c < KGRP; ++c) {
           const float4 pu = w[2 * c], pv = w[2 * c + 1];  // {P.re, P.im, M.re, M.im}
@@ -860,10 +868,6 @@ cudaError_t raise_smem_limit_fn(const void *kernel, size_t bytes) {
 // and the self-energy SPEEI/SPEI (forces.f:1426-1447).
 int host_inifur(mdx_ctx *ctx) {
   const int icell = ctx->p.icell;
-  if (icell == 1 && ctx->mixed()) {
-    ctx->err = "the truncated octahedron runs on the FP64 path only";
-    return MDX_ERR_UNSUPPORTED;
-  }
   DevData &d = ctx->dv;
   ctx->drop_graphs();  // k-set buffers are reallocated below
   const double alphad = ctx->p.alphad;
@@ -934,18 +938,23 @@ int host_inifur(mdx_ctx *ctx) {
   // longest chunks first (stable): the lanes of a warp share a length
   std::stable_sort(chunks.begin(), chunks.end(),
                    [](const Chunk &a, const Chunk &b) { return a.len > b.len; });
-  // column groups of the mixed passes: columns sorted by m (then by column
-  // index), four at a time, the last group of an m padded
+  // column groups of the mixed passes: columns sorted by m and z offset
+  // (then by column index), four at a time, the last group of an (m, zoff)
+  // padded; a group's columns share their z records (the octahedron's
+  // columns hold the nz of one parity: zoff 0 or 1, zstep 2)
   std::vector<int> order(cols.size());
   for (size_t c = 0; c < cols.size(); ++c) order[c] = (int)c;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return cols[a].m < cols[b].m; });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return cols[a].m != cols[b].m ? cols[a].m < cols[b].m : cols[a].zoff < cols[b].zoff;
+  });
   std::vector<KGroup> groups;
   int woff = 0;
   for (size_t p = 0; p < order.size();) {
-    const int m = cols[order[p]].m;
-    KGroup g{m, m + 1, woff, 0, {-1, -1, -1, -1}};
-    for (int s = 0; s < KGRP && p < order.size() && cols[order[p]].m == m; ++s, ++p) {
+    const int m = cols[order[p]].m, zo = cols[order[p]].zoff;
+    KGroup g{m, m + 1, woff, zo, {-1, -1, -1, -1}};
+    for (int s = 0; s < KGRP && p < order.size() && cols[order[p]].m == m &&
+                    cols[order[p]].zoff == zo;
+         ++s, ++p) {
       g.col[s] = order[p];
       cols[order[p]].wpos = RF_REC * woff + 2 * s;
     }
@@ -964,6 +973,7 @@ int host_inifur(mdx_ctx *ctx) {
   d.kx = kx;
   d.ky = ky;
   d.kz = kz;
+  d.zstep = zstep;
   d.nkv = nkv;
   d.ncol = (int)cols.size();
   ctx->nkv = nkv;
@@ -990,7 +1000,7 @@ int host_inifur(mdx_ctx *ctx) {
                       cudaMemcpyHostToDevice));
   d.nchunk = (int)chunks.size();
   // shared-memory tile of the S(k) kernels: TILE atoms x all table rows
-  const size_t sh = ctx->mixed() ? 2 * sizeof(float2) * TILE * (kx + ky + kz + SCH)
+  const size_t sh = ctx->mixed() ? 2 * sizeof(float2) * TILE * (kx + ky + kz + SCH * zstep)
                                  : sizeof(double2) * TILE * (kx + ky + kz);
   if (sh > SFAC_SMEM_MAX) {
     ctx->err = "reciprocal k-set too large for the structure-factor tile";
@@ -1008,8 +1018,10 @@ int host_inifur(mdx_ctx *ctx) {
   // the dynamic shared-memory limit of a kernel is process-wide, shared by
   // every context: only ever raise it
   if (ctx->mixed()) {
-    MDX_CUDA(raise_smem_limit(k_rforce32, shr));
-    MDX_CUDA(raise_smem_limit(k_sfac32, sh));
+    MDX_CUDA(raise_smem_limit(k_rforce32<1>, shr));
+    MDX_CUDA(raise_smem_limit(k_rforce32<2>, shr));
+    MDX_CUDA(raise_smem_limit(k_sfac32<1>, sh));
+    MDX_CUDA(raise_smem_limit(k_sfac32<2>, sh));
   } else {
     MDX_CUDA(raise_smem_limit(k_sfac, sh));
   }
@@ -1020,8 +1032,8 @@ int host_inifur(mdx_ctx *ctx) {
     int nsm = 0, dev = 0, per_sm = 0;
     MDX_CUDA(cudaGetDevice(&dev));
     MDX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rforce32,
-                                                             32 * RF_PARTS, shr));
+    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, zstep == 2 ? k_rforce32<2> : k_rforce32<1>, 32 * RF_PARTS, shr));
     const double slots = (double)std::max(1, per_sm) * nsm;
     const double tiles = (double)((d.n + RF_BATOMS - 1) / RF_BATOMS);
     int best = 1;
@@ -1059,7 +1071,8 @@ int host_inifur(mdx_ctx *ctx) {
   // against 1e-8 for the FP32 FMA pass, so it is not the default.
   if (ctx->mixed()) {
     const char *env = std::getenv("MDX_EWALD_TC");
-    const int mode = env && env[0] >= '0' && env[0] <= '2' ? env[0] - '0' : 1;
+    // the octahedron's stepped z records: the CUDA-core passes only
+    const int mode = icell == 1 ? 0 : env && env[0] >= '0' && env[0] <= '2' ? env[0] - '0' : 1;
     d.tc_on = d.tcs_on = false;
     if (mode >= 1 && tc_force_setup(ctx, cols, KMAZ) < 0) return MDX_ERR_CUDA;
     if (mode >= 2 && tc_sfac_setup(ctx, cols) < 0) return MDX_ERR_CUDA;
@@ -1070,7 +1083,8 @@ int host_inifur(mdx_ctx *ctx) {
     int nsm = 0, dev = 0, per_sm = 0;
     MDX_CUDA(cudaGetDevice(&dev));
     MDX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sfac32, 128, sh));
+    MDX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, zstep == 2 ? k_sfac32<2> : k_sfac32<1>, 128, sh));
     const int nib = std::max(1, ((int)items.size() + 127) / 128);
     int ns = std::max(1, std::max(1, per_sm) * nsm / nib);
     ns = std::min(ns, std::max(1, d.n / 128));  // at least 128 atoms a slice
@@ -1193,7 +1207,7 @@ int furir_sfac(mdx_ctx *ctx, bool *skip) {
   MDX_CUDA(cudaMemsetAsync(d.sk, 0, sizeof(double2) * d.nkv, ctx->stream));
   {
     MDX_TIMER(ctx, MDX_T_EW_SFAC);
-    const size_t sh = mx ? 2 * sizeof(float2) * TILE * (d.kx + d.ky + d.kz + SCH)
+    const size_t sh = mx ? 2 * sizeof(float2) * TILE * (d.kx + d.ky + d.kz + SCH * d.zstep)
                          : sizeof(double2) * TILE * (d.kx + d.ky + d.kz);
     dim3 grid;
     if (mx && d.tcs_on) {
@@ -1201,7 +1215,8 @@ int furir_sfac(mdx_ctx *ctx, bool *skip) {
     } else {
       if (mx) {
         grid = dim3((d.nsitem + 127) / 128, d.sfac_nslice);
-        k_sfac32<<<grid, 128, sh, ctx->stream>>>(
+        auto kern = d.zstep == 2 ? k_sfac32<2> : k_sfac32<1>;
+        kern<<<grid, 128, sh, ctx->stream>>>(
             d.n, d.nsitem, reinterpret_cast<const SItem *>(d.sitems), d.kgroups, d.cols,
             d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.sfac_slice, d.sk, d.sk_part, d.nkv);
       } else {
@@ -1274,9 +1289,10 @@ int launch_furir(mdx_ctx *ctx) {
   } else if (mx) {
     const size_t shr = sizeof(float2) * RF_BATOMS * d.kz;
     const dim3 grid((d.n + RF_BATOMS - 1) / RF_BATOMS, d.rf_nsplit);
-    k_rforce32<<<grid, 32 * RF_PARTS, shr, ctx->stream>>>(
-        d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.colrvf, ctx->fix,
-        d.gfix);
+    auto kern = d.zstep == 2 ? k_rforce32<2> : k_rforce32<1>;
+    kern<<<grid, 32 * RF_PARTS, shr, ctx->stream>>>(
+        d.n, d.rf_part, d.kgroups, d.cols, d.wkf, d.tabxf, d.ldn, d.kx, d.ky, d.kz, d.colrvf,
+        ctx->fix, d.gfix);
   } else {
     k_rforce64<<<rblocks, RF_ATOMS * RF_PARTS, 0, ctx->stream>>>(
         d.n, d.ncol, d.cols, d.wp64, d.tabx, d.taby, d.tabz, d.colrv, d.gx, d.gy, d.gz);

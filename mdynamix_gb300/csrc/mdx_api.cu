@@ -938,9 +938,8 @@ int mdx_set_params(mdx_ctx *ctx, const mdx_params *p) {
     ctx->err = "ICELL must be 0 (rectangular), 1 (truncated octahedron) or 2 (hexagonal)";
     return MDX_ERR_ARG;
   }
-  if ((p->icell == 1 && ctx->mixed()) || (p->icell != 0 && p->rskin > 0.0)) {
-    ctx->err = "non-rectangular cells: the reference's list mode only; the truncated "
-               "octahedron on the FP64 path only";
+  if (p->icell != 0 && p->rskin > 0.0) {
+    ctx->err = "non-rectangular cells: the reference's list mode only (no Verlet skin)";
     return MDX_ERR_UNSUPPORTED;
   }
   if (p->boxl <= 0 || p->boyl <= 0 || p->bozl <= 0 || p->rcut <= 0 || p->nfreq < 1 ||

@@ -147,7 +147,8 @@ __host__ __device__ __forceinline__ size_t list_slot(int i, int k, int cap, bool
 // both signs of nz.  col[s] < 0 marks a padding slot (W = 0).
 constexpr int KGRP = 4;
 struct KGroup {
-  int m, len, woff, pad;  // len = m + 1 records
+  int m, len, woff;  // len = m + 1 records
+  int zoff;          // the columns' common z offset: record p is z = zoff + zstep p
   int col[KGRP];
 };
 
@@ -212,6 +213,7 @@ struct DevData {
   // SHAKE (per type: first bond record, bond count)
   // Ewald
   int nkv, ncol, kx, ky, kz;  // table rows: n = 0..KMAX, 0..KMAY, 0..KMAZ
+  int zstep;                    // z step of a column's records (2: truncated octahedron)
   int ldn;                      // row stride (atoms) of the FP32 tables, n rounded up to 128
   KCol *cols;
   void *kchunks;                // column chunks of the S(k) kernel
@@ -506,15 +508,17 @@ __device__ __forceinline__ void pbc_rectf(float &dx, float &dy, float &dz,
   if (fabsf(dy) > hby) dy = dy - fsignf(by, dy);
 }
 
-// The hexagonal cell's fold of PBC (service.f:956-979) in FP32, for the
-// mixed path's pair vectors: x already within +-BOXL/2 and y within +-BOYL
-// (the fixed-point differences), the four tests of the reference in its
-// order.  on = 0: rectangular cell, nothing to do.
-struct HexF {
-  int on;
-  float hbx, by, boxy3, boxyc;
+// The non-rectangular cells' part of PBC (service.f:956-986) in FP32, for
+// the mixed path's pair vectors, which arrive as fixed-point differences
+// (x within +-BOXL/2, z within +-BOZL/2, y within +-BOYL in the hexagonal
+// cell and +-BOYL/2 otherwise): the hexagonal cell's four tests in the
+// reference's order, or the truncated octahedron's corner fold.  kind 0:
+// rectangular, nothing to do.
+struct CellF {
+  int kind;  // ICELL
+  float hbx, bx, by, boxy3, boxyc;
 };
-__device__ __forceinline__ void pbc_hexf(float &xx, float &yy, const HexF &h) {
+__device__ __forceinline__ void pbc_hexf(float &xx, float &yy, const CellF &h) {
   float xy = h.boxyc * xx;
   if (yy > h.boxy3 - xy && (xx > 0.f || yy > 2.f * h.boxy3 - xy)) {
     yy = yy - h.by;
@@ -534,6 +538,17 @@ __device__ __forceinline__ void pbc_hexf(float &xx, float &yy, const HexF &h) {
   if (yy < -h.boxy3 + xy) {
     yy = yy + h.by;
     xx = xx - h.hbx;
+  }
+}
+__device__ __forceinline__ void pbc_cellf(float &xx, float &yy, float &zz, const CellF &c) {
+  if (c.kind == 2) {
+    pbc_hexf(xx, yy, c);
+  } else if (c.kind == 1) {  // CORSS: 4/3 is the reference's REAL*4 constant
+    const float corss =
+        c.hbx * (float)(int)((4.0f / 3.0f) * (fabsf(xx) + fabsf(yy) + fabsf(zz)) / c.bx);
+    xx = xx - copysignf(corss, xx);
+    yy = yy - copysignf(corss, yy);
+    zz = zz - copysignf(corss, zz);
   }
 }
 

@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
     const double *__restrict__ X, const double *__restrict__ Y,
     const double *__restrict__ Z, double escale,
     unsigned long long *__restrict__ slots, double *__restrict__ split,
-    const int *__restrict__ owner_of, HexF hex) {
+    const int *__restrict__ owner_of, CellF cf) {
   __shared__ double s_split[2 * MDX_NTPP + 2 * MDX_NT];
   if (SPLIT) {
     for (int k = threadIdx.x; k < 2 * MDX_NTPP + 2 * MDX_NT; k += blockDim.x) s_split[k] = 0.0;
@@ -362,8 +362,8 @@ __global__ void __launch_bounds__(256, PAIR32_BLOCKS) k_pair32(
       }
       float DX = idiff(pi.x, pj.x, sx);
       float DY = idiff(pi.y, pj.y, sy);
-      const float DZ = idiff(pi.z, pj.z, sz);
-      if (hex.on) pbc_hexf(DX, DY, hex);
+      float DZ = idiff(pi.z, pj.z, sz);
+      if (cf.kind) pbc_cellf(DX, DY, DZ, cf);
       const float RR = DX * DX + DY * DY + DZ * DZ;
       if (SHORT || RR <= pc.rc2f) {  // skin mode: long-row pairs beyond RCUT skipped
         const float R1I = rsqrtf(RR);
@@ -612,14 +612,14 @@ __device__ __forceinline__ void slots_out(const float (&a)[P_NSLOT], float escal
   }
 }
 
-template <bool SHORT, bool ENER, int TPO>
+template <bool SHORT, bool ENER, int TPO, bool CELL>
 __global__ void __launch_bounds__(256, (SHORT && !ENER) ? PAIR32X2_BLOCKS_SHORT : PAIR32X2_BLOCKS)
 k_pair32x2(
     int n, const int4 *__restrict__ posi, const int4 *__restrict__ posn,
     const float4 *__restrict__ stab, const int *__restrict__ cnt, const int *__restrict__ idx,
     int cap, PairTables tb, TypeConst tc, PairConst pc, float sx, float sy, float sz,
     FixScale fsc, unsigned long long *__restrict__ ffix,
-    unsigned long long *__restrict__ slots, const int *__restrict__ owner_of, HexF hex) {
+    unsigned long long *__restrict__ slots, const int *__restrict__ owner_of, CellF cf) {
   // TPO adjacent lanes per owner atom; lane k0 of an owner takes entries
   // k0 + 2 TPO m and k0 + TPO + 2 TPO m as one pair.  Owner order as in
   // k_pair32.
@@ -659,12 +659,12 @@ k_pair32x2(
       const bool same_b = hb && ((unsigned)pb.w >> MDX_SITE_BITS) == mi;
       if (same_a || same_b) {
         float dxa = fixdiff(pi.x, pa.x, sx), dya = fixdiff(pi.y, pa.y, sy);
-        const float dza = fixdiff(pi.z, pa.z, sz);
+        float dza = fixdiff(pi.z, pa.z, sz);
         float dxb = fixdiff(pi.x, pb.x, sx), dyb = fixdiff(pi.y, pb.y, sy);
-        const float dzb = fixdiff(pi.z, pb.z, sz);
-        if (hex.on) {
-          pbc_hexf(dxa, dya, hex);
-          pbc_hexf(dxb, dyb, hex);
+        float dzb = fixdiff(pi.z, pb.z, sz);
+        if (CELL) {
+          pbc_cellf(dxa, dya, dza, cf);
+          pbc_cellf(dxb, dyb, dzb, cf);
         }
         // the owner's own molecule: one entry at a time, other entry too
         const int nja = __float_as_int(sa.z), njb = __float_as_int(sb.z);
@@ -724,11 +724,11 @@ k_pair32x2(
                                    (float)(int)((unsigned)pi.x - (unsigned)pb.x)), sx2);
       float2 DY = mul2(make_float2((float)(int)((unsigned)pi.y - (unsigned)pa.y),
                                    (float)(int)((unsigned)pi.y - (unsigned)pb.y)), sy2);
-      const float2 DZ = mul2(make_float2((float)(int)((unsigned)pi.z - (unsigned)pa.z),
-                                         (float)(int)((unsigned)pi.z - (unsigned)pb.z)), sz2);
-      if (hex.on) {
-        pbc_hexf(DX.x, DY.x, hex);
-        pbc_hexf(DX.y, DY.y, hex);
+      float2 DZ = mul2(make_float2((float)(int)((unsigned)pi.z - (unsigned)pa.z),
+                                   (float)(int)((unsigned)pi.z - (unsigned)pb.z)), sz2);
+      if (CELL) {  // a non-rectangular cell (a template parameter: no cost otherwise)
+        pbc_cellf(DX.x, DY.x, DZ.x, cf);
+        pbc_cellf(DX.y, DY.y, DZ.y, cf);
       }
       float2 RR = fma2(DZ, DZ, fma2(DY, DY, mul2(DX, DX)));
       // an empty half or a pair beyond RCUT (skin mode) contributes nothing
@@ -958,12 +958,12 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     const double sxs = ctx->boxl / 4294967296.0, sys = fix_period_y(ctx) / 4294967296.0,
                  szs = ctx->bozl / 4294967296.0;
     const double escale = ctx->fix.escale;
-    // the hexagonal cell's fold after the fixed-point differences (its y
-    // period is 2 BOYL there); BOXY3 and 0.5 / cos30 as cell_pbc forms them
-    HexF hex{};
-    if (ctx->p.icell == 2) {
+    // the cell's fold after the fixed-point differences (the hexagonal
+    // cell's y period is 2 BOYL); BOXY3 and 0.5 / cos30 as cell_pbc forms them
+    CellF cf{};
+    if (ctx->p.icell != 0) {
       const CellPbc c = cell_pbc(ctx);
-      hex = HexF{1, (float)c.hbx, (float)c.by, (float)c.boxy3,
+      cf = CellF{ctx->p.icell, (float)c.hbx, (float)c.bx, (float)c.by, (float)c.boxy3,
                  (float)(0.5 / (double)0.8660254037844386f)};
     }
     // threads per owner atom: the context's tuning (the energy-split sweeps
@@ -975,11 +975,16 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
   k_pair32<S, P, E, K><<<grid32, T, 0, ctx->stream>>>(                            \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d),                 \
       ctx->tc, ctx->pc, (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, d.X,  \
-      d.Y, d.Z, escale, slots, split_buf, S ? nullptr : d.cell_list, hex)
-#define LP32X2(S, E, K)                                                           \
-  k_pair32x2<S, E, K><<<grid32, T, 0, ctx->stream>>>(                             \
+      d.Y, d.Z, escale, slots, split_buf, S ? nullptr : d.cell_list, cf)
+#define LP32X2C(S, E, K, C)                                                       \
+  k_pair32x2<S, E, K, C><<<grid32, T, 0, ctx->stream>>>(                          \
       d.n, d.posi, d.cell_pos, d.stab, cnt, idx, cap, tables(d), ctx->tc, ctx->pc, \
-      (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, slots, S ? nullptr : d.cell_list, hex)
+      (float)sxs, (float)sys, (float)szs, ctx->fix, ffix, slots, S ? nullptr : d.cell_list, cf)
+#define LP32X2(S, E, K)                        \
+  do {                                         \
+    if (cf.kind) LP32X2C(S, E, K, true);       \
+    else LP32X2C(S, E, K, false);              \
+  } while (0)
     // the paired sweeps cover Ewald without MDEE's shifted Coulomb
     const bool paired = !ctx->pc.lmnbl && !ctx->pc.lmdee;
 #define LP32E(S, K)                            \
@@ -1010,6 +1015,7 @@ int launch_pair(mdx_ctx *ctx, bool shrt, bool split, bool ener) {
     }
 #undef LP32E
 #undef LP32X2
+#undef LP32X2C
 #undef LP32
     MDX_LAUNCHED(ctx);
     if (ener) {

@@ -341,14 +341,18 @@ def test_cell_shapes_sultan_shake(icell):
     assert max(np.abs(gx - ox).max(), np.abs(gy - oy).max(), np.abs(gz - oz).max()) < 1e-9
 
 
-def test_cell_hexagonal_mixed():
-    """The mixed path in the hexagonal cell: fixed-point y words of period
-    2 BOYL, the cell's fold in FP32 after the integer differences, the X
-    phase of the Ewald tables as the sum of the x and y words.  Against the
-    FP64 path: force RMS error under 1e-5 in SLFORCES / FFORCES / ALLFORCE,
-    energies and virials to 1e-4, eleven DOUBLE steps tracking it to 1e-5 A."""
+@pytest.mark.parametrize("icell", [1, 2])
+def test_cell_shapes_mixed(icell):
+    """The mixed path in the two cells.  Hexagonal: fixed-point y words of
+    period 2 BOYL, the cell's fold in FP32 after the integer differences, the
+    X phase of the Ewald tables as the sum of the x and y words.  Truncated
+    octahedron: the corner fold in FP32, the k-set's columns grouped by the
+    parity of their nz and read every other z by the CUDA-core S(k) and force
+    passes.  Against the FP64 path: force RMS error under 1e-5 in SLFORCES /
+    FFORCES / ALLFORCE, energies and virials to 1e-4, eleven DOUBLE steps
+    tracking it to 1e-5 A."""
     from mdynamix_gb300.mdx import ForcePath
-    s, st = cell_system(2)
+    s, st = cell_system(icell)
     g64 = ForcePath(s, precision=MDX_FP64)
     g32 = ForcePath(s, precision=MDX_MIXED)
     for g in (g64, g32):
@@ -380,8 +384,12 @@ def test_cell_hexagonal_mixed():
 
 
 def test_cell_shapes_refused_where_not_built():
-    """The mixed path refuses the truncated octahedron (FP64 only)."""
+    """Non-rectangular cells with a Verlet skin are refused (the skin's
+    displacement check and rectangular-grid build are not written for
+    them)."""
     from mdynamix_gb300.mdx import ForcePath, MdxError
-    s, st = cell_system(1)
-    with pytest.raises(MdxError):
-        ForcePath(s, precision=MDX_MIXED)
+    base = systems.spcfw(n=256, ions=2, rcut=8.0)
+    for prec in (MDX_FP64, MDX_MIXED):
+        s = systems.build(dataclasses.replace(base, icell=1, rskin=1.0))[0]
+        with pytest.raises(MdxError):
+            ForcePath(s, precision=prec)
