@@ -508,7 +508,7 @@ __device__ __forceinline__ void pbc_rectf(float &dx, float &dy, float &dz,
   if (fabsf(dy) > hby) dy = dy - fsignf(by, dy);
 }
 
-// The non-rectangular cells' part of PBC (service.f:956-986) in FP32, for
+// The non-rectangular cells' part of PBC (service.f:956-988) in FP32, for
 // the mixed path's pair vectors, which arrive as fixed-point differences
 // (x within +-BOXL/2, z within +-BOZL/2, y within +-BOYL in the hexagonal
 // cell and +-BOYL/2 otherwise): the hexagonal cell's four tests in the
